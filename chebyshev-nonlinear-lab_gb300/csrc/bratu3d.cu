@@ -1,0 +1,341 @@
+// bratu3d.cu — Bratu3D residual, Jacobian-vector products and second directional derivatives
+// (problems/bratu3d.hpp, operators/operator.hpp:101-134) on the GPU.
+//
+// Layout: n^3 FP64 values, index (i*n + j)*n + k with k fastest, Dirichlet zeros implicit.
+// Kernels march along i: a block covers a 32 x 8 tile of (k, j) and walks a chunk of i planes,
+// keeping the i-1, i, i+1 values of its column in registers, so each point issues five loads.
+// The 7-point sums follow the reference's operation order (6v, then minus the i-1, i+1, j-1,
+// j+1, k-1, k+1 neighbours; a missing neighbour subtracts +0.0, which leaves every value
+// unchanged), so the stencil results equal the reference's bit for bit; only exp may differ by
+// an ulp between CUDA and the host C library.
+#include <cmath>
+#include <limits>
+
+#include "numa_internal.hpp"
+
+namespace numa::gpu {
+namespace {
+
+constexpr int BX = 32, BY = 8;
+
+struct March {
+    dim3 grid;
+    int ichunk;
+};
+
+// Grid of (k tiles, j tiles, i chunks).  Chunks of 8 planes keep ~1M threads in flight at
+// n = 255; the chunk grows when a fused reduction would exceed kMaxRedBlocks partials.
+March march_shape(int n, bool reducing) {
+    const int kb = (n + BX - 1) / BX, jb = (n + BY - 1) / BY;
+    int ichunk = n >= 64 ? 8 : (n >= 16 ? 4 : 1);
+    if (reducing) {
+        const long cols = (long)kb * jb;
+        const long max_chunks = kMaxRedBlocks / cols;
+        if (max_chunks < 1) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "grid too large for a fused reduction");
+        const long need = (n + max_chunks - 1) / max_chunks;
+        if (need > ichunk) ichunk = (int)need;
+    }
+    March m;
+    m.ichunk = ichunk;
+    m.grid = dim3(kb, jb, (n + ichunk - 1) / ichunk);
+    return m;
+}
+
+// Minus the 7-point Laplacian without the h^-2 factor, on a value column marching in i.
+struct Col {
+    double below, cur;
+};
+
+__device__ __forceinline__ double lap_sum(const double* __restrict__ v, size_t p, size_t plane, int n, int i,
+                                          int j, int k, double below, double cur, double& above) {
+    above = (i + 1 < n) ? v[p + plane] : 0.0;
+    const double jm = (j > 0) ? v[p - n] : 0.0;
+    const double jp = (j + 1 < n) ? v[p + n] : 0.0;
+    const double km = (k > 0) ? v[p - 1] : 0.0;
+    const double kp = (k + 1 < n) ? v[p + 1] : 0.0;
+    double s = 6.0 * cur;
+    s = s - below;
+    s = s - above;
+    s = s - jm;
+    s = s - jp;
+    s = s - km;
+    s = s - kp;
+    return s;
+}
+
+// F = h^-2 (6u - sum) - lambda e^u; optionally c = lambda e^u and ||F||.
+template <bool WRITE_C, bool NORM>
+__global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, double* __restrict__ F,
+                                                 double* __restrict__ c_out, int n, int ichunk, double lam,
+                                                 double h2inv, RedArgs red, double* norm_out) {
+    const int k = blockIdx.x * BX + threadIdx.x;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    const int i0 = blockIdx.z * ichunk;
+    const int i1 = min(i0 + ichunk, n);
+    const size_t plane = (size_t)n * n;
+    double acc[1] = {0.0};
+    if (k < n && j < n) {
+        size_t p = ((size_t)i0 * n + j) * n + k;
+        double below = (i0 > 0) ? u[p - plane] : 0.0;
+        double cur = u[p];
+        for (int i = i0; i < i1; ++i) {
+            double above;
+            const double s = lap_sum(u, p, plane, n, i, j, k, below, cur, above);
+            const double e = lam * exp(cur);
+            const double f = h2inv * s - e;
+            F[p] = f;
+            if (WRITE_C) c_out[p] = e;
+            if (NORM) acc[0] = __fma_rn(f, f, acc[0]);
+            below = cur;
+            cur = above;
+            p += plane;
+        }
+    }
+    if (NORM) {
+        __shared__ double sm[1][32];
+        block_sum<1>(acc, sm);
+        grid_reduce_finish<1>(acc, red, [norm_out] __device__(const double(&t)[1]) { *norm_out = __dsqrt_rn(t[0]); });
+    }
+}
+
+// c = lambda e^u
+__global__ void k_coef(const double* __restrict__ u, double* __restrict__ c, size_t N, double lam) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) c[p] = lam * exp(u[p]);
+}
+
+// out = h^-2 (6v - sum) - c v, with c given (FROM_X: c = lambda e^x formed here).
+template <bool FROM_X>
+__global__ void __launch_bounds__(BX* BY) k_jvp(const double* __restrict__ cx, const double* __restrict__ v,
+                                                double* __restrict__ out, int n, int ichunk, double lam,
+                                                double h2inv) {
+    const int k = blockIdx.x * BX + threadIdx.x;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    const int i0 = blockIdx.z * ichunk;
+    const int i1 = min(i0 + ichunk, n);
+    if (k >= n || j >= n) return;
+    const size_t plane = (size_t)n * n;
+    size_t p = ((size_t)i0 * n + j) * n + k;
+    double below = (i0 > 0) ? v[p - plane] : 0.0;
+    double cur = v[p];
+    for (int i = i0; i < i1; ++i) {
+        double above;
+        const double s = lap_sum(v, p, plane, n, i, j, k, below, cur, above);
+        const double c = FROM_X ? lam * exp(cx[p]) : cx[p];
+        out[p] = h2inv * s - c * cur;
+        below = cur;
+        cur = above;
+        p += plane;
+    }
+}
+
+// Mixed precision: FP32 arithmetic on FP64 vectors with an FP32 coefficient.
+__global__ void __launch_bounds__(BX* BY) k_jvp32(const float* __restrict__ c32, const double* __restrict__ v,
+                                                  double* __restrict__ out, int n, int ichunk, float h2inv) {
+    const int k = blockIdx.x * BX + threadIdx.x;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    const int i0 = blockIdx.z * ichunk;
+    const int i1 = min(i0 + ichunk, n);
+    if (k >= n || j >= n) return;
+    const size_t plane = (size_t)n * n;
+    size_t p = ((size_t)i0 * n + j) * n + k;
+    float below = (i0 > 0) ? (float)v[p - plane] : 0.0f;
+    float cur = (float)v[p];
+    for (int i = i0; i < i1; ++i) {
+        const float above = (i + 1 < n) ? (float)v[p + plane] : 0.0f;
+        const float jm = (j > 0) ? (float)v[p - n] : 0.0f;
+        const float jp = (j + 1 < n) ? (float)v[p + n] : 0.0f;
+        const float km = (k > 0) ? (float)v[p - 1] : 0.0f;
+        const float kp = (k + 1 < n) ? (float)v[p + 1] : 0.0f;
+        float s = 6.0f * cur;
+        s = s - below;
+        s = s - above;
+        s = s - jm;
+        s = s - jp;
+        s = s - km;
+        s = s - kp;
+        out[p] = (double)(h2inv * s - c32[p] * cur);
+        below = cur;
+        cur = above;
+        p += plane;
+    }
+}
+
+// out = -c v v  (bratu3d.hpp:52: -lambda * exp(u) * v * v, evaluated left to right)
+__global__ void k_d2(const double* __restrict__ c, const double* __restrict__ v, double* __restrict__ out, size_t N) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) {
+        const double vv = v[p];
+        out[p] = ((-c[p]) * vv) * vv;
+    }
+}
+
+// d = 6 h^-2 - c
+__global__ void k_jacobi_diag(const double* __restrict__ c, double* __restrict__ d, size_t N, double six_h2inv) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) d[p] = six_h2inv - c[p];
+}
+
+// ||v|| and the finite-difference step h = scale (1 + ||x||) / ||v|| on the device; a zero
+// direction raises the flag that makes the quotient kernels write zeros (operator.hpp:105-106).
+__global__ void __launch_bounds__(kRedThreads) k_fd_step(const double* __restrict__ v, size_t N, RedArgs red,
+                                                         double scale, double* slots /* h, 1/h, zero, xnorm */) {
+    __shared__ double sm[1][32];
+    double s[1] = {0.0};
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) s[0] = __fma_rn(v[i], v[i], s[0]);
+    block_sum<1>(s, sm);
+    grid_reduce_finish<1>(s, red, [slots, scale] __device__(const double(&t)[1]) {
+        const double nv = __dsqrt_rn(t[0]);
+        if (nv == 0.0) {
+            slots[0] = 0.0;
+            slots[1] = 0.0;
+            slots[2] = 1.0;
+        } else {
+            const double h = __ddiv_rn(scale * (1.0 + slots[3]), nv);
+            slots[0] = h;
+            slots[1] = h * h;
+            slots[2] = 0.0;
+        }
+    });
+}
+
+// xp = x + s h v with h from the device (s = +1 or -1): operator.hpp:109-110, :126-128.
+__global__ void k_fd_shift(const double* __restrict__ x, const double* __restrict__ v, const double* __restrict__ slots,
+                           double sign, double* __restrict__ xp, size_t N) {
+    const double a = sign * slots[0];
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) xp[p] = x[p] + a * v[p];
+}
+
+// out = (f1 - f0) / h  (operator.hpp:113)
+__global__ void k_fd_quot(const double* __restrict__ f1, const double* __restrict__ f0,
+                          const double* __restrict__ slots, double* __restrict__ out, size_t N) {
+    const double h = slots[0];
+    const bool zero = slots[2] != 0.0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride)
+        out[p] = zero ? 0.0 : __ddiv_rn(f1[p] - f0[p], h);
+}
+
+// out = (fp - 2 f0 + fm) / (h h)  (operator.hpp:132-133)
+__global__ void k_fd2_quot(const double* __restrict__ fp, const double* __restrict__ f0, const double* __restrict__ fm,
+                           const double* __restrict__ slots, double* __restrict__ out, size_t N) {
+    const double hh = slots[1];
+    const bool zero = slots[2] != 0.0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride)
+        out[p] = zero ? 0.0 : __ddiv_rn(fp[p] - 2.0 * f0[p] + fm[p], hh);
+}
+
+unsigned ew_grid(const Context& ctx, size_t N) {
+    size_t want = (N + 255) / 256;
+    size_t cap = static_cast<size_t>(ctx.sm_count) * 16;
+    if (want > cap) want = cap;
+    return static_cast<unsigned>(want < 1 ? 1 : want);
+}
+
+}  // namespace
+
+Bratu3D::Bratu3D(Context& ctx, size_t n, double lambda)
+    : ctx_(ctx), n_(n), N_(n * n * n), lambda_(lambda), h2inv_((n + 1.0) * (n + 1.0)) {
+    if (n == 0) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Bratu3D needs n > 0");
+    if (n > 65535 * 8) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "grid too large");
+}
+
+void Bratu3D::eval(const double* x, double* out, double* c_out, double* norm_out) {
+    const int n = (int)n_;
+    const bool norm = norm_out != nullptr;
+    March m = march_shape(n, norm);
+    dim3 blk(BX, BY);
+    if (c_out && norm)
+        k_eval<true, true><<<m.grid, blk, 0, ctx_.stream>>>(x, out, c_out, n, m.ichunk, lambda_, h2inv_, ctx_.red, norm_out);
+    else if (c_out)
+        k_eval<true, false><<<m.grid, blk, 0, ctx_.stream>>>(x, out, c_out, n, m.ichunk, lambda_, h2inv_, ctx_.red, nullptr);
+    else if (norm)
+        k_eval<false, true><<<m.grid, blk, 0, ctx_.stream>>>(x, out, nullptr, n, m.ichunk, lambda_, h2inv_, ctx_.red, norm_out);
+    else
+        k_eval<false, false><<<m.grid, blk, 0, ctx_.stream>>>(x, out, nullptr, n, m.ichunk, lambda_, h2inv_, ctx_.red, nullptr);
+    ctx_.count_launch();
+    ctx_.check_launch("bratu3d eval");
+}
+
+void Bratu3D::coef(const double* x, double* c) {
+    k_coef<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(x, c, N_, lambda_);
+    ctx_.count_launch();
+    ctx_.check_launch("bratu3d coef");
+}
+
+void Bratu3D::jvp_c(const double* c, const double* v, double* out) {
+    March m = march_shape((int)n_, false);
+    k_jvp<false><<<m.grid, dim3(BX, BY), 0, ctx_.stream>>>(c, v, out, (int)n_, m.ichunk, lambda_, h2inv_);
+    ctx_.count_launch();
+    ctx_.check_launch("bratu3d jvp");
+}
+
+void Bratu3D::jvp_c32(const float* c32, const double* v, double* out) {
+    March m = march_shape((int)n_, false);
+    k_jvp32<<<m.grid, dim3(BX, BY), 0, ctx_.stream>>>(c32, v, out, (int)n_, m.ichunk, (float)h2inv_);
+    ctx_.count_launch();
+    ctx_.check_launch("bratu3d jvp32");
+}
+
+void Bratu3D::jvp_x(const double* x, const double* v, double* out) {
+    March m = march_shape((int)n_, false);
+    k_jvp<true><<<m.grid, dim3(BX, BY), 0, ctx_.stream>>>(x, v, out, (int)n_, m.ichunk, lambda_, h2inv_);
+    ctx_.count_launch();
+    ctx_.check_launch("bratu3d jvp(x)");
+}
+
+void Bratu3D::d2_c(const double* c, const double* v, double* out) {
+    k_d2<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(c, v, out, N_);
+    ctx_.count_launch();
+    ctx_.check_launch("bratu3d d2");
+}
+
+void Bratu3D::jacobi_diag_c(const double* c, double* d) {
+    k_jacobi_diag<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(c, d, N_, 6.0 * h2inv_);
+    ctx_.count_launch();
+    ctx_.check_launch("bratu3d jacobi_diag");
+}
+
+void Bratu3D::jvp_fd(const double* x, const double* f0, const double* xnorm_dev, const double* v, double* out) {
+    // h = sqrt(eps) (1 + ||x||) / ||v||; sqrt(eps) = 2^-26 exactly.
+    double* slots = ctx_.scalar(kSlotFdH);
+    dev_copy(ctx_, xnorm_dev, slots + 3, 1);
+    const double scale = std::sqrt(std::numeric_limits<double>::epsilon());
+    k_fd_step<<<ctx_.red_grid(N_), kRedThreads, 0, ctx_.stream>>>(v, N_, ctx_.red, scale, slots);
+    ctx_.count_launch();
+    s1_.resize(N_);
+    s2_.resize(N_);
+    k_fd_shift<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(x, v, slots, 1.0, s1_.p, N_);
+    ctx_.count_launch();
+    eval(s1_.p, s2_.p);
+    k_fd_quot<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(s2_.p, f0, slots, out, N_);
+    ctx_.count_launch();
+    ctx_.check_launch("jvp_fd");
+}
+
+void Bratu3D::d2_fd(const double* x, const double* f0, const double* xnorm_dev, const double* v, double* out) {
+    // h = eps^(1/4) (1 + ||x||) / ||v||; eps^(1/4) = 2^-13 exactly.
+    double* slots = ctx_.scalar(kSlotFdH);
+    dev_copy(ctx_, xnorm_dev, slots + 3, 1);
+    const double scale = std::pow(std::numeric_limits<double>::epsilon(), 0.25);
+    k_fd_step<<<ctx_.red_grid(N_), kRedThreads, 0, ctx_.stream>>>(v, N_, ctx_.red, scale, slots);
+    ctx_.count_launch();
+    s1_.resize(N_);
+    s2_.resize(N_);
+    s3_.resize(N_);
+    // fp into s2, fm into s3 (s1 holds the shifted point in turn)
+    k_fd_shift<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(x, v, slots, 1.0, s1_.p, N_);
+    ctx_.count_launch();
+    eval(s1_.p, s2_.p);
+    k_fd_shift<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(x, v, slots, -1.0, s1_.p, N_);
+    ctx_.count_launch();
+    eval(s1_.p, s3_.p);
+    k_fd2_quot<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(s2_.p, f0, s3_.p, slots, out, N_);
+    ctx_.count_launch();
+    ctx_.check_launch("d2_fd");
+}
+
+}  // namespace numa::gpu

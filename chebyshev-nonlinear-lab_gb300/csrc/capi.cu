@@ -1,0 +1,822 @@
+// capi.cu — the extern "C" boundary of libnuma_gpu.so (declared in include/numa_gpu.h).
+//
+// Every entry point validates its handles and sizes, runs the C++ implementation and converts
+// exceptions into status codes (the reference reports failure through result structs and, for
+// PoissonMG, std::invalid_argument / std::overflow_error: those map to
+// NUMA_GPU_ERR_INVALID_ARGUMENT / NUMA_GPU_ERR_OVERFLOW).
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+
+#include "numa_internal.hpp"
+
+using namespace numa::gpu;
+
+struct numa_gpu_bratu3d {
+    numa_gpu_ctx* ctx;
+    std::unique_ptr<Bratu3D> impl;
+};
+struct numa_gpu_mg {
+    numa_gpu_ctx* ctx;
+    std::unique_ptr<PoissonMG> impl;
+};
+struct numa_gpu_provider {
+    numa_gpu_ctx* ctx;
+    std::unique_ptr<Provider> impl;
+    size_t N;  // 0 = any size (identity)
+};
+struct numa_gpu_krylov_space {
+    numa_gpu_ctx* ctx;
+    KrylovSpace impl;
+};
+
+namespace {
+
+// Per-context caches owned by the C layer.
+struct CtxExtras {
+    std::unique_ptr<Gmres> gmres;
+    size_t gmres_N = 0;
+    // numa_gpu_solve_bratu3d_host keeps its operator, provider and vector between calls
+    std::unique_ptr<Bratu3D> host_op;
+    std::unique_ptr<Provider> host_pc;
+    DeviceArray<double> host_x;
+    size_t host_n = 0;
+    double host_lambda = 0.0;
+    int host_kind = -1, host_prec = -1;
+};
+
+struct CtxHandle : numa_gpu_ctx {
+    std::unique_ptr<Context> own;
+    CtxExtras extras;
+};
+
+CtxExtras& extras(numa_gpu_ctx* c) { return static_cast<CtxHandle*>(c)->extras; }
+
+template <class F>
+int guard(numa_gpu_ctx* ctx, F&& fn) {
+    try {
+        fn();
+        if (ctx && ctx->impl) ctx->impl->last_error.clear();
+        return NUMA_GPU_OK;
+    } catch (const Status& s) {
+        if (ctx && ctx->impl) ctx->impl->last_error = s.what();
+        return s.code;
+    } catch (const std::bad_alloc&) {
+        if (ctx && ctx->impl) ctx->impl->last_error = "host allocation failed";
+        return NUMA_GPU_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception& e) {
+        if (ctx && ctx->impl) ctx->impl->last_error = e.what();
+        return NUMA_GPU_ERR_CUDA;
+    }
+}
+
+void need(bool cond, int code, const char* msg) {
+    if (!cond) throw Status(code, msg);
+}
+
+void same_ctx(numa_gpu_ctx* a, const numa_gpu_vec* v) {
+    need(v != nullptr, NUMA_GPU_ERR_INVALID_ARGUMENT, "null vector");
+    need(v->ctx == a, NUMA_GPU_ERR_INVALID_ARGUMENT, "vector belongs to another context");
+}
+
+void sized(const numa_gpu_vec* v, size_t N) {
+    need(v->n == N, NUMA_GPU_ERR_SIZE_MISMATCH, "vector length does not match the operator size");
+}
+
+Gmres& gmres_for(numa_gpu_ctx* c, size_t N) {
+    CtxExtras& e = extras(c);
+    if (!e.gmres || e.gmres_N != N) {
+        e.gmres = std::make_unique<Gmres>(*c->impl, N);
+        e.gmres_N = N;
+    }
+    return *e.gmres;
+}
+
+// C callbacks as LinearOp / Precond over non-owning vector views.
+struct CallbackOp : LinearOp {
+    numa_gpu_ctx* ctx;
+    numa_gpu_apply_fn fn;
+    void* user;
+    size_t N;
+    void apply(const double* v, double* out) override {
+        numa_gpu_vec vv{ctx, const_cast<double*>(v), N, false}, ov{ctx, out, N, false};
+        if (fn(user, &vv, &ov) != 0) throw Status(NUMA_GPU_ERR_CALLBACK, "apply callback returned an error");
+    }
+};
+struct CallbackPrec : Precond {
+    numa_gpu_ctx* ctx;
+    numa_gpu_precond_fn fn;
+    void* user;
+    size_t N;
+    void apply(const double* r, double* z) override {
+        numa_gpu_vec rv{ctx, const_cast<double*>(r), N, false}, zv{ctx, z, N, false};
+        if (fn(user, &rv, &zv) != 0) throw Status(NUMA_GPU_ERR_CALLBACK, "precond callback returned an error");
+    }
+};
+
+// Jacobian of a Bratu3D at a fixed point.
+struct BratuJacOp : LinearOp {
+    Bratu3D& f;
+    int mode;
+    const double *x, *c, *fx, *xnorm;
+    BratuJacOp(Bratu3D& f_, int m) : f(f_), mode(m), x(nullptr), c(nullptr), fx(nullptr), xnorm(nullptr) {}
+    void apply(const double* v, double* out) override {
+        if (mode == NUMA_GPU_DERIV_FD) f.jvp_fd(x, fx, xnorm, v, out);
+        else f.jvp_c(c, v, out);
+    }
+};
+struct ProviderPrec : Precond {
+    Provider* p;
+    void apply(const double* r, double* z) override { p->apply(r, z); }
+};
+
+void fill_gmres(const GmresResult& g, numa_gmres_result* out) {
+    if (!out) return;
+    out->iters = g.iters;
+    out->matvecs = g.matvecs;
+    out->precs = g.precs;
+    out->rel_res = g.rel_res;
+    out->converged = g.converged ? 1 : 0;
+    out->breakdown = g.breakdown ? 1 : 0;
+}
+
+GmresOptions gopts(double rtol, size_t restart, size_t max_iters, int zero_guess, int orth, int flexible) {
+    GmresOptions o;
+    o.rtol = rtol;
+    o.restart = restart;
+    o.max_iters = max_iters;
+    o.zero_guess = zero_guess != 0;
+    o.orth = orth;
+    o.flexible = flexible != 0;
+    return o;
+}
+
+}  // namespace
+
+extern "C" {
+
+int numa_gpu_abi_version(void) { return NUMA_GPU_ABI_VERSION; }
+
+const char* numa_gpu_status_string(int s) {
+    switch (s) {
+        case NUMA_GPU_OK: return "ok";
+        case NUMA_GPU_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case NUMA_GPU_ERR_OVERFLOW: return "size overflow";
+        case NUMA_GPU_ERR_SIZE_MISMATCH: return "size mismatch";
+        case NUMA_GPU_ERR_CUDA: return "CUDA error";
+        case NUMA_GPU_ERR_OUT_OF_MEMORY: return "out of memory";
+        case NUMA_GPU_ERR_NO_DEVICE: return "no CUDA device";
+        case NUMA_GPU_ERR_CALLBACK: return "callback error";
+        case NUMA_GPU_ERR_NOT_SUPPORTED: return "not supported";
+        default: return "unknown status";
+    }
+}
+
+void numa_krylov_params_default(numa_krylov_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->rtol_nl = 1e-8;
+    p->max_nl = 50;
+    p->eta_init = 0.5;
+    p->eta_max = 0.9;
+    p->gamma = 0.9;
+    p->alpha = 2.0;
+    p->eta2_factor = 10.0;
+    p->eta2_max = 0.5;
+    p->gmres_restart = 50;
+    p->gmres_max_iters = 500;
+    p->armijo = 1e-4;
+    p->min_lambda = 1e-4;
+}
+
+// ------------------------------------------------------------------------------ context
+int numa_gpu_ctx_create(int device, numa_gpu_ctx** out) {
+    if (!out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    try {
+        auto h = std::make_unique<CtxHandle>();
+        h->own = std::make_unique<Context>(device);
+        h->impl = h->own.get();
+        *out = h.release();
+        return NUMA_GPU_OK;
+    } catch (const Status& s) {
+        return s.code;
+    } catch (const std::bad_alloc&) {
+        return NUMA_GPU_ERR_OUT_OF_MEMORY;
+    } catch (...) {
+        return NUMA_GPU_ERR_CUDA;
+    }
+}
+
+int numa_gpu_ctx_destroy(numa_gpu_ctx* ctx) {
+    if (!ctx) return NUMA_GPU_OK;
+    CtxHandle* h = static_cast<CtxHandle*>(ctx);
+    h->extras = CtxExtras();
+    delete h;
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_ctx_synchronize(numa_gpu_ctx* ctx) {
+    if (!ctx) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(ctx, [&] { ctx->impl->sync(); });
+}
+
+const char* numa_gpu_ctx_last_error(numa_gpu_ctx* ctx) {
+    if (!ctx || !ctx->impl) return "";
+    return ctx->impl->last_error.c_str();
+}
+
+int numa_gpu_ctx_set_timing(numa_gpu_ctx* ctx, int enable) {
+    if (!ctx) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    ctx->impl->timing = enable != 0;
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_ctx_kernel_launches(numa_gpu_ctx* ctx, uint64_t* out) {
+    if (!ctx || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = ctx->impl->launches;
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_ctx_reset_kernel_launches(numa_gpu_ctx* ctx) {
+    if (!ctx) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    ctx->impl->launches = 0;
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_ctx_stream(numa_gpu_ctx* ctx, void** stream_out) {
+    if (!ctx || !stream_out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *stream_out = reinterpret_cast<void*>(ctx->impl->stream);
+    return NUMA_GPU_OK;
+}
+
+// ------------------------------------------------------------------------------ vectors
+int numa_gpu_vec_create(numa_gpu_ctx* ctx, size_t n, numa_gpu_vec** out) {
+    if (!ctx || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        auto v = std::make_unique<numa_gpu_vec>();
+        v->ctx = ctx;
+        v->n = n;
+        v->owns = true;
+        v->d = nullptr;
+        if (n > 0) {
+            cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&v->d), n * sizeof(double));
+            if (e == cudaErrorMemoryAllocation) {
+                cudaGetLastError();
+                throw Status(NUMA_GPU_ERR_OUT_OF_MEMORY, "cudaMalloc failed for a vector");
+            }
+            NUMA_CUDA(e);
+            NUMA_CUDA(cudaMemsetAsync(v->d, 0, n * sizeof(double), ctx->impl->stream));
+        }
+        *out = v.release();
+    });
+}
+
+int numa_gpu_vec_destroy(numa_gpu_vec* v) {
+    if (!v) return NUMA_GPU_OK;
+    if (v->owns && v->d) {
+        cudaStreamSynchronize(v->ctx->impl->stream);
+        cudaFree(v->d);
+    }
+    delete v;
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_vec_size(const numa_gpu_vec* v, size_t* n) {
+    if (!v || !n) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *n = v->n;
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_vec_device_ptr(numa_gpu_vec* v, double** dptr) {
+    if (!v || !dptr) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *dptr = v->d;
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_vec_upload(numa_gpu_vec* v, const double* host, size_t n) {
+    if (!v || (!host && n)) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(v->ctx, [&] {
+        need(n == v->n, NUMA_GPU_ERR_SIZE_MISMATCH, "upload length differs from the vector length");
+        if (n) NUMA_CUDA(cudaMemcpyAsync(v->d, host, n * sizeof(double), cudaMemcpyHostToDevice, v->ctx->impl->stream));
+        v->ctx->impl->sync();
+    });
+}
+
+int numa_gpu_vec_download(const numa_gpu_vec* v, double* host, size_t n) {
+    if (!v || (!host && n)) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(v->ctx, [&] {
+        need(n == v->n, NUMA_GPU_ERR_SIZE_MISMATCH, "download length differs from the vector length");
+        if (n) NUMA_CUDA(cudaMemcpyAsync(host, v->d, n * sizeof(double), cudaMemcpyDeviceToHost, v->ctx->impl->stream));
+        v->ctx->impl->sync();
+    });
+}
+
+int numa_gpu_vec_fill(numa_gpu_vec* v, double value) {
+    if (!v) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(v->ctx, [&] { dev_fill(*v->ctx->impl, v->d, value, v->n); });
+}
+
+int numa_gpu_vec_copy(const numa_gpu_vec* src, numa_gpu_vec* dst) {
+    if (!src || !dst) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(dst->ctx, [&] {
+        same_ctx(dst->ctx, src);
+        need(src->n == dst->n, NUMA_GPU_ERR_SIZE_MISMATCH, "copy between vectors of different lengths");
+        dev_copy(*dst->ctx->impl, src->d, dst->d, src->n);
+    });
+}
+
+int numa_gpu_vec_dot(const numa_gpu_vec* a, const numa_gpu_vec* b, double* out) {
+    if (!a || !b || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(a->ctx, [&] {
+        same_ctx(a->ctx, b);
+        need(a->n == b->n, NUMA_GPU_ERR_SIZE_MISMATCH, "dot of vectors of different lengths");
+        Context& c = *a->ctx->impl;
+        if (a->n == 0) {
+            *out = 0.0;
+            return;
+        }
+        dev_dot(c, a->d, b->d, a->n, c.scalar(kSlotTmp0));
+        *out = c.fetch1(c.scalar(kSlotTmp0));
+    });
+}
+
+int numa_gpu_vec_norm2(const numa_gpu_vec* a, double* out) {
+    if (!a || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(a->ctx, [&] {
+        Context& c = *a->ctx->impl;
+        if (a->n == 0) {
+            *out = 0.0;
+            return;
+        }
+        dev_norm2(c, a->d, a->n, c.scalar(kSlotTmp0));
+        *out = c.fetch1(c.scalar(kSlotTmp0));
+    });
+}
+
+int numa_gpu_vec_axpy(double a, const numa_gpu_vec* x, numa_gpu_vec* y) {
+    if (!x || !y) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(y->ctx, [&] {
+        same_ctx(y->ctx, x);
+        need(x->n == y->n, NUMA_GPU_ERR_SIZE_MISMATCH, "axpy of vectors of different lengths");
+        dev_axpy(*y->ctx->impl, a, x->d, y->d, x->n);
+    });
+}
+
+// ------------------------------------------------------------------------------ Bratu3D
+int numa_gpu_bratu3d_create(numa_gpu_ctx* ctx, size_t n, double lambda, numa_gpu_bratu3d** out) {
+    if (!ctx || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        need(n > 0, NUMA_GPU_ERR_INVALID_ARGUMENT, "Bratu3D needs n > 0");
+        need(n <= 65535, NUMA_GPU_ERR_OVERFLOW, "Bratu3D grid too large");
+        auto h = std::make_unique<numa_gpu_bratu3d>();
+        h->ctx = ctx;
+        h->impl = std::make_unique<Bratu3D>(*ctx->impl, n, lambda);
+        *out = h.release();
+    });
+}
+
+int numa_gpu_bratu3d_destroy(numa_gpu_bratu3d* op) {
+    if (op) {
+        cudaStreamSynchronize(op->ctx->impl->stream);
+        delete op;
+    }
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_bratu3d_size(const numa_gpu_bratu3d* op, size_t* N) {
+    if (!op || !N) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *N = op->impl->size();
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_bratu3d_eval(numa_gpu_bratu3d* op, const numa_gpu_vec* x, numa_gpu_vec* out) {
+    if (!op) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(op->ctx, [&] {
+        same_ctx(op->ctx, x);
+        same_ctx(op->ctx, out);
+        sized(x, op->impl->size());
+        sized(out, op->impl->size());
+        need(x->d != out->d, NUMA_GPU_ERR_INVALID_ARGUMENT, "eval input and output must differ");
+        op->impl->eval(x->d, out->d);
+    });
+}
+
+int numa_gpu_bratu3d_jvp(numa_gpu_bratu3d* op, const numa_gpu_vec* x, const numa_gpu_vec* v, numa_gpu_vec* out,
+                         int mode) {
+    if (!op) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(op->ctx, [&] {
+        for (const numa_gpu_vec* q : {x, v, (const numa_gpu_vec*)out}) {
+            same_ctx(op->ctx, q);
+            sized(q, op->impl->size());
+        }
+        need(out->d != x->d && out->d != v->d, NUMA_GPU_ERR_INVALID_ARGUMENT, "jvp output must not alias an input");
+        Bratu3D& f = *op->impl;
+        Context& c = *op->ctx->impl;
+        if (mode == NUMA_GPU_DERIV_FD) {
+            DeviceArray<double> f0(f.size());
+            f.eval(x->d, f0.p);
+            dev_norm2(c, x->d, f.size(), c.scalar(kSlotTmp1));
+            f.jvp_fd(x->d, f0.p, c.scalar(kSlotTmp1), v->d, out->d);
+            c.sync();
+        } else {
+            need(mode == NUMA_GPU_DERIV_ANALYTIC, NUMA_GPU_ERR_INVALID_ARGUMENT, "unknown derivative mode");
+            f.jvp_x(x->d, v->d, out->d);
+        }
+    });
+}
+
+int numa_gpu_bratu3d_d2(numa_gpu_bratu3d* op, const numa_gpu_vec* x, const numa_gpu_vec* v, numa_gpu_vec* out,
+                        int mode) {
+    if (!op) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(op->ctx, [&] {
+        for (const numa_gpu_vec* q : {x, v, (const numa_gpu_vec*)out}) {
+            same_ctx(op->ctx, q);
+            sized(q, op->impl->size());
+        }
+        need(out->d != x->d && out->d != v->d, NUMA_GPU_ERR_INVALID_ARGUMENT, "d2 output must not alias an input");
+        Bratu3D& f = *op->impl;
+        Context& c = *op->ctx->impl;
+        DeviceArray<double> tmp(f.size());
+        if (mode == NUMA_GPU_DERIV_FD) {
+            f.eval(x->d, tmp.p);
+            dev_norm2(c, x->d, f.size(), c.scalar(kSlotTmp1));
+            f.d2_fd(x->d, tmp.p, c.scalar(kSlotTmp1), v->d, out->d);
+        } else {
+            need(mode == NUMA_GPU_DERIV_ANALYTIC, NUMA_GPU_ERR_INVALID_ARGUMENT, "unknown derivative mode");
+            f.coef(x->d, tmp.p);
+            f.d2_c(tmp.p, v->d, out->d);
+        }
+        c.sync();
+    });
+}
+
+int numa_gpu_bratu3d_jacobi_diag(numa_gpu_bratu3d* op, const numa_gpu_vec* x, numa_gpu_vec* d) {
+    if (!op) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(op->ctx, [&] {
+        same_ctx(op->ctx, x);
+        same_ctx(op->ctx, d);
+        sized(x, op->impl->size());
+        sized(d, op->impl->size());
+        if (x->d == d->d) {
+            DeviceArray<double> tmp(op->impl->size());
+            op->impl->coef(x->d, tmp.p);
+            op->impl->jacobi_diag_c(tmp.p, d->d);
+            op->ctx->impl->sync();
+        } else {
+            op->impl->coef(x->d, d->d);
+            op->impl->jacobi_diag_c(d->d, d->d);
+        }
+    });
+}
+
+// ------------------------------------------------------------------------------ multigrid
+int numa_gpu_mg_create_ex(numa_gpu_ctx* ctx, size_t n, int pre, int post, int precision, int max_levels,
+                          numa_gpu_mg** out) {
+    if (!ctx || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        auto h = std::make_unique<numa_gpu_mg>();
+        h->ctx = ctx;
+        h->impl = std::make_unique<PoissonMG>(*ctx->impl, n, pre, post, precision, max_levels);
+        *out = h.release();
+    });
+}
+
+int numa_gpu_mg_create(numa_gpu_ctx* ctx, size_t n, int pre, int post, numa_gpu_mg** out) {
+    return numa_gpu_mg_create_ex(ctx, n, pre, post, NUMA_GPU_FP64, 0, out);
+}
+
+int numa_gpu_mg_destroy(numa_gpu_mg* mg) {
+    if (mg) {
+        cudaStreamSynchronize(mg->ctx->impl->stream);
+        delete mg;
+    }
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_mg_levels(const numa_gpu_mg* mg, size_t* levels) {
+    if (!mg || !levels) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *levels = mg->impl->levels();
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_mg_apply(numa_gpu_mg* mg, const numa_gpu_vec* r, numa_gpu_vec* z) {
+    if (!mg) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(mg->ctx, [&] {
+        same_ctx(mg->ctx, r);
+        same_ctx(mg->ctx, z);
+        need(r->n == mg->impl->size(), NUMA_GPU_ERR_INVALID_ARGUMENT,
+             "PoissonMG received a residual of incompatible size");
+        need(z->n == r->n, NUMA_GPU_ERR_SIZE_MISMATCH, "output vector length differs");
+        mg->impl->apply(r->d, z->d);
+    });
+}
+
+// ------------------------------------------------------------------------------ providers
+int numa_gpu_provider_create_identity(numa_gpu_ctx* ctx, numa_gpu_provider** out) {
+    if (!ctx || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        auto h = std::make_unique<numa_gpu_provider>();
+        h->ctx = ctx;
+        h->N = 0;
+        h->impl = nullptr;
+        *out = h.release();
+    });
+}
+
+int numa_gpu_provider_create_poisson_mg(numa_gpu_ctx* ctx, size_t n, int pre, int post, int precision,
+                                        numa_gpu_provider** out) {
+    if (!ctx || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        auto h = std::make_unique<numa_gpu_provider>();
+        h->ctx = ctx;
+        h->impl = make_mg_provider(*ctx->impl, n, pre, post, precision, 0);
+        h->N = n * n * n;
+        *out = h.release();
+    });
+}
+
+int numa_gpu_provider_create_jacobi(numa_gpu_bratu3d* op, numa_gpu_provider** out) {
+    if (!op || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(op->ctx, [&] {
+        auto h = std::make_unique<numa_gpu_provider>();
+        h->ctx = op->ctx;
+        h->impl = make_jacobi_provider(*op->impl);
+        h->N = op->impl->size();
+        *out = h.release();
+    });
+}
+
+int numa_gpu_provider_destroy(numa_gpu_provider* p) {
+    if (p) {
+        cudaStreamSynchronize(p->ctx->impl->stream);
+        delete p;
+    }
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_provider_make(numa_gpu_provider* p, const numa_gpu_vec* x) {
+    if (!p) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(p->ctx, [&] {
+        same_ctx(p->ctx, x);
+        if (p->N) sized(x, p->N);
+        if (p->impl) p->impl->make(x->d, nullptr);
+    });
+}
+
+int numa_gpu_provider_apply(numa_gpu_provider* p, const numa_gpu_vec* r, numa_gpu_vec* z) {
+    if (!p) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(p->ctx, [&] {
+        same_ctx(p->ctx, r);
+        same_ctx(p->ctx, z);
+        if (p->N) sized(r, p->N);
+        need(r->n == z->n, NUMA_GPU_ERR_SIZE_MISMATCH, "output vector length differs");
+        if (p->impl) p->impl->apply(r->d, z->d);
+        else dev_copy(*p->ctx->impl, r->d, z->d, r->n);
+    });
+}
+
+// ------------------------------------------------------------------------------ GMRES
+int numa_gpu_krylov_space_create(numa_gpu_ctx* ctx, numa_gpu_krylov_space** out) {
+    if (!ctx || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        auto h = std::make_unique<numa_gpu_krylov_space>();
+        h->ctx = ctx;
+        *out = h.release();
+    });
+}
+
+int numa_gpu_krylov_space_destroy(numa_gpu_krylov_space* s) {
+    if (s) {
+        cudaStreamSynchronize(s->ctx->impl->stream);
+        delete s;
+    }
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_krylov_space_k(const numa_gpu_krylov_space* s, size_t* k) {
+    if (!s || !k) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *k = s->impl.k;
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_gmres(numa_gpu_ctx* ctx, numa_gpu_apply_fn apply, void* apply_user, numa_gpu_precond_fn precond,
+                   void* precond_user, const numa_gpu_vec* b, numa_gpu_vec* x, double rtol, size_t restart,
+                   size_t max_iters, int zero_guess, int orth, int flexible, numa_gpu_krylov_space* save,
+                   const numa_gpu_vec* r_init, numa_gmres_result* result) {
+    if (!ctx || !apply || !result) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    std::memset(result, 0, sizeof(*result));
+    return guard(ctx, [&] {
+        same_ctx(ctx, b);
+        same_ctx(ctx, x);
+        need(b->n == x->n, NUMA_GPU_ERR_SIZE_MISMATCH, "b and x differ in length");
+        const size_t N = b->n;
+        if (r_init) {
+            same_ctx(ctx, r_init);
+            if (r_init->n != N) {  // gmres.hpp:86-90
+                result->rel_res = 1.0;
+                result->breakdown = 1;
+                return;
+            }
+        }
+        if (save) need(save->ctx == ctx, NUMA_GPU_ERR_INVALID_ARGUMENT, "space belongs to another context");
+        CallbackOp A;
+        A.ctx = ctx;
+        A.fn = apply;
+        A.user = apply_user;
+        A.N = N;
+        CallbackPrec M;
+        M.ctx = ctx;
+        M.fn = precond;
+        M.user = precond_user;
+        M.N = N;
+        GmresResult g = gmres_for(ctx, N).solve(A, precond ? &M : nullptr, b->d, x->d,
+                                                gopts(rtol, restart, max_iters, zero_guess, orth, flexible),
+                                                save ? &save->impl : nullptr, r_init ? r_init->d : nullptr);
+        ctx->impl->sync();
+        fill_gmres(g, result);
+    });
+}
+
+static void bratu_jac_setup(numa_gpu_bratu3d* op, const numa_gpu_vec* xpt, int jvp_mode, BratuJacOp& J,
+                            DeviceArray<double>& buf) {
+    Bratu3D& f = *op->impl;
+    Context& c = *op->ctx->impl;
+    const size_t N = f.size();
+    J.x = xpt->d;
+    if (jvp_mode == NUMA_GPU_DERIV_FD) {
+        buf.resize(N);
+        f.eval(xpt->d, buf.p);
+        dev_norm2(c, xpt->d, N, c.scalar(kSlotTmp1));
+        J.fx = buf.p;
+        J.xnorm = c.scalar(kSlotTmp1);
+    } else {
+        need(jvp_mode == NUMA_GPU_DERIV_ANALYTIC, NUMA_GPU_ERR_INVALID_ARGUMENT, "unknown derivative mode");
+        buf.resize(N);
+        f.coef(xpt->d, buf.p);
+        J.c = buf.p;
+    }
+}
+
+int numa_gpu_gmres_bratu3d(numa_gpu_bratu3d* op, const numa_gpu_vec* xpt, int jvp_mode, numa_gpu_provider* provider,
+                           const numa_gpu_vec* b, numa_gpu_vec* x, double rtol, size_t restart, size_t max_iters,
+                           int zero_guess, int orth, int flexible, numa_gpu_krylov_space* save,
+                           const numa_gpu_vec* r_init, numa_gmres_result* result) {
+    if (!op || !result) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    std::memset(result, 0, sizeof(*result));
+    return guard(op->ctx, [&] {
+        const size_t N = op->impl->size();
+        for (const numa_gpu_vec* q : {xpt, b, (const numa_gpu_vec*)x}) {
+            same_ctx(op->ctx, q);
+            sized(q, N);
+        }
+        if (r_init) {
+            same_ctx(op->ctx, r_init);
+            if (r_init->n != N) {
+                result->rel_res = 1.0;
+                result->breakdown = 1;
+                return;
+            }
+        }
+        if (provider) {
+            need(provider->ctx == op->ctx, NUMA_GPU_ERR_INVALID_ARGUMENT, "provider belongs to another context");
+            need(provider->N == 0 || provider->N == N, NUMA_GPU_ERR_SIZE_MISMATCH, "provider size differs");
+        }
+        BratuJacOp J(*op->impl, jvp_mode);
+        DeviceArray<double> buf;
+        bratu_jac_setup(op, xpt, jvp_mode, J, buf);
+        ProviderPrec M;
+        M.p = provider ? provider->impl.get() : nullptr;
+        GmresResult g = gmres_for(op->ctx, N).solve(J, M.p ? &M : nullptr, b->d, x->d,
+                                                    gopts(rtol, restart, max_iters, zero_guess, orth, flexible),
+                                                    save ? &save->impl : nullptr, r_init ? r_init->d : nullptr);
+        op->ctx->impl->sync();
+        fill_gmres(g, result);
+    });
+}
+
+int numa_gpu_gmres_recycled_bratu3d(numa_gpu_bratu3d* op, const numa_gpu_vec* xpt, int jvp_mode,
+                                    numa_gpu_provider* provider, const numa_gpu_vec* b, numa_gpu_vec* x, double rtol,
+                                    size_t restart, size_t max_iters, int orth, const numa_gpu_krylov_space* space,
+                                    numa_gpu_krylov_space* save, numa_gmres_result* result) {
+    if (!op || !result || !space) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    std::memset(result, 0, sizeof(*result));
+    return guard(op->ctx, [&] {
+        const size_t N = op->impl->size();
+        for (const numa_gpu_vec* q : {xpt, b, (const numa_gpu_vec*)x}) {
+            same_ctx(op->ctx, q);
+            sized(q, N);
+        }
+        need(space->ctx == op->ctx, NUMA_GPU_ERR_INVALID_ARGUMENT, "space belongs to another context");
+        BratuJacOp J(*op->impl, jvp_mode);
+        DeviceArray<double> buf;
+        bratu_jac_setup(op, xpt, jvp_mode, J, buf);
+        ProviderPrec M;
+        M.p = provider ? provider->impl.get() : nullptr;
+        GmresResult g = gmres_for(op->ctx, N).solve_recycled(J, M.p ? &M : nullptr, b->d, x->d,
+                                                             gopts(rtol, restart, max_iters, 1, orth, 0), space->impl,
+                                                             save ? &save->impl : nullptr);
+        op->ctx->impl->sync();
+        fill_gmres(g, result);
+    });
+}
+
+// ------------------------------------------------------------------------------ drivers
+double numa_gpu_forcing(const numa_krylov_params* p, size_t k, double rnorm, double rprev, double eta_prev,
+                        double res0) {
+    return forcing(params_from_c(p), k, rnorm, rprev, eta_prev, res0);
+}
+
+static int run_driver(int method, numa_gpu_bratu3d* op, numa_gpu_vec* x, const numa_krylov_params* p,
+                      numa_gpu_provider* provider, numa_krylov_result* result) {
+    if (!op || !x || !result) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    std::memset(result, 0, sizeof(*result));
+    const int rc = guard(op->ctx, [&] {
+        same_ctx(op->ctx, x);
+        sized(x, op->impl->size());
+        if (provider) {
+            need(provider->ctx == op->ctx, NUMA_GPU_ERR_INVALID_ARGUMENT, "provider belongs to another context");
+            need(provider->N == 0 || provider->N == x->n, NUMA_GPU_ERR_SIZE_MISMATCH, "provider size differs");
+        }
+        KrylovParams kp = params_from_c(p);
+        Provider* pc = provider ? provider->impl.get() : nullptr;
+        if (method == NUMA_GPU_METHOD_NK) newton_krylov(*op->impl, x->d, kp, pc, *result);
+        else if (method == NUMA_GPU_METHOD_TF2018) tf_chebyshev_2018(*op->impl, x->d, kp, pc, *result);
+        else {
+            if (method == NUMA_GPU_METHOD_CHEB_REC) kp.recycle = true;
+            chebyshev_inexact(*op->impl, x->d, kp, pc, *result);
+        }
+    });
+    result->status = rc;
+    return rc;
+}
+
+int numa_gpu_newton_krylov(numa_gpu_bratu3d* op, numa_gpu_vec* x, const numa_krylov_params* p,
+                           numa_gpu_provider* provider, numa_krylov_result* result) {
+    return run_driver(NUMA_GPU_METHOD_NK, op, x, p, provider, result);
+}
+
+int numa_gpu_chebyshev_inexact(numa_gpu_bratu3d* op, numa_gpu_vec* x, const numa_krylov_params* p,
+                               numa_gpu_provider* provider, numa_krylov_result* result) {
+    return run_driver(NUMA_GPU_METHOD_CHEB, op, x, p, provider, result);
+}
+
+int numa_gpu_tf_chebyshev_2018(numa_gpu_bratu3d* op, numa_gpu_vec* x, const numa_krylov_params* p,
+                               numa_gpu_provider* provider, numa_krylov_result* result) {
+    return run_driver(NUMA_GPU_METHOD_TF2018, op, x, p, provider, result);
+}
+
+int numa_gpu_solve_bratu3d_host(numa_gpu_ctx* ctx, size_t n, double lambda, int method, int precond_kind,
+                                int mg_precision, const numa_krylov_params* p, const double* x0, double* x_out,
+                                numa_krylov_result* result) {
+    if (!ctx || !x0 || !x_out || !result) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    std::memset(result, 0, sizeof(*result));
+    const int rc = guard(ctx, [&] {
+        need(n > 0 && n <= 65535, NUMA_GPU_ERR_INVALID_ARGUMENT, "grid size out of range");
+        need(method >= NUMA_GPU_METHOD_NK && method <= NUMA_GPU_METHOD_TF2018, NUMA_GPU_ERR_INVALID_ARGUMENT,
+             "unknown method");
+        need(precond_kind >= NUMA_GPU_PRECOND_NONE && precond_kind <= NUMA_GPU_PRECOND_JACOBI,
+             NUMA_GPU_ERR_INVALID_ARGUMENT, "unknown preconditioner");
+        Context& c = *ctx->impl;
+        CtxExtras& e = extras(ctx);
+        if (!e.host_op || e.host_n != n || e.host_lambda != lambda) {
+            e.host_pc.reset();
+            e.host_op = std::make_unique<Bratu3D>(c, n, lambda);
+            e.host_n = n;
+            e.host_lambda = lambda;
+            e.host_kind = -1;
+        }
+        if (e.host_kind != precond_kind || e.host_prec != mg_precision || !e.host_pc) {
+            if (precond_kind == NUMA_GPU_PRECOND_POISSON_MG) e.host_pc = make_mg_provider(c, n, 2, 2, mg_precision, 0);
+            else if (precond_kind == NUMA_GPU_PRECOND_JACOBI) e.host_pc = make_jacobi_provider(*e.host_op);
+            else e.host_pc = make_identity_provider(c, n * n * n);
+            e.host_kind = precond_kind;
+            e.host_prec = mg_precision;
+        }
+        const size_t N = n * n * n;
+        e.host_x.resize(N);
+        NUMA_CUDA(cudaMemcpyAsync(e.host_x.p, x0, N * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        KrylovParams kp = params_from_c(p);
+        Provider* pc = e.host_pc.get();
+        if (method == NUMA_GPU_METHOD_NK) newton_krylov(*e.host_op, e.host_x.p, kp, pc, *result);
+        else if (method == NUMA_GPU_METHOD_TF2018) tf_chebyshev_2018(*e.host_op, e.host_x.p, kp, pc, *result);
+        else {
+            if (method == NUMA_GPU_METHOD_CHEB_REC) kp.recycle = true;
+            chebyshev_inexact(*e.host_op, e.host_x.p, kp, pc, *result);
+        }
+        NUMA_CUDA(cudaMemcpyAsync(x_out, e.host_x.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        c.sync();
+    });
+    result->status = rc;
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,280 @@
+// common.cuh — shared device helpers and the host-side context of libnuma_gpu.
+//
+// Design notes for GB300 (sm_103a):
+//  * FP64 arithmetic runs at ~1.2 TFLOP/s on this part (measured), 1/58 of FP32, so every FP64
+//    kernel here is bound by its FP64 instruction count, not by HBM.  Kernels therefore avoid
+//    redundant FP64 work (no halo recomputation, cached lambda*e^u, precomputed b*h^2, the
+//    3-operation correctly-rounded division by 6 below) and trade memory traffic for FP64 ops.
+//  * FP32 kernels (the mixed-precision V-cycle) are bound by HBM bandwidth.
+//  * The library is built with -fmad=false: no multiply-add is contracted unless written as an
+//    explicit fma, so element-wise results follow the reference's IEEE operation sequence.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+#include "../../include/numa_gpu.h"
+
+namespace numa::gpu {
+
+// ------------------------------------------------------------------------------------------
+// Errors: internal code throws Status; the C ABI converts it to an int status code.
+struct Status : std::runtime_error {
+    int code;
+    Status(int c, const std::string& msg) : std::runtime_error(msg), code(c) {}
+};
+
+[[noreturn]] void throw_cuda(cudaError_t e, const char* what, const char* file, int line);
+
+#define NUMA_CUDA(expr)                                                              \
+    do {                                                                             \
+        cudaError_t numa_cuda_err_ = (expr);                                         \
+        if (numa_cuda_err_ != cudaSuccess)                                           \
+            ::numa::gpu::throw_cuda(numa_cuda_err_, #expr, __FILE__, __LINE__);      \
+    } while (0)
+
+// ------------------------------------------------------------------------------------------
+// Reduction protocol.  A reducing kernel accumulates per-thread FP64 sums, reduces them within
+// the block (warp shuffles, then shared memory), writes one partial per block and result, and
+// takes a ticket; the last block to arrive sums the partials in block order and calls the
+// kernel's finaliser.  The summation order depends only on the launch shape, so results are
+// reproducible run to run.
+constexpr int kMaxRedBlocks = 8192;   // partials per result
+constexpr int kMaxRedResults = 64;    // results per reducing kernel (multi-dot width)
+constexpr int kRedThreads = 256;
+
+struct RedArgs {
+    double* partials;   // kMaxRedBlocks * kMaxRedResults
+    unsigned* ticket;   // one counter, reset to 0 by the last block
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum of R values per thread; every thread of the block must call it.  Returns the
+// block totals in warp 0 lane 0 (others hold unspecified values).
+template <int R>
+__device__ __forceinline__ void block_sum(double (&v)[R], double (*smem)[32]) {
+    const int lane = threadIdx.x & 31;
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int warp = tid >> 5;
+    const int nwarps = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        double s = warp_sum(v[r]);
+        if ((tid & 31) == 0) smem[r][warp] = s;
+    }
+    (void)lane;
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            double s = (tid < nwarps) ? smem[r][tid] : 0.0;
+            v[r] = warp_sum(s);
+        }
+    }
+    __syncthreads();
+}
+
+// Publishes this block's totals and, in the last block to finish, reduces all partials and
+// calls fin(totals) on thread 0.  `v` must hold the block totals in thread 0 (block_sum output).
+template <int R, class Fin>
+__device__ __forceinline__ void grid_reduce_finish(const double (&v)[R], RedArgs red, Fin fin) {
+    __shared__ bool am_last;
+    __shared__ double tot_smem[R][32];
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
+    const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    if (tid == 0) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) red.partials[(size_t)r * kMaxRedBlocks + bid] = v[r];
+        __threadfence();
+        const unsigned t = atomicAdd(red.ticket, 1u);
+        am_last = (t == nblocks - 1);
+    }
+    __syncthreads();
+    if (!am_last) return;
+    __threadfence();
+    const int nthreads = blockDim.x * blockDim.y * blockDim.z;
+    double acc[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        double s = 0.0;
+        for (unsigned b = tid; b < nblocks; b += nthreads) s += __ldcg(red.partials + (size_t)r * kMaxRedBlocks + b);
+        acc[r] = s;
+    }
+    block_sum<R>(acc, tot_smem);
+    if (tid == 0) {
+        fin(acc);
+        *red.ticket = 0u;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Correctly rounded s / 6 in three FP64 operations (Markstein's correction: q = s*RN(1/6),
+// e = s - 6q exactly by FMA, q + e*RN(1/6)).  Equal to IEEE s / 6.0 for every finite s outside
+// the subnormal range (checked against IEEE division on the GPU and on 2e8 random values on the
+// CPU); the sign of a zero result may differ, which no later operation observes.
+__device__ __forceinline__ double div6(double s) {
+    const double r = 0.16666666666666666;  // RN(1/6)
+    const double q = __dmul_rn(s, r);
+    const double e = __fma_rn(-q, 6.0, s);
+    return __fma_rn(e, r, q);
+}
+__device__ __forceinline__ float div6(float s) {
+    const float r = 0.16666667f;
+    const float q = __fmul_rn(s, r);
+    const float e = __fmaf_rn(-q, 6.0f, s);
+    return __fmaf_rn(e, r, q);
+}
+
+// a / d given rd = RN(1/d): the same correction for a runtime divisor.  Within one ulp of IEEE
+// division and equal to it for all but rare (a, d) pairs.
+__device__ __forceinline__ double div_by(double a, double d, double rd) {
+    const double q = __dmul_rn(a, rd);
+    const double e = __fma_rn(-q, d, a);
+    return __fma_rn(e, rd, q);
+}
+
+// ------------------------------------------------------------------------------------------
+// Host-side context: one device, one stream, reduction scratch and device scalars.
+constexpr int kNumScalars = 2048;
+constexpr size_t kMaxRestart = 250;  // GMRES(m) limit of the device scalar layout below
+
+struct Context {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    RedArgs red{};
+    double* d_scalars = nullptr;  // kNumScalars device scalars
+    double* h_scalars = nullptr;  // pinned host mirror
+    cudaEvent_t done = nullptr;
+    uint64_t launches = 0;
+    bool timing = false;
+    std::string last_error;
+
+    explicit Context(int dev);
+    ~Context();
+    Context(const Context&) = delete;
+    Context& operator=(const Context&) = delete;
+
+    void sync();
+    // Copies count device doubles to host memory and waits for them.
+    void fetch(const double* dsrc, int count, double* host);
+    double fetch1(const double* dsrc) {
+        double v;
+        fetch(dsrc, 1, &v);
+        return v;
+    }
+    double* scalar(int slot) { return d_scalars + slot; }
+    // Number of blocks of kRedThreads threads for a grid-stride reduction over N elements.
+    unsigned red_grid(size_t N) const;
+    void count_launch(unsigned n = 1) { launches += n; }
+    void check_launch(const char* what);
+};
+
+// Device scalar slots with fixed roles.
+enum ScalarSlot : int {
+    kSlotTmp0 = 0,        // public-API reductions
+    kSlotTmp1 = 1,
+    kSlotNormF = 8,       // ||F|| of the last evaluation
+    kSlotFdH = 16,        // finite-difference step h, 1/h, zero-direction flag
+    kSlotFdRh = 17,
+    kSlotFdZero = 18,
+    kSlotFdXnorm = 19,
+    kSlotGmresH = 64,     // Hessenberg column, m + 2 entries
+    kSlotGmresH2 = 320,   // CGS2 second-pass coefficients, up to 16
+    kSlotGmresY = 400,    // least-squares solution y, m entries
+    kSlotGmresCoef = 700, // recycled-solve coefficients, 2k + 1 entries
+};
+
+// Pinned host staging for small vectors moving to the device.
+struct PinnedBuf {
+    double* p = nullptr;
+    size_t cap = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf&) = delete;
+    PinnedBuf& operator=(const PinnedBuf&) = delete;
+    ~PinnedBuf() {
+        if (p) cudaFreeHost(p);
+    }
+    double* get(size_t count) {
+        if (count > cap) {
+            if (p) cudaFreeHost(p);
+            p = nullptr;
+            cap = 0;
+            NUMA_CUDA(cudaMallocHost(reinterpret_cast<void**>(&p), count * sizeof(double)));
+            cap = count;
+        }
+        return p;
+    }
+};
+
+// Owning device array with capacity reuse.
+template <class T>
+struct DeviceArray {
+    T* p = nullptr;
+    size_t n = 0;
+    size_t cap = 0;
+    DeviceArray() = default;
+    explicit DeviceArray(size_t count) { resize(count); }
+    ~DeviceArray() { release(); }
+    DeviceArray(const DeviceArray&) = delete;
+    DeviceArray& operator=(const DeviceArray&) = delete;
+    DeviceArray(DeviceArray&& o) noexcept : p(o.p), n(o.n), cap(o.cap) { o.p = nullptr; o.n = o.cap = 0; }
+    DeviceArray& operator=(DeviceArray&& o) noexcept {
+        if (this != &o) {
+            release();
+            p = o.p; n = o.n; cap = o.cap;
+            o.p = nullptr; o.n = o.cap = 0;
+        }
+        return *this;
+    }
+    void resize(size_t count) {
+        if (count > cap) {
+            release();
+            if (count > 0) {
+                cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+                if (e == cudaErrorMemoryAllocation) {
+                    cudaGetLastError();
+                    p = nullptr;
+                    throw Status(NUMA_GPU_ERR_OUT_OF_MEMORY, "cudaMalloc failed: out of device memory");
+                }
+                NUMA_CUDA(e);
+            }
+            cap = count;
+        }
+        n = count;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = cap = 0;
+    }
+    void swap(DeviceArray& o) noexcept {
+        std::swap(p, o.p);
+        std::swap(n, o.n);
+        std::swap(cap, o.cap);
+    }
+};
+
+}  // namespace numa::gpu
+
+// Public opaque handle types (declared in numa_gpu.h).
+struct numa_gpu_ctx {
+    numa::gpu::Context* impl;
+};
+
+struct numa_gpu_vec {
+    numa_gpu_ctx* ctx;
+    double* d;
+    size_t n;
+    bool owns;
+};

@@ -1,0 +1,554 @@
+"""Python binding of libnuma_gpu.so (ctypes over the C ABI of include/numa_gpu.h).
+
+The objects mirror the reference's C++ interfaces (namespace numa::op):
+``Bratu3D`` (eval / jvp / d2 / jacobi_diag), ``PoissonMG`` (V-cycle), preconditioner
+``Provider`` objects (make / apply), ``gmres`` / ``gmres_recycled`` and the drivers
+``newton_krylov``, ``chebyshev_inexact`` and ``tf_chebyshev_2018``.  Vectors live on the GPU
+(``Vec``); ``Vec.from_numpy`` / ``Vec.numpy`` move them to and from host memory.
+
+There is no CPU fallback: loading fails loudly when the library has not been built, and every
+call that needs a GPU raises ``NumaGPUError`` when there is none.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = Path(os.environ.get("NUMA_GPU_LIB", HERE / "libnuma_gpu.so"))
+
+# enums (include/numa_gpu.h)
+OK = 0
+FP64, FP32 = 0, 1
+ANALYTIC, FD = 0, 1
+MGS, CGS2 = 0, 1
+METHODS = {"nk": 0, "cheb": 1, "rec": 2, "tf2018": 3}
+PRECONDS = {"none": 0, "mg": 1, "jacobi": 2}
+
+
+class KrylovParams(C.Structure):
+    """numa_krylov_params: KrylovParams (methods/krylov_newton.hpp:24-38) plus extensions."""
+    _fields_ = [
+        ("rtol_nl", C.c_double), ("max_nl", C.c_uint64), ("eta_init", C.c_double),
+        ("eta_max", C.c_double), ("gamma", C.c_double), ("alpha", C.c_double),
+        ("eta2_factor", C.c_double), ("eta2_max", C.c_double), ("gmres_restart", C.c_uint64),
+        ("gmres_max_iters", C.c_uint64), ("armijo", C.c_double), ("min_lambda", C.c_double),
+        ("recycle", C.c_int32), ("jvp_mode", C.c_int32), ("d2_mode", C.c_int32),
+        ("orth", C.c_int32), ("flexible", C.c_int32), ("jvp_precision", C.c_int32),
+        ("reserved", C.c_int32 * 4),
+    ]
+
+
+class KrylovResult(C.Structure):
+    """numa_krylov_result: KrylovResult (krylov_newton.hpp:40-49) plus timers."""
+    _fields_ = [
+        ("converged", C.c_int32), ("status", C.c_int32), ("iters", C.c_uint64),
+        ("n_F", C.c_uint64), ("n_JVP", C.c_uint64), ("n_D2", C.c_uint64),
+        ("n_lin_iters", C.c_uint64), ("n_lin_failures", C.c_uint64), ("n_prec", C.c_uint64),
+        ("res0", C.c_double), ("res", C.c_double), ("t_F", C.c_double), ("t_JVP", C.c_double),
+        ("t_D2", C.c_double), ("t_prec", C.c_double), ("t_setup_dynamic", C.c_double),
+        ("t_total", C.c_double),
+    ]
+
+
+class GmresResult(C.Structure):
+    """numa_gmres_result: GmresResult (linalg/gmres.hpp:14-21)."""
+    _fields_ = [
+        ("iters", C.c_uint64), ("matvecs", C.c_uint64), ("precs", C.c_uint64),
+        ("rel_res", C.c_double), ("converged", C.c_int32), ("breakdown", C.c_int32),
+    ]
+
+
+def to_dict(s) -> dict:
+    return {name: getattr(s, name) for name, _ in s._fields_ if name != "reserved"}
+
+
+APPLY_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p)
+PRECOND_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p)
+
+_P = C.c_void_p
+_PP = C.POINTER(C.c_void_p)
+_SZ = C.c_size_t
+_D = C.c_double
+_I = C.c_int
+_F64P = C.POINTER(C.c_double)
+
+# name -> (argtypes, restype)
+SIGNATURES = {
+    "numa_gpu_abi_version": ([], _I),
+    "numa_gpu_status_string": ([_I], C.c_char_p),
+    "numa_krylov_params_default": ([C.POINTER(KrylovParams)], None),
+    "numa_gpu_ctx_create": ([_I, _PP], _I),
+    "numa_gpu_ctx_destroy": ([_P], _I),
+    "numa_gpu_ctx_synchronize": ([_P], _I),
+    "numa_gpu_ctx_last_error": ([_P], C.c_char_p),
+    "numa_gpu_ctx_set_timing": ([_P, _I], _I),
+    "numa_gpu_ctx_kernel_launches": ([_P, C.POINTER(C.c_uint64)], _I),
+    "numa_gpu_ctx_reset_kernel_launches": ([_P], _I),
+    "numa_gpu_ctx_stream": ([_P, _PP], _I),
+    "numa_gpu_vec_create": ([_P, _SZ, _PP], _I),
+    "numa_gpu_vec_destroy": ([_P], _I),
+    "numa_gpu_vec_size": ([_P, C.POINTER(_SZ)], _I),
+    "numa_gpu_vec_device_ptr": ([_P, _PP], _I),
+    "numa_gpu_vec_upload": ([_P, _F64P, _SZ], _I),
+    "numa_gpu_vec_download": ([_P, _F64P, _SZ], _I),
+    "numa_gpu_vec_fill": ([_P, _D], _I),
+    "numa_gpu_vec_copy": ([_P, _P], _I),
+    "numa_gpu_vec_dot": ([_P, _P, _F64P], _I),
+    "numa_gpu_vec_norm2": ([_P, _F64P], _I),
+    "numa_gpu_vec_axpy": ([_D, _P, _P], _I),
+    "numa_gpu_bratu3d_create": ([_P, _SZ, _D, _PP], _I),
+    "numa_gpu_bratu3d_destroy": ([_P], _I),
+    "numa_gpu_bratu3d_size": ([_P, C.POINTER(_SZ)], _I),
+    "numa_gpu_bratu3d_eval": ([_P, _P, _P], _I),
+    "numa_gpu_bratu3d_jvp": ([_P, _P, _P, _P, _I], _I),
+    "numa_gpu_bratu3d_d2": ([_P, _P, _P, _P, _I], _I),
+    "numa_gpu_bratu3d_jacobi_diag": ([_P, _P, _P], _I),
+    "numa_gpu_mg_create": ([_P, _SZ, _I, _I, _PP], _I),
+    "numa_gpu_mg_create_ex": ([_P, _SZ, _I, _I, _I, _I, _PP], _I),
+    "numa_gpu_mg_destroy": ([_P], _I),
+    "numa_gpu_mg_levels": ([_P, C.POINTER(_SZ)], _I),
+    "numa_gpu_mg_apply": ([_P, _P, _P], _I),
+    "numa_gpu_provider_create_identity": ([_P, _PP], _I),
+    "numa_gpu_provider_create_poisson_mg": ([_P, _SZ, _I, _I, _I, _PP], _I),
+    "numa_gpu_provider_create_jacobi": ([_P, _PP], _I),
+    "numa_gpu_provider_destroy": ([_P], _I),
+    "numa_gpu_provider_make": ([_P, _P], _I),
+    "numa_gpu_provider_apply": ([_P, _P, _P], _I),
+    "numa_gpu_krylov_space_create": ([_P, _PP], _I),
+    "numa_gpu_krylov_space_destroy": ([_P], _I),
+    "numa_gpu_krylov_space_k": ([_P, C.POINTER(_SZ)], _I),
+    "numa_gpu_gmres": ([_P, APPLY_FN, _P, PRECOND_FN, _P, _P, _P, _D, _SZ, _SZ, _I, _I, _I, _P, _P,
+                        C.POINTER(GmresResult)], _I),
+    "numa_gpu_gmres_bratu3d": ([_P, _P, _I, _P, _P, _P, _D, _SZ, _SZ, _I, _I, _I, _P, _P,
+                                C.POINTER(GmresResult)], _I),
+    "numa_gpu_gmres_recycled_bratu3d": ([_P, _P, _I, _P, _P, _P, _D, _SZ, _SZ, _I, _P, _P,
+                                         C.POINTER(GmresResult)], _I),
+    "numa_gpu_forcing": ([C.POINTER(KrylovParams), _SZ, _D, _D, _D, _D], _D),
+    "numa_gpu_newton_krylov": ([_P, _P, C.POINTER(KrylovParams), _P, C.POINTER(KrylovResult)], _I),
+    "numa_gpu_chebyshev_inexact": ([_P, _P, C.POINTER(KrylovParams), _P, C.POINTER(KrylovResult)], _I),
+    "numa_gpu_tf_chebyshev_2018": ([_P, _P, C.POINTER(KrylovParams), _P, C.POINTER(KrylovResult)], _I),
+    "numa_gpu_solve_bratu3d_host": ([_P, _SZ, _D, _I, _I, _I, C.POINTER(KrylovParams), _F64P, _F64P,
+                                     C.POINTER(KrylovResult)], _I),
+}
+
+_lib = None
+
+
+def load(path: str | Path | None = None) -> C.CDLL:
+    """Loads libnuma_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise ImportError(f"{p} not found: build it with chebyshev-nonlinear-lab_gb300/build.py")
+    lib = C.CDLL(str(p))
+    for name, (args, res) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class NumaGPUError(RuntimeError):
+    def __init__(self, code: int, where: str, detail: str = ""):
+        self.code = code
+        lib = load()
+        msg = f"{where}: {lib.numa_gpu_status_string(code).decode()} ({code})"
+        if detail:
+            msg += f": {detail}"
+        super().__init__(msg)
+
+
+def default_params(**kw) -> KrylovParams:
+    """KrylovParams{} (methods/krylov_newton.hpp:24-38) with keyword overrides."""
+    p = KrylovParams()
+    load().numa_krylov_params_default(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Context:
+    """One device and one stream (numa_gpu_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.numa_gpu_ctx_create(device, C.byref(h))
+        if rc != OK:
+            raise NumaGPUError(rc, "numa_gpu_ctx_create")
+        self.h = h
+
+    def check(self, rc: int, where: str):
+        if rc != OK:
+            raise NumaGPUError(rc, where, self.lib.numa_gpu_ctx_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.lib.numa_gpu_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        self.check(self.lib.numa_gpu_ctx_synchronize(self.h), "synchronize")
+
+    def set_timing(self, on: bool):
+        self.check(self.lib.numa_gpu_ctx_set_timing(self.h, int(on)), "set_timing")
+
+    def kernel_launches(self) -> int:
+        v = C.c_uint64()
+        self.check(self.lib.numa_gpu_ctx_kernel_launches(self.h, C.byref(v)), "kernel_launches")
+        return v.value
+
+    def reset_kernel_launches(self):
+        self.check(self.lib.numa_gpu_ctx_reset_kernel_launches(self.h), "reset_kernel_launches")
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self.check(self.lib.numa_gpu_ctx_stream(self.h, C.byref(s)), "stream")
+        return s.value or 0
+
+    def vec(self, n: int) -> "Vec":
+        return Vec(self, n)
+
+    def from_numpy(self, a) -> "Vec":
+        a = _f64(a).ravel()
+        v = Vec(self, a.size)
+        v.upload(a)
+        return v
+
+
+class Vec:
+    """A device FP64 vector (numa_gpu_vec); the reference's DVec on the GPU."""
+
+    def __init__(self, ctx: Context, n: int, handle=None):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.n = int(n)
+        if handle is None:
+            h = C.c_void_p()
+            ctx.check(self.lib.numa_gpu_vec_create(ctx.h, self.n, C.byref(h)), "vec_create")
+            self.h = h
+            self.owned = True
+        else:
+            self.h = C.c_void_p(handle)
+            self.owned = False
+
+    def close(self):
+        if self.owned and self.h:
+            self.lib.numa_gpu_vec_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, a):
+        a = _f64(a).ravel()
+        self.ctx.check(self.lib.numa_gpu_vec_upload(self.h, a.ctypes.data_as(_F64P), a.size), "vec_upload")
+        return self
+
+    def numpy(self) -> np.ndarray:
+        out = np.empty(self.n)
+        self.ctx.check(self.lib.numa_gpu_vec_download(self.h, out.ctypes.data_as(_F64P), self.n), "vec_download")
+        return out
+
+    def fill(self, v: float):
+        self.ctx.check(self.lib.numa_gpu_vec_fill(self.h, float(v)), "vec_fill")
+        return self
+
+    def copy_from(self, src: "Vec"):
+        self.ctx.check(self.lib.numa_gpu_vec_copy(src.h, self.h), "vec_copy")
+        return self
+
+    def dot(self, other: "Vec") -> float:
+        out = C.c_double()
+        self.ctx.check(self.lib.numa_gpu_vec_dot(self.h, other.h, C.byref(out)), "vec_dot")
+        return out.value
+
+    def norm2(self) -> float:
+        out = C.c_double()
+        self.ctx.check(self.lib.numa_gpu_vec_norm2(self.h, C.byref(out)), "vec_norm2")
+        return out.value
+
+    def axpy(self, a: float, x: "Vec"):
+        """self += a * x"""
+        self.ctx.check(self.lib.numa_gpu_vec_axpy(float(a), x.h, self.h), "vec_axpy")
+        return self
+
+    def device_ptr(self) -> int:
+        p = C.c_void_p()
+        self.ctx.check(self.lib.numa_gpu_vec_device_ptr(self.h, C.byref(p)), "vec_device_ptr")
+        return p.value or 0
+
+
+class Bratu3D:
+    """Bratu3D(n, lambda) (problems/bratu3d.hpp:12-16) on the GPU."""
+
+    def __init__(self, ctx: Context, n: int, lam: float = 1.0):
+        self.ctx, self.lib, self.n, self.lam = ctx, ctx.lib, int(n), float(lam)
+        h = C.c_void_p()
+        ctx.check(self.lib.numa_gpu_bratu3d_create(ctx.h, self.n, self.lam, C.byref(h)), "bratu3d_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.numa_gpu_bratu3d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def size(self) -> int:
+        return self.n ** 3
+
+    def eval(self, x: Vec, out: Vec):
+        self.ctx.check(self.lib.numa_gpu_bratu3d_eval(self.h, x.h, out.h), "bratu3d_eval")
+
+    def jvp(self, x: Vec, v: Vec, out: Vec, mode: int = ANALYTIC):
+        self.ctx.check(self.lib.numa_gpu_bratu3d_jvp(self.h, x.h, v.h, out.h, mode), "bratu3d_jvp")
+
+    def d2(self, x: Vec, v: Vec, out: Vec, mode: int = ANALYTIC):
+        self.ctx.check(self.lib.numa_gpu_bratu3d_d2(self.h, x.h, v.h, out.h, mode), "bratu3d_d2")
+
+    def jacobi_diag(self, x: Vec, d: Vec):
+        self.ctx.check(self.lib.numa_gpu_bratu3d_jacobi_diag(self.h, x.h, d.h), "bratu3d_jacobi_diag")
+
+
+class PoissonMG:
+    """PoissonMG(n, pre, post) (linalg/poisson_mg.hpp:24-64); precision / max_levels extend it."""
+
+    def __init__(self, ctx: Context, n: int, pre: int = 2, post: int = 2, precision: int = FP64,
+                 max_levels: int = 0):
+        self.ctx, self.lib, self.n = ctx, ctx.lib, int(n)
+        h = C.c_void_p()
+        ctx.check(self.lib.numa_gpu_mg_create_ex(ctx.h, self.n, pre, post, precision, max_levels, C.byref(h)),
+                  "mg_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.numa_gpu_mg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def levels(self) -> int:
+        v = C.c_size_t()
+        self.ctx.check(self.lib.numa_gpu_mg_levels(self.h, C.byref(v)), "mg_levels")
+        return v.value
+
+    def __call__(self, r: Vec, z: Vec):
+        self.ctx.check(self.lib.numa_gpu_mg_apply(self.h, r.h, z.h), "mg_apply")
+
+
+class Provider:
+    """A preconditioner provider: make(x) binds it, apply(r, z) applies it."""
+
+    def __init__(self, ctx: Context, handle, kind: str):
+        self.ctx, self.lib, self.h, self.kind = ctx, ctx.lib, handle, kind
+
+    @classmethod
+    def identity(cls, ctx: Context) -> "Provider":
+        h = C.c_void_p()
+        ctx.check(ctx.lib.numa_gpu_provider_create_identity(ctx.h, C.byref(h)), "provider_identity")
+        return cls(ctx, h, "none")
+
+    @classmethod
+    def poisson_mg(cls, ctx: Context, n: int, pre: int = 2, post: int = 2, precision: int = FP64) -> "Provider":
+        h = C.c_void_p()
+        ctx.check(ctx.lib.numa_gpu_provider_create_poisson_mg(ctx.h, n, pre, post, precision, C.byref(h)),
+                  "provider_poisson_mg")
+        return cls(ctx, h, "mg")
+
+    @classmethod
+    def jacobi(cls, op: Bratu3D) -> "Provider":
+        h = C.c_void_p()
+        op.ctx.check(op.lib.numa_gpu_provider_create_jacobi(op.h, C.byref(h)), "provider_jacobi")
+        p = cls(op.ctx, h, "jacobi")
+        p._op = op  # keep the operator alive
+        return p
+
+    @classmethod
+    def create(cls, ctx: Context, kind: str, op: Bratu3D, precision: int = FP64) -> "Provider | None":
+        if kind == "mg":
+            return cls.poisson_mg(ctx, op.n, precision=precision)
+        if kind == "jacobi":
+            return cls.jacobi(op)
+        return cls.identity(ctx)
+
+    def close(self):
+        if self.h:
+            self.lib.numa_gpu_provider_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def make(self, x: Vec):
+        self.ctx.check(self.lib.numa_gpu_provider_make(self.h, x.h), "provider_make")
+        return self
+
+    def apply(self, r: Vec, z: Vec):
+        self.ctx.check(self.lib.numa_gpu_provider_apply(self.h, r.h, z.h), "provider_apply")
+
+
+class KrylovSpace:
+    """Saved Arnoldi basis (linalg/gmres.hpp:25-35), on the device."""
+
+    def __init__(self, ctx: Context):
+        self.ctx, self.lib = ctx, ctx.lib
+        h = C.c_void_p()
+        ctx.check(self.lib.numa_gpu_krylov_space_create(ctx.h, C.byref(h)), "krylov_space_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.numa_gpu_krylov_space_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def k(self) -> int:
+        v = C.c_size_t()
+        self.ctx.check(self.lib.numa_gpu_krylov_space_k(self.h, C.byref(v)), "krylov_space_k")
+        return v.value
+
+
+def gmres(ctx: Context, apply, b: Vec, x: Vec, rtol: float, restart: int, max_iters: int, precond=None,
+          zero_guess: bool = True, orth: int = MGS, flexible: bool = False, save: KrylovSpace | None = None,
+          r_init: Vec | None = None) -> dict:
+    """gmres(apply, precond, b, x, ...) (linalg/gmres.hpp:61-65) with Python callables
+    apply(v: Vec, out: Vec) and precond(r: Vec, z: Vec) on device vectors."""
+    errors = []
+
+    def _wrap(fn):
+        def cb(user, vp, op):
+            try:
+                fn(Vec(ctx, b.n, vp), Vec(ctx, b.n, op))
+                return 0
+            except Exception as e:  # reported through the status code
+                errors.append(e)
+                return 1
+        return cb
+
+    a_cb = APPLY_FN(_wrap(apply))
+    p_cb = PRECOND_FN(_wrap(precond)) if precond is not None else PRECOND_FN()
+    res = GmresResult()
+    rc = ctx.lib.numa_gpu_gmres(ctx.h, a_cb, None, p_cb, None, b.h, x.h, rtol, restart, max_iters,
+                                int(zero_guess), orth, int(flexible), save.h if save else None,
+                                r_init.h if r_init else None, C.byref(res))
+    if errors:
+        raise errors[0]
+    ctx.check(rc, "gmres")
+    return to_dict(res)
+
+
+def gmres_bratu3d(op: Bratu3D, xpt: Vec, b: Vec, x: Vec, rtol: float, restart: int, max_iters: int,
+                  provider: Provider | None = None, jvp_mode: int = ANALYTIC, zero_guess: bool = True,
+                  orth: int = MGS, flexible: bool = False, save: KrylovSpace | None = None,
+                  r_init: Vec | None = None) -> dict:
+    res = GmresResult()
+    op.ctx.check(op.lib.numa_gpu_gmres_bratu3d(op.h, xpt.h, jvp_mode, provider.h if provider else None, b.h, x.h,
+                                               rtol, restart, max_iters, int(zero_guess), orth, int(flexible),
+                                               save.h if save else None, r_init.h if r_init else None,
+                                               C.byref(res)), "gmres_bratu3d")
+    return to_dict(res)
+
+
+def gmres_recycled_bratu3d(op: Bratu3D, xpt: Vec, b: Vec, x: Vec, rtol: float, restart: int, max_iters: int,
+                           space: KrylovSpace, provider: Provider | None = None, jvp_mode: int = ANALYTIC,
+                           orth: int = MGS, save: KrylovSpace | None = None) -> dict:
+    res = GmresResult()
+    op.ctx.check(op.lib.numa_gpu_gmres_recycled_bratu3d(op.h, xpt.h, jvp_mode, provider.h if provider else None,
+                                                        b.h, x.h, rtol, restart, max_iters, orth, space.h,
+                                                        save.h if save else None, C.byref(res)),
+                 "gmres_recycled_bratu3d")
+    return to_dict(res)
+
+
+def forcing(params: KrylovParams, k: int, rnorm: float, rprev: float, eta_prev: float, res0: float) -> float:
+    return load().numa_gpu_forcing(C.byref(params), k, rnorm, rprev, eta_prev, res0)
+
+
+def _driver(name: str, op: Bratu3D, x: Vec, params: KrylovParams | None, provider: Provider | None) -> dict:
+    p = params if params is not None else default_params()
+    res = KrylovResult()
+    rc = getattr(op.lib, name)(op.h, x.h, C.byref(p), provider.h if provider else None, C.byref(res))
+    op.ctx.check(rc, name)
+    return to_dict(res)
+
+
+def newton_krylov(op: Bratu3D, x: Vec, params: KrylovParams | None = None, provider: Provider | None = None) -> dict:
+    """newton_krylov (methods/krylov_newton.hpp:69-114); x: x0 in, solution out."""
+    return _driver("numa_gpu_newton_krylov", op, x, params, provider)
+
+
+def chebyshev_inexact(op: Bratu3D, x: Vec, params: KrylovParams | None = None,
+                      provider: Provider | None = None) -> dict:
+    """chebyshev_inexact (methods/krylov_newton.hpp:116-189)."""
+    return _driver("numa_gpu_chebyshev_inexact", op, x, params, provider)
+
+
+def tf_chebyshev_2018(op: Bratu3D, x: Vec, params: KrylovParams | None = None,
+                      provider: Provider | None = None) -> dict:
+    """tf_chebyshev_2018 (methods/tf_chebyshev_2018.hpp:52-132)."""
+    return _driver("numa_gpu_tf_chebyshev_2018", op, x, params, provider)
+
+
+def solve(op: Bratu3D, x: Vec, method: str = "nk", params: KrylovParams | None = None,
+          provider: Provider | None = None) -> dict:
+    p = params if params is not None else default_params()
+    if method == "rec":
+        p.recycle = 1
+        return chebyshev_inexact(op, x, p, provider)
+    return {"nk": newton_krylov, "cheb": chebyshev_inexact, "tf2018": tf_chebyshev_2018}[method](op, x, p, provider)
+
+
+def solve_bratu3d_host(ctx: Context, n: int, lam: float, x0: np.ndarray, out: np.ndarray | None = None,
+                       method: str = "nk", precond: str = "mg", mg_precision: int = FP64,
+                       params: KrylovParams | None = None) -> tuple[np.ndarray, dict]:
+    """Host buffers in, host buffers out (numa_gpu_solve_bratu3d_host)."""
+    p = params if params is not None else default_params()
+    x0 = _f64(x0).ravel()
+    if out is None:
+        out = np.empty(n ** 3)
+    res = KrylovResult()
+    rc = ctx.lib.numa_gpu_solve_bratu3d_host(ctx.h, n, lam, METHODS[method], PRECONDS[precond], mg_precision,
+                                             C.byref(p), x0.ctypes.data_as(_F64P), out.ctypes.data_as(_F64P),
+                                             C.byref(res))
+    ctx.check(rc, "solve_bratu3d_host")
+    return out, to_dict(res)

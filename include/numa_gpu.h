@@ -1,0 +1,279 @@
+/*
+ * numa_gpu.h — C ABI of libnuma_gpu.so, the GB300 (sm_103a) implementation of the
+ * matrix-free nonlinear-solve path of kapumota/chebyshev-nonlinear-lab (namespace numa::op).
+ *
+ * The reference exposes this path as header-only C++20 templates with no ABI.  Each entry
+ * point below replaces one of those interfaces; the citation beside it names the reference
+ * file:line whose behaviour it reproduces (paths relative to the reference project root).
+ *
+ * Conventions (shared by every function):
+ *   - Every function returns an int status: NUMA_GPU_OK (0) or a numa_gpu_status code.
+ *     Numerical failure is NOT an error status: it is reported in the result structs
+ *     (converged / breakdown / n_lin_failures), exactly as the reference does.
+ *   - Handles own device memory; *_destroy frees it.  Host buffers belong to the caller.
+ *   - All work is stream-ordered on the context's stream; calls that return a scalar or a
+ *     result struct to the host synchronise that stream first.
+ *   - Objects are not thread-safe (the reference's PoissonMG keeps mutable work arrays,
+ *     linalg/poisson_mg.hpp:11); one host thread drives one context.
+ *   - Vectors are FP64, lexicographic (i*n + j)*n + k with k fastest (problems/bratu3d.hpp:85),
+ *     Dirichlet boundary values implicit (no ghost layer).
+ */
+#ifndef NUMA_GPU_H
+#define NUMA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NUMA_GPU_ABI_VERSION 1
+
+/* ---------------------------------------------------------------- status codes */
+typedef enum numa_gpu_status {
+    NUMA_GPU_OK = 0,
+    NUMA_GPU_ERR_INVALID_ARGUMENT = 1, /* std::invalid_argument in PoissonMG (poisson_mg.hpp:29-36, :71-74) */
+    NUMA_GPU_ERR_OVERFLOW = 2,         /* std::overflow_error in PoissonMG (poisson_mg.hpp:38-42) */
+    NUMA_GPU_ERR_SIZE_MISMATCH = 3,    /* vector lengths disagree with the operator size */
+    NUMA_GPU_ERR_CUDA = 4,             /* a CUDA runtime call failed; see numa_gpu_last_error */
+    NUMA_GPU_ERR_OUT_OF_MEMORY = 5,
+    NUMA_GPU_ERR_NO_DEVICE = 6,
+    NUMA_GPU_ERR_CALLBACK = 7,         /* a user apply/precond callback returned non-zero */
+    NUMA_GPU_ERR_NOT_SUPPORTED = 8
+} numa_gpu_status;
+
+/* ---------------------------------------------------------------- enums */
+typedef enum numa_gpu_precision {
+    NUMA_GPU_FP64 = 0,
+    NUMA_GPU_FP32 = 1
+} numa_gpu_precision;
+
+/* How a directional derivative is formed. */
+typedef enum numa_gpu_deriv_mode {
+    NUMA_GPU_DERIV_ANALYTIC = 0, /* Bratu3D::jvp / Bratu3D::d2 (problems/bratu3d.hpp:33-56) */
+    NUMA_GPU_DERIV_FD = 1        /* jvp_fd / d2_fd (operators/operator.hpp:100-134) */
+} numa_gpu_deriv_mode;
+
+/* Arnoldi orthogonalisation. */
+typedef enum numa_gpu_orth {
+    NUMA_GPU_ORTH_MGS = 0, /* modified Gram-Schmidt, the reference (linalg/gmres.hpp:141-144) */
+    NUMA_GPU_ORTH_CGS2 = 1 /* classical Gram-Schmidt with one reorthogonalisation, fused multi-dot */
+} numa_gpu_orth;
+
+/* Nonlinear methods of the reference's R1 drivers. */
+typedef enum numa_gpu_method {
+    NUMA_GPU_METHOD_NK = 0,       /* newton_krylov (methods/krylov_newton.hpp:69-114) */
+    NUMA_GPU_METHOD_CHEB = 1,     /* chebyshev_inexact (krylov_newton.hpp:116-189) */
+    NUMA_GPU_METHOD_CHEB_REC = 2, /* chebyshev_inexact with recycle = true */
+    NUMA_GPU_METHOD_TF2018 = 3    /* tf_chebyshev_2018 (methods/tf_chebyshev_2018.hpp:52-132) */
+} numa_gpu_method;
+
+/* Preconditioner providers (the reference's Provider::make(x) -> Bound protocol). */
+typedef enum numa_gpu_precond_kind {
+    NUMA_GPU_PRECOND_NONE = 0,       /* NoPrecond / IdentityPrecond (krylov_newton.hpp:20-22, gmres.hpp:37-39) */
+    NUMA_GPU_PRECOND_POISSON_MG = 1, /* PoissonMGProvider (linalg/poisson_mg.hpp:303-320) */
+    NUMA_GPU_PRECOND_JACOBI = 2      /* BratuJacobi (problems/bratu3d.hpp:104-120) */
+} numa_gpu_precond_kind;
+
+/* ---------------------------------------------------------------- parameter / result structs */
+
+/* KrylovParams (methods/krylov_newton.hpp:24-38), field for field, plus GPU extensions whose
+ * zero value is the reference behaviour. */
+typedef struct numa_krylov_params {
+    double rtol_nl;            /* ||F|| <= rtol_nl * ||F(x0)||            default 1e-8 */
+    uint64_t max_nl;           /*                                           default 50 */
+    double eta_init;           /*                                           default 0.5 */
+    double eta_max;            /*                                           default 0.9 */
+    double gamma;              /* Eisenstat-Walker choice 2                 default 0.9 */
+    double alpha;              /*                                           default 2.0 */
+    double eta2_factor;        /* tolerance of the second Chebyshev solve   default 10 */
+    double eta2_max;           /*                                           default 0.5 */
+    uint64_t gmres_restart;    /*                                           default 50 */
+    uint64_t gmres_max_iters;  /*                                           default 500 */
+    double armijo;             /*                                           default 1e-4 */
+    double min_lambda;         /*                                           default 1e-4 */
+    int32_t recycle;           /* recycle the Krylov space between the two Chebyshev solves */
+    /* --- extensions (0 = reference behaviour) --- */
+    int32_t jvp_mode;          /* numa_gpu_deriv_mode of the Krylov matvec */
+    int32_t d2_mode;           /* numa_gpu_deriv_mode of F''(x)[z,z] */
+    int32_t orth;              /* numa_gpu_orth */
+    int32_t flexible;          /* 1 = FGMRES (stores Z_j = M^-1 v_j; no extra precond per cycle) */
+    int32_t jvp_precision;     /* numa_gpu_precision of the Krylov matvec arithmetic */
+    int32_t reserved[4];
+} numa_krylov_params;
+
+/* KrylovResult (krylov_newton.hpp:40-49) without x (the solution is written into the caller's
+ * vector), plus the per-primitive timers of operators/timing.hpp:16-24 (seconds; measured with
+ * CUDA events on the context stream when timing is enabled, else 0). */
+typedef struct numa_krylov_result {
+    int32_t converged;
+    int32_t status;            /* NUMA_GPU_OK, or the error that ended the solve */
+    uint64_t iters;
+    uint64_t n_F;
+    uint64_t n_JVP;
+    uint64_t n_D2;
+    uint64_t n_lin_iters;
+    uint64_t n_lin_failures;
+    uint64_t n_prec;
+    double res0;
+    double res;
+    double t_F;
+    double t_JVP;
+    double t_D2;
+    double t_prec;
+    double t_setup_dynamic;
+    double t_total;
+} numa_krylov_result;
+
+/* GmresResult (linalg/gmres.hpp:14-21). */
+typedef struct numa_gmres_result {
+    uint64_t iters;
+    uint64_t matvecs;
+    uint64_t precs;
+    double rel_res;
+    int32_t converged;
+    int32_t breakdown;
+} numa_gmres_result;
+
+/* ---------------------------------------------------------------- opaque handles */
+typedef struct numa_gpu_ctx numa_gpu_ctx;
+typedef struct numa_gpu_vec numa_gpu_vec;
+typedef struct numa_gpu_bratu3d numa_gpu_bratu3d;
+typedef struct numa_gpu_mg numa_gpu_mg;
+typedef struct numa_gpu_provider numa_gpu_provider;
+typedef struct numa_gpu_krylov_space numa_gpu_krylov_space;
+
+/* ---------------------------------------------------------------- library / context */
+int numa_gpu_abi_version(void);
+const char* numa_gpu_status_string(int status);
+void numa_krylov_params_default(numa_krylov_params* p);  /* KrylovParams{} defaults */
+
+int numa_gpu_ctx_create(int device, numa_gpu_ctx** out);
+int numa_gpu_ctx_destroy(numa_gpu_ctx* ctx);
+int numa_gpu_ctx_synchronize(numa_gpu_ctx* ctx);
+/* Message of the last failing call on this context ("" if none). */
+const char* numa_gpu_ctx_last_error(numa_gpu_ctx* ctx);
+/* 1 = record per-primitive CUDA-event timers into numa_krylov_result (adds event records). */
+int numa_gpu_ctx_set_timing(numa_gpu_ctx* ctx, int enable);
+/* Number of kernels this library launched on the context since creation / the last reset. */
+int numa_gpu_ctx_kernel_launches(numa_gpu_ctx* ctx, uint64_t* out);
+int numa_gpu_ctx_reset_kernel_launches(numa_gpu_ctx* ctx);
+/* The context's cudaStream_t, as an opaque pointer (for callers that order their own work). */
+int numa_gpu_ctx_stream(numa_gpu_ctx* ctx, void** stream_out);
+
+/* ---------------------------------------------------------------- device vectors (DVec) */
+int numa_gpu_vec_create(numa_gpu_ctx* ctx, size_t n, numa_gpu_vec** out);
+int numa_gpu_vec_destroy(numa_gpu_vec* v);
+int numa_gpu_vec_size(const numa_gpu_vec* v, size_t* n);
+int numa_gpu_vec_device_ptr(numa_gpu_vec* v, double** dptr);
+int numa_gpu_vec_upload(numa_gpu_vec* v, const double* host, size_t n);
+int numa_gpu_vec_download(const numa_gpu_vec* v, double* host, size_t n);
+int numa_gpu_vec_fill(numa_gpu_vec* v, double value);
+int numa_gpu_vec_copy(const numa_gpu_vec* src, numa_gpu_vec* dst);
+/* BLAS-1 of operators/operator.hpp:19-41. */
+int numa_gpu_vec_dot(const numa_gpu_vec* a, const numa_gpu_vec* b, double* out);   /* dot   :19-27 */
+int numa_gpu_vec_norm2(const numa_gpu_vec* a, double* out);                        /* norm2 :29 */
+int numa_gpu_vec_axpy(double a, const numa_gpu_vec* x, numa_gpu_vec* y);           /* axpy  :32-41 */
+
+/* ---------------------------------------------------------------- Bratu3D operator */
+/* Bratu3D(n, lambda) (problems/bratu3d.hpp:12-16). */
+int numa_gpu_bratu3d_create(numa_gpu_ctx* ctx, size_t n, double lambda, numa_gpu_bratu3d** out);
+int numa_gpu_bratu3d_destroy(numa_gpu_bratu3d* op);
+int numa_gpu_bratu3d_size(const numa_gpu_bratu3d* op, size_t* N);
+/* out = F(x)                          Bratu3D::eval (bratu3d.hpp:21-31) */
+int numa_gpu_bratu3d_eval(numa_gpu_bratu3d* op, const numa_gpu_vec* x, numa_gpu_vec* out);
+/* out = F'(x) v   mode ANALYTIC: Bratu3D::jvp (bratu3d.hpp:33-43); FD: jvp_fd (operator.hpp:101-114) */
+int numa_gpu_bratu3d_jvp(numa_gpu_bratu3d* op, const numa_gpu_vec* x, const numa_gpu_vec* v,
+                         numa_gpu_vec* out, int mode);
+/* out = F''(x)[v,v] mode ANALYTIC: Bratu3D::d2 (bratu3d.hpp:46-56); FD: d2_fd (operator.hpp:118-134) */
+int numa_gpu_bratu3d_d2(numa_gpu_bratu3d* op, const numa_gpu_vec* x, const numa_gpu_vec* v,
+                        numa_gpu_vec* out, int mode);
+/* d = 6 h^-2 - lambda e^x             Bratu3D::jacobi_diag (bratu3d.hpp:59-69) */
+int numa_gpu_bratu3d_jacobi_diag(numa_gpu_bratu3d* op, const numa_gpu_vec* x, numa_gpu_vec* d);
+
+/* ---------------------------------------------------------------- Poisson multigrid */
+/* PoissonMG(n, pre, post) (linalg/poisson_mg.hpp:26-64): levels while n is odd, down to 1. */
+int numa_gpu_mg_create(numa_gpu_ctx* ctx, size_t n, int pre, int post, numa_gpu_mg** out);
+/* Extension: precision of the V-cycle arithmetic (FP64 = reference) and a cap on the level
+ * count (0 = the reference hierarchy). */
+int numa_gpu_mg_create_ex(numa_gpu_ctx* ctx, size_t n, int pre, int post, int precision,
+                          int max_levels, numa_gpu_mg** out);
+int numa_gpu_mg_destroy(numa_gpu_mg* mg);
+int numa_gpu_mg_levels(const numa_gpu_mg* mg, size_t* levels);    /* PoissonMG::levels :66 */
+/* z = one V-cycle applied to r        PoissonMG::operator() (poisson_mg.hpp:69-80) */
+int numa_gpu_mg_apply(numa_gpu_mg* mg, const numa_gpu_vec* r, numa_gpu_vec* z);
+
+/* ---------------------------------------------------------------- preconditioner providers */
+/* Provider::make(x) -> Bound, Bound(r, z) (krylov_newton.hpp:20-22, poisson_mg.hpp:303-320,
+ * bratu3d.hpp:104-120).  A provider owns what it creates (the MG hierarchy, the diagonal). */
+int numa_gpu_provider_create_identity(numa_gpu_ctx* ctx, numa_gpu_provider** out);
+int numa_gpu_provider_create_poisson_mg(numa_gpu_ctx* ctx, size_t n, int pre, int post, int precision,
+                                        numa_gpu_provider** out);
+int numa_gpu_provider_create_jacobi(numa_gpu_bratu3d* op, numa_gpu_provider** out);
+int numa_gpu_provider_destroy(numa_gpu_provider* p);
+int numa_gpu_provider_make(numa_gpu_provider* p, const numa_gpu_vec* x);            /* make(x)  */
+int numa_gpu_provider_apply(numa_gpu_provider* p, const numa_gpu_vec* r, numa_gpu_vec* z); /* Bound(r,z) */
+
+/* ---------------------------------------------------------------- GMRES */
+/* KrylovSpace (gmres.hpp:25-35): Arnoldi basis of the last cycle, kept on the device. */
+int numa_gpu_krylov_space_create(numa_gpu_ctx* ctx, numa_gpu_krylov_space** out);
+int numa_gpu_krylov_space_destroy(numa_gpu_krylov_space* s);
+int numa_gpu_krylov_space_k(const numa_gpu_krylov_space* s, size_t* k);
+
+/* User callbacks on device vectors: apply computes out = A v, precond computes z = M^-1 r.
+ * Return 0 on success. */
+typedef int (*numa_gpu_apply_fn)(void* user, const numa_gpu_vec* v, numa_gpu_vec* out);
+typedef int (*numa_gpu_precond_fn)(void* user, const numa_gpu_vec* r, numa_gpu_vec* z);
+
+/* gmres(apply, precond, b, x, rtol, restart, max_iters, zero_guess, save, r_init)
+ * (linalg/gmres.hpp:61-223).  precond may be NULL (IdentityPrecond).  save and r_init may be
+ * NULL.  orth selects MGS (reference) or CGS2; flexible = 1 selects FGMRES. */
+int numa_gpu_gmres(numa_gpu_ctx* ctx, numa_gpu_apply_fn apply, void* apply_user,
+                   numa_gpu_precond_fn precond, void* precond_user,
+                   const numa_gpu_vec* b, numa_gpu_vec* x, double rtol, size_t restart,
+                   size_t max_iters, int zero_guess, int orth, int flexible,
+                   numa_gpu_krylov_space* save, const numa_gpu_vec* r_init,
+                   numa_gmres_result* result);
+/* The same with the Bratu3D Jacobian at xpt as A (apply = f.jvp(xpt, .), mode = jvp mode) and a
+ * bound provider as M (provider may be NULL): the form the nonlinear drivers use internally. */
+int numa_gpu_gmres_bratu3d(numa_gpu_bratu3d* op, const numa_gpu_vec* xpt, int jvp_mode,
+                           numa_gpu_provider* provider, const numa_gpu_vec* b, numa_gpu_vec* x,
+                           double rtol, size_t restart, size_t max_iters, int zero_guess,
+                           int orth, int flexible, numa_gpu_krylov_space* save,
+                           const numa_gpu_vec* r_init, numa_gmres_result* result);
+/* gmres_recycled (linalg/gmres.hpp:229-323) with the Bratu3D Jacobian at xpt. */
+int numa_gpu_gmres_recycled_bratu3d(numa_gpu_bratu3d* op, const numa_gpu_vec* xpt, int jvp_mode,
+                                    numa_gpu_provider* provider, const numa_gpu_vec* b,
+                                    numa_gpu_vec* x, double rtol, size_t restart,
+                                    size_t max_iters, int orth,
+                                    const numa_gpu_krylov_space* space,
+                                    numa_gpu_krylov_space* save, numa_gmres_result* result);
+
+/* ---------------------------------------------------------------- nonlinear drivers */
+/* Eisenstat-Walker forcing term, detail::forcing (krylov_newton.hpp:54-65); host arithmetic. */
+double numa_gpu_forcing(const numa_krylov_params* p, size_t k, double rnorm, double rprev,
+                        double eta_prev, double res0);
+/* newton_krylov(f, x0, p, pc) (krylov_newton.hpp:69-114).  x holds x0 on entry and the final
+ * iterate on return (KrylovResult::x).  provider may be NULL (NoPrecond). */
+int numa_gpu_newton_krylov(numa_gpu_bratu3d* op, numa_gpu_vec* x, const numa_krylov_params* p,
+                           numa_gpu_provider* provider, numa_krylov_result* result);
+/* chebyshev_inexact(f, x0, p, pc) (krylov_newton.hpp:116-189); p->recycle selects recycling. */
+int numa_gpu_chebyshev_inexact(numa_gpu_bratu3d* op, numa_gpu_vec* x, const numa_krylov_params* p,
+                               numa_gpu_provider* provider, numa_krylov_result* result);
+/* tf_chebyshev_2018(f, x0, p, pc) (methods/tf_chebyshev_2018.hpp:52-132). */
+int numa_gpu_tf_chebyshev_2018(numa_gpu_bratu3d* op, numa_gpu_vec* x, const numa_krylov_params* p,
+                               numa_gpu_provider* provider, numa_krylov_result* result);
+
+/* One call from host buffers to host buffers: Bratu3D(n, lambda), provider of precond_kind
+ * (MG with pre = post = 2 and mg_precision), method of numa_gpu_method, x0[n^3] -> x_out[n^3].
+ * The shape of apps/smoke_bratu.cpp:125-148 and apps/run_campaign.cpp:344-390. */
+int numa_gpu_solve_bratu3d_host(numa_gpu_ctx* ctx, size_t n, double lambda, int method,
+                                int precond_kind, int mg_precision, const numa_krylov_params* p,
+                                const double* x0, double* x_out, numa_krylov_result* result);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* NUMA_GPU_H */

@@ -1,0 +1,1048 @@
+// numa_oracle.cpp — CPU restatement of the reference's matrix-free nonlinear-solve path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the oracle that the GPU library is checked against
+// (tests/, __graft_entry__.smoke()) and the CPU baseline that bench.py times.  Nothing in the
+// product library links, loads or calls it.
+//
+// It restates, in plain C++20 + OpenMP, the algorithms of kapumota/chebyshev-nonlinear-lab
+// (namespace numa::op), citing the reference file:line each function follows.  Parallelism
+// mirrors the reference exactly (OpenMP where the reference has it, serial where it is serial:
+// the multigrid V-cycle and most GMRES loops), so that its timings stand for the reference's.
+// It is pinned against the reference itself: tests/golden/ holds outputs of the reference's own
+// headers compiled here (oracle/build_ref.sh, oracle/ref_driver.cpp), and the reference's
+// published count table (docs/research/R1_OPERATOR_INTERFACE.md:113-121).
+//
+// Floating-point contraction is disabled at build time (-ffp-contract=off) so that the
+// element-wise arithmetic is the IEEE sequence written here.
+//
+// C API at the end (extern "C"), used from Python through ctypes.
+
+#include "../include/numa_gpu.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstddef>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <stdexcept>
+#include <utility>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace oracle {
+
+using DVec = std::vector<double>;
+using Clock = std::chrono::steady_clock;
+
+static double seconds_since(Clock::time_point t0) {
+    return std::chrono::duration<double>(Clock::now() - t0).count();
+}
+
+// ---------------------------------------------------------------- BLAS-1 (operator.hpp:19-41)
+static double dot(const DVec& a, const DVec& b) {
+    double s = 0.0;
+    const long n = static_cast<long>(a.size());
+#pragma omp parallel for reduction(+ : s) schedule(static) if (n > 4096)
+    for (long i = 0; i < n; ++i) s += a[i] * b[i];
+    return s;
+}
+
+static double norm2(const DVec& a) { return std::sqrt(dot(a, a)); }
+
+static void axpy(double a, const DVec& x, DVec& y) {
+    const long n = static_cast<long>(x.size());
+#pragma omp parallel for schedule(static) if (n > 4096)
+    for (long i = 0; i < n; ++i) y[i] += a * x[i];
+}
+
+// ---------------------------------------------------------------- Bratu3D (problems/bratu3d.hpp)
+struct Bratu {
+    std::size_t n;
+    double lambda;
+    double h2inv;  // (n+1)^2, bratu3d.hpp:15
+
+    Bratu(std::size_t n_, double lam) : n(n_), lambda(lam), h2inv((n_ + 1.0) * (n_ + 1.0)) {}
+    std::size_t size() const { return n * n * n; }
+
+    // out = h^-2 (6 v - sum of the six neighbours), Dirichlet zeros skipped (bratu3d.hpp:73-95).
+    void neg_laplacian(const DVec& v, DVec& out) const {
+        out.resize(v.size());
+        const long nl = static_cast<long>(n);
+        const std::size_t plane = n * n;
+#pragma omp parallel for collapse(2) schedule(static) if (nl > 16)
+        for (long i = 0; i < nl; ++i)
+            for (long j = 0; j < nl; ++j) {
+                const std::size_t row = (static_cast<std::size_t>(i) * n + j) * n;
+                for (std::size_t k = 0; k < n; ++k) {
+                    const std::size_t p = row + k;
+                    double acc = 6.0 * v[p];
+                    if (i > 0) acc -= v[p - plane];
+                    if (i + 1 < nl) acc -= v[p + plane];
+                    if (j > 0) acc -= v[p - n];
+                    if (j + 1 < nl) acc -= v[p + n];
+                    if (k > 0) acc -= v[p - 1];
+                    if (k + 1 < n) acc -= v[p + 1];
+                    out[p] = h2inv * acc;
+                }
+            }
+    }
+
+    // F(u) = -lap u - lambda e^u (bratu3d.hpp:21-31)
+    void eval(const DVec& u, DVec& out) const {
+        neg_laplacian(u, out);
+        const long cnt = static_cast<long>(out.size());
+#pragma omp parallel for schedule(static) if (cnt > 4096)
+        for (long p = 0; p < cnt; ++p) out[p] -= lambda * std::exp(u[p]);
+    }
+
+    // F'(u) v = -lap v - lambda e^u v (bratu3d.hpp:33-43)
+    void jvp(const DVec& u, const DVec& v, DVec& out) const {
+        neg_laplacian(v, out);
+        const long cnt = static_cast<long>(out.size());
+#pragma omp parallel for schedule(static) if (cnt > 4096)
+        for (long p = 0; p < cnt; ++p) out[p] -= lambda * std::exp(u[p]) * v[p];
+    }
+
+    // F''(u)[v,v] = -lambda e^u v^2 (bratu3d.hpp:46-56)
+    void d2(const DVec& u, const DVec& v, DVec& out) const {
+        out.resize(u.size());
+        const long cnt = static_cast<long>(out.size());
+#pragma omp parallel for schedule(static) if (cnt > 4096)
+        for (long p = 0; p < cnt; ++p) out[p] = -lambda * std::exp(u[p]) * v[p] * v[p];
+    }
+
+    // d = 6 h^-2 - lambda e^u (bratu3d.hpp:59-69)
+    void jacobi_diag(const DVec& u, DVec& d) const {
+        d.resize(u.size());
+        const long cnt = static_cast<long>(d.size());
+#pragma omp parallel for schedule(static) if (cnt > 4096)
+        for (long p = 0; p < cnt; ++p) d[p] = 6.0 * h2inv - lambda * std::exp(u[p]);
+    }
+};
+
+// Forward-difference J v with two F evaluations (operator.hpp:101-114).
+template <class Op>
+static void jvp_fd(const Op& f, const DVec& x, const DVec& v, DVec& out) {
+    const std::size_t N = x.size();
+    out.assign(N, 0.0);
+    const double nv = norm2(v);
+    if (nv == 0.0) return;
+    const double h = std::sqrt(std::numeric_limits<double>::epsilon()) * (1.0 + norm2(x)) / nv;
+    DVec xp = x, f0(N), f1(N);
+    axpy(h, v, xp);
+    f.eval(x, f0);
+    f.eval(xp, f1);
+    for (std::size_t p = 0; p < N; ++p) out[p] = (f1[p] - f0[p]) / h;
+}
+
+// Central second difference with three F evaluations, step eps^(1/4) (operator.hpp:118-134).
+template <class Op>
+static void d2_fd(const Op& f, const DVec& x, const DVec& v, DVec& out) {
+    const std::size_t N = x.size();
+    out.assign(N, 0.0);
+    const double nv = norm2(v);
+    if (nv == 0.0) return;
+    const double h = std::pow(std::numeric_limits<double>::epsilon(), 0.25) * (1.0 + norm2(x)) / nv;
+    DVec xp = x, xm = x, f0(N), fp(N), fm(N);
+    axpy(h, v, xp);
+    axpy(-h, v, xm);
+    f.eval(x, f0);
+    f.eval(xp, fp);
+    f.eval(xm, fm);
+    for (std::size_t p = 0; p < N; ++p) out[p] = (fp[p] - 2.0 * f0[p] + fm[p]) / (h * h);
+}
+
+// Operator wrapper: which derivative forms the drivers see, plus call timers (timing.hpp:37-75).
+struct Timers {
+    double t_F = 0, t_JVP = 0, t_D2 = 0, t_prec = 0, t_setup = 0;
+};
+
+struct BratuOp {
+    const Bratu& f;
+    int jvp_mode;  // 0 analytic, 1 FD
+    int d2_mode;
+    Timers* timers;
+
+    std::size_t size() const { return f.size(); }
+    void eval(const DVec& x, DVec& out) const {
+        auto t0 = Clock::now();
+        f.eval(x, out);
+        timers->t_F += seconds_since(t0);
+    }
+    void jvp(const DVec& x, const DVec& v, DVec& out) const {
+        auto t0 = Clock::now();
+        if (jvp_mode == 1) jvp_fd(f, x, v, out); else f.jvp(x, v, out);
+        timers->t_JVP += seconds_since(t0);
+    }
+    void d2(const DVec& x, const DVec& v, DVec& out) const {
+        auto t0 = Clock::now();
+        if (d2_mode == 1) d2_fd(f, x, v, out); else f.d2(x, v, out);
+        timers->t_D2 += seconds_since(t0);
+    }
+};
+
+// ---------------------------------------------------------------- PoissonMG (linalg/poisson_mg.hpp)
+class PoissonMG {
+public:
+    struct Level {
+        std::size_t n = 0;
+        double h2inv = 0.0;
+        DVec x, b, r;
+    };
+
+    // Levels while n is odd, halving (m-1)/2 and h2inv/4, down to n = 1 (poisson_mg.hpp:26-64).
+    PoissonMG(std::size_t n, int pre = 2, int post = 2) : pre_(pre), post_(post) {
+        if (n == 0) throw std::invalid_argument("PoissonMG: grid size must be positive");
+        if (pre < 0 || post < 0) throw std::invalid_argument("PoissonMG: negative sweep count");
+        const std::size_t maxs = std::numeric_limits<std::size_t>::max();
+        if (n > maxs / n || n * n > maxs / n) throw std::overflow_error("PoissonMG: n^3 overflows");
+        std::size_t m = n;
+        double h2 = (static_cast<double>(n) + 1.0) * (static_cast<double>(n) + 1.0);
+        for (;;) {
+            Level L;
+            L.n = m;
+            L.h2inv = h2;
+            L.x.assign(m * m * m, 0.0);
+            L.b.assign(m * m * m, 0.0);
+            L.r.assign(m * m * m, 0.0);
+            levels_.push_back(std::move(L));
+            if (m % 2 == 0 || m <= 1) break;
+            m = (m - 1) / 2;
+            h2 /= 4.0;
+        }
+    }
+
+    std::size_t levels() const { return levels_.size(); }
+
+    // z = V-cycle(r) (poisson_mg.hpp:69-80)
+    void apply(const DVec& r, DVec& z) const {
+        Level& top = levels_[0];
+        if (r.size() != top.x.size()) throw std::invalid_argument("PoissonMG: residual size mismatch");
+        top.b = r;
+        std::fill(top.x.begin(), top.x.end(), 0.0);
+        cycle(0);
+        z = top.x;
+    }
+    void operator()(const DVec& r, DVec& z) const { apply(r, z); }
+
+    // One red-black Gauss-Seidel sweep; order 0 = colour 0 then 1, order 1 reversed.
+    // Colour of (i,j,k) is (i+j+k)&1 (poisson_mg.hpp:99-126).
+    static void smooth(Level& L, int order) {
+        const std::size_t n = L.n, plane = n * n;
+        const double inv = 1.0 / L.h2inv;
+        for (int pass = 0; pass < 2; ++pass) {
+            const std::size_t colour = static_cast<std::size_t>(order == 0 ? pass : 1 - pass);
+            for (std::size_t i = 0; i < n; ++i)
+                for (std::size_t j = 0; j < n; ++j)
+                    for (std::size_t k = (i + j + colour) & 1; k < n; k += 2) {
+                        const std::size_t p = (i * n + j) * n + k;
+                        double acc = L.b[p] * inv;
+                        if (i > 0) acc += L.x[p - plane];
+                        if (i + 1 < n) acc += L.x[p + plane];
+                        if (j > 0) acc += L.x[p - n];
+                        if (j + 1 < n) acc += L.x[p + n];
+                        if (k > 0) acc += L.x[p - 1];
+                        if (k + 1 < n) acc += L.x[p + 1];
+                        L.x[p] = acc / 6.0;
+                    }
+        }
+    }
+
+    // r = b - h^-2 (6x - sum nbrs) (poisson_mg.hpp:128-149)
+    static void residual(Level& L) {
+        const std::size_t n = L.n, plane = n * n;
+        for (std::size_t i = 0; i < n; ++i)
+            for (std::size_t j = 0; j < n; ++j)
+                for (std::size_t k = 0; k < n; ++k) {
+                    const std::size_t p = (i * n + j) * n + k;
+                    double acc = 6.0 * L.x[p];
+                    if (i > 0) acc -= L.x[p - plane];
+                    if (i + 1 < n) acc -= L.x[p + plane];
+                    if (j > 0) acc -= L.x[p - n];
+                    if (j + 1 < n) acc -= L.x[p + n];
+                    if (k > 0) acc -= L.x[p - 1];
+                    if (k + 1 < n) acc -= L.x[p + 1];
+                    L.r[p] = L.b[p] - L.h2inv * acc;
+                }
+    }
+
+    // 27-point full weighting, coarse I <-> fine 2I+1, weights (1/4,1/2,1/4)^3; the sum runs
+    // a outer, b middle, c inner, each weight product formed as wa*wb*wc (poisson_mg.hpp:152-188).
+    static void restrict_to(const Level& F, Level& C) {
+        static const double w[3] = {0.25, 0.5, 0.25};
+        const std::size_t nf = F.n, nc = C.n;
+        for (std::size_t I = 0; I < nc; ++I)
+            for (std::size_t J = 0; J < nc; ++J)
+                for (std::size_t K = 0; K < nc; ++K) {
+                    double acc = 0.0;
+                    for (int a = 0; a < 3; ++a) {
+                        const std::size_t fi = 2 * I + a;
+                        if (fi >= nf) continue;
+                        for (int b = 0; b < 3; ++b) {
+                            const std::size_t fj = 2 * J + b;
+                            if (fj >= nf) continue;
+                            for (int c = 0; c < 3; ++c) {
+                                const std::size_t fk = 2 * K + c;
+                                if (fk >= nf) continue;
+                                acc += w[a] * w[b] * w[c] * F.r[(fi * nf + fj) * nf + fk];
+                            }
+                        }
+                    }
+                    C.b[(I * nc + J) * nc + K] = acc;
+                }
+    }
+
+    // 1D interpolation stencil of fine index f over a coarse grid of size nc
+    // (poisson_mg.hpp:191-220): odd f -> coarse (f-1)/2 with weight 1; even f -> coarse f/2-1
+    // and f/2 (those inside the grid) with weight 1/2 each.
+    static int interp_1d(std::size_t f, std::size_t nc, std::size_t idx[2], double wt[2]) {
+        if (f % 2 == 1) {
+            idx[0] = (f - 1) / 2;
+            wt[0] = 1.0;
+            return 1;
+        }
+        int cnt = 0;
+        const std::size_t right = f / 2;
+        if (right >= 1) { idx[cnt] = right - 1; wt[cnt] = 0.5; ++cnt; }
+        if (right < nc) { idx[cnt] = right; wt[cnt] = 0.5; ++cnt; }
+        return cnt;
+    }
+
+    // Trilinear interpolation added into the fine x (poisson_mg.hpp:222-260).
+    static void prolong_add(const Level& C, Level& F) {
+        const std::size_t nf = F.n, nc = C.n;
+        for (std::size_t i = 0; i < nf; ++i) {
+            std::size_t ci[2]; double wi[2];
+            const int ni = interp_1d(i, nc, ci, wi);
+            for (std::size_t j = 0; j < nf; ++j) {
+                std::size_t cj[2]; double wj[2];
+                const int nj = interp_1d(j, nc, cj, wj);
+                for (std::size_t k = 0; k < nf; ++k) {
+                    std::size_t ck[2]; double wk[2];
+                    const int nk = interp_1d(k, nc, ck, wk);
+                    double acc = 0.0;
+                    for (int a = 0; a < ni; ++a)
+                        for (int b = 0; b < nj; ++b)
+                            for (int c = 0; c < nk; ++c)
+                                acc += wi[a] * wj[b] * wk[c] * C.x[(ci[a] * nc + cj[b]) * nc + ck[c]];
+                    F.x[(i * nf + j) * nf + k] += acc;
+                }
+            }
+        }
+    }
+
+    // V(pre, post); coarsest n == 1 solved exactly, else 30 alternating sweeps
+    // (poisson_mg.hpp:262-294).
+    void cycle(std::size_t l) const {
+        Level& L = levels_[l];
+        if (l + 1 == levels_.size()) {
+            if (L.n == 1) {
+                L.x[0] = L.b[0] / (6.0 * L.h2inv);
+            } else {
+                for (int s = 0; s < 30; ++s) smooth(L, s % 2);
+            }
+            return;
+        }
+        for (int s = 0; s < pre_; ++s) smooth(L, 0);
+        residual(L);
+        Level& C = levels_[l + 1];
+        restrict_to(L, C);
+        std::fill(C.x.begin(), C.x.end(), 0.0);
+        cycle(l + 1);
+        prolong_add(C, L);
+        for (int s = 0; s < post_; ++s) smooth(L, 1);
+    }
+
+    mutable std::vector<Level> levels_;
+
+private:
+    int pre_, post_;
+};
+
+// ---------------------------------------------------------------- preconditioner providers
+// A bound preconditioner is "z = M^-1 r"; make(x) binds it at a nonlinear iterate
+// (krylov_newton.hpp:20-22, poisson_mg.hpp:303-320, bratu3d.hpp:104-120).
+struct Provider {
+    int kind = 0;  // numa_gpu_precond_kind
+    const Bratu* f = nullptr;
+    std::shared_ptr<PoissonMG> mg;
+    DVec diag;
+    Timers* timers = nullptr;
+
+    void make(const DVec& x) {
+        auto t0 = Clock::now();
+        if (kind == NUMA_GPU_PRECOND_JACOBI) f->jacobi_diag(x, diag);
+        if (timers) timers->t_setup += seconds_since(t0);
+    }
+    void operator()(const DVec& r, DVec& z) const {
+        auto t0 = Clock::now();
+        if (kind == NUMA_GPU_PRECOND_POISSON_MG) {
+            mg->apply(r, z);
+        } else if (kind == NUMA_GPU_PRECOND_JACOBI) {
+            z.resize(r.size());
+            for (std::size_t p = 0; p < r.size(); ++p) z[p] = r[p] / diag[p];
+        } else {
+            z = r;
+        }
+        if (timers) timers->t_prec += seconds_since(t0);
+    }
+};
+
+// ---------------------------------------------------------------- GMRES (linalg/gmres.hpp)
+struct GmresResult {
+    std::size_t iters = 0, matvecs = 0, precs = 0;
+    double rel_res = 0.0;
+    bool converged = false, breakdown = false;
+};
+
+struct KrylovSpace {
+    std::vector<DVec> V;
+    std::vector<std::vector<double>> Hbar;
+    std::size_t k = 0;
+    void clear() { V.clear(); Hbar.clear(); k = 0; }
+};
+
+// Restarted right-preconditioned GMRES(m), modified Gram-Schmidt Arnoldi, Givens rotations
+// (gmres.hpp:61-223).  The matvec counter includes restart residuals; each cycle ends with one
+// more preconditioner application to V y.
+template <class Apply, class Precond>
+static GmresResult gmres(const Apply& A, const Precond& M, const DVec& b, DVec& x, double rtol,
+                         std::size_t m, std::size_t max_iters, bool zero_guess = true,
+                         KrylovSpace* save = nullptr, const DVec* r_init = nullptr) {
+    const std::size_t N = b.size();
+    GmresResult res;
+    if (save) save->clear();
+    const double bnorm = norm2(b);
+    if (bnorm == 0.0) { x.assign(N, 0.0); res.converged = true; return res; }
+    if (m == 0) { res.rel_res = 1.0; res.breakdown = true; return res; }
+    if (max_iters == 0) { res.rel_res = 1.0; return res; }
+    if (r_init && r_init->size() != N) { res.rel_res = 1.0; res.breakdown = true; return res; }
+    if (zero_guess) x.assign(N, 0.0);
+
+    DVec r(N), w(N), z(N), comb(N);
+    std::vector<DVec> V(m + 1, DVec(N));
+    std::vector<std::vector<double>> H(m + 1, std::vector<double>(m, 0.0));
+    std::vector<std::vector<double>> Hraw(m + 1, std::vector<double>(m, 0.0));
+    std::vector<double> cs(m), sn(m), g(m + 1), y(m);
+
+    bool given = r_init != nullptr;
+    bool first = zero_guess;
+    std::size_t k_last = 0;
+
+    while (res.iters < max_iters) {
+        if (given) { r = *r_init; given = false; first = false; }
+        else if (first) { r = b; first = false; }
+        else {
+            A(x, w);
+            ++res.matvecs;
+            for (std::size_t p = 0; p < N; ++p) r[p] = b[p] - w[p];
+        }
+        const double beta = norm2(r);
+        res.rel_res = beta / bnorm;
+        if (res.rel_res <= rtol) { res.converged = true; k_last = 0; break; }
+
+        for (auto& row : Hraw) std::fill(row.begin(), row.end(), 0.0);
+        for (std::size_t p = 0; p < N; ++p) V[0][p] = r[p] / beta;
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+
+        std::size_t k = 0;
+        k_last = 0;
+        while (k < m && res.iters < max_iters) {
+            const std::size_t j = k;
+            M(V[j], z);
+            ++res.precs;
+            A(z, w);
+            ++res.matvecs;
+            for (std::size_t i = 0; i <= j; ++i) {
+                H[i][j] = dot(w, V[i]);
+                axpy(-H[i][j], V[i], w);
+            }
+            H[j + 1][j] = norm2(w);
+            if (H[j + 1][j] > 0.0) {
+                for (std::size_t p = 0; p < N; ++p) V[j + 1][p] = w[p] / H[j + 1][j];
+            } else {
+                std::fill(V[j + 1].begin(), V[j + 1].end(), 0.0);
+            }
+            for (std::size_t i = 0; i <= j + 1; ++i) Hraw[i][j] = H[i][j];
+            for (std::size_t i = 0; i < j; ++i) {
+                const double t = cs[i] * H[i][j] + sn[i] * H[i + 1][j];
+                H[i + 1][j] = -sn[i] * H[i][j] + cs[i] * H[i + 1][j];
+                H[i][j] = t;
+            }
+            const double den = std::hypot(H[j][j], H[j + 1][j]);
+            if (!(den > 0.0) || !std::isfinite(den)) { res.breakdown = true; return res; }
+            cs[j] = H[j][j] / den;
+            sn[j] = H[j + 1][j] / den;
+            H[j][j] = den;
+            H[j + 1][j] = 0.0;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            ++k;
+            ++res.iters;
+            k_last = k;
+            res.rel_res = std::abs(g[j + 1]) / bnorm;
+            if (res.rel_res <= rtol) break;
+        }
+        for (std::size_t ii = k; ii-- > 0;) {
+            const double piv = H[ii][ii];
+            if (!(std::abs(piv) > 0.0) || !std::isfinite(piv)) { res.breakdown = true; return res; }
+            double s = g[ii];
+            for (std::size_t jj = ii + 1; jj < k; ++jj) s -= H[ii][jj] * y[jj];
+            y[ii] = s / piv;
+        }
+        std::fill(comb.begin(), comb.end(), 0.0);
+        for (std::size_t i = 0; i < k; ++i) axpy(y[i], V[i], comb);
+        M(comb, z);
+        ++res.precs;
+        axpy(1.0, z, x);
+        if (res.rel_res <= rtol) { res.converged = true; break; }
+    }
+    if (save && k_last > 0) {
+        save->k = k_last;
+        save->V = V;
+        save->Hbar.assign(k_last + 1, std::vector<double>(k_last, 0.0));
+        for (std::size_t i = 0; i <= k_last; ++i)
+            for (std::size_t j = 0; j < k_last; ++j) save->Hbar[i][j] = Hraw[i][j];
+    }
+    return res;
+}
+
+static bool space_usable(const KrylovSpace& s, std::size_t N) {
+    if (s.k == 0 || s.V.size() < s.k + 1 || s.Hbar.size() < s.k + 1) return false;
+    for (std::size_t i = 0; i <= s.k; ++i)
+        if (s.Hbar[i].size() < s.k) return false;
+    for (std::size_t i = 0; i <= s.k; ++i)
+        if (s.V[i].size() != N) return false;
+    return true;
+}
+
+// Second solve with the same A and M: least-squares projection of b on the saved space
+// (k+1 dots, QR of Hbar by Givens), initial guess M^-1 V y, residual b - V Hbar y, then GMRES
+// from that residual; falls back to a fresh GMRES if the space is unusable or singular
+// (gmres.hpp:229-323).
+template <class Apply, class Precond>
+static GmresResult gmres_recycled(const Apply& A, const Precond& M, const DVec& b, DVec& x,
+                                  double rtol, std::size_t m, std::size_t max_iters,
+                                  const KrylovSpace& sp, KrylovSpace* save = nullptr) {
+    const std::size_t k = sp.k, N = b.size();
+    x.assign(N, 0.0);
+    if (!space_usable(sp, N)) return gmres(A, M, b, x, rtol, m, max_iters, true, save);
+    std::vector<double> rhs(k + 1, 0.0);
+    for (std::size_t i = 0; i <= k; ++i) rhs[i] = dot(sp.V[i], b);
+    auto R = sp.Hbar;
+    std::vector<double> cs(k, 0.0), sn(k, 0.0);
+    for (std::size_t j = 0; j < k; ++j) {
+        for (std::size_t i = 0; i < j; ++i) {
+            const double t = cs[i] * R[i][j] + sn[i] * R[i + 1][j];
+            R[i + 1][j] = -sn[i] * R[i][j] + cs[i] * R[i + 1][j];
+            R[i][j] = t;
+        }
+        const double den = std::hypot(R[j][j], R[j + 1][j]);
+        if (!(den > 0.0) || !std::isfinite(den)) return gmres(A, M, b, x, rtol, m, max_iters, true, save);
+        cs[j] = R[j][j] / den;
+        sn[j] = R[j + 1][j] / den;
+        R[j][j] = den;
+        R[j + 1][j] = 0.0;
+        const double t = cs[j] * rhs[j] + sn[j] * rhs[j + 1];
+        rhs[j + 1] = -sn[j] * rhs[j] + cs[j] * rhs[j + 1];
+        rhs[j] = t;
+    }
+    std::vector<double> y(k, 0.0);
+    for (std::size_t ii = k; ii-- > 0;) {
+        const double piv = R[ii][ii];
+        if (!(std::abs(piv) > 0.0) || !std::isfinite(piv)) {
+            x.assign(N, 0.0);
+            return gmres(A, M, b, x, rtol, m, max_iters, true, save);
+        }
+        double s = rhs[ii];
+        for (std::size_t jj = ii + 1; jj < k; ++jj) s -= R[ii][jj] * y[jj];
+        y[ii] = s / piv;
+    }
+    DVec resid = b, comb(N, 0.0), x0(N, 0.0);
+    for (std::size_t i = 0; i <= k; ++i) {
+        double c = 0.0;
+        for (std::size_t j = 0; j < k; ++j) c += sp.Hbar[i][j] * y[j];
+        axpy(-c, sp.V[i], resid);
+    }
+    for (std::size_t j = 0; j < k; ++j) axpy(y[j], sp.V[j], comb);
+    M(comb, x0);
+    x = std::move(x0);
+    GmresResult out = gmres(A, M, b, x, rtol, m, max_iters, false, save, &resid);
+    ++out.precs;
+    return out;
+}
+
+// ---------------------------------------------------------------- nonlinear drivers (methods/)
+struct Params {
+    double rtol_nl = 1e-8;
+    std::size_t max_nl = 50;
+    double eta_init = 0.5, eta_max = 0.9, gamma = 0.9, alpha = 2.0;
+    double eta2_factor = 10.0, eta2_max = 0.5;
+    std::size_t restart = 50, max_iters = 500;
+    double armijo = 1e-4, min_lambda = 1e-4;
+    bool recycle = false;
+};
+
+struct Result {
+    DVec x;
+    bool converged = false;
+    std::size_t iters = 0, n_F = 0, n_JVP = 0, n_D2 = 0, n_lin_iters = 0, n_lin_failures = 0, n_prec = 0;
+    double res0 = 0.0, res = 0.0;
+};
+
+// Eisenstat-Walker choice 2 with Kelley's safeguard and the oversolve floor
+// 0.5 rtol_nl res0 / rnorm (krylov_newton.hpp:54-65).
+static double forcing(const Params& p, std::size_t k, double rnorm, double rprev, double eta_prev,
+                      double res0) {
+    if (k == 0) return p.eta_init;
+    double eta = p.gamma * std::pow(rnorm / rprev, p.alpha);
+    const double safe = p.gamma * std::pow(eta_prev, p.alpha);
+    if (safe > 0.1) eta = std::max(eta, safe);
+    eta = std::min(eta, p.eta_max);
+    eta = std::max(eta, 0.5 * p.rtol_nl * res0 / rnorm);
+    return std::min(eta, p.eta_max);
+}
+
+// Inexact Newton with Armijo backtracking; J z = F, step x - lambda z (krylov_newton.hpp:69-114).
+template <class Op>
+static Result newton_krylov(const Op& f, DVec x, const Params& p, Provider& pc) {
+    const std::size_t N = f.size();
+    Result out;
+    DVec Fx(N), Fn(N), z(N), xn(N);
+    f.eval(x, Fx); ++out.n_F;
+    double rnorm = norm2(Fx);
+    out.res0 = rnorm;
+    double rprev = rnorm, eta_prev = p.eta_init;
+    for (std::size_t k = 0; k < p.max_nl; ++k) {
+        if (rnorm <= p.rtol_nl * out.res0) { out.converged = true; break; }
+        const double eta = forcing(p, k, rnorm, rprev, eta_prev, out.res0);
+        pc.make(x);
+        auto A = [&](const DVec& v, DVec& o) { f.jvp(x, v, o); };
+        z.assign(N, 0.0);
+        const GmresResult g = gmres(A, pc, Fx, z, eta, p.restart, p.max_iters);
+        out.n_JVP += g.matvecs;
+        out.n_lin_iters += g.iters;
+        out.n_prec += g.precs;
+        if (!g.converged) ++out.n_lin_failures;
+        if (g.breakdown) break;
+        double lam = 1.0;
+        bool ok = false;
+        while (lam >= p.min_lambda) {
+            for (std::size_t q = 0; q < N; ++q) xn[q] = x[q] - lam * z[q];
+            f.eval(xn, Fn); ++out.n_F;
+            if (norm2(Fn) <= (1.0 - p.armijo * lam) * rnorm) { ok = true; break; }
+            lam *= 0.5;
+        }
+        if (!ok) break;
+        x = xn; Fx = Fn;
+        rprev = rnorm; rnorm = norm2(Fx); eta_prev = eta;
+        ++out.iters;
+    }
+    if (rnorm <= p.rtol_nl * out.res0) out.converged = true;
+    out.x = std::move(x);
+    out.res = rnorm;
+    return out;
+}
+
+// Inexact Chebyshev: J z = F, J u = F''(x)[z,z], trial x - z - u/2, Newton backtracking
+// fallback (krylov_newton.hpp:116-189).
+template <class Op>
+static Result chebyshev_inexact(const Op& f, DVec x, const Params& p, Provider& pc) {
+    const std::size_t N = f.size();
+    Result out;
+    DVec Fx(N), Fn(N), z(N), u(N), w(N), xn(N);
+    f.eval(x, Fx); ++out.n_F;
+    double rnorm = norm2(Fx);
+    out.res0 = rnorm;
+    double rprev = rnorm, eta_prev = p.eta_init;
+    for (std::size_t k = 0; k < p.max_nl; ++k) {
+        if (rnorm <= p.rtol_nl * out.res0) { out.converged = true; break; }
+        const double eta1 = forcing(p, k, rnorm, rprev, eta_prev, out.res0);
+        const double eta2 = std::min(p.eta2_max, p.eta2_factor * eta1);
+        pc.make(x);
+        auto A = [&](const DVec& v, DVec& o) { f.jvp(x, v, o); };
+        z.assign(N, 0.0);
+        KrylovSpace space;
+        const GmresResult g1 = gmres(A, pc, Fx, z, eta1, p.restart, p.max_iters, true,
+                                     p.recycle ? &space : nullptr);
+        out.n_JVP += g1.matvecs;
+        out.n_lin_iters += g1.iters;
+        out.n_prec += g1.precs;
+        if (!g1.converged) ++out.n_lin_failures;
+        if (g1.breakdown) break;
+        f.d2(x, z, w); ++out.n_D2;
+        u.assign(N, 0.0);
+        const GmresResult g2 = p.recycle
+            ? gmres_recycled(A, pc, w, u, eta2, p.restart, p.max_iters, space)
+            : gmres(A, pc, w, u, eta2, p.restart, p.max_iters);
+        out.n_JVP += g2.matvecs;
+        out.n_lin_iters += g2.iters;
+        out.n_prec += g2.precs;
+        if (!g2.converged) ++out.n_lin_failures;
+        bool ok = false;
+        if (!g2.breakdown) {
+            for (std::size_t q = 0; q < N; ++q) xn[q] = x[q] - z[q] - 0.5 * u[q];
+            f.eval(xn, Fn); ++out.n_F;
+            if (norm2(Fn) < rnorm) ok = true;
+        }
+        if (!ok) {
+            double lam = 1.0;
+            while (lam >= p.min_lambda) {
+                for (std::size_t q = 0; q < N; ++q) xn[q] = x[q] - lam * z[q];
+                f.eval(xn, Fn); ++out.n_F;
+                if (norm2(Fn) <= (1.0 - p.armijo * lam) * rnorm) { ok = true; break; }
+                lam *= 0.5;
+            }
+        }
+        if (!ok) break;
+        x = xn; Fx = Fn;
+        rprev = rnorm; rnorm = norm2(Fx); eta_prev = eta1;
+        ++out.iters;
+    }
+    if (rnorm <= p.rtol_nl * out.res0) out.converged = true;
+    out.x = std::move(x);
+    out.res = rnorm;
+    return out;
+}
+
+// Tensor-free Chebyshev (Eustaquio-Ribeiro-Dumett 2018, alpha = 0): curvature from two JVPs at
+// x and x + h d1, h = clamp(sqrt(eps) ||x|| / ||d1||, 2 eps, 0.5) (tf_chebyshev_2018.hpp:23-132).
+static double tf2018_step(const DVec& x, const DVec& d1) {
+    const double eps = std::numeric_limits<double>::epsilon();
+    const double nd = norm2(d1);
+    if (!(nd > 0.0)) return 2.0 * eps;
+    const double raw = std::sqrt(eps) * norm2(x) / nd;
+    return std::clamp(raw, 2.0 * eps, 0.5);
+}
+
+template <class Op>
+static Result tf_chebyshev_2018(const Op& f, DVec x, const Params& p, Provider& pc) {
+    const std::size_t N = f.size();
+    Result out;
+    DVec Fx(N), Fn(N), z(N), d1(N), d2v(N), curv(N), rhs2(N), j0(N), j1(N);
+    f.eval(x, Fx); ++out.n_F;
+    double rnorm = norm2(Fx);
+    out.res0 = rnorm;
+    const double eps = std::numeric_limits<double>::epsilon();
+    for (std::size_t k = 0; k < p.max_nl; ++k) {
+        if (rnorm <= p.rtol_nl * out.res0) { out.converged = true; break; }
+        const double eta1 = std::clamp(std::min(1e-8, rnorm * rnorm), 2.0 * eps, 1e-8);
+        const double eta2 = std::clamp(std::min(1e-8, rnorm), 2.0 * eps, 1e-8);
+        pc.make(x);
+        auto A = [&](const DVec& v, DVec& o) { f.jvp(x, v, o); };
+        z.assign(N, 0.0);
+        const GmresResult g1 = gmres(A, pc, Fx, z, eta1, p.restart, p.max_iters);
+        out.n_JVP += g1.matvecs;
+        out.n_lin_iters += g1.iters;
+        out.n_prec += g1.precs;
+        if (!g1.converged) { ++out.n_lin_failures; break; }
+        if (g1.breakdown) break;
+        d1 = z;
+        for (double& e : d1) e = -e;
+        const double h = tf2018_step(x, d1);
+        DVec xh = x;
+        axpy(h, d1, xh);
+        f.jvp(x, d1, j0);
+        f.jvp(xh, d1, j1);
+        curv.resize(N);
+        for (std::size_t q = 0; q < N; ++q) curv[q] = (j1[q] - j0[q]) / h;
+        out.n_JVP += 2;
+        for (std::size_t q = 0; q < N; ++q) rhs2[q] = -0.5 * curv[q];
+        d2v.assign(N, 0.0);
+        const GmresResult g2 = gmres(A, pc, rhs2, d2v, eta2, p.restart, p.max_iters);
+        out.n_JVP += g2.matvecs;
+        out.n_lin_iters += g2.iters;
+        out.n_prec += g2.precs;
+        if (!g2.converged) { ++out.n_lin_failures; break; }
+        if (g2.breakdown) break;
+        axpy(1.0, d1, x);
+        axpy(1.0, d2v, x);
+        f.eval(x, Fn); ++out.n_F;
+        Fx = Fn;
+        rnorm = norm2(Fx);
+        ++out.iters;
+        if (!std::isfinite(rnorm)) break;
+    }
+    if (rnorm <= p.rtol_nl * out.res0) out.converged = true;
+    out.x = std::move(x);
+    out.res = rnorm;
+    return out;
+}
+
+static Params to_params(const numa_krylov_params* cp) {
+    Params p;
+    if (!cp) return p;
+    p.rtol_nl = cp->rtol_nl;
+    p.max_nl = cp->max_nl;
+    p.eta_init = cp->eta_init;
+    p.eta_max = cp->eta_max;
+    p.gamma = cp->gamma;
+    p.alpha = cp->alpha;
+    p.eta2_factor = cp->eta2_factor;
+    p.eta2_max = cp->eta2_max;
+    p.restart = cp->gmres_restart;
+    p.max_iters = cp->gmres_max_iters;
+    p.armijo = cp->armijo;
+    p.min_lambda = cp->min_lambda;
+    p.recycle = cp->recycle != 0;
+    return p;
+}
+
+}  // namespace oracle
+
+// ============================================================================ C API (ctypes)
+using namespace oracle;
+
+extern "C" {
+
+int oracle_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void oracle_set_threads(int t) {
+#ifdef _OPENMP
+    if (t > 0) omp_set_num_threads(t);
+#else
+    (void)t;
+#endif
+}
+
+double oracle_dot(size_t N, const double* a, const double* b) {
+    DVec A(a, a + N), B(b, b + N);
+    return dot(A, B);
+}
+
+void oracle_bratu3d_eval(size_t n, double lambda, const double* u, double* out) {
+    Bratu f(n, lambda);
+    DVec U(u, u + f.size()), O;
+    f.eval(U, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+}
+
+void oracle_bratu3d_jvp(size_t n, double lambda, const double* u, const double* v, double* out, int mode) {
+    Bratu f(n, lambda);
+    DVec U(u, u + f.size()), V(v, v + f.size()), O;
+    if (mode == 1) jvp_fd(f, U, V, O); else f.jvp(U, V, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+}
+
+void oracle_bratu3d_d2(size_t n, double lambda, const double* u, const double* v, double* out, int mode) {
+    Bratu f(n, lambda);
+    DVec U(u, u + f.size()), V(v, v + f.size()), O;
+    if (mode == 1) d2_fd(f, U, V, O); else f.d2(U, V, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+}
+
+void oracle_bratu3d_jacobi_diag(size_t n, double lambda, const double* u, double* d) {
+    Bratu f(n, lambda);
+    DVec U(u, u + f.size()), D;
+    f.jacobi_diag(U, D);
+    std::memcpy(d, D.data(), D.size() * sizeof(double));
+}
+
+// Returns the level count, or -1 / -2 for the reference's invalid_argument / overflow_error.
+int oracle_mg_levels(size_t n, int pre, int post) {
+    try {
+        PoissonMG mg(n, pre, post);
+        return static_cast<int>(mg.levels());
+    } catch (const std::overflow_error&) {
+        return -2;
+    } catch (const std::invalid_argument&) {
+        return -1;
+    }
+}
+
+int oracle_mg_apply(size_t n, int pre, int post, const double* r, double* z) {
+    try {
+        PoissonMG mg(n, pre, post);
+        DVec R(r, r + n * n * n), Z;
+        mg.apply(R, Z);
+        std::memcpy(z, Z.data(), Z.size() * sizeof(double));
+        return 0;
+    } catch (...) {
+        return -1;
+    }
+}
+
+// Single V-cycle stages on one level (for kernel-level parity).
+void oracle_mg_smooth(size_t n, double h2inv, double* x, const double* b, int order) {
+    PoissonMG::Level L;
+    L.n = n; L.h2inv = h2inv;
+    L.x.assign(x, x + n * n * n);
+    L.b.assign(b, b + n * n * n);
+    PoissonMG::smooth(L, order);
+    std::memcpy(x, L.x.data(), L.x.size() * sizeof(double));
+}
+
+void oracle_mg_residual(size_t n, double h2inv, const double* x, const double* b, double* r) {
+    PoissonMG::Level L;
+    L.n = n; L.h2inv = h2inv;
+    L.x.assign(x, x + n * n * n);
+    L.b.assign(b, b + n * n * n);
+    L.r.assign(n * n * n, 0.0);
+    PoissonMG::residual(L);
+    std::memcpy(r, L.r.data(), L.r.size() * sizeof(double));
+}
+
+void oracle_mg_restrict(size_t nf, const double* rf, double* bc) {
+    PoissonMG::Level F, C;
+    F.n = nf; F.r.assign(rf, rf + nf * nf * nf);
+    C.n = (nf - 1) / 2; C.b.assign(C.n * C.n * C.n, 0.0);
+    PoissonMG::restrict_to(F, C);
+    std::memcpy(bc, C.b.data(), C.b.size() * sizeof(double));
+}
+
+void oracle_mg_prolong_add(size_t nc, const double* xc, double* xf) {
+    PoissonMG::Level F, C;
+    C.n = nc; C.x.assign(xc, xc + nc * nc * nc);
+    F.n = 2 * nc + 1; F.x.assign(xf, xf + F.n * F.n * F.n);
+    PoissonMG::prolong_add(C, F);
+    std::memcpy(xf, F.x.data(), F.x.size() * sizeof(double));
+}
+
+static void fill_gmres_result(const GmresResult& g, numa_gmres_result* out) {
+    if (!out) return;
+    out->iters = g.iters;
+    out->matvecs = g.matvecs;
+    out->precs = g.precs;
+    out->rel_res = g.rel_res;
+    out->converged = g.converged ? 1 : 0;
+    out->breakdown = g.breakdown ? 1 : 0;
+}
+
+static Provider make_provider(int kind, const Bratu& f, std::size_t n, Timers* t) {
+    Provider pc;
+    pc.kind = kind;
+    pc.f = &f;
+    pc.timers = t;
+    if (kind == NUMA_GPU_PRECOND_POISSON_MG) pc.mg = std::make_shared<PoissonMG>(n);
+    return pc;
+}
+
+// GMRES on the Bratu3D Jacobian at xpt (analytic or FD matvec) with a provider bound at xpt.
+int oracle_gmres_bratu3d(size_t n, double lambda, const double* xpt, int jvp_mode, int precond_kind,
+                         const double* b, double* x, double rtol, size_t restart, size_t max_iters,
+                         int zero_guess, numa_gmres_result* out) {
+    Bratu f(n, lambda);
+    Timers t;
+    BratuOp op{f, jvp_mode, 0, &t};
+    const std::size_t N = f.size();
+    DVec X(xpt, xpt + N), B(b, b + N), S(x, x + N);
+    Provider pc = make_provider(precond_kind, f, n, &t);
+    pc.make(X);
+    auto A = [&](const DVec& v, DVec& o) { op.jvp(X, v, o); };
+    GmresResult g = gmres(A, pc, B, S, rtol, restart, max_iters, zero_guess != 0);
+    std::memcpy(x, S.data(), N * sizeof(double));
+    fill_gmres_result(g, out);
+    return 0;
+}
+
+// gmres with save, then gmres_recycled on a second right-hand side (the reference test
+// tests/test_operators.cpp:235-275): writes both solutions and both results.
+int oracle_gmres_recycle_pair(size_t n, double lambda, const double* xpt, int precond_kind,
+                              const double* b1, const double* b2, double rtol, size_t restart,
+                              size_t max_iters, double* z1, double* u2, size_t* k_saved,
+                              numa_gmres_result* r1, numa_gmres_result* r2) {
+    Bratu f(n, lambda);
+    Timers t;
+    const std::size_t N = f.size();
+    DVec X(xpt, xpt + N), B1(b1, b1 + N), B2(b2, b2 + N), Z(N, 0.0), U;
+    Provider pc = make_provider(precond_kind, f, n, &t);
+    pc.make(X);
+    auto A = [&](const DVec& v, DVec& o) { f.jvp(X, v, o); };
+    KrylovSpace sp;
+    GmresResult g1 = gmres(A, pc, B1, Z, rtol, restart, max_iters, true, &sp);
+    GmresResult g2 = gmres_recycled(A, pc, B2, U, rtol, restart, max_iters, sp);
+    std::memcpy(z1, Z.data(), N * sizeof(double));
+    std::memcpy(u2, U.data(), N * sizeof(double));
+    if (k_saved) *k_saved = sp.k;
+    fill_gmres_result(g1, r1);
+    fill_gmres_result(g2, r2);
+    return 0;
+}
+
+// GMRES on the plain -Laplacian with the V-cycle (tests/test_operators.cpp:207-233).
+int oracle_gmres_poisson_mg(size_t n, const double* b, double* x, double rtol, size_t restart,
+                            size_t max_iters, numa_gmres_result* out) {
+    Bratu lap(n, 0.0);
+    PoissonMG mg(n);
+    const std::size_t N = n * n * n;
+    DVec B(b, b + N), S(N, 0.0);
+    auto A = [&](const DVec& v, DVec& o) { lap.neg_laplacian(v, o); };
+    auto M = [&](const DVec& r, DVec& z) { mg.apply(r, z); };
+    GmresResult g = gmres(A, M, B, S, rtol, restart, max_iters);
+    std::memcpy(x, S.data(), N * sizeof(double));
+    fill_gmres_result(g, out);
+    return 0;
+}
+
+// Full nonlinear solve of Bratu3D(n, lambda) from x0 with method / provider kind.
+int oracle_solve_bratu3d(size_t n, double lambda, int method, int precond_kind,
+                         const numa_krylov_params* cp, const double* x0, double* x_out,
+                         numa_krylov_result* res) {
+    try {
+        auto t_start = Clock::now();
+        Bratu f(n, lambda);
+        Timers t;
+        const int jm = cp ? cp->jvp_mode : 0;
+        const int dm = cp ? cp->d2_mode : 0;
+        BratuOp op{f, jm, dm, &t};
+        Params p = to_params(cp);
+        if (method == NUMA_GPU_METHOD_CHEB_REC) p.recycle = true;
+        auto t_setup = Clock::now();
+        Provider pc = make_provider(precond_kind, f, n, &t);
+        const double setup_static = seconds_since(t_setup);
+        DVec X0(x0, x0 + f.size());
+        Result r;
+        switch (method) {
+            case NUMA_GPU_METHOD_NK: r = newton_krylov(op, X0, p, pc); break;
+            case NUMA_GPU_METHOD_CHEB:
+            case NUMA_GPU_METHOD_CHEB_REC: r = chebyshev_inexact(op, X0, p, pc); break;
+            case NUMA_GPU_METHOD_TF2018: r = tf_chebyshev_2018(op, X0, p, pc); break;
+            default: return NUMA_GPU_ERR_INVALID_ARGUMENT;
+        }
+        if (x_out) std::memcpy(x_out, r.x.data(), r.x.size() * sizeof(double));
+        if (res) {
+            std::memset(res, 0, sizeof(*res));
+            res->converged = r.converged ? 1 : 0;
+            res->iters = r.iters;
+            res->n_F = r.n_F;
+            res->n_JVP = r.n_JVP;
+            res->n_D2 = r.n_D2;
+            res->n_lin_iters = r.n_lin_iters;
+            res->n_lin_failures = r.n_lin_failures;
+            res->n_prec = r.n_prec;
+            res->res0 = r.res0;
+            res->res = r.res;
+            res->t_F = t.t_F;
+            res->t_JVP = t.t_JVP;
+            res->t_D2 = t.t_D2;
+            res->t_prec = t.t_prec;
+            res->t_setup_dynamic = t.t_setup + setup_static;
+            res->t_total = seconds_since(t_start);
+        }
+        return 0;
+    } catch (const std::overflow_error&) {
+        return NUMA_GPU_ERR_OVERFLOW;
+    } catch (const std::invalid_argument&) {
+        return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    }
+}
+
+double oracle_forcing(const numa_krylov_params* cp, size_t k, double rnorm, double rprev,
+                      double eta_prev, double res0) {
+    return forcing(to_params(cp), k, rnorm, rprev, eta_prev, res0);
+}
+
+}  // extern "C"
