@@ -243,6 +243,13 @@ Bratu3D::Bratu3D(Context& ctx, size_t n, double lambda)
     if (n > 65535 * 8) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "grid too large");
 }
 
+Bratu3D::~Bratu3D() = default;
+
+SolverWorkspace& Bratu3D::workspace() {
+    if (!ws_) ws_ = std::make_unique<SolverWorkspace>(ctx_, N_);
+    return *ws_;
+}
+
 void Bratu3D::eval(const double* x, double* out, double* c_out, double* norm_out) {
     const int n = (int)n_;
     const bool norm = norm_out != nullptr;

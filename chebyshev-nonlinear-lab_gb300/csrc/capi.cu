@@ -819,4 +819,15 @@ int numa_gpu_solve_bratu3d_host(numa_gpu_ctx* ctx, size_t n, double lambda, int 
     return rc;
 }
 
+// ------------------------------------------------------------------------------ diagnostics
+int numa_gpu_diag_fp64_peak(numa_gpu_ctx* ctx, double* tflops) {
+    if (!ctx || !tflops) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(ctx, [&] { *tflops = diag_fp64_peak_tflops(*ctx->impl); });
+}
+
+int numa_gpu_diag_time_smoother(numa_gpu_mg* mg, int reps, double* ms_per_pass) {
+    if (!mg || !ms_per_pass || reps < 1) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(mg->ctx, [&] { *ms_per_pass = mg->impl->time_finest_pass(reps); });
+}
+
 }  // extern "C"

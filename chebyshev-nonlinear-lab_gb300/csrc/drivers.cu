@@ -210,15 +210,17 @@ struct SolveState {
     const KrylovParams& p;
     size_t N;
     double* user_x;
-    DeviceArray<double> xa, xb, Fa, Fb, ca, cb, z, u, w, scratch;
-    DeviceArray<float> c32;
+    SolverWorkspace& W;
+    DeviceArray<double>&xb, &Fa, &Fb, &ca, &cb, &z, &u, &w, &scratch, &xnorm;
+    DeviceArray<float>& c32;
+    Gmres& gmres;
     double *x, *xn, *Fx, *Fn, *cx, *cn;
     Timers timers;
-    Gmres gmres;
-    DeviceArray<double> xnorm;  // ||x|| for finite differences
 
     SolveState(Bratu3D& f_, const KrylovParams& p_, double* x0)
-        : f(f_), ctx(f_.ctx()), p(p_), N(f_.size()), user_x(x0), timers(f_.ctx()), gmres(f_.ctx(), f_.size()) {
+        : f(f_), ctx(f_.ctx()), p(p_), N(f_.size()), user_x(x0), W(f_.workspace()), xb(W.xb), Fa(W.Fa), Fb(W.Fb),
+          ca(W.ca), cb(W.cb), z(W.z), u(W.u), w(W.w), scratch(W.scratch), xnorm(W.xnorm), c32(W.c32),
+          gmres(W.gmres), timers(f_.ctx()) {
         xb.resize(N);
         Fa.resize(N);
         Fb.resize(N);
@@ -401,7 +403,7 @@ void chebyshev_inexact(Bratu3D& f, double* x0, const KrylovParams& p, Provider* 
     const size_t N = S.N;
     S.u.resize(N);
     S.w.resize(N);
-    KrylovSpace space;
+    KrylovSpace& space = S.W.space;
     {
         Timers::Scope s(&S.timers, kT_F);
         f.eval(S.x, S.Fx, S.cx, S.ctx.scalar(kSlotNormF));

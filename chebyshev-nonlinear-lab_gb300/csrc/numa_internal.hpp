@@ -30,9 +30,15 @@ void dev_cheb_step(Context& ctx, const double* x, const double* z, const double*
 void dev_scale_inplace(Context& ctx, double* y, double a, size_t N);
 
 // ------------------------------------------------------------------------------ Bratu3D
+struct SolverWorkspace;
+
 class Bratu3D {
 public:
     Bratu3D(Context& ctx, size_t n, double lambda);
+    ~Bratu3D();
+    // Device work arrays of the nonlinear drivers for this operator, kept between solves so
+    // that a solve allocates nothing after the first (created on first use).
+    SolverWorkspace& workspace();
     size_t size() const { return N_; }
     size_t grid() const { return n_; }
     double lambda() const { return lambda_; }
@@ -66,6 +72,7 @@ private:
     size_t n_, N_;
     double lambda_, h2inv_;
     DeviceArray<double> s1_, s2_, s3_;  // FD scratch
+    std::unique_ptr<SolverWorkspace> ws_;
 };
 
 // ------------------------------------------------------------------------------ PoissonMG
@@ -78,6 +85,9 @@ public:
     int precision() const { return precision_; }
     // z = V-cycle(r); r and z are FP64 device vectors of size n^3 (poisson_mg.hpp:69-80).
     void apply(const double* r, double* z);
+    // Diagnostic: average time (ms) of one red-black colour pass on the finest level, timed with
+    // CUDA events over `reps` back-to-back passes on the context stream.
+    double time_finest_pass(int reps);
 
     struct Level;
 
@@ -168,6 +178,15 @@ private:
     PinnedBuf pin_;
 };
 
+// Persistent arrays of a nonlinear solve (see Bratu3D::workspace).
+struct SolverWorkspace {
+    explicit SolverWorkspace(Context& ctx, size_t N) : gmres(ctx, N) {}
+    DeviceArray<double> xb, Fa, Fb, ca, cb, z, u, w, scratch, xnorm;
+    DeviceArray<float> c32;
+    Gmres gmres;
+    KrylovSpace space;
+};
+
 // ------------------------------------------------------------------------------ drivers
 struct KrylovParams {
     double rtol_nl = 1e-8;
@@ -182,6 +201,7 @@ struct KrylovParams {
 };
 
 KrylovParams params_from_c(const numa_krylov_params* p);
+double diag_fp64_peak_tflops(Context& ctx);
 double forcing(const KrylovParams& p, size_t k, double rnorm, double rprev, double eta_prev, double res0);
 
 // x holds x0 on entry and the final iterate on return.

@@ -373,4 +373,42 @@ void PoissonMG::apply(const double* r, double* z) {
     ctx_.check_launch("mg apply");
 }
 
+double PoissonMG::time_finest_pass(int reps) {
+    Level& L0 = *levels_[0];
+    const int n = L0.n;
+    const size_t N = N0_;
+    const dim3 blk(BX, BY);
+    const dim3 cgrid(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n);
+    cudaEvent_t a, b;
+    NUMA_CUDA(cudaEventCreate(&a));
+    NUMA_CUDA(cudaEventCreate(&b));
+    float ms = 0.f;
+    if (precision_ == NUMA_GPU_FP64) {
+        DeviceArray<double> x(N);
+        NUMA_CUDA(cudaMemsetAsync(x.p, 0, N * sizeof(double), ctx_.stream));
+        NUMA_CUDA(cudaMemsetAsync(L0.bs64.p, 0, N * sizeof(double), ctx_.stream));
+        k_rbgs<double, false, false><<<cgrid, blk, 0, ctx_.stream>>>(x.p, L0.bs64.p, nullptr, n, 0);
+        NUMA_CUDA(cudaEventRecord(a, ctx_.stream));
+        for (int r = 0; r < reps; ++r)
+            k_rbgs<double, false, false><<<cgrid, blk, 0, ctx_.stream>>>(x.p, L0.bs64.p, nullptr, n, r & 1);
+        NUMA_CUDA(cudaEventRecord(b, ctx_.stream));
+        NUMA_CUDA(cudaEventSynchronize(b));
+    } else {
+        NUMA_CUDA(cudaMemsetAsync(L0.x32.p, 0, N * sizeof(float), ctx_.stream));
+        NUMA_CUDA(cudaMemsetAsync(L0.bs32.p, 0, N * sizeof(float), ctx_.stream));
+        k_rbgs<float, false, false><<<cgrid, blk, 0, ctx_.stream>>>(L0.x32.p, L0.bs32.p, nullptr, n, 0);
+        NUMA_CUDA(cudaEventRecord(a, ctx_.stream));
+        for (int r = 0; r < reps; ++r)
+            k_rbgs<float, false, false><<<cgrid, blk, 0, ctx_.stream>>>(L0.x32.p, L0.bs32.p, nullptr, n, r & 1);
+        NUMA_CUDA(cudaEventRecord(b, ctx_.stream));
+        NUMA_CUDA(cudaEventSynchronize(b));
+    }
+    ctx_.count_launch(reps + 1);
+    NUMA_CUDA(cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    ctx_.check_launch("time_finest_pass");
+    return reps > 0 ? ms / reps : 0.0;
+}
+
 }  // namespace numa::gpu

@@ -133,6 +133,8 @@ SIGNATURES = {
     "numa_gpu_tf_chebyshev_2018": ([_P, _P, C.POINTER(KrylovParams), _P, C.POINTER(KrylovResult)], _I),
     "numa_gpu_solve_bratu3d_host": ([_P, _SZ, _D, _I, _I, _I, C.POINTER(KrylovParams), _F64P, _F64P,
                                      C.POINTER(KrylovResult)], _I),
+    "numa_gpu_diag_fp64_peak": ([_P, _F64P], _I),
+    "numa_gpu_diag_time_smoother": ([_P, _I, _F64P], _I),
 }
 
 _lib = None
@@ -223,6 +225,12 @@ class Context:
         s = C.c_void_p()
         self.check(self.lib.numa_gpu_ctx_stream(self.h, C.byref(s)), "stream")
         return s.value or 0
+
+    def fp64_peak_tflops(self) -> float:
+        """Measured FP64 FMA throughput of this GPU (diagnostic)."""
+        v = C.c_double()
+        self.check(self.lib.numa_gpu_diag_fp64_peak(self.h, C.byref(v)), "diag_fp64_peak")
+        return v.value
 
     def vec(self, n: int) -> "Vec":
         return Vec(self, n)
@@ -361,6 +369,12 @@ class PoissonMG:
     def levels(self) -> int:
         v = C.c_size_t()
         self.ctx.check(self.lib.numa_gpu_mg_levels(self.h, C.byref(v)), "mg_levels")
+        return v.value
+
+    def time_smoother(self, reps: int = 20) -> float:
+        """Average ms of one finest-level colour pass (diagnostic)."""
+        v = C.c_double()
+        self.ctx.check(self.lib.numa_gpu_diag_time_smoother(self.h, reps, C.byref(v)), "diag_time_smoother")
         return v.value
 
     def __call__(self, r: Vec, z: Vec):

@@ -272,6 +272,14 @@ int numa_gpu_solve_bratu3d_host(numa_gpu_ctx* ctx, size_t n, double lambda, int 
                                 int precond_kind, int mg_precision, const numa_krylov_params* p,
                                 const double* x0, double* x_out, numa_krylov_result* result);
 
+/* ---------------------------------------------------------------- diagnostics */
+/* No counterpart in the reference: measurements for roofline reports.
+ * FP64 FMA throughput of the context's GPU in TFLOP/s (eight independent FMA chains per thread). */
+int numa_gpu_diag_fp64_peak(numa_gpu_ctx* ctx, double* tflops);
+/* Average duration in ms of one red-black Gauss-Seidel colour pass on the finest level of mg
+ * (the V-cycle's dominant kernel), over reps back-to-back launches timed with CUDA events. */
+int numa_gpu_diag_time_smoother(numa_gpu_mg* mg, int reps, double* ms_per_pass);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

@@ -50,14 +50,21 @@ def test_bratu_operator(gpu, oracle, n, lam):
     op.jacobi_diag(du, out)
     Dg = oracle.jacobi_diag(n, lam, u)
     assert np.all(np.abs(out.numpy() - Dg) <= exp_tol(c, Dg))
-    # finite differences: the step comes from reductions, so compare to 1e-6 (the reference
-    # test's FD-vs-analytic bound, tests/test_operators.cpp:46) and to the oracle's FD form
+    # finite differences: the step h comes from reductions (summation order differs), and the
+    # differences cancel, so the GPU's FD result is held to the accuracy of the oracle's own FD
+    # result against the analytic derivative; at the reference test's size (n = 6) also to the
+    # reference test's bounds (tests/test_operators.cpp:46, :60)
     op.jvp(du, dv, out, G.FD)
-    assert rel_err(out.numpy(), J) < 1e-6
-    assert rel_err(out.numpy(), oracle.jvp(n, lam, u, v, 1)) < 1e-6
+    Jfd = oracle.jvp(n, lam, u, v, 1)
+    assert rel_err(out.numpy(), J) <= 2 * rel_err(Jfd, J) + 1e-9
     op.d2(du, dw, out, G.FD)
-    assert rel_err(out.numpy(), D) < 1e-4  # tests/test_operators.cpp:60
-    assert rel_err(out.numpy(), oracle.d2(n, lam, u, w, 1)) < 1e-4
+    Dfd = oracle.d2(n, lam, u, w, 1)
+    assert rel_err(out.numpy(), D) <= 2 * rel_err(Dfd, D) + 1e-7
+    if n <= 8:
+        op.jvp(du, dv, out, G.FD)
+        assert rel_err(out.numpy(), J) < 1e-6
+        op.d2(du, dw, out, G.FD)
+        assert rel_err(out.numpy(), D) < 1e-4
 
 
 def test_bratu_operator_golden(gpu, ref_vectors):
