@@ -28,7 +28,7 @@ NVCC_FLAGS = [
     "--extended-lambda", "-Xptxas", "-warn-spills", f"-I{INCLUDE}",
 ]
 SOURCES = ["context.cu", "bratu3d.cu", "poisson_mg.cu", "gmres.cu", "drivers.cu", "capi.cu", "diag.cu"]
-HEADERS = ["common.cuh", "numa_internal.hpp"]
+HEADERS = ["common.cuh", "numa_internal.hpp", "mg_kernels.cuh"]
 
 
 def nvcc() -> str:

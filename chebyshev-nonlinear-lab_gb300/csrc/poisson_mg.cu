@@ -22,7 +22,7 @@
 #include <cstring>
 #include <limits>
 
-#include "numa_internal.hpp"
+#include "mg_kernels.cuh"
 
 namespace numa::gpu {
 
@@ -35,177 +35,6 @@ struct PoissonMG::Level {
 };
 
 namespace {
-
-constexpr int BX = 32, BY = 8;
-
-template <class T> __device__ __forceinline__ T zero() { return T(0); }
-
-// One colour pass of red-black Gauss-Seidel.  FIRST: x is zero before this pass, so the update
-// is bs / 6.  OUT_Z: also store the result as FP64 into z.
-template <class T, bool FIRST, bool OUT_Z>
-__global__ void __launch_bounds__(BX* BY) k_rbgs(T* __restrict__ x, const T* __restrict__ bs, double* __restrict__ z,
-                                                 int n, int colour) {
-    const int kk = blockIdx.x * BX + threadIdx.x;
-    const int j = blockIdx.y * BY + threadIdx.y;
-    const int i = blockIdx.z;
-    if (j >= n) return;
-    const int k = 2 * kk + ((i + j + colour) & 1);
-    if (k >= n) return;
-    const size_t plane = (size_t)n * n;
-    const size_t p = ((size_t)i * n + j) * n + k;
-    T v;
-    if (FIRST) {
-        v = div6(bs[p]);
-    } else {
-        T acc = bs[p];
-        acc = acc + ((i > 0) ? x[p - plane] : zero<T>());
-        acc = acc + ((i + 1 < n) ? x[p + plane] : zero<T>());
-        acc = acc + ((j > 0) ? x[p - n] : zero<T>());
-        acc = acc + ((j + 1 < n) ? x[p + n] : zero<T>());
-        acc = acc + ((k > 0) ? x[p - 1] : zero<T>());
-        acc = acc + ((k + 1 < n) ? x[p + 1] : zero<T>());
-        v = div6(acc);
-    }
-    x[p] = v;
-    if (OUT_Z) z[p] = (double)v;
-}
-
-// r = b - h^-2 (6x - sum of neighbours) (poisson_mg.hpp:128-149), marching in i.
-template <class T>
-__global__ void __launch_bounds__(BX* BY) k_residual(const T* __restrict__ x, const T* __restrict__ b,
-                                                     T* __restrict__ r, int n, int ichunk, T h2inv) {
-    const int k = blockIdx.x * BX + threadIdx.x;
-    const int j = blockIdx.y * BY + threadIdx.y;
-    const int i0 = blockIdx.z * ichunk;
-    const int i1 = min(i0 + ichunk, n);
-    if (k >= n || j >= n) return;
-    const size_t plane = (size_t)n * n;
-    size_t p = ((size_t)i0 * n + j) * n + k;
-    T below = (i0 > 0) ? x[p - plane] : zero<T>();
-    T cur = x[p];
-    for (int i = i0; i < i1; ++i) {
-        const T above = (i + 1 < n) ? x[p + plane] : zero<T>();
-        T s = T(6) * cur;
-        s = s - below;
-        s = s - above;
-        s = s - ((j > 0) ? x[p - n] : zero<T>());
-        s = s - ((j + 1 < n) ? x[p + n] : zero<T>());
-        s = s - ((k > 0) ? x[p - 1] : zero<T>());
-        s = s - ((k + 1 < n) ? x[p + 1] : zero<T>());
-        r[p] = b[p] - h2inv * s;
-        below = cur;
-        cur = above;
-        p += plane;
-    }
-}
-
-__device__ __forceinline__ double fma_t(double a, double b, double c) { return __fma_rn(a, b, c); }
-__device__ __forceinline__ float fma_t(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-
-// Coarse b = sum over the 27 fine points 2I+{0,1,2} of (w_a w_b w_c) r, weights (1/4,1/2,1/4),
-// summed a (i) outer, b (j), c (k) inner (poisson_mg.hpp:152-188).  Each weight product is a
-// power of two, so w*r is exact and the FMA equals the reference's multiply-then-add.  Also
-// stores bs = b * inv_c for the smoother.
-template <class T>
-__global__ void __launch_bounds__(BX* BY) k_restrict(const T* __restrict__ rf, T* __restrict__ bc,
-                                                     T* __restrict__ bsc, int nf, int nc, double inv_c) {
-    const int K = blockIdx.x * BX + threadIdx.x;
-    const int J = blockIdx.y * BY + threadIdx.y;
-    const int I = blockIdx.z;
-    if (K >= nc || J >= nc) return;
-    const T w[3] = {T(0.25), T(0.5), T(0.25)};
-    T acc = zero<T>();
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const int fi = 2 * I + a;
-        if (fi >= nf) continue;
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-            const int fj = 2 * J + b;
-            if (fj >= nf) continue;
-            const T wab = w[a] * w[b];
-            const T* row = rf + ((size_t)fi * nf + fj) * nf;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const int fk = 2 * K + c;
-                if (fk >= nf) continue;
-                acc = fma_t(wab * w[c], row[fk], acc);
-            }
-        }
-    }
-    const size_t q = ((size_t)I * nc + J) * nc + K;
-    bc[q] = acc;
-    bsc[q] = (T)((double)acc * inv_c);
-}
-
-// 1D interpolation stencil (poisson_mg.hpp:191-220).
-__device__ __forceinline__ int interp(int f, int nc, int (&idx)[2]) {
-    if (f & 1) {
-        idx[0] = (f - 1) >> 1;
-        return 1;
-    }
-    int cnt = 0;
-    const int right = f >> 1;
-    if (right >= 1) idx[cnt++] = right - 1;
-    if (right < nc) idx[cnt++] = right;
-    return cnt;
-}
-
-// Fine x += trilinear interpolation of coarse x (poisson_mg.hpp:222-260).  COLOUR0_ONLY:
-// only points with (i+j+k) even.  Weights: 1 for an odd index, 1/2 per term for an even one;
-// products are powers of two, so w * xc is exact and the FMA equals the reference's sum.
-template <class T, bool COLOUR0_ONLY>
-__global__ void __launch_bounds__(BX* BY) k_prolong(const T* __restrict__ xc, T* __restrict__ xf, int nc, int nf) {
-    const int t = blockIdx.x * BX + threadIdx.x;
-    const int j = blockIdx.y * BY + threadIdx.y;
-    const int i = blockIdx.z;
-    if (j >= nf) return;
-    const int k = COLOUR0_ONLY ? 2 * t + ((i + j) & 1) : t;
-    if (k >= nf) return;
-    int ci[2], cj[2], ck[2];
-    const int ni = interp(i, nc, ci), nj = interp(j, nc, cj), nk = interp(k, nc, ck);
-    const T wi = (ni == 1 && (i & 1)) ? T(1) : T(0.5);
-    const T wj = (nj == 1 && (j & 1)) ? T(1) : T(0.5);
-    const T wk = (nk == 1 && (k & 1)) ? T(1) : T(0.5);
-    T acc = zero<T>();
-    for (int a = 0; a < ni; ++a)
-        for (int b = 0; b < nj; ++b) {
-            const T* row = xc + ((size_t)ci[a] * nc + cj[b]) * nc;
-            for (int c = 0; c < nk; ++c) acc = fma_t(wi * wj * wk, row[ck[c]], acc);
-        }
-    const size_t p = ((size_t)i * nf + j) * nf + k;
-    xf[p] = xf[p] + acc;
-}
-
-// bs = r * inv at the finest FP64 level.
-__global__ void k_scale_in64(const double* __restrict__ r, double* __restrict__ bs, double inv, size_t N) {
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) bs[p] = r[p] * inv;
-}
-
-// b32 = (float) r, bs32 = (float)(r * inv) at the finest FP32 level.
-__global__ void k_scale_in32(const double* __restrict__ r, float* __restrict__ b, float* __restrict__ bs, double inv,
-                             size_t N) {
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) {
-        const double v = r[p];
-        b[p] = (float)v;
-        bs[p] = (float)(v * inv);
-    }
-}
-
-__global__ void k_to64(const float* __restrict__ x, double* __restrict__ z, size_t N) {
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) z[p] = (double)x[p];
-}
-
-// Coarsest level with one point: x = b / (6 h^-2) (poisson_mg.hpp:267-269).
-template <class T>
-__global__ void k_single(const T* __restrict__ b, T* __restrict__ x, double* __restrict__ z, double six_h2inv) {
-    const T v = (T)((double)b[0] / six_h2inv);
-    x[0] = v;
-    if (z) z[0] = (double)v;
-}
 
 template <class T> T* xp(PoissonMG::Level& L);
 template <> double* xp<double>(PoissonMG::Level& L) { return L.x64.p; }
