@@ -27,7 +27,7 @@ NVCC_FLAGS = [
     *ARCH, "-O3", "-lineinfo", "-std=c++20", "-Xcompiler", "-fPIC", "-fmad=false",
     "--extended-lambda", "-Xptxas", "-warn-spills", f"-I{INCLUDE}",
 ]
-SOURCES = ["context.cu", "bratu3d.cu", "poisson_mg.cu", "gmres.cu", "drivers.cu", "capi.cu", "diag.cu"]
+SOURCES = ["context.cu", "bratu3d.cu", "poisson_mg.cu", "gmres.cu", "drivers.cu", "capi.cu", "diag.cu", "mg_noalloc.cu"]
 HEADERS = ["common.cuh", "numa_internal.hpp", "mg_kernels.cuh"]
 
 

@@ -169,6 +169,7 @@ const char* numa_gpu_status_string(int s) {
         case NUMA_GPU_ERR_NO_DEVICE: return "no CUDA device";
         case NUMA_GPU_ERR_CALLBACK: return "callback error";
         case NUMA_GPU_ERR_NOT_SUPPORTED: return "not supported";
+        case NUMA_GPU_ERR_TOO_LARGE: return "too large for the fixed scratch array";
         default: return "unknown status";
     }
 }

@@ -133,6 +133,7 @@ SIGNATURES = {
     "numa_gpu_tf_chebyshev_2018": ([_P, _P, C.POINTER(KrylovParams), _P, C.POINTER(KrylovResult)], _I),
     "numa_gpu_solve_bratu3d_host": ([_P, _SZ, _D, _I, _I, _I, C.POINTER(KrylovParams), _F64P, _F64P,
                                      C.POINTER(KrylovResult)], _I),
+    "numa_gpu_mg_apply_noalloc": ([_SZ, _I, _I, _P, _P, _P], _I),
     "numa_gpu_diag_fp64_peak": ([_P, _F64P], _I),
     "numa_gpu_diag_time_smoother": ([_P, _I, _F64P], _I),
 }
@@ -512,6 +513,17 @@ def gmres_recycled_bratu3d(op: Bratu3D, xpt: Vec, b: Vec, x: Vec, rtol: float, r
                                                         save.h if save else None, C.byref(res)),
                  "gmres_recycled_bratu3d")
     return to_dict(res)
+
+
+def mg_apply_noalloc(n: int, r: Vec, z: Vec, pre: int = 2, post: int = 2, stream: int | None = None) -> int:
+    """One FP64 V-cycle with no device allocation (numa_gpu_mg_apply_noalloc): for callers that
+    cannot allocate device memory when they apply the preconditioner.  Grids up to 63^3; work
+    arrays in a fixed 4.8 MB static device array shared by all calls (order calls on one
+    stream).  Enqueues on `stream` (default: the vectors' context stream) and returns the
+    status code without waiting."""
+    s = r.ctx.stream() if stream is None else stream
+    return r.lib.numa_gpu_mg_apply_noalloc(n, pre, post, C.c_void_p(r.device_ptr()), C.c_void_p(z.device_ptr()),
+                                          C.c_void_p(s))
 
 
 def forcing(params: KrylovParams, k: int, rnorm: float, rprev: float, eta_prev: float, res0: float) -> float:

@@ -40,7 +40,8 @@ typedef enum numa_gpu_status {
     NUMA_GPU_ERR_OUT_OF_MEMORY = 5,
     NUMA_GPU_ERR_NO_DEVICE = 6,
     NUMA_GPU_ERR_CALLBACK = 7,         /* a user apply/precond callback returned non-zero */
-    NUMA_GPU_ERR_NOT_SUPPORTED = 8
+    NUMA_GPU_ERR_NOT_SUPPORTED = 8,
+    NUMA_GPU_ERR_TOO_LARGE = 9         /* the problem does not fit a fixed-size scratch array */
 } numa_gpu_status;
 
 /* ---------------------------------------------------------------- enums */
@@ -271,6 +272,23 @@ int numa_gpu_tf_chebyshev_2018(numa_gpu_bratu3d* op, numa_gpu_vec* x, const numa
 int numa_gpu_solve_bratu3d_host(numa_gpu_ctx* ctx, size_t n, double lambda, int method,
                                 int precond_kind, int mg_precision, const numa_krylov_params* p,
                                 const double* x0, double* x_out, numa_krylov_result* result);
+
+/* ---------------------------------------------------------------- V-cycle without allocation */
+/* No counterpart in the reference.  For callers that cannot allocate device memory when they
+ * apply the preconditioner (while a stream is being captured into a CUDA graph, inside another
+ * library's solver callback, under a device-memory budget fixed up front): one FP64 V-cycle
+ * z = M^-1 r of PoissonMG(n, pre, post) on grids up to 63^3, bit-identical to
+ * numa_gpu_mg_apply, with every work array in one static device array of
+ * NUMA_GPU_NOALLOC_MAX_DOUBLES doubles (4.8 MB, held by each GPU that loads the library until
+ * the process exits).  r and z are distinct device arrays of n^3 doubles on the current device;
+ * the work is enqueued on `stream` (a cudaStream_t, NULL for the default stream) and the call
+ * returns without waiting.  It calls no cudaMalloc, cudaFree or allocating library routine.
+ * The first call on each device, with that device current, resolves the array's address with
+ * cudaGetSymbolAddress: make it before any stream capture.  Every call shares the array, so
+ * calls that may run concurrently on the GPU race: order them on one stream.  Returns
+ * NUMA_GPU_ERR_TOO_LARGE when the hierarchy of n does not fit the array. */
+#define NUMA_GPU_NOALLOC_MAX_DOUBLES 600832
+int numa_gpu_mg_apply_noalloc(size_t n, int pre, int post, const double* r, double* z, void* stream);
 
 /* ---------------------------------------------------------------- diagnostics */
 /* No counterpart in the reference: measurements for roofline reports.
