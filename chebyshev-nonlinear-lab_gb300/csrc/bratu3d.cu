@@ -42,10 +42,6 @@ March march_shape(int n, bool reducing) {
 }
 
 // Minus the 7-point Laplacian without the h^-2 factor, on a value column marching in i.
-struct Col {
-    double below, cur;
-};
-
 __device__ __forceinline__ double lap_sum(const double* __restrict__ v, size_t p, size_t plane, int n, int i,
                                           int j, int k, double below, double cur, double& above) {
     above = (i + 1 < n) ? v[p + plane] : 0.0;
@@ -129,36 +125,57 @@ __global__ void __launch_bounds__(BX* BY) k_jvp(const double* __restrict__ cx, c
     }
 }
 
-// Mixed precision: FP32 arithmetic on FP64 vectors with an FP32 coefficient.
+// Mixed precision: F'(x) v in FP32 arithmetic on FP64 vectors with an FP32 coefficient.  Each
+// FP64 value is converted once (integer arithmetic, no FP64 instruction) into a shared-memory
+// plane of the tile with a 1-point halo; three plane slots roll along i.
 __global__ void __launch_bounds__(BX* BY) k_jvp32(const float* __restrict__ c32, const double* __restrict__ v,
                                                   double* __restrict__ out, int n, int ichunk, float h2inv) {
-    const int k = blockIdx.x * BX + threadIdx.x;
-    const int j = blockIdx.y * BY + threadIdx.y;
+    __shared__ float S[3][BY + 2][BX + 2];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
+    const int k0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
+    const int k = k0 + tx, j = j0 + ty;
     const int i0 = blockIdx.z * ichunk;
     const int i1 = min(i0 + ichunk, n);
-    if (k >= n || j >= n) return;
     const size_t plane = (size_t)n * n;
-    size_t p = ((size_t)i0 * n + j) * n + k;
-    float below = (i0 > 0) ? (float)v[p - plane] : 0.0f;
-    float cur = (float)v[p];
+    auto load = [&](int p) {
+        float(*T)[BX + 2] = S[(p + 3) % 3];
+        for (int e = tid; e < (BY + 2) * (BX + 2); e += BX * BY) {
+            const int r = e / (BX + 2), c = e - r * (BX + 2);
+            const int jj = j0 - 1 + r, kk = k0 - 1 + c;
+            float val = 0.0f;
+            if (p >= 0 && p < n && jj >= 0 && jj < n && kk >= 0 && kk < n)
+                val = f64_to_f32(v[(size_t)p * plane + (size_t)jj * n + kk]);
+            T[r][c] = val;
+        }
+    };
+    load(i0 - 1);
+    load(i0);
     for (int i = i0; i < i1; ++i) {
-        const float above = (i + 1 < n) ? (float)v[p + plane] : 0.0f;
-        const float jm = (j > 0) ? (float)v[p - n] : 0.0f;
-        const float jp = (j + 1 < n) ? (float)v[p + n] : 0.0f;
-        const float km = (k > 0) ? (float)v[p - 1] : 0.0f;
-        const float kp = (k + 1 < n) ? (float)v[p + 1] : 0.0f;
-        float s = 6.0f * cur;
-        s = s - below;
-        s = s - above;
-        s = s - jm;
-        s = s - jp;
-        s = s - km;
-        s = s - kp;
-        out[p] = (double)(h2inv * s - c32[p] * cur);
-        below = cur;
-        cur = above;
-        p += plane;
+        load(i + 1);
+        __syncthreads();
+        if (k < n && j < n) {
+            const float(*Tm)[BX + 2] = S[(i + 2) % 3];
+            const float(*T0)[BX + 2] = S[i % 3];
+            const float(*Tp)[BX + 2] = S[(i + 1) % 3];
+            const float cur = T0[ty + 1][tx + 1];
+            float s = 6.0f * cur;
+            s = s - Tm[ty + 1][tx + 1];
+            s = s - Tp[ty + 1][tx + 1];
+            s = s - T0[ty][tx + 1];
+            s = s - T0[ty + 2][tx + 1];
+            s = s - T0[ty + 1][tx];
+            s = s - T0[ty + 1][tx + 2];
+            const size_t g = (size_t)i * plane + (size_t)j * n + k;
+            out[g] = f32_to_f64(h2inv * s - c32[g] * cur);
+        }
+        __syncthreads();
     }
+}
+
+// c32 = RN32(c) (integer conversion)
+__global__ void k_coef32(const double* __restrict__ c, float* __restrict__ c32, size_t N) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) c32[i] = f64_to_f32(c[i]);
 }
 
 // out = -c v v  (bratu3d.hpp:52: -lambda * exp(u) * v * v, evaluated left to right)
@@ -285,6 +302,12 @@ void Bratu3D::jvp_c32(const float* c32, const double* v, double* out) {
     k_jvp32<<<m.grid, dim3(BX, BY), 0, ctx_.stream>>>(c32, v, out, (int)n_, m.ichunk, (float)h2inv_);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d jvp32");
+}
+
+void Bratu3D::coef32(const double* c, float* c32) {
+    k_coef32<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(c, c32, N_);
+    ctx_.count_launch();
+    ctx_.check_launch("bratu3d coef32");
 }
 
 void Bratu3D::jvp_x(const double* x, const double* v, double* out) {

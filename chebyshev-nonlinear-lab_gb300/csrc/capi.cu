@@ -423,6 +423,13 @@ int numa_gpu_bratu3d_jvp(numa_gpu_bratu3d* op, const numa_gpu_vec* x, const numa
             dev_norm2(c, x->d, f.size(), c.scalar(kSlotTmp1));
             f.jvp_fd(x->d, f0.p, c.scalar(kSlotTmp1), v->d, out->d);
             c.sync();
+        } else if (mode == NUMA_GPU_DERIV_ANALYTIC_FP32) {
+            DeviceArray<double> c64(f.size());
+            DeviceArray<float> c32(f.size());
+            f.coef(x->d, c64.p);
+            f.coef32(c64.p, c32.p);
+            f.jvp_c32(c32.p, v->d, out->d);
+            c.sync();  // the temporaries are freed on return
         } else {
             need(mode == NUMA_GPU_DERIV_ANALYTIC, NUMA_GPU_ERR_INVALID_ARGUMENT, "unknown derivative mode");
             f.jvp_x(x->d, v->d, out->d);

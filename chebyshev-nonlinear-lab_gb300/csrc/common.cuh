@@ -144,6 +144,42 @@ __device__ __forceinline__ double div_by(double a, double d, double rd) {
 }
 
 // ------------------------------------------------------------------------------------------
+// FP64 <-> FP32 conversions in integer arithmetic.  On this GPU the hardware conversion
+// instructions issue on the (slow) FP64 pipe; these use only integer instructions and give the
+// same results: round-to-nearest-even from the IEEE-754 bit fields, with the rare cases (float
+// subnormals, NaN) handed to the hardware instruction.
+__device__ __forceinline__ float f64_to_f32(double d) {
+    const unsigned hi = (unsigned)__double2hiint(d);
+    const unsigned lo = (unsigned)__double2loint(d);
+    const unsigned sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7FFu);
+    const int ef = e - 896;  // re-biased exponent (1023 -> 127)
+    if (ef >= 1 && ef < 255) {
+        unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);  // top 23 fraction bits
+        const unsigned rem = lo & 0x1FFFFFFFu;             // the 29 bits dropped
+        unsigned bits = ((unsigned)ef << 23) | m;
+        bits += (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) ? 1u : 0u;  // carries into the exponent
+        if (bits >= 0x7F800000u) bits = 0x7F800000u;                                // overflow to infinity
+        return __uint_as_float(sign | bits);
+    }
+    if (e == 0 || ef <= -25) return __uint_as_float(sign);  // zero, or too small for a float subnormal
+    if (ef >= 255 && e != 0x7FF) return __uint_as_float(sign | 0x7F800000u);
+    return __double2float_rn(d);  // float subnormals, infinities and NaN: the hardware conversion
+}
+
+__device__ __forceinline__ double f32_to_f64(float f) {
+    const unsigned b = __float_as_uint(f);
+    const unsigned ef = (b >> 23) & 0xFFu;
+    if (ef - 1u < 254u) {  // normal: exact re-bias and shift
+        const unsigned hi = (b & 0x80000000u) | ((ef + 896u) << 20) | ((b & 0x7FFFFFu) >> 3);
+        const unsigned lo = b << 29;
+        return __hiloint2double((int)hi, (int)lo);
+    }
+    if ((b & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
+    return (double)f;  // subnormal, infinity, NaN
+}
+
+// ------------------------------------------------------------------------------------------
 // Host-side context: one device, one stream, reduction scratch and device scalars.
 constexpr int kNumScalars = 2048;
 constexpr size_t kMaxRestart = 250;  // GMRES(m) limit of the device scalar layout below

@@ -183,11 +183,6 @@ private:
     Timers& t_;
 };
 
-__global__ void k_to32(const double* __restrict__ c, float* __restrict__ c32, size_t N) {
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) c32[i] = (float)c[i];
-}
-
 // (j1 - j0) / h  (tf_chebyshev_2018.hpp:46-48)
 __global__ void k_quot(const double* __restrict__ a, const double* __restrict__ b, double h, double* __restrict__ out,
                        size_t N) {
@@ -254,8 +249,7 @@ struct SolveState {
         const float* c32p = nullptr;
         if (p.jvp_precision == NUMA_GPU_FP32 && p.jvp_mode == NUMA_GPU_DERIV_ANALYTIC) {
             c32.resize(N);
-            k_to32<<<ew_grid(ctx, N), 256, 0, ctx.stream>>>(cx, c32.p, N);
-            ctx.count_launch();
+            f.coef32(cx, c32.p);
             c32p = c32.p;
         }
         if (p.jvp_mode == NUMA_GPU_DERIV_FD || p.d2_mode == NUMA_GPU_DERIV_FD) dev_norm2(ctx, x, N, xnorm.p);

@@ -52,8 +52,9 @@ public:
     void coef(const double* x, double* c);
     // out = F'(x) v with the coefficient c = lambda e^x already formed (bratu3d.hpp:33-43).
     void jvp_c(const double* c, const double* v, double* out);
-    // Mixed precision: the same with FP32 arithmetic (c32 = (float)c), FP64 in and out.
+    // Mixed precision: the same with FP32 arithmetic (c32 = RN32(c)), FP64 in and out.
     void jvp_c32(const float* c32, const double* v, double* out);
+    void coef32(const double* c, float* c32);
     // out = F'(x) v computing e^x in the kernel.
     void jvp_x(const double* x, const double* v, double* out);
     // out = F''(x)[v,v] = -c v^2 (bratu3d.hpp:46-56).
@@ -93,6 +94,7 @@ public:
 
 private:
     template <class T> void cycle(size_t l);
+    void cycle32(size_t l);
     Context& ctx_;
     // Finest-level arrays of the cycle in progress (the FP64 cycle works in the caller's r and z).
     void* x0_ = nullptr;

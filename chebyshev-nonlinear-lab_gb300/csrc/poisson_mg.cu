@@ -19,6 +19,7 @@
 //    place, so no copies in or out.
 // The FP64 cycle reproduces the reference V-cycle bit for bit.  The FP32 cycle (precision
 // extension) runs the same steps in single precision.
+#include <algorithm>
 #include <cstring>
 #include <limits>
 
@@ -31,7 +32,8 @@ struct PoissonMG::Level {
     double h2inv = 0.0;
     double inv = 0.0;  // 1.0 / h2inv, as the reference forms it (poisson_mg.hpp:101)
     DeviceArray<double> x64, b64, bs64;
-    DeviceArray<float> x32, b32, bs32;
+    DeviceArray<float> x32, x32b, b32, bs32;  // FP32 cycle: x32 / x32b ping-pong between fused sweeps
+    float* cur32 = nullptr;                   // the FP32 iterate after this level's last sweep
 };
 
 namespace {
@@ -82,6 +84,7 @@ PoissonMG::PoissonMG(Context& ctx, size_t n, int pre, int post, int precision, i
             }
         } else {
             L->x32.resize(Nl);
+            L->x32b.resize(Nl);
             L->b32.resize(Nl);
             L->bs32.resize(Nl);
         }
@@ -173,6 +176,78 @@ void PoissonMG::cycle(size_t l) {
     ctx_.check_launch("mg cycle");
 }
 
+// The FP32 cycle (precision extension): the same steps as cycle<double>, with each red-black
+// sweep one fused kernel (k_rbgs_sweep32) that reads the previous iterate and writes the next
+// (ping-pong between x32 and x32b), and the finest level's last sweep writing z in FP64.
+void PoissonMG::cycle32(size_t l) {
+    Level& L = *levels_[l];
+    const int n = L.n;
+    const bool finest = (l == 0);
+    double* z = finest ? z0_ : nullptr;
+    cudaStream_t s = ctx_.stream;
+    const int ichunk = std::min(32, std::max(2, n / 16));
+    const dim3 sgrid((n + SW_TK - 1) / SW_TK, (n + SW_TJ - 1) / SW_TJ, (n + ichunk - 1) / ichunk);
+    float* bufs[2] = {L.x32.p, L.x32b.p};
+    int cur = 0;  // bufs[cur] holds the iterate
+    bool have = false;
+    const float* bs = L.bs32.p;
+    // one sweep (order 0: colour 0 first): from the iterate (or from zero) into the other buffer
+    auto sweep = [&](int order, bool last_to_z) {
+        const int c0 = order == 0 ? 0 : 1;
+        float* out = bufs[have ? 1 - cur : cur];
+        const float* in = bufs[cur];
+        if (!have) k_rbgs_sweep32<true, true, false><<<sgrid, SW_THREADS, 0, s>>>(in, out, bs, nullptr, n, c0, ichunk);
+        else if (last_to_z) k_rbgs_sweep32<false, true, true><<<sgrid, SW_THREADS, 0, s>>>(in, out, bs, z, n, c0, ichunk);
+        else k_rbgs_sweep32<false, true, false><<<sgrid, SW_THREADS, 0, s>>>(in, out, bs, nullptr, n, c0, ichunk);
+        ctx_.count_launch();
+        if (have) cur = 1 - cur;
+        have = true;
+    };
+    if (l + 1 == levels_.size()) {
+        if (n == 1) {
+            k_single<float><<<1, 1, 0, s>>>(L.b32.p, bufs[0], z, 6.0 * L.h2inv);
+            ctx_.count_launch();
+        } else {
+            for (int sw = 0; sw < 30; ++sw) sweep(sw % 2, z != nullptr && sw == 29);
+        }
+        L.cur32 = bufs[cur];
+        ctx_.check_launch("mg coarsest (fp32)");
+        return;
+    }
+    for (int sw = 0; sw < pre_; ++sw) sweep(0, false);
+    if (pre_ == 0) {
+        NUMA_CUDA(cudaMemsetAsync(bufs[cur], 0, (size_t)n * n * n * sizeof(float), s));
+        have = true;
+    }
+    float* x = bufs[cur];
+    float* r = reinterpret_cast<float*>(scratch_r_.p);
+    const dim3 blk(BX, BY);
+    {
+        const int ich = n >= 64 ? 8 : 1;
+        const dim3 g((n + BX - 1) / BX, (n + BY - 1) / BY, (n + ich - 1) / ich);
+        k_residual<float><<<g, blk, 0, s>>>(x, L.b32.p, r, n, ich, (float)L.h2inv);
+        ctx_.count_launch();
+    }
+    Level& C = *levels_[l + 1];
+    const int nc = C.n;
+    k_restrict<float><<<dim3((nc + BX - 1) / BX, (nc + BY - 1) / BY, nc), blk, 0, s>>>(r, C.b32.p, C.bs32.p, n, nc,
+                                                                                       C.inv);
+    ctx_.count_launch();
+    cycle32(l + 1);
+    if (post_ > 0)
+        k_prolong<float, true><<<dim3(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n), blk, 0, s>>>(C.cur32, x, nc, n);
+    else
+        k_prolong<float, false><<<dim3((n + BX - 1) / BX, (n + BY - 1) / BY, n), blk, 0, s>>>(C.cur32, x, nc, n);
+    ctx_.count_launch();
+    for (int sw = 0; sw < post_; ++sw) sweep(1, z != nullptr && sw == post_ - 1);
+    if (z != nullptr && post_ == 0) {
+        k_to64<<<ew_grid(ctx_, (size_t)n * n * n), 256, 0, s>>>(bufs[cur], z, (size_t)n * n * n);
+        ctx_.count_launch();
+    }
+    L.cur32 = bufs[cur];
+    ctx_.check_launch("mg cycle (fp32)");
+}
+
 void PoissonMG::apply(const double* r, double* z) {
     Level& L0 = *levels_[0];
     const size_t N = N0_;
@@ -191,13 +266,10 @@ void PoissonMG::apply(const double* r, double* z) {
         z0_ = nullptr;
         cycle<double>(0);
     } else {
-        k_scale_in32<<<ew_grid(ctx_, N), 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, L0.inv, N);
+        k_scale_in32<<<ew_grid(ctx_, N), 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, (float)L0.inv, N);
         ctx_.count_launch();
-        x0_ = L0.x32.p;
-        b0_ = L0.b32.p;
-        bs0_ = L0.bs32.p;
         z0_ = z;
-        cycle<float>(0);
+        cycle32(0);
     }
     ctx_.check_launch("mg apply");
 }
@@ -223,12 +295,19 @@ double PoissonMG::time_finest_pass(int reps) {
         NUMA_CUDA(cudaEventRecord(b, ctx_.stream));
         NUMA_CUDA(cudaEventSynchronize(b));
     } else {
+        // the FP32 cycle's dominant kernel: one fused red-black sweep (x32 -> x32b -> x32 ...)
         NUMA_CUDA(cudaMemsetAsync(L0.x32.p, 0, N * sizeof(float), ctx_.stream));
+        NUMA_CUDA(cudaMemsetAsync(L0.x32b.p, 0, N * sizeof(float), ctx_.stream));
         NUMA_CUDA(cudaMemsetAsync(L0.bs32.p, 0, N * sizeof(float), ctx_.stream));
-        k_rbgs<float, false, false><<<cgrid, blk, 0, ctx_.stream>>>(L0.x32.p, L0.bs32.p, nullptr, n, 0);
+        const int ichunk = std::min(32, std::max(2, n / 16));
+        const dim3 sgrid((n + SW_TK - 1) / SW_TK, (n + SW_TJ - 1) / SW_TJ, (n + ichunk - 1) / ichunk);
+        float* bufs[2] = {L0.x32.p, L0.x32b.p};
+        k_rbgs_sweep32<false, true, false><<<sgrid, SW_THREADS, 0, ctx_.stream>>>(bufs[0], bufs[1], L0.bs32.p, nullptr,
+                                                                                  n, 0, ichunk);
         NUMA_CUDA(cudaEventRecord(a, ctx_.stream));
         for (int r = 0; r < reps; ++r)
-            k_rbgs<float, false, false><<<cgrid, blk, 0, ctx_.stream>>>(L0.x32.p, L0.bs32.p, nullptr, n, r & 1);
+            k_rbgs_sweep32<false, true, false><<<sgrid, SW_THREADS, 0, ctx_.stream>>>(
+                bufs[(r + 1) & 1], bufs[r & 1], L0.bs32.p, nullptr, n, r & 1, ichunk);
         NUMA_CUDA(cudaEventRecord(b, ctx_.stream));
         NUMA_CUDA(cudaEventSynchronize(b));
     }

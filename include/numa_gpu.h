@@ -52,8 +52,9 @@ typedef enum numa_gpu_precision {
 
 /* How a directional derivative is formed. */
 typedef enum numa_gpu_deriv_mode {
-    NUMA_GPU_DERIV_ANALYTIC = 0, /* Bratu3D::jvp / Bratu3D::d2 (problems/bratu3d.hpp:33-56) */
-    NUMA_GPU_DERIV_FD = 1        /* jvp_fd / d2_fd (operators/operator.hpp:100-134) */
+    NUMA_GPU_DERIV_ANALYTIC = 0,     /* Bratu3D::jvp / Bratu3D::d2 (problems/bratu3d.hpp:33-56) */
+    NUMA_GPU_DERIV_FD = 1,           /* jvp_fd / d2_fd (operators/operator.hpp:100-134) */
+    NUMA_GPU_DERIV_ANALYTIC_FP32 = 2 /* extension, jvp only: the analytic product in FP32 arithmetic */
 } numa_gpu_deriv_mode;
 
 /* Arnoldi orthogonalisation. */

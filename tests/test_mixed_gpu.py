@@ -1,0 +1,180 @@
+"""Mixed-precision kernels (an extension of the reference path) against a numpy float32
+restatement of the same arithmetic: the FP32 V-cycle (fused red-black sweeps, integer
+FP64<->FP32 conversions) and the FP32 Jacobian-vector product must match it bit for bit; numpy's
+float32 operations are IEEE single precision, and x/6 is correctly rounded in both."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle.oracle_lib import make_point
+
+pytestmark = pytest.mark.gpu
+
+F = np.float32
+
+
+def _G():
+    import numa_gpu
+    return numa_gpu
+
+
+def shifted(x, axis, d):
+    """x shifted so that out[i] = x[i + d] along axis, zero outside (Dirichlet)."""
+    out = np.zeros_like(x)
+    n = x.shape[axis]
+    src = [slice(None)] * 3
+    dst = [slice(None)] * 3
+    if d > 0:
+        src[axis], dst[axis] = slice(d, n), slice(0, n - d)
+    else:
+        src[axis], dst[axis] = slice(0, n + d), slice(-d, n)
+    out[tuple(dst)] = x[tuple(src)]
+    return out
+
+
+def colour_mask(n):
+    i, j, k = np.indices((n, n, n))
+    return (i + j + k) & 1
+
+
+def rb_pass(x, bs, colour, mask):
+    acc = bs.copy()
+    for axis in (0, 1, 2):
+        acc = acc + shifted(x, axis, -1)
+        acc = acc + shifted(x, axis, +1)
+    new = acc / F(6)
+    x = x.copy()
+    x[mask == colour] = new[mask == colour]
+    return x
+
+
+def vcycle32(r64, n, pre=2, post=2):
+    """The FP32 V-cycle of this library (poisson_mg.cu cycle32) in numpy float32."""
+    levels = []
+    m, h2 = n, (n + 1.0) ** 2
+    while True:
+        levels.append((m, h2, 1.0 / h2))
+        if m % 2 == 0 or m <= 1:
+            break
+        m, h2 = (m - 1) // 2, h2 / 4.0
+    w = np.array([0.25, 0.5, 0.25], dtype=F)
+
+    def cycle(l, b, bs):
+        m, h2, _ = levels[l]
+        mask = colour_mask(m)
+        x = np.zeros((m, m, m), F)
+        if l + 1 == len(levels):
+            if m == 1:
+                return np.array([[[F(np.float64(b[0, 0, 0]) / (6.0 * h2))]]], F)
+            for sw in range(30):
+                c0 = sw % 2
+                x = rb_pass(x, bs, c0, mask)
+                x = rb_pass(x, bs, 1 - c0, mask)
+            return x
+        for _ in range(pre):
+            x = rb_pass(x, bs, 0, mask)
+            x = rb_pass(x, bs, 1, mask)
+        s = F(6) * x
+        for axis in (0, 1, 2):
+            s = s - shifted(x, axis, -1)
+            s = s - shifted(x, axis, +1)
+        r = b - F(h2) * s
+        mc, _, invc = levels[l + 1]
+        acc = np.zeros((mc, mc, mc), F)
+        for a in range(3):
+            for bb in range(3):
+                for c in range(3):
+                    acc = acc + (w[a] * w[bb] * w[c]) * r[a:a + 2 * mc:2, bb:bb + 2 * mc:2, c:c + 2 * mc:2]
+        xc = cycle(l + 1, acc, acc * F(invc))
+        # trilinear prolongation at colour-0 points (post > 0)
+        pr = np.zeros((m, m, m), F)
+        idx = np.arange(m)
+        terms = []
+        for f in idx:
+            if f % 2 == 1:
+                terms.append([((f - 1) // 2, F(1))])
+            else:
+                t = []
+                if f // 2 >= 1:
+                    t.append((f // 2 - 1, F(0.5)))
+                if f // 2 < mc:
+                    t.append((f // 2, F(0.5)))
+                terms.append(t)
+        for i in range(m):
+            for j in range(m):
+                for k in range(m):
+                    if post > 0 and (i + j + k) & 1:
+                        continue
+                    acc2 = F(0)
+                    for ci, wi in terms[i]:
+                        for cj, wj in terms[j]:
+                            for ck, wk in terms[k]:
+                                acc2 = F(acc2 + (wi * wj * wk) * xc[ci, cj, ck])
+                    pr[i, j, k] = acc2
+        x = x + pr
+        for _ in range(post):
+            x = rb_pass(x, bs, 1, mask)
+            x = rb_pass(x, bs, 0, mask)
+        return x
+
+    b = r64.reshape(n, n, n).astype(F)
+    bs = b * F(levels[0][2])
+    return cycle(0, b, bs).astype(np.float64).ravel()
+
+
+@pytest.mark.parametrize("n", [1, 3, 7, 15, 16, 21])
+def test_fp32_vcycle_bit_exact(gpu, n):
+    G = _G()
+    N = n ** 3
+    rng = np.random.default_rng(n)
+    r = make_point(N, 1.0) + rng.uniform(-1e-3, 1e-3, N)
+    mg = G.PoissonMG(gpu, n, precision=G.FP32)
+    z = gpu.vec(N)
+    z.fill(5.0)
+    for _ in range(2):
+        mg(gpu.from_numpy(r), z)
+        assert np.array_equal(z.numpy(), vcycle32(r, n))
+
+
+@pytest.mark.parametrize("n", [2, 6, 33, 64])
+def test_fp32_jvp_bit_exact(gpu, n):
+    G = _G()
+    N = n ** 3
+    rng = np.random.default_rng(3 * n)
+    u = make_point(N, 0.3)
+    v = rng.uniform(-1, 1, N) * 10.0 ** rng.integers(-30, 30, N)
+    v[:5] = [0.0, -0.0, 1e-300, -3.5e38, 2.0 ** -130]  # zero, underflow, overflow, float subnormal
+    op = G.Bratu3D(gpu, n, 6.0)
+    out = gpu.vec(N)
+    op.jvp(gpu.from_numpy(u), gpu.from_numpy(v), out, G.ANALYTIC_FP32)
+    # numpy float32 restatement; c = RN32(lambda e^u) with numpy's exp (CUDA's may differ by an
+    # ulp in FP64, which moves the FP32 rounding only for values within an ulp of a float
+    # rounding boundary: probability ~2^-29 per element)
+    c = 6.0 * np.exp(u)
+    with np.errstate(over="ignore", invalid="ignore"):
+        vf = v.reshape(n, n, n).astype(F)
+        s = F(6) * vf
+        for axis in (0, 1, 2):
+            s = s - shifted(vf, axis, -1)
+            s = s - shifted(vf, axis, +1)
+        want = (F((n + 1.0) ** 2) * s - c.reshape(n, n, n).astype(F) * vf).astype(np.float64).ravel()
+    got = out.numpy()
+    same = (got == want) | (np.isnan(got) & np.isnan(want))
+    assert same.all(), np.flatnonzero(~same)[:10]
+
+
+def test_mixed_solve_agrees_with_fp64(gpu):
+    G = _G()
+    n = 31
+    op = G.Bratu3D(gpu, n, 6.0)
+    pc64 = G.Provider.poisson_mg(gpu, n)
+    pc32 = G.Provider.poisson_mg(gpu, n, precision=G.FP32)
+    x64, x32 = gpu.vec(n ** 3), gpu.vec(n ** 3)
+    r64 = G.newton_krylov(op, x64, G.default_params(rtol_nl=1e-10, gmres_restart=30), pc64)
+    r32 = G.newton_krylov(op, x32, G.default_params(rtol_nl=1e-10, gmres_restart=30, flexible=1,
+                                                    jvp_precision=G.FP32), pc32)
+    assert r64["converged"] and r32["converged"]
+    assert r32["res"] <= 1e-10 * r32["res0"]
+    a, b = x32.numpy(), x64.numpy()
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-8
