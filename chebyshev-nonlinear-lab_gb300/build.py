@@ -40,6 +40,25 @@ def _mtime(p: Path) -> float:
     return p.stat().st_mtime if p.exists() else -1.0
 
 
+APPS = {"run_campaign_gpu": HERE / "apps" / "run_campaign_gpu.cpp"}
+
+
+def build_apps(force: bool = False) -> list[Path]:
+    """C++ applications over the C++ adaptor (include/numa/gpu/numa_gpu.hpp), linked to the library."""
+    outs = []
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    for name, src in APPS.items():
+        exe = HERE / name
+        if force or _mtime(exe) < max(_mtime(src), _mtime(LIB), _mtime(INCLUDE / "numa" / "gpu" / "numa_gpu.hpp")):
+            cmd = [cxx, "-std=c++20", "-O2", f"-I{INCLUDE}", str(src), "-o", str(exe), f"-L{HERE}", "-lnuma_gpu",
+                   f"-Wl,-rpath,{HERE}"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"building {name} failed:\n{r.stderr}")
+        outs.append(exe)
+    return outs
+
+
 def build(force: bool = False, verbose: bool = False) -> Path:
     OBJ.mkdir(exist_ok=True)
     deps = [CSRC / h for h in HEADERS] + [INCLUDE / "numa_gpu.h"]
@@ -71,3 +90,4 @@ def build(force: bool = False, verbose: bool = False) -> Path:
 
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(*build_apps(force="--force" in sys.argv))

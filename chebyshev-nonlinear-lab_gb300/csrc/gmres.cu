@@ -7,8 +7,8 @@
 //
 // Orthogonalisation:
 //  * MGS (reference, gmres.hpp:141-144): one kernel per basis vector, each fusing the previous
-//    axpy w -= h_{i-1} V_{i-1} with the next inner product <w, V_i>; the last one fuses the final
-//    axpy with ||w||.  2(j+1)+1 FP64 operations per point, j+2 launches per step.
+//    axpy w -= h_{i-1} V_{i-1} (one FMA) with the next inner product <w, V_i>; the last one fuses
+//    the final axpy with ||w||.  2(j+1)+1 FP64 operations per point, j+2 launches per step.
 //  * CGS2: h = V^T w; w -= V h fused with h' = V^T w; w -= V h' fused with ||w||; H = h + h'.
 //    Three passes over the basis, 4(j+1)+1 FP64 operations per point; for j+1 <= 16.
 // On this GPU FP64 arithmetic, not bandwidth, bounds these kernels, so MGS is the cheaper of
@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(kRedThreads) k_mgs(double* __restrict__ w, con
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) {
         double wi = w[i];
         if (HAS_PREV) {
-            wi = wi + a * Vprev[i];
+            wi = __fma_rn(a, Vprev[i], wi);
             w[i] = wi;
         }
         s[0] = NORM ? __fma_rn(wi, wi, s[0]) : __fma_rn(wi, Vcur[i], s[0]);
@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs(double* __restrict__ w, con
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) {
         double wi = w[i];
         if (MODE != 0) {
-            for (int r = 0; r < cnt; ++r) wi = wi - hs[r] * V[(size_t)r * ldv + i];
+            for (int r = 0; r < cnt; ++r) wi = __fma_rn(-hs[r], V[(size_t)r * ldv + i], wi);
             w[i] = wi;
         }
         if (MODE == 2) {
@@ -101,10 +101,13 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs(double* __restrict__ w, con
     });
 }
 
-// dst = src / d (gmres.hpp:128, :149), correctly rounded division by a runtime scalar.
+// dst = src / d (gmres.hpp:128, :149) as src * RN(1/d): one FP64 instruction instead of a
+// division (within 1.5 ulp of it; the basis vectors already differ from the reference's in the
+// last bits through the order of the inner-product sums).
 __global__ void k_div(const double* __restrict__ src, double d, double rd, double* __restrict__ dst, size_t N) {
+    (void)d;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) dst[i] = div_by(src[i], d, rd);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) dst[i] = src[i] * rd;
 }
 
 // r = b - w (gmres.hpp:116)
@@ -113,8 +116,9 @@ __global__ void k_sub(const double* __restrict__ b, const double* __restrict__ w
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) r[i] = b[i] - w[i];
 }
 
-// out = base + sum_i coef[i] * V_i, accumulated in i order per element, as the reference's
-// sequence of axpy calls does (gmres.hpp:198-199 with base = 0; :304-310 with base = b).
+// out = base + sum_i coef[i] * V_i, accumulated in i order per element as the reference's
+// sequence of axpy calls does (gmres.hpp:198-199 with base = 0; :304-310 with base = b), each
+// term fused into one FMA.
 __global__ void k_combine(const double* __restrict__ base, const double* __restrict__ V, size_t ldv, int cnt,
                           const double* __restrict__ coef, double* __restrict__ out, size_t N) {
     extern __shared__ double cs[];
@@ -123,7 +127,7 @@ __global__ void k_combine(const double* __restrict__ base, const double* __restr
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) {
         double t = base ? base[i] : 0.0;
-        for (int r = 0; r < cnt; ++r) t = t + cs[r] * V[(size_t)r * ldv + i];
+        for (int r = 0; r < cnt; ++r) t = __fma_rn(cs[r], V[(size_t)r * ldv + i], t);
         out[i] = t;
     }
 }

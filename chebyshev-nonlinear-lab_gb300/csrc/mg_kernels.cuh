@@ -194,106 +194,195 @@ namespace {
 // by HBM bandwidth.  The same arithmetic per point as two k_rbgs<float> passes (the colour-c0
 // update, then the colour-c1 update from the new c0 values), so the result is identical.
 //
-// A block owns a 32 (k) x 16 (j) tile and a chunk of i planes and streams the planes through a
-// ring of four shared-memory slots, each holding one plane of the tile with a 2-point halo:
-//   load raw plane p+1; update colour c0 of plane p over the tile plus a 1-point halo (its
-//   in-plane neighbours reach 2 points out); update colour c1 of plane p-1 over the tile (all
-//   its neighbours are colour-c0 values now final); store plane p-1.
+// A block owns a 32 (k) x 16 (j) tile and a chunk of i planes and streams the planes through
+// shared memory: x planes with a 2-point halo in a ring of five slots, b h^2 planes with a
+// 1-point halo in a ring of three.  Step p: start the asynchronous copies (cp.async) of x plane
+// p+2 and b h^2 plane p+1; wait for those of the step before; update colour c0 of plane p over
+// the tile plus a 1-point halo (its in-plane neighbours reach 2 points out); update colour c1
+// of plane p-1 over the tile (all its neighbours are final colour-c0 values); store plane p-1.
+// The copies of one step overlap the arithmetic of the previous one.
 // The sweep is out of place (xin -> xout): blocks read halo planes that neighbouring blocks
 // write, so reads must see the values from before the sweep.  FIRST: xin is zero (no loads).
 constexpr int SW_TK = 32, SW_TJ = 16;
-constexpr int SW_SK = SW_TK + 4, SW_SJ = SW_TJ + 4;
+constexpr int SW_SK = SW_TK + 4, SW_SJ = SW_TJ + 4;  // x tile with a 2-point halo
+constexpr int SW_BK = SW_TK + 2, SW_BJ = SW_TJ + 2;  // b h^2 tile with a 1-point halo
 constexpr int SW_PLANE = SW_SK * SW_SJ;
+constexpr int SW_BPLANE = SW_BK * SW_BJ;
 constexpr int SW_THREADS = 256;
+constexpr int SW_XSLOTS = 5, SW_BSLOTS = 3;
 
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+    const int n = valid ? 4 : 0;  // 0: nothing is read, the 4 bytes are zero-filled
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
+}
+
+// Every thread's roles are fixed for the whole kernel and their offsets computed once: three
+// elements of each x-plane copy and of each b h^2-plane copy, two horizontally adjacent halo
+// positions for the colour-c0 update (exactly one of the two has colour c0 on any plane), two
+// adjacent interior positions for the colour-c1 update, two interior values to store.
 template <bool FIRST, bool OUT_X, bool OUT_Z>
 __global__ void __launch_bounds__(SW_THREADS) k_rbgs_sweep32(const float* __restrict__ xin, float* __restrict__ xout,
                                                             const float* __restrict__ bs, double* __restrict__ z,
                                                             int n, int c0, int ichunk) {
-    __shared__ float P[4][SW_PLANE];
+    __shared__ float X[SW_XSLOTS * SW_PLANE];
+    __shared__ float B[SW_BSLOTS * SW_BPLANE];
     const int tid = threadIdx.x;
     const int k0 = blockIdx.x * SW_TK, j0 = blockIdx.y * SW_TJ;
     const int ib = blockIdx.z * ichunk;
     const int ie = min(ib + ichunk, n);
-    const int c1 = 1 - c0;
     const size_t plane = (size_t)n * n;
-    auto slot = [](int p) { return (p + 8) & 3; };
 
-    auto load = [&](int p) {
-        float* S = P[slot(p)];
-        const bool inside = !FIRST && p >= 0 && p < n;
-        for (int e = tid; e < SW_PLANE; e += SW_THREADS) {
-            const int sj = e / SW_SK, sk = e - sj * SW_SK;
-            const int j = j0 - 2 + sj, k = k0 - 2 + sk;
-            float v = 0.0f;
-            if (inside && j >= 0 && j < n && k >= 0 && k < n) v = xin[(size_t)p * plane + (size_t)j * n + k];
-            S[e] = v;
-        }
-    };
-    // one Gauss-Seidel update at smem index e of plane p (neighbours in the slots of p-1, p, p+1)
-    auto update = [&](int p, int j, int k) {
-        const int e = (j - j0 + 2) * SW_SK + (k - k0 + 2);
-        const float* Sm = P[slot(p - 1)];
-        const float* Sp = P[slot(p + 1)];
-        float* S = P[slot(p)];
-        float acc = bs[(size_t)p * plane + (size_t)j * n + k];
-        acc = acc + Sm[e];
-        acc = acc + Sp[e];
-        acc = acc + S[e - SW_SK];
-        acc = acc + S[e + SW_SK];
-        acc = acc + S[e - 1];
-        acc = acc + S[e + 1];
-        S[e] = div6(acc);
-    };
-    // colour c0 of plane p over the tile and a 1-point halo (rows j0-1 .. j0+16, 17 points a row)
-    auto upd0 = [&](int p) {
-        if (p < 0 || p >= n) return;
-        constexpr int rows = SW_TJ + 2, per = (SW_TK + 2) / 2;
-        for (int t = tid; t < rows * per; t += SW_THREADS) {
-            const int r = t / per, q = t - r * per;
-            const int j = j0 - 1 + r;
-            const int k = k0 - 1 + ((c0 + p + j + k0 + 1) & 1) + 2 * q;
-            if (j >= 0 && j < n && k >= 0 && k < n) update(p, j, k);
-        }
-    };
-    // colour c1 of plane p over the tile (16 points a row, one per thread)
-    auto upd1 = [&](int p) {
-        const int r = tid / (SW_TK / 2), q = tid - r * (SW_TK / 2);
-        const int j = j0 + r;
-        const int k = k0 + ((c1 + p + j + k0) & 1) + 2 * q;
-        if (j < n && k < n) update(p, j, k);
-    };
-    auto store = [&](int p) {
-        const float* S = P[slot(p)];
-        for (int e = tid; e < SW_TK * SW_TJ; e += SW_THREADS) {
-            const int r = e / SW_TK, c = e - r * SW_TK;
-            const int j = j0 + r, k = k0 + c;
-            if (j < n && k < n) {
-                const float v = S[(r + 2) * SW_SK + (c + 2)];
-                const size_t g = (size_t)p * plane + (size_t)j * n + k;
-                if (OUT_X) xout[g] = v;
-                if (OUT_Z) z[g] = f32_to_f64(v);
+    // copies: element e of the x tile (row e / SW_SK) and of the b h^2 tile (row e / SW_BK)
+    int xg[3], bg[3];
+    bool xv[3], bv[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const int e = tid + q * SW_THREADS;
+        int r = e / SW_SK, c = e - r * SW_SK;
+        int j = j0 - 2 + r, k = k0 - 2 + c;
+        xv[q] = e < SW_PLANE && j >= 0 && j < n && k >= 0 && k < n;
+        xg[q] = xv[q] ? j * n + k : 0;
+        r = e / SW_BK;
+        c = e - r * SW_BK;
+        j = j0 - 1 + r;
+        k = k0 - 1 + c;
+        bv[q] = e < SW_BPLANE && j >= 0 && j < n && k >= 0 && k < n;
+        bg[q] = bv[q] ? j * n + k : 0;
+    }
+    // colour-c0 pairs over the 1-point halo: 18 rows x 17 pairs (k0-1+2q, k0+2q)
+    constexpr int NPAIR0 = (SW_TJ + 2) * ((SW_TK + 2) / 2);
+    int h_xo[2], h_bo[2], h_par[2];
+    bool h_va[2], h_vb[2], h_on[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int t = tid + q * SW_THREADS;
+        h_on[q] = t < NPAIR0;
+        const int r = t / ((SW_TK + 2) / 2), qq = t - r * ((SW_TK + 2) / 2);
+        const int j = j0 - 1 + r, ka = k0 - 1 + 2 * qq;
+        h_xo[q] = (r + 1) * SW_SK + (2 * qq + 1);
+        h_bo[q] = r * SW_BK + 2 * qq;
+        h_par[q] = (j + ka) & 1;
+        const bool jin = j >= 0 && j < n;
+        h_va[q] = h_on[q] && jin && ka >= 0 && ka < n;
+        h_vb[q] = h_on[q] && jin && ka + 1 < n;
+    }
+    // colour-c1 pair in the interior: row tid / 16, columns k0+2q, k0+2q+1
+    const int ir = tid / (SW_TK / 2), iq = tid - ir * (SW_TK / 2);
+    const int i_xo = (ir + 2) * SW_SK + (2 * iq + 2);
+    const int i_bo = (ir + 1) * SW_BK + (2 * iq + 1);
+    const int i_par = (j0 + ir + k0 + 2 * iq) & 1;
+    const bool i_va = j0 + ir < n && k0 + 2 * iq < n;
+    const bool i_vb = j0 + ir < n && k0 + 2 * iq + 1 < n;
+    // stores: interior elements tid and tid + 256 (row e / 32)
+    int s_xo[2], s_g[2];
+    bool s_v[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int e = tid + q * SW_THREADS;
+        const int r = e / SW_TK, c = e - r * SW_TK;
+        s_xo[q] = (r + 2) * SW_SK + (c + 2);
+        s_v[q] = j0 + r < n && k0 + c < n;
+        s_g[q] = s_v[q] ? (j0 + r) * n + (k0 + c) : 0;
+    }
+
+    auto load_x = [&](int p, float* S) {
+        const bool pin = p >= 0 && p < n;
+        const float* src = xin + (pin ? (size_t)p * plane : 0);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const int e = tid + q * SW_THREADS;
+            if (e < SW_PLANE) {
+                if (FIRST) S[e] = 0.0f;
+                else cp_async4(S + e, src + xg[q], pin && xv[q]);
             }
         }
     };
+    auto load_b = [&](int p, float* S) {
+        const bool pin = p >= 0 && p < n;
+        const float* src = bs + (pin ? (size_t)p * plane : 0);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const int e = tid + q * SW_THREADS;
+            if (e < SW_BPLANE) cp_async4(S + e, src + bg[q], pin && bv[q]);
+        }
+    };
+    auto gs = [](const float* Bp, const float* Xm, float* X0, const float* Xp, int xo, int bo) {
+        float acc = Bp[bo];
+        acc = acc + Xm[xo];
+        acc = acc + Xp[xo];
+        acc = acc + X0[xo - SW_SK];
+        acc = acc + X0[xo + SW_SK];
+        acc = acc + X0[xo - 1];
+        acc = acc + X0[xo + 1];
+        X0[xo] = div6(acc);
+    };
+    // colour c0 of plane p (ring slots of p-1, p, p+1 and its b h^2 slot)
+    auto upd0 = [&](int p, const float* Xm, float* X0, const float* Xp, const float* Bp) {
+        if (p < 0 || p >= n) return;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            if (!h_on[q]) continue;
+            const bool first = ((p + h_par[q]) & 1) == c0;  // the even-column member has colour c0
+            if (first ? h_va[q] : h_vb[q]) gs(Bp, Xm, X0, Xp, h_xo[q] + (first ? 0 : 1), h_bo[q] + (first ? 0 : 1));
+        }
+    };
+    auto upd1 = [&](int p, const float* Xm, float* X0, const float* Xp, const float* Bp) {
+        const bool first = ((p + i_par) & 1) != c0;  // colour c1 = the other colour
+        if (first ? i_va : i_vb) gs(Bp, Xm, X0, Xp, i_xo + (first ? 0 : 1), i_bo + (first ? 0 : 1));
+    };
+    auto store = [&](int p, const float* S) {
+        const size_t base = (size_t)p * plane;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            if (!s_v[q]) continue;
+            const float v = S[s_xo[q]];
+            if (OUT_X) xout[base + s_g[q]] = v;
+            if (OUT_Z) z[base + s_g[q]] = f32_to_f64(v);
+        }
+    };
+    auto xslot = [&](int s) { return X + s * SW_PLANE; };
+    auto bslot = [&](int s) { return B + s * SW_BPLANE; };
+    auto wrap5 = [](int s) { return s >= SW_XSLOTS ? s - SW_XSLOTS : s; };
+    auto wrap3 = [](int s) { return s >= SW_BSLOTS ? s - SW_BSLOTS : s; };
 
-    load(ib - 2);
-    load(ib - 1);
-    load(ib);
+    // ring positions: x plane q lives in slot (q - ib + 2) mod 5, b h^2 plane q in (q - ib + 1) mod 3
+    load_x(ib - 2, xslot(0));
+    load_x(ib - 1, xslot(1));
+    load_x(ib, xslot(2));
+    load_x(ib + 1, xslot(3));
+    load_b(ib - 1, bslot(0));
+    load_b(ib, bslot(1));
+    cp_async_commit();
+    cp_async_wait<0>();
     __syncthreads();
-    upd0(ib - 1);
-    __syncthreads();
+    upd0(ib - 1, xslot(0), xslot(1), xslot(2), bslot(0));
+    int sx = 2, sb = 1;  // slots of x plane p and b h^2 plane p
     for (int p = ib; p <= ie; ++p) {
-        load(p + 1);
         __syncthreads();
-        upd0(p);
+        load_x(p + 2, xslot(wrap5(sx + 2)));
+        load_b(p + 1, bslot(wrap3(sb + 1)));
+        cp_async_commit();
+        cp_async_wait<1>();
+        __syncthreads();
+        float* Xm1 = xslot(wrap5(sx + 4));
+        float* X0 = xslot(sx);
+        upd0(p, Xm1, X0, xslot(wrap5(sx + 1)), bslot(sb));
         __syncthreads();
         if (p - 1 >= ib) {
-            upd1(p - 1);
+            upd1(p - 1, xslot(wrap5(sx + 3)), Xm1, X0, bslot(wrap3(sb + 2)));
             __syncthreads();
-            store(p - 1);
+            store(p - 1, Xm1);
         }
+        sx = wrap5(sx + 1);
+        sb = wrap3(sb + 1);
     }
+    cp_async_wait<0>();
 }
 
 }  // namespace

@@ -100,7 +100,34 @@ PoissonMG::PoissonMG(Context& ctx, size_t n, int pre, int post, int precision, i
     }
 }
 
-PoissonMG::~PoissonMG() = default;
+PoissonMG::~PoissonMG() {
+    if (coarse_exec_) cudaGraphExecDestroy(coarse_exec_);
+}
+
+void PoissonMG::coarse_cycle() {
+    if (!coarse_exec_) {
+        const uint64_t before = ctx_.launches;
+        NUMA_CUDA(cudaStreamBeginCapture(ctx_.stream, cudaStreamCaptureModeThreadLocal));
+        cudaGraph_t graph = nullptr;
+        try {
+            if (precision_ == NUMA_GPU_FP64) cycle<double>(1);
+            else cycle32(1);
+        } catch (...) {
+            cudaStreamEndCapture(ctx_.stream, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            throw;
+        }
+        NUMA_CUDA(cudaStreamEndCapture(ctx_.stream, &graph));
+        const cudaError_t e = cudaGraphInstantiate(&coarse_exec_, graph, 0);
+        cudaGraphDestroy(graph);
+        NUMA_CUDA(e);
+        coarse_kernels_ = ctx_.launches - before;
+        ctx_.launches = before;
+    }
+    NUMA_CUDA(cudaGraphLaunch(coarse_exec_, ctx_.stream));
+    ctx_.count_launch(static_cast<unsigned>(coarse_kernels_));
+}
 
 template <class T>
 void PoissonMG::cycle(size_t l) {
@@ -159,7 +186,8 @@ void PoissonMG::cycle(size_t l) {
         ctx_.count_launch();
     }
     ctx_.check_launch("mg restrict");
-    cycle<T>(l + 1);
+    if (l == 0) coarse_cycle();
+    else cycle<T>(l + 1);
     if (post_ > 0) {
         const dim3 g(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n);
         k_prolong<T, true><<<g, blk, 0, s>>>(xp<T>(C), x, nc, n);
@@ -233,7 +261,8 @@ void PoissonMG::cycle32(size_t l) {
     k_restrict<float><<<dim3((nc + BX - 1) / BX, (nc + BY - 1) / BY, nc), blk, 0, s>>>(r, C.b32.p, C.bs32.p, n, nc,
                                                                                        C.inv);
     ctx_.count_launch();
-    cycle32(l + 1);
+    if (l == 0) coarse_cycle();
+    else cycle32(l + 1);
     if (post_ > 0)
         k_prolong<float, true><<<dim3(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n), blk, 0, s>>>(C.cur32, x, nc, n);
     else

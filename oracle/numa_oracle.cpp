@@ -365,13 +365,288 @@ private:
     int pre_, post_;
 };
 
+// ---------------------------------------------------------------- HelmholtzMG2D (linalg/helmholtz_mg2d.hpp)
+// 2D V-cycle for alpha I - nu Lap_h, 5-point stencil, red-black Gauss-Seidel (colour (i+j)&1),
+// 9-point full weighting, bilinear additive prolongation; levels while n is odd, s = nu h^-2
+// quartered per level (helmholtz_mg2d.hpp:15-32); coarsest n = 1 exact, else 30 sweeps.
+class HelmholtzMG2D {
+public:
+    struct Level {
+        std::size_t n = 0;
+        double s = 0.0;
+        DVec x, b, r;
+    };
+    HelmholtzMG2D(std::size_t n, double alpha, double nu, int pre = 2, int post = 2)
+        : alpha_(alpha), pre_(pre), post_(post) {
+        std::size_t m = n;
+        double s = nu * (static_cast<double>(n) + 1.0) * (static_cast<double>(n) + 1.0);
+        for (;;) {
+            Level L;
+            L.n = m;
+            L.s = s;
+            L.x.assign(m * m, 0.0);
+            L.b.assign(m * m, 0.0);
+            L.r.assign(m * m, 0.0);
+            levels_.push_back(std::move(L));
+            if (m % 2 == 0 || m <= 1) break;
+            m = (m - 1) / 2;
+            s /= 4.0;
+        }
+    }
+    std::size_t levels() const { return levels_.size(); }
+    void apply(const DVec& r, DVec& z) const {
+        Level& L0 = levels_[0];
+        L0.b = r;
+        std::fill(L0.x.begin(), L0.x.end(), 0.0);
+        cycle(0);
+        z = L0.x;
+    }
+
+    // (helmholtz_mg2d.hpp:51-70): x = (b + s * sum of the 4 neighbours) / (alpha + 4 s)
+    void smooth(Level& L, int order) const {
+        const std::size_t n = L.n;
+        const double den = alpha_ + 4.0 * L.s;
+        for (int pass = 0; pass < 2; ++pass) {
+            const std::size_t colour = (order == 0) ? pass : 1 - pass;
+#pragma omp parallel for schedule(static) if (n * n > 4096)
+            for (long ii = 0; ii < static_cast<long>(n); ++ii) {
+                const std::size_t i = static_cast<std::size_t>(ii);
+                for (std::size_t j = (i + colour) & 1; j < n; j += 2) {
+                    const std::size_t p = i * n + j;
+                    double nb = 0.0;
+                    if (i > 0) nb += L.x[p - n];
+                    if (i + 1 < n) nb += L.x[p + n];
+                    if (j > 0) nb += L.x[p - 1];
+                    if (j + 1 < n) nb += L.x[p + 1];
+                    L.x[p] = (L.b[p] + L.s * nb) / den;
+                }
+            }
+        }
+    }
+    // r = b - (alpha x + s (4x - nb)) (helmholtz_mg2d.hpp:72-87)
+    void residual(Level& L) const {
+        const std::size_t n = L.n;
+#pragma omp parallel for schedule(static) if (n * n > 4096)
+        for (long ii = 0; ii < static_cast<long>(n); ++ii) {
+            const std::size_t i = static_cast<std::size_t>(ii);
+            for (std::size_t j = 0; j < n; ++j) {
+                const std::size_t p = i * n + j;
+                double nb = 0.0;
+                if (i > 0) nb += L.x[p - n];
+                if (i + 1 < n) nb += L.x[p + n];
+                if (j > 0) nb += L.x[p - 1];
+                if (j + 1 < n) nb += L.x[p + 1];
+                L.r[p] = L.b[p] - (alpha_ * L.x[p] + L.s * (4.0 * L.x[p] - nb));
+            }
+        }
+    }
+    // 9-point full weighting, coarse I <-> fine 2I+1 (helmholtz_mg2d.hpp:89-108)
+    static void restrict_to(const Level& F, Level& C) {
+        static const double w[3] = {0.25, 0.5, 0.25};
+        const std::size_t nf = F.n, nc = C.n;
+#pragma omp parallel for schedule(static) if (nc * nc > 4096)
+        for (long II = 0; II < static_cast<long>(nc); ++II)
+            for (std::size_t J = 0; J < nc; ++J) {
+                const std::size_t I = static_cast<std::size_t>(II);
+                double acc = 0.0;
+                for (int a = 0; a < 3; ++a) {
+                    const std::size_t fi = 2 * I + a;
+                    if (fi >= nf) continue;
+                    for (int b = 0; b < 3; ++b) {
+                        const std::size_t fj = 2 * J + b;
+                        if (fj >= nf) continue;
+                        acc += w[a] * w[b] * F.r[fi * nf + fj];
+                    }
+                }
+                C.b[I * nc + J] = acc;
+            }
+    }
+    // bilinear additive prolongation (helmholtz_mg2d.hpp:110-136)
+    static void prolong_add(const Level& C, Level& F) {
+        const std::size_t nf = F.n, nc = C.n;
+#pragma omp parallel for schedule(static) if (nf * nf > 4096)
+        for (long ii = 0; ii < static_cast<long>(nf); ++ii) {
+            const std::size_t i = static_cast<std::size_t>(ii);
+            std::size_t ci[2]; double wi[2];
+            const int ni = PoissonMG::interp_1d(i, nc, ci, wi);
+            for (std::size_t j = 0; j < nf; ++j) {
+                std::size_t cj[2]; double wj[2];
+                const int nj = PoissonMG::interp_1d(j, nc, cj, wj);
+                double acc = 0.0;
+                for (int a = 0; a < ni; ++a)
+                    for (int b = 0; b < nj; ++b) acc += wi[a] * wj[b] * C.x[ci[a] * nc + cj[b]];
+                F.x[i * nf + j] += acc;
+            }
+        }
+    }
+    void cycle(std::size_t l) const {
+        Level& L = levels_[l];
+        if (l + 1 == levels_.size()) {
+            if (L.n == 1) L.x[0] = L.b[0] / (alpha_ + 4.0 * L.s);
+            else
+                for (int s = 0; s < 30; ++s) smooth(L, s % 2);
+            return;
+        }
+        for (int s = 0; s < pre_; ++s) smooth(L, 0);
+        residual(L);
+        Level& C = levels_[l + 1];
+        restrict_to(L, C);
+        std::fill(C.x.begin(), C.x.end(), 0.0);
+        cycle(l + 1);
+        prolong_add(C, L);
+        for (int s = 0; s < post_; ++s) smooth(L, 1);
+    }
+    mutable std::vector<Level> levels_;
+
+private:
+    double alpha_;
+    int pre_, post_;
+};
+
+// ---------------------------------------------------------------- Burgers2D (problems/burgers2d.hpp)
+// One implicit-Euler step of 2D viscous Burgers with a manufactured root:
+// F(w) = w/dt + (u u_x + v u_y, u v_x + v v_y) - nu Lap_h w - g, w = (u, v) on n^2 interior
+// points each, central differences, homogeneous Dirichlet; g makes w* = a (sin pi x sin pi y,
+// sin 2 pi x sin pi y) an exact discrete root (burgers2d.hpp:25-52).
+struct Burgers {
+    std::size_t n;
+    double nu, dt, amp;
+    DVec source, exact;
+
+    Burgers(std::size_t n_, double nu_, double dt_, double amp_) : n(n_), nu(nu_), dt(dt_), amp(amp_) {
+        if (n == 0 || !(nu > 0.0) || !(dt > 0.0) || !std::isfinite(nu) || !std::isfinite(dt) || !std::isfinite(amp))
+            throw std::invalid_argument("Burgers2D: invalid n, nu or dt");
+        const double pi = std::acos(-1.0);
+        const double h = 1.0 / (static_cast<double>(n) + 1.0);
+        const std::size_t nn = n * n;
+        exact.assign(2 * nn, 0.0);
+        for (std::size_t i = 0; i < n; ++i)
+            for (std::size_t j = 0; j < n; ++j) {
+                const double y = (static_cast<double>(i) + 1.0) * h;
+                const double x = (static_cast<double>(j) + 1.0) * h;
+                exact[i * n + j] = amp * std::sin(pi * x) * std::sin(pi * y);
+                exact[nn + i * n + j] = amp * std::sin(2.0 * pi * x) * std::sin(pi * y);
+            }
+        DVec g;
+        eval_raw(exact, g);
+        source = std::move(g);
+    }
+    std::size_t size() const { return 2 * n * n; }
+
+    double at(const DVec& a, std::size_t comp, long i, long j) const {
+        if (i < 0 || j < 0 || i >= static_cast<long>(n) || j >= static_cast<long>(n)) return 0.0;
+        return a[comp * n * n + static_cast<std::size_t>(i) * n + static_cast<std::size_t>(j)];
+    }
+
+    // (burgers2d.hpp:169-210)
+    void eval_raw(const DVec& w, DVec& out) const {
+        const std::size_t nn = n * n;
+        const double h = 1.0 / (static_cast<double>(n) + 1.0);
+        const double inv2h = 1.0 / (2.0 * h), invh2 = 1.0 / (h * h), invdt = 1.0 / dt;
+        out.assign(size(), 0.0);
+#pragma omp parallel for schedule(static) if (nn > 4096)
+        for (long i = 0; i < static_cast<long>(n); ++i)
+            for (long j = 0; j < static_cast<long>(n); ++j) {
+                const std::size_t p = static_cast<std::size_t>(i) * n + static_cast<std::size_t>(j);
+                const double u = w[p], v = w[nn + p];
+                const double ux = (at(w, 0, i, j + 1) - at(w, 0, i, j - 1)) * inv2h;
+                const double uy = (at(w, 0, i + 1, j) - at(w, 0, i - 1, j)) * inv2h;
+                const double vx = (at(w, 1, i, j + 1) - at(w, 1, i, j - 1)) * inv2h;
+                const double vy = (at(w, 1, i + 1, j) - at(w, 1, i - 1, j)) * inv2h;
+                const double lu = (at(w, 0, i, j + 1) + at(w, 0, i, j - 1) + at(w, 0, i + 1, j) + at(w, 0, i - 1, j) -
+                                   4.0 * u) * invh2;
+                const double lv = (at(w, 1, i, j + 1) + at(w, 1, i, j - 1) + at(w, 1, i + 1, j) + at(w, 1, i - 1, j) -
+                                   4.0 * v) * invh2;
+                out[p] = invdt * u + u * ux + v * uy - nu * lu;
+                out[nn + p] = invdt * v + u * vx + v * vy - nu * lv;
+            }
+    }
+    void eval(const DVec& w, DVec& out) const {
+        eval_raw(w, out);
+        for (std::size_t q = 0; q < out.size(); ++q) out[q] -= source[q];
+    }
+    // (burgers2d.hpp:71-123)
+    void jvp(const DVec& w, const DVec& d, DVec& out) const {
+        const std::size_t nn = n * n;
+        const double h = 1.0 / (static_cast<double>(n) + 1.0);
+        const double inv2h = 1.0 / (2.0 * h), invh2 = 1.0 / (h * h), invdt = 1.0 / dt;
+        out.assign(size(), 0.0);
+#pragma omp parallel for schedule(static) if (nn > 4096)
+        for (long i = 0; i < static_cast<long>(n); ++i)
+            for (long j = 0; j < static_cast<long>(n); ++j) {
+                const std::size_t p = static_cast<std::size_t>(i) * n + static_cast<std::size_t>(j);
+                const double u = w[p], v = w[nn + p], du = d[p], dv = d[nn + p];
+                const double ux = (at(w, 0, i, j + 1) - at(w, 0, i, j - 1)) * inv2h;
+                const double uy = (at(w, 0, i + 1, j) - at(w, 0, i - 1, j)) * inv2h;
+                const double vx = (at(w, 1, i, j + 1) - at(w, 1, i, j - 1)) * inv2h;
+                const double vy = (at(w, 1, i + 1, j) - at(w, 1, i - 1, j)) * inv2h;
+                const double dux = (at(d, 0, i, j + 1) - at(d, 0, i, j - 1)) * inv2h;
+                const double duy = (at(d, 0, i + 1, j) - at(d, 0, i - 1, j)) * inv2h;
+                const double dvx = (at(d, 1, i, j + 1) - at(d, 1, i, j - 1)) * inv2h;
+                const double dvy = (at(d, 1, i + 1, j) - at(d, 1, i - 1, j)) * inv2h;
+                const double ldu = (at(d, 0, i, j + 1) + at(d, 0, i, j - 1) + at(d, 0, i + 1, j) + at(d, 0, i - 1, j) -
+                                    4.0 * du) * invh2;
+                const double ldv = (at(d, 1, i, j + 1) + at(d, 1, i, j - 1) + at(d, 1, i + 1, j) + at(d, 1, i - 1, j) -
+                                    4.0 * dv) * invh2;
+                out[p] = invdt * du + du * ux + u * dux + dv * uy + v * duy - nu * ldu;
+                out[nn + p] = invdt * dv + du * vx + u * dvx + dv * vy + v * dvy - nu * ldv;
+            }
+    }
+    // exact second derivative 2 (du dux + dv duy, du dvx + dv dvy) (burgers2d.hpp:125-160)
+    void d2(const DVec& w, const DVec& d, DVec& out) const {
+        (void)w;
+        const std::size_t nn = n * n;
+        const double h = 1.0 / (static_cast<double>(n) + 1.0);
+        const double inv2h = 1.0 / (2.0 * h);
+        out.assign(size(), 0.0);
+#pragma omp parallel for schedule(static) if (nn > 4096)
+        for (long i = 0; i < static_cast<long>(n); ++i)
+            for (long j = 0; j < static_cast<long>(n); ++j) {
+                const std::size_t p = static_cast<std::size_t>(i) * n + static_cast<std::size_t>(j);
+                const double du = d[p], dv = d[nn + p];
+                const double dux = (at(d, 0, i, j + 1) - at(d, 0, i, j - 1)) * inv2h;
+                const double duy = (at(d, 0, i + 1, j) - at(d, 0, i - 1, j)) * inv2h;
+                const double dvx = (at(d, 1, i, j + 1) - at(d, 1, i, j - 1)) * inv2h;
+                const double dvy = (at(d, 1, i + 1, j) - at(d, 1, i - 1, j)) * inv2h;
+                out[p] = 2.0 * (du * dux + dv * duy);
+                out[nn + p] = 2.0 * (du * dvx + dv * dvy);
+            }
+    }
+};
+
+struct BurgersOp {
+    const Burgers& f;
+    int jvp_mode, d2_mode;
+    Timers* timers;
+    std::size_t size() const { return f.size(); }
+    void eval(const DVec& x, DVec& out) const {
+        auto t0 = Clock::now();
+        f.eval(x, out);
+        timers->t_F += seconds_since(t0);
+    }
+    void jvp(const DVec& x, const DVec& v, DVec& out) const {
+        auto t0 = Clock::now();
+        if (jvp_mode == 1) jvp_fd(f, x, v, out); else f.jvp(x, v, out);
+        timers->t_JVP += seconds_since(t0);
+    }
+    void d2(const DVec& x, const DVec& v, DVec& out) const {
+        auto t0 = Clock::now();
+        if (d2_mode == 1) d2_fd(f, x, v, out); else f.d2(x, v, out);
+        timers->t_D2 += seconds_since(t0);
+    }
+};
+
 // ---------------------------------------------------------------- preconditioner providers
+constexpr int kBurgersMG = 3;
+
 // A bound preconditioner is "z = M^-1 r"; make(x) binds it at a nonlinear iterate
 // (krylov_newton.hpp:20-22, poisson_mg.hpp:303-320, bratu3d.hpp:104-120).
 struct Provider {
-    int kind = 0;  // numa_gpu_precond_kind
+    int kind = 0;  // numa_gpu_precond_kind, or kBurgersMG
     const Bratu* f = nullptr;
     std::shared_ptr<PoissonMG> mg;
+    std::shared_ptr<HelmholtzMG2D> hmg;  // BurgersMGProvider (burgers2d.hpp:220-246)
+    std::size_t nn = 0;
     DVec diag;
     Timers* timers = nullptr;
 
@@ -384,6 +659,13 @@ struct Provider {
         auto t0 = Clock::now();
         if (kind == NUMA_GPU_PRECOND_POISSON_MG) {
             mg->apply(r, z);
+        } else if (kind == kBurgersMG) {
+            DVec ru(r.begin(), r.begin() + nn), rv(r.begin() + nn, r.end()), zu, zv;
+            hmg->apply(ru, zu);
+            hmg->apply(rv, zv);
+            z.resize(r.size());
+            std::copy(zu.begin(), zu.end(), z.begin());
+            std::copy(zv.begin(), zv.end(), z.begin() + nn);
         } else if (kind == NUMA_GPU_PRECOND_JACOBI) {
             z.resize(r.size());
             for (std::size_t p = 0; p < r.size(); ++p) z[p] = r[p] / diag[p];
@@ -1043,6 +1325,107 @@ int oracle_solve_bratu3d(size_t n, double lambda, int method, int precond_kind,
 double oracle_forcing(const numa_krylov_params* cp, size_t k, double rnorm, double rprev,
                       double eta_prev, double res0) {
     return forcing(to_params(cp), k, rnorm, rprev, eta_prev, res0);
+}
+
+// ---- Burgers2D and HelmholtzMG2D
+int oracle_burgers2d_exact(size_t n, double nu, double dt, double amp, double* out) {
+    try {
+        Burgers f(n, nu, dt, amp);
+        std::memcpy(out, f.exact.data(), f.size() * sizeof(double));
+        return 0;
+    } catch (...) {
+        return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    }
+}
+
+int oracle_burgers2d_eval(size_t n, double nu, double dt, double amp, const double* w, double* out) {
+    Burgers f(n, nu, dt, amp);
+    DVec W(w, w + f.size()), O;
+    f.eval(W, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+    return 0;
+}
+
+int oracle_burgers2d_jvp(size_t n, double nu, double dt, double amp, const double* w, const double* d, double* out,
+                         int mode) {
+    Burgers f(n, nu, dt, amp);
+    DVec W(w, w + f.size()), D(d, d + f.size()), O;
+    if (mode == 1) jvp_fd(f, W, D, O); else f.jvp(W, D, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+    return 0;
+}
+
+int oracle_burgers2d_d2(size_t n, double nu, double dt, double amp, const double* w, const double* d, double* out,
+                        int mode) {
+    Burgers f(n, nu, dt, amp);
+    DVec W(w, w + f.size()), D(d, d + f.size()), O;
+    if (mode == 1) d2_fd(f, W, D, O); else f.d2(W, D, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+    return 0;
+}
+
+int oracle_hmg2d_levels(size_t n, double alpha, double nu) {
+    HelmholtzMG2D mg(n, alpha, nu);
+    return static_cast<int>(mg.levels());
+}
+
+int oracle_hmg2d_apply(size_t n, double alpha, double nu, int pre, int post, const double* r, double* z) {
+    HelmholtzMG2D mg(n, alpha, nu, pre, post);
+    DVec R(r, r + n * n), Z;
+    mg.apply(R, Z);
+    std::memcpy(z, Z.data(), Z.size() * sizeof(double));
+    return 0;
+}
+
+// Burgers2D(n, nu, dt, amp) from x0 with NoPrecond (precond_kind 0) or BurgersMGProvider (1).
+int oracle_solve_burgers2d(size_t n, double nu, double dt, double amp, int method, int precond_kind,
+                           const numa_krylov_params* cp, const double* x0, double* x_out, numa_krylov_result* res) {
+    try {
+        auto t_start = Clock::now();
+        Burgers f(n, nu, dt, amp);
+        Timers t;
+        BurgersOp op{f, cp ? cp->jvp_mode : 0, cp ? cp->d2_mode : 0, &t};
+        Params p = to_params(cp);
+        if (method == NUMA_GPU_METHOD_CHEB_REC) p.recycle = true;
+        Provider pc;
+        pc.timers = &t;
+        if (precond_kind == NUMA_GPU_PRECOND_POISSON_MG) {
+            pc.kind = kBurgersMG;
+            pc.hmg = std::make_shared<HelmholtzMG2D>(n, 1.0 / dt, nu);
+            pc.nn = n * n;
+        }
+        DVec X0(x0, x0 + f.size());
+        Result r;
+        switch (method) {
+            case NUMA_GPU_METHOD_NK: r = newton_krylov(op, X0, p, pc); break;
+            case NUMA_GPU_METHOD_CHEB:
+            case NUMA_GPU_METHOD_CHEB_REC: r = chebyshev_inexact(op, X0, p, pc); break;
+            case NUMA_GPU_METHOD_TF2018: r = tf_chebyshev_2018(op, X0, p, pc); break;
+            default: return NUMA_GPU_ERR_INVALID_ARGUMENT;
+        }
+        if (x_out) std::memcpy(x_out, r.x.data(), r.x.size() * sizeof(double));
+        if (res) {
+            std::memset(res, 0, sizeof(*res));
+            res->converged = r.converged ? 1 : 0;
+            res->iters = r.iters;
+            res->n_F = r.n_F;
+            res->n_JVP = r.n_JVP;
+            res->n_D2 = r.n_D2;
+            res->n_lin_iters = r.n_lin_iters;
+            res->n_lin_failures = r.n_lin_failures;
+            res->n_prec = r.n_prec;
+            res->res0 = r.res0;
+            res->res = r.res;
+            res->t_F = t.t_F;
+            res->t_JVP = t.t_JVP;
+            res->t_D2 = t.t_D2;
+            res->t_prec = t.t_prec;
+            res->t_total = seconds_since(t_start);
+        }
+        return 0;
+    } catch (const std::invalid_argument&) {
+        return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    }
 }
 
 }  // extern "C"

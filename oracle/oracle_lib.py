@@ -114,6 +114,14 @@ class Oracle:
         self._solve = fn("solve_bratu3d", [sz, dbl, i32, i32, C.POINTER(KrylovParams), F64P, F64P,
                                            C.POINTER(KrylovResult)], i32)
         self._forcing = fn("forcing", [C.POINTER(KrylovParams), sz, dbl, dbl, dbl, dbl], dbl)
+        self._bexact = fn("burgers2d_exact", [sz, dbl, dbl, dbl, F64P], i32)
+        self._beval = fn("burgers2d_eval", [sz, dbl, dbl, dbl, F64P, F64P], i32)
+        self._bjvp = fn("burgers2d_jvp", [sz, dbl, dbl, dbl, F64P, F64P, F64P, i32], i32)
+        self._bd2 = fn("burgers2d_d2", [sz, dbl, dbl, dbl, F64P, F64P, F64P, i32], i32)
+        self._hlev = fn("hmg2d_levels", [sz, dbl, dbl], i32)
+        self._happly = fn("hmg2d_apply", [sz, dbl, dbl, i32, i32, F64P, F64P], i32)
+        self._bsolve = fn("solve_burgers2d", [sz, dbl, dbl, dbl, i32, i32, C.POINTER(KrylovParams), F64P, F64P,
+                                              C.POINTER(KrylovResult)], i32)
         if prefix == "oracle_":
             self._smooth = fn("mg_smooth", [sz, dbl, F64P, F64P, i32])
             self._resid = fn("mg_residual", [sz, dbl, F64P, F64P, F64P])
@@ -223,6 +231,51 @@ class Oracle:
                          C.byref(res))
         if rc != 0:
             raise ValueError(f"oracle solve failed with status {rc}")
+        return x, struct_dict(res)
+
+    # ---- Burgers2D / HelmholtzMG2D
+    def burgers_exact(self, n, nu, dt, amp):
+        out = np.empty(2 * n * n)
+        if self._bexact(n, nu, dt, amp, _ptr(out)) != 0:
+            raise ValueError("Burgers2D rejected the arguments")
+        return out
+
+    def burgers_eval(self, n, nu, dt, amp, w):
+        w = _f64(w)
+        out = np.empty(2 * n * n)
+        self._beval(n, nu, dt, amp, _ptr(w), _ptr(out))
+        return out
+
+    def burgers_jvp(self, n, nu, dt, amp, w, d, mode=0):
+        w, d = _f64(w), _f64(d)
+        out = np.empty(2 * n * n)
+        self._bjvp(n, nu, dt, amp, _ptr(w), _ptr(d), _ptr(out), mode)
+        return out
+
+    def burgers_d2(self, n, nu, dt, amp, w, d, mode=0):
+        w, d = _f64(w), _f64(d)
+        out = np.empty(2 * n * n)
+        self._bd2(n, nu, dt, amp, _ptr(w), _ptr(d), _ptr(out), mode)
+        return out
+
+    def hmg2d_levels(self, n, alpha, nu):
+        return self._hlev(n, alpha, nu)
+
+    def hmg2d_apply(self, n, alpha, nu, r, pre=2, post=2):
+        r = _f64(r)
+        z = np.empty(n * n)
+        self._happly(n, alpha, nu, pre, post, _ptr(r), _ptr(z))
+        return z
+
+    def solve_burgers(self, n, nu, dt, amp, method="nk", precond="mg", params=None, x0=None):
+        p = params if params is not None else default_params()
+        x0 = np.zeros(2 * n * n) if x0 is None else _f64(x0)
+        x = np.empty(2 * n * n)
+        res = KrylovResult()
+        rc = self._bsolve(n, nu, dt, amp, METHODS[method], 1 if precond == "mg" else 0, C.byref(p), _ptr(x0),
+                          _ptr(x), C.byref(res))
+        if rc != 0:
+            raise ValueError(f"Burgers2D solve failed with status {rc}")
         return x, struct_dict(res)
 
     def forcing(self, params, k, rnorm, rprev, eta_prev, res0):

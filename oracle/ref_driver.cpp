@@ -16,6 +16,8 @@
 #include <numa/methods/tf_chebyshev_2018.hpp>
 #include <numa/operators/operator.hpp>
 #include <numa/problems/bratu3d.hpp>
+#include <numa/problems/burgers2d.hpp>
+#include <numa/linalg/helmholtz_mg2d.hpp>
 
 #include "../include/numa_gpu.h"
 
@@ -226,6 +228,92 @@ int ref_solve_bratu3d(size_t n, double lambda, int method, int precond_kind,
 double ref_forcing(const numa_krylov_params* cp, size_t k, double rnorm, double rprev,
                    double eta_prev, double res0) {
     return numa::op::detail::forcing(to_params(cp), k, rnorm, rprev, eta_prev, res0);
+}
+
+// ---- Burgers2D and HelmholtzMG2D (problems/burgers2d.hpp, linalg/helmholtz_mg2d.hpp)
+int ref_burgers2d_exact(size_t n, double nu, double dt, double amp, double* out) {
+    Burgers2D f(n, nu, dt, amp);
+    std::memcpy(out, f.exact().data(), f.size() * sizeof(double));
+    return 0;
+}
+
+int ref_burgers2d_eval(size_t n, double nu, double dt, double amp, const double* w, double* out) {
+    Burgers2D f(n, nu, dt, amp);
+    DVec W(w, w + f.size()), O;
+    f.eval(W, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+    return 0;
+}
+
+int ref_burgers2d_jvp(size_t n, double nu, double dt, double amp, const double* w, const double* d, double* out,
+                      int mode) {
+    Burgers2D f(n, nu, dt, amp);
+    DVec W(w, w + f.size()), D(d, d + f.size()), O;
+    if (mode == 1) jvp_fd(f, W, D, O); else f.jvp(W, D, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+    return 0;
+}
+
+int ref_burgers2d_d2(size_t n, double nu, double dt, double amp, const double* w, const double* d, double* out,
+                     int mode) {
+    Burgers2D f(n, nu, dt, amp);
+    DVec W(w, w + f.size()), D(d, d + f.size()), O;
+    if (mode == 1) d2_fd(f, W, D, O); else f.d2(W, D, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+    return 0;
+}
+
+int ref_hmg2d_levels(size_t n, double alpha, double nu) {
+    HelmholtzMG2D mg(n, alpha, nu);
+    return static_cast<int>(mg.levels());
+}
+
+int ref_hmg2d_apply(size_t n, double alpha, double nu, int pre, int post, const double* r, double* z) {
+    HelmholtzMG2D mg(n, alpha, nu, pre, post);
+    DVec R(r, r + n * n), Z;
+    mg(R, Z);
+    std::memcpy(z, Z.data(), Z.size() * sizeof(double));
+    return 0;
+}
+
+namespace {
+struct FdBurgers {
+    const Burgers2D& f;
+    int jvp_mode, d2_mode;
+    std::size_t size() const { return f.size(); }
+    void eval(const DVec& x, DVec& out) const { f.eval(x, out); }
+    void jvp(const DVec& x, const DVec& v, DVec& out) const {
+        if (jvp_mode == 1) jvp_fd(f, x, v, out); else f.jvp(x, v, out);
+    }
+    void d2(const DVec& x, const DVec& v, DVec& out) const {
+        if (d2_mode == 1) d2_fd(f, x, v, out); else f.d2(x, v, out);
+    }
+};
+}  // namespace
+
+int ref_solve_burgers2d(size_t n, double nu, double dt, double amp, int method, int precond_kind,
+                        const numa_krylov_params* cp, const double* x0, double* x_out, numa_krylov_result* res) {
+    Burgers2D f(n, nu, dt, amp);
+    FdBurgers op{f, cp ? cp->jvp_mode : 0, cp ? cp->d2_mode : 0};
+    const KrylovParams p = to_params(cp);
+    DVec X0(x0, x0 + f.size());
+    KrylovResult r = precond_kind == NUMA_GPU_PRECOND_POISSON_MG ? run(method, op, X0, p, BurgersMGProvider(n, nu, dt))
+                                                                 : run(method, op, X0, p, NoPrecond{});
+    if (x_out) std::memcpy(x_out, r.x.data(), r.x.size() * sizeof(double));
+    if (res) {
+        std::memset(res, 0, sizeof(*res));
+        res->converged = r.converged;
+        res->iters = r.iters;
+        res->n_F = r.n_F;
+        res->n_JVP = r.n_JVP;
+        res->n_D2 = r.n_D2;
+        res->n_lin_iters = r.n_lin_iters;
+        res->n_lin_failures = r.n_lin_failures;
+        res->n_prec = r.n_prec;
+        res->res0 = r.res0;
+        res->res = r.res;
+    }
+    return 0;
 }
 
 }  // extern "C"

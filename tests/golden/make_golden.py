@@ -17,9 +17,10 @@ records what the reference computes:
 * ``reference_vectors.npz`` — operator, V-cycle and GMRES outputs on the reference tests'
   deterministic inputs (make_point, tests/test_operators.cpp:19-23), and the 31^3 lambda=6
   Newton-Krylov solution;
-* ``c1_bratu_jacobi.json`` — the reference's own published calibration rows for Bratu3D with
-  the Jacobi preconditioner (experiments/c1/amendment01/calibration_combined.csv, repetition 1),
-  read from the CSV, not recomputed.
+* ``c1_bratu_jacobi.json`` / ``c1_burgers_mg.json`` — the reference's own published calibration
+  rows for Bratu3D with the Jacobi preconditioner and for Burgers2D with its multigrid provider
+  (experiments/c1/amendment01/calibration_combined.csv, repetition 1), read from the CSV, not
+  recomputed; ``c1_csv_header.txt`` — that file's header line.
 """
 from __future__ import annotations
 
@@ -144,6 +145,34 @@ def main() -> None:
         for rn, rp, ep in ((1.0, 2.0, 0.5), (1e-3, 1e-1, 0.9), (1e-8, 1e-6, 1e-3), (5.0, 5.0, 0.2)):
             forcing.append([k_, rn, rp, ep, 100.0, ref.forcing(p, k_, rn, rp, ep, 100.0)])
     gm["forcing_rtol1e-10_res0_100"] = forcing
+    # Burgers2D and HelmholtzMG2D (tests/test_burgers.cpp): the 15^2 manufactured problem, its
+    # operators on the test's points, V-cycles, and solves from the test's perturbed start.
+    bn, bnu, bdt, bamp = 15, 0.05, 0.1, 1.0
+    exact = ref.burgers_exact(bn, bnu, bdt, bamp)
+    vectors["burgers_n15_exact"] = exact
+    vectors["burgers_n15_eval_exact"] = ref.burgers_eval(bn, bnu, bdt, bamp, exact)
+    bx = 0.5 * np.sin(0.37 * np.arange(2 * bn * bn) + 0.5)
+    bv = 0.7 * np.sin(0.37 * np.arange(2 * bn * bn) + 1.1)
+    vectors["burgers_n15_x"], vectors["burgers_n15_v"] = bx, bv
+    for mode, tag in ((0, ""), (1, "_fd")):
+        vectors[f"burgers_n15_jvp{tag}"] = ref.burgers_jvp(bn, bnu, bdt, bamp, bx, bv, mode)
+        vectors[f"burgers_n15_d2{tag}"] = ref.burgers_d2(bn, bnu, bdt, bamp, bx, bv, mode)
+    gm["hmg2d_levels"] = {str(n): ref.hmg2d_levels(n, 10.0, 0.05) for n in (1, 3, 7, 15, 16, 31, 63)}
+    for n in (15, 31):
+        vectors[f"hmg2d_n{n}_z"] = ref.hmg2d_apply(n, 10.0, 0.05, make_point(n * n, 1.0))
+    burgers_solves = []
+    x0 = ref.burgers_exact(31, 0.05, 0.1, 1.0) + 0.05 * np.sin(1.3 * np.arange(2 * 31 * 31))
+    for method in ("nk", "cheb", "rec", "tf2018"):
+        for precond in ("mg", "none"):
+            x, res = ref.solve_burgers(31, 0.05, 0.1, 1.0, method, precond, default_params(), x0)
+            burgers_solves.append(dict(n=31, nu=0.05, dt=0.1, amp=1.0, method=method, precond=precond,
+                                       start="exact+0.05sin(1.3i)", result={k: res[k] for k in (
+                                           "converged", "iters", "n_F", "n_JVP", "n_D2", "n_lin_iters",
+                                           "n_lin_failures", "n_prec", "res0", "res")},
+                                       solution=solution_stats(x)))
+            if method == "nk" and precond == "mg":
+                vectors["burgers_n31_nk_mg_x"] = x
+    gm["burgers_solves"] = burgers_solves
     (HERE / "reference_small.json").write_text(json.dumps(gm, indent=1))
     np.savez_compressed(HERE / "reference_vectors.npz", **vectors)
 
@@ -159,6 +188,20 @@ def main() -> None:
                 "max_nl", "eta_init", "eta_max", "gamma", "alpha", "eta2_factor", "eta2_max", "restart",
                 "maxlin", "t_total", "threads")})
     (HERE / "c1_bratu_jacobi.json").write_text(json.dumps(rows, indent=0))
+    brows = []
+    with open(CALIBRATION_CSV) as fh:
+        for r in csv.DictReader(fh):
+            if r["problem"] != "burgers" or r["repetition"] != "1":
+                continue
+            kv = dict(item.split("=") for item in r["instance_id"].split(";"))
+            brows.append(dict({k: r[k] for k in (
+                "n", "param", "method", "precond", "internal_candidate_id", "success", "nonlinear_iters", "n_F",
+                "n_JVP", "n_D2", "n_lin", "n_lin_failures", "n_prec", "residual_rel", "rtol", "max_nl", "eta_init",
+                "eta_max", "gamma", "alpha", "eta2_factor", "eta2_max", "restart", "maxlin")},
+                dt=kv["dt"], amp=kv["amp"]))
+    (HERE / "c1_burgers_mg.json").write_text(json.dumps(brows, indent=0))
+    with open(CALIBRATION_CSV) as fh:
+        (HERE / "c1_csv_header.txt").write_text(fh.readline())
     print(len(out_counts), "solves,", len(vectors), "vectors,", len(rows), "calibration rows")
 
 
