@@ -334,10 +334,10 @@ def run_ours(args) -> int:
         peaks = json.loads(PEAKS_FILE.read_text()) if PEAKS_FILE.exists() else {}
         hbm_peak = float(peaks.get("hbm_gbs", FALLBACK_HBM_GBS))
         eb = 8 if mgp == G.FP64 else 4
-        # algorithmic bytes of the dominant kernel.  FP64: one colour pass reads the own-colour
-        # right-hand side (N/2) and the other-colour neighbours (N/2) once and writes the
-        # own-colour values (N/2).  FP32: one fused sweep reads x and b h^2 and writes x (3 N).
-        pass_bytes = 3 * (N / 2) * eb if mgp == G.FP64 else 3 * N * eb
+        # algorithmic bytes of the dominant kernel, one red-black colour pass: the own-colour
+        # right-hand side (N/2) and the other-colour neighbours (N/2) read once, the own-colour
+        # values (N/2) written once
+        pass_bytes = 3 * (N / 2) * eb
         achieved = pass_bytes / (ms_pass * 1e-3) / 1e9
         # FP64 instructions of one pass: per updated point 6 adds + 3 for the division by 6
         # (one multiply, two FMAs); the FP64 pipe issues one such instruction per lane-cycle,
@@ -346,7 +346,7 @@ def run_ours(args) -> int:
         traffic = load_profile_traffic(mgp)
         roofline = {
             "kernel": (f"k_rbgs<double> colour pass, {n}^3" if mgp == G.FP64 else
-                       f"k_rbgs_sweep32 fused red-black sweep, {n}^3"),
+                       f"k_rbgs_split colour pass (FP32, colour-split layout), {n}^3"),
             "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
             "traffic": traffic, "ms_per_launch": ms_pass,
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback",

@@ -24,10 +24,13 @@ INCLUDE = HERE.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
-    *ARCH, "-O3", "-lineinfo", "-std=c++20", "-Xcompiler", "-fPIC", "-fmad=false",
+    *ARCH, "-O3", "-lineinfo", "-std=c++20", "-Xcompiler", "-fPIC,-ffp-contract=off", "-fmad=false",
     "--extended-lambda", "-Xptxas", "-warn-spills", f"-I{INCLUDE}",
 ]
-SOURCES = ["context.cu", "bratu3d.cu", "poisson_mg.cu", "gmres.cu", "drivers.cu", "capi.cu", "diag.cu", "mg_noalloc.cu"]
+SOURCES = [
+    "context.cu", "bratu3d.cu", "ops.cu", "poisson_mg.cu", "hmg2d.cu", "gmres.cu", "drivers.cu", "capi.cu", "diag.cu",
+    "mg_noalloc.cu",
+]
 HEADERS = ["common.cuh", "numa_internal.hpp", "mg_kernels.cuh"]
 
 
@@ -50,7 +53,7 @@ def build_apps(force: bool = False) -> list[Path]:
     for name, src in APPS.items():
         exe = HERE / name
         if force or _mtime(exe) < max(_mtime(src), _mtime(LIB), _mtime(INCLUDE / "numa" / "gpu" / "numa_gpu.hpp")):
-            cmd = [cxx, "-std=c++20", "-O2", f"-I{INCLUDE}", str(src), "-o", str(exe), f"-L{HERE}", "-lnuma_gpu",
+            cmd = [cxx, "-std=c++20", "-O2", "-ffp-contract=off", f"-I{INCLUDE}", str(src), "-o", str(exe), f"-L{HERE}", "-lnuma_gpu",
                    f"-Wl,-rpath,{HERE}"]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:

@@ -193,58 +193,6 @@ __global__ void k_jacobi_diag(const double* __restrict__ c, double* __restrict__
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) d[p] = six_h2inv - c[p];
 }
 
-// ||v|| and the finite-difference step h = scale (1 + ||x||) / ||v|| on the device; a zero
-// direction raises the flag that makes the quotient kernels write zeros (operator.hpp:105-106).
-__global__ void __launch_bounds__(kRedThreads) k_fd_step(const double* __restrict__ v, size_t N, RedArgs red,
-                                                         double scale, double* slots /* h, 1/h, zero, xnorm */) {
-    __shared__ double sm[1][32];
-    double s[1] = {0.0};
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) s[0] = __fma_rn(v[i], v[i], s[0]);
-    block_sum<1>(s, sm);
-    grid_reduce_finish<1>(s, red, [slots, scale] __device__(const double(&t)[1]) {
-        const double nv = __dsqrt_rn(t[0]);
-        if (nv == 0.0) {
-            slots[0] = 0.0;
-            slots[1] = 0.0;
-            slots[2] = 1.0;
-        } else {
-            const double h = __ddiv_rn(scale * (1.0 + slots[3]), nv);
-            slots[0] = h;
-            slots[1] = h * h;
-            slots[2] = 0.0;
-        }
-    });
-}
-
-// xp = x + s h v with h from the device (s = +1 or -1): operator.hpp:109-110, :126-128.
-__global__ void k_fd_shift(const double* __restrict__ x, const double* __restrict__ v, const double* __restrict__ slots,
-                           double sign, double* __restrict__ xp, size_t N) {
-    const double a = sign * slots[0];
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) xp[p] = x[p] + a * v[p];
-}
-
-// out = (f1 - f0) / h  (operator.hpp:113)
-__global__ void k_fd_quot(const double* __restrict__ f1, const double* __restrict__ f0,
-                          const double* __restrict__ slots, double* __restrict__ out, size_t N) {
-    const double h = slots[0];
-    const bool zero = slots[2] != 0.0;
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride)
-        out[p] = zero ? 0.0 : __ddiv_rn(f1[p] - f0[p], h);
-}
-
-// out = (fp - 2 f0 + fm) / (h h)  (operator.hpp:132-133)
-__global__ void k_fd2_quot(const double* __restrict__ fp, const double* __restrict__ f0, const double* __restrict__ fm,
-                           const double* __restrict__ slots, double* __restrict__ out, size_t N) {
-    const double hh = slots[1];
-    const bool zero = slots[2] != 0.0;
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride)
-        out[p] = zero ? 0.0 : __ddiv_rn(fp[p] - 2.0 * f0[p] + fm[p], hh);
-}
-
 unsigned ew_grid(const Context& ctx, size_t N) {
     size_t want = (N + 255) / 256;
     size_t cap = static_cast<size_t>(ctx.sm_count) * 16;
@@ -255,16 +203,25 @@ unsigned ew_grid(const Context& ctx, size_t N) {
 }  // namespace
 
 Bratu3D::Bratu3D(Context& ctx, size_t n, double lambda)
-    : ctx_(ctx), n_(n), N_(n * n * n), lambda_(lambda), h2inv_((n + 1.0) * (n + 1.0)) {
+    : NonlinearOp(ctx), n_(n), N_(n * n * n), lambda_(lambda), h2inv_((n + 1.0) * (n + 1.0)) {
     if (n == 0) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Bratu3D needs n > 0");
     if (n > 65535 * 8) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "grid too large");
 }
 
 Bratu3D::~Bratu3D() = default;
 
-SolverWorkspace& Bratu3D::workspace() {
-    if (!ws_) ws_ = std::make_unique<SolverWorkspace>(ctx_, N_);
-    return *ws_;
+void Bratu3D::bind(const double*, const double* cache, int precision) {
+    bound_c_ = cache;
+    bound_precision_ = precision;
+    if (precision == NUMA_GPU_FP32) {
+        c32_.resize(N_);
+        coef32(cache, c32_.p);
+    }
+}
+
+void Bratu3D::jvp_bound(const double* v, double* out) {
+    if (bound_precision_ == NUMA_GPU_FP32) jvp_c32(c32_.p, v, out);
+    else jvp_c(bound_c_, v, out);
 }
 
 void Bratu3D::eval(const double* x, double* out, double* c_out, double* norm_out) {
@@ -327,45 +284,6 @@ void Bratu3D::jacobi_diag_c(const double* c, double* d) {
     k_jacobi_diag<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(c, d, N_, 6.0 * h2inv_);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d jacobi_diag");
-}
-
-void Bratu3D::jvp_fd(const double* x, const double* f0, const double* xnorm_dev, const double* v, double* out) {
-    // h = sqrt(eps) (1 + ||x||) / ||v||; sqrt(eps) = 2^-26 exactly.
-    double* slots = ctx_.scalar(kSlotFdH);
-    dev_copy(ctx_, xnorm_dev, slots + 3, 1);
-    const double scale = std::sqrt(std::numeric_limits<double>::epsilon());
-    k_fd_step<<<ctx_.red_grid(N_), kRedThreads, 0, ctx_.stream>>>(v, N_, ctx_.red, scale, slots);
-    ctx_.count_launch();
-    s1_.resize(N_);
-    s2_.resize(N_);
-    k_fd_shift<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(x, v, slots, 1.0, s1_.p, N_);
-    ctx_.count_launch();
-    eval(s1_.p, s2_.p);
-    k_fd_quot<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(s2_.p, f0, slots, out, N_);
-    ctx_.count_launch();
-    ctx_.check_launch("jvp_fd");
-}
-
-void Bratu3D::d2_fd(const double* x, const double* f0, const double* xnorm_dev, const double* v, double* out) {
-    // h = eps^(1/4) (1 + ||x||) / ||v||; eps^(1/4) = 2^-13 exactly.
-    double* slots = ctx_.scalar(kSlotFdH);
-    dev_copy(ctx_, xnorm_dev, slots + 3, 1);
-    const double scale = std::pow(std::numeric_limits<double>::epsilon(), 0.25);
-    k_fd_step<<<ctx_.red_grid(N_), kRedThreads, 0, ctx_.stream>>>(v, N_, ctx_.red, scale, slots);
-    ctx_.count_launch();
-    s1_.resize(N_);
-    s2_.resize(N_);
-    s3_.resize(N_);
-    // fp into s2, fm into s3 (s1 holds the shifted point in turn)
-    k_fd_shift<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(x, v, slots, 1.0, s1_.p, N_);
-    ctx_.count_launch();
-    eval(s1_.p, s2_.p);
-    k_fd_shift<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(x, v, slots, -1.0, s1_.p, N_);
-    ctx_.count_launch();
-    eval(s1_.p, s3_.p);
-    k_fd2_quot<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(s2_.p, f0, s3_.p, slots, out, N_);
-    ctx_.count_launch();
-    ctx_.check_launch("d2_fd");
 }
 
 }  // namespace numa::gpu

@@ -30,6 +30,14 @@ struct numa_gpu_krylov_space {
     numa_gpu_ctx* ctx;
     KrylovSpace impl;
 };
+struct numa_gpu_burgers2d {
+    numa_gpu_ctx* ctx;
+    std::unique_ptr<Burgers2D> impl;
+};
+struct numa_gpu_hmg2d {
+    numa_gpu_ctx* ctx;
+    std::unique_ptr<HelmholtzMG2D> impl;
+};
 
 namespace {
 
@@ -44,6 +52,13 @@ struct CtxExtras {
     size_t host_n = 0;
     double host_lambda = 0.0;
     int host_kind = -1, host_prec = -1;
+    // numa_gpu_solve_burgers2d_host likewise
+    std::unique_ptr<Burgers2D> bh_op;
+    std::unique_ptr<Provider> bh_pc;
+    DeviceArray<double> bh_x;
+    size_t bh_n = 0;
+    double bh_nu = 0.0, bh_dt = 0.0, bh_amp = 0.0;
+    int bh_kind = -1;
 };
 
 struct CtxHandle : numa_gpu_ctx {
@@ -130,6 +145,56 @@ struct ProviderPrec : Precond {
     Provider* p;
     void apply(const double* r, double* z) override { p->apply(r, z); }
 };
+
+// Checks a driver's vector and provider against an operator of size N.
+void check_driver_args(numa_gpu_ctx* ctx, const numa_gpu_vec* x, size_t N, const numa_gpu_provider* provider) {
+    same_ctx(ctx, x);
+    sized(x, N);
+    if (provider) {
+        need(provider->ctx == ctx, NUMA_GPU_ERR_INVALID_ARGUMENT, "provider belongs to another context");
+        need(provider->N == 0 || provider->N == N, NUMA_GPU_ERR_SIZE_MISMATCH, "provider size differs");
+    }
+}
+
+// method of numa_gpu_method on any operator (the reference's templated drivers).
+void dispatch_driver(int method, NonlinearOp& f, double* x, const numa_krylov_params* p, Provider* pc,
+                     numa_krylov_result& out) {
+    need(method >= NUMA_GPU_METHOD_NK && method <= NUMA_GPU_METHOD_TF2018, NUMA_GPU_ERR_INVALID_ARGUMENT,
+         "unknown method");
+    KrylovParams kp = params_from_c(p);
+    if (method == NUMA_GPU_METHOD_NK) newton_krylov(f, x, kp, pc, out);
+    else if (method == NUMA_GPU_METHOD_TF2018) tf_chebyshev_2018(f, x, kp, pc, out);
+    else {
+        if (method == NUMA_GPU_METHOD_CHEB_REC) kp.recycle = true;
+        chebyshev_inexact(f, x, kp, pc, out);
+    }
+}
+
+// out = F'(x) v or F''(x)[v, v] of any operator, analytic or by finite differences, for the
+// per-operator entry points (temporaries are freed on return, hence the synchronisation).
+void op_derivative(NonlinearOp& f, bool second, const double* x, const double* v, double* out, int mode) {
+    Context& c = f.ctx();
+    const size_t N = f.size();
+    if (mode == NUMA_GPU_DERIV_FD) {
+        DeviceArray<double> f0(N);
+        f.eval(x, f0.p, nullptr, nullptr);
+        dev_norm2(c, x, N, c.scalar(kSlotTmp1));
+        if (second) f.d2_fd(x, f0.p, c.scalar(kSlotTmp1), v, out);
+        else f.jvp_fd(x, f0.p, c.scalar(kSlotTmp1), v, out);
+        c.sync();
+        return;
+    }
+    need(mode == NUMA_GPU_DERIV_ANALYTIC, NUMA_GPU_ERR_INVALID_ARGUMENT, "unknown derivative mode");
+    if (!second) {
+        f.jvp_at(x, v, out);
+        return;
+    }
+    DeviceArray<double> cache(f.cache_size());
+    DeviceArray<double> tmp(f.cache_size() ? N : 0);
+    if (f.cache_size()) f.eval(x, tmp.p, cache.p, nullptr);
+    f.d2(x, cache.p, v, out);
+    c.sync();
+}
 
 void fill_gmres(const GmresResult& g, numa_gmres_result* out) {
     if (!out) return;
@@ -821,6 +886,183 @@ int numa_gpu_solve_bratu3d_host(numa_gpu_ctx* ctx, size_t n, double lambda, int 
             chebyshev_inexact(*e.host_op, e.host_x.p, kp, pc, *result);
         }
         NUMA_CUDA(cudaMemcpyAsync(x_out, e.host_x.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        c.sync();
+    });
+    result->status = rc;
+    return rc;
+}
+
+// ------------------------------------------------------------------------------ Burgers2D
+int numa_gpu_burgers2d_create(numa_gpu_ctx* ctx, size_t n, double nu, double dt, double amplitude,
+                              numa_gpu_burgers2d** out) {
+    if (!ctx || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        auto h = std::make_unique<numa_gpu_burgers2d>();
+        h->ctx = ctx;
+        h->impl = std::make_unique<Burgers2D>(*ctx->impl, n, nu, dt, amplitude);
+        *out = h.release();
+    });
+}
+
+int numa_gpu_burgers2d_destroy(numa_gpu_burgers2d* op) {
+    if (op) {
+        cudaStreamSynchronize(op->ctx->impl->stream);
+        delete op;
+    }
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_burgers2d_size(const numa_gpu_burgers2d* op, size_t* N) {
+    if (!op || !N) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *N = op->impl->size();
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_burgers2d_cell_reynolds(const numa_gpu_burgers2d* op, double* out) {
+    if (!op || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = op->impl->cell_reynolds();
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_burgers2d_exact(numa_gpu_burgers2d* op, numa_gpu_vec* out) {
+    if (!op) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(op->ctx, [&] {
+        same_ctx(op->ctx, out);
+        sized(out, op->impl->size());
+        dev_copy(*op->ctx->impl, op->impl->exact(), out->d, op->impl->size());
+    });
+}
+
+int numa_gpu_burgers2d_eval(numa_gpu_burgers2d* op, const numa_gpu_vec* w, numa_gpu_vec* out) {
+    if (!op) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(op->ctx, [&] {
+        same_ctx(op->ctx, w);
+        same_ctx(op->ctx, out);
+        sized(w, op->impl->size());
+        sized(out, op->impl->size());
+        need(w->d != out->d, NUMA_GPU_ERR_INVALID_ARGUMENT, "eval input and output must differ");
+        op->impl->eval(w->d, out->d, nullptr, nullptr);
+    });
+}
+
+static int burgers_derivative(numa_gpu_burgers2d* op, bool second, const numa_gpu_vec* w, const numa_gpu_vec* d,
+                              numa_gpu_vec* out, int mode) {
+    if (!op) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(op->ctx, [&] {
+        for (const numa_gpu_vec* q : {w, d, (const numa_gpu_vec*)out}) {
+            same_ctx(op->ctx, q);
+            sized(q, op->impl->size());
+        }
+        need(out->d != w->d && out->d != d->d, NUMA_GPU_ERR_INVALID_ARGUMENT, "output must not alias an input");
+        op_derivative(*op->impl, second, w->d, d->d, out->d, mode);
+    });
+}
+
+int numa_gpu_burgers2d_jvp(numa_gpu_burgers2d* op, const numa_gpu_vec* w, const numa_gpu_vec* d, numa_gpu_vec* out,
+                           int mode) {
+    return burgers_derivative(op, false, w, d, out, mode);
+}
+
+int numa_gpu_burgers2d_d2(numa_gpu_burgers2d* op, const numa_gpu_vec* w, const numa_gpu_vec* d, numa_gpu_vec* out,
+                          int mode) {
+    return burgers_derivative(op, true, w, d, out, mode);
+}
+
+int numa_gpu_burgers2d_solve(numa_gpu_burgers2d* op, int method, numa_gpu_vec* x, const numa_krylov_params* p,
+                             numa_gpu_provider* provider, numa_krylov_result* result) {
+    if (!op || !x || !result) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    std::memset(result, 0, sizeof(*result));
+    const int rc = guard(op->ctx, [&] {
+        check_driver_args(op->ctx, x, op->impl->size(), provider);
+        dispatch_driver(method, *op->impl, x->d, p, provider ? provider->impl.get() : nullptr, *result);
+    });
+    result->status = rc;
+    return rc;
+}
+
+// ------------------------------------------------------------------------------ HelmholtzMG2D
+int numa_gpu_hmg2d_create(numa_gpu_ctx* ctx, size_t n, double alpha, double nu, int pre, int post,
+                          numa_gpu_hmg2d** out) {
+    if (!ctx || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        auto h = std::make_unique<numa_gpu_hmg2d>();
+        h->ctx = ctx;
+        h->impl = std::make_unique<HelmholtzMG2D>(*ctx->impl, n, alpha, nu, pre, post);
+        *out = h.release();
+    });
+}
+
+int numa_gpu_hmg2d_destroy(numa_gpu_hmg2d* mg) {
+    if (mg) {
+        cudaStreamSynchronize(mg->ctx->impl->stream);
+        delete mg;
+    }
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_hmg2d_levels(const numa_gpu_hmg2d* mg, size_t* levels) {
+    if (!mg || !levels) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *levels = mg->impl->levels();
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_hmg2d_apply(numa_gpu_hmg2d* mg, const numa_gpu_vec* r, numa_gpu_vec* z) {
+    if (!mg) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(mg->ctx, [&] {
+        same_ctx(mg->ctx, r);
+        same_ctx(mg->ctx, z);
+        sized(r, mg->impl->size());
+        sized(z, mg->impl->size());
+        mg->impl->apply(r->d, z->d);
+    });
+}
+
+int numa_gpu_provider_create_burgers_mg(numa_gpu_ctx* ctx, size_t n, double nu, double dt,
+                                        numa_gpu_provider** out) {
+    if (!ctx || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        need(n > 0, NUMA_GPU_ERR_INVALID_ARGUMENT, "BurgersMGProvider needs n > 0");
+        need(nu > 0.0 && dt > 0.0, NUMA_GPU_ERR_INVALID_ARGUMENT, "BurgersMGProvider needs nu > 0 and dt > 0");
+        auto h = std::make_unique<numa_gpu_provider>();
+        h->ctx = ctx;
+        h->impl = make_burgers_mg_provider(*ctx->impl, n, nu, dt, 2, 2);
+        h->N = 2 * n * n;
+        *out = h.release();
+    });
+}
+
+int numa_gpu_solve_burgers2d_host(numa_gpu_ctx* ctx, size_t n, double nu, double dt, double amplitude, int method,
+                                  int precond_kind, const numa_krylov_params* p, const double* x0, double* x_out,
+                                  numa_krylov_result* result) {
+    if (!ctx || !x0 || !x_out || !result) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    std::memset(result, 0, sizeof(*result));
+    const int rc = guard(ctx, [&] {
+        need(precond_kind == NUMA_GPU_PRECOND_NONE || precond_kind == NUMA_GPU_PRECOND_BURGERS_MG,
+             NUMA_GPU_ERR_INVALID_ARGUMENT, "Burgers2D takes the preconditioner NONE or BURGERS_MG");
+        Context& c = *ctx->impl;
+        CtxExtras& e = extras(ctx);
+        if (!e.bh_op || e.bh_n != n || e.bh_nu != nu || e.bh_dt != dt || e.bh_amp != amplitude) {
+            e.bh_pc.reset();
+            e.bh_op = std::make_unique<Burgers2D>(c, n, nu, dt, amplitude);
+            e.bh_n = n;
+            e.bh_nu = nu;
+            e.bh_dt = dt;
+            e.bh_amp = amplitude;
+            e.bh_kind = -1;
+        }
+        const size_t N = e.bh_op->size();
+        if (e.bh_kind != precond_kind || !e.bh_pc) {
+            if (precond_kind == NUMA_GPU_PRECOND_BURGERS_MG) e.bh_pc = make_burgers_mg_provider(c, n, nu, dt, 2, 2);
+            else e.bh_pc = make_identity_provider(c, N);
+            e.bh_kind = precond_kind;
+        }
+        e.bh_x.resize(N);
+        NUMA_CUDA(cudaMemcpyAsync(e.bh_x.p, x0, N * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        dispatch_driver(method, *e.bh_op, e.bh_x.p, p, e.bh_pc.get(), *result);
+        NUMA_CUDA(cudaMemcpyAsync(x_out, e.bh_x.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
         c.sync();
     });
     result->status = rc;

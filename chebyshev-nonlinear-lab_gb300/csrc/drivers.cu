@@ -4,9 +4,10 @@
 //
 // The control flow, counters, forcing terms, line searches and acceptance tests are the
 // reference's, statement for statement; only the vector work runs as kernels, and each scalar
-// the host decides on (a norm) is read back once.  The Jacobian coefficient c = lambda e^x is
-// produced by the residual evaluation of x itself and reused by every Jacobian product,
-// F''(x)[z,z] and the Jacobi diagonal at that iterate.
+// the host decides on (a norm) is read back once.  The drivers run on any NonlinearOp
+// (Bratu3D, Burgers2D).  An operator's per-iterate cache (for Bratu3D the coefficient
+// c = lambda e^x) is produced by the residual evaluation of x itself and reused by every
+// Jacobian product, F''(x)[z,z] and the Jacobi diagonal at that iterate.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -142,32 +143,28 @@ private:
 };
 
 // ------------------------------------------------------------------------------ Jacobian operator
-// apply(v, out) = F'(x) v at the bound iterate x (krylov_newton.hpp:86): analytic with the
-// cached coefficient, in FP32 arithmetic (precision extension), or finite differences.
+// apply(v, out) = F'(x) v at the bound iterate x (krylov_newton.hpp:86): the operator's analytic
+// product bound at x (FP64, or FP32 arithmetic where the operator offers it), or finite
+// differences.
 class JacobianOp : public LinearOp {
 public:
-    JacobianOp(Bratu3D& f, Timers& t, int mode, int precision)
-        : f_(f), t_(t), mode_(mode), precision_(precision) {}
-    void bind(const double* x, const double* fx, const double* c, const float* c32, const double* xnorm) {
+    JacobianOp(NonlinearOp& f, Timers& t, int mode) : f_(f), t_(t), mode_(mode) {}
+    void bind(const double* x, const double* fx, const double* xnorm) {
         x_ = x;
         fx_ = fx;
-        c_ = c;
-        c32_ = c32;
         xnorm_ = xnorm;
     }
     void apply(const double* v, double* out) override {
         Timers::Scope s(&t_, kT_JVP);
         if (mode_ == NUMA_GPU_DERIV_FD) f_.jvp_fd(x_, fx_, xnorm_, v, out);
-        else if (precision_ == NUMA_GPU_FP32) f_.jvp_c32(c32_, v, out);
-        else f_.jvp_c(c_, v, out);
+        else f_.jvp_bound(v, out);
     }
 
 private:
-    Bratu3D& f_;
+    NonlinearOp& f_;
     Timers& t_;
-    int mode_, precision_;
-    const double *x_ = nullptr, *fx_ = nullptr, *c_ = nullptr, *xnorm_ = nullptr;
-    const float* c32_ = nullptr;
+    int mode_;
+    const double *x_ = nullptr, *fx_ = nullptr, *xnorm_ = nullptr;
 };
 
 class TimedPrecond : public Precond {
@@ -197,38 +194,40 @@ unsigned ew_grid(const Context& ctx, size_t N) {
     return static_cast<unsigned>(want < 1 ? 1 : want);
 }
 
-// Shared state of a nonlinear solve: the iterate, its residual and Jacobian coefficient, and
-// the trial point, swapped by pointer on acceptance (x = xn; Fx = Fn).
+// Shared state of a nonlinear solve: the iterate, its residual and operator cache, and the
+// trial point, swapped by pointer on acceptance (x = xn; Fx = Fn).
 struct SolveState {
-    Bratu3D& f;
+    NonlinearOp& f;
     Context& ctx;
     const KrylovParams& p;
     size_t N;
     double* user_x;
     SolverWorkspace& W;
     DeviceArray<double>&xb, &Fa, &Fb, &ca, &cb, &z, &u, &w, &scratch, &xnorm;
-    DeviceArray<float>& c32;
     Gmres& gmres;
     double *x, *xn, *Fx, *Fn, *cx, *cn;
     Timers timers;
 
-    SolveState(Bratu3D& f_, const KrylovParams& p_, double* x0)
+    SolveState(NonlinearOp& f_, const KrylovParams& p_, double* x0)
         : f(f_), ctx(f_.ctx()), p(p_), N(f_.size()), user_x(x0), W(f_.workspace()), xb(W.xb), Fa(W.Fa), Fb(W.Fb),
-          ca(W.ca), cb(W.cb), z(W.z), u(W.u), w(W.w), scratch(W.scratch), xnorm(W.xnorm), c32(W.c32),
-          gmres(W.gmres), timers(f_.ctx()) {
+          ca(W.ca), cb(W.cb), z(W.z), u(W.u), w(W.w), scratch(W.scratch), xnorm(W.xnorm), gmres(W.gmres),
+          timers(f_.ctx()) {
         xb.resize(N);
         Fa.resize(N);
         Fb.resize(N);
-        ca.resize(N);
-        cb.resize(N);
+        const size_t nc = f.cache_size();
+        if (nc) {
+            ca.resize(nc);
+            cb.resize(nc);
+        }
         z.resize(N);
         xnorm.resize(1);
         x = user_x;
         xn = xb.p;
         Fx = Fa.p;
         Fn = Fb.p;
-        cx = ca.p;
-        cn = cb.p;
+        cx = nc ? ca.p : nullptr;
+        cn = nc ? cb.p : nullptr;
     }
     // F(xn) with its coefficient and norm; returns ||F(xn)||.
     double eval_trial() {
@@ -246,14 +245,9 @@ struct SolveState {
     // Binds the Jacobian operator and the provider at the current iterate (make(x) timed as
     // dynamic setup, timing.hpp:98-103).
     void bind(JacobianOp& J, Provider* pc) {
-        const float* c32p = nullptr;
-        if (p.jvp_precision == NUMA_GPU_FP32 && p.jvp_mode == NUMA_GPU_DERIV_ANALYTIC) {
-            c32.resize(N);
-            f.coef32(cx, c32.p);
-            c32p = c32.p;
-        }
+        if (p.jvp_mode == NUMA_GPU_DERIV_ANALYTIC) f.bind(x, cx, p.jvp_precision);
         if (p.jvp_mode == NUMA_GPU_DERIV_FD || p.d2_mode == NUMA_GPU_DERIV_FD) dev_norm2(ctx, x, N, xnorm.p);
-        J.bind(x, Fx, cx, c32p, xnorm.p);
+        J.bind(x, Fx, xnorm.p);
         if (pc) {
             Timers::Scope s(&timers, kT_SETUP);
             pc->make(x, cx);
@@ -333,11 +327,11 @@ double forcing(const KrylovParams& p, size_t k, double rnorm, double rprev, doub
 
 // ------------------------------------------------------------------------------ newton_krylov
 // krylov_newton.hpp:69-114
-void newton_krylov(Bratu3D& f, double* x0, const KrylovParams& p, Provider* pc, numa_krylov_result& out) {
+void newton_krylov(NonlinearOp& f, double* x0, const KrylovParams& p, Provider* pc, numa_krylov_result& out) {
     const auto t0 = std::chrono::steady_clock::now();
     std::memset(&out, 0, sizeof(out));
     SolveState S(f, p, x0);
-    JacobianOp J(f, S.timers, p.jvp_mode, p.jvp_precision);
+    JacobianOp J(f, S.timers, p.jvp_mode);
     TimedPrecond M(pc, S.timers);
     Precond* Mp = pc ? &M : nullptr;
     const size_t N = S.N;
@@ -387,11 +381,11 @@ void newton_krylov(Bratu3D& f, double* x0, const KrylovParams& p, Provider* pc, 
 
 // ------------------------------------------------------------------------------ chebyshev_inexact
 // krylov_newton.hpp:116-189
-void chebyshev_inexact(Bratu3D& f, double* x0, const KrylovParams& p, Provider* pc, numa_krylov_result& out) {
+void chebyshev_inexact(NonlinearOp& f, double* x0, const KrylovParams& p, Provider* pc, numa_krylov_result& out) {
     const auto t0 = std::chrono::steady_clock::now();
     std::memset(&out, 0, sizeof(out));
     SolveState S(f, p, x0);
-    JacobianOp J(f, S.timers, p.jvp_mode, p.jvp_precision);
+    JacobianOp J(f, S.timers, p.jvp_mode);
     TimedPrecond M(pc, S.timers);
     Precond* Mp = pc ? &M : nullptr;
     const size_t N = S.N;
@@ -421,7 +415,7 @@ void chebyshev_inexact(Bratu3D& f, double* x0, const KrylovParams& p, Provider* 
         {
             Timers::Scope s(&S.timers, kT_D2);
             if (p.d2_mode == NUMA_GPU_DERIV_FD) f.d2_fd(S.x, S.Fx, S.xnorm.p, S.z.p, S.w.p);
-            else f.d2_c(S.cx, S.z.p, S.w.p);
+            else f.d2(S.x, S.cx, S.z.p, S.w.p);
         }
         ++out.n_D2;
         const GmresResult g2 = p.recycle ? S.gmres.solve_recycled(J, Mp, S.w.p, S.u.p, gmres_opts(p, eta2), space)
@@ -468,11 +462,11 @@ void chebyshev_inexact(Bratu3D& f, double* x0, const KrylovParams& p, Provider* 
 
 // ------------------------------------------------------------------------------ tf_chebyshev_2018
 // methods/tf_chebyshev_2018.hpp:52-132
-void tf_chebyshev_2018(Bratu3D& f, double* x0, const KrylovParams& p, Provider* pc, numa_krylov_result& out) {
+void tf_chebyshev_2018(NonlinearOp& f, double* x0, const KrylovParams& p, Provider* pc, numa_krylov_result& out) {
     const auto t0 = std::chrono::steady_clock::now();
     std::memset(&out, 0, sizeof(out));
     SolveState S(f, p, x0);
-    JacobianOp J(f, S.timers, p.jvp_mode, p.jvp_precision);
+    JacobianOp J(f, S.timers, p.jvp_mode);
     TimedPrecond M(pc, S.timers);
     Precond* Mp = pc ? &M : nullptr;
     Context& ctx = S.ctx;
@@ -520,12 +514,14 @@ void tf_chebyshev_2018(Bratu3D& f, double* x0, const KrylovParams& p, Provider* 
             Timers::Scope s(&S.timers, kT_JVP);
             if (p.jvp_mode == NUMA_GPU_DERIV_FD) {
                 f.jvp_fd(S.x, S.Fx, S.xnorm.p, d1, j0);
-                f.eval(S.xn, S.Fn);  // F(xh), recomputed inside jvp_fd by the reference
+                f.eval(S.xn, S.Fn, nullptr, nullptr);  // F(xh), recomputed inside jvp_fd by the reference
                 dev_norm2(ctx, S.xn, N, sl + 2);
                 f.jvp_fd(S.xn, S.Fn, sl + 2, d1, j1);
             } else {
-                f.jvp_c(S.cx, d1, j0);
-                f.jvp_x(S.xn, d1, j1);
+                // FP64 products whatever the Krylov product's precision: the curvature is a
+                // difference quotient at h ~ sqrt(eps)
+                f.jvp_cached(S.x, S.cx, d1, j0);
+                f.jvp_at(S.xn, d1, j1);
             }
         }
         out.n_JVP += 2;

@@ -6,6 +6,7 @@
 // capi.cu wraps them.
 #pragma once
 
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <memory>
@@ -29,25 +30,77 @@ void dev_cheb_step(Context& ctx, const double* x, const double* z, const double*
 // y = -y (tf_chebyshev_2018.hpp:95-96) and y = -0.5 y (:100-102)
 void dev_scale_inplace(Context& ctx, double* y, double a, size_t N);
 
-// ------------------------------------------------------------------------------ Bratu3D
+// ------------------------------------------------------------------------------ operators
 struct SolverWorkspace;
 
-class Bratu3D {
+// A nonlinear operator on the device: the GPU form of the reference's NonlinearOperator /
+// SecondOrderOperator concepts (operators/operator.hpp:43-58), which the drivers run on.
+class NonlinearOp {
 public:
-    Bratu3D(Context& ctx, size_t n, double lambda);
-    ~Bratu3D();
+    explicit NonlinearOp(Context& ctx) : ctx_(ctx) {}
+    virtual ~NonlinearOp();
+    Context& ctx() { return ctx_; }
+    virtual size_t size() const = 0;
+    // Doubles of data an iterate keeps for the Jacobian at it (0: none).
+    virtual size_t cache_size() const = 0;
+    // out = F(x); cache := the Jacobian data at x (when cache_size() > 0); norm_out := ||F(x)||
+    // as a device scalar (optional).
+    virtual void eval(const double* x, double* out, double* cache, double* norm_out) = 0;
+    // Binds J(x) for jvp_bound: the iterate, its cache, and the precision of the product
+    // (NUMA_GPU_FP32 where the operator has a mixed-precision product, else FP64).
+    virtual void bind(const double* x, const double* cache, int precision) = 0;
+    virtual void jvp_bound(const double* v, double* out) = 0;
+    // out = F'(x) v at an arbitrary point (no cache).
+    virtual void jvp_at(const double* x, const double* v, double* out) = 0;
+    // out = F'(x) v in FP64 at an iterate with its cache (the cache lets an operator skip work).
+    virtual void jvp_cached(const double* x, const double* cache, const double* v, double* out) {
+        (void)cache;
+        jvp_at(x, v, out);
+    }
+    // out = F''(x)[v, v] at an iterate with its cache.
+    virtual void d2(const double* x, const double* cache, const double* v, double* out) = 0;
+
+    // Finite-difference forms of operators/operator.hpp:101-134 over eval.  f0 = F(x) must be
+    // supplied (the same vector the reference recomputes inside the call); xnorm = ||x|| as a
+    // device scalar.
+    void jvp_fd(const double* x, const double* f0, const double* xnorm_dev, const double* v, double* out);
+    void d2_fd(const double* x, const double* f0, const double* xnorm_dev, const double* v, double* out);
+
     // Device work arrays of the nonlinear drivers for this operator, kept between solves so
     // that a solve allocates nothing after the first (created on first use).
     SolverWorkspace& workspace();
-    size_t size() const { return N_; }
+
+protected:
+    Context& ctx_;
+
+private:
+    DeviceArray<double> fd1_, fd2_, fd3_;  // finite-difference scratch
+    std::unique_ptr<SolverWorkspace> ws_;
+};
+
+// ------------------------------------------------------------------------------ Bratu3D
+class Bratu3D : public NonlinearOp {
+public:
+    Bratu3D(Context& ctx, size_t n, double lambda);
+    ~Bratu3D() override;
+    size_t size() const override { return N_; }
     size_t grid() const { return n_; }
     double lambda() const { return lambda_; }
     double h2inv() const { return h2inv_; }
-    Context& ctx() { return ctx_; }
 
-    // out = F(x).  Optional: c_out = lambda e^x (the Jacobian coefficient at x) and
-    // norm_out = ||F(x)|| (device scalar).  bratu3d.hpp:21-31
-    void eval(const double* x, double* out, double* c_out = nullptr, double* norm_out = nullptr);
+    // NonlinearOp: the cache of an iterate x is c = lambda e^x.
+    size_t cache_size() const override { return N_; }
+    void eval(const double* x, double* out, double* cache, double* norm_out) override;
+    void bind(const double* x, const double* cache, int precision) override;
+    void jvp_bound(const double* v, double* out) override;
+    void jvp_at(const double* x, const double* v, double* out) override { jvp_x(x, v, out); }
+    void jvp_cached(const double*, const double* cache, const double* v, double* out) override {
+        jvp_c(cache, v, out);
+    }
+    void d2(const double* x, const double* cache, const double* v, double* out) override { d2_c(cache, v, out); }
+
+    // out = F(x) (bratu3d.hpp:21-31)
+    void eval(const double* x, double* out) { eval(x, out, nullptr, nullptr); }
     // c = lambda e^x
     void coef(const double* x, double* c);
     // out = F'(x) v with the coefficient c = lambda e^x already formed (bratu3d.hpp:33-43).
@@ -62,18 +115,39 @@ public:
     // d = 6 h^-2 - c (bratu3d.hpp:59-69).
     void jacobi_diag_c(const double* c, double* d);
 
-    // Finite-difference forms of operators/operator.hpp:101-134.  f0 = F(x) must be supplied
-    // (it is the same vector the reference recomputes inside the call); xnorm = ||x|| as a
-    // device scalar.  Scratch vectors come from the object.
-    void jvp_fd(const double* x, const double* f0, const double* xnorm_dev, const double* v, double* out);
-    void d2_fd(const double* x, const double* f0, const double* xnorm_dev, const double* v, double* out);
-
 private:
-    Context& ctx_;
     size_t n_, N_;
     double lambda_, h2inv_;
-    DeviceArray<double> s1_, s2_, s3_;  // FD scratch
-    std::unique_ptr<SolverWorkspace> ws_;
+    const double* bound_c_ = nullptr;
+    int bound_precision_ = NUMA_GPU_FP64;
+    DeviceArray<float> c32_;
+};
+
+// ------------------------------------------------------------------------------ Burgers2D
+// One implicit-Euler step of 2D viscous Burgers with a manufactured root
+// (problems/burgers2d.hpp:23-218): w = (u, v), 2 n^2 unknowns.
+class Burgers2D : public NonlinearOp {
+public:
+    Burgers2D(Context& ctx, size_t n, double nu, double dt, double amplitude);
+    size_t size() const override { return 2 * n_ * n_; }
+    size_t grid() const { return n_; }
+    double nu() const { return nu_; }
+    double dt() const { return dt_; }
+    const double* exact() const { return exact_.p; }
+    double cell_reynolds() const { return std::abs(amp_) / (nu_ * (static_cast<double>(n_) + 1.0)); }
+    size_t cache_size() const override { return 0; }
+    void eval(const double* x, double* out, double* cache, double* norm_out) override;
+    void bind(const double* x, const double*, int) override { bound_x_ = x; }
+    void jvp_bound(const double* v, double* out) override { jvp_at(bound_x_, v, out); }
+    void jvp_at(const double* x, const double* v, double* out) override;
+    void d2(const double* x, const double* cache, const double* v, double* out) override;
+
+private:
+    size_t n_;
+    double nu_, dt_, amp_;
+    double inv2h_, invh2_, invdt_;
+    DeviceArray<double> source_, exact_;
+    const double* bound_x_ = nullptr;
 };
 
 // ------------------------------------------------------------------------------ PoissonMG
@@ -113,13 +187,38 @@ private:
     DeviceArray<double> alias_b_;     // copy of r when r and z alias
 };
 
+// ------------------------------------------------------------------------------ HelmholtzMG2D
+// 2D V-cycle for alpha I - nu Lap_h (linalg/helmholtz_mg2d.hpp:13-158), FP64, bit-exact.
+class HelmholtzMG2D {
+public:
+    HelmholtzMG2D(Context& ctx, size_t n, double alpha, double nu, int pre, int post);
+    ~HelmholtzMG2D();
+    size_t levels() const { return levels_.size(); }
+    size_t size() const { return N0_; }
+    // z = V-cycle(r), n^2 FP64 device vectors (helmholtz_mg2d.hpp:36-42).
+    void apply(const double* r, double* z);
+    struct Level;
+
+private:
+    void cycle(size_t l);
+    Context& ctx_;
+    size_t N0_;
+    double alpha_;
+    int pre_, post_;
+    std::vector<std::unique_ptr<Level>> levels_;
+    DeviceArray<double> resid_, alias_;
+    double* x0_ = nullptr;
+    const double* b0_ = nullptr;
+};
+
 // ------------------------------------------------------------------------------ providers
 // Provider::make(x) -> Bound; Bound(r, z) (krylov_newton.hpp:20-22).
 class Provider {
 public:
     virtual ~Provider() = default;
-    // Binds at the nonlinear iterate x; c = lambda e^x when the caller has it (may be null).
-    virtual void make(const double* x, const double* c) = 0;
+    // Binds at the nonlinear iterate x; cache = the operator's Jacobian data at x (for Bratu3D
+    // c = lambda e^x) when the caller has it (may be null).
+    virtual void make(const double* x, const double* cache) = 0;
     virtual void apply(const double* r, double* z) = 0;
     virtual int kind() const = 0;
 };
@@ -128,6 +227,9 @@ std::unique_ptr<Provider> make_identity_provider(Context& ctx, size_t N);
 std::unique_ptr<Provider> make_mg_provider(Context& ctx, size_t n, int pre, int post, int precision,
                                            int max_levels);
 std::unique_ptr<Provider> make_jacobi_provider(Bratu3D& op);
+// BurgersMGProvider (problems/burgers2d.hpp:220-246): the HelmholtzMG2D V-cycle of
+// (1/dt) I - nu Lap_h applied to each component.
+std::unique_ptr<Provider> make_burgers_mg_provider(Context& ctx, size_t n, double nu, double dt, int pre, int post);
 
 // ------------------------------------------------------------------------------ GMRES
 struct GmresResult {
@@ -185,11 +287,10 @@ private:
     PinnedBuf pin_;
 };
 
-// Persistent arrays of a nonlinear solve (see Bratu3D::workspace).
+// Persistent arrays of a nonlinear solve (see NonlinearOp::workspace).
 struct SolverWorkspace {
     explicit SolverWorkspace(Context& ctx, size_t N) : gmres(ctx, N) {}
     DeviceArray<double> xb, Fa, Fb, ca, cb, z, u, w, scratch, xnorm;
-    DeviceArray<float> c32;
     Gmres gmres;
     KrylovSpace space;
 };
@@ -212,8 +313,8 @@ double diag_fp64_peak_tflops(Context& ctx);
 double forcing(const KrylovParams& p, size_t k, double rnorm, double rprev, double eta_prev, double res0);
 
 // x holds x0 on entry and the final iterate on return.
-void newton_krylov(Bratu3D& f, double* x, const KrylovParams& p, Provider* pc, numa_krylov_result& out);
-void chebyshev_inexact(Bratu3D& f, double* x, const KrylovParams& p, Provider* pc, numa_krylov_result& out);
-void tf_chebyshev_2018(Bratu3D& f, double* x, const KrylovParams& p, Provider* pc, numa_krylov_result& out);
+void newton_krylov(NonlinearOp& f, double* x, const KrylovParams& p, Provider* pc, numa_krylov_result& out);
+void chebyshev_inexact(NonlinearOp& f, double* x, const KrylovParams& p, Provider* pc, numa_krylov_result& out);
+void tf_chebyshev_2018(NonlinearOp& f, double* x, const KrylovParams& p, Provider* pc, numa_krylov_result& out);
 
 }  // namespace numa::gpu

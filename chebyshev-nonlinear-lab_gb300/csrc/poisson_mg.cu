@@ -32,8 +32,8 @@ struct PoissonMG::Level {
     double h2inv = 0.0;
     double inv = 0.0;  // 1.0 / h2inv, as the reference forms it (poisson_mg.hpp:101)
     DeviceArray<double> x64, b64, bs64;
-    DeviceArray<float> x32, x32b, b32, bs32;  // FP32 cycle: x32 / x32b ping-pong between fused sweeps
-    float* cur32 = nullptr;                   // the FP32 iterate after this level's last sweep
+    DeviceArray<float> x32, b32, bs32;  // FP32 cycle (colour-split layout when n is odd)
+    float* cur32 = nullptr;             // the FP32 iterate of this level
 };
 
 namespace {
@@ -84,7 +84,6 @@ PoissonMG::PoissonMG(Context& ctx, size_t n, int pre, int post, int precision, i
             }
         } else {
             L->x32.resize(Nl);
-            L->x32b.resize(Nl);
             L->b32.resize(Nl);
             L->bs32.resize(Nl);
         }
@@ -204,76 +203,85 @@ void PoissonMG::cycle(size_t l) {
     ctx_.check_launch("mg cycle");
 }
 
-// The FP32 cycle (precision extension): the same steps as cycle<double>, with each red-black
-// sweep one fused kernel (k_rbgs_sweep32) that reads the previous iterate and writes the next
-// (ping-pong between x32 and x32b), and the finest level's last sweep writing z in FP64.
+// The FP32 cycle (precision extension): the same steps as cycle<double> in single precision.
+// Levels of odd n (all but an even coarsest) keep x, b and b h^2 in the colour-split layout
+// (mg_kernels.cuh), where every colour pass streams its own colour contiguously.
 void PoissonMG::cycle32(size_t l) {
     Level& L = *levels_[l];
     const int n = L.n;
     const bool finest = (l == 0);
+    const bool split = (n & 1) != 0;
     double* z = finest ? z0_ : nullptr;
     cudaStream_t s = ctx_.stream;
-    const int ichunk = std::min(32, std::max(2, n / 16));
-    const dim3 sgrid((n + SW_TK - 1) / SW_TK, (n + SW_TJ - 1) / SW_TJ, (n + ichunk - 1) / ichunk);
-    float* bufs[2] = {L.x32.p, L.x32b.p};
-    int cur = 0;  // bufs[cur] holds the iterate
-    bool have = false;
+    const size_t Nl = (size_t)n * n * n;
+    float* x = L.x32.p;
+    const float* b = L.b32.p;
     const float* bs = L.bs32.p;
-    // one sweep (order 0: colour 0 first): from the iterate (or from zero) into the other buffer
-    auto sweep = [&](int order, bool last_to_z) {
-        const int c0 = order == 0 ? 0 : 1;
-        float* out = bufs[have ? 1 - cur : cur];
-        const float* in = bufs[cur];
-        if (!have) k_rbgs_sweep32<true, true, false><<<sgrid, SW_THREADS, 0, s>>>(in, out, bs, nullptr, n, c0, ichunk);
-        else if (last_to_z) k_rbgs_sweep32<false, true, true><<<sgrid, SW_THREADS, 0, s>>>(in, out, bs, z, n, c0, ichunk);
-        else k_rbgs_sweep32<false, true, false><<<sgrid, SW_THREADS, 0, s>>>(in, out, bs, nullptr, n, c0, ichunk);
+    const dim3 blk(BX, BY);
+    const dim3 cgrid(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n);
+    auto pass = [&](int colour, bool first) {
+        if (split) {
+            if (first) k_rbgs_split<true><<<cgrid, blk, 0, s>>>(x, bs, n, colour);
+            else k_rbgs_split<false><<<cgrid, blk, 0, s>>>(x, bs, n, colour);
+        } else {
+            if (first) k_rbgs<float, true, false><<<cgrid, blk, 0, s>>>(x, bs, nullptr, n, colour);
+            else k_rbgs<float, false, false><<<cgrid, blk, 0, s>>>(x, bs, nullptr, n, colour);
+        }
         ctx_.count_launch();
-        if (have) cur = 1 - cur;
-        have = true;
     };
+    auto sweep = [&](int order, bool first) {
+        const int c0 = order == 0 ? 0 : 1;
+        pass(c0, first);
+        pass(1 - c0, false);
+    };
+    auto out_z = [&]() {
+        if (!z) return;
+        if (split) k_to64_split<<<ew_grid(ctx_, Nl), 256, 0, s>>>(x, z, Nl);
+        else k_to64<<<ew_grid(ctx_, Nl), 256, 0, s>>>(x, z, Nl);
+        ctx_.count_launch();
+    };
+    L.cur32 = x;
     if (l + 1 == levels_.size()) {
         if (n == 1) {
-            k_single<float><<<1, 1, 0, s>>>(L.b32.p, bufs[0], z, 6.0 * L.h2inv);
+            k_single<float><<<1, 1, 0, s>>>(b, x, nullptr, 6.0 * L.h2inv);
             ctx_.count_launch();
         } else {
-            for (int sw = 0; sw < 30; ++sw) sweep(sw % 2, z != nullptr && sw == 29);
+            for (int sw = 0; sw < 30; ++sw) sweep(sw % 2, sw == 0);
         }
-        L.cur32 = bufs[cur];
+        out_z();
         ctx_.check_launch("mg coarsest (fp32)");
         return;
     }
-    for (int sw = 0; sw < pre_; ++sw) sweep(0, false);
-    if (pre_ == 0) {
-        NUMA_CUDA(cudaMemsetAsync(bufs[cur], 0, (size_t)n * n * n * sizeof(float), s));
-        have = true;
-    }
-    float* x = bufs[cur];
+    // a level with a coarser one below is odd, hence split
+    for (int sw = 0; sw < pre_; ++sw) sweep(0, sw == 0);
+    if (pre_ == 0) NUMA_CUDA(cudaMemsetAsync(x, 0, Nl * sizeof(float), s));
     float* r = reinterpret_cast<float*>(scratch_r_.p);
-    const dim3 blk(BX, BY);
     {
         const int ich = n >= 64 ? 8 : 1;
         const dim3 g((n + BX - 1) / BX, (n + BY - 1) / BY, (n + ich - 1) / ich);
-        k_residual<float><<<g, blk, 0, s>>>(x, L.b32.p, r, n, ich, (float)L.h2inv);
+        k_residual_split<<<g, blk, 0, s>>>(x, b, r, n, ich, (float)L.h2inv);
         ctx_.count_launch();
     }
     Level& C = *levels_[l + 1];
     const int nc = C.n;
-    k_restrict<float><<<dim3((nc + BX - 1) / BX, (nc + BY - 1) / BY, nc), blk, 0, s>>>(r, C.b32.p, C.bs32.p, n, nc,
-                                                                                       C.inv);
+    const dim3 rg((nc + BX - 1) / BX, (nc + BY - 1) / BY, nc);
+    if (nc & 1) k_restrict_split<<<rg, blk, 0, s>>>(r, C.b32.p, C.bs32.p, n, nc, (float)C.inv);
+    else k_restrict<float><<<rg, blk, 0, s>>>(r, C.b32.p, C.bs32.p, n, nc, C.inv);
     ctx_.count_launch();
     if (l == 0) coarse_cycle();
     else cycle32(l + 1);
-    if (post_ > 0)
-        k_prolong<float, true><<<dim3(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n), blk, 0, s>>>(C.cur32, x, nc, n);
-    else
-        k_prolong<float, false><<<dim3((n + BX - 1) / BX, (n + BY - 1) / BY, n), blk, 0, s>>>(C.cur32, x, nc, n);
-    ctx_.count_launch();
-    for (int sw = 0; sw < post_; ++sw) sweep(1, z != nullptr && sw == post_ - 1);
-    if (z != nullptr && post_ == 0) {
-        k_to64<<<ew_grid(ctx_, (size_t)n * n * n), 256, 0, s>>>(bufs[cur], z, (size_t)n * n * n);
-        ctx_.count_launch();
+    const dim3 pg0(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n), pga((n + BX - 1) / BX, (n + BY - 1) / BY, n);
+    const bool csplit = (nc & 1) != 0;
+    if (post_ > 0) {
+        if (csplit) k_prolong_split<true, false><<<pg0, blk, 0, s>>>(C.cur32, x, nc, n);
+        else k_prolong_split<false, false><<<pg0, blk, 0, s>>>(C.cur32, x, nc, n);
+    } else {
+        if (csplit) k_prolong_split<true, true><<<pga, blk, 0, s>>>(C.cur32, x, nc, n);
+        else k_prolong_split<false, true><<<pga, blk, 0, s>>>(C.cur32, x, nc, n);
     }
-    L.cur32 = bufs[cur];
+    ctx_.count_launch();
+    for (int sw = 0; sw < post_; ++sw) sweep(1, false);
+    out_z();
     ctx_.check_launch("mg cycle (fp32)");
 }
 
@@ -295,7 +303,8 @@ void PoissonMG::apply(const double* r, double* z) {
         z0_ = nullptr;
         cycle<double>(0);
     } else {
-        k_scale_in32<<<ew_grid(ctx_, N), 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, (float)L0.inv, N);
+        if (L0.n & 1) k_scale_in32_split<<<ew_grid(ctx_, N), 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, (float)L0.inv, N);
+        else k_scale_in32<<<ew_grid(ctx_, N), 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, (float)L0.inv, N);
         ctx_.count_launch();
         z0_ = z;
         cycle32(0);
@@ -324,19 +333,12 @@ double PoissonMG::time_finest_pass(int reps) {
         NUMA_CUDA(cudaEventRecord(b, ctx_.stream));
         NUMA_CUDA(cudaEventSynchronize(b));
     } else {
-        // the FP32 cycle's dominant kernel: one fused red-black sweep (x32 -> x32b -> x32 ...)
+        // the FP32 cycle's dominant kernel: one colour pass on the split layout
         NUMA_CUDA(cudaMemsetAsync(L0.x32.p, 0, N * sizeof(float), ctx_.stream));
-        NUMA_CUDA(cudaMemsetAsync(L0.x32b.p, 0, N * sizeof(float), ctx_.stream));
         NUMA_CUDA(cudaMemsetAsync(L0.bs32.p, 0, N * sizeof(float), ctx_.stream));
-        const int ichunk = std::min(32, std::max(2, n / 16));
-        const dim3 sgrid((n + SW_TK - 1) / SW_TK, (n + SW_TJ - 1) / SW_TJ, (n + ichunk - 1) / ichunk);
-        float* bufs[2] = {L0.x32.p, L0.x32b.p};
-        k_rbgs_sweep32<false, true, false><<<sgrid, SW_THREADS, 0, ctx_.stream>>>(bufs[0], bufs[1], L0.bs32.p, nullptr,
-                                                                                  n, 0, ichunk);
+        k_rbgs_split<false><<<cgrid, blk, 0, ctx_.stream>>>(L0.x32.p, L0.bs32.p, n, 0);
         NUMA_CUDA(cudaEventRecord(a, ctx_.stream));
-        for (int r = 0; r < reps; ++r)
-            k_rbgs_sweep32<false, true, false><<<sgrid, SW_THREADS, 0, ctx_.stream>>>(
-                bufs[(r + 1) & 1], bufs[r & 1], L0.bs32.p, nullptr, n, r & 1, ichunk);
+        for (int r = 0; r < reps; ++r) k_rbgs_split<false><<<cgrid, blk, 0, ctx_.stream>>>(L0.x32.p, L0.bs32.p, n, r & 1);
         NUMA_CUDA(cudaEventRecord(b, ctx_.stream));
         NUMA_CUDA(cudaEventSynchronize(b));
     }

@@ -1,9 +1,10 @@
 """Python binding of libnuma_gpu.so (ctypes over the C ABI of include/numa_gpu.h).
 
 The objects mirror the reference's C++ interfaces (namespace numa::op):
-``Bratu3D`` (eval / jvp / d2 / jacobi_diag), ``PoissonMG`` (V-cycle), preconditioner
-``Provider`` objects (make / apply), ``gmres`` / ``gmres_recycled`` and the drivers
-``newton_krylov``, ``chebyshev_inexact`` and ``tf_chebyshev_2018``.  Vectors live on the GPU
+``Bratu3D`` (eval / jvp / d2 / jacobi_diag), ``Burgers2D`` (eval / jvp / d2 / exact),
+``PoissonMG`` and ``HelmholtzMG2D`` (V-cycles), preconditioner ``Provider`` objects
+(make / apply), ``gmres`` / ``gmres_recycled`` and the drivers ``newton_krylov``,
+``chebyshev_inexact`` and ``tf_chebyshev_2018`` on either operator.  Vectors live on the GPU
 (``Vec``); ``Vec.from_numpy`` / ``Vec.numpy`` move them to and from host memory.
 
 There is no CPU fallback: loading fails loudly when the library has not been built, and every
@@ -26,7 +27,7 @@ FP64, FP32 = 0, 1
 ANALYTIC, FD, ANALYTIC_FP32 = 0, 1, 2
 MGS, CGS2 = 0, 1
 METHODS = {"nk": 0, "cheb": 1, "rec": 2, "tf2018": 3}
-PRECONDS = {"none": 0, "mg": 1, "jacobi": 2}
+PRECONDS = {"none": 0, "mg": 1, "jacobi": 2, "burgers_mg": 3}
 
 
 class KrylovParams(C.Structure):
@@ -107,6 +108,22 @@ SIGNATURES = {
     "numa_gpu_bratu3d_jvp": ([_P, _P, _P, _P, _I], _I),
     "numa_gpu_bratu3d_d2": ([_P, _P, _P, _P, _I], _I),
     "numa_gpu_bratu3d_jacobi_diag": ([_P, _P, _P], _I),
+    "numa_gpu_burgers2d_create": ([_P, _SZ, _D, _D, _D, _PP], _I),
+    "numa_gpu_burgers2d_destroy": ([_P], _I),
+    "numa_gpu_burgers2d_size": ([_P, C.POINTER(_SZ)], _I),
+    "numa_gpu_burgers2d_cell_reynolds": ([_P, _F64P], _I),
+    "numa_gpu_burgers2d_exact": ([_P, _P], _I),
+    "numa_gpu_burgers2d_eval": ([_P, _P, _P], _I),
+    "numa_gpu_burgers2d_jvp": ([_P, _P, _P, _P, _I], _I),
+    "numa_gpu_burgers2d_d2": ([_P, _P, _P, _P, _I], _I),
+    "numa_gpu_burgers2d_solve": ([_P, _I, _P, C.POINTER(KrylovParams), _P, C.POINTER(KrylovResult)], _I),
+    "numa_gpu_hmg2d_create": ([_P, _SZ, _D, _D, _I, _I, _PP], _I),
+    "numa_gpu_hmg2d_destroy": ([_P], _I),
+    "numa_gpu_hmg2d_levels": ([_P, C.POINTER(_SZ)], _I),
+    "numa_gpu_hmg2d_apply": ([_P, _P, _P], _I),
+    "numa_gpu_provider_create_burgers_mg": ([_P, _SZ, _D, _D, _PP], _I),
+    "numa_gpu_solve_burgers2d_host": ([_P, _SZ, _D, _D, _D, _I, _I, C.POINTER(KrylovParams), _F64P, _F64P,
+                                       C.POINTER(KrylovResult)], _I),
     "numa_gpu_mg_create": ([_P, _SZ, _I, _I, _PP], _I),
     "numa_gpu_mg_create_ex": ([_P, _SZ, _I, _I, _I, _I, _PP], _I),
     "numa_gpu_mg_destroy": ([_P], _I),
@@ -345,6 +362,79 @@ class Bratu3D:
         self.ctx.check(self.lib.numa_gpu_bratu3d_jacobi_diag(self.h, x.h, d.h), "bratu3d_jacobi_diag")
 
 
+class Burgers2D:
+    """Burgers2D(n, nu, dt, amplitude) (problems/burgers2d.hpp:23-52) on the GPU; N = 2 n^2."""
+
+    def __init__(self, ctx: Context, n: int, nu: float, dt: float, amplitude: float = 1.0):
+        self.ctx, self.lib, self.n = ctx, ctx.lib, int(n)
+        self.nu, self.dt, self.amplitude = float(nu), float(dt), float(amplitude)
+        h = C.c_void_p()
+        ctx.check(self.lib.numa_gpu_burgers2d_create(ctx.h, self.n, self.nu, self.dt, self.amplitude, C.byref(h)),
+                  "burgers2d_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.numa_gpu_burgers2d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def size(self) -> int:
+        return 2 * self.n * self.n
+
+    def cell_reynolds(self) -> float:
+        v = C.c_double()
+        self.ctx.check(self.lib.numa_gpu_burgers2d_cell_reynolds(self.h, C.byref(v)), "burgers2d_cell_reynolds")
+        return v.value
+
+    def exact(self, out: Vec):
+        self.ctx.check(self.lib.numa_gpu_burgers2d_exact(self.h, out.h), "burgers2d_exact")
+
+    def eval(self, w: Vec, out: Vec):
+        self.ctx.check(self.lib.numa_gpu_burgers2d_eval(self.h, w.h, out.h), "burgers2d_eval")
+
+    def jvp(self, w: Vec, d: Vec, out: Vec, mode: int = ANALYTIC):
+        self.ctx.check(self.lib.numa_gpu_burgers2d_jvp(self.h, w.h, d.h, out.h, mode), "burgers2d_jvp")
+
+    def d2(self, w: Vec, d: Vec, out: Vec, mode: int = ANALYTIC):
+        self.ctx.check(self.lib.numa_gpu_burgers2d_d2(self.h, w.h, d.h, out.h, mode), "burgers2d_d2")
+
+
+class HelmholtzMG2D:
+    """HelmholtzMG2D(n, alpha, nu, pre, post) (linalg/helmholtz_mg2d.hpp:13-32): one V-cycle per call."""
+
+    def __init__(self, ctx: Context, n: int, alpha: float, nu: float, pre: int = 2, post: int = 2):
+        self.ctx, self.lib, self.n = ctx, ctx.lib, int(n)
+        h = C.c_void_p()
+        ctx.check(self.lib.numa_gpu_hmg2d_create(ctx.h, self.n, float(alpha), float(nu), pre, post, C.byref(h)),
+                  "hmg2d_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.numa_gpu_hmg2d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def levels(self) -> int:
+        v = C.c_size_t()
+        self.ctx.check(self.lib.numa_gpu_hmg2d_levels(self.h, C.byref(v)), "hmg2d_levels")
+        return v.value
+
+    def __call__(self, r: Vec, z: Vec):
+        self.ctx.check(self.lib.numa_gpu_hmg2d_apply(self.h, r.h, z.h), "hmg2d_apply")
+
+
 class PoissonMG:
     """PoissonMG(n, pre, post) (linalg/poisson_mg.hpp:24-64); precision / max_levels extend it."""
 
@@ -410,7 +500,16 @@ class Provider:
         return p
 
     @classmethod
-    def create(cls, ctx: Context, kind: str, op: Bratu3D, precision: int = FP64) -> "Provider | None":
+    def burgers_mg(cls, ctx: Context, n: int, nu: float, dt: float) -> "Provider":
+        """BurgersMGProvider(n, nu, dt) (problems/burgers2d.hpp:220-246)."""
+        h = C.c_void_p()
+        ctx.check(ctx.lib.numa_gpu_provider_create_burgers_mg(ctx.h, n, nu, dt, C.byref(h)), "provider_burgers_mg")
+        return cls(ctx, h, "burgers_mg")
+
+    @classmethod
+    def create(cls, ctx: Context, kind: str, op, precision: int = FP64) -> "Provider | None":
+        if isinstance(op, Burgers2D):
+            return cls.burgers_mg(ctx, op.n, op.nu, op.dt) if kind == "mg" else cls.identity(ctx)
         if kind == "mg":
             return cls.poisson_mg(ctx, op.n, precision=precision)
         if kind == "jacobi":
@@ -530,10 +629,17 @@ def forcing(params: KrylovParams, k: int, rnorm: float, rprev: float, eta_prev: 
     return load().numa_gpu_forcing(C.byref(params), k, rnorm, rprev, eta_prev, res0)
 
 
-def _driver(name: str, op: Bratu3D, x: Vec, params: KrylovParams | None, provider: Provider | None) -> dict:
+_DRIVER_METHOD = {"numa_gpu_newton_krylov": 0, "numa_gpu_chebyshev_inexact": 1, "numa_gpu_tf_chebyshev_2018": 3}
+
+
+def _driver(name: str, op, x: Vec, params: KrylovParams | None, provider: Provider | None) -> dict:
     p = params if params is not None else default_params()
     res = KrylovResult()
-    rc = getattr(op.lib, name)(op.h, x.h, C.byref(p), provider.h if provider else None, C.byref(res))
+    if isinstance(op, Burgers2D):
+        rc = op.lib.numa_gpu_burgers2d_solve(op.h, _DRIVER_METHOD[name], x.h, C.byref(p),
+                                             provider.h if provider else None, C.byref(res))
+    else:
+        rc = getattr(op.lib, name)(op.h, x.h, C.byref(p), provider.h if provider else None, C.byref(res))
     op.ctx.check(rc, name)
     return to_dict(res)
 
@@ -577,4 +683,20 @@ def solve_bratu3d_host(ctx: Context, n: int, lam: float, x0: np.ndarray, out: np
                                              C.byref(p), x0.ctypes.data_as(_F64P), out.ctypes.data_as(_F64P),
                                              C.byref(res))
     ctx.check(rc, "solve_bratu3d_host")
+    return out, to_dict(res)
+
+
+def solve_burgers2d_host(ctx: Context, n: int, nu: float, dt: float, amplitude: float, x0: np.ndarray,
+                         out: np.ndarray | None = None, method: str = "nk", precond: str = "mg",
+                         params: KrylovParams | None = None) -> tuple[np.ndarray, dict]:
+    """Host buffers in, host buffers out (numa_gpu_solve_burgers2d_host); precond "mg" or "none"."""
+    p = params if params is not None else default_params()
+    x0 = _f64(x0).ravel()
+    if out is None:
+        out = np.empty(2 * n * n)
+    res = KrylovResult()
+    kind = PRECONDS["burgers_mg"] if precond == "mg" else PRECONDS["none"]
+    rc = ctx.lib.numa_gpu_solve_burgers2d_host(ctx.h, n, nu, dt, amplitude, METHODS[method], kind, C.byref(p),
+                                               x0.ctypes.data_as(_F64P), out.ctypes.data_as(_F64P), C.byref(res))
+    ctx.check(rc, "solve_burgers2d_host")
     return out, to_dict(res)

@@ -75,7 +75,8 @@ typedef enum numa_gpu_method {
 typedef enum numa_gpu_precond_kind {
     NUMA_GPU_PRECOND_NONE = 0,       /* NoPrecond / IdentityPrecond (krylov_newton.hpp:20-22, gmres.hpp:37-39) */
     NUMA_GPU_PRECOND_POISSON_MG = 1, /* PoissonMGProvider (linalg/poisson_mg.hpp:303-320) */
-    NUMA_GPU_PRECOND_JACOBI = 2      /* BratuJacobi (problems/bratu3d.hpp:104-120) */
+    NUMA_GPU_PRECOND_JACOBI = 2,     /* BratuJacobi (problems/bratu3d.hpp:104-120) */
+    NUMA_GPU_PRECOND_BURGERS_MG = 3  /* BurgersMGProvider (problems/burgers2d.hpp:220-246) */
 } numa_gpu_precond_kind;
 
 /* ---------------------------------------------------------------- parameter / result structs */
@@ -145,6 +146,8 @@ typedef struct numa_gpu_bratu3d numa_gpu_bratu3d;
 typedef struct numa_gpu_mg numa_gpu_mg;
 typedef struct numa_gpu_provider numa_gpu_provider;
 typedef struct numa_gpu_krylov_space numa_gpu_krylov_space;
+typedef struct numa_gpu_burgers2d numa_gpu_burgers2d;
+typedef struct numa_gpu_hmg2d numa_gpu_hmg2d;
 
 /* ---------------------------------------------------------------- library / context */
 int numa_gpu_abi_version(void);
@@ -194,6 +197,26 @@ int numa_gpu_bratu3d_d2(numa_gpu_bratu3d* op, const numa_gpu_vec* x, const numa_
 /* d = 6 h^-2 - lambda e^x             Bratu3D::jacobi_diag (bratu3d.hpp:59-69) */
 int numa_gpu_bratu3d_jacobi_diag(numa_gpu_bratu3d* op, const numa_gpu_vec* x, numa_gpu_vec* d);
 
+/* ---------------------------------------------------------------- Burgers2D operator */
+/* Burgers2D(n, nu, dt, amplitude) (problems/burgers2d.hpp:23-52): one implicit-Euler step of 2D
+ * viscous Burgers with the manufactured root w*; N = 2 n^2, w = (u, v) component-major. */
+int numa_gpu_burgers2d_create(numa_gpu_ctx* ctx, size_t n, double nu, double dt, double amplitude,
+                              numa_gpu_burgers2d** out);
+int numa_gpu_burgers2d_destroy(numa_gpu_burgers2d* op);
+int numa_gpu_burgers2d_size(const numa_gpu_burgers2d* op, size_t* N);
+/* |amplitude| / (nu (n + 1))           Burgers2D::cell_reynolds (burgers2d.hpp:59-62) */
+int numa_gpu_burgers2d_cell_reynolds(const numa_gpu_burgers2d* op, double* out);
+/* out = w*                             Burgers2D::exact (burgers2d.hpp:63) */
+int numa_gpu_burgers2d_exact(numa_gpu_burgers2d* op, numa_gpu_vec* out);
+/* out = F(w)                           Burgers2D::eval (burgers2d.hpp:65-69) */
+int numa_gpu_burgers2d_eval(numa_gpu_burgers2d* op, const numa_gpu_vec* w, numa_gpu_vec* out);
+/* out = F'(w) d   mode ANALYTIC: Burgers2D::jvp (burgers2d.hpp:71-123); FD: jvp_fd */
+int numa_gpu_burgers2d_jvp(numa_gpu_burgers2d* op, const numa_gpu_vec* w, const numa_gpu_vec* d,
+                           numa_gpu_vec* out, int mode);
+/* out = F''(w)[d,d] mode ANALYTIC: Burgers2D::d2 (burgers2d.hpp:125-160); FD: d2_fd */
+int numa_gpu_burgers2d_d2(numa_gpu_burgers2d* op, const numa_gpu_vec* w, const numa_gpu_vec* d,
+                          numa_gpu_vec* out, int mode);
+
 /* ---------------------------------------------------------------- Poisson multigrid */
 /* PoissonMG(n, pre, post) (linalg/poisson_mg.hpp:26-64): levels while n is odd, down to 1. */
 int numa_gpu_mg_create(numa_gpu_ctx* ctx, size_t n, int pre, int post, numa_gpu_mg** out);
@@ -206,6 +229,16 @@ int numa_gpu_mg_levels(const numa_gpu_mg* mg, size_t* levels);    /* PoissonMG::
 /* z = one V-cycle applied to r        PoissonMG::operator() (poisson_mg.hpp:69-80) */
 int numa_gpu_mg_apply(numa_gpu_mg* mg, const numa_gpu_vec* r, numa_gpu_vec* z);
 
+/* ---------------------------------------------------------------- 2D Helmholtz multigrid */
+/* HelmholtzMG2D(n, alpha, nu, pre, post) (linalg/helmholtz_mg2d.hpp:13-32): V-cycle for
+ * alpha I - nu Lap_h on n^2 points, levels while n is odd; FP64, bit-identical to the reference. */
+int numa_gpu_hmg2d_create(numa_gpu_ctx* ctx, size_t n, double alpha, double nu, int pre, int post,
+                          numa_gpu_hmg2d** out);
+int numa_gpu_hmg2d_destroy(numa_gpu_hmg2d* mg);
+int numa_gpu_hmg2d_levels(const numa_gpu_hmg2d* mg, size_t* levels);  /* levels() :34 */
+/* z = one V-cycle applied to r          HelmholtzMG2D::operator() (helmholtz_mg2d.hpp:36-42) */
+int numa_gpu_hmg2d_apply(numa_gpu_hmg2d* mg, const numa_gpu_vec* r, numa_gpu_vec* z);
+
 /* ---------------------------------------------------------------- preconditioner providers */
 /* Provider::make(x) -> Bound, Bound(r, z) (krylov_newton.hpp:20-22, poisson_mg.hpp:303-320,
  * bratu3d.hpp:104-120).  A provider owns what it creates (the MG hierarchy, the diagonal). */
@@ -213,6 +246,9 @@ int numa_gpu_provider_create_identity(numa_gpu_ctx* ctx, numa_gpu_provider** out
 int numa_gpu_provider_create_poisson_mg(numa_gpu_ctx* ctx, size_t n, int pre, int post, int precision,
                                         numa_gpu_provider** out);
 int numa_gpu_provider_create_jacobi(numa_gpu_bratu3d* op, numa_gpu_provider** out);
+/* BurgersMGProvider(n, nu, dt): HelmholtzMG2D(n, 1/dt, nu) V(2,2) on u and on v. */
+int numa_gpu_provider_create_burgers_mg(numa_gpu_ctx* ctx, size_t n, double nu, double dt,
+                                        numa_gpu_provider** out);
 int numa_gpu_provider_destroy(numa_gpu_provider* p);
 int numa_gpu_provider_make(numa_gpu_provider* p, const numa_gpu_vec* x);            /* make(x)  */
 int numa_gpu_provider_apply(numa_gpu_provider* p, const numa_gpu_vec* r, numa_gpu_vec* z); /* Bound(r,z) */
@@ -267,12 +303,23 @@ int numa_gpu_chebyshev_inexact(numa_gpu_bratu3d* op, numa_gpu_vec* x, const numa
 int numa_gpu_tf_chebyshev_2018(numa_gpu_bratu3d* op, numa_gpu_vec* x, const numa_krylov_params* p,
                                numa_gpu_provider* provider, numa_krylov_result* result);
 
+/* The three drivers on a Burgers2D: method of numa_gpu_method (CHEB_REC sets p->recycle).
+ * The same functions as above, templated in the reference on the operator type. */
+int numa_gpu_burgers2d_solve(numa_gpu_burgers2d* op, int method, numa_gpu_vec* x,
+                             const numa_krylov_params* p, numa_gpu_provider* provider,
+                             numa_krylov_result* result);
+
 /* One call from host buffers to host buffers: Bratu3D(n, lambda), provider of precond_kind
  * (MG with pre = post = 2 and mg_precision), method of numa_gpu_method, x0[n^3] -> x_out[n^3].
  * The shape of apps/smoke_bratu.cpp:125-148 and apps/run_campaign.cpp:344-390. */
 int numa_gpu_solve_bratu3d_host(numa_gpu_ctx* ctx, size_t n, double lambda, int method,
                                 int precond_kind, int mg_precision, const numa_krylov_params* p,
                                 const double* x0, double* x_out, numa_krylov_result* result);
+/* The same for Burgers2D(n, nu, dt, amplitude), precond_kind NONE or BURGERS_MG, x0[2n^2] ->
+ * x_out[2n^2] (apps/run_campaign.cpp:577-593). */
+int numa_gpu_solve_burgers2d_host(numa_gpu_ctx* ctx, size_t n, double nu, double dt, double amplitude,
+                                  int method, int precond_kind, const numa_krylov_params* p,
+                                  const double* x0, double* x_out, numa_krylov_result* result);
 
 /* ---------------------------------------------------------------- V-cycle without allocation */
 /* No counterpart in the reference.  For callers that cannot allocate device memory when they
