@@ -6,8 +6,8 @@
 // keeping the i-1, i, i+1 values of its column in registers, so each point issues five loads.
 // The 7-point sums follow the reference's operation order (6v, then minus the i-1, i+1, j-1,
 // j+1, k-1, k+1 neighbours; a missing neighbour subtracts +0.0, which leaves every value
-// unchanged), so the stencil results equal the reference's bit for bit; only exp may differ by
-// an ulp between CUDA and the host C library.
+// unchanged), so the stencil results equal the reference's bit for bit; only e^x may differ by
+// an ulp between the table-driven exp_tang (common.cuh) and the host C library.
 #include <cmath>
 #include <limits>
 
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, d
         for (int i = i0; i < i1; ++i) {
             double above;
             const double s = lap_sum(u, p, plane, n, i, j, k, below, cur, above);
-            const double e = lam * exp(cur);
+            const double e = lam * exp_tang(cur);
             const double f = h2inv * s - e;
             F[p] = f;
             if (WRITE_C) c_out[p] = e;
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, d
 // c = lambda e^u
 __global__ void k_coef(const double* __restrict__ u, double* __restrict__ c, size_t N, double lam) {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) c[p] = lam * exp(u[p]);
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) c[p] = lam * exp_tang(u[p]);
 }
 
 // out = h^-2 (6v - sum) - c v, with c given (FROM_X: c = lambda e^x formed here).
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(BX* BY) k_jvp(const double* __restrict__ cx, c
     for (int i = i0; i < i1; ++i) {
         double above;
         const double s = lap_sum(v, p, plane, n, i, j, k, below, cur, above);
-        const double c = FROM_X ? lam * exp(cx[p]) : cx[p];
+        const double c = FROM_X ? lam * exp_tang(cx[p]) : cx[p];
         out[p] = h2inv * s - c * cur;
         below = cur;
         cur = above;
@@ -127,36 +127,62 @@ __global__ void __launch_bounds__(BX* BY) k_jvp(const double* __restrict__ cx, c
 
 // Mixed precision: F'(x) v in FP32 arithmetic on FP64 vectors with an FP32 coefficient.  Each
 // FP64 value is converted once (integer arithmetic, no FP64 instruction) into a shared-memory
-// plane of the tile with a 1-point halo; three plane slots roll along i.
+// plane of the tile with a 1-point halo; three plane slots roll along i.  Software-pipelined:
+// the raw values of plane i+2 and the coefficient of plane i+1 are loaded into registers while
+// plane i is computed, so the loads' latency overlaps the arithmetic.
 __global__ void __launch_bounds__(BX* BY) k_jvp32(const float* __restrict__ c32, const double* __restrict__ v,
                                                   double* __restrict__ out, int n, int ichunk, float h2inv) {
-    __shared__ float S[3][BY + 2][BX + 2];
+    constexpr int TW = BX + 2, TH = BY + 2, TE = TW * TH;  // 34 x 10 tile, 340 values
+    constexpr int PER = (TE + BX * BY - 1) / (BX * BY);    // values per thread and plane (2)
+    __shared__ float S[3][TH][TW];
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
     const int k0 = blockIdx.x * BX, j0 = blockIdx.y * BY;
     const int k = k0 + tx, j = j0 + ty;
     const int i0 = blockIdx.z * ichunk;
     const int i1 = min(i0 + ichunk, n);
     const size_t plane = (size_t)n * n;
-    auto load = [&](int p) {
-        float(*T)[BX + 2] = S[(p + 3) % 3];
-        for (int e = tid; e < (BY + 2) * (BX + 2); e += BX * BY) {
-            const int r = e / (BX + 2), c = e - r * (BX + 2);
-            const int jj = j0 - 1 + r, kk = k0 - 1 + c;
-            float val = 0.0f;
-            if (p >= 0 && p < n && jj >= 0 && jj < n && kk >= 0 && kk < n)
-                val = f64_to_f32(v[(size_t)p * plane + (size_t)jj * n + kk]);
-            T[r][c] = val;
+    // this thread's tile elements: offset within a plane (or -1 outside the grid) and position
+    int off[PER], pos[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int e = tid + q * BX * BY;
+        const int r = e / TW, cc = e - r * TW;
+        const int jj = j0 - 1 + r, kk = k0 - 1 + cc;
+        pos[q] = e < TE ? e : -1;
+        off[q] = (e < TE && jj >= 0 && jj < n && kk >= 0 && kk < n) ? jj * n + kk : -1;
+    }
+    double raw[PER];
+    auto issue = [&](int p) {
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            raw[q] = 0.0;
+            if (p >= 0 && p < n && off[q] >= 0) raw[q] = v[(size_t)p * plane + off[q]];
         }
     };
-    load(i0 - 1);
-    load(i0);
+    auto commit = [&](int p) {
+        float* T = &S[(p + 3) % 3][0][0];
+#pragma unroll
+        for (int q = 0; q < PER; ++q)
+            if (pos[q] >= 0) T[pos[q]] = f64_to_f32(raw[q]);
+    };
+    const bool inside = k < n && j < n;
+    const size_t col = (size_t)j * n + k;
+    issue(i0 - 1);
+    commit(i0 - 1);
+    issue(i0);
+    commit(i0);
+    issue(i0 + 1);
+    float cnext = (inside && i0 < i1) ? c32[(size_t)i0 * plane + col] : 0.0f;
     for (int i = i0; i < i1; ++i) {
-        load(i + 1);
+        commit(i + 1);
+        if (i + 2 <= i1) issue(i + 2);
+        const float cc = cnext;
+        if (inside && i + 1 < i1) cnext = c32[(size_t)(i + 1) * plane + col];
         __syncthreads();
-        if (k < n && j < n) {
-            const float(*Tm)[BX + 2] = S[(i + 2) % 3];
-            const float(*T0)[BX + 2] = S[i % 3];
-            const float(*Tp)[BX + 2] = S[(i + 1) % 3];
+        if (inside) {
+            const float(*Tm)[TW] = S[(i + 2) % 3];
+            const float(*T0)[TW] = S[i % 3];
+            const float(*Tp)[TW] = S[(i + 1) % 3];
             const float cur = T0[ty + 1][tx + 1];
             float s = 6.0f * cur;
             s = s - Tm[ty + 1][tx + 1];
@@ -165,8 +191,7 @@ __global__ void __launch_bounds__(BX* BY) k_jvp32(const float* __restrict__ c32,
             s = s - T0[ty + 2][tx + 1];
             s = s - T0[ty + 1][tx];
             s = s - T0[ty + 1][tx + 2];
-            const size_t g = (size_t)i * plane + (size_t)j * n + k;
-            out[g] = f32_to_f64(h2inv * s - c32[g] * cur);
+            out[(size_t)i * plane + col] = f32_to_f64(h2inv * s - cc * cur);
         }
         __syncthreads();
     }

@@ -1075,6 +1075,20 @@ int numa_gpu_diag_fp64_peak(numa_gpu_ctx* ctx, double* tflops) {
     return guard(ctx, [&] { *tflops = diag_fp64_peak_tflops(*ctx->impl); });
 }
 
+int numa_gpu_diag_exp(const numa_gpu_vec* x, numa_gpu_vec* out, numa_gpu_vec* cuda_ref) {
+    if (!x || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(x->ctx, [&] {
+        same_ctx(x->ctx, out);
+        need(out->n == x->n, NUMA_GPU_ERR_SIZE_MISMATCH, "output length differs");
+        need(out->d != x->d, NUMA_GPU_ERR_INVALID_ARGUMENT, "output must not alias the input");
+        if (cuda_ref) {
+            same_ctx(x->ctx, cuda_ref);
+            need(cuda_ref->n == x->n, NUMA_GPU_ERR_SIZE_MISMATCH, "reference length differs");
+        }
+        diag_exp(*x->ctx->impl, x->d, out->d, cuda_ref ? cuda_ref->d : nullptr, x->n);
+    });
+}
+
 int numa_gpu_diag_time_smoother(numa_gpu_mg* mg, int reps, double* ms_per_pass) {
     if (!mg || !ms_per_pass || reps < 1) return NUMA_GPU_ERR_INVALID_ARGUMENT;
     return guard(mg->ctx, [&] { *ms_per_pass = mg->impl->time_finest_pass(reps); });

@@ -1,5 +1,6 @@
 // diag.cu — diagnostics for the roofline report: the measured FP64 FMA rate of this GPU and
 // event-timed launches of the dominant kernels.  No counterpart in the reference.
+#include <algorithm>
 #include <cmath>
 
 #include "numa_internal.hpp"
@@ -25,7 +26,24 @@ __global__ void k_fma_chain(double* out, int iters, double a, double b) {
     if (s == -12345.678) out[0] = s;  // keeps the chains live; never true for these inputs
 }
 
+// out = exp_tang(x) and, in ref, CUDA's exp(x) (for accuracy tests of the table-driven e^x)
+__global__ void k_exp_pair(const double* __restrict__ x, double* __restrict__ out, double* __restrict__ ref,
+                           size_t N) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) {
+        out[p] = exp_tang(x[p]);
+        if (ref) ref[p] = exp(x[p]);
+    }
+}
+
 }  // namespace
+
+void diag_exp(Context& ctx, const double* x, double* out, double* ref, size_t N) {
+    size_t g = (N + 255) / 256, cap = (size_t)ctx.sm_count * 16;
+    k_exp_pair<<<(unsigned)std::max<size_t>(1, std::min(g, cap)), 256, 0, ctx.stream>>>(x, out, ref, N);
+    ctx.count_launch();
+    ctx.check_launch("diag exp");
+}
 
 double diag_fp64_peak_tflops(Context& ctx) {
     const int blocks = ctx.sm_count * 8, threads = 256, iters = 2000;

@@ -169,6 +169,7 @@ public:
 private:
     template <class T> void cycle(size_t l);
     void cycle32(size_t l);
+    bool first_fused32(size_t l) const;
     // The levels below the finest touch only the hierarchy's own arrays, so their part of the
     // cycle is captured once into a CUDA graph and replayed (one launch instead of ~10 a level).
     void coarse_cycle();
@@ -310,6 +311,8 @@ struct KrylovParams {
 
 KrylovParams params_from_c(const numa_krylov_params* p);
 double diag_fp64_peak_tflops(Context& ctx);
+// out = the library's e^x (exp_tang) of x; ref (optional) = CUDA's exp(x).
+void diag_exp(Context& ctx, const double* x, double* out, double* ref, size_t N);
 double forcing(const KrylovParams& p, size_t k, double rnorm, double rprev, double eta_prev, double res0);
 
 // x holds x0 on entry and the final iterate on return.

@@ -67,6 +67,8 @@ PoissonMG::PoissonMG(Context& ctx, size_t n, int pre, int post, int precision, i
     if (precision != NUMA_GPU_FP64 && precision != NUMA_GPU_FP32)
         throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "unknown precision");
     N0_ = n * n * n;
+    if (precision == NUMA_GPU_FP32 && N0_ >= (size_t{1} << 31))
+        throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "the FP32 V-cycle uses 32-bit indices: n^3 must be below 2^31");
     size_t m = n;
     double h2 = (static_cast<double>(n) + 1.0) * (static_cast<double>(n) + 1.0);
     for (;;) {
@@ -205,7 +207,21 @@ void PoissonMG::cycle(size_t l) {
 
 // The FP32 cycle (precision extension): the same steps as cycle<double> in single precision.
 // Levels of odd n (all but an even coarsest) keep x, b and b h^2 in the colour-split layout
-// (mg_kernels.cuh), where every colour pass streams its own colour contiguously.
+// (mg_kernels.cuh), where every colour pass streams its own colour contiguously.  Three fusions
+// remove whole passes over the finest level: the first smoothing pass of a split level (colour 0
+// from x = 0) is written by the kernel that produces the level's right-hand side (the FP64 to
+// FP32 conversion of r, or the restriction); the last pass of the cycle writes z in FP64 for
+// both colours instead of storing x; and prolongation touches only the colour-0 fine points when
+// post-smoothing follows.
+
+// True when level l's first smoothing pass is fused into the producer of its right-hand side.
+bool PoissonMG::first_fused32(size_t l) const {
+    const Level& L = *levels_[l];
+    if (!(L.n & 1)) return false;
+    if (l + 1 == levels_.size()) return L.n > 1;  // coarsest: 30 sweeps, the first from x = 0
+    return pre_ > 0;
+}
+
 void PoissonMG::cycle32(size_t l) {
     Level& L = *levels_[l];
     const int n = L.n;
@@ -218,70 +234,80 @@ void PoissonMG::cycle32(size_t l) {
     const float* b = L.b32.p;
     const float* bs = L.bs32.p;
     const dim3 blk(BX, BY);
+    const Split g = make_split(n);
+    const int ich = n >= 64 ? 4 : 1;
     const dim3 cgrid(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n);
-    auto pass = [&](int colour, bool first) {
+    const bool fused_first = first_fused32(l);
+    // pass(colour, first, last): last = the final pass of the cycle on the finest level
+    auto pass = [&](int colour, bool first, bool last) {
         if (split) {
-            if (first) k_rbgs_split<true><<<cgrid, blk, 0, s>>>(x, bs, n, colour);
-            else k_rbgs_split<false><<<cgrid, blk, 0, s>>>(x, bs, n, colour);
+            if (first && fused_first) return;  // already written by the producer of b
+            if (first) launch_pass_split<kPassFirst>(x, bs, nullptr, g, colour, s);
+            else if (last && z) launch_pass_split<kPassLastZ>(x, bs, z, g, colour, s);
+            else launch_pass_split<kPassFull>(x, bs, nullptr, g, colour, s);
         } else {
             if (first) k_rbgs<float, true, false><<<cgrid, blk, 0, s>>>(x, bs, nullptr, n, colour);
             else k_rbgs<float, false, false><<<cgrid, blk, 0, s>>>(x, bs, nullptr, n, colour);
         }
         ctx_.count_launch();
     };
-    auto sweep = [&](int order, bool first) {
+    auto sweep = [&](int order, bool first, bool last) {
         const int c0 = order == 0 ? 0 : 1;
-        pass(c0, first);
-        pass(1 - c0, false);
+        pass(c0, first, false);
+        pass(1 - c0, false, last);
     };
+    // z from x when no pass wrote it
     auto out_z = [&]() {
-        if (!z) return;
-        if (split) k_to64_split<<<ew_grid(ctx_, Nl), 256, 0, s>>>(x, z, Nl);
+        if (split) k_to64_split<<<ew_grid(ctx_, Nl), 256, 0, s>>>(x, z, (int)Nl, g.half);
         else k_to64<<<ew_grid(ctx_, Nl), 256, 0, s>>>(x, z, Nl);
         ctx_.count_launch();
     };
     L.cur32 = x;
     if (l + 1 == levels_.size()) {
         if (n == 1) {
-            k_single<float><<<1, 1, 0, s>>>(b, x, nullptr, 6.0 * L.h2inv);
+            k_single<float><<<1, 1, 0, s>>>(b, x, z, 6.0 * L.h2inv);
             ctx_.count_launch();
         } else {
-            for (int sw = 0; sw < 30; ++sw) sweep(sw % 2, sw == 0);
+            for (int sw = 0; sw < 30; ++sw) sweep(sw % 2, sw == 0, sw == 29);
+            if (z && !split) out_z();
         }
-        out_z();
         ctx_.check_launch("mg coarsest (fp32)");
         return;
     }
     // a level with a coarser one below is odd, hence split
-    for (int sw = 0; sw < pre_; ++sw) sweep(0, sw == 0);
+    for (int sw = 0; sw < pre_; ++sw) sweep(0, sw == 0, false);
     if (pre_ == 0) NUMA_CUDA(cudaMemsetAsync(x, 0, Nl * sizeof(float), s));
     float* r = reinterpret_cast<float*>(scratch_r_.p);
     {
-        const int ich = n >= 64 ? 8 : 1;
-        const dim3 g((n + BX - 1) / BX, (n + BY - 1) / BY, (n + ich - 1) / ich);
-        k_residual_split<<<g, blk, 0, s>>>(x, b, r, n, ich, (float)L.h2inv);
+        const dim3 rgd(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, (n + ich - 1) / ich);
+        k_residual_split<<<rgd, blk, 0, s>>>(x, b, r, g, ich, (float)L.h2inv);
         ctx_.count_launch();
     }
     Level& C = *levels_[l + 1];
     const int nc = C.n;
+    const bool csplit = (nc & 1) != 0;
+    const Split gc = make_split(nc);
     const dim3 rg((nc + BX - 1) / BX, (nc + BY - 1) / BY, nc);
-    if (nc & 1) k_restrict_split<<<rg, blk, 0, s>>>(r, C.b32.p, C.bs32.p, n, nc, (float)C.inv);
-    else k_restrict<float><<<rg, blk, 0, s>>>(r, C.b32.p, C.bs32.p, n, nc, C.inv);
+    if (csplit && first_fused32(l + 1))
+        k_restrict_split<true><<<rg, blk, 0, s>>>(r, C.b32.p, C.bs32.p, C.x32.p, n, nc, gc.half, (float)C.inv);
+    else if (csplit)
+        k_restrict_split<false><<<rg, blk, 0, s>>>(r, C.b32.p, C.bs32.p, C.x32.p, n, nc, gc.half, (float)C.inv);
+    else
+        k_restrict<float><<<rg, blk, 0, s>>>(r, C.b32.p, C.bs32.p, n, nc, C.inv);
     ctx_.count_launch();
     if (l == 0) coarse_cycle();
     else cycle32(l + 1);
-    const dim3 pg0(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n), pga((n + BX - 1) / BX, (n + BY - 1) / BY, n);
-    const bool csplit = (nc & 1) != 0;
+    const dim3 cg((nc + 1 + BX - 1) / BX, (nc + 1 + BY - 1) / BY, nc + 1);
     if (post_ > 0) {
-        if (csplit) k_prolong_split<true, false><<<pg0, blk, 0, s>>>(C.cur32, x, nc, n);
-        else k_prolong_split<false, false><<<pg0, blk, 0, s>>>(C.cur32, x, nc, n);
+        if (csplit) k_prolong_split<true, false><<<cg, blk, 0, s>>>(C.cur32, x, nc, gc.half, n, g.half);
+        else k_prolong_split<false, false><<<cg, blk, 0, s>>>(C.cur32, x, nc, gc.half, n, g.half);
     } else {
-        if (csplit) k_prolong_split<true, true><<<pga, blk, 0, s>>>(C.cur32, x, nc, n);
-        else k_prolong_split<false, true><<<pga, blk, 0, s>>>(C.cur32, x, nc, n);
+        if (csplit) k_prolong_split<true, true><<<cg, blk, 0, s>>>(C.cur32, x, nc, gc.half, n, g.half);
+        else k_prolong_split<false, true><<<cg, blk, 0, s>>>(C.cur32, x, nc, gc.half, n, g.half);
     }
     ctx_.count_launch();
-    for (int sw = 0; sw < post_; ++sw) sweep(1, false);
-    out_z();
+    for (int sw = 0; sw < post_; ++sw) sweep(1, false, sw == post_ - 1);
+    if (z && post_ == 0) out_z();
     ctx_.check_launch("mg cycle (fp32)");
 }
 
@@ -303,8 +329,18 @@ void PoissonMG::apply(const double* r, double* z) {
         z0_ = nullptr;
         cycle<double>(0);
     } else {
-        if (L0.n & 1) k_scale_in32_split<<<ew_grid(ctx_, N), 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, (float)L0.inv, N);
-        else k_scale_in32<<<ew_grid(ctx_, N), 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, (float)L0.inv, N);
+        if (L0.n & 1) {
+            const Split g = make_split(L0.n);
+            const unsigned grid = ew_grid(ctx_, (size_t)g.half);
+            if (first_fused32(0))
+                k_scale_in32_split<true><<<grid, 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, L0.x32.p,
+                                                                        (float)L0.inv, (int)N, g.half);
+            else
+                k_scale_in32_split<false><<<grid, 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, L0.x32.p,
+                                                                         (float)L0.inv, (int)N, g.half);
+        } else {
+            k_scale_in32<<<ew_grid(ctx_, N), 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, (float)L0.inv, N);
+        }
         ctx_.count_launch();
         z0_ = z;
         cycle32(0);
@@ -333,12 +369,14 @@ double PoissonMG::time_finest_pass(int reps) {
         NUMA_CUDA(cudaEventRecord(b, ctx_.stream));
         NUMA_CUDA(cudaEventSynchronize(b));
     } else {
-        // the FP32 cycle's dominant kernel: one colour pass on the split layout
+        // the FP32 cycle's dominant kernel: one colour pass on the split layout (odd n)
+        if (!(n & 1)) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "the FP32 pass timing needs an odd grid");
         NUMA_CUDA(cudaMemsetAsync(L0.x32.p, 0, N * sizeof(float), ctx_.stream));
         NUMA_CUDA(cudaMemsetAsync(L0.bs32.p, 0, N * sizeof(float), ctx_.stream));
-        k_rbgs_split<false><<<cgrid, blk, 0, ctx_.stream>>>(L0.x32.p, L0.bs32.p, n, 0);
+        const Split g = make_split(n);
+        launch_pass_split<kPassFull>(L0.x32.p, L0.bs32.p, nullptr, g, 0, ctx_.stream);
         NUMA_CUDA(cudaEventRecord(a, ctx_.stream));
-        for (int r = 0; r < reps; ++r) k_rbgs_split<false><<<cgrid, blk, 0, ctx_.stream>>>(L0.x32.p, L0.bs32.p, n, r & 1);
+        for (int r = 0; r < reps; ++r) launch_pass_split<kPassFull>(L0.x32.p, L0.bs32.p, nullptr, g, r & 1, ctx_.stream);
         NUMA_CUDA(cudaEventRecord(b, ctx_.stream));
         NUMA_CUDA(cudaEventSynchronize(b));
     }

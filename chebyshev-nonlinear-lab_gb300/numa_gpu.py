@@ -153,6 +153,7 @@ SIGNATURES = {
     "numa_gpu_mg_apply_noalloc": ([_SZ, _I, _I, _P, _P, _P], _I),
     "numa_gpu_diag_fp64_peak": ([_P, _F64P], _I),
     "numa_gpu_diag_time_smoother": ([_P, _I, _F64P], _I),
+    "numa_gpu_diag_exp": ([_P, _P, _P], _I),
 }
 
 _lib = None
@@ -623,6 +624,11 @@ def mg_apply_noalloc(n: int, r: Vec, z: Vec, pre: int = 2, post: int = 2, stream
     s = r.ctx.stream() if stream is None else stream
     return r.lib.numa_gpu_mg_apply_noalloc(n, pre, post, C.c_void_p(r.device_ptr()), C.c_void_p(z.device_ptr()),
                                           C.c_void_p(s))
+
+
+def diag_exp(x: "Vec", out: "Vec", cuda_ref: "Vec | None" = None):
+    """out = the library's FP64 e^x (table-driven, as in the residual kernels); cuda_ref = CUDA's exp."""
+    x.ctx.check(x.lib.numa_gpu_diag_exp(x.h, out.h, cuda_ref.h if cuda_ref is not None else None), "diag_exp")
 
 
 def forcing(params: KrylovParams, k: int, rnorm: float, rprev: float, eta_prev: float, res0: float) -> float:

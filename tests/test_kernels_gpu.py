@@ -187,3 +187,36 @@ def test_max_levels_extension(gpu, oracle):
     dz = gpu.vec(31 ** 3)
     mg(gpu.from_numpy(make_point(31 ** 3, 1.0)), dz)
     assert np.all(np.isfinite(dz.numpy()))
+
+
+def _ulp_diff(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """|a - b| in units of the last place, for finite positive doubles (ordered bit patterns)."""
+    ia, ib = a.view(np.int64), b.view(np.int64)
+    return np.abs(ia - ib)
+
+
+def test_exp_table_driven(gpu):
+    """The residual kernels' e^x (Tang's table-driven method) against the host C library and
+    CUDA's exp: within 1 ulp everywhere, exact at the special values."""
+    import numa_gpu as G
+    rng = np.random.default_rng(1234)
+    x = np.concatenate([
+        rng.uniform(-707.9, 707.9, 600_000),
+        rng.uniform(-2.0, 2.0, 600_000),            # the Bratu range
+        rng.uniform(-1e-6, 1e-6, 50_000),
+        np.arange(-22000, 22000) * (np.log(2) / 32),  # table boundaries
+        np.array([0.0, -0.0, 1e-300, -1e-300, 707.99, -707.99, 708.0, -708.0, 709.7, -745.2, -746.0, 710.0,
+                  np.inf, -np.inf, np.nan]),
+    ])
+    xv, out, ref = gpu.from_numpy(x), gpu.vec(x.size), gpu.vec(x.size)
+    G.diag_exp(xv, out, ref)
+    got, cuda = out.numpy(), ref.numpy()
+    host = np.exp(x)
+    fin = np.isfinite(host) & (host > 0) & (host >= np.finfo(float).tiny)
+    assert _ulp_diff(got[fin], host[fin]).max() <= 1
+    assert _ulp_diff(got[fin], cuda[fin]).max() <= 2
+    # most results are correctly rounded (equal to the host's)
+    assert np.mean(got[fin] == host[fin]) > 0.99
+    special = ~fin
+    assert np.array_equal(got[special], cuda[special], equal_nan=True)
+    assert np.all(got[x == 0.0] == 1.0)
