@@ -217,9 +217,11 @@ enum SplitPass { kPassFull = 0, kPassFirst = 1, kPassLastZ = 2 };
 // One colour pass of red-black Gauss-Seidel on the split layout, with the per-point arithmetic
 // of k_rbgs<float> (b h^2 plus the six neighbours in the order i-1, i+1, j-1, j+1, k-1, k+1, then
 // / 6).  A thread owns the k-pair {2kk, 2kk+1} of row j and marches over ICH planes; its point of
-// colour c alternates between the two members from plane to plane.  The colour halves are
-// separate restrict pointers (they never overlap), so the loads of all ICH planes can be in
-// flight together.
+// colour c alternates between the two members from plane to plane.  The level arrays are padded
+// (x by more than a colour plane on each side, b h^2 at the end), so every load is issued
+// unconditionally: first all loads of the ICH planes, then the arithmetic, with a select putting
+// +0.0 in place of a neighbour outside the grid.  The colour halves are separate restrict
+// pointers (they never overlap).
 //   kPassFirst: x is zero before the pass, x = bs / 6.
 //   kPassLastZ: the final pass of the cycle: x is not stored; z (FP64, natural layout) receives
 //               both members of the pair (the other member holds its value from the previous pass).
@@ -235,50 +237,52 @@ __global__ void __launch_bounds__(BX* BY) k_pass_split(float* __restrict__ own, 
     const int P = n * n;
     const int o_km = c - 1, o_kp = c, o_jm = c - g.hn - 1, o_jp = c + g.hn, o_im = c - g.hP - 1, o_ip = c + g.hP;
     const bool jlo = j > 0, jhi = j + 1 < n;
-    int k = 2 * kk + ((i0 + j + c) & 1);
-    int L = (i0 * n + j) * n + k;
+    const int kA = 2 * kk + ((i0 + j + c) & 1);  // the point's k on planes i0, i0 + 2, ...
+    const int LA = (i0 * n + j) * n + kA;
+    float bv[ICH], v_im[ICH], v_ip[ICH], v_jm[ICH], v_jp[ICH], v_km[ICH], v_kp[ICH];
+#pragma unroll
+    for (int s = 0; s < ICH; ++s) {
+        const int k = (s & 1) ? (kA ^ 1) : kA;
+        const int L = LA + s * P + (k - kA);
+        const int m = (i0 + s < n) ? (L >> 1) : 0;  // planes past the grid load harmlessly
+        bv[s] = bown[m];
+        if (MODE != kPassFirst) {
+            v_im[s] = oth[m + o_im];
+            v_ip[s] = oth[m + o_ip];
+            v_jm[s] = oth[m + o_jm];
+            v_jp[s] = oth[m + o_jp];
+            v_km[s] = oth[m + o_km];
+            v_kp[s] = oth[m + o_kp];
+        }
+    }
 #pragma unroll
     for (int s = 0; s < ICH; ++s) {
         const int i = i0 + s;
         if (i >= n) break;
+        const int k = (s & 1) ? (kA ^ 1) : kA;
+        const int L = LA + s * P + (k - kA);
         const int m = L >> 1;
-        const bool valid = k < n;
         if (MODE == kPassLastZ) {
             const int ko = k ^ 1;
-            if (ko < n) z[L - k + ko] = f32_to_f64(oth[m + (ko > k ? o_kp : o_km)]);
+            if (ko < n) z[L - k + ko] = f32_to_f64(ko > k ? v_kp[s] : v_km[s]);
         }
-        if (valid) {
+        if (k < n) {
             float v;
             if (MODE == kPassFirst) {
-                v = div6(bown[m]);
+                v = div6(bv[s]);
             } else {
-                float acc = bown[m], t;
-                t = 0.0f;
-                if (i > 0) t = oth[m + o_im];
-                acc = acc + t;
-                t = 0.0f;
-                if (i + 1 < n) t = oth[m + o_ip];
-                acc = acc + t;
-                t = 0.0f;
-                if (jlo) t = oth[m + o_jm];
-                acc = acc + t;
-                t = 0.0f;
-                if (jhi) t = oth[m + o_jp];
-                acc = acc + t;
-                t = 0.0f;
-                if (k > 0) t = oth[m + o_km];
-                acc = acc + t;
-                t = 0.0f;
-                if (k + 1 < n) t = oth[m + o_kp];
-                acc = acc + t;
+                float acc = bv[s];
+                acc = acc + ((i > 0) ? v_im[s] : 0.0f);
+                acc = acc + ((i + 1 < n) ? v_ip[s] : 0.0f);
+                acc = acc + (jlo ? v_jm[s] : 0.0f);
+                acc = acc + (jhi ? v_jp[s] : 0.0f);
+                acc = acc + ((k > 0) ? v_km[s] : 0.0f);
+                acc = acc + ((k + 1 < n) ? v_kp[s] : 0.0f);
                 v = div6(acc);
             }
             if (MODE == kPassLastZ) z[L] = f32_to_f64(v);
             else own[m] = v;
         }
-        const int kn = k ^ 1;
-        L += P + (kn - k);
-        k = kn;
     }
 }
 
@@ -301,69 +305,71 @@ inline void launch_pass_split(float* x, const float* bs, double* z, const Split&
 
 // r (natural layout) = b - h^-2 (6x - sum of neighbours) with x and b split: the order of
 // k_residual (6x, then - i-1, - i+1, - j-1, - j+1, - k-1, - k+1).  A thread owns the k-pair
-// {2kk, 2kk+1} of row j (colours cA and 1 - cA) and marches over ichunk planes.
+// {2kk, 2kk+1} of row j (colours cA and 1 - cA) and marches over ICH planes; as in k_pass_split the
+// padded arrays let every load be issued unconditionally, and selects replace the neighbours
+// outside the grid by +0.0.
+template <int ICH>
 __global__ void __launch_bounds__(BX* BY) k_residual_split(const float* __restrict__ x, const float* __restrict__ b,
-                                                           float* __restrict__ r, Split g, int ichunk, float h2inv) {
+                                                           float* __restrict__ r, Split g, float h2inv) {
     const int kk = blockIdx.x * BX + threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
     const int n = g.n;
     if (j >= n || 2 * kk >= n) return;
-    const int i0 = blockIdx.z * ichunk;
-    const int i1 = min(i0 + ichunk, n);
+    const int i0 = blockIdx.z * ICH;
     const int P = n * n;
     const bool jlo = j > 0, jhi = j + 1 < n, hasB = 2 * kk + 1 < n, kloA = kk > 0, khiB = 2 * kk + 2 < n;
-    int LA = (i0 * n + j) * n + 2 * kk;
-    for (int i = i0; i < i1; ++i, LA += P) {
-        const int cA = (i + j) & 1, cB = cA ^ 1;
+    const int LA0 = (i0 * n + j) * n + 2 * kk;
+    float xa[ICH], xb[ICH], ba[ICH], bb[ICH];
+    float a_im[ICH], a_ip[ICH], a_jm[ICH], a_jp[ICH], a_km[ICH];
+    float b_im[ICH], b_ip[ICH], b_jm[ICH], b_jp[ICH], b_kp[ICH];
+#pragma unroll
+    for (int s = 0; s < ICH; ++s) {
+        const int cA = (i0 + s + j) & 1, cB = cA ^ 1;
+        const int LA = (i0 + s < n) ? LA0 + s * P : 0;  // planes past the grid load harmlessly
+        const int mA = LA >> 1, mB = (LA + 1) >> 1;
+        const float* ownA = x + (cA ? g.half : 0);  // colour cA = B's other colour
+        const float* othA = x + (cA ? 0 : g.half);  // colour cB = A's other colour
+        xa[s] = ownA[mA];
+        xb[s] = othA[mA + cA];
+        ba[s] = b[(cA ? g.half : 0) + mA];
+        bb[s] = b[(cB ? g.half : 0) + mB];
+        a_im[s] = othA[mA + cA - g.hP - 1];
+        a_ip[s] = othA[mA + cA + g.hP];
+        a_jm[s] = othA[mA + cA - g.hn - 1];
+        a_jp[s] = othA[mA + cA + g.hn];
+        a_km[s] = othA[mA + cA - 1];
+        b_im[s] = ownA[mB + cB - g.hP - 1];
+        b_ip[s] = ownA[mB + cB + g.hP];
+        b_jm[s] = ownA[mB + cB - g.hn - 1];
+        b_jp[s] = ownA[mB + cB + g.hn];
+        b_kp[s] = ownA[mB + cB];
+    }
+#pragma unroll
+    for (int s = 0; s < ICH; ++s) {
+        const int i = i0 + s;
+        if (i >= n) break;
         const bool ilo = i > 0, ihi = i + 1 < n;
-        // member A: k = 2kk, colour cA; its other-colour neighbours live in half cB
-        const float* ownA = x + (cA ? g.half : 0);
-        const float* othA = x + (cA ? 0 : g.half);
-        const int mA = LA >> 1;
-        const float xa = ownA[mA];
-        float xb = 0.0f;
-        if (hasB) xb = othA[mA + cA];  // member B (k = 2kk + 1) lives in A's other half
+        const int LA = LA0 + s * P;
+        const float xbv = hasB ? xb[s] : 0.0f;
         {
-            float s = 6.0f * xa, t;
-            t = 0.0f;
-            if (ilo) t = othA[mA + cA - g.hP - 1];
-            s = s - t;
-            t = 0.0f;
-            if (ihi) t = othA[mA + cA + g.hP];
-            s = s - t;
-            t = 0.0f;
-            if (jlo) t = othA[mA + cA - g.hn - 1];
-            s = s - t;
-            t = 0.0f;
-            if (jhi) t = othA[mA + cA + g.hn];
-            s = s - t;
-            t = 0.0f;
-            if (kloA) t = othA[mA + cA - 1];
-            s = s - t;
-            s = s - xb;
-            r[LA] = b[(cA ? g.half : 0) + mA] - h2inv * s;
+            float t = 6.0f * xa[s];
+            t = t - (ilo ? a_im[s] : 0.0f);
+            t = t - (ihi ? a_ip[s] : 0.0f);
+            t = t - (jlo ? a_jm[s] : 0.0f);
+            t = t - (jhi ? a_jp[s] : 0.0f);
+            t = t - (kloA ? a_km[s] : 0.0f);
+            t = t - xbv;
+            r[LA] = ba[s] - h2inv * t;
         }
         if (hasB) {
-            const int LB = LA + 1, mB = LB >> 1;
-            const float* othB = ownA;  // B's other colour is cA
-            float s = 6.0f * xb, t;
-            t = 0.0f;
-            if (ilo) t = othB[mB + cB - g.hP - 1];
-            s = s - t;
-            t = 0.0f;
-            if (ihi) t = othB[mB + cB + g.hP];
-            s = s - t;
-            t = 0.0f;
-            if (jlo) t = othB[mB + cB - g.hn - 1];
-            s = s - t;
-            t = 0.0f;
-            if (jhi) t = othB[mB + cB + g.hn];
-            s = s - t;
-            s = s - xa;
-            t = 0.0f;
-            if (khiB) t = othB[mB + cB];
-            s = s - t;
-            r[LB] = b[(cB ? g.half : 0) + mB] - h2inv * s;
+            float t = 6.0f * xbv;
+            t = t - (ilo ? b_im[s] : 0.0f);
+            t = t - (ihi ? b_ip[s] : 0.0f);
+            t = t - (jlo ? b_jm[s] : 0.0f);
+            t = t - (jhi ? b_jp[s] : 0.0f);
+            t = t - xa[s];
+            t = t - (khiB ? b_kp[s] : 0.0f);
+            r[LA + 1] = bb[s] - h2inv * t;
         }
     }
 }
@@ -501,6 +507,180 @@ __global__ void k_scale_in32_split(const double* __restrict__ r, float* __restri
 __global__ void k_to64_split(const float* __restrict__ x, double* __restrict__ z, int N, int half) {
     const int stride = gridDim.x * blockDim.x;
     for (int L = blockIdx.x * blockDim.x + threadIdx.x; L < N; L += stride) z[L] = f32_to_f64(x[split_at(L, half)]);
+}
+
+// ------------------------------------------------------------------------------------------
+// The tail of a V-cycle in one CTA: every level from lb (n <= 15) down to the coarsest, with all
+// arrays in shared memory (natural layout) and __syncthreads() between passes instead of one
+// kernel launch per pass.  The arithmetic of each step is that of the per-level kernels above
+// (colour pass, residual, restriction, prolongation, single-point solve), so the result is the
+// same as the launched sequence.  Level lb's b and b h^2 come from global memory (split layout
+// when SPLIT_IO) and its x goes back there for the prolongation into the level above.
+constexpr int kMaxTail = 6;
+struct TailParams {
+    int levels;                  // levels handled: lb .. lb + levels - 1 (the coarsest)
+    int n[kMaxTail];
+    double h2inv[kMaxTail];      // h^-2 of each level
+    double inv[kMaxTail];        // 1 / h^-2 of each level (b h^2 = b * inv)
+    double six_h2inv[kMaxTail];  // 6 h^-2 (single-point solve)
+    int pre, post;
+    int half;                    // split geometry of level lb (SPLIT_IO)
+};
+
+template <class T>
+__device__ void tail_pass(T* __restrict__ x, const T* __restrict__ bs, int n, int c, bool first) {
+    const int np = (n + 1) / 2, total = n * n * np, P = n * n;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int kk = t % np, row = t / np, j = row % n, i = row / n;
+        const int k = 2 * kk + ((i + j + c) & 1);
+        if (k >= n) continue;
+        const int p = (i * n + j) * n + k;
+        T v;
+        if (first) {
+            v = div6(bs[p]);
+        } else {
+            T acc = bs[p];
+            acc = acc + ((i > 0) ? x[p - P] : zero<T>());
+            acc = acc + ((i + 1 < n) ? x[p + P] : zero<T>());
+            acc = acc + ((j > 0) ? x[p - n] : zero<T>());
+            acc = acc + ((j + 1 < n) ? x[p + n] : zero<T>());
+            acc = acc + ((k > 0) ? x[p - 1] : zero<T>());
+            acc = acc + ((k + 1 < n) ? x[p + 1] : zero<T>());
+            v = div6(acc);
+        }
+        x[p] = v;
+    }
+    __syncthreads();
+}
+
+template <class T>
+__device__ void tail_residual(const T* __restrict__ x, const T* __restrict__ b, T* __restrict__ r, int n, T h2inv) {
+    const int N = n * n * n, P = n * n;
+    for (int p = threadIdx.x; p < N; p += blockDim.x) {
+        const int k = p % n, j = (p / n) % n, i = p / P;
+        T s = T(6) * x[p];
+        s = s - ((i > 0) ? x[p - P] : zero<T>());
+        s = s - ((i + 1 < n) ? x[p + P] : zero<T>());
+        s = s - ((j > 0) ? x[p - n] : zero<T>());
+        s = s - ((j + 1 < n) ? x[p + n] : zero<T>());
+        s = s - ((k > 0) ? x[p - 1] : zero<T>());
+        s = s - ((k + 1 < n) ? x[p + 1] : zero<T>());
+        r[p] = b[p] - h2inv * s;
+    }
+    __syncthreads();
+}
+
+template <class T>
+__device__ void tail_restrict(const T* __restrict__ rf, T* __restrict__ bc, T* __restrict__ bsc, int nf, int nc,
+                              T inv_c) {
+    const int Nc = nc * nc * nc;
+    const T w[3] = {T(0.25), T(0.5), T(0.25)};
+    for (int q = threadIdx.x; q < Nc; q += blockDim.x) {
+        const int K = q % nc, J = (q / nc) % nc, I = q / (nc * nc);
+        T acc = zero<T>();
+        for (int a = 0; a < 3; ++a) {
+            const int fi = 2 * I + a;
+            if (fi >= nf) continue;
+            for (int bb = 0; bb < 3; ++bb) {
+                const int fj = 2 * J + bb;
+                if (fj >= nf) continue;
+                const T wab = w[a] * w[bb];
+                for (int c = 0; c < 3; ++c) {
+                    const int fk = 2 * K + c;
+                    if (fk >= nf) continue;
+                    acc = fma_t(wab * w[c], rf[(fi * nf + fj) * nf + fk], acc);
+                }
+            }
+        }
+        bc[q] = acc;
+        bsc[q] = acc * inv_c;
+    }
+    __syncthreads();
+}
+
+template <class T>
+__device__ void tail_prolong(const T* __restrict__ xc, T* __restrict__ xf, int nc, int nf, bool colour0_only) {
+    const int Nf = nf * nf * nf;
+    for (int p = threadIdx.x; p < Nf; p += blockDim.x) {
+        const int k = p % nf, j = (p / nf) % nf, i = p / (nf * nf);
+        if (colour0_only && ((i + j + k) & 1)) continue;
+        int ci[2], cj[2], ck[2];
+        const int ni = interp(i, nc, ci), nj = interp(j, nc, cj), nk = interp(k, nc, ck);
+        const T wi = (ni == 1 && (i & 1)) ? T(1) : T(0.5);
+        const T wj = (nj == 1 && (j & 1)) ? T(1) : T(0.5);
+        const T wk = (nk == 1 && (k & 1)) ? T(1) : T(0.5);
+        T acc = zero<T>();
+        for (int a = 0; a < ni; ++a)
+            for (int bb = 0; bb < nj; ++bb)
+                for (int c = 0; c < nk; ++c) acc = fma_t(wi * wj * wk, xc[(ci[a] * nc + cj[bb]) * nc + ck[c]], acc);
+        xf[p] = xf[p] + acc;
+    }
+    __syncthreads();
+}
+
+template <class T, bool SPLIT_IO>
+__global__ void __launch_bounds__(512) k_mg_tail(const T* __restrict__ b_g, const T* __restrict__ bs_g,
+                                                 T* __restrict__ x_g, TailParams tp) {
+    extern __shared__ __align__(16) unsigned char tail_smem[];
+    T* base = reinterpret_cast<T*>(tail_smem);
+    T *X[kMaxTail], *B[kMaxTail], *BS[kMaxTail];
+    int off = 0;
+    for (int l = 0; l < tp.levels; ++l) {
+        const int Nl = tp.n[l] * tp.n[l] * tp.n[l];
+        X[l] = base + off;
+        B[l] = base + off + Nl;
+        BS[l] = base + off + 2 * Nl;
+        off += 3 * Nl;
+    }
+    T* R = base + off;  // residual scratch, the size of level lb
+    {
+        const int n = tp.n[0], N = n * n * n;
+        for (int p = threadIdx.x; p < N; p += blockDim.x) {
+            const int q = SPLIT_IO ? split_at(p, tp.half) : p;
+            B[0][p] = b_g[q];
+            BS[0][p] = bs_g[q];
+        }
+        __syncthreads();
+    }
+    const int last = tp.levels - 1;
+    for (int l = 0; l < last; ++l) {  // down: pre-smoothing, residual, restriction
+        const int n = tp.n[l];
+        for (int sw = 0; sw < tp.pre; ++sw) {
+            tail_pass<T>(X[l], BS[l], n, 0, sw == 0);
+            tail_pass<T>(X[l], BS[l], n, 1, false);
+        }
+        if (tp.pre == 0) {
+            for (int p = threadIdx.x; p < n * n * n; p += blockDim.x) X[l][p] = zero<T>();
+            __syncthreads();
+        }
+        tail_residual<T>(X[l], B[l], R, n, (T)tp.h2inv[l]);
+        tail_restrict<T>(R, B[l + 1], BS[l + 1], n, tp.n[l + 1], (T)tp.inv[l + 1]);
+    }
+    {  // coarsest
+        const int n = tp.n[last];
+        if (n == 1) {
+            if (threadIdx.x == 0) X[last][0] = (T)((double)B[last][0] / tp.six_h2inv[last]);
+            __syncthreads();
+        } else {
+            for (int sw = 0; sw < 30; ++sw) {
+                const int c0 = (sw % 2 == 0) ? 0 : 1;
+                tail_pass<T>(X[last], BS[last], n, c0, sw == 0);
+                tail_pass<T>(X[last], BS[last], n, 1 - c0, false);
+            }
+        }
+    }
+    for (int l = last - 1; l >= 0; --l) {  // up: prolongation, post-smoothing
+        const int n = tp.n[l];
+        tail_prolong<T>(X[l + 1], X[l], tp.n[l + 1], n, tp.post > 0);
+        for (int sw = 0; sw < tp.post; ++sw) {
+            tail_pass<T>(X[l], BS[l], n, 1, false);
+            tail_pass<T>(X[l], BS[l], n, 0, false);
+        }
+    }
+    {
+        const int n = tp.n[0], N = n * n * n;
+        for (int p = threadIdx.x; p < N; p += blockDim.x) x_g[SPLIT_IO ? split_at(p, tp.half) : p] = X[0][p];
+    }
 }
 
 }  // namespace

@@ -170,6 +170,10 @@ private:
     template <class T> void cycle(size_t l);
     void cycle32(size_t l);
     bool first_fused32(size_t l) const;
+    // FP32 cycle: levels from tail_l_ (n <= 15) down run in one CTA (k_mg_tail); SIZE_MAX = none.
+    size_t tail_l_ = SIZE_MAX;
+    size_t tail_smem_ = 0;
+    void launch_tail32();
     // The levels below the finest touch only the hierarchy's own arrays, so their part of the
     // cycle is captured once into a CUDA graph and replayed (one launch instead of ~10 a level).
     void coarse_cycle();

@@ -33,6 +33,7 @@ struct PoissonMG::Level {
     double inv = 0.0;  // 1.0 / h2inv, as the reference forms it (poisson_mg.hpp:101)
     DeviceArray<double> x64, b64, bs64;
     DeviceArray<float> x32, b32, bs32;  // FP32 cycle (colour-split layout when n is odd)
+    float* xs = nullptr;                // x32 past its front padding: the level's FP32 x
     float* cur32 = nullptr;             // the FP32 iterate of this level
 };
 
@@ -40,7 +41,7 @@ namespace {
 
 template <class T> T* xp(PoissonMG::Level& L);
 template <> double* xp<double>(PoissonMG::Level& L) { return L.x64.p; }
-template <> float* xp<float>(PoissonMG::Level& L) { return L.x32.p; }
+template <> float* xp<float>(PoissonMG::Level& L) { return L.xs; }
 template <class T> T* bp(PoissonMG::Level& L);
 template <> double* bp<double>(PoissonMG::Level& L) { return L.b64.p; }
 template <> float* bp<float>(PoissonMG::Level& L) { return L.b32.p; }
@@ -85,9 +86,14 @@ PoissonMG::PoissonMG(Context& ctx, size_t n, int pre, int post, int precision, i
                 L->b64.resize(Nl);
             }
         } else {
-            L->x32.resize(Nl);
-            L->b32.resize(Nl);
-            L->bs32.resize(Nl);
+            // x is padded by more than one plane of a colour on both sides, b and b h^2 at the end:
+            // the FP32 kernels load every neighbour unconditionally (boundary values are then
+            // replaced by zero with a select), and no load leaves the allocation
+            const size_t pad = ((m * m - 1) / 2 + m + 2 + 31) / 32 * 32;
+            L->x32.resize(Nl + 2 * pad);
+            L->xs = L->x32.p + pad;
+            L->b32.resize(Nl + 64);
+            L->bs32.resize(Nl + 64);
         }
         levels_.push_back(std::move(L));
         if (m % 2 == 0 || m <= 1) break;
@@ -99,6 +105,45 @@ PoissonMG::PoissonMG(Context& ctx, size_t n, int pre, int post, int precision, i
         if (precision == NUMA_GPU_FP64) scratch_r_.resize(N0_);
         else scratch_r_.resize((N0_ + 1) / 2);  // N0 floats
     }
+    // FP32: the levels of n <= 15 below the finest run as one CTA with shared-memory arrays
+    if (precision == NUMA_GPU_FP32) {
+        for (size_t l = 1; l < levels_.size(); ++l) {
+            if (levels_[l]->n > 15) continue;
+            if (levels_.size() - l > (size_t)kMaxTail) break;
+            size_t elems = 0;
+            for (size_t m = l; m < levels_.size(); ++m) elems += 3 * (size_t)levels_[m]->n * levels_[m]->n * levels_[m]->n;
+            elems += (size_t)levels_[l]->n * levels_[l]->n * levels_[l]->n;
+            tail_smem_ = elems * sizeof(float);
+            NUMA_CUDA(cudaFuncSetAttribute(k_mg_tail<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)tail_smem_));
+            NUMA_CUDA(cudaFuncSetAttribute(k_mg_tail<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)tail_smem_));
+            tail_l_ = l;
+            break;
+        }
+    }
+}
+
+void PoissonMG::launch_tail32() {
+    Level& L = *levels_[tail_l_];
+    TailParams tp{};
+    tp.levels = (int)(levels_.size() - tail_l_);
+    for (int m = 0; m < tp.levels; ++m) {
+        const Level& M = *levels_[tail_l_ + m];
+        tp.n[m] = M.n;
+        tp.h2inv[m] = M.h2inv;
+        tp.inv[m] = M.inv;
+        tp.six_h2inv[m] = 6.0 * M.h2inv;
+    }
+    tp.pre = pre_;
+    tp.post = post_;
+    const bool split = (L.n & 1) != 0;
+    tp.half = split ? make_split(L.n).half : 0;
+    if (split) k_mg_tail<float, true><<<1, 512, tail_smem_, ctx_.stream>>>(L.b32.p, L.bs32.p, L.xs, tp);
+    else k_mg_tail<float, false><<<1, 512, tail_smem_, ctx_.stream>>>(L.b32.p, L.bs32.p, L.xs, tp);
+    ctx_.count_launch();
+    L.cur32 = L.xs;
+    ctx_.check_launch("mg tail (fp32)");
 }
 
 PoissonMG::~PoissonMG() {
@@ -217,12 +262,16 @@ void PoissonMG::cycle(size_t l) {
 // True when level l's first smoothing pass is fused into the producer of its right-hand side.
 bool PoissonMG::first_fused32(size_t l) const {
     const Level& L = *levels_[l];
-    if (!(L.n & 1)) return false;
+    if (!(L.n & 1) || l == tail_l_) return false;
     if (l + 1 == levels_.size()) return L.n > 1;  // coarsest: 30 sweeps, the first from x = 0
     return pre_ > 0;
 }
 
 void PoissonMG::cycle32(size_t l) {
+    if (l == tail_l_) {
+        launch_tail32();
+        return;
+    }
     Level& L = *levels_[l];
     const int n = L.n;
     const bool finest = (l == 0);
@@ -230,7 +279,7 @@ void PoissonMG::cycle32(size_t l) {
     double* z = finest ? z0_ : nullptr;
     cudaStream_t s = ctx_.stream;
     const size_t Nl = (size_t)n * n * n;
-    float* x = L.x32.p;
+    float* x = L.xs;
     const float* b = L.b32.p;
     const float* bs = L.bs32.p;
     const dim3 blk(BX, BY);
@@ -280,7 +329,8 @@ void PoissonMG::cycle32(size_t l) {
     float* r = reinterpret_cast<float*>(scratch_r_.p);
     {
         const dim3 rgd(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, (n + ich - 1) / ich);
-        k_residual_split<<<rgd, blk, 0, s>>>(x, b, r, g, ich, (float)L.h2inv);
+        if (ich == 4) k_residual_split<4><<<rgd, blk, 0, s>>>(x, b, r, g, (float)L.h2inv);
+        else k_residual_split<1><<<rgd, blk, 0, s>>>(x, b, r, g, (float)L.h2inv);
         ctx_.count_launch();
     }
     Level& C = *levels_[l + 1];
@@ -289,9 +339,9 @@ void PoissonMG::cycle32(size_t l) {
     const Split gc = make_split(nc);
     const dim3 rg((nc + BX - 1) / BX, (nc + BY - 1) / BY, nc);
     if (csplit && first_fused32(l + 1))
-        k_restrict_split<true><<<rg, blk, 0, s>>>(r, C.b32.p, C.bs32.p, C.x32.p, n, nc, gc.half, (float)C.inv);
+        k_restrict_split<true><<<rg, blk, 0, s>>>(r, C.b32.p, C.bs32.p, C.xs, n, nc, gc.half, (float)C.inv);
     else if (csplit)
-        k_restrict_split<false><<<rg, blk, 0, s>>>(r, C.b32.p, C.bs32.p, C.x32.p, n, nc, gc.half, (float)C.inv);
+        k_restrict_split<false><<<rg, blk, 0, s>>>(r, C.b32.p, C.bs32.p, C.xs, n, nc, gc.half, (float)C.inv);
     else
         k_restrict<float><<<rg, blk, 0, s>>>(r, C.b32.p, C.bs32.p, n, nc, C.inv);
     ctx_.count_launch();
@@ -333,10 +383,10 @@ void PoissonMG::apply(const double* r, double* z) {
             const Split g = make_split(L0.n);
             const unsigned grid = ew_grid(ctx_, (size_t)g.half);
             if (first_fused32(0))
-                k_scale_in32_split<true><<<grid, 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, L0.x32.p,
+                k_scale_in32_split<true><<<grid, 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, L0.xs,
                                                                         (float)L0.inv, (int)N, g.half);
             else
-                k_scale_in32_split<false><<<grid, 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, L0.x32.p,
+                k_scale_in32_split<false><<<grid, 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, L0.xs,
                                                                          (float)L0.inv, (int)N, g.half);
         } else {
             k_scale_in32<<<ew_grid(ctx_, N), 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, (float)L0.inv, N);
@@ -371,12 +421,12 @@ double PoissonMG::time_finest_pass(int reps) {
     } else {
         // the FP32 cycle's dominant kernel: one colour pass on the split layout (odd n)
         if (!(n & 1)) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "the FP32 pass timing needs an odd grid");
-        NUMA_CUDA(cudaMemsetAsync(L0.x32.p, 0, N * sizeof(float), ctx_.stream));
+        NUMA_CUDA(cudaMemsetAsync(L0.xs, 0, N * sizeof(float), ctx_.stream));
         NUMA_CUDA(cudaMemsetAsync(L0.bs32.p, 0, N * sizeof(float), ctx_.stream));
         const Split g = make_split(n);
-        launch_pass_split<kPassFull>(L0.x32.p, L0.bs32.p, nullptr, g, 0, ctx_.stream);
+        launch_pass_split<kPassFull>(L0.xs, L0.bs32.p, nullptr, g, 0, ctx_.stream);
         NUMA_CUDA(cudaEventRecord(a, ctx_.stream));
-        for (int r = 0; r < reps; ++r) launch_pass_split<kPassFull>(L0.x32.p, L0.bs32.p, nullptr, g, r & 1, ctx_.stream);
+        for (int r = 0; r < reps; ++r) launch_pass_split<kPassFull>(L0.xs, L0.bs32.p, nullptr, g, r & 1, ctx_.stream);
         NUMA_CUDA(cudaEventRecord(b, ctx_.stream));
         NUMA_CUDA(cudaEventSynchronize(b));
     }

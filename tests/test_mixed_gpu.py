@@ -123,7 +123,7 @@ def vcycle32(r64, n, pre=2, post=2):
     return cycle(0, b, bs).astype(np.float64).ravel()
 
 
-@pytest.mark.parametrize("n", [1, 3, 7, 15, 16, 21])
+@pytest.mark.parametrize("n", [1, 3, 7, 15, 16, 21, 23, 31, 63])
 def test_fp32_vcycle_bit_exact(gpu, n):
     G = _G()
     N = n ** 3
