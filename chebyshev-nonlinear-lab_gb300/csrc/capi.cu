@@ -34,6 +34,11 @@ struct numa_gpu_burgers2d {
     numa_gpu_ctx* ctx;
     std::unique_ptr<Burgers2D> impl;
 };
+struct numa_gpu_learned {
+    numa_gpu_ctx* ctx;
+    LearnedNet* impl;
+    ~numa_gpu_learned() { learned_destroy(impl); }
+};
 struct numa_gpu_hmg2d {
     numa_gpu_ctx* ctx;
     std::unique_ptr<HelmholtzMG2D> impl;
@@ -1087,6 +1092,68 @@ int numa_gpu_diag_exp(const numa_gpu_vec* x, numa_gpu_vec* out, numa_gpu_vec* cu
         }
         diag_exp(*x->ctx->impl, x->d, out->d, cuda_ref ? cuda_ref->d : nullptr, x->n);
     });
+}
+
+int numa_gpu_diag_conv3d(numa_gpu_ctx* ctx, size_t n, int cin, int cout, int adjoint, const float* x,
+                         const float* w, const float* bias, float* y) {
+    if (!ctx || !x || !w || !y) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(ctx, [&] {
+        need(n >= 1 && n <= 63, NUMA_GPU_ERR_INVALID_ARGUMENT, "grid size must be in 1..63");
+        diag_conv3d(*ctx->impl, (int)n, cin, cout, adjoint, x, w, bias, y);
+    });
+}
+
+// ------------------------------------------------------------------------------ learned preconditioner
+int numa_gpu_learned_create(numa_gpu_ctx* ctx, size_t n0, uint64_t seed, numa_gpu_learned** out) {
+    if (!ctx || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        auto h = std::make_unique<numa_gpu_learned>();
+        h->ctx = ctx;
+        h->impl = learned_create(*ctx->impl, (int)n0, seed);
+        *out = h.release();
+    });
+}
+
+int numa_gpu_learned_destroy(numa_gpu_learned* net) {
+    if (net) {
+        cudaStreamSynchronize(net->ctx->impl->stream);
+        delete net;
+    }
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_learned_num_params(const numa_gpu_learned* net, size_t* n) {
+    if (!net || !n) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *n = learned_num_params(*net->impl);
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_learned_get_params(numa_gpu_learned* net, float* host, size_t n) {
+    if (!net || !host) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(net->ctx, [&] {
+        need(n == learned_num_params(*net->impl), NUMA_GPU_ERR_SIZE_MISMATCH, "parameter count differs");
+        learned_get_params(*net->impl, host);
+    });
+}
+
+int numa_gpu_learned_set_params(numa_gpu_learned* net, const float* host, size_t n) {
+    if (!net || !host) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(net->ctx, [&] {
+        need(n == learned_num_params(*net->impl), NUMA_GPU_ERR_SIZE_MISMATCH, "parameter count differs");
+        learned_set_params(*net->impl, host);
+    });
+}
+
+int numa_gpu_learned_forward(numa_gpu_learned* net, const float* features, float* out) {
+    if (!net || !features || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(net->ctx, [&] { learned_forward_host(*net->ctx->impl, *net->impl, features, out); });
+}
+
+int numa_gpu_learned_gradient(numa_gpu_learned* net, const float* features, const float* target, float* loss,
+                              float* grad) {
+    if (!net || !features || !target || !loss || !grad) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(net->ctx, [&] { learned_grad_host(*net->ctx->impl, *net->impl, features, target, loss, grad); });
 }
 
 int numa_gpu_diag_time_smoother(numa_gpu_mg* mg, int reps, double* ms_per_pass) {

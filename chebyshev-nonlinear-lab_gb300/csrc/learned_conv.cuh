@@ -1,0 +1,264 @@
+// learned_conv.cuh — 3x3x3 convolutions of the learned preconditioner on the 5th-generation
+// tensor cores (tcgen05.mma, BF16 operands, FP32 accumulators in tensor memory).
+//
+// Activation layout ("8-channel planes"): a tensor of C channels on an n^3 grid is C/8 planes;
+// plane p holds channels 8p..8p+7 of every voxel of the zero-padded grid (n+2)^3 as one 16-byte
+// row per voxel, x fastest, with slack rows before and after (VoxGrid).  The halo is zero and
+// never written, so a convolution reads zeros outside the grid without a test.
+//
+// Implicit GEMM: a tile is 128 consecutive rows of the padded grid (M = 128, some rows are halo
+// and their outputs are dropped); the 27 taps are the same rows shifted by dz (n+2)^2 + dy (n+2)
+// + dx.  Each CTA copies, per tile, three spans of rows (one per dz) into shared memory; the A
+// operand of tap (dz, dy, dx) is then the span of dz started dy (n+2) + dx rows later, i.e. a
+// shared-memory descriptor with a shifted start address.  With 16-byte rows the span is in the
+// canonical no-swizzle K-major layout of the tensor cores: core matrices of 8 rows x 16 bytes
+// (stride-dimension offset 128 B), the two 8-channel halves of a 16-channel K step one plane
+// apart (leading-dimension offset = span bytes).  The weights of the layer stay in shared memory
+// for the whole kernel in the same layout (B operand, N = C_out rows).  One thread issues the
+// 27 * C_in/16 MMAs of a tile (K = 16 each) into a tensor-memory accumulator of 128 lanes x C_out
+// FP32 columns; tcgen05.commit signals an mbarrier; the four warps read their 32 lanes back with
+// tcgen05.ld and apply bias / ReLU / the BF16 conversion.
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+
+namespace numa::gpu {
+
+// Geometry of an n^3 grid in the 8-channel plane layout.
+struct VoxGrid {
+    int n;      // interior points per dimension
+    int np;     // n + 2
+    int pp;     // (n + 2)^2
+    int front;  // slack rows before the padded grid in each plane
+    int rows;   // rows per plane: front + (n+2)^3 + back
+    int span;   // rows of one shared-memory span: 128 + 2 (n + 2) + 2, rounded up to 8
+    int tiles;  // tiles of 128 rows covering the planes z = 1..n of the padded grid
+};
+
+inline VoxGrid make_voxgrid(int n) {
+    VoxGrid g;
+    g.n = n;
+    g.np = n + 2;
+    g.pp = g.np * g.np;
+    g.front = ((g.np + 2 + 63) / 64) * 64;
+    g.rows = g.front + g.np * g.pp + 256 + g.np + 64;
+    g.span = ((128 + 2 * g.np + 2 + 7) / 8) * 8;
+    g.tiles = (n * g.pp + 127) / 128;
+    return g;
+}
+
+// ------------------------------------------------------------------------------ PTX wrappers
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor (tcgen05), no swizzle: start address, leading-dimension byte
+// offset (between the core matrices along K), stride-dimension byte offset (between 8-row groups),
+// descriptor version 1.
+__device__ __forceinline__ uint64_t umma_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M x N.
+__host__ __device__ constexpr uint32_t umma_idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+// Waits for the phase of the given parity to complete; gives up after `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int limit) {
+    for (int i = 0; i < limit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Warp-wide: allocate / free `ncols` tensor-memory columns (power of two >= 32); the address goes
+// to *slot (shared memory).
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_free(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// 16 consecutive FP32 columns of this thread's tensor-memory lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// Shared memory of k_conv3d_tc: resident weights, then the three spans.
+template <int CIN, int COUT>
+__host__ __device__ constexpr size_t conv_weight_bytes() {
+    return (size_t)27 * (CIN / 16) * 2 * COUT * 16;
+}
+// The span region carries 16 spans of slack: even a reading of the A descriptor with its two byte
+// offsets exchanged (rows 8 apart by a span) stays inside the allocation.
+template <int CIN, int COUT>
+inline size_t conv_smem_bytes(const VoxGrid& g) {
+    return conv_weight_bytes<CIN, COUT>() + (size_t)(3 * (CIN / 8) + 16) * g.span * 16;
+}
+
+constexpr int kConvWaitLimit = 1 << 22;
+
+// out = act(conv(in) + bias) on the 8-channel plane layout, or (OUT32) FP32 channel-last output of
+// the interior voxels [((z-1) n + y-1) n + x-1][C_out] without activation.
+//   wg: the layer's BF16 weights in the B-operand layout [tap][k16 chunk][half][C_out][8].
+//   err: set to 1 when an mbarrier wait gives up (no tile after that is computed).
+template <int CIN, int COUT, bool OUT32>
+__global__ void __launch_bounds__(128) k_conv3d_tc(const uint4* __restrict__ in, const uint4* __restrict__ wg,
+                                                   const float* __restrict__ bias, uint4* __restrict__ out,
+                                                   float* __restrict__ out32, VoxGrid g, int relu,
+                                                   unsigned* __restrict__ err) {
+    static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT >= 16 && COUT <= 32, "channel counts");
+    constexpr int KC = CIN / 16, PL = CIN / 8;
+    constexpr uint32_t kCols = 32;
+    extern __shared__ __align__(128) unsigned char conv_smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    uint4* w_s = reinterpret_cast<uint4*>(conv_smem);
+    uint4* a_s = reinterpret_cast<uint4*>(conv_smem + conv_weight_bytes<CIN, COUT>());
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    for (int e = tid; e < (int)(conv_weight_bytes<CIN, COUT>() / 16); e += 128) w_s[e] = wg[e];
+    if (warp == 0) tmem_alloc(&tmem_slot, kCols);
+    if (tid == 0) mbar_init(smem_addr(&mbar), 1);
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t bar = smem_addr(&mbar);
+    constexpr uint32_t idesc = umma_idesc_bf16(128, COUT);
+    bool ok = true;
+
+    int it = 0;
+    for (int t = blockIdx.x; t < g.tiles; t += gridDim.x, ++it) {
+        const int start = g.pp + 128 * t;  // padded row of tile row 0
+        const int total = 3 * PL * g.span;
+        for (int e = tid; e < total; e += 128) {
+            const int r = e % g.span, rest = e / g.span, p = rest % PL, dz = rest / PL;
+            const int q = start + (dz - 1) * g.pp - g.np - 1 + r;
+            a_s[e] = in[(size_t)p * g.rows + g.front + q];
+        }
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            uint32_t acc = 0;
+            const uint32_t a0 = smem_addr(a_s), w0 = smem_addr(w_s);
+#pragma unroll 1
+            for (int tap = 0; tap < 27; ++tap) {
+                const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+#pragma unroll
+                for (int kc = 0; kc < KC; ++kc) {
+                    const uint32_t aa = a0 + (uint32_t)(((dz * PL + 2 * kc) * g.span + dy * g.np + dx) * 16);
+                    const uint32_t bb = w0 + (uint32_t)((tap * KC + kc) * 2 * COUT * 16);
+                    umma_bf16(tmem, umma_sdesc(aa, (uint32_t)g.span * 16, 128), umma_sdesc(bb, COUT * 16, 128),
+                              idesc, acc);
+                    acc = 1;
+                }
+            }
+            umma_commit(bar);
+        }
+        // every thread waits (bounded); the block gives up together, so no barrier is left unmatched
+        const int waited = mbar_wait(bar, (uint32_t)(it & 1), kConvWaitLimit) ? 1 : 0;
+        if (!__syncthreads_and(waited)) {
+            ok = false;
+            if (tid == 0) atomicOr(err, 1u);
+            break;
+        }
+        tc_fence_after();
+        float v[COUT];
+#pragma unroll
+        for (int c = 0; c < COUT; c += 16) {
+            float part[16];
+            tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, part);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) v[c + i] = part[i];
+        }
+        const int q = start + 32 * warp + lane;
+        const int x = q % g.np, y = (q / g.np) % g.np, z = q / g.pp;
+        if (x >= 1 && x <= g.n && y >= 1 && y <= g.n && z >= 1 && z <= g.n) {
+            if (OUT32) {
+                float* o = out32 + ((size_t)((z - 1) * g.n + (y - 1)) * g.n + (x - 1)) * COUT;
+#pragma unroll
+                for (int c = 0; c < COUT; ++c) o[c] = v[c] + (bias ? bias[c] : 0.0f);
+            } else {
+#pragma unroll
+                for (int c8 = 0; c8 < COUT / 8; ++c8) {
+                    float w8[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        float s = v[8 * c8 + i] + (bias ? bias[8 * c8 + i] : 0.0f);
+                        w8[i] = (relu && s < 0.0f) ? 0.0f : s;
+                    }
+                    uint4 pk;
+                    pk.x = pack_bf16x2(w8[0], w8[1]);
+                    pk.y = pack_bf16x2(w8[2], w8[3]);
+                    pk.z = pack_bf16x2(w8[4], w8[5]);
+                    pk.w = pack_bf16x2(w8[6], w8[7]);
+                    out[(size_t)c8 * g.rows + g.front + q] = pk;
+                }
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+    }
+    (void)ok;
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_free(tmem, kCols);
+}
+
+}  // namespace numa::gpu

@@ -317,6 +317,23 @@ KrylovParams params_from_c(const numa_krylov_params* p);
 double diag_fp64_peak_tflops(Context& ctx);
 // out = the library's e^x (exp_tang) of x; ref (optional) = CUDA's exp(x).
 void diag_exp(Context& ctx, const double* x, double* out, double* ref, size_t N);
+// One tensor-core 3x3x3 convolution from host buffers (learned.cu): y = conv(x, W) + b, FP32
+// channel-last in and out, BF16 operands; flip = the adjoint convolution (gradient with respect to
+// the input, W of shape [27][cin][cout] used as [27][cout][cin] with the taps reversed).
+void diag_conv3d(Context& ctx, int n, int cin, int cout, int flip, const float* x_h, const float* w_h,
+                 const float* b_h, float* y_h);
+
+// The learned preconditioner's network (learned_net.cu).
+class LearnedNet;
+LearnedNet* learned_create(Context& ctx, int n0, uint64_t seed);
+void learned_destroy(LearnedNet* net);
+size_t learned_num_params(const LearnedNet& net);
+int learned_n0(const LearnedNet& net);
+void learned_get_params(const LearnedNet& net, float* host);
+void learned_set_params(LearnedNet& net, const float* host);
+void learned_forward_host(Context& ctx, LearnedNet& net, const float* feat, float* out);
+void learned_grad_host(Context& ctx, LearnedNet& net, const float* feat, const float* target, float* loss,
+                       float* grad);
 double forcing(const KrylovParams& p, size_t k, double rnorm, double rprev, double eta_prev, double res0);
 
 // x holds x0 on entry and the final iterate on return.

@@ -14,6 +14,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from pathlib import Path
 
 import numpy as np
@@ -76,6 +77,7 @@ _SZ = C.c_size_t
 _D = C.c_double
 _I = C.c_int
 _F64P = C.POINTER(C.c_double)
+_F32P = C.POINTER(C.c_float)
 
 # name -> (argtypes, restype)
 SIGNATURES = {
@@ -154,6 +156,14 @@ SIGNATURES = {
     "numa_gpu_diag_fp64_peak": ([_P, _F64P], _I),
     "numa_gpu_diag_time_smoother": ([_P, _I, _F64P], _I),
     "numa_gpu_diag_exp": ([_P, _P, _P], _I),
+    "numa_gpu_diag_conv3d": ([_P, _SZ, _I, _I, _I, _F32P, _F32P, _F32P, _F32P], _I),
+    "numa_gpu_learned_create": ([_P, _SZ, C.c_uint64, _PP], _I),
+    "numa_gpu_learned_destroy": ([_P], _I),
+    "numa_gpu_learned_num_params": ([_P, C.POINTER(_SZ)], _I),
+    "numa_gpu_learned_get_params": ([_P, _F32P, _SZ], _I),
+    "numa_gpu_learned_set_params": ([_P, _F32P, _SZ], _I),
+    "numa_gpu_learned_forward": ([_P, _F32P, _F32P], _I),
+    "numa_gpu_learned_gradient": ([_P, _F32P, _F32P, _F32P, _F32P], _I),
 }
 
 _lib = None
@@ -210,6 +220,11 @@ class Context:
         if rc != OK:
             raise NumaGPUError(rc, "numa_gpu_ctx_create")
         self.h = h
+        self._children = weakref.WeakSet()
+
+    def _adopt(self, obj):
+        """Objects created on this context are closed before it (whatever the order of garbage collection)."""
+        self._children.add(obj)
 
     def check(self, rc: int, where: str):
         if rc != OK:
@@ -217,6 +232,11 @@ class Context:
 
     def close(self):
         if self.h:
+            for child in list(self._children):
+                try:
+                    child.close()
+                except Exception:
+                    pass
             self.lib.numa_gpu_ctx_destroy(self.h)
             self.h = None
 
@@ -273,6 +293,7 @@ class Vec:
             ctx.check(self.lib.numa_gpu_vec_create(ctx.h, self.n, C.byref(h)), "vec_create")
             self.h = h
             self.owned = True
+            ctx._adopt(self)
         else:
             self.h = C.c_void_p(handle)
             self.owned = False
@@ -335,6 +356,7 @@ class Bratu3D:
         h = C.c_void_p()
         ctx.check(self.lib.numa_gpu_bratu3d_create(ctx.h, self.n, self.lam, C.byref(h)), "bratu3d_create")
         self.h = h
+        self.ctx._adopt(self)
 
     def close(self):
         if self.h:
@@ -373,6 +395,7 @@ class Burgers2D:
         ctx.check(self.lib.numa_gpu_burgers2d_create(ctx.h, self.n, self.nu, self.dt, self.amplitude, C.byref(h)),
                   "burgers2d_create")
         self.h = h
+        self.ctx._adopt(self)
 
     def close(self):
         if self.h:
@@ -415,6 +438,7 @@ class HelmholtzMG2D:
         ctx.check(self.lib.numa_gpu_hmg2d_create(ctx.h, self.n, float(alpha), float(nu), pre, post, C.byref(h)),
                   "hmg2d_create")
         self.h = h
+        self.ctx._adopt(self)
 
     def close(self):
         if self.h:
@@ -436,6 +460,59 @@ class HelmholtzMG2D:
         self.ctx.check(self.lib.numa_gpu_hmg2d_apply(self.h, r.h, z.h), "hmg2d_apply")
 
 
+class LearnedNet:
+    """The learned preconditioner's network (include/numa_gpu.h, numa_gpu_learned_*)."""
+
+    def __init__(self, ctx: Context, n0: int = 31, seed: int = 1):
+        self.ctx, self.lib, self.n0 = ctx, ctx.lib, int(n0)
+        h = C.c_void_p()
+        ctx.check(self.lib.numa_gpu_learned_create(ctx.h, self.n0, seed, C.byref(h)), "learned_create")
+        self.h = h
+        self.ctx._adopt(self)
+
+    def close(self):
+        if self.h:
+            self.lib.numa_gpu_learned_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def num_params(self) -> int:
+        v = C.c_size_t()
+        self.ctx.check(self.lib.numa_gpu_learned_num_params(self.h, C.byref(v)), "learned_num_params")
+        return v.value
+
+    def get_params(self) -> np.ndarray:
+        p = np.empty(self.num_params(), dtype=np.float32)
+        self.ctx.check(self.lib.numa_gpu_learned_get_params(self.h, p.ctypes.data_as(_F32P), p.size), "get_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self.ctx.check(self.lib.numa_gpu_learned_set_params(self.h, p.ctypes.data_as(_F32P), p.size), "set_params")
+
+    def forward(self, features) -> np.ndarray:
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        out = np.empty(self.n0 ** 3, dtype=np.float32)
+        self.ctx.check(self.lib.numa_gpu_learned_forward(self.h, f.ctypes.data_as(_F32P), out.ctypes.data_as(_F32P)),
+                       "learned_forward")
+        return out
+
+    def gradient(self, features, target):
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        g = np.empty(self.num_params(), dtype=np.float32)
+        self.ctx.check(self.lib.numa_gpu_learned_gradient(self.h, f.ctypes.data_as(_F32P), t.ctypes.data_as(_F32P),
+                                                          loss.ctypes.data_as(_F32P), g.ctypes.data_as(_F32P)),
+                       "learned_gradient")
+        return float(loss[0]), g
+
+
 class PoissonMG:
     """PoissonMG(n, pre, post) (linalg/poisson_mg.hpp:24-64); precision / max_levels extend it."""
 
@@ -446,6 +523,7 @@ class PoissonMG:
         ctx.check(self.lib.numa_gpu_mg_create_ex(ctx.h, self.n, pre, post, precision, max_levels, C.byref(h)),
                   "mg_create")
         self.h = h
+        self.ctx._adopt(self)
 
     def close(self):
         if self.h:
@@ -478,6 +556,7 @@ class Provider:
 
     def __init__(self, ctx: Context, handle, kind: str):
         self.ctx, self.lib, self.h, self.kind = ctx, ctx.lib, handle, kind
+        ctx._adopt(self)
 
     @classmethod
     def identity(cls, ctx: Context) -> "Provider":
@@ -544,6 +623,7 @@ class KrylovSpace:
         h = C.c_void_p()
         ctx.check(self.lib.numa_gpu_krylov_space_create(ctx.h, C.byref(h)), "krylov_space_create")
         self.h = h
+        self.ctx._adopt(self)
 
     def close(self):
         if self.h:
@@ -629,6 +709,22 @@ def mg_apply_noalloc(n: int, r: Vec, z: Vec, pre: int = 2, post: int = 2, stream
 def diag_exp(x: "Vec", out: "Vec", cuda_ref: "Vec | None" = None):
     """out = the library's FP64 e^x (table-driven, as in the residual kernels); cuda_ref = CUDA's exp."""
     x.ctx.check(x.lib.numa_gpu_diag_exp(x.h, out.h, cuda_ref.h if cuda_ref is not None else None), "diag_exp")
+
+
+def diag_conv3d(ctx: Context, n: int, x: np.ndarray, w: np.ndarray, bias: np.ndarray | None = None,
+                adjoint: bool = False) -> np.ndarray:
+    """One tensor-core 3x3x3 convolution (BF16 operands, FP32 accumulation), host arrays in and out.
+    x: [n^3, cin] (adjoint: [n^3, cout]), w: [27, cin, cout]; returns [n^3, cout] (adjoint: [n^3, cin])."""
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    cin, cout = int(w.shape[1]), int(w.shape[2])
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.empty((n ** 3, cin if adjoint else cout), dtype=np.float32)
+    b = None if bias is None else np.ascontiguousarray(bias, dtype=np.float32)
+    rc = ctx.lib.numa_gpu_diag_conv3d(ctx.h, n, cin, cout, 1 if adjoint else 0, x.ctypes.data_as(_F32P),
+                                      w.ctypes.data_as(_F32P), None if b is None else b.ctypes.data_as(_F32P),
+                                      y.ctypes.data_as(_F32P))
+    ctx.check(rc, "diag_conv3d")
+    return y
 
 
 def forcing(params: KrylovParams, k: int, rnorm: float, rprev: float, eta_prev: float, res0: float) -> float:

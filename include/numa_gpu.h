@@ -148,6 +148,7 @@ typedef struct numa_gpu_provider numa_gpu_provider;
 typedef struct numa_gpu_krylov_space numa_gpu_krylov_space;
 typedef struct numa_gpu_burgers2d numa_gpu_burgers2d;
 typedef struct numa_gpu_hmg2d numa_gpu_hmg2d;
+typedef struct numa_gpu_learned numa_gpu_learned;
 
 /* ---------------------------------------------------------------- library / context */
 int numa_gpu_abi_version(void);
@@ -321,6 +322,23 @@ int numa_gpu_solve_burgers2d_host(numa_gpu_ctx* ctx, size_t n, double nu, double
                                   int method, int precond_kind, const numa_krylov_params* p,
                                   const double* x0, double* x_out, numa_krylov_result* result);
 
+/* ---------------------------------------------------------------- learned preconditioner */
+/* No counterpart in the reference.  A 4-level 3D convolutional network on the multigrid hierarchy
+ * (base grid n0 in {15, 31, 63}, then (n-1)/2 three times; 16/32 channels, ~0.22M parameters) that
+ * maps three feature fields (residual, Jacobian coefficient, V-cycle output, restricted to n0^3) to
+ * a correction; BF16 activations, convolutions and their input gradients on the tensor cores,
+ * FP32 master weights.  Parameters are FP32, layer by layer: W[27][cin][cout] then b[cout]. */
+int numa_gpu_learned_create(numa_gpu_ctx* ctx, size_t n0, uint64_t seed, numa_gpu_learned** out);
+int numa_gpu_learned_destroy(numa_gpu_learned* net);
+int numa_gpu_learned_num_params(const numa_gpu_learned* net, size_t* n);
+int numa_gpu_learned_get_params(numa_gpu_learned* net, float* host, size_t n);
+int numa_gpu_learned_set_params(numa_gpu_learned* net, const float* host, size_t n);
+/* out[n0^3] = channel 0 of the network applied to features[n0^3][3] (host buffers). */
+int numa_gpu_learned_forward(numa_gpu_learned* net, const float* features, float* out);
+/* loss = mean (out - target)^2 and its gradient with respect to the parameters (host buffers). */
+int numa_gpu_learned_gradient(numa_gpu_learned* net, const float* features, const float* target, float* loss,
+                              float* grad);
+
 /* ---------------------------------------------------------------- V-cycle without allocation */
 /* No counterpart in the reference.  For callers that cannot allocate device memory when they
  * apply the preconditioner (while a stream is being captured into a CUDA graph, inside another
@@ -348,6 +366,14 @@ int numa_gpu_diag_time_smoother(numa_gpu_mg* mg, int reps, double* ms_per_pass);
 /* out = e^x as the residual kernels compute it (Tang's table-driven method, FP64); cuda_ref
  * (may be NULL) = CUDA's exp(x).  For accuracy checks of the exponential. */
 int numa_gpu_diag_exp(const numa_gpu_vec* x, numa_gpu_vec* out, numa_gpu_vec* cuda_ref);
+/* One 3x3x3 convolution of the learned preconditioner on the tensor cores (tcgen05, BF16 operands,
+ * FP32 accumulation), host buffers in and out, zero padding: y[v][co] = bias[co] +
+ * sum_{tap, ci} x[v + tap][ci] w[tap][ci][co] on an n^3 grid (n <= 63), x channel-last [n^3][cin],
+ * w [27][cin][cout] with tap = (dz*3 + dy)*3 + dx, offsets d - 1.  adjoint = 1 runs the
+ * convolution with the reversed, transposed kernel (the gradient with respect to the input):
+ * x is then [n^3][cout] and y [n^3][cin].  cin, cout in {16, 32}; bias may be NULL. */
+int numa_gpu_diag_conv3d(numa_gpu_ctx* ctx, size_t n, int cin, int cout, int adjoint, const float* x,
+                         const float* w, const float* bias, float* y);
 
 #ifdef __cplusplus
 } /* extern "C" */

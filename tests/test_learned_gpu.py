@@ -1,0 +1,73 @@
+"""The learned preconditioner's tensor-core kernels against the CPU restatement
+(oracle/learned_oracle.py): the 3x3x3 convolution (tcgen05, BF16 operands, FP32 accumulation) and
+its adjoint.  Inputs are rounded to BF16 on both sides, so the only difference left is the order of
+the FP32 accumulation: relative error well below 1e-5."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle.learned_oracle import bf16, conv3d, conv3d_adjoint
+
+pytestmark = pytest.mark.gpu
+
+
+def _G():
+    import numa_gpu
+    return numa_gpu
+
+
+@pytest.mark.parametrize("n", [1, 3, 7, 15, 31])
+@pytest.mark.parametrize("cin,cout", [(16, 16), (16, 32), (32, 16), (32, 32)])
+def test_conv3d_tensor_cores(gpu, n, cin, cout):
+    G = _G()
+    rng = np.random.default_rng(7 * n + cin + 3 * cout)
+    x = bf16(rng.standard_normal((n ** 3, cin)))
+    w = bf16(rng.standard_normal((27, cin, cout)) * 0.2)
+    b = rng.standard_normal(cout).astype(np.float32)
+    y = G.diag_conv3d(gpu, n, x, w, b)
+    ref = conv3d(x, w, n, b)
+    scale = np.abs(ref).max() + 1e-30
+    assert np.abs(y - ref).max() / scale < 1e-5
+
+
+@pytest.mark.parametrize("n", [3, 15])
+@pytest.mark.parametrize("cin,cout", [(16, 32), (32, 16)])
+def test_conv3d_adjoint_tensor_cores(gpu, n, cin, cout):
+    G = _G()
+    rng = np.random.default_rng(11 * n + cin)
+    g = bf16(rng.standard_normal((n ** 3, cout)))
+    w = bf16(rng.standard_normal((27, cin, cout)) * 0.2)
+    dx = G.diag_conv3d(gpu, n, g, w, adjoint=True)
+    ref = conv3d_adjoint(g, w, n)
+    assert np.abs(dx - ref).max() / (np.abs(ref).max() + 1e-30) < 1e-5
+
+
+def test_network_forward_and_gradient(gpu):
+    """The whole network, forward and backward, on the GPU against the oracle in its BF16 mode (every
+    stored activation and gradient rounded as the GPU does): outputs, loss and each layer's weight
+    gradient agree to the FP32-accumulation level, up to the odd BF16 value rounded the other way."""
+    from oracle.learned_oracle import LAYERS, unet_backward, unet_forward
+    G = _G()
+    n0 = 15
+    net = G.LearnedNet(gpu, n0, seed=5)
+    p = net.get_params()
+    rng = np.random.default_rng(9)
+    feat = rng.standard_normal((n0 ** 3, 3)).astype(np.float32)
+    t = (rng.standard_normal(n0 ** 3) * 0.1).astype(np.float32)
+    out = net.forward(feat)
+    ref, cache = unet_forward(p, feat, n0, bf=True)
+    assert np.linalg.norm(out - ref) <= 1e-2 * np.linalg.norm(ref)
+    loss, g = net.gradient(feat, t)
+    rloss, rg = unet_backward(cache, t, bf=True)
+    assert abs(loss - rloss) <= 1e-3 * rloss
+    o, errs = 0, []
+    for ci, co, _, _ in LAYERS:
+        sz = 27 * ci * co + co
+        a, b = g[o:o + sz], rg[o:o + sz]
+        errs.append(float(np.linalg.norm(a - b) / (np.linalg.norm(b) + 1e-30)))
+        o += sz
+    cos = float(g @ rg) / (np.linalg.norm(g) * np.linalg.norm(rg))
+    print("per-layer relative gradient error", ["%.2e" % e for e in errs], "cosine", cos)
+    assert max(errs) <= 5e-2, errs
+    assert cos > 0.999
