@@ -286,6 +286,20 @@ void Bratu3D::jvp_c32(const float* c32, const double* v, double* out) {
     ctx_.check_launch("bratu3d jvp32");
 }
 
+// The FP32 Jacobian product of Bratu3D(n) with a given FP32 coefficient, and RN32(c), for callers
+// that hold the coefficient themselves (the learned preconditioner).
+void bratu_jvp32(Context& ctx, int n, double h2inv, const float* c32, const double* v, double* out) {
+    March m = march_shape(n, false);
+    k_jvp32<<<m.grid, dim3(BX, BY), 0, ctx.stream>>>(c32, v, out, n, m.ichunk, (float)h2inv);
+    ctx.count_launch();
+    ctx.check_launch("bratu jvp32");
+}
+
+void bratu_coef32(Context& ctx, const double* c, float* c32, size_t N) {
+    k_coef32<<<ew_grid(ctx, N), 256, 0, ctx.stream>>>(c, c32, N);
+    ctx.count_launch();
+}
+
 void Bratu3D::coef32(const double* c, float* c32) {
     k_coef32<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(c, c32, N_);
     ctx_.count_launch();

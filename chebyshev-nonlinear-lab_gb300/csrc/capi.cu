@@ -1156,6 +1156,42 @@ int numa_gpu_learned_gradient(numa_gpu_learned* net, const float* features, cons
     return guard(net->ctx, [&] { learned_grad_host(*net->ctx->impl, *net->impl, features, target, loss, grad); });
 }
 
+int numa_gpu_learned_train(numa_gpu_learned* net, const numa_learned_train_params* p,
+                           numa_learned_train_report* report) {
+    if (!net || !p || !report) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    std::memset(report, 0, sizeof(*report));
+    return guard(net->ctx, [&] {
+        need(p->instances > 0 && p->states > 0 && p->rhs_per_state >= 0 && p->epochs >= 0 && p->batch > 0,
+             NUMA_GPU_ERR_INVALID_ARGUMENT, "invalid training sizes");
+        need(p->lambda_max >= p->lambda_min && p->solve_rtol > 0.0 && p->lr > 0.0f, NUMA_GPU_ERR_INVALID_ARGUMENT,
+             "invalid training parameters");
+        learned_train(*net->ctx->impl, *net->impl, *p, *report);
+    });
+}
+
+int numa_gpu_provider_create_learned(numa_gpu_ctx* ctx, size_t n, numa_gpu_learned* net, double stall,
+                                     numa_gpu_provider** out) {
+    if (!ctx || !net || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        need(net->ctx == ctx, NUMA_GPU_ERR_INVALID_ARGUMENT, "network belongs to another context");
+        need(stall > 0.0, NUMA_GPU_ERR_INVALID_ARGUMENT, "stall factor must be positive");
+        auto h = std::make_unique<numa_gpu_provider>();
+        h->ctx = ctx;
+        h->impl = make_learned_provider(*ctx->impl, n, *net->impl, stall);
+        h->N = n * n * n;
+        *out = h.release();
+    });
+}
+
+int numa_gpu_provider_learned_stats(numa_gpu_provider* p, size_t* applies, size_t* fallbacks) {
+    if (!p || !applies || !fallbacks) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(p->ctx, [&] {
+        need(p->impl != nullptr, NUMA_GPU_ERR_INVALID_ARGUMENT, "not a learned preconditioner");
+        learned_provider_stats(*p->impl, applies, fallbacks);
+    });
+}
+
 int numa_gpu_diag_time_smoother(numa_gpu_mg* mg, int reps, double* ms_per_pass) {
     if (!mg || !ms_per_pass || reps < 1) return NUMA_GPU_ERR_INVALID_ARGUMENT;
     return guard(mg->ctx, [&] { *ms_per_pass = mg->impl->time_finest_pass(reps); });

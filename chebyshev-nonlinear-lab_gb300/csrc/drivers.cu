@@ -174,6 +174,7 @@ public:
         Timers::Scope s(&t_, kT_PREC);
         p_->apply(r, z);
     }
+    void progress(size_t iters, double rel_res) override { p_->progress(iters, rel_res); }
 
 private:
     Provider* p_;

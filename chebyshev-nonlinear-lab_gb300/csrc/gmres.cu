@@ -303,6 +303,7 @@ GmresResult Gmres::solve(LinearOp& A, Precond* M, const double* b, double* x, co
             ++res.iters;
             k_last = k;
             res.rel_res = std::abs(g[j + 1]) / bnorm;
+            if (M) M->progress(res.iters, res.rel_res);
             if (res.rel_res <= o.rtol) break;
         }
         for (size_t ii = k; ii-- > 0;) {

@@ -11,6 +11,8 @@
 // Every convolution is 3x3x3 with bias and ReLU except d0b, whose channel 0 is the output.  R and P
 // are the multigrid's full-weighting restriction and trilinear prolongation applied per channel;
 // their adjoints are P / 8 and 8 R.
+#include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <random>
@@ -360,6 +362,474 @@ void learned_grad_host(Context& ctx, LearnedNet& net, const float* feat, const f
     NUMA_CUDA(cudaMemcpyAsync(grad, net.grad(), net.num_params() * sizeof(float), cudaMemcpyDeviceToHost, ctx.stream));
     ctx.sync();
     net.check_errors();
+}
+
+// ------------------------------------------------------------------------------ the preconditioner
+// Features and correction live on the multigrid level l whose grid is the network's base n0:
+// fine n -> (n-1)/2 -> ... -> n0.  Fields are carried between the fine grid and level l by the
+// multigrid's full-weighting restriction and trilinear prolongation, FP32, natural layout.
+namespace {
+
+__device__ __forceinline__ int split_at_l(int L, int half) { return (L >> 1) + (L & 1) * half; }
+
+// out (nc^3, FP32) = R(f), f the finest FP32 level in the colour-split layout (odd nf)
+__global__ void k_rest_from_split(const float* __restrict__ f, float* __restrict__ out, int nf, int half) {
+    const int nc = (nf - 1) / 2, Nc = nc * nc * nc;
+    const float w[3] = {0.25f, 0.5f, 0.25f};
+    const int stride = gridDim.x * blockDim.x;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < Nc; q += stride) {
+        const int K = q % nc, J = (q / nc) % nc, I = q / (nc * nc);
+        float acc = 0.0f;
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b)
+                for (int c = 0; c < 3; ++c) {
+                    const int L = ((2 * I + a) * nf + (2 * J + b)) * nf + 2 * K + c;
+                    acc = __fmaf_rn(w[a] * w[b] * w[c], f[split_at_l(L, half)], acc);
+                }
+        out[q] = acc;
+    }
+}
+
+// out (nc^3, FP32) = R(f), f natural (FP64 or FP32)
+template <class T>
+__global__ void k_rest_nat(const T* __restrict__ f, float* __restrict__ out, int nf) {
+    const int nc = (nf - 1) / 2, Nc = nc * nc * nc;
+    const float w[3] = {0.25f, 0.5f, 0.25f};
+    const int stride = gridDim.x * blockDim.x;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < Nc; q += stride) {
+        const int K = q % nc, J = (q / nc) % nc, I = q / (nc * nc);
+        float acc = 0.0f;
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b)
+                for (int c = 0; c < 3; ++c) {
+                    const size_t L = ((size_t)(2 * I + a) * nf + (2 * J + b)) * nf + 2 * K + c;
+                    acc = __fmaf_rn(w[a] * w[b] * w[c], (float)f[L], acc);
+                }
+        out[q] = acc;
+    }
+}
+
+__device__ __forceinline__ float prolong_at(const float* __restrict__ c, int nc, int i, int j, int k) {
+    int ci[2], cj[2], ck[2];
+    auto terms = [nc](int f, int (&idx)[2]) {
+        if (f & 1) {
+            idx[0] = (f - 1) >> 1;
+            return 1;
+        }
+        int cnt = 0;
+        const int r = f >> 1;
+        if (r >= 1) idx[cnt++] = r - 1;
+        if (r < nc) idx[cnt++] = r;
+        return cnt;
+    };
+    const int ni = terms(i, ci), nj = terms(j, cj), nk = terms(k, ck);
+    const float wt = ((i & 1) ? 1.0f : 0.5f) * ((j & 1) ? 1.0f : 0.5f) * ((k & 1) ? 1.0f : 0.5f);
+    float acc = 0.0f;
+    for (int a = 0; a < ni; ++a)
+        for (int b = 0; b < nj; ++b)
+            for (int q = 0; q < nk; ++q) acc = __fmaf_rn(wt, c[((size_t)ci[a] * nc + cj[b]) * nc + ck[q]], acc);
+    return acc;
+}
+
+// f (nf^3 = (2 nc + 1)^3, FP32) = P(c)
+__global__ void k_prolong_nat(const float* __restrict__ c, float* __restrict__ f, int nc) {
+    const int nf = 2 * nc + 1, Nf = nf * nf * nf;
+    const int stride = gridDim.x * blockDim.x;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < Nf; p += stride)
+        f[p] = prolong_at(c, nc, p / (nf * nf), (p / nf) % nf, p % nf);
+}
+
+// z (fine FP64) += s * P(c), s a device scalar
+__global__ void k_prolong_add_fine(const float* __restrict__ c, double* __restrict__ z, int nc,
+                                   const float* __restrict__ s) {
+    const int nf = 2 * nc + 1;
+    const size_t Nf = (size_t)nf * nf * nf;
+    const float sc = *s;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < Nf; p += stride) {
+        const int i = (int)(p / ((size_t)nf * nf)), j = (int)((p / nf) % nf), k = (int)(p % nf);
+        z[p] = z[p] + f32_to_f64(sc * prolong_at(c, nc, i, j, k));
+    }
+}
+
+// s = max(sqrt(mean a^2), tiny); scales = {1/s, 1/10, 0} (one block)
+__global__ void k_rms_scales(const float* __restrict__ a, int N, float* __restrict__ s, float* __restrict__ scales) {
+    __shared__ float sm[32];
+    float acc = 0.0f;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) acc = __fmaf_rn(a[i], a[i], acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.0f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm[w];
+        const float r = fmaxf(sqrtf(t / (float)N), 1e-30f);
+        *s = r;
+        scales[0] = 1.0f / r;
+        scales[1] = 0.1f;
+        scales[2] = 0.0f;
+    }
+}
+
+// out[v] = y32[16 v] (channel 0 of the network output)
+__global__ void k_channel0(const float* __restrict__ y32, float* __restrict__ out, int N) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < N; v += stride) out[v] = y32[(size_t)16 * v];
+}
+
+// r = sum of 8 Gaussian bumps: params [8][5] = (cx, cy, cz, width, amplitude) on the unit cube
+__global__ void k_bumps(double* __restrict__ r, int n, const float* __restrict__ bp) {
+    const size_t N = (size_t)n * n * n;
+    const float h = 1.0f / (float)(n + 1);
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) {
+        const float x = (float)(p % n + 1) * h, y = (float)((p / n) % n + 1) * h, z = (float)(p / ((size_t)n * n) + 1) * h;
+        float acc = 0.0f;
+        for (int b = 0; b < 8; ++b) {
+            const float dx = x - bp[5 * b], dy = y - bp[5 * b + 1], dz = z - bp[5 * b + 2], w = bp[5 * b + 3];
+            acc += bp[5 * b + 4] * expf(-(dx * dx + dy * dy + dz * dz) / (2.0f * w * w));
+        }
+        r[p] = (double)acc;
+    }
+}
+
+__global__ void k_axpby64(const double* __restrict__ a, double alpha, const double* __restrict__ b, double beta,
+                          double* __restrict__ out, size_t N) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) out[p] = alpha * a[p] + beta * b[p];
+}
+
+// t = x / s (device scalar)
+__global__ void k_div_scalar(const float* __restrict__ x, const float* __restrict__ s, float* __restrict__ t, int N) {
+    const float inv = 1.0f / *s;
+    const int stride = gridDim.x * blockDim.x;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < N; v += stride) t[v] = x[v] * inv;
+}
+
+unsigned ew(const Context& ctx, size_t N) {
+    return (unsigned)std::max<size_t>(1, std::min<size_t>((N + 255) / 256, (size_t)ctx.sm_count * 16));
+}
+
+}  // namespace
+
+// The restriction / prolongation chains between a fine grid and the network's level.
+class LevelChain {
+public:
+    LevelChain(Context& ctx, int n_fine, int n0) : ctx_(ctx) {
+        int n = n_fine;
+        ns_.push_back(n);
+        while (n > n0) {
+            if (!(n & 1)) break;
+            n = (n - 1) / 2;
+            ns_.push_back(n);
+        }
+        if (n != n0 || ns_.size() < 2)
+            throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT,
+                         "learned preconditioner: the fine grid must coarsen to the network's base grid");
+        for (size_t l = 1; l < ns_.size(); ++l) {
+            const size_t Nl = (size_t)ns_[l] * ns_[l] * ns_[l];
+            a_.emplace_back(Nl);
+            b_.emplace_back(Nl);
+        }
+    }
+    int levels() const { return (int)ns_.size() - 1; }
+    int n_at(int l) const { return ns_[l]; }
+    size_t N0() const { return (size_t)ns_.back() * ns_.back() * ns_.back(); }
+    // out (base grid, FP32) = R^l f; the first step reads the fine array (split FP32, or natural T)
+    const float* restrict_split(const float* f_split, float* out) {
+        const int nf = ns_[0];
+        const int half = (int)(((size_t)nf * nf * nf + 1) / 2);
+        float* cur = levels() == 1 ? out : a_[0].p;
+        k_rest_from_split<<<ew(ctx_, a_[0].n), 256, 0, ctx_.stream>>>(f_split, cur, nf, half);
+        ctx_.count_launch();
+        return chain(cur, out);
+    }
+    template <class T>
+    const float* restrict_nat(const T* f, float* out) {
+        float* cur = levels() == 1 ? out : a_[0].p;
+        k_rest_nat<T><<<ew(ctx_, a_[0].n), 256, 0, ctx_.stream>>>(f, cur, ns_[0]);
+        ctx_.count_launch();
+        return chain(cur, out);
+    }
+    // z (fine FP64) += s * P^l d (d on the base grid)
+    void prolong_add(const float* d, double* z, const float* s) {
+        const float* cur = d;
+        for (int l = levels(); l > 1; --l) {
+            float* nxt = b_[l - 2].p;  // level l-1
+            k_prolong_nat<<<ew(ctx_, b_[l - 2].n), 256, 0, ctx_.stream>>>(cur, nxt, ns_[l]);
+            ctx_.count_launch();
+            cur = nxt;
+        }
+        k_prolong_add_fine<<<ew(ctx_, (size_t)ns_[0] * ns_[0] * ns_[0]), 256, 0, ctx_.stream>>>(cur, z, ns_[1], s);
+        ctx_.count_launch();
+    }
+
+private:
+    const float* chain(float* cur, float* out) {
+        for (int l = 1; l < levels(); ++l) {
+            float* nxt = (l + 1 == levels()) ? out : a_[l].p;
+            k_rest_nat<float><<<ew(ctx_, (size_t)ns_[l + 1] * ns_[l + 1] * ns_[l + 1]), 256, 0, ctx_.stream>>>(cur, nxt,
+                                                                                                          ns_[l]);
+            ctx_.count_launch();
+            cur = nxt;
+        }
+        return out;
+    }
+    Context& ctx_;
+    std::vector<int> ns_;
+    std::vector<DeviceArray<float>> a_, b_;
+};
+
+// z = V(r) + s P^l net(R^l q / s, R^l c / 10) with q = r - J V(r) the residual the V-cycle leaves and
+// s = rms(R^l q): the network stands in for the coarse solve of the error equation J e = q, which
+// the Poisson V-cycle (built for -Laplacian alone) does not see the -c term of.  FGMRES's
+// preconditioner; the plain V-cycle serves the rest of a linear solve once the residual reduction
+// per iteration stalls.
+class LearnedProvider : public Provider {
+public:
+    LearnedProvider(Context& ctx, size_t n, LearnedNet& net, double stall)
+        : ctx_(ctx), mg_(ctx, n, 2, 2, NUMA_GPU_FP32, 0), net_(net), chain_(ctx, (int)n, net.n0()), stall_(stall),
+          n_((int)n), h2inv_((n + 1.0) * (n + 1.0)) {
+        const size_t N0 = chain_.N0(), N = n * n * n;
+        c32_.resize(N);
+        w_.resize(N);
+        r0_.resize(N0);
+        c0_.resize(N0);
+        d0_.resize(N0);
+        s_.resize(4);
+        NUMA_CUDA(cudaMemsetAsync(c0_.p, 0, N0 * sizeof(float), ctx_.stream));
+    }
+    void make(const double* x, const double* cache) override {
+        (void)x;
+        if (cache) {
+            chain_.restrict_nat<double>(cache, c0_.p);
+            bratu_coef32(ctx_, cache, c32_.p, c32_.n);
+        } else {
+            NUMA_CUDA(cudaMemsetAsync(c0_.p, 0, c0_.n * sizeof(float), ctx_.stream));
+            NUMA_CUDA(cudaMemsetAsync(c32_.p, 0, c32_.n * sizeof(float), ctx_.stream));
+        }
+        use_net_ = true;
+        prev_ = 1.0;
+    }
+    void apply(const double* r, double* z) override {
+        mg_.apply(r, z);
+        if (!use_net_) return;
+        const int N0 = (int)chain_.N0();
+        // q = r - J z, restricted
+        bratu_jvp32(ctx_, n_, h2inv_, c32_.p, z, w_.p);
+        k_axpby64<<<ew(ctx_, w_.n), 256, 0, ctx_.stream>>>(r, 1.0, w_.p, -1.0, w_.p, w_.n);
+        ctx_.count_launch();
+        chain_.restrict_nat<double>(w_.p, r0_.p);
+        k_rms_scales<<<1, 512, 0, ctx_.stream>>>(r0_.p, N0, s_.p, s_.p + 1);
+        ctx_.count_launch();
+        planes_features(ctx_, r0_.p, c0_.p, r0_.p, s_.p + 1, net_.feature_planes(), net_.grid(0));
+        net_.forward(net_.feature_planes(), net_.out32());
+        k_channel0<<<ew(ctx_, N0), 256, 0, ctx_.stream>>>(net_.out32(), d0_.p, N0);
+        ctx_.count_launch();
+        chain_.prolong_add(d0_.p, z, s_.p);
+        ++net_applies_;
+    }
+    void progress(size_t iters, double rel_res) override {
+        if (iters <= 1) prev_ = 1.0;
+        if (use_net_ && iters >= 2 && rel_res > stall_ * prev_) {
+            use_net_ = false;
+            ++fallbacks_;
+        }
+        prev_ = rel_res;
+    }
+    int kind() const override { return NUMA_GPU_PRECOND_LEARNED; }
+    size_t net_applies() const { return net_applies_; }
+    size_t fallbacks() const { return fallbacks_; }
+
+private:
+    Context& ctx_;
+    PoissonMG mg_;
+    LearnedNet& net_;
+    LevelChain chain_;
+    double stall_;
+    int n_;
+    double h2inv_;
+    DeviceArray<float> r0_, c0_, d0_, s_, c32_;
+    DeviceArray<double> w_;
+    bool use_net_ = true;
+    double prev_ = 1.0;
+    size_t net_applies_ = 0, fallbacks_ = 0;
+};
+
+std::unique_ptr<Provider> make_learned_provider(Context& ctx, size_t n, LearnedNet& net, double stall) {
+    return std::make_unique<LearnedProvider>(ctx, n, net, stall);
+}
+
+void learned_provider_stats(Provider& p, size_t* applies, size_t* fallbacks) {
+    auto* lp = dynamic_cast<LearnedProvider*>(&p);
+    if (!lp) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "not a learned preconditioner");
+    *applies = lp->net_applies();
+    *fallbacks = lp->fallbacks();
+}
+
+// ------------------------------------------------------------------------------ training
+namespace {
+// J e = r at a Bratu3D iterate with coefficient c (FP64 analytic product)
+struct CoefJacobian : LinearOp {
+    Bratu3D& f;
+    const double* c;
+    CoefJacobian(Bratu3D& op, const double* cc) : f(op), c(cc) {}
+    void apply(const double* v, double* out) override { f.jvp_c(c, v, out); }
+};
+struct MGPre : Precond {
+    PoissonMG& mg;
+    explicit MGPre(PoissonMG& m) : mg(m) {}
+    void apply(const double* r, double* z) override { mg.apply(r, z); }
+};
+}  // namespace
+
+void learned_train(Context& ctx, LearnedNet& net, const numa_learned_train_params& p, numa_learned_train_report& rep) {
+    std::memset(&rep, 0, sizeof(rep));
+    const int n = (int)p.n_fine;
+    const size_t N = (size_t)n * n * n;
+    LevelChain chain(ctx, n, net.n0());
+    const size_t N0 = chain.N0();
+    const int per_state = 1 + p.krylov_per_state + p.rhs_per_state;
+    const size_t samples = (size_t)p.instances * p.states * per_state;
+    if (samples == 0) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "no training samples requested");
+    DeviceArray<float> feats(samples * 2 * N0), targets(samples * N0);
+    DeviceArray<double> u(N), us(N), c(N), F(N), r(N), e(N), zmg(N), diff(N), qres(N);
+    DeviceArray<float> c32(N);
+    const double h2inv = (n + 1.0) * (n + 1.0);
+    DeviceArray<float> tmp(N0), sc(4), bp(40);
+    PoissonMG mg(ctx, (size_t)n, 2, 2, NUMA_GPU_FP32, 0);
+    Gmres gm(ctx, N);
+    std::mt19937_64 rng(p.seed);
+    std::uniform_real_distribution<double> U01(0.0, 1.0);
+    const auto t0 = std::chrono::steady_clock::now();
+    size_t k = 0;
+    for (int inst = 0; inst < p.instances; ++inst) {
+        const double lam = p.lambda_min + (p.lambda_max - p.lambda_min) * U01(rng);
+        Bratu3D op(ctx, (size_t)n, lam);
+        // u* by the mixed Newton-Krylov solve
+        NUMA_CUDA(cudaMemsetAsync(u.p, 0, N * sizeof(double), ctx.stream));
+        {
+            KrylovParams kp;
+            kp.rtol_nl = 1e-8;
+            kp.restart = 30;
+            kp.flexible = true;
+            kp.jvp_precision = NUMA_GPU_FP32;
+            auto pc = make_mg_provider(ctx, (size_t)n, 2, 2, NUMA_GPU_FP32, 0);
+            numa_krylov_result res;
+            newton_krylov(op, u.p, kp, pc.get(), res);
+        }
+        for (int st = 0; st < p.states; ++st) {
+            const double sfac = p.states == 1 ? 1.0 : (double)st / (double)(p.states - 1);
+            k_axpby64<<<ew(ctx, N), 256, 0, ctx.stream>>>(u.p, sfac, u.p, 0.0, us.p, N);
+            ctx.count_launch();
+            op.eval(us.p, F.p, c.p, nullptr);
+            const float* c0 = chain.restrict_nat<double>(c.p, tmp.p);
+            bratu_coef32(ctx, c.p, c32.p, N);
+            // r = a seeded sum of 8 Gaussian bumps (centres in the cube, widths 0.05..0.2, amplitudes +-1)
+            auto bumps = [&]() {
+                float h[40];
+                for (int b = 0; b < 8; ++b) {
+                    h[5 * b] = (float)U01(rng);
+                    h[5 * b + 1] = (float)U01(rng);
+                    h[5 * b + 2] = (float)U01(rng);
+                    h[5 * b + 3] = (float)(0.05 + 0.15 * U01(rng));
+                    h[5 * b + 4] = (float)(2.0 * U01(rng) - 1.0);
+                }
+                NUMA_CUDA(cudaMemcpyAsync(bp.p, h, sizeof(h), cudaMemcpyHostToDevice, ctx.stream));
+                k_bumps<<<ew(ctx, N), 256, 0, ctx.stream>>>(r.p, n, bp.p);
+                ctx.count_launch();
+            };
+            KrylovSpace space;
+            size_t kry = 0;  // Arnoldi vectors available from the F(u) solve
+            for (int q = 0; q < per_state; ++q) {
+                if (q == 0) {
+                    dev_copy(ctx, F.p, r.p, N);
+                } else if (q <= p.krylov_per_state && (size_t)q <= kry) {
+                    dev_copy(ctx, space.V.p + (size_t)q * N, r.p, N);  // V_q of the F(u) solve
+                } else {
+                    bumps();  // (also when the F(u) solve stopped before V_q)
+                }
+                // e = J^-1 r (GMG-preconditioned FGMRES), z = V(r)
+                CoefJacobian J(op, c.p);
+                MGPre M(mg);
+                GmresOptions o;
+                o.rtol = p.solve_rtol;
+                o.restart = 30;
+                o.max_iters = 300;
+                o.flexible = true;
+                if (q == 0) {
+                    space.clear();
+                    gm.solve(J, &M, r.p, e.p, o, &space);
+                    kry = space.k;
+                } else {
+                    gm.solve(J, &M, r.p, e.p, o);
+                }
+                mg.apply(r.p, zmg.p);
+                // the residual the V-cycle leaves, q = r - J z (the provider's FP32 product)
+                bratu_jvp32(ctx, n, h2inv, c32.p, zmg.p, qres.p);
+                k_axpby64<<<ew(ctx, N), 256, 0, ctx.stream>>>(r.p, 1.0, qres.p, -1.0, qres.p, N);
+                ctx.count_launch();
+                float* fr = feats.p + k * 2 * N0;
+                float* fc = fr + N0;
+                chain.restrict_nat<double>(qres.p, fr);
+                k_rms_scales<<<1, 512, 0, ctx.stream>>>(fr, (int)N0, sc.p, sc.p + 1);
+                ctx.count_launch();
+                k_div_scalar<<<ew(ctx, N0), 256, 0, ctx.stream>>>(fr, sc.p, fr, (int)N0);
+                ctx.count_launch();
+                // coefficient feature (scaled by 1/10 when the planes are formed)
+                NUMA_CUDA(cudaMemcpyAsync(fc, c0, N0 * sizeof(float), cudaMemcpyDeviceToDevice, ctx.stream));
+                // target = R^l (e - z) / s
+                k_axpby64<<<ew(ctx, N), 256, 0, ctx.stream>>>(e.p, 1.0, zmg.p, -1.0, diff.p, N);
+                ctx.count_launch();
+                float* tt = targets.p + k * N0;
+                chain.restrict_nat<double>(diff.p, tt);
+                k_div_scalar<<<ew(ctx, N0), 256, 0, ctx.stream>>>(tt, sc.p, tt, (int)N0);
+                ctx.count_launch();
+                ++k;
+            }
+        }
+        ctx.check_launch("learned training data");
+    }
+    ctx.sync();
+    rep.samples = k;
+    rep.gen_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    {
+        std::vector<float> th(k * N0);
+        NUMA_CUDA(cudaMemcpyAsync(th.data(), targets.p, th.size() * sizeof(float), cudaMemcpyDeviceToHost, ctx.stream));
+        ctx.sync();
+        double acc = 0.0;
+        for (float v : th) acc += (double)v * v;
+        rep.target_ms = (float)(acc / (double)th.size());
+    }
+    // training: Adam over shuffled samples, gradients summed over a batch
+    const auto t1 = std::chrono::steady_clock::now();
+    std::vector<size_t> order(k);
+    for (size_t i = 0; i < k; ++i) order[i] = i;
+    DeviceArray<float> loss(1), scales(4);
+    const float sc_h[4] = {1.0f, 0.1f, 0.0f, 0.0f};
+    NUMA_CUDA(cudaMemcpyAsync(scales.p, sc_h, sizeof(sc_h), cudaMemcpyHostToDevice, ctx.stream));
+    const int batch = std::max(1, p.batch);
+    for (int ep = 0; ep < p.epochs; ++ep) {
+        std::shuffle(order.begin(), order.end(), rng);
+        NUMA_CUDA(cudaMemsetAsync(loss.p, 0, sizeof(float), ctx.stream));
+        for (size_t i = 0; i < k; i += batch) {
+            net.zero_grad();
+            for (size_t b = i; b < std::min(k, i + batch); ++b) {
+                const float* fr = feats.p + order[b] * 2 * N0;
+                planes_features(ctx, fr, fr + N0, fr, scales.p, net.feature_planes(), net.grid(0));
+                net.loss_and_backward(net.feature_planes(), targets.p + order[b] * N0, loss.p);
+            }
+            net.adam(p.lr);
+        }
+        float lh = 0.0f;
+        NUMA_CUDA(cudaMemcpyAsync(&lh, loss.p, sizeof(float), cudaMemcpyDeviceToHost, ctx.stream));
+        ctx.sync();
+        lh /= (float)k;
+        if (ep == 0) rep.loss_first = lh;
+        rep.loss_last = lh;
+    }
+    net.check_errors();
+    rep.train_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
 }
 
 }  // namespace numa::gpu

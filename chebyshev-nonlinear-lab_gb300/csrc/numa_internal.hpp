@@ -123,6 +123,9 @@ private:
     DeviceArray<float> c32_;
 };
 
+void bratu_jvp32(Context& ctx, int n, double h2inv, const float* c32, const double* v, double* out);
+void bratu_coef32(Context& ctx, const double* c, float* c32, size_t N);
+
 // ------------------------------------------------------------------------------ Burgers2D
 // One implicit-Euler step of 2D viscous Burgers with a manufactured root
 // (problems/burgers2d.hpp:23-218): w = (u, v), 2 n^2 unknowns.
@@ -163,6 +166,8 @@ public:
     // Diagnostic: average time (ms) of one red-black colour pass on the finest level, timed with
     // CUDA events over `reps` back-to-back passes on the context stream.
     double time_finest_pass(int reps);
+    // FP32 cycle: RN32(r) of the last apply on the finest level and its layout (colour-split when odd).
+    const float* fine_b32() const;
 
     struct Level;
 
@@ -226,6 +231,10 @@ public:
     virtual void make(const double* x, const double* cache) = 0;
     virtual void apply(const double* r, double* z) = 0;
     virtual int kind() const = 0;
+    virtual void progress(size_t iters, double rel_res) {
+        (void)iters;
+        (void)rel_res;
+    }
 };
 
 std::unique_ptr<Provider> make_identity_provider(Context& ctx, size_t N);
@@ -260,6 +269,12 @@ struct LinearOp {
 struct Precond {
     virtual ~Precond() = default;
     virtual void apply(const double* r, double* z) = 0;
+    // Called by GMRES after each Arnoldi step with the iteration count of the solve and the relative
+    // residual estimate (a preconditioner may change strategy on stagnation, as FGMRES allows).
+    virtual void progress(size_t iters, double rel_res) {
+        (void)iters;
+        (void)rel_res;
+    }
 };
 
 struct GmresOptions {
@@ -334,6 +349,10 @@ void learned_set_params(LearnedNet& net, const float* host);
 void learned_forward_host(Context& ctx, LearnedNet& net, const float* feat, float* out);
 void learned_grad_host(Context& ctx, LearnedNet& net, const float* feat, const float* target, float* loss,
                        float* grad);
+void learned_train(Context& ctx, LearnedNet& net, const numa_learned_train_params& p, numa_learned_train_report& rep);
+class Provider;
+std::unique_ptr<Provider> make_learned_provider(Context& ctx, size_t n, LearnedNet& net, double stall);
+void learned_provider_stats(Provider& p, size_t* applies, size_t* fallbacks);
 double forcing(const KrylovParams& p, size_t k, double rnorm, double rprev, double eta_prev, double res0);
 
 // x holds x0 on entry and the final iterate on return.

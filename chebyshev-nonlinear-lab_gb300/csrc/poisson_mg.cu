@@ -398,6 +398,8 @@ void PoissonMG::apply(const double* r, double* z) {
     ctx_.check_launch("mg apply");
 }
 
+const float* PoissonMG::fine_b32() const { return levels_[0]->b32.p; }
+
 double PoissonMG::time_finest_pass(int reps) {
     Level& L0 = *levels_[0];
     const int n = L0.n;

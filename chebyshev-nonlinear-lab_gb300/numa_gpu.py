@@ -44,6 +44,22 @@ class KrylovParams(C.Structure):
     ]
 
 
+class LearnedTrainParams(C.Structure):
+    """numa_learned_train_params"""
+    _fields_ = [
+        ("n_fine", C.c_size_t), ("lambda_min", C.c_double), ("lambda_max", C.c_double),
+        ("instances", C.c_int32), ("states", C.c_int32), ("rhs_per_state", C.c_int32), ("krylov_per_state", C.c_int32),
+        ("epochs", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float), ("seed", C.c_uint64),
+        ("solve_rtol", C.c_double),
+    ]
+
+
+class LearnedTrainReport(C.Structure):
+    """numa_learned_train_report"""
+    _fields_ = [("samples", C.c_size_t), ("gen_seconds", C.c_double), ("train_seconds", C.c_double),
+                ("loss_first", C.c_float), ("loss_last", C.c_float), ("target_ms", C.c_float)]
+
+
 class KrylovResult(C.Structure):
     """numa_krylov_result: KrylovResult (krylov_newton.hpp:40-49) plus timers."""
     _fields_ = [
@@ -164,6 +180,9 @@ SIGNATURES = {
     "numa_gpu_learned_set_params": ([_P, _F32P, _SZ], _I),
     "numa_gpu_learned_forward": ([_P, _F32P, _F32P], _I),
     "numa_gpu_learned_gradient": ([_P, _F32P, _F32P, _F32P, _F32P], _I),
+    "numa_gpu_learned_train": ([_P, C.POINTER(LearnedTrainParams), C.POINTER(LearnedTrainReport)], _I),
+    "numa_gpu_provider_create_learned": ([_P, _SZ, _P, _D, _PP], _I),
+    "numa_gpu_provider_learned_stats": ([_P, C.POINTER(_SZ), C.POINTER(_SZ)], _I),
 }
 
 _lib = None
@@ -502,6 +521,16 @@ class LearnedNet:
                        "learned_forward")
         return out
 
+    def train(self, n_fine: int, instances: int = 8, states: int = 3, rhs_per_state: int = 8,
+              krylov_per_state: int = 4, epochs: int = 4, batch: int = 8, lr: float = 1e-3, lambda_min: float = 1.0,
+              lambda_max: float = 6.5, seed: int = 7, solve_rtol: float = 1e-6) -> dict:
+        """Generates residual-error pairs on the GPU and trains (numa_gpu_learned_train)."""
+        p = LearnedTrainParams(n_fine, lambda_min, lambda_max, instances, states, rhs_per_state, krylov_per_state,
+                               epochs, batch, lr, seed, solve_rtol)
+        rep = LearnedTrainReport()
+        self.ctx.check(self.lib.numa_gpu_learned_train(self.h, C.byref(p), C.byref(rep)), "learned_train")
+        return to_dict(rep)
+
     def gradient(self, features, target):
         f = np.ascontiguousarray(features, dtype=np.float32)
         t = np.ascontiguousarray(target, dtype=np.float32)
@@ -585,6 +614,20 @@ class Provider:
         h = C.c_void_p()
         ctx.check(ctx.lib.numa_gpu_provider_create_burgers_mg(ctx.h, n, nu, dt, C.byref(h)), "provider_burgers_mg")
         return cls(ctx, h, "burgers_mg")
+
+    @classmethod
+    def learned(cls, ctx: Context, n: int, net: "LearnedNet", stall: float = 0.9) -> "Provider":
+        """FP32 V-cycle + learned coarse correction (for FGMRES)."""
+        h = C.c_void_p()
+        ctx.check(ctx.lib.numa_gpu_provider_create_learned(ctx.h, n, net.h, stall, C.byref(h)), "provider_learned")
+        p = cls(ctx, h, "learned")
+        p._net = net
+        return p
+
+    def learned_stats(self) -> tuple[int, int]:
+        a, f = C.c_size_t(), C.c_size_t()
+        self.ctx.check(self.lib.numa_gpu_provider_learned_stats(self.h, C.byref(a), C.byref(f)), "learned_stats")
+        return a.value, f.value
 
     @classmethod
     def create(cls, ctx: Context, kind: str, op, precision: int = FP64) -> "Provider | None":

@@ -76,7 +76,8 @@ typedef enum numa_gpu_precond_kind {
     NUMA_GPU_PRECOND_NONE = 0,       /* NoPrecond / IdentityPrecond (krylov_newton.hpp:20-22, gmres.hpp:37-39) */
     NUMA_GPU_PRECOND_POISSON_MG = 1, /* PoissonMGProvider (linalg/poisson_mg.hpp:303-320) */
     NUMA_GPU_PRECOND_JACOBI = 2,     /* BratuJacobi (problems/bratu3d.hpp:104-120) */
-    NUMA_GPU_PRECOND_BURGERS_MG = 3  /* BurgersMGProvider (problems/burgers2d.hpp:220-246) */
+    NUMA_GPU_PRECOND_BURGERS_MG = 3, /* BurgersMGProvider (problems/burgers2d.hpp:220-246) */
+    NUMA_GPU_PRECOND_LEARNED = 4     /* extension: FP32 V-cycle + learned coarse correction (FGMRES) */
 } numa_gpu_precond_kind;
 
 /* ---------------------------------------------------------------- parameter / result structs */
@@ -338,6 +339,42 @@ int numa_gpu_learned_forward(numa_gpu_learned* net, const float* features, float
 /* loss = mean (out - target)^2 and its gradient with respect to the parameters (host buffers). */
 int numa_gpu_learned_gradient(numa_gpu_learned* net, const float* features, const float* target, float* loss,
                               float* grad);
+
+/* Training on the GPU from residual-error pairs of GMG-preconditioned solves: for `instances`
+ * seeded lambda ~ U[lambda_min, lambda_max], Bratu3D(n_fine, lambda) is solved (mixed
+ * Newton-Krylov), and at the states u = s u*, s = 0, 1/(states-1), ..., 1, the Jacobian systems
+ * J e = r are solved by FGMRES(30) + FP32 V-cycle to solve_rtol for r = F(u), the first
+ * krylov_per_state Arnoldi vectors of that solve (the inputs FGMRES gives the preconditioner) and
+ * rhs_per_state seeded sums of 8 Gaussian bumps.  With q = r - J V r (the residual one FP32
+ * V-cycle leaves) the network learns R^l (e - V r) / rms(R^l q) from (R^l q / rms, R^l c / 10) on
+ * the level l of the fine hierarchy whose grid is n0; Adam, gradients summed over a batch. */
+typedef struct numa_learned_train_params {
+    size_t n_fine;
+    double lambda_min, lambda_max;
+    int instances, states, rhs_per_state, krylov_per_state;
+    int epochs, batch;
+    float lr;
+    uint64_t seed;
+    double solve_rtol;
+} numa_learned_train_params;
+typedef struct numa_learned_train_report {
+    size_t samples;
+    double gen_seconds, train_seconds;
+    float loss_first, loss_last;  /* mean loss per sample, first and last epoch */
+    float target_ms;              /* mean squared target: the loss of predicting zero */
+} numa_learned_train_report;
+int numa_gpu_learned_train(numa_gpu_learned* net, const numa_learned_train_params* p,
+                           numa_learned_train_report* report);
+/* FGMRES preconditioner for Bratu3D(n) (odd n coarsening to the network's base grid): z = V(r) +
+ * s P^l net(R^l q / s, R^l c / 10), q = r - J V(r), s = rms(R^l q), with the FP32 V-cycle and the
+ * FP32 Jacobian product at the iterate the provider was made at (make needs the coefficient
+ * lambda e^u, which the nonlinear drivers pass; the public make(x) has none); during one linear
+ * solve it falls back to the plain V-cycle once an iteration reduces the residual by less than the
+ * factor `stall` (e.g. 0.9).  Use with flexible = 1.  The network must outlive the provider. */
+int numa_gpu_provider_create_learned(numa_gpu_ctx* ctx, size_t n, numa_gpu_learned* net, double stall,
+                                     numa_gpu_provider** out);
+/* Network applications and fallbacks of a learned provider since its creation. */
+int numa_gpu_provider_learned_stats(numa_gpu_provider* p, size_t* applies, size_t* fallbacks);
 
 /* ---------------------------------------------------------------- V-cycle without allocation */
 /* No counterpart in the reference.  For callers that cannot allocate device memory when they
