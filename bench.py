@@ -59,9 +59,10 @@ def parse_args(argv=None):
     ap.add_argument("--method", choices=["nk", "cheb", "rec", "tf2018"], default="nk")
     ap.add_argument("--path", choices=["fp64", "mixed"], default="fp64", help="headline path")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner leg")
     ap.add_argument("--cpu-sample-n", type=int, default=127)
     ap.add_argument("--cpu-reps", type=int, default=2)
-    ap.add_argument("--kernel-case", choices=["none", "vcycle", "solve"], default="none",
+    ap.add_argument("--kernel-case", choices=["none", "vcycle", "solve", "conv"], default="none",
                     help="profiling driver: run only this small case (for ncu)")
     return ap.parse_args(argv)
 
@@ -300,6 +301,24 @@ def run_ours(args) -> int:
                                    stream)
     x_other = x.numpy() if dist.rank == 0 else None
 
+    # the learned preconditioner beside the V-cycle inside FGMRES (trained here, on this GPU, from
+    # GMG-preconditioned solves of this grid at seeded lambda; lambda of the bench is held out)
+    learned = None
+    if not args.no_learned:
+        try:
+            net = G.LearnedNet(ctx, 31, seed=3)
+            trep = net.train(n, instances=4, states=3, rhs_per_state=2, krylov_per_state=8, epochs=8, batch=4,
+                             lr=2e-3, seed=11)
+            pcl = G.Provider.learned(ctx, n, net, stall=0.9)
+            sec_l, res_l, _ = timed_solves(G, ctx, op, pcl, x, u0, args.method, params_for(G, "mixed"),
+                                           max(1, args.steps // 2), 1, dist, stream)
+            x_l = x.numpy() if dist.rank == 0 else None
+            applies, fallbacks = pcl.learned_stats()
+            learned = {"s": sec_l, "res": res_l, "x": x_l, "training": trep, "applies": applies,
+                       "fallbacks": fallbacks}
+        except G.NumaGPUError as exc:
+            learned = {"skipped": str(exc)}
+
     # end to end through the host-buffer entry point, pinned buffers
     h_in = torch.zeros(N, dtype=torch.float64, pin_memory=True).numpy()
     h_out = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
@@ -382,6 +401,7 @@ def run_ours(args) -> int:
                                "other_counts": {k: res_o[k] for k in ("iters", "n_JVP", "n_prec", "converged")},
                                "note": "mixed = FP32 V-cycle + FP32 Jacobian products inside FGMRES(30), FP64 "
                                        "residual / updates / Arnoldi; no learned preconditioner"},
+            "learned_mixed": learned_summary(learned, fp64_sec, x_head if args.path == "fp64" else x_other),
             "clocks": clk.summary(),
             "e2e": {"value": e2e_sec, "unit": "s", "h2d_bytes_per_step": N * 8, "d2h_bytes_per_step": N * 8,
                     "api": "numa_gpu_solve_bratu3d_host, pinned host buffers"},
@@ -393,6 +413,26 @@ def run_ours(args) -> int:
         print(json.dumps(line), flush=True)
     dist.close()
     return 0
+
+
+def learned_summary(learned, fp64_sec, x_fp64):
+    """The learned-preconditioner leg of the JSON line."""
+    if learned is None:
+        return None
+    if "skipped" in learned:
+        return learned
+    r = learned["res"]
+    return {
+        "s": learned["s"], "ratio_vs_plain": fp64_sec / learned["s"],
+        "counts": {k: r[k] for k in ("iters", "n_JVP", "n_lin_iters", "n_prec", "converged")},
+        "rel_err_vs_fp64": float(np.linalg.norm(learned["x"] - x_fp64) / np.linalg.norm(x_fp64)),
+        "net_applies": learned["applies"], "fallbacks_to_vcycle": learned["fallbacks"],
+        "training": {k: learned["training"][k] for k in ("samples", "gen_seconds", "train_seconds", "loss_first",
+                                                          "loss_last", "target_ms")},
+        "note": "FGMRES(30) preconditioned by the FP32 V-cycle plus a 4-level 3D conv net (BF16, tcgen05) on the "
+                "31^3 level, fed the residual the V-cycle leaves and lambda e^u; trained on this GPU before the "
+                "timed solves (training time not in s); falls back to the V-cycle when an iteration stalls",
+    }
 
 
 def load_profile_traffic(mgp) -> float | None:
@@ -409,6 +449,16 @@ def load_profile_traffic(mgp) -> float | None:
 def run_kernel_case(G, ctx, args) -> int:
     """Small fixed cases for ncu captures: a few V-cycles, or one solve."""
     n, N = args.n, args.n ** 3
+    if args.kernel_case == "conv":
+        # the learned preconditioner's tensor-core convolution at its largest supported shape
+        rng = np.random.default_rng(0)
+        nc = 63
+        xin = rng.standard_normal((nc ** 3, 32)).astype(np.float32)
+        w = (rng.standard_normal((27, 32, 32)) * 0.1).astype(np.float32)
+        for _ in range(max(1, args.steps)):
+            G.diag_conv3d(ctx, nc, xin, w)
+        print(json.dumps({"kernel_case": "conv", "n": nc, "launches": ctx.kernel_launches()}))
+        return 0
     if args.kernel_case == "vcycle":
         for prec in (G.FP64, G.FP32):
             mg = G.PoissonMG(ctx, n, precision=prec)

@@ -141,11 +141,11 @@ template <int CIN, int COUT>
 __host__ __device__ constexpr size_t conv_weight_bytes() {
     return (size_t)27 * (CIN / 16) * 2 * COUT * 16;
 }
-// The span region carries 16 spans of slack: even a reading of the A descriptor with its two byte
-// offsets exchanged (rows 8 apart by a span) stays inside the allocation.
+// Weights plus the three spans: two CTAs fit on an SM at every supported shape (<= 105 KB each),
+// so one CTA's copies overlap the other's MMAs and epilogue.
 template <int CIN, int COUT>
 inline size_t conv_smem_bytes(const VoxGrid& g) {
-    return conv_weight_bytes<CIN, COUT>() + (size_t)(3 * (CIN / 8) + 16) * g.span * 16;
+    return conv_weight_bytes<CIN, COUT>() + (size_t)3 * (CIN / 8) * g.span * 16;
 }
 
 constexpr int kConvWaitLimit = 1 << 22;
