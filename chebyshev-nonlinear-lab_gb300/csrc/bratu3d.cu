@@ -59,11 +59,13 @@ __device__ __forceinline__ double lap_sum(const double* __restrict__ v, size_t p
     return s;
 }
 
-// F = h^-2 (6u - sum) - lambda e^u; optionally c = lambda e^u and ||F||.
-template <bool WRITE_C, bool NORM>
+// F = h^-2 (6u - sum) - lambda e^u; optionally c = lambda e^u and ||F||.  The last step is one FMA
+// (F differs from the reference's two roundings by at most half an ulp, as e^u already may).
+// C32: also c32 = RN32(c) (the mixed path's FP32 Jacobian coefficient, integer conversion).
+template <bool WRITE_C, bool NORM, bool C32>
 __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, double* __restrict__ F,
-                                                 double* __restrict__ c_out, int n, int ichunk, double lam,
-                                                 double h2inv, RedArgs red, double* norm_out) {
+                                                 double* __restrict__ c_out, float* __restrict__ c32_out, int n,
+                                                 int ichunk, double lam, double h2inv, RedArgs red, double* norm_out) {
     const int k = blockIdx.x * BX + threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
     const int i0 = blockIdx.z * ichunk;
@@ -78,9 +80,10 @@ __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, d
             double above;
             const double s = lap_sum(u, p, plane, n, i, j, k, below, cur, above);
             const double e = lam * exp_tang(cur);
-            const double f = h2inv * s - e;
+            const double f = __fma_rn(h2inv, s, -e);  // h^-2 s - e with one rounding
             F[p] = f;
             if (WRITE_C) c_out[p] = e;
+            if (C32) c32_out[p] = f64_to_f32(e);
             if (NORM) acc[0] = __fma_rn(f, f, acc[0]);
             below = cur;
             cur = above;
@@ -239,13 +242,18 @@ void Bratu3D::bind(const double*, const double* cache, int precision) {
     bound_c_ = cache;
     bound_precision_ = precision;
     if (precision == NUMA_GPU_FP32) {
-        c32_.resize(N_);
-        coef32(cache, c32_.p);
+        if (mixed_cache_) {
+            bound_c32_ = reinterpret_cast<const float*>(cache + N_);  // written by the evaluation
+        } else {
+            c32_.resize(N_);
+            coef32(cache, c32_.p);
+            bound_c32_ = c32_.p;
+        }
     }
 }
 
 void Bratu3D::jvp_bound(const double* v, double* out) {
-    if (bound_precision_ == NUMA_GPU_FP32) jvp_c32(c32_.p, v, out);
+    if (bound_precision_ == NUMA_GPU_FP32) jvp_c32(bound_c32_, v, out);
     else jvp_c(bound_c_, v, out);
 }
 
@@ -254,14 +262,20 @@ void Bratu3D::eval(const double* x, double* out, double* c_out, double* norm_out
     const bool norm = norm_out != nullptr;
     March m = march_shape(n, norm);
     dim3 blk(BX, BY);
-    if (c_out && norm)
-        k_eval<true, true><<<m.grid, blk, 0, ctx_.stream>>>(x, out, c_out, n, m.ichunk, lambda_, h2inv_, ctx_.red, norm_out);
+    float* c32 = (c_out && mixed_cache_) ? reinterpret_cast<float*>(c_out + N_) : nullptr;
+    const double lam = lambda_, h2 = h2inv_;
+    if (c32 && norm)
+        k_eval<true, true, true><<<m.grid, blk, 0, ctx_.stream>>>(x, out, c_out, c32, n, m.ichunk, lam, h2, ctx_.red, norm_out);
+    else if (c32)
+        k_eval<true, false, true><<<m.grid, blk, 0, ctx_.stream>>>(x, out, c_out, c32, n, m.ichunk, lam, h2, ctx_.red, nullptr);
+    else if (c_out && norm)
+        k_eval<true, true, false><<<m.grid, blk, 0, ctx_.stream>>>(x, out, c_out, nullptr, n, m.ichunk, lam, h2, ctx_.red, norm_out);
     else if (c_out)
-        k_eval<true, false><<<m.grid, blk, 0, ctx_.stream>>>(x, out, c_out, n, m.ichunk, lambda_, h2inv_, ctx_.red, nullptr);
+        k_eval<true, false, false><<<m.grid, blk, 0, ctx_.stream>>>(x, out, c_out, nullptr, n, m.ichunk, lam, h2, ctx_.red, nullptr);
     else if (norm)
-        k_eval<false, true><<<m.grid, blk, 0, ctx_.stream>>>(x, out, nullptr, n, m.ichunk, lambda_, h2inv_, ctx_.red, norm_out);
+        k_eval<false, true, false><<<m.grid, blk, 0, ctx_.stream>>>(x, out, nullptr, nullptr, n, m.ichunk, lam, h2, ctx_.red, norm_out);
     else
-        k_eval<false, false><<<m.grid, blk, 0, ctx_.stream>>>(x, out, nullptr, n, m.ichunk, lambda_, h2inv_, ctx_.red, nullptr);
+        k_eval<false, false, false><<<m.grid, blk, 0, ctx_.stream>>>(x, out, nullptr, nullptr, n, m.ichunk, lam, h2, ctx_.red, nullptr);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d eval");
 }

@@ -293,9 +293,10 @@ enum ScalarSlot : int {
     kSlotFdZero = 18,
     kSlotFdXnorm = 19,
     kSlotGmresH = 64,     // Hessenberg column, m + 2 entries
-    kSlotGmresH2 = 320,   // CGS2 second-pass coefficients, up to 16
+    kSlotGmresH2 = 320,   // CGS2 second-pass coefficients, up to 8
     kSlotGmresY = 400,    // least-squares solution y, m entries
     kSlotGmresCoef = 700, // recycled-solve coefficients, 2k + 1 entries
+    kSlotGmresSig2 = 1250, // lazily normalised basis: 1 / norm^2 of each vector, m + 1 entries
 };
 
 // Pinned host staging for small vectors moving to the device.

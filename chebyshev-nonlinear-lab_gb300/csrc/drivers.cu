@@ -216,6 +216,7 @@ struct SolveState {
         xb.resize(N);
         Fa.resize(N);
         Fb.resize(N);
+        f.prepare_cache(p.jvp_mode == NUMA_GPU_DERIV_ANALYTIC ? p.jvp_precision : NUMA_GPU_FP64);
         const size_t nc = f.cache_size();
         if (nc) {
             ca.resize(nc);
@@ -261,8 +262,9 @@ struct SolveState {
     }
 };
 
-GmresOptions gmres_opts(const KrylovParams& p, double rtol) {
+GmresOptions gmres_opts(const KrylovParams& p, double rtol, double bnorm = -1.0) {
     GmresOptions o;
+    o.bnorm = bnorm;
     o.rtol = rtol;
     o.restart = p.restart;
     o.max_iters = p.max_iters;
@@ -351,7 +353,7 @@ void newton_krylov(NonlinearOp& f, double* x0, const KrylovParams& p, Provider* 
         }
         const double eta = forcing(p, k, rnorm, rprev, eta_prev, out.res0);
         S.bind(J, pc);
-        const GmresResult g = S.gmres.solve(J, Mp, S.Fx, S.z.p, gmres_opts(p, eta));
+        const GmresResult g = S.gmres.solve(J, Mp, S.Fx, S.z.p, gmres_opts(p, eta, rnorm));
         add_lin(out, g);
         if (g.breakdown) break;
         double lam = 1.0;
@@ -410,7 +412,8 @@ void chebyshev_inexact(NonlinearOp& f, double* x0, const KrylovParams& p, Provid
         const double eta2 = std::min(p.eta2_max, p.eta2_factor * eta1);
         S.bind(J, pc);
         space.clear();
-        const GmresResult g1 = S.gmres.solve(J, Mp, S.Fx, S.z.p, gmres_opts(p, eta1), p.recycle ? &space : nullptr);
+        const GmresResult g1 =
+            S.gmres.solve(J, Mp, S.Fx, S.z.p, gmres_opts(p, eta1, rnorm), p.recycle ? &space : nullptr);
         add_lin(out, g1);
         if (g1.breakdown) break;
         {
@@ -494,7 +497,7 @@ void tf_chebyshev_2018(NonlinearOp& f, double* x0, const KrylovParams& p, Provid
         const double eta1 = std::clamp(std::min(1e-8, rnorm * rnorm), 2.0 * eps, 1e-8);
         const double eta2 = std::clamp(std::min(1e-8, rnorm), 2.0 * eps, 1e-8);
         S.bind(J, pc);
-        const GmresResult g1 = S.gmres.solve(J, Mp, S.Fx, S.z.p, gmres_opts(p, eta1));
+        const GmresResult g1 = S.gmres.solve(J, Mp, S.Fx, S.z.p, gmres_opts(p, eta1, rnorm));
         add_lin(out, g1);
         if (!g1.converged) break;
         if (g1.breakdown) break;

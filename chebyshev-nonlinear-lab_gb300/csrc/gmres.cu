@@ -22,7 +22,7 @@
 namespace numa::gpu {
 namespace {
 
-constexpr int kMaxCgs = 16;
+constexpr int kMaxCgs = 8;  // largest basis count of the fused classical Gram-Schmidt kernels
 
 struct StoreAt {
     double* out;
@@ -64,41 +64,80 @@ struct StoreVec {
     }
 };
 
-// MODE 0: h[r] = <w, V_r>.
-// MODE 1: w -= sum_r hin[r] V_r, then h[r] = <w, V_r>.
-// MODE 2: w -= sum_r hin[r] V_r, then h[0] = ||w||.
-template <int MODE>
-__global__ void __launch_bounds__(kRedThreads) k_cgs(double* __restrict__ w, const double* __restrict__ V, size_t ldv,
-                                                     int cnt, const double* __restrict__ hin, size_t N, RedArgs red,
-                                                     double* __restrict__ hout) {
-    __shared__ double sm[kMaxCgs][32];
-    __shared__ double hs[kMaxCgs];
-    if (MODE != 0 && threadIdx.x < kMaxCgs) hs[threadIdx.x] = threadIdx.x < (unsigned)cnt ? hin[threadIdx.x] : 0.0;
-    __syncthreads();
-    double s[kMaxCgs];
+// Fused classical Gram-Schmidt passes over CNT basis vectors (CNT a compile-time count, so the CNT
+// partial sums stay in registers through the two-level reduction).  The vectors are v0 (r = 0) and
+// V + r ldv (r >= 1), so a first vector can live outside the basis array.
+// MODE 0: h[r] = <w, v_r>.
+// MODE 1: wout = w - sum_r hin[r] v_r, then h[r] = <wout, v_r>.
+// MODE 2: wout = w - sum_r hin[r] sig2[r] v_r (sig2 = 1 when null), then h[0] = ||wout|| and, when
+//         sig2_out is given, *sig2_out = 1 / ||wout||^2 (0 for a zero vector).
+template <int CNT, int MODE>
+__global__ void __launch_bounds__(kRedThreads) k_cgs(const double* w, const double* __restrict__ v0,
+                                                     const double* __restrict__ V, size_t ldv,
+                                                     const double* __restrict__ hin, const double* __restrict__ sig2,
+                                                     size_t N, RedArgs red, double* __restrict__ hout, double* wout,
+                                                     double* __restrict__ sig2_out) {
+    constexpr int R = MODE == 2 ? 1 : CNT;
+    __shared__ double sm[R][32];
+    double hs[CNT];
 #pragma unroll
-    for (int r = 0; r < kMaxCgs; ++r) s[r] = 0.0;
+    for (int r = 0; r < CNT; ++r) hs[r] = MODE != 0 ? hin[r] * (sig2 ? sig2[r] : 1.0) : 0.0;
+    double s[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) s[r] = 0.0;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) {
         double wi = w[i];
         if (MODE != 0) {
-            for (int r = 0; r < cnt; ++r) wi = __fma_rn(-hs[r], V[(size_t)r * ldv + i], wi);
-            w[i] = wi;
+#pragma unroll
+            for (int r = 0; r < CNT; ++r) wi = __fma_rn(-hs[r], r == 0 ? v0[i] : V[(size_t)r * ldv + i], wi);
+            wout[i] = wi;
         }
         if (MODE == 2) {
             s[0] = __fma_rn(wi, wi, s[0]);
         } else {
 #pragma unroll
-            for (int r = 0; r < kMaxCgs; ++r)
-                if (r < cnt) s[r] = __fma_rn(wi, V[(size_t)r * ldv + i], s[r]);
+            for (int r = 0; r < CNT; ++r) s[r] = __fma_rn(wi, r == 0 ? v0[i] : V[(size_t)r * ldv + i], s[r]);
         }
     }
-    block_sum<kMaxCgs>(s, sm);
-    const int nres = MODE == 2 ? 1 : cnt;
-    grid_reduce_finish<kMaxCgs>(s, red, [hout, nres] __device__(const double(&t)[kMaxCgs]) {
-        if (MODE == 2) hout[0] = __dsqrt_rn(t[0]);
-        else for (int r = 0; r < nres; ++r) hout[r] = t[r];
+    block_sum<R>(s, sm);
+    grid_reduce_finish<R>(s, red, [hout, sig2_out] __device__(const double(&t)[R]) {
+        if (MODE == 2) {
+            const double nrm = __dsqrt_rn(t[0]);
+            hout[0] = nrm;
+            if (sig2_out) *sig2_out = t[0] > 0.0 ? 1.0 / t[0] : 0.0;
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) hout[r] = t[r];
+        }
     });
+}
+
+// Launches k_cgs<cnt, MODE>; false when cnt is above the largest compiled count.
+template <int MODE>
+bool launch_cgs(Context& ctx, int cnt, const double* w, const double* v0, const double* V, size_t N,
+                const double* hin, const double* sig2, double* hout, double* wout, double* sig2_out) {
+    const unsigned g = ctx.red_grid(N);
+    switch (cnt) {
+#define NUMA_CGS_CASE(K)                                                                                       \
+    case K:                                                                                                    \
+        k_cgs<K, MODE><<<g, kRedThreads, 0, ctx.stream>>>(w, v0, V, N, hin, sig2, N, ctx.red, hout, wout,   \
+                                                          sig2_out);                                         \
+        break;
+        NUMA_CGS_CASE(1)
+        NUMA_CGS_CASE(2)
+        NUMA_CGS_CASE(3)
+        NUMA_CGS_CASE(4)
+        NUMA_CGS_CASE(5)
+        NUMA_CGS_CASE(6)
+        NUMA_CGS_CASE(7)
+        NUMA_CGS_CASE(8)
+#undef NUMA_CGS_CASE
+        default:
+            return false;
+    }
+    ctx.count_launch();
+    return true;
 }
 
 // dst = src / d (gmres.hpp:128, :149) as src * RN(1/d): one FP64 instruction instead of a
@@ -131,6 +170,23 @@ __global__ void k_combine(const double* __restrict__ base, const double* __restr
         out[i] = t;
     }
 }
+
+// x += sum_i coef[i] V_i in one pass (the flexible update; x is read and written in place)
+__global__ void k_combine_add(const double* __restrict__ V, size_t ldv, int cnt, const double* __restrict__ coef,
+                              double* x, size_t N) {
+    extern __shared__ double cs[];
+    for (int r = threadIdx.x; r < cnt; r += blockDim.x) cs[r] = coef[r];
+    __syncthreads();
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) {
+        double t = x[i];
+        for (int r = 0; r < cnt; ++r) t = __fma_rn(cs[r], V[(size_t)r * ldv + i], t);
+        x[i] = t;
+    }
+}
+
+// *out = v (one device scalar from a host value, stream-ordered)
+__global__ void k_set_scalar(double* __restrict__ out, double v) { *out = v; }
 
 unsigned ew_grid(const Context& ctx, size_t N) {
     size_t want = (N + 255) / 256;
@@ -171,18 +227,168 @@ void Gmres::arnoldi_cgs2(size_t j, double* w) {
     double* hcol = ctx_.scalar(kSlotGmresH);
     double* h2 = ctx_.scalar(kSlotGmresH2);
     const size_t N = N_;
-    const unsigned g = ctx_.red_grid(N);
     const int cnt = (int)(j + 1);
-    k_cgs<0><<<g, kRedThreads, 0, ctx_.stream>>>(w, V_.p, N, cnt, nullptr, N, ctx_.red, hcol);
-    k_cgs<1><<<g, kRedThreads, 0, ctx_.stream>>>(w, V_.p, N, cnt, hcol, N, ctx_.red, h2);
-    k_cgs<2><<<g, kRedThreads, 0, ctx_.stream>>>(w, V_.p, N, cnt, h2, N, ctx_.red, hcol + j + 1);
-    ctx_.count_launch(3);
+    launch_cgs<0>(ctx_, cnt, w, V_.p, V_.p, N, nullptr, nullptr, hcol, nullptr, nullptr);
+    launch_cgs<1>(ctx_, cnt, w, V_.p, V_.p, N, hcol, nullptr, h2, w, nullptr);
+    launch_cgs<2>(ctx_, cnt, w, V_.p, V_.p, N, h2, nullptr, hcol + j + 1, w, nullptr);
     ctx_.check_launch("arnoldi cgs2");
     // H = h + h' is formed on the host after the column is read (see solve).
 }
 
+// Classical Gram-Schmidt, one pass: h = V^T w in one multi-dot, then w -= V h and ||w|| in one
+// update (2j + 5 vector passes against 4j + 5 for the fused MGS chain).  For the few Arnoldi steps a
+// well-preconditioned solve takes, the loss of orthogonality is at rounding level.
+void Gmres::arnoldi_cgs1(size_t j, double* w) {
+    double* hcol = ctx_.scalar(kSlotGmresH);
+    const size_t N = N_;
+    const int cnt = (int)(j + 1);
+    launch_cgs<0>(ctx_, cnt, w, V_.p, V_.p, N, nullptr, nullptr, hcol, nullptr, nullptr);
+    launch_cgs<2>(ctx_, cnt, w, V_.p, V_.p, N, hcol, nullptr, hcol + j + 1, w, nullptr);
+    ctx_.check_launch("arnoldi cgs1");
+}
+
+// Flexible GMRES with one-pass classical Gram-Schmidt and lazily normalised basis vectors: the
+// basis keeps v~_j = w~ as the update pass writes it, with sigma_j = 1/||v~_j|| (sigma_j^2 on the
+// device, sigma_j on the host), so no pass divides a vector.  The preconditioned vectors are
+// z_j := sigma_j M(v~_j) (FGMRES admits any z_j), A z_j = sigma_j A M(v~_j), and the Hessenberg
+// entries and the final coefficients carry the sigmas: h_ij = sigma_j sigma_i <A M(v~_j), v~_i>,
+// h_{j+1,j} = sigma_j ||w~||, x += sum_j (y_j sigma_j) M(v~_j).  The first basis vector is the
+// right-hand side (or residual) itself, read in place.  Cycles are at most kMaxCgs steps long.
+GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* x, const GmresOptions& o,
+                              const double* r_init) {
+    const size_t N = N_;
+    const size_t m = std::min(o.restart, (size_t)kMaxCgs);
+    GmresResult res;
+    double* sl = ctx_.scalar(kSlotGmresH);
+    double* sig2 = ctx_.scalar(kSlotGmresSig2);
+    double bnorm = o.bnorm;
+    if (bnorm < 0.0) {
+        dev_norm2(ctx_, b, N, sl);
+        bnorm = ctx_.fetch1(sl);
+    }
+    if (bnorm == 0.0) {
+        dev_fill(ctx_, x, 0.0, N);
+        res.converged = true;
+        return res;
+    }
+    if (o.restart == 0) {
+        res.rel_res = 1.0;
+        res.breakdown = true;
+        return res;
+    }
+    if (o.max_iters == 0) {
+        res.rel_res = 1.0;
+        return res;
+    }
+    if (o.zero_guess) dev_fill(ctx_, x, 0.0, N);
+    V_.resize((m + 1) * N);
+    Z_.resize(m * N);
+    w_.resize(N);
+    r_.resize(N);
+    std::vector<std::vector<double>> H(m + 1, std::vector<double>(m, 0.0));
+    std::vector<double> cs(m), sn(m), g(m + 1), y(m), col(m + 2), sig(m + 1);
+    double* ydev = ctx_.scalar(kSlotGmresY);
+    bool given = r_init != nullptr;
+    bool first = o.zero_guess;
+    const unsigned eg = ew_grid(ctx_, N);
+    while (res.iters < o.max_iters) {
+        const double* v0;
+        double beta;
+        if (given) {
+            v0 = r_init;
+            given = false;
+            first = false;
+            dev_norm2(ctx_, v0, N, sl);
+            beta = ctx_.fetch1(sl);
+        } else if (first) {
+            v0 = b;
+            first = false;
+            beta = bnorm;
+        } else {
+            A.apply(x, w_.p);
+            ++res.matvecs;
+            k_sub<<<eg, 256, 0, ctx_.stream>>>(b, w_.p, r_.p, N);
+            ctx_.count_launch();
+            v0 = r_.p;
+            dev_norm2(ctx_, v0, N, sl);
+            beta = ctx_.fetch1(sl);
+        }
+        res.rel_res = beta / bnorm;
+        if (res.rel_res <= o.rtol) {
+            res.converged = true;
+            break;
+        }
+        k_set_scalar<<<1, 1, 0, ctx_.stream>>>(sig2, 1.0 / (beta * beta));
+        ctx_.count_launch();
+        sig[0] = 1.0 / beta;
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        size_t k = 0;
+        while (k < m && res.iters < o.max_iters) {
+            const size_t j = k;
+            const double* vj = j == 0 ? v0 : V_.p + j * N;
+            double* zj = Z_.p + j * N;
+            precond_apply(M, vj, zj);
+            ++res.precs;
+            A.apply(zj, w_.p);
+            ++res.matvecs;
+            const int cnt = (int)(j + 1);
+            launch_cgs<0>(ctx_, cnt, w_.p, v0, V_.p, N, nullptr, nullptr, sl, nullptr, nullptr);
+            launch_cgs<2>(ctx_, cnt, w_.p, v0, V_.p, N, sl, sig2, sl + j + 1, V_.p + (j + 1) * N, sig2 + j + 1);
+            ctx_.check_launch("arnoldi (lazy cgs1)");
+            ctx_.fetch(sl, (int)(j + 2), col.data());
+            for (size_t i = 0; i <= j; ++i) H[i][j] = sig[j] * sig[i] * col[i];
+            H[j + 1][j] = sig[j] * col[j + 1];
+            sig[j + 1] = col[j + 1] > 0.0 ? 1.0 / col[j + 1] : 0.0;
+            for (size_t i = 0; i < j; ++i) {
+                const double t = cs[i] * H[i][j] + sn[i] * H[i + 1][j];
+                H[i + 1][j] = -sn[i] * H[i][j] + cs[i] * H[i + 1][j];
+                H[i][j] = t;
+            }
+            const double den = std::hypot(H[j][j], H[j + 1][j]);
+            if (!(den > 0.0) || !std::isfinite(den)) {
+                res.breakdown = true;
+                return res;
+            }
+            cs[j] = H[j][j] / den;
+            sn[j] = H[j + 1][j] / den;
+            H[j][j] = den;
+            H[j + 1][j] = 0.0;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            ++k;
+            ++res.iters;
+            res.rel_res = std::abs(g[j + 1]) / bnorm;
+            if (M) M->progress(res.iters, res.rel_res);
+            if (res.rel_res <= o.rtol) break;
+        }
+        for (size_t ii = k; ii-- > 0;) {
+            const double piv = H[ii][ii];
+            if (!(std::abs(piv) > 0.0) || !std::isfinite(piv)) {
+                res.breakdown = true;
+                return res;
+            }
+            double t = g[ii];
+            for (size_t jj = ii + 1; jj < k; ++jj) t -= H[ii][jj] * y[jj];
+            y[ii] = t / piv;
+        }
+        double* yh = pin_.get(m);
+        for (size_t jj = 0; jj < k; ++jj) yh[jj] = y[jj] * sig[jj];
+        NUMA_CUDA(cudaMemcpyAsync(ydev, yh, k * sizeof(double), cudaMemcpyHostToDevice, ctx_.stream));
+        k_combine_add<<<eg, 256, k * sizeof(double), ctx_.stream>>>(Z_.p, N, (int)k, ydev, x, N);
+        ctx_.count_launch();
+        ctx_.check_launch("gmres update (lazy)");
+        if (res.rel_res <= o.rtol) {
+            res.converged = true;
+            break;
+        }
+    }
+    return res;
+}
+
 GmresResult Gmres::solve(LinearOp& A, Precond* M, const double* b, double* x, const GmresOptions& o,
                          KrylovSpace* save, const double* r_init) {
+    if (o.flexible && o.orth == NUMA_GPU_ORTH_CGS1 && !save) return solve_lazy(A, M, b, x, o, r_init);
     const size_t N = N_;
     const size_t m = o.restart;
     GmresResult res;
@@ -209,6 +415,7 @@ GmresResult Gmres::solve(LinearOp& A, Precond* M, const double* b, double* x, co
     if (o.zero_guess) dev_fill(ctx_, x, 0.0, N);
 
     const bool cgs2 = o.orth == NUMA_GPU_ORTH_CGS2;
+    const bool cgs1 = o.orth == NUMA_GPU_ORTH_CGS1;
     V_.resize((m + 1) * N);
     if (o.flexible) Z_.resize(m * N);
     w_.resize(N);
@@ -270,6 +477,9 @@ GmresResult Gmres::solve(LinearOp& A, Precond* M, const double* b, double* x, co
                 ctx_.fetch(sl, (int)(j + 2), col.data());
                 ctx_.fetch(ctx_.scalar(kSlotGmresH2), (int)(j + 1), col2.data());
                 for (size_t i = 0; i <= j; ++i) col[i] += col2[i];
+            } else if (cgs1 && j + 1 <= (size_t)kMaxCgs) {
+                arnoldi_cgs1(j, w_.p);
+                ctx_.fetch(sl, (int)(j + 2), col.data());
             } else {
                 arnoldi_mgs(j, w_.p);
                 ctx_.fetch(sl, (int)(j + 2), col.data());

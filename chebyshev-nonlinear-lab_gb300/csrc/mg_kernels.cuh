@@ -225,17 +225,19 @@ enum SplitPass { kPassFull = 0, kPassFirst = 1, kPassLastZ = 2 };
 //   kPassFirst: x is zero before the pass, x = bs / 6.
 //   kPassLastZ: the final pass of the cycle: x is not stored; z (FP64, natural layout) receives
 //               both members of the pair (the other member holds its value from the previous pass).
-template <int MODE, int ICH>
+//   NN > 0: the grid size is a compile-time constant, so every neighbour offset is an immediate of
+//           the load instruction (one add per point forms the base m + c).
+template <int MODE, int ICH, int NN>
 __global__ void __launch_bounds__(BX* BY) k_pass_split(float* __restrict__ own, const float* __restrict__ oth,
                                                        const float* __restrict__ bown, double* __restrict__ z,
                                                        Split g, int c) {
     const int kk = blockIdx.x * BX + threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
-    const int n = g.n;
+    const int n = NN > 0 ? NN : g.n;
     if (j >= n || 2 * kk >= n) return;
     const int i0 = blockIdx.z * ICH;
     const int P = n * n;
-    const int o_km = c - 1, o_kp = c, o_jm = c - g.hn - 1, o_jp = c + g.hn, o_im = c - g.hP - 1, o_ip = c + g.hP;
+    const int hn = NN > 0 ? (NN - 1) / 2 : g.hn, hP = NN > 0 ? (NN * NN - 1) / 2 : g.hP;
     const bool jlo = j > 0, jhi = j + 1 < n;
     const int kA = 2 * kk + ((i0 + j + c) & 1);  // the point's k on planes i0, i0 + 2, ...
     const int LA = (i0 * n + j) * n + kA;
@@ -247,12 +249,13 @@ __global__ void __launch_bounds__(BX* BY) k_pass_split(float* __restrict__ own, 
         const int m = (i0 + s < n) ? (L >> 1) : 0;  // planes past the grid load harmlessly
         bv[s] = bown[m];
         if (MODE != kPassFirst) {
-            v_im[s] = oth[m + o_im];
-            v_ip[s] = oth[m + o_ip];
-            v_jm[s] = oth[m + o_jm];
-            v_jp[s] = oth[m + o_jp];
-            v_km[s] = oth[m + o_km];
-            v_kp[s] = oth[m + o_kp];
+            const float* q = oth + (m + c);  // the neighbours at fixed offsets from here
+            v_im[s] = q[-hP - 1];
+            v_ip[s] = q[hP];
+            v_jm[s] = q[-hn - 1];
+            v_jp[s] = q[hn];
+            v_km[s] = q[-1];
+            v_kp[s] = q[0];
         }
     }
 #pragma unroll
@@ -296,10 +299,12 @@ inline void launch_pass_split(float* x, const float* bs, double* z, const Split&
     const dim3 blk(BX, BY);
     if (n >= 64) {
         const dim3 grid(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, (n + 3) / 4);
-        k_pass_split<MODE, 4><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c);
+        if (n == 255) k_pass_split<MODE, 4, 255><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c);
+        else if (n == 127) k_pass_split<MODE, 4, 127><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c);
+        else k_pass_split<MODE, 4, 0><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c);
     } else {
         const dim3 grid(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n);
-        k_pass_split<MODE, 1><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c);
+        k_pass_split<MODE, 1, 0><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c);
     }
 }
 

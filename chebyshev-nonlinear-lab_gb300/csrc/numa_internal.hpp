@@ -43,6 +43,9 @@ public:
     virtual size_t size() const = 0;
     // Doubles of data an iterate keeps for the Jacobian at it (0: none).
     virtual size_t cache_size() const = 0;
+    // Announces the precision the Jacobian products of the coming solve will use, before any
+    // evaluation (an operator may then keep what that precision needs in the cache).
+    virtual void prepare_cache(int precision) { (void)precision; }
     // out = F(x); cache := the Jacobian data at x (when cache_size() > 0); norm_out := ||F(x)||
     // as a device scalar (optional).
     virtual void eval(const double* x, double* out, double* cache, double* norm_out) = 0;
@@ -88,8 +91,10 @@ public:
     double lambda() const { return lambda_; }
     double h2inv() const { return h2inv_; }
 
-    // NonlinearOp: the cache of an iterate x is c = lambda e^x.
-    size_t cache_size() const override { return N_; }
+    // NonlinearOp: the cache of an iterate x is c = lambda e^x; for FP32 products it also holds
+    // RN32(c) (N floats after the N doubles), written by the evaluation itself.
+    size_t cache_size() const override { return mixed_cache_ ? N_ + (N_ + 1) / 2 : N_; }
+    void prepare_cache(int precision) override { mixed_cache_ = precision == NUMA_GPU_FP32; }
     void eval(const double* x, double* out, double* cache, double* norm_out) override;
     void bind(const double* x, const double* cache, int precision) override;
     void jvp_bound(const double* v, double* out) override;
@@ -119,7 +124,9 @@ private:
     size_t n_, N_;
     double lambda_, h2inv_;
     const double* bound_c_ = nullptr;
+    const float* bound_c32_ = nullptr;
     int bound_precision_ = NUMA_GPU_FP64;
+    bool mixed_cache_ = false;
     DeviceArray<float> c32_;
 };
 
@@ -284,6 +291,7 @@ struct GmresOptions {
     bool zero_guess = true;
     int orth = NUMA_GPU_ORTH_MGS;
     bool flexible = false;
+    double bnorm = -1.0;  // ||b|| when the caller knows it (>= 0), used by the flexible CGS1 solver
 };
 
 class Gmres {
@@ -300,6 +308,9 @@ public:
 private:
     void arnoldi_mgs(size_t j, double* w);
     void arnoldi_cgs2(size_t j, double* w);
+    void arnoldi_cgs1(size_t j, double* w);
+    GmresResult solve_lazy(LinearOp& A, Precond* M, const double* b, double* x, const GmresOptions& o,
+                           const double* r_init);
     void precond_apply(Precond* M, const double* r, double* z);
     Context& ctx_;
     size_t N_;

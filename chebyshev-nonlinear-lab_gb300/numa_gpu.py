@@ -26,7 +26,7 @@ LIB_PATH = Path(os.environ.get("NUMA_GPU_LIB", HERE / "libnuma_gpu.so"))
 OK = 0
 FP64, FP32 = 0, 1
 ANALYTIC, FD, ANALYTIC_FP32 = 0, 1, 2
-MGS, CGS2 = 0, 1
+MGS, CGS2, CGS1 = 0, 1, 2
 METHODS = {"nk": 0, "cheb": 1, "rec": 2, "tf2018": 3}
 PRECONDS = {"none": 0, "mg": 1, "jacobi": 2, "burgers_mg": 3}
 

@@ -60,7 +60,8 @@ typedef enum numa_gpu_deriv_mode {
 /* Arnoldi orthogonalisation. */
 typedef enum numa_gpu_orth {
     NUMA_GPU_ORTH_MGS = 0, /* modified Gram-Schmidt, the reference (linalg/gmres.hpp:141-144) */
-    NUMA_GPU_ORTH_CGS2 = 1 /* classical Gram-Schmidt with one reorthogonalisation, fused multi-dot */
+    NUMA_GPU_ORTH_CGS2 = 1, /* classical Gram-Schmidt with one reorthogonalisation, fused multi-dot */
+    NUMA_GPU_ORTH_CGS1 = 2  /* classical Gram-Schmidt, one pass (multi-dot, then update and norm) */
 } numa_gpu_orth;
 
 /* Nonlinear methods of the reference's R1 drivers. */

@@ -152,6 +152,24 @@ def test_cgs2_matches_mgs(gpu):
     assert ga["converged"] and gb["converged"]
     assert abs(ga["iters"] - gb["iters"]) <= 1
     assert rel_err(xa.numpy(), xb.numpy()) < 1e-9
+    xc = gpu.vec(N)
+    gc = G.gmres_bratu3d(op, xpt, b, xc, 1e-10, 30, 300, provider=pc, orth=G.CGS1)
+    assert gc["converged"] and abs(ga["iters"] - gc["iters"]) <= 1
+    assert rel_err(xa.numpy(), xc.numpy()) < 1e-9
+
+
+def test_mixed_path_with_cgs1(gpu):
+    """The mixed path as the benchmark runs it (FGMRES, FP32 V-cycle and J v, one-pass classical
+    Gram-Schmidt) against the FP64 drop-in: same Newton count, solution within 1e-8."""
+    G = _G()
+    n, lam = 63, 6.0
+    op = G.Bratu3D(gpu, n, lam)
+    x64, xm = gpu.vec(n ** 3), gpu.vec(n ** 3)
+    r64 = G.newton_krylov(op, x64, G.default_params(rtol_nl=1e-10, gmres_restart=30), G.Provider.poisson_mg(gpu, n))
+    pm = G.default_params(rtol_nl=1e-10, gmres_restart=30, flexible=1, jvp_precision=G.FP32, orth=G.CGS1)
+    rm = G.newton_krylov(op, xm, pm, G.Provider.poisson_mg(gpu, n, precision=G.FP32))
+    assert rm["converged"] and abs(rm["iters"] - r64["iters"]) <= 1
+    assert rel_err(xm.numpy(), x64.numpy()) < 1e-8
 
 
 def test_fgmres_fp32_preconditioner(gpu):
