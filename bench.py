@@ -367,7 +367,7 @@ def run_ours(args) -> int:
         traffic = load_profile_traffic(mgp)
         roofline = {
             "kernel": (f"k_rbgs<double> colour pass, {n}^3" if mgp == G.FP64 else
-                       f"k_rbgs_split colour pass (FP32, colour-split layout), {n}^3"),
+                       f"k_pass_split colour pass (FP32, colour-split layout), {n}^3"),
             "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
             "traffic": traffic, "ms_per_launch": ms_pass,
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback",
@@ -440,7 +440,7 @@ def learned_summary(learned, fp64_sec, x_fp64):
 
 def load_profile_traffic(mgp) -> float | None:
     """DRAM bytes per launch of the colour pass from the committed ncu summary, if present."""
-    f = ROOT / "profiles" / ("k_rbgs_fp64_255.json" if mgp == 0 else "k_rbgs_fp32_255.json")
+    f = ROOT / "profiles" / ("k_rbgs_fp64_255.json" if mgp == 0 else "k_pass_split_fp32_255.json")
     if f.exists():
         try:
             return float(json.loads(f.read_text())["dram_bytes_per_launch"])
