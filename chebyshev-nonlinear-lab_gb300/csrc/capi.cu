@@ -5,6 +5,7 @@
 // PoissonMG, std::invalid_argument / std::overflow_error: those map to
 // NUMA_GPU_ERR_INVALID_ARGUMENT / NUMA_GPU_ERR_OVERFLOW).
 #include <cstring>
+#include <mutex>
 #include <memory>
 #include <new>
 #include <string>
@@ -333,6 +334,7 @@ int numa_gpu_vec_create(numa_gpu_ctx* ctx, size_t n, numa_gpu_vec** out) {
         v->owns = true;
         v->d = nullptr;
         if (n > 0) {
+            std::lock_guard<std::recursive_mutex> lk(alloc_capture_mutex());
             cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&v->d), n * sizeof(double));
             if (e == cudaErrorMemoryAllocation) {
                 cudaGetLastError();
@@ -349,6 +351,7 @@ int numa_gpu_vec_destroy(numa_gpu_vec* v) {
     if (!v) return NUMA_GPU_OK;
     if (v->owns && v->d) {
         cudaStreamSynchronize(v->ctx->impl->stream);
+        std::lock_guard<std::recursive_mutex> lk(alloc_capture_mutex());
         cudaFree(v->d);
     }
     delete v;
@@ -1072,6 +1075,95 @@ int numa_gpu_solve_burgers2d_host(numa_gpu_ctx* ctx, size_t n, double nu, double
     });
     result->status = rc;
     return rc;
+}
+
+// ------------------------------------------------------------------------------ batched solves
+static std::mutex g_batch_err_mutex;
+static std::string g_batch_err;
+
+static void set_batch_error(const char* msg) {
+    std::lock_guard<std::mutex> lk(g_batch_err_mutex);
+    g_batch_err = msg;
+}
+
+const char* numa_gpu_batch_last_error(void) {
+    std::lock_guard<std::mutex> lk(g_batch_err_mutex);
+    return g_batch_err.c_str();
+}
+
+struct numa_gpu_batch {
+    std::unique_ptr<BatchExecutor> impl;
+};
+
+int numa_gpu_batch_create(int device, int workers, numa_gpu_batch** out) {
+    if (!out || workers < 1) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    set_batch_error("");
+    try {
+        auto h = std::make_unique<numa_gpu_batch>();
+        h->impl = std::make_unique<BatchExecutor>(device, workers);
+        *out = h.release();
+        return NUMA_GPU_OK;
+    } catch (const Status& s) {
+        set_batch_error(s.what());
+        return s.code;
+    } catch (const std::exception& e) {
+        set_batch_error(e.what());
+        return NUMA_GPU_ERR_CUDA;
+    }
+}
+
+int numa_gpu_batch_destroy(numa_gpu_batch* b) {
+    delete b;
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_batch_solve(numa_gpu_batch* b, const numa_batch_instance* inst, size_t count, int method,
+                         int mg_precision, const numa_krylov_params* p, numa_batch_result* results,
+                         double* wall_seconds) {
+    if (!b || (count && (!inst || !results))) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    if (method < NUMA_GPU_METHOD_NK || method > NUMA_GPU_METHOD_TF2018) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    if (mg_precision != NUMA_GPU_FP64 && mg_precision != NUMA_GPU_FP32) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    for (size_t i = 0; i < count; ++i)
+        if (inst[i].n == 0 || inst[i].n > 1290) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    std::memset(results, 0, count * sizeof(numa_batch_result));
+    set_batch_error("");
+    try {
+        b->impl->solve(inst, count, method, mg_precision, p, results, wall_seconds);
+        return NUMA_GPU_OK;
+    } catch (const Status& s) {
+        set_batch_error(s.what());
+        return s.code;
+    } catch (const std::exception& e) {
+        set_batch_error(e.what());
+        return NUMA_GPU_ERR_CUDA;
+    }
+}
+
+int numa_gpu_solve_batch(int device, const numa_batch_instance* inst, size_t count, int method, int mg_precision,
+                         const numa_krylov_params* p, int workers, numa_batch_result* results,
+                         double* wall_seconds) {
+    if ((count && (!inst || !results)) || workers < 1) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    if (method < NUMA_GPU_METHOD_NK || method > NUMA_GPU_METHOD_TF2018) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    if (mg_precision != NUMA_GPU_FP64 && mg_precision != NUMA_GPU_FP32) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    for (size_t i = 0; i < count; ++i)
+        if (inst[i].n == 0 || inst[i].n > 1290) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    std::memset(results, 0, count * sizeof(numa_batch_result));
+    set_batch_error("");
+    try {
+        BatchExecutor ex(device, workers);
+        ex.solve(inst, count, method, mg_precision, p, results, wall_seconds);
+        return NUMA_GPU_OK;
+    } catch (const Status& s) {
+        set_batch_error(s.what());
+        return s.code;
+    } catch (const std::bad_alloc&) {
+        set_batch_error("host allocation failed");
+        return NUMA_GPU_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception& e) {
+        set_batch_error(e.what());
+        return NUMA_GPU_ERR_CUDA;
+    }
 }
 
 // ------------------------------------------------------------------------------ diagnostics

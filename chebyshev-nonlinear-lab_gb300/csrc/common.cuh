@@ -14,6 +14,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 
@@ -247,6 +248,13 @@ __device__ __forceinline__ double exp_tang(double x) {
 }
 
 // ------------------------------------------------------------------------------------------
+// One process-wide lock held across every CUDA-graph capture and around every device or pinned
+// allocation and free: cudaFree / cudaMallocHost may synchronise the whole device, which would
+// break a capture another thread (another context) has in progress.  Recursive, so a capture
+// that allocated would fail in CUDA rather than deadlock here.
+std::recursive_mutex& alloc_capture_mutex();
+
+// ------------------------------------------------------------------------------------------
 // Host-side context: one device, one stream, reduction scratch and device scalars.
 constexpr int kNumScalars = 2048;
 constexpr size_t kMaxRestart = 250;  // GMRES(m) limit of the device scalar layout below
@@ -307,10 +315,14 @@ struct PinnedBuf {
     PinnedBuf(const PinnedBuf&) = delete;
     PinnedBuf& operator=(const PinnedBuf&) = delete;
     ~PinnedBuf() {
-        if (p) cudaFreeHost(p);
+        if (p) {
+            std::lock_guard<std::recursive_mutex> lk(alloc_capture_mutex());
+            cudaFreeHost(p);
+        }
     }
     double* get(size_t count) {
         if (count > cap) {
+            std::lock_guard<std::recursive_mutex> lk(alloc_capture_mutex());
             if (p) cudaFreeHost(p);
             p = nullptr;
             cap = 0;
@@ -343,6 +355,7 @@ struct DeviceArray {
     }
     void resize(size_t count) {
         if (count > cap) {
+            std::lock_guard<std::recursive_mutex> lk(alloc_capture_mutex());
             release();
             if (count > 0) {
                 cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
@@ -358,7 +371,10 @@ struct DeviceArray {
         n = count;
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            std::lock_guard<std::recursive_mutex> lk(alloc_capture_mutex());
+            cudaFree(p);
+        }
         p = nullptr;
         n = cap = 0;
     }

@@ -15,6 +15,11 @@ void throw_cuda(cudaError_t e, const char* what, const char* file, int line) {
     throw Status(NUMA_GPU_ERR_CUDA, buf);
 }
 
+std::recursive_mutex& alloc_capture_mutex() {
+    static std::recursive_mutex m;
+    return m;
+}
+
 Context::Context(int dev) : device(dev) {
     int count = 0;
     cudaError_t e = cudaGetDeviceCount(&count);
@@ -26,6 +31,7 @@ Context::Context(int dev) : device(dev) {
     NUMA_CUDA(cudaSetDevice(dev));
     NUMA_CUDA(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev));
     NUMA_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    std::lock_guard<std::recursive_mutex> lk(alloc_capture_mutex());
     NUMA_CUDA(cudaMalloc(reinterpret_cast<void**>(&red.partials),
                          sizeof(double) * kMaxRedBlocks * kMaxRedResults));
     NUMA_CUDA(cudaMalloc(reinterpret_cast<void**>(&red.ticket), sizeof(unsigned)));
@@ -39,6 +45,7 @@ Context::Context(int dev) : device(dev) {
 
 Context::~Context() {
     if (stream) cudaStreamSynchronize(stream);
+    std::lock_guard<std::recursive_mutex> lk(alloc_capture_mutex());
     if (red.partials) cudaFree(red.partials);
     if (red.ticket) cudaFree(red.ticket);
     if (d_scalars) cudaFree(d_scalars);

@@ -90,6 +90,8 @@ public:
     size_t grid() const { return n_; }
     double lambda() const { return lambda_; }
     double h2inv() const { return h2inv_; }
+    // A new lambda for the same grid (kernels take lambda as a parameter; nothing is cached on it).
+    void set_lambda(double lambda) { lambda_ = lambda; }
 
     // NonlinearOp: the cache of an iterate x is c = lambda e^x; for FP32 products it also holds
     // RN32(c) (N floats after the N doubles), written by the evaluation itself.
@@ -365,6 +367,21 @@ class Provider;
 std::unique_ptr<Provider> make_learned_provider(Context& ctx, size_t n, LearnedNet& net, double stall);
 void learned_provider_stats(Provider& p, size_t* applies, size_t* fallbacks);
 double forcing(const KrylovParams& p, size_t k, double rnorm, double rprev, double eta_prev, double res0);
+
+// Many independent Bratu3D solves on one device (batch.cu); results[i] for inst[i].
+struct BatchWorker;
+class BatchExecutor {
+public:
+    BatchExecutor(int device, int workers);
+    ~BatchExecutor();
+    int workers() const { return (int)workers_.size(); }
+    void solve(const numa_batch_instance* inst, size_t count, int method, int mg_precision,
+               const numa_krylov_params* params, numa_batch_result* results, double* wall_seconds);
+
+private:
+    int device_;
+    std::vector<std::unique_ptr<BatchWorker>> workers_;
+};
 
 // x holds x0 on entry and the final iterate on return.
 void newton_krylov(NonlinearOp& f, double* x, const KrylovParams& p, Provider* pc, numa_krylov_result& out);

@@ -152,6 +152,8 @@ PoissonMG::~PoissonMG() {
 
 void PoissonMG::coarse_cycle() {
     if (!coarse_exec_) {
+        // no other thread may allocate or free (and so synchronise the device) during the capture
+        std::lock_guard<std::recursive_mutex> lk(alloc_capture_mutex());
         const uint64_t before = ctx_.launches;
         NUMA_CUDA(cudaStreamBeginCapture(ctx_.stream, cudaStreamCaptureModeThreadLocal));
         cudaGraph_t graph = nullptr;

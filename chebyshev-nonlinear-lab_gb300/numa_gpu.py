@@ -60,6 +60,16 @@ class LearnedTrainReport(C.Structure):
                 ("loss_first", C.c_float), ("loss_last", C.c_float), ("target_ms", C.c_float)]
 
 
+class BatchInstance(C.Structure):
+    _fields_ = [("n", C.c_size_t), ("lambda_", C.c_double)]
+
+
+class BatchResult(C.Structure):
+    _fields_ = [("converged", C.c_int32), ("status", C.c_int32), ("iters", C.c_uint64), ("n_F", C.c_uint64),
+                ("n_JVP", C.c_uint64), ("n_lin_iters", C.c_uint64), ("n_prec", C.c_uint64), ("res_rel", C.c_double),
+                ("seconds", C.c_double)]
+
+
 class KrylovResult(C.Structure):
     """numa_krylov_result: KrylovResult (krylov_newton.hpp:40-49) plus timers."""
     _fields_ = [
@@ -173,6 +183,13 @@ SIGNATURES = {
     "numa_gpu_diag_time_smoother": ([_P, _I, _F64P], _I),
     "numa_gpu_diag_exp": ([_P, _P, _P], _I),
     "numa_gpu_diag_conv3d": ([_P, _SZ, _I, _I, _I, _F32P, _F32P, _F32P, _F32P], _I),
+    "numa_gpu_solve_batch": ([_I, C.POINTER(BatchInstance), _SZ, _I, _I, C.POINTER(KrylovParams), _I,
+                              C.POINTER(BatchResult), _F64P], _I),
+    "numa_gpu_batch_last_error": ([], C.c_char_p),
+    "numa_gpu_batch_create": ([_I, _I, _PP], _I),
+    "numa_gpu_batch_destroy": ([_P], _I),
+    "numa_gpu_batch_solve": ([_P, C.POINTER(BatchInstance), _SZ, _I, _I, C.POINTER(KrylovParams),
+                              C.POINTER(BatchResult), _F64P], _I),
     "numa_gpu_learned_create": ([_P, _SZ, C.c_uint64, _PP], _I),
     "numa_gpu_learned_destroy": ([_P], _I),
     "numa_gpu_learned_num_params": ([_P, C.POINTER(_SZ)], _I),
@@ -845,3 +862,53 @@ def solve_burgers2d_host(ctx: Context, n: int, nu: float, dt: float, amplitude: 
                                                x0.ctypes.data_as(_F64P), out.ctypes.data_as(_F64P), C.byref(res))
     ctx.check(rc, "solve_burgers2d_host")
     return out, to_dict(res)
+
+
+def solve_batch(instances, method: str = "nk", mg_precision: int = FP32, params: KrylovParams | None = None,
+                workers: int = 16, device: int = 0) -> tuple[list[dict], float]:
+    """numa_gpu_solve_batch: instances = [(n, lambda), ...]; returns per-instance results and wall seconds."""
+    lib = load()
+    arr = (BatchInstance * len(instances))(*[BatchInstance(int(n), float(lam)) for n, lam in instances])
+    res = (BatchResult * len(instances))()
+    wall = C.c_double()
+    p = params if params is not None else default_params()
+    rc = lib.numa_gpu_solve_batch(device, arr, len(instances), METHODS[method], mg_precision, C.byref(p), workers, res,
+                                  C.byref(wall))
+    if rc != OK:
+        raise NumaGPUError(rc, "numa_gpu_solve_batch", lib.numa_gpu_batch_last_error().decode())
+    return [to_dict(r) for r in res], wall.value
+
+
+class BatchExecutor:
+    """numa_gpu_batch_*: worker contexts and solvers kept between batches."""
+
+    def __init__(self, workers: int = 16, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.numa_gpu_batch_create(device, workers, C.byref(h))
+        if rc != OK:
+            raise NumaGPUError(rc, "numa_gpu_batch_create", self.lib.numa_gpu_batch_last_error().decode())
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.numa_gpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, instances, method: str = "nk", mg_precision: int = FP32,
+              params: KrylovParams | None = None) -> tuple[list[dict], float]:
+        arr = (BatchInstance * len(instances))(*[BatchInstance(int(n), float(lam)) for n, lam in instances])
+        res = (BatchResult * len(instances))()
+        wall = C.c_double()
+        p = params if params is not None else default_params()
+        rc = self.lib.numa_gpu_batch_solve(self.h, arr, len(instances), METHODS[method], mg_precision, C.byref(p),
+                                           res, C.byref(wall))
+        if rc != OK:
+            raise NumaGPUError(rc, "numa_gpu_batch_solve", self.lib.numa_gpu_batch_last_error().decode())
+        return [to_dict(r) for r in res], wall.value

@@ -377,6 +377,36 @@ int numa_gpu_provider_create_learned(numa_gpu_ctx* ctx, size_t n, numa_gpu_learn
 /* Network applications and fallbacks of a learned provider since its creation. */
 int numa_gpu_provider_learned_stats(numa_gpu_provider* p, size_t* applies, size_t* fallbacks);
 
+/* ---------------------------------------------------------------- batched solves */
+/* No counterpart in the reference.  Solves Bratu3D(inst[i].n, inst[i].lambda) from u0 = 0 for every
+ * instance with `method` and a PoissonMG V(2,2) provider of mg_precision, concurrently: `workers`
+ * host threads, each with its own context and stream on `device`, take instances largest first;
+ * operators, hierarchies and workspaces are kept per grid size and reused.  results[i] holds the
+ * counts of instance i; *wall_seconds the wall time of the whole batch (including the first use
+ * of each grid size on each worker). */
+typedef struct numa_batch_instance {
+    size_t n;
+    double lambda;
+} numa_batch_instance;
+typedef struct numa_batch_result {
+    int32_t converged, status;
+    uint64_t iters, n_F, n_JVP, n_lin_iters, n_prec;
+    double res_rel, seconds;
+} numa_batch_result;
+int numa_gpu_solve_batch(int device, const numa_batch_instance* inst, size_t count, int method, int mg_precision,
+                         const numa_krylov_params* p, int workers, numa_batch_result* results,
+                         double* wall_seconds);
+/* The same with the workers' device state (contexts, operators, hierarchies, workspaces) kept
+ * between calls: create once, solve many batches, destroy. */
+typedef struct numa_gpu_batch numa_gpu_batch;
+int numa_gpu_batch_create(int device, int workers, numa_gpu_batch** out);
+int numa_gpu_batch_destroy(numa_gpu_batch* b);
+int numa_gpu_batch_solve(numa_gpu_batch* b, const numa_batch_instance* inst, size_t count, int method,
+                         int mg_precision, const numa_krylov_params* p, numa_batch_result* results,
+                         double* wall_seconds);
+/* Message of the last failing batched call in this process ("" if it succeeded). */
+const char* numa_gpu_batch_last_error(void);
+
 /* ---------------------------------------------------------------- V-cycle without allocation */
 /* No counterpart in the reference.  For callers that cannot allocate device memory when they
  * apply the preconditioner (while a stream is being captured into a CUDA graph, inside another
