@@ -28,7 +28,7 @@ NVCC_FLAGS = [
     "--extended-lambda", "-Xptxas", "-warn-spills", f"-I{INCLUDE}",
 ]
 SOURCES = [
-    "context.cu", "bratu3d.cu", "ops.cu", "poisson_mg.cu", "hmg2d.cu", "gmres.cu", "drivers.cu", "capi.cu", "diag.cu",
+    "context.cu", "bratu3d.cu", "ops.cu", "poisson_mg.cu", "hmg2d.cu", "brusselator.cu", "gmres.cu", "drivers.cu", "capi.cu", "diag.cu",
     "mg_noalloc.cu", "learned.cu", "learned_net.cu", "batch.cu",
 ]
 HEADERS = ["common.cuh", "numa_internal.hpp", "mg_kernels.cuh", "learned_conv.cuh"]

@@ -1,0 +1,764 @@
+// brusselator.cu — the Brusselator family on the GPU.
+//
+// * Brusselator1D: the reference's Brusselator1DStep (problems/brusselator1d.hpp:22-192), one
+//   implicit-Euler step of the 1D reaction-diffusion system with Dirichlet u = 1, v = 3, and its
+//   point-block Jacobi preconditioner BrusselatorJacobi (:194-222).  Every expression follows the
+//   reference's order of operations (the library is compiled without FMA contraction), so F, J v,
+//   F'' and the block solves are bit-identical to the reference.
+// * Brusselator2D: the same reaction terms with parameters A, B, D_u, D_v, dt on an n x n periodic
+//   grid of the unit square (h = 1/n), the 2-species reaction-diffusion configuration; and
+//   BrussMG2D, a geometric multigrid for the coupled 2x2-block Jacobian K(w) - diag(D_u, D_v) Lap_h,
+//   in FP64 (bit-identical to the CPU restatement) or FP32.
+//
+// Layouts.  Operator vectors are the reference's: w = (u, v) component-major, each plane
+// row-major (i * n + j).  Inside BrussMG2D every level keeps (u, v) interleaved per point (one
+// 8-byte FP32 or 16-byte FP64 pair), and the 2x2 block (k11, k12, k21, k22) per point (16 or
+// 32 bytes), so a point-block update is one vector load of each.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "numa_internal.hpp"
+
+namespace numa::gpu {
+
+namespace {
+
+// ============================================================================== Brusselator1D
+struct B1Geom {
+    int n;
+    double invdt, h2inv, alpha, A, B, base;
+};
+
+// F(w) (brusselator1d.hpp:47-69): boundary values u = 1, v = 3 outside the grid.
+__global__ void __launch_bounds__(256) k_b1_eval(const double* __restrict__ w, const double* __restrict__ prev,
+                                                 double* __restrict__ out, B1Geom G) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = G.n;
+    if (i >= n) return;
+    const double u = w[i], v = w[n + i];
+    const double um = i > 0 ? w[i - 1] : 1.0, up = i + 1 < n ? w[i + 1] : 1.0;
+    const double vm = i > 0 ? w[n + i - 1] : 3.0, vp = i + 1 < n ? w[n + i + 1] : 3.0;
+    const double lu = (um - 2.0 * u + up) * G.h2inv;
+    const double lv = (vm - 2.0 * v + vp) * G.h2inv;
+    out[i] = (u - prev[i]) * G.invdt - G.alpha * lu - G.A - u * u * v + (G.B + 1.0) * u;
+    out[n + i] = (v - prev[n + i]) * G.invdt - G.alpha * lv - G.B * u + u * u * v;
+}
+
+// F'(w) d (:71-98): a direction is zero outside the grid.
+__global__ void __launch_bounds__(256) k_b1_jvp(const double* __restrict__ w, const double* __restrict__ d,
+                                                double* __restrict__ out, B1Geom G) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = G.n;
+    if (i >= n) return;
+    const double u = w[i], v = w[n + i], du = d[i], dv = d[n + i];
+    const double dum = i > 0 ? d[i - 1] : 0.0, dup = i + 1 < n ? d[i + 1] : 0.0;
+    const double dvm = i > 0 ? d[n + i - 1] : 0.0, dvp = i + 1 < n ? d[n + i + 1] : 0.0;
+    const double ldu = (dum - 2.0 * du + dup) * G.h2inv;
+    const double ldv = (dvm - 2.0 * dv + dvp) * G.h2inv;
+    out[i] = G.invdt * du - G.alpha * ldu - (2.0 * u * v) * du - u * u * dv + (G.B + 1.0) * du;
+    out[n + i] = G.invdt * dv - G.alpha * ldv - G.B * du + (2.0 * u * v) * du + u * u * dv;
+}
+
+// F''(w)[d, d] = (-q, q), q = 2 v du^2 + 4 u du dv (:100-118).  Also the 2D operator's (any plane size).
+__global__ void __launch_bounds__(256) k_bruss_d2(const double* __restrict__ w, const double* __restrict__ d,
+                                                  double* __restrict__ out, size_t m) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const double u = w[i], v = w[m + i], du = d[i], dv = d[m + i];
+    const double q = 2.0 * v * du * du + 4.0 * u * du * dv;
+    out[i] = -q;
+    out[m + i] = q;
+}
+
+// The 2x2 point blocks without the off-diagonal diffusion (:120-141), one plane each.
+__global__ void __launch_bounds__(256) k_b1_blocks(const double* __restrict__ w, double* __restrict__ a, B1Geom G) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = G.n;
+    if (i >= n) return;
+    const double u = w[i], v = w[n + i];
+    a[i] = G.base - 2.0 * u * v + (G.B + 1.0);
+    a[n + i] = -u * u;
+    a[2 * n + i] = -G.B + 2.0 * u * v;
+    a[3 * n + i] = G.base + u * u;
+}
+
+// BrusselatorJacobi::Bound (:198-214): z = block^-1 r, or z = r where the determinant is not
+// finite or below 1e-14 in magnitude.
+__global__ void __launch_bounds__(256) k_b1_block_apply(const double* __restrict__ a, const double* __restrict__ r,
+                                                        double* __restrict__ z, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double a11 = a[i], a12 = a[n + i], a21 = a[2 * n + i], a22 = a[3 * n + i];
+    const double ru = r[i], rv = r[n + i];
+    const double det = a11 * a22 - a12 * a21;
+    if (!isfinite(det) || fabs(det) < 1e-14) {
+        z[i] = ru;
+        z[n + i] = rv;
+        return;
+    }
+    z[i] = (a22 * ru - a12 * rv) / det;
+    z[n + i] = (-a21 * ru + a11 * rv) / det;
+}
+
+// ============================================================================== Brusselator2D
+struct B2Geom {
+    int n;
+    double h2inv, invdt, A, B, Du, Dv;
+};
+
+__device__ __forceinline__ double lap5(const double* __restrict__ a, int n, int i, int j, double c) {
+    const int jm = j == 0 ? n - 1 : j - 1, jp = j + 1 == n ? 0 : j + 1;
+    const int im = i == 0 ? n - 1 : i - 1, ip = i + 1 == n ? 0 : i + 1;
+    const size_t r = (size_t)i * n;
+    return (((a[r + jm] + a[r + jp]) + a[(size_t)im * n + j]) + a[(size_t)ip * n + j]) - 4.0 * c;
+}
+
+// F(w) = (w - w_prev)/dt - D Lap_h w - reaction, the reference's 1D expressions on the periodic
+// 5-point stencil; optionally ||F||.  Blocks of 32 x 8 stride over rows, so the grid has at
+// most kMaxRedBlocks blocks.
+template <bool NORM>
+__global__ void __launch_bounds__(256) k_b2_eval(const double* __restrict__ w, const double* __restrict__ prev,
+                                                 double* __restrict__ out, B2Geom G, RedArgs red, double* norm_out) {
+    const int n = G.n;
+    const size_t nn = (size_t)n * n;
+    const int j = blockIdx.x * 32 + threadIdx.x;
+    const double* wu = w;
+    const double* wv = w + nn;
+    double acc[1] = {0.0};
+    if (j < n) {
+        for (int i = blockIdx.y * 8 + threadIdx.y; i < n; i += gridDim.y * 8) {
+            const size_t p = (size_t)i * n + j;
+            const double u = wu[p], v = wv[p];
+            const double lu = lap5(wu, n, i, j, u) * G.h2inv;
+            const double lv = lap5(wv, n, i, j, v) * G.h2inv;
+            const double fu = (u - prev[p]) * G.invdt - G.Du * lu - G.A - u * u * v + (G.B + 1.0) * u;
+            const double fv = (v - prev[nn + p]) * G.invdt - G.Dv * lv - G.B * u + u * u * v;
+            out[p] = fu;
+            out[nn + p] = fv;
+            if (NORM) acc[0] = __fma_rn(fv, fv, __fma_rn(fu, fu, acc[0]));
+        }
+    }
+    if (NORM) {
+        __shared__ double sm[1][32];
+        block_sum<1>(acc, sm);
+        grid_reduce_finish<1>(acc, red, [norm_out] __device__(const double(&t)[1]) { *norm_out = __dsqrt_rn(t[0]); });
+    }
+}
+
+__global__ void __launch_bounds__(256) k_b2_jvp(const double* __restrict__ w, const double* __restrict__ d,
+                                                double* __restrict__ out, B2Geom G) {
+    const int n = G.n;
+    const size_t nn = (size_t)n * n;
+    const int j = blockIdx.x * 32 + threadIdx.x;
+    if (j >= n) return;
+    for (int i = blockIdx.y * 8 + threadIdx.y; i < n; i += gridDim.y * 8) {
+        const size_t p = (size_t)i * n + j;
+        const double u = w[p], v = w[nn + p], du = d[p], dv = d[nn + p];
+        const double ldu = lap5(d, n, i, j, du) * G.h2inv;
+        const double ldv = lap5(d + nn, n, i, j, dv) * G.h2inv;
+        out[p] = G.invdt * du - G.Du * ldu - (2.0 * u * v) * du - u * u * dv + (G.B + 1.0) * du;
+        out[nn + p] = G.invdt * dv - G.Dv * ldv - G.B * du + (2.0 * u * v) * du + u * u * dv;
+    }
+}
+
+dim3 b2_grid(int n) {
+    const unsigned gx = (unsigned)((n + 31) / 32);
+    const unsigned rows = (unsigned)((n + 7) / 8);
+    const unsigned gy = std::max(1u, std::min(rows, (unsigned)kMaxRedBlocks / gx));
+    return dim3(gx, gy);
+}
+
+// ============================================================================== BrussMG2D kernels
+template <class T> struct P2;
+template <> struct P2<float> { using t = float2; };
+template <> struct P2<double> { using t = double2; };
+
+template <class T>
+struct Blk {
+    T k11, k12, k21, k22;
+};
+
+__device__ __forceinline__ Blk<float> load_blk(const float* __restrict__ K, size_t p) {
+    const float4 q = __ldg(reinterpret_cast<const float4*>(K) + p);
+    return {q.x, q.y, q.z, q.w};
+}
+__device__ __forceinline__ Blk<double> load_blk(const double* __restrict__ K, size_t p) {
+    const double2 a = __ldg(reinterpret_cast<const double2*>(K) + 2 * p);
+    const double2 b = __ldg(reinterpret_cast<const double2*>(K) + 2 * p + 1);
+    return {a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ void store_blk(float* K, size_t p, const Blk<float>& k) {
+    reinterpret_cast<float4*>(K)[p] = make_float4(k.k11, k.k12, k.k21, k.k22);
+}
+__device__ __forceinline__ void store_blk(double* K, size_t p, const Blk<double>& k) {
+    reinterpret_cast<double2*>(K)[2 * p] = make_double2(k.k11, k.k12);
+    reinterpret_cast<double2*>(K)[2 * p + 1] = make_double2(k.k21, k.k22);
+}
+
+template <class T>
+__device__ __forceinline__ typename P2<T>::t ld2(const T* a, size_t p) {
+    return reinterpret_cast<const typename P2<T>::t*>(a)[p];
+}
+template <class T>
+__device__ __forceinline__ void st2(T* a, size_t p, T u, T v) {
+    typename P2<T>::t q;
+    q.x = u;
+    q.y = v;
+    reinterpret_cast<typename P2<T>::t*>(a)[p] = q;
+}
+
+// Point-block Gauss-Seidel update: (K + 4 diag(s_u, s_v)) (u, v) = (b_u + s_u S_u, b_v + s_v S_v),
+// S = ((W + E) + S) + N, by Cramer's rule with two divisions.
+template <class T>
+__device__ __forceinline__ void block_update(const Blk<T>& k, T su, T sv, T su4, T sv4, T bu, T bv, T Su, T Sv,
+                                             T& u, T& v) {
+    const T ru = bu + su * Su;
+    const T rv = bv + sv * Sv;
+    const T m11 = k.k11 + su4, m22 = k.k22 + sv4;
+    const T det = m11 * m22 - k.k12 * k.k21;
+    u = (m22 * ru - k.k12 * rv) / det;
+    v = (m11 * rv - k.k21 * ru) / det;
+}
+
+struct LvlArgs {
+    int n;
+    double su, sv;
+};
+
+template <class T>
+__device__ __forceinline__ void nbr_sums(const T* __restrict__ X, int n, int i, int j, T& Su, T& Sv) {
+    const int jm = j == 0 ? n - 1 : j - 1, jp = j + 1 == n ? 0 : j + 1;
+    const int im = i == 0 ? n - 1 : i - 1, ip = i + 1 == n ? 0 : i + 1;
+    const size_t r = (size_t)i * n;
+    const auto w = ld2(X, r + jm), e = ld2(X, r + jp), s = ld2(X, (size_t)im * n + j), nn = ld2(X, (size_t)ip * n + j);
+    Su = ((w.x + e.x) + s.x) + nn.x;
+    Sv = ((w.y + e.y) + s.y) + nn.y;
+}
+
+enum { kBPassNormal = 0, kBPassFirst = 1, kBPassLast = 2 };
+
+// One colour of red-black point-block Gauss-Seidel on one level.  Thread (jj, i) owns the pair
+// of row i's points 2jj and 2jj + 1 (one of each colour) and updates the one of this colour.
+//  Normal: x_c updated from the other colour.
+//  First (colour 0, x = 0 before the pass): x_0 = block^-1 b (neighbour sums are zeros), x_1 = 0;
+//    on the finest level the right-hand side is read from r (FP64 planes) and stored as b.
+//  Last (finest level, colour 0, the cycle's final pass): also writes z (FP64 planes) for both points.
+template <class T, int MODE>
+__global__ void __launch_bounds__(256) k_bmg_pass(T* __restrict__ X, T* __restrict__ Bv, const T* __restrict__ K,
+                                                  LvlArgs L, int colour, const double* __restrict__ r64,
+                                                  double* __restrict__ z64) {
+    const int n = L.n;
+    const int jj = blockIdx.x * 32 + threadIdx.x;
+    const int i = blockIdx.y * 8 + threadIdx.y;
+    if (i >= n || 2 * jj >= n) return;
+    const T su = (T)L.su, sv = (T)L.sv, su4 = (T)(4.0 * L.su), sv4 = (T)(4.0 * L.sv);
+    const int j = 2 * jj + ((i + colour) & 1);
+    const int jo = 2 * jj + 1 - ((i + colour) & 1);
+    const size_t p = (size_t)i * n + j, po = (size_t)i * n + jo;
+    const size_t nn = (size_t)n * n;
+    T bu, bv;
+    if (MODE == kBPassFirst && r64) {
+        bu = (T)r64[p];
+        bv = (T)r64[nn + p];
+        st2(Bv, p, bu, bv);
+        st2(Bv, po, (T)r64[po], (T)r64[nn + po]);
+    } else {
+        const auto b = ld2(Bv, p);
+        bu = b.x;
+        bv = b.y;
+    }
+    T Su, Sv;
+    if (MODE == kBPassFirst) {
+        Su = T(0);
+        Sv = T(0);
+    } else {
+        nbr_sums(X, n, i, j, Su, Sv);
+    }
+    T u, v;
+    block_update(load_blk(K, p), su, sv, su4, sv4, bu, bv, Su, Sv, u, v);
+    st2(X, p, u, v);
+    if (MODE == kBPassFirst) st2(X, po, T(0), T(0));
+    if (MODE == kBPassLast) {
+        const auto o = ld2(X, po);
+        z64[p] = (double)u;
+        z64[nn + p] = (double)v;
+        z64[po] = (double)o.x;
+        z64[nn + po] = (double)o.y;
+    }
+}
+
+// Residual r = b - (K x - diag(s) (S - 4x)) on the finest-level points that a 16 x 16 tile of
+// coarse points covers (33 x 33, periodic), kept in shared memory, then 9-point full weighting
+// ((4c + 2((W + E) + (S + N))) + (((SW + SE) + NW) + NE)) / 16 into the coarse right-hand side.
+template <class T>
+__global__ void __launch_bounds__(256) k_bmg_restrict(const T* __restrict__ X, const T* __restrict__ Bv,
+                                                      const T* __restrict__ K, LvlArgs L, T* __restrict__ Bc) {
+    constexpr int TS = 16, FS = 2 * TS + 1;
+    __shared__ T su_s[FS][FS + 1], sv_s[FS][FS + 1];
+    const int nf = L.n, nc = nf / 2;
+    const int I0 = blockIdx.y * TS, J0 = blockIdx.x * TS;
+    const int tid = threadIdx.y * TS + threadIdx.x;
+    const T su = (T)L.su, sv = (T)L.sv;
+    for (int idx = tid; idx < FS * FS; idx += TS * TS) {
+        const int a = idx / FS, b = idx - a * FS;
+        const int fi = (2 * I0 - 1 + a + nf) % nf, fj = (2 * J0 - 1 + b + nf) % nf;
+        const size_t p = (size_t)fi * nf + fj;
+        const auto x = ld2(X, p);
+        const auto bb = ld2(Bv, p);
+        const Blk<T> k = load_blk(K, p);
+        T Su, Sv;
+        nbr_sums(X, nf, fi, fj, Su, Sv);
+        su_s[a][b] = bb.x - ((k.k11 * x.x + k.k12 * x.y) + su * (T(4) * x.x - Su));
+        sv_s[a][b] = bb.y - ((k.k21 * x.x + k.k22 * x.y) + sv * (T(4) * x.y - Sv));
+    }
+    __syncthreads();
+    const int I = I0 + threadIdx.y, J = J0 + threadIdx.x;
+    if (I >= nc || J >= nc) return;
+    const int a = 2 * threadIdx.y + 1, b = 2 * threadIdx.x + 1;
+    auto fw = [a, b](const T (*f)[FS + 1]) {
+        const T ctr = f[a][b];
+        const T edge = (f[a][b - 1] + f[a][b + 1]) + (f[a - 1][b] + f[a + 1][b]);
+        const T corner = ((f[a - 1][b - 1] + f[a - 1][b + 1]) + f[a + 1][b - 1]) + f[a + 1][b + 1];
+        return ((T(4) * ctr + T(2) * edge) + corner) * T(0.0625);
+    };
+    st2(Bc, (size_t)I * nc + J, fw(su_s), fw(sv_s));
+}
+
+// x_fine += bilinear periodic interpolation of x_coarse; thread per coarse point (I, J) owns
+// fine (2I + {0,1}, 2J + {0,1}).
+template <class T>
+__global__ void __launch_bounds__(256) k_bmg_prolong(const T* __restrict__ Xc, int nc, T* __restrict__ Xf) {
+    const int J = blockIdx.x * 32 + threadIdx.x;
+    const int I = blockIdx.y * 8 + threadIdx.y;
+    if (I >= nc || J >= nc) return;
+    const int I1 = I + 1 == nc ? 0 : I + 1, J1 = J + 1 == nc ? 0 : J + 1;
+    const auto c00 = ld2(Xc, (size_t)I * nc + J), c10 = ld2(Xc, (size_t)I1 * nc + J);
+    const auto c01 = ld2(Xc, (size_t)I * nc + J1), c11 = ld2(Xc, (size_t)I1 * nc + J1);
+    const int nf = 2 * nc;
+    const size_t f00 = (size_t)(2 * I) * nf + 2 * J, f10 = f00 + nf;
+    auto add = [Xf](size_t p, T du, T dv) {
+        const auto x = ld2(Xf, p);
+        st2(Xf, p, x.x + du, x.y + dv);
+    };
+    add(f00, c00.x, c00.y);
+    add(f10, T(0.5) * (c00.x + c10.x), T(0.5) * (c00.y + c10.y));
+    add(f00 + 1, T(0.5) * (c00.x + c01.x), T(0.5) * (c00.y + c01.y));
+    add(f10 + 1, T(0.25) * (((c00.x + c10.x) + c01.x) + c11.x), T(0.25) * (((c00.y + c10.y) + c01.y) + c11.y));
+}
+
+// The coarsest level in one block: x = 0, then `sweeps` red-black sweeps (colour 0, 1).
+template <class T>
+__global__ void __launch_bounds__(1024) k_bmg_coarsest(T* __restrict__ X, const T* __restrict__ Bv,
+                                                       const T* __restrict__ K, LvlArgs L, int sweeps) {
+    const int n = L.n;
+    const int nn = n * n;
+    const T su = (T)L.su, sv = (T)L.sv, su4 = (T)(4.0 * L.su), sv4 = (T)(4.0 * L.sv);
+    for (int p = threadIdx.x; p < nn; p += blockDim.x) st2(X, p, T(0), T(0));
+    __syncthreads();
+    for (int s = 0; s < sweeps; ++s) {
+        for (int c = 0; c < 2; ++c) {
+            for (int p = threadIdx.x; p < nn; p += blockDim.x) {
+                const int i = p / n, j = p - i * n;
+                if (((i + j) & 1) != c) continue;
+                T Su, Sv, u, v;
+                nbr_sums(X, n, i, j, Su, Sv);
+                const auto b = ld2(Bv, p);
+                block_update(load_blk(K, p), su, sv, su4, sv4, b.x, b.y, Su, Sv, u, v);
+                st2(X, p, u, v);
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// K at the finest level from the FP64 state: [[1/dt + B + 1 - 2uv, -u^2], [2uv - B, 1/dt + u^2]].
+template <class T>
+__global__ void __launch_bounds__(256) k_bmg_kfine(const double* __restrict__ w, size_t nn, double c1, double c2,
+                                                   double B, T* __restrict__ K) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nn) return;
+    const double u = w[p], v = w[nn + p];
+    Blk<T> k;
+    k.k11 = (T)(c1 - (2.0 * u) * v);
+    k.k12 = (T)(-(u * u));
+    k.k21 = (T)((2.0 * u) * v - B);
+    k.k22 = (T)(c2 + u * u);
+    store_blk(K, p, k);
+}
+
+// Full weighting of the four block components to the next coarser level.
+template <class T>
+__global__ void __launch_bounds__(256) k_bmg_krestrict(const T* __restrict__ Kf, int nf, T* __restrict__ Kc) {
+    const int nc = nf / 2;
+    const int J = blockIdx.x * 32 + threadIdx.x;
+    const int I = blockIdx.y * 8 + threadIdx.y;
+    if (I >= nc || J >= nc) return;
+    const int i = 2 * I, j = 2 * J;
+    const int im = i == 0 ? nf - 1 : i - 1, ip = i + 1, jm = j == 0 ? nf - 1 : j - 1, jp = j + 1;
+    auto at = [Kf, nf](int a, int b) { return load_blk(Kf, (size_t)a * nf + b); };
+    const Blk<T> c = at(i, j), w = at(i, jm), e = at(i, jp), s = at(im, j), nth = at(ip, j);
+    const Blk<T> sw = at(im, jm), se = at(im, jp), nw = at(ip, jm), ne = at(ip, jp);
+    auto fw = [](T ctr, T w_, T e_, T s_, T n_, T sw_, T se_, T nw_, T ne_) {
+        const T edge = (w_ + e_) + (s_ + n_);
+        const T corner = ((sw_ + se_) + nw_) + ne_;
+        return ((T(4) * ctr + T(2) * edge) + corner) * T(0.0625);
+    };
+    Blk<T> o;
+    o.k11 = fw(c.k11, w.k11, e.k11, s.k11, nth.k11, sw.k11, se.k11, nw.k11, ne.k11);
+    o.k12 = fw(c.k12, w.k12, e.k12, s.k12, nth.k12, sw.k12, se.k12, nw.k12, ne.k12);
+    o.k21 = fw(c.k21, w.k21, e.k21, s.k21, nth.k21, sw.k21, se.k21, nw.k21, ne.k21);
+    o.k22 = fw(c.k22, w.k22, e.k22, s.k22, nth.k22, sw.k22, se.k22, nw.k22, ne.k22);
+    store_blk(Kc, (size_t)I * nc + J, o);
+}
+
+// FP64 planes <-> interleaved level pairs (used only when the finest level is also the coarsest).
+template <class T>
+__global__ void k_bmg_in(const double* __restrict__ r, size_t nn, T* __restrict__ B) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < nn) st2(B, p, (T)r[p], (T)r[nn + p]);
+}
+template <class T>
+__global__ void k_bmg_out(const T* __restrict__ X, size_t nn, double* __restrict__ z) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < nn) {
+        const auto x = ld2(X, p);
+        z[p] = (double)x.x;
+        z[nn + p] = (double)x.y;
+    }
+}
+
+constexpr int kBmgCoarsestSweeps = 30;
+constexpr int kBmgOneBlockPoints = 4096;
+
+}  // namespace
+
+// ============================================================================== Brusselator1D
+Brusselator1D::Brusselator1D(Context& ctx, size_t n, double dt) : NonlinearOp(ctx), n_(n), dt_(dt) {
+    if (n == 0 || !(dt > 0.0) || !std::isfinite(dt))
+        throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Brusselator1DStep requires valid n and dt");
+    if (n > (size_t)1 << 28) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "Brusselator1DStep grid too large");
+    h_ = 1.0 / (static_cast<double>(n) + 1.0);
+    h2inv_ = 1.0 / (h_ * h_);
+    // previous state u = 1 + sin(2 pi x), v = 3 at x = (i + 1) h (brusselator1d.hpp:30-37)
+    std::vector<double> prev(2 * n);
+    const double pi = std::acos(-1.0);
+    for (size_t i = 0; i < n; ++i) {
+        const double x = (static_cast<double>(i) + 1.0) * h_;
+        prev[i] = 1.0 + std::sin(2.0 * pi * x);
+        prev[n + i] = 3.0;
+    }
+    prev_.resize(2 * n);
+    NUMA_CUDA(cudaMemcpyAsync(prev_.p, prev.data(), 2 * n * sizeof(double), cudaMemcpyHostToDevice, ctx_.stream));
+    ctx_.sync();
+}
+
+static B1Geom b1_geom(size_t n, double dt, double h2inv) {
+    B1Geom G;
+    G.n = (int)n;
+    G.invdt = 1.0 / dt;
+    G.h2inv = h2inv;
+    G.alpha = Brusselator1D::kAlpha;
+    G.A = Brusselator1D::kA;
+    G.B = Brusselator1D::kB;
+    G.base = 1.0 / dt + 2.0 * Brusselator1D::kAlpha * h2inv;
+    return G;
+}
+
+void Brusselator1D::eval(const double* x, double* out, double*, double* norm_out) {
+    k_b1_eval<<<(unsigned)((n_ + 255) / 256), 256, 0, ctx_.stream>>>(x, prev_.p, out, b1_geom(n_, dt_, h2inv_));
+    ctx_.count_launch();
+    ctx_.check_launch("Brusselator1D eval");
+    if (norm_out) dev_norm2(ctx_, out, size(), norm_out);
+}
+
+void Brusselator1D::jvp_at(const double* x, const double* v, double* out) {
+    k_b1_jvp<<<(unsigned)((n_ + 255) / 256), 256, 0, ctx_.stream>>>(x, v, out, b1_geom(n_, dt_, h2inv_));
+    ctx_.count_launch();
+    ctx_.check_launch("Brusselator1D jvp");
+}
+
+void Brusselator1D::d2(const double* x, const double*, const double* v, double* out) {
+    k_bruss_d2<<<(unsigned)((n_ + 255) / 256), 256, 0, ctx_.stream>>>(x, v, out, n_);
+    ctx_.count_launch();
+    ctx_.check_launch("Brusselator1D d2");
+}
+
+void Brusselator1D::blocks(const double* x, double* a) {
+    k_b1_blocks<<<(unsigned)((n_ + 255) / 256), 256, 0, ctx_.stream>>>(x, a, b1_geom(n_, dt_, h2inv_));
+    ctx_.count_launch();
+    ctx_.check_launch("Brusselator1D blocks");
+}
+
+void brusselator_block_apply(Context& ctx, const double* a, const double* r, double* z, size_t n) {
+    k_b1_block_apply<<<(unsigned)((n + 255) / 256), 256, 0, ctx.stream>>>(a, r, z, (int)n);
+    ctx.count_launch();
+    ctx.check_launch("BrusselatorJacobi apply");
+}
+
+namespace {
+// BrusselatorJacobi (brusselator1d.hpp:194-222): make(x) forms the point blocks at x.
+class BrussJacobiProvider final : public Provider {
+public:
+    explicit BrussJacobiProvider(Brusselator1D& op) : op_(op) { a_.resize(4 * op.grid()); }
+    void make(const double* x, const double*) override { op_.blocks(x, a_.p); }
+    void apply(const double* r, double* z) override { brusselator_block_apply(op_.ctx(), a_.p, r, z, op_.grid()); }
+    int kind() const override { return NUMA_GPU_PRECOND_BRUSS_JACOBI; }
+
+private:
+    Brusselator1D& op_;
+    DeviceArray<double> a_;
+};
+}  // namespace
+
+std::unique_ptr<Provider> make_bruss_jacobi_provider(Brusselator1D& op) {
+    return std::make_unique<BrussJacobiProvider>(op);
+}
+
+// ============================================================================== Brusselator2D
+Brusselator2D::Brusselator2D(Context& ctx, size_t n, const numa_brusselator2d_params& p)
+    : NonlinearOp(ctx), n_(n), P_(p) {
+    if (n < 3 || !(p.dt > 0.0) || !std::isfinite(p.dt) || !(p.Du >= 0.0) || !(p.Dv >= 0.0) || !std::isfinite(p.A) ||
+        !std::isfinite(p.B) || !std::isfinite(p.Du) || !std::isfinite(p.Dv))
+        throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Brusselator2D requires n >= 3, dt > 0, D >= 0");
+    if (n > 46340) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "Brusselator2D grid too large");
+    prev_.resize(2 * n * n);
+    dev_fill(ctx_, prev_.p, 0.0, 2 * n * n);
+}
+
+static B2Geom b2_geom(size_t n, const numa_brusselator2d_params& P) {
+    B2Geom G;
+    G.n = (int)n;
+    G.h2inv = static_cast<double>(n) * static_cast<double>(n);
+    G.invdt = 1.0 / P.dt;
+    G.A = P.A;
+    G.B = P.B;
+    G.Du = P.Du;
+    G.Dv = P.Dv;
+    return G;
+}
+
+void Brusselator2D::set_previous(const double* w) { dev_copy(ctx_, w, prev_.p, size()); }
+
+void Brusselator2D::eval(const double* x, double* out, double*, double* norm_out) {
+    const dim3 grid = b2_grid((int)n_);
+    if (norm_out)
+        k_b2_eval<true><<<grid, dim3(32, 8), 0, ctx_.stream>>>(x, prev_.p, out, b2_geom(n_, P_), ctx_.red, norm_out);
+    else
+        k_b2_eval<false><<<grid, dim3(32, 8), 0, ctx_.stream>>>(x, prev_.p, out, b2_geom(n_, P_), ctx_.red, nullptr);
+    ctx_.count_launch();
+    ctx_.check_launch("Brusselator2D eval");
+}
+
+void Brusselator2D::jvp_at(const double* x, const double* v, double* out) {
+    k_b2_jvp<<<b2_grid((int)n_), dim3(32, 8), 0, ctx_.stream>>>(x, v, out, b2_geom(n_, P_));
+    ctx_.count_launch();
+    ctx_.check_launch("Brusselator2D jvp");
+}
+
+void Brusselator2D::d2(const double* x, const double*, const double* v, double* out) {
+    const size_t nn = n_ * n_;
+    k_bruss_d2<<<(unsigned)((nn + 255) / 256), 256, 0, ctx_.stream>>>(x, v, out, nn);
+    ctx_.count_launch();
+    ctx_.check_launch("Brusselator2D d2");
+}
+
+// ============================================================================== BrussMG2D
+struct BrussMG2D::Level {
+    int n;
+    double su, sv;
+    DeviceArray<double> x, b, k;  // level pairs and blocks in the multigrid's precision
+};
+
+BrussMG2D::BrussMG2D(Context& ctx, size_t n, const numa_brusselator2d_params& p, int precision, int pre, int post)
+    : ctx_(ctx), n0_(n), P_(p), precision_(precision), pre_(pre), post_(post) {
+    if (n < 4 || n % 2 != 0) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "BrussMG2D needs an even n >= 4");
+    if (n > 46340) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "BrussMG2D grid too large");
+    if (pre < 1 || post < 1) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "BrussMG2D needs pre >= 1 and post >= 1");
+    if (precision != NUMA_GPU_FP64 && precision != NUMA_GPU_FP32)
+        throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "BrussMG2D precision must be FP64 or FP32");
+    if (!(p.dt > 0.0) || !(p.Du >= 0.0) || !(p.Dv >= 0.0))
+        throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "BrussMG2D requires dt > 0 and D >= 0");
+    const size_t esz = precision == NUMA_GPU_FP64 ? 8 : 4;
+    size_t m = n;
+    for (;;) {
+        auto L = std::make_unique<Level>();
+        L->n = (int)m;
+        L->su = p.Du * (static_cast<double>(m) * static_cast<double>(m));
+        L->sv = p.Dv * (static_cast<double>(m) * static_cast<double>(m));
+        const size_t mm = m * m;
+        L->x.resize((2 * mm * esz + 7) / 8);
+        L->b.resize((2 * mm * esz + 7) / 8);
+        L->k.resize((4 * mm * esz + 7) / 8);
+        levels_.push_back(std::move(L));
+        if (m % 4 != 0 || m / 2 < 4) break;
+        m /= 2;
+    }
+}
+
+BrussMG2D::~BrussMG2D() {
+    if (coarse_exec_) cudaGraphExecDestroy(coarse_exec_);
+}
+
+template <class T>
+static T* tp(DeviceArray<double>& a) {
+    return reinterpret_cast<T*>(a.p);
+}
+
+void BrussMG2D::set_state(const double* w) {
+    const size_t nn = n0_ * n0_;
+    const double c1 = 1.0 / P_.dt + (P_.B + 1.0), c2 = 1.0 / P_.dt;
+    const unsigned g = (unsigned)((nn + 255) / 256);
+    if (precision_ == NUMA_GPU_FP64)
+        k_bmg_kfine<double><<<g, 256, 0, ctx_.stream>>>(w, nn, c1, c2, P_.B, tp<double>(levels_[0]->k));
+    else
+        k_bmg_kfine<float><<<g, 256, 0, ctx_.stream>>>(w, nn, c1, c2, P_.B, tp<float>(levels_[0]->k));
+    ctx_.count_launch();
+    for (size_t l = 0; l + 1 < levels_.size(); ++l) {
+        const int nc = levels_[l + 1]->n;
+        const dim3 grid((unsigned)((nc + 31) / 32), (unsigned)((nc + 7) / 8));
+        if (precision_ == NUMA_GPU_FP64)
+            k_bmg_krestrict<double><<<grid, dim3(32, 8), 0, ctx_.stream>>>(tp<double>(levels_[l]->k), levels_[l]->n,
+                                                                          tp<double>(levels_[l + 1]->k));
+        else
+            k_bmg_krestrict<float><<<grid, dim3(32, 8), 0, ctx_.stream>>>(tp<float>(levels_[l]->k), levels_[l]->n,
+                                                                         tp<float>(levels_[l + 1]->k));
+        ctx_.count_launch();
+    }
+    ctx_.check_launch("BrussMG2D set_state");
+}
+
+template <class T>
+void BrussMG2D::cycle(size_t l) {
+    Level& L = *levels_[l];
+    const int n = L.n;
+    const bool finest = l == 0;
+    const bool coarsest = l + 1 == levels_.size();
+    cudaStream_t s = ctx_.stream;
+    T* X = tp<T>(L.x);
+    T* Bv = tp<T>(L.b);
+    const T* K = tp<T>(L.k);
+    const LvlArgs A{n, L.su, L.sv};
+    const dim3 blk(32, 8);
+    const dim3 pgrid((unsigned)((n / 2 + 31) / 32), (unsigned)((n + 7) / 8));
+    const size_t nn = (size_t)n * n;
+    if (coarsest) {
+        if (finest) {
+            k_bmg_in<T><<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(r0_, nn, Bv);
+            ctx_.count_launch();
+        }
+        if (nn <= (size_t)kBmgOneBlockPoints) {
+            k_bmg_coarsest<T><<<1, 1024, 0, s>>>(X, Bv, K, A, kBmgCoarsestSweeps);
+            ctx_.count_launch();
+        } else {
+            k_bmg_pass<T, kBPassFirst><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 0, nullptr, nullptr);
+            k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 1, nullptr, nullptr);
+            ctx_.count_launch(2);
+            for (int k = 1; k < kBmgCoarsestSweeps; ++k) {
+                k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 0, nullptr, nullptr);
+                k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 1, nullptr, nullptr);
+                ctx_.count_launch(2);
+            }
+        }
+        if (finest) {
+            k_bmg_out<T><<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(X, nn, z0_);
+            ctx_.count_launch();
+        }
+        return;
+    }
+    // pre-smoothing: colours 0, 1; the first pass starts from x = 0
+    k_bmg_pass<T, kBPassFirst><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 0, finest ? r0_ : nullptr, nullptr);
+    k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 1, nullptr, nullptr);
+    ctx_.count_launch(2);
+    for (int k = 1; k < pre_; ++k) {
+        k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 0, nullptr, nullptr);
+        k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 1, nullptr, nullptr);
+        ctx_.count_launch(2);
+    }
+    Level& C = *levels_[l + 1];
+    const int nc = C.n;
+    k_bmg_restrict<T><<<dim3((unsigned)((nc + 15) / 16), (unsigned)((nc + 15) / 16)), dim3(16, 16), 0, s>>>(
+        X, Bv, K, A, tp<T>(C.b));
+    ctx_.count_launch();
+    if (finest) coarse_cycle();
+    else cycle<T>(l + 1);
+    k_bmg_prolong<T><<<dim3((unsigned)((nc + 31) / 32), (unsigned)((nc + 7) / 8)), blk, 0, s>>>(tp<T>(C.x), nc, X);
+    ctx_.count_launch();
+    // post-smoothing: colours 1, 0; the very last pass of the finest level writes z
+    for (int k = 0; k < post_; ++k) {
+        k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 1, nullptr, nullptr);
+        if (finest && k + 1 == post_)
+            k_bmg_pass<T, kBPassLast><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 0, nullptr, z0_);
+        else
+            k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 0, nullptr, nullptr);
+        ctx_.count_launch(2);
+    }
+}
+
+// Levels 1 and below as one CUDA graph: their arrays never move, and the blocks K are updated in
+// place by set_state, so the graph captured on first use stays valid.
+void BrussMG2D::coarse_cycle() {
+    if (!coarse_exec_) {
+        std::lock_guard<std::recursive_mutex> lk(alloc_capture_mutex());
+        const uint64_t before = ctx_.launches;
+        NUMA_CUDA(cudaStreamBeginCapture(ctx_.stream, cudaStreamCaptureModeThreadLocal));
+        cudaGraph_t graph = nullptr;
+        try {
+            if (precision_ == NUMA_GPU_FP64) cycle<double>(1);
+            else cycle<float>(1);
+        } catch (...) {
+            cudaStreamEndCapture(ctx_.stream, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            throw;
+        }
+        NUMA_CUDA(cudaStreamEndCapture(ctx_.stream, &graph));
+        const cudaError_t e = cudaGraphInstantiate(&coarse_exec_, graph, 0);
+        cudaGraphDestroy(graph);
+        NUMA_CUDA(e);
+        coarse_kernels_ = ctx_.launches - before;
+        ctx_.launches = before;
+    }
+    NUMA_CUDA(cudaGraphLaunch(coarse_exec_, ctx_.stream));
+    ctx_.count_launch(static_cast<unsigned>(coarse_kernels_));
+}
+
+void BrussMG2D::apply(const double* r, double* z) {
+    const size_t N = size();
+    // the finest pass reads r while the last one writes z: an aliased call goes through a copy
+    const double* rin = r;
+    if (r == z) {
+        alias_.resize(N);
+        dev_copy(ctx_, r, alias_.p, N);
+        rin = alias_.p;
+    }
+    r0_ = rin;
+    z0_ = z;
+    if (precision_ == NUMA_GPU_FP64) cycle<double>(0);
+    else cycle<float>(0);
+    ctx_.check_launch("BrussMG2D apply");
+}
+
+namespace {
+// Provider over BrussMG2D: make(x) sets the blocks at the Newton iterate.
+class BrussMGProvider final : public Provider {
+public:
+    BrussMGProvider(Context& ctx, size_t n, const numa_brusselator2d_params& p, int precision, int pre, int post)
+        : mg_(ctx, n, p, precision, pre, post) {}
+    void make(const double* x, const double*) override { mg_.set_state(x); }
+    void apply(const double* r, double* z) override { mg_.apply(r, z); }
+    int kind() const override { return NUMA_GPU_PRECOND_BRUSS_MG; }
+
+private:
+    BrussMG2D mg_;
+};
+}  // namespace
+
+std::unique_ptr<Provider> make_bruss_mg_provider(Context& ctx, size_t n, const numa_brusselator2d_params& p,
+                                                 int precision, int pre, int post) {
+    return std::make_unique<BrussMGProvider>(ctx, n, p, precision, pre, post);
+}
+
+}  // namespace numa::gpu

@@ -44,6 +44,18 @@ struct numa_gpu_hmg2d {
     numa_gpu_ctx* ctx;
     std::unique_ptr<HelmholtzMG2D> impl;
 };
+struct numa_gpu_brusselator1d {
+    numa_gpu_ctx* ctx;
+    std::unique_ptr<Brusselator1D> impl;
+};
+struct numa_gpu_brusselator2d {
+    numa_gpu_ctx* ctx;
+    std::unique_ptr<Brusselator2D> impl;
+};
+struct numa_gpu_bmg2d {
+    numa_gpu_ctx* ctx;
+    std::unique_ptr<BrussMG2D> impl;
+};
 
 namespace {
 
@@ -65,6 +77,13 @@ struct CtxExtras {
     size_t bh_n = 0;
     double bh_nu = 0.0, bh_dt = 0.0, bh_amp = 0.0;
     int bh_kind = -1;
+    // numa_gpu_brusselator2d_advance_host likewise
+    std::unique_ptr<Brusselator2D> b2_op;
+    std::unique_ptr<Provider> b2_pc;
+    DeviceArray<double> b2_x;
+    size_t b2_n = 0;
+    numa_brusselator2d_params b2_p{};
+    int b2_kind = -1, b2_prec = -1;
 };
 
 struct CtxHandle : numa_gpu_ctx {
@@ -1075,6 +1094,316 @@ int numa_gpu_solve_burgers2d_host(numa_gpu_ctx* ctx, size_t n, double nu, double
     });
     result->status = rc;
     return rc;
+}
+
+// ------------------------------------------------------------------------------ Brusselator1D
+int numa_gpu_brusselator1d_create(numa_gpu_ctx* ctx, size_t n, double dt, numa_gpu_brusselator1d** out) {
+    if (!ctx || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        auto h = std::make_unique<numa_gpu_brusselator1d>();
+        h->ctx = ctx;
+        h->impl = std::make_unique<Brusselator1D>(*ctx->impl, n, dt);
+        *out = h.release();
+    });
+}
+
+int numa_gpu_brusselator1d_destroy(numa_gpu_brusselator1d* op) {
+    if (op) {
+        cudaStreamSynchronize(op->ctx->impl->stream);
+        delete op;
+    }
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_brusselator1d_size(const numa_gpu_brusselator1d* op, size_t* N) {
+    if (!op || !N) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *N = op->impl->size();
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_brusselator1d_previous(numa_gpu_brusselator1d* op, numa_gpu_vec* out) {
+    if (!op) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(op->ctx, [&] {
+        same_ctx(op->ctx, out);
+        sized(out, op->impl->size());
+        dev_copy(*op->ctx->impl, op->impl->previous(), out->d, op->impl->size());
+    });
+}
+
+extern "C++" {
+template <class Op>
+static int op_eval(numa_gpu_ctx* ctx, Op& op, const numa_gpu_vec* w, numa_gpu_vec* out) {
+    return guard(ctx, [&] {
+        same_ctx(ctx, w);
+        same_ctx(ctx, out);
+        sized(w, op.size());
+        sized(out, op.size());
+        need(w->d != out->d, NUMA_GPU_ERR_INVALID_ARGUMENT, "eval input and output must differ");
+        op.eval(w->d, out->d, nullptr, nullptr);
+    });
+}
+
+template <class Op>
+static int op_deriv(numa_gpu_ctx* ctx, Op& op, bool second, const numa_gpu_vec* w, const numa_gpu_vec* d,
+                    numa_gpu_vec* out, int mode) {
+    return guard(ctx, [&] {
+        for (const numa_gpu_vec* q : {w, d, (const numa_gpu_vec*)out}) {
+            same_ctx(ctx, q);
+            sized(q, op.size());
+        }
+        need(out->d != w->d && out->d != d->d, NUMA_GPU_ERR_INVALID_ARGUMENT, "output must not alias an input");
+        op_derivative(op, second, w->d, d->d, out->d, mode);
+    });
+}
+}  // extern "C++"
+
+int numa_gpu_brusselator1d_eval(numa_gpu_brusselator1d* op, const numa_gpu_vec* w, numa_gpu_vec* out) {
+    if (!op) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return op_eval(op->ctx, *op->impl, w, out);
+}
+
+int numa_gpu_brusselator1d_jvp(numa_gpu_brusselator1d* op, const numa_gpu_vec* w, const numa_gpu_vec* d,
+                               numa_gpu_vec* out, int mode) {
+    if (!op) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return op_deriv(op->ctx, *op->impl, false, w, d, out, mode);
+}
+
+int numa_gpu_brusselator1d_d2(numa_gpu_brusselator1d* op, const numa_gpu_vec* w, const numa_gpu_vec* d,
+                              numa_gpu_vec* out, int mode) {
+    if (!op) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return op_deriv(op->ctx, *op->impl, true, w, d, out, mode);
+}
+
+int numa_gpu_brusselator1d_solve(numa_gpu_brusselator1d* op, int method, numa_gpu_vec* x, const numa_krylov_params* p,
+                                 numa_gpu_provider* provider, numa_krylov_result* result) {
+    if (!op || !x || !result) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    std::memset(result, 0, sizeof(*result));
+    const int rc = guard(op->ctx, [&] {
+        check_driver_args(op->ctx, x, op->impl->size(), provider);
+        dispatch_driver(method, *op->impl, x->d, p, provider ? provider->impl.get() : nullptr, *result);
+    });
+    result->status = rc;
+    return rc;
+}
+
+int numa_gpu_provider_create_brusselator_jacobi(numa_gpu_brusselator1d* op, numa_gpu_provider** out) {
+    if (!op || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(op->ctx, [&] {
+        auto h = std::make_unique<numa_gpu_provider>();
+        h->ctx = op->ctx;
+        h->impl = make_bruss_jacobi_provider(*op->impl);
+        h->N = op->impl->size();
+        *out = h.release();
+    });
+}
+
+int numa_gpu_solve_brusselator1d_host(numa_gpu_ctx* ctx, size_t n, double dt, int method, int precond_kind,
+                                      const numa_krylov_params* p, const double* x0, double* x_out,
+                                      numa_krylov_result* result) {
+    if (!ctx || !x_out || !result) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    std::memset(result, 0, sizeof(*result));
+    const int rc = guard(ctx, [&] {
+        need(precond_kind == NUMA_GPU_PRECOND_NONE || precond_kind == NUMA_GPU_PRECOND_BRUSS_JACOBI,
+             NUMA_GPU_ERR_INVALID_ARGUMENT, "Brusselator1DStep takes the preconditioner NONE or BRUSS_JACOBI");
+        Context& c = *ctx->impl;
+        Brusselator1D op(c, n, dt);
+        std::unique_ptr<Provider> pc = precond_kind == NUMA_GPU_PRECOND_BRUSS_JACOBI
+                                           ? make_bruss_jacobi_provider(op)
+                                           : make_identity_provider(c, op.size());
+        const size_t N = op.size();
+        DeviceArray<double> x(N);
+        if (x0) NUMA_CUDA(cudaMemcpyAsync(x.p, x0, N * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        else dev_copy(c, op.previous(), x.p, N);
+        dispatch_driver(method, op, x.p, p, pc.get(), *result);
+        NUMA_CUDA(cudaMemcpyAsync(x_out, x.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        c.sync();
+    });
+    result->status = rc;
+    return rc;
+}
+
+// ------------------------------------------------------------------------------ Brusselator2D
+int numa_gpu_brusselator2d_create(numa_gpu_ctx* ctx, size_t n, const numa_brusselator2d_params* prm,
+                                  numa_gpu_brusselator2d** out) {
+    if (!ctx || !out || !prm) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        auto h = std::make_unique<numa_gpu_brusselator2d>();
+        h->ctx = ctx;
+        h->impl = std::make_unique<Brusselator2D>(*ctx->impl, n, *prm);
+        *out = h.release();
+    });
+}
+
+int numa_gpu_brusselator2d_destroy(numa_gpu_brusselator2d* op) {
+    if (op) {
+        cudaStreamSynchronize(op->ctx->impl->stream);
+        delete op;
+    }
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_brusselator2d_size(const numa_gpu_brusselator2d* op, size_t* N) {
+    if (!op || !N) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *N = op->impl->size();
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_brusselator2d_set_previous(numa_gpu_brusselator2d* op, const numa_gpu_vec* w) {
+    if (!op) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(op->ctx, [&] {
+        same_ctx(op->ctx, w);
+        sized(w, op->impl->size());
+        op->impl->set_previous(w->d);
+    });
+}
+
+int numa_gpu_brusselator2d_eval(numa_gpu_brusselator2d* op, const numa_gpu_vec* w, numa_gpu_vec* out) {
+    if (!op) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return op_eval(op->ctx, *op->impl, w, out);
+}
+
+int numa_gpu_brusselator2d_jvp(numa_gpu_brusselator2d* op, const numa_gpu_vec* w, const numa_gpu_vec* d,
+                               numa_gpu_vec* out, int mode) {
+    if (!op) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return op_deriv(op->ctx, *op->impl, false, w, d, out, mode);
+}
+
+int numa_gpu_brusselator2d_d2(numa_gpu_brusselator2d* op, const numa_gpu_vec* w, const numa_gpu_vec* d,
+                              numa_gpu_vec* out, int mode) {
+    if (!op) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return op_deriv(op->ctx, *op->impl, true, w, d, out, mode);
+}
+
+int numa_gpu_brusselator2d_solve(numa_gpu_brusselator2d* op, int method, numa_gpu_vec* x, const numa_krylov_params* p,
+                                 numa_gpu_provider* provider, numa_krylov_result* result) {
+    if (!op || !x || !result) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    std::memset(result, 0, sizeof(*result));
+    const int rc = guard(op->ctx, [&] {
+        check_driver_args(op->ctx, x, op->impl->size(), provider);
+        dispatch_driver(method, *op->impl, x->d, p, provider ? provider->impl.get() : nullptr, *result);
+    });
+    result->status = rc;
+    return rc;
+}
+
+// `steps` implicit-Euler steps: each step takes the current state as the previous time level and as
+// the Newton start, and leaves its solution in x.
+static void advance(Brusselator2D& op, int method, size_t steps, double* x, const numa_krylov_params* p,
+                    Provider* pc, numa_krylov_result* results) {
+    for (size_t k = 0; k < steps; ++k) {
+        op.set_previous(x);
+        numa_krylov_result r;
+        std::memset(&r, 0, sizeof(r));
+        dispatch_driver(method, op, x, p, pc, r);
+        if (results) results[k] = r;
+    }
+}
+
+int numa_gpu_brusselator2d_advance(numa_gpu_brusselator2d* op, int method, size_t steps, numa_gpu_vec* x,
+                                   const numa_krylov_params* p, numa_gpu_provider* provider,
+                                   numa_krylov_result* results) {
+    if (!op || !x) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    if (results) std::memset(results, 0, steps * sizeof(numa_krylov_result));
+    return guard(op->ctx, [&] {
+        check_driver_args(op->ctx, x, op->impl->size(), provider);
+        advance(*op->impl, method, steps, x->d, p, provider ? provider->impl.get() : nullptr, results);
+    });
+}
+
+int numa_gpu_provider_create_brusselator_mg(numa_gpu_brusselator2d* op, int precision, int pre, int post,
+                                            numa_gpu_provider** out) {
+    if (!op || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(op->ctx, [&] {
+        auto h = std::make_unique<numa_gpu_provider>();
+        h->ctx = op->ctx;
+        h->impl = make_bruss_mg_provider(*op->ctx->impl, op->impl->grid(), op->impl->params(), precision, pre, post);
+        h->N = op->impl->size();
+        *out = h.release();
+    });
+}
+
+int numa_gpu_brusselator2d_advance_host(numa_gpu_ctx* ctx, size_t n, const numa_brusselator2d_params* prm,
+                                        size_t steps, int method, int precond_kind, int mg_precision,
+                                        const numa_krylov_params* p, const double* x0, double* x_out,
+                                        numa_krylov_result* results) {
+    if (!ctx || !prm || !x0 || !x_out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    if (results) std::memset(results, 0, steps * sizeof(numa_krylov_result));
+    return guard(ctx, [&] {
+        need(precond_kind == NUMA_GPU_PRECOND_NONE || precond_kind == NUMA_GPU_PRECOND_BRUSS_MG,
+             NUMA_GPU_ERR_INVALID_ARGUMENT, "Brusselator2D takes the preconditioner NONE or BRUSS_MG");
+        Context& c = *ctx->impl;
+        CtxExtras& e = extras(ctx);
+        if (!e.b2_op || e.b2_n != n || std::memcmp(&e.b2_p, prm, sizeof(*prm)) != 0) {
+            e.b2_pc.reset();
+            e.b2_op = std::make_unique<Brusselator2D>(c, n, *prm);
+            e.b2_n = n;
+            e.b2_p = *prm;
+            e.b2_kind = -1;
+        }
+        const size_t N = e.b2_op->size();
+        if (e.b2_kind != precond_kind || e.b2_prec != mg_precision || !e.b2_pc) {
+            if (precond_kind == NUMA_GPU_PRECOND_BRUSS_MG) e.b2_pc = make_bruss_mg_provider(c, n, *prm, mg_precision, 2, 2);
+            else e.b2_pc = make_identity_provider(c, N);
+            e.b2_kind = precond_kind;
+            e.b2_prec = mg_precision;
+        }
+        e.b2_x.resize(N);
+        NUMA_CUDA(cudaMemcpyAsync(e.b2_x.p, x0, N * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        advance(*e.b2_op, method, steps, e.b2_x.p, p, e.b2_pc.get(), results);
+        NUMA_CUDA(cudaMemcpyAsync(x_out, e.b2_x.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        c.sync();
+    });
+}
+
+// ------------------------------------------------------------------------------ BrussMG2D
+int numa_gpu_bmg2d_create(numa_gpu_ctx* ctx, size_t n, const numa_brusselator2d_params* prm, int precision, int pre,
+                          int post, numa_gpu_bmg2d** out) {
+    if (!ctx || !out || !prm) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        auto h = std::make_unique<numa_gpu_bmg2d>();
+        h->ctx = ctx;
+        h->impl = std::make_unique<BrussMG2D>(*ctx->impl, n, *prm, precision, pre, post);
+        *out = h.release();
+    });
+}
+
+int numa_gpu_bmg2d_destroy(numa_gpu_bmg2d* mg) {
+    if (mg) {
+        cudaStreamSynchronize(mg->ctx->impl->stream);
+        delete mg;
+    }
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_bmg2d_levels(const numa_gpu_bmg2d* mg, size_t* levels) {
+    if (!mg || !levels) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *levels = mg->impl->levels();
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_bmg2d_set_state(numa_gpu_bmg2d* mg, const numa_gpu_vec* w) {
+    if (!mg) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(mg->ctx, [&] {
+        same_ctx(mg->ctx, w);
+        sized(w, mg->impl->size());
+        mg->impl->set_state(w->d);
+    });
+}
+
+int numa_gpu_bmg2d_apply(numa_gpu_bmg2d* mg, const numa_gpu_vec* r, numa_gpu_vec* z) {
+    if (!mg) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(mg->ctx, [&] {
+        same_ctx(mg->ctx, r);
+        same_ctx(mg->ctx, z);
+        sized(r, mg->impl->size());
+        sized(z, mg->impl->size());
+        mg->impl->apply(r->d, z->d);
+    });
 }
 
 // ------------------------------------------------------------------------------ batched solves

@@ -162,6 +162,92 @@ private:
     const double* bound_x_ = nullptr;
 };
 
+// ------------------------------------------------------------------------------ Brusselator
+// Brusselator1DStep (problems/brusselator1d.hpp:22-192): one implicit-Euler step of the 1D
+// Brusselator, A = 1, B = 3, alpha = 1/50, Dirichlet u = 1, v = 3; w = (u, v), 2 n unknowns.
+class Brusselator1D : public NonlinearOp {
+public:
+    static constexpr double kA = 1.0, kB = 3.0, kAlpha = 1.0 / 50.0;
+    Brusselator1D(Context& ctx, size_t n, double dt);
+    size_t size() const override { return 2 * n_; }
+    size_t grid() const { return n_; }
+    double dt() const { return dt_; }
+    // the previous time level u = 1 + sin(2 pi x), v = 3 (the natural Newton start)
+    const double* previous() const { return prev_.p; }
+    size_t cache_size() const override { return 0; }
+    void eval(const double* x, double* out, double* cache, double* norm_out) override;
+    void bind(const double* x, const double*, int) override { bound_x_ = x; }
+    void jvp_bound(const double* v, double* out) override { jvp_at(bound_x_, v, out); }
+    void jvp_at(const double* x, const double* v, double* out) override;
+    void d2(const double* x, const double* cache, const double* v, double* out) override;
+    // the 2x2 point blocks at x as planes a11 | a12 | a21 | a22 (local_jacobi_blocks, :120-141)
+    void blocks(const double* x, double* a);
+
+private:
+    size_t n_;
+    double dt_, h_ = 0.0, h2inv_ = 0.0;
+    DeviceArray<double> prev_;
+    const double* bound_x_ = nullptr;
+};
+
+// z = block^-1 r per point (BrusselatorJacobi::Bound, brusselator1d.hpp:198-214).
+void brusselator_block_apply(Context& ctx, const double* a, const double* r, double* z, size_t n);
+
+// Implicit-Euler step of the 2-species Brusselator on an n x n periodic grid (h = 1/n):
+// F(w) = (w - w_prev)/dt - diag(D_u, D_v) Lap_h w - (A + u^2 v - (B+1) u, B u - u^2 v).
+class Brusselator2D : public NonlinearOp {
+public:
+    Brusselator2D(Context& ctx, size_t n, const numa_brusselator2d_params& p);
+    size_t size() const override { return 2 * n_ * n_; }
+    size_t grid() const { return n_; }
+    const numa_brusselator2d_params& params() const { return P_; }
+    const double* previous() const { return prev_.p; }
+    void set_previous(const double* w);
+    size_t cache_size() const override { return 0; }
+    void eval(const double* x, double* out, double* cache, double* norm_out) override;
+    void bind(const double* x, const double*, int) override { bound_x_ = x; }
+    void jvp_bound(const double* v, double* out) override { jvp_at(bound_x_, v, out); }
+    void jvp_at(const double* x, const double* v, double* out) override;
+    void d2(const double* x, const double* cache, const double* v, double* out) override;
+
+private:
+    size_t n_;
+    numa_brusselator2d_params P_;
+    DeviceArray<double> prev_;
+    const double* bound_x_ = nullptr;
+};
+
+// Periodic geometric multigrid V(pre, post) for the coupled 2x2-block Jacobian of Brusselator2D,
+// K(w) - diag(D_u, D_v) Lap_h: levels halve n while the coarse n is even and >= 4, red-black
+// point-block Gauss-Seidel, full weighting of residuals and blocks, bilinear periodic
+// prolongation, 30 sweeps on the coarsest level; FP64 or FP32 level arrays.
+class BrussMG2D {
+public:
+    BrussMG2D(Context& ctx, size_t n, const numa_brusselator2d_params& p, int precision, int pre, int post);
+    ~BrussMG2D();
+    size_t levels() const { return levels_.size(); }
+    size_t size() const { return 2 * n0_ * n0_; }
+    // blocks K at the state w (FP64 planes), restricted to every level
+    void set_state(const double* w);
+    // z = V-cycle(r), FP64 planes in and out
+    void apply(const double* r, double* z);
+    struct Level;
+
+private:
+    template <class T> void cycle(size_t l);
+    void coarse_cycle();
+    Context& ctx_;
+    size_t n0_;
+    numa_brusselator2d_params P_;
+    int precision_, pre_, post_;
+    std::vector<std::unique_ptr<Level>> levels_;
+    DeviceArray<double> alias_;
+    const double* r0_ = nullptr;
+    double* z0_ = nullptr;
+    cudaGraphExec_t coarse_exec_ = nullptr;
+    uint64_t coarse_kernels_ = 0;
+};
+
 // ------------------------------------------------------------------------------ PoissonMG
 class PoissonMG {
 public:
@@ -253,6 +339,11 @@ std::unique_ptr<Provider> make_jacobi_provider(Bratu3D& op);
 // BurgersMGProvider (problems/burgers2d.hpp:220-246): the HelmholtzMG2D V-cycle of
 // (1/dt) I - nu Lap_h applied to each component.
 std::unique_ptr<Provider> make_burgers_mg_provider(Context& ctx, size_t n, double nu, double dt, int pre, int post);
+// BrusselatorJacobi (problems/brusselator1d.hpp:194-222).
+std::unique_ptr<Provider> make_bruss_jacobi_provider(Brusselator1D& op);
+// BrussMG2D bound at each Newton iterate.
+std::unique_ptr<Provider> make_bruss_mg_provider(Context& ctx, size_t n, const numa_brusselator2d_params& p,
+                                                 int precision, int pre, int post);
 
 // ------------------------------------------------------------------------------ GMRES
 struct GmresResult {

@@ -28,7 +28,7 @@ FP64, FP32 = 0, 1
 ANALYTIC, FD, ANALYTIC_FP32 = 0, 1, 2
 MGS, CGS2, CGS1 = 0, 1, 2
 METHODS = {"nk": 0, "cheb": 1, "rec": 2, "tf2018": 3}
-PRECONDS = {"none": 0, "mg": 1, "jacobi": 2, "burgers_mg": 3}
+PRECONDS = {"none": 0, "mg": 1, "jacobi": 2, "burgers_mg": 3, "bruss_jacobi": 5, "bruss_mg": 6}
 
 
 class KrylovParams(C.Structure):
@@ -58,6 +58,17 @@ class LearnedTrainReport(C.Structure):
     """numa_learned_train_report"""
     _fields_ = [("samples", C.c_size_t), ("gen_seconds", C.c_double), ("train_seconds", C.c_double),
                 ("loss_first", C.c_float), ("loss_last", C.c_float), ("target_ms", C.c_float)]
+
+
+class BrusselatorParams(C.Structure):
+    """numa_brusselator2d_params of include/numa_gpu.h."""
+    _fields_ = [("A", C.c_double), ("B", C.c_double), ("Du", C.c_double), ("Dv", C.c_double), ("dt", C.c_double)]
+
+
+def brusselator_params(A: float = 1.0, B: float = 3.4, Du: float = 0.002, Dv: float = 0.002,
+                       dt: float = 0.01) -> BrusselatorParams:
+    """The 2-species 2048^2 configuration's parameters by default."""
+    return BrusselatorParams(A, B, Du, Dv, dt)
 
 
 class BatchInstance(C.Structure):
@@ -149,6 +160,34 @@ SIGNATURES = {
     "numa_gpu_hmg2d_destroy": ([_P], _I),
     "numa_gpu_hmg2d_levels": ([_P, C.POINTER(_SZ)], _I),
     "numa_gpu_hmg2d_apply": ([_P, _P, _P], _I),
+    "numa_gpu_brusselator1d_create": ([_P, _SZ, _D, _PP], _I),
+    "numa_gpu_brusselator1d_destroy": ([_P], _I),
+    "numa_gpu_brusselator1d_size": ([_P, C.POINTER(_SZ)], _I),
+    "numa_gpu_brusselator1d_previous": ([_P, _P], _I),
+    "numa_gpu_brusselator1d_eval": ([_P, _P, _P], _I),
+    "numa_gpu_brusselator1d_jvp": ([_P, _P, _P, _P, _I], _I),
+    "numa_gpu_brusselator1d_d2": ([_P, _P, _P, _P, _I], _I),
+    "numa_gpu_brusselator1d_solve": ([_P, _I, _P, C.POINTER(KrylovParams), _P, C.POINTER(KrylovResult)], _I),
+    "numa_gpu_provider_create_brusselator_jacobi": ([_P, _PP], _I),
+    "numa_gpu_solve_brusselator1d_host": ([_P, _SZ, _D, _I, _I, C.POINTER(KrylovParams), _F64P, _F64P,
+                                           C.POINTER(KrylovResult)], _I),
+    "numa_gpu_brusselator2d_create": ([_P, _SZ, C.POINTER(BrusselatorParams), _PP], _I),
+    "numa_gpu_brusselator2d_destroy": ([_P], _I),
+    "numa_gpu_brusselator2d_size": ([_P, C.POINTER(_SZ)], _I),
+    "numa_gpu_brusselator2d_set_previous": ([_P, _P], _I),
+    "numa_gpu_brusselator2d_eval": ([_P, _P, _P], _I),
+    "numa_gpu_brusselator2d_jvp": ([_P, _P, _P, _P, _I], _I),
+    "numa_gpu_brusselator2d_d2": ([_P, _P, _P, _P, _I], _I),
+    "numa_gpu_brusselator2d_solve": ([_P, _I, _P, C.POINTER(KrylovParams), _P, C.POINTER(KrylovResult)], _I),
+    "numa_gpu_brusselator2d_advance": ([_P, _I, _SZ, _P, C.POINTER(KrylovParams), _P, C.POINTER(KrylovResult)], _I),
+    "numa_gpu_provider_create_brusselator_mg": ([_P, _I, _I, _I, _PP], _I),
+    "numa_gpu_brusselator2d_advance_host": ([_P, _SZ, C.POINTER(BrusselatorParams), _SZ, _I, _I, _I,
+                                             C.POINTER(KrylovParams), _F64P, _F64P, C.POINTER(KrylovResult)], _I),
+    "numa_gpu_bmg2d_create": ([_P, _SZ, C.POINTER(BrusselatorParams), _I, _I, _I, _PP], _I),
+    "numa_gpu_bmg2d_destroy": ([_P], _I),
+    "numa_gpu_bmg2d_levels": ([_P, C.POINTER(_SZ)], _I),
+    "numa_gpu_bmg2d_set_state": ([_P, _P], _I),
+    "numa_gpu_bmg2d_apply": ([_P, _P, _P], _I),
     "numa_gpu_provider_create_burgers_mg": ([_P, _SZ, _D, _D, _PP], _I),
     "numa_gpu_solve_burgers2d_host": ([_P, _SZ, _D, _D, _D, _I, _I, C.POINTER(KrylovParams), _F64P, _F64P,
                                        C.POINTER(KrylovResult)], _I),
@@ -465,6 +504,125 @@ class Burgers2D:
         self.ctx.check(self.lib.numa_gpu_burgers2d_d2(self.h, w.h, d.h, out.h, mode), "burgers2d_d2")
 
 
+class _Handle:
+    """A C handle with a destroy function, closed before its context."""
+    _destroy = ""
+
+    def close(self):
+        if getattr(self, "h", None):
+            getattr(self.lib, self._destroy)(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Brusselator1D(_Handle):
+    """Brusselator1DStep(n, dt) (problems/brusselator1d.hpp:22-45) on the GPU; N = 2 n."""
+    _destroy = "numa_gpu_brusselator1d_destroy"
+
+    def __init__(self, ctx: Context, n: int, dt: float):
+        self.ctx, self.lib, self.n, self.dt = ctx, ctx.lib, int(n), float(dt)
+        h = C.c_void_p()
+        ctx.check(self.lib.numa_gpu_brusselator1d_create(ctx.h, self.n, self.dt, C.byref(h)), "brusselator1d_create")
+        self.h = h
+        self.ctx._adopt(self)
+
+    def size(self) -> int:
+        return 2 * self.n
+
+    def previous(self, out: Vec):
+        self.ctx.check(self.lib.numa_gpu_brusselator1d_previous(self.h, out.h), "brusselator1d_previous")
+
+    def eval(self, w: Vec, out: Vec):
+        self.ctx.check(self.lib.numa_gpu_brusselator1d_eval(self.h, w.h, out.h), "brusselator1d_eval")
+
+    def jvp(self, w: Vec, d: Vec, out: Vec, mode: int = ANALYTIC):
+        self.ctx.check(self.lib.numa_gpu_brusselator1d_jvp(self.h, w.h, d.h, out.h, mode), "brusselator1d_jvp")
+
+    def d2(self, w: Vec, d: Vec, out: Vec, mode: int = ANALYTIC):
+        self.ctx.check(self.lib.numa_gpu_brusselator1d_d2(self.h, w.h, d.h, out.h, mode), "brusselator1d_d2")
+
+
+class Brusselator2D(_Handle):
+    """Implicit-Euler step of the periodic 2-species Brusselator on n x n; N = 2 n^2."""
+    _destroy = "numa_gpu_brusselator2d_destroy"
+
+    def __init__(self, ctx: Context, n: int, params: BrusselatorParams | None = None):
+        self.ctx, self.lib, self.n = ctx, ctx.lib, int(n)
+        self.params = params if params is not None else brusselator_params()
+        h = C.c_void_p()
+        ctx.check(self.lib.numa_gpu_brusselator2d_create(ctx.h, self.n, C.byref(self.params), C.byref(h)),
+                  "brusselator2d_create")
+        self.h = h
+        self.ctx._adopt(self)
+
+    def size(self) -> int:
+        return 2 * self.n * self.n
+
+    def set_previous(self, w: Vec):
+        self.ctx.check(self.lib.numa_gpu_brusselator2d_set_previous(self.h, w.h), "brusselator2d_set_previous")
+
+    def eval(self, w: Vec, out: Vec):
+        self.ctx.check(self.lib.numa_gpu_brusselator2d_eval(self.h, w.h, out.h), "brusselator2d_eval")
+
+    def jvp(self, w: Vec, d: Vec, out: Vec, mode: int = ANALYTIC):
+        self.ctx.check(self.lib.numa_gpu_brusselator2d_jvp(self.h, w.h, d.h, out.h, mode), "brusselator2d_jvp")
+
+    def d2(self, w: Vec, d: Vec, out: Vec, mode: int = ANALYTIC):
+        self.ctx.check(self.lib.numa_gpu_brusselator2d_d2(self.h, w.h, d.h, out.h, mode), "brusselator2d_d2")
+
+    def advance(self, x: Vec, steps: int, method: str = "nk", params: KrylovParams | None = None,
+                provider: "Provider | None" = None) -> list[dict]:
+        """`steps` implicit-Euler steps from the state x (overwritten); one result per step."""
+        p = params if params is not None else default_params()
+        if method == "rec":
+            p.recycle = 1
+        res = (KrylovResult * steps)()
+        rc = self.lib.numa_gpu_brusselator2d_advance(self.h, METHODS[method], steps, x.h, C.byref(p),
+                                                     provider.h if provider else None, res)
+        self.ctx.check(rc, "brusselator2d_advance")
+        return [to_dict(r) for r in res]
+
+
+class BrussMG2D(_Handle):
+    """The coupled-block periodic multigrid of Brusselator2D: set_state(w), then apply(r, z)."""
+    _destroy = "numa_gpu_bmg2d_destroy"
+
+    def __init__(self, ctx: Context, n: int, params: BrusselatorParams | None = None, precision: int = FP64,
+                 pre: int = 2, post: int = 2):
+        self.ctx, self.lib, self.n = ctx, ctx.lib, int(n)
+        self.params = params if params is not None else brusselator_params()
+        h = C.c_void_p()
+        ctx.check(self.lib.numa_gpu_bmg2d_create(ctx.h, self.n, C.byref(self.params), precision, pre, post,
+                                                 C.byref(h)), "bmg2d_create")
+        self.h = h
+        self.ctx._adopt(self)
+
+    def levels(self) -> int:
+        v = C.c_size_t()
+        self.ctx.check(self.lib.numa_gpu_bmg2d_levels(self.h, C.byref(v)), "bmg2d_levels")
+        return v.value
+
+    def set_state(self, w: Vec):
+        self.ctx.check(self.lib.numa_gpu_bmg2d_set_state(self.h, w.h), "bmg2d_set_state")
+
+    def apply(self, r: Vec, z: Vec):
+        self.ctx.check(self.lib.numa_gpu_bmg2d_apply(self.h, r.h, z.h), "bmg2d_apply")
+
+
+def brusselator2d_initial(n: int, A: float = 1.0, B: float = 3.4, seed: int = 20261203) -> np.ndarray:
+    """u = A + 0.01 N(0,1), v = B/A + 0.01 N(0,1) per point from numpy's PCG64 stream of `seed`
+    (2 n^2 normals: the u plane first)."""
+    z = np.random.default_rng(seed).standard_normal(2 * n * n)
+    z[: n * n] = A + 0.01 * z[: n * n]
+    z[n * n:] = B / A + 0.01 * z[n * n:]
+    return z
+
+
 class HelmholtzMG2D:
     """HelmholtzMG2D(n, alpha, nu, pre, post) (linalg/helmholtz_mg2d.hpp:13-32): one V-cycle per call."""
 
@@ -633,6 +791,25 @@ class Provider:
         return cls(ctx, h, "burgers_mg")
 
     @classmethod
+    def brusselator_jacobi(cls, op: "Brusselator1D") -> "Provider":
+        """BrusselatorJacobi{op} (problems/brusselator1d.hpp:194-222)."""
+        h = C.c_void_p()
+        op.ctx.check(op.lib.numa_gpu_provider_create_brusselator_jacobi(op.h, C.byref(h)), "provider_bruss_jacobi")
+        p = cls(op.ctx, h, "bruss_jacobi")
+        p._op = op
+        return p
+
+    @classmethod
+    def brusselator_mg(cls, op: "Brusselator2D", precision: int = FP64, pre: int = 2, post: int = 2) -> "Provider":
+        """The coupled-block periodic multigrid, bound at each Newton iterate."""
+        h = C.c_void_p()
+        op.ctx.check(op.lib.numa_gpu_provider_create_brusselator_mg(op.h, precision, pre, post, C.byref(h)),
+                     "provider_bruss_mg")
+        p = cls(op.ctx, h, "bruss_mg")
+        p._op = op
+        return p
+
+    @classmethod
     def learned(cls, ctx: Context, n: int, net: "LearnedNet", stall: float = 0.9) -> "Provider":
         """FP32 V-cycle + learned coarse correction (for FGMRES)."""
         h = C.c_void_p()
@@ -650,6 +827,10 @@ class Provider:
     def create(cls, ctx: Context, kind: str, op, precision: int = FP64) -> "Provider | None":
         if isinstance(op, Burgers2D):
             return cls.burgers_mg(ctx, op.n, op.nu, op.dt) if kind == "mg" else cls.identity(ctx)
+        if isinstance(op, Brusselator1D):
+            return cls.brusselator_jacobi(op) if kind == "jacobi" else cls.identity(ctx)
+        if isinstance(op, Brusselator2D):
+            return cls.brusselator_mg(op, precision) if kind == "mg" else cls.identity(ctx)
         if kind == "mg":
             return cls.poisson_mg(ctx, op.n, precision=precision)
         if kind == "jacobi":
@@ -800,6 +981,10 @@ def _driver(name: str, op, x: Vec, params: KrylovParams | None, provider: Provid
     if isinstance(op, Burgers2D):
         rc = op.lib.numa_gpu_burgers2d_solve(op.h, _DRIVER_METHOD[name], x.h, C.byref(p),
                                              provider.h if provider else None, C.byref(res))
+    elif isinstance(op, (Brusselator1D, Brusselator2D)):
+        fn = "numa_gpu_brusselator1d_solve" if isinstance(op, Brusselator1D) else "numa_gpu_brusselator2d_solve"
+        rc = getattr(op.lib, fn)(op.h, _DRIVER_METHOD[name], x.h, C.byref(p), provider.h if provider else None,
+                                 C.byref(res))
     else:
         rc = getattr(op.lib, name)(op.h, x.h, C.byref(p), provider.h if provider else None, C.byref(res))
     op.ctx.check(rc, name)
@@ -862,6 +1047,42 @@ def solve_burgers2d_host(ctx: Context, n: int, nu: float, dt: float, amplitude: 
                                                x0.ctypes.data_as(_F64P), out.ctypes.data_as(_F64P), C.byref(res))
     ctx.check(rc, "solve_burgers2d_host")
     return out, to_dict(res)
+
+
+def solve_brusselator1d_host(ctx: Context, n: int, dt: float, x0: np.ndarray | None = None, method: str = "nk",
+                             precond: str = "jacobi", params: KrylovParams | None = None) -> tuple[np.ndarray, dict]:
+    """Host buffers (numa_gpu_solve_brusselator1d_host); x0 None: the previous state; precond "jacobi" or "none"."""
+    p = params if params is not None else default_params()
+    out = np.empty(2 * n)
+    res = KrylovResult()
+    kind = PRECONDS["bruss_jacobi"] if precond == "jacobi" else PRECONDS["none"]
+    keep = None if x0 is None else _f64(x0).ravel()
+    x0p = None if keep is None else keep.ctypes.data_as(_F64P)
+    rc = ctx.lib.numa_gpu_solve_brusselator1d_host(ctx.h, n, dt, METHODS[method], kind, C.byref(p), x0p,
+                                                   out.ctypes.data_as(_F64P), C.byref(res))
+    ctx.check(rc, "solve_brusselator1d_host")
+    return out, to_dict(res)
+
+
+def brusselator2d_advance_host(ctx: Context, n: int, x0: np.ndarray, steps: int, params: BrusselatorParams | None = None,
+                               method: str = "nk", precond: str = "mg", mg_precision: int = FP32,
+                               kparams: KrylovParams | None = None, out: np.ndarray | None = None
+                               ) -> tuple[np.ndarray, list[dict]]:
+    """Host buffers (numa_gpu_brusselator2d_advance_host): `steps` implicit-Euler steps from x0."""
+    prm = params if params is not None else brusselator_params()
+    p = kparams if kparams is not None else default_params()
+    if method == "rec":
+        p.recycle = 1
+    x0 = _f64(x0).ravel()
+    if out is None:
+        out = np.empty(2 * n * n)
+    res = (KrylovResult * steps)()
+    kind = PRECONDS["bruss_mg"] if precond == "mg" else PRECONDS["none"]
+    rc = ctx.lib.numa_gpu_brusselator2d_advance_host(ctx.h, n, C.byref(prm), steps, METHODS[method], kind,
+                                                     mg_precision, C.byref(p), x0.ctypes.data_as(_F64P),
+                                                     out.ctypes.data_as(_F64P), res)
+    ctx.check(rc, "brusselator2d_advance_host")
+    return out, [to_dict(r) for r in res]
 
 
 def solve_batch(instances, method: str = "nk", mg_precision: int = FP32, params: KrylovParams | None = None,

@@ -78,10 +78,19 @@ typedef enum numa_gpu_precond_kind {
     NUMA_GPU_PRECOND_POISSON_MG = 1, /* PoissonMGProvider (linalg/poisson_mg.hpp:303-320) */
     NUMA_GPU_PRECOND_JACOBI = 2,     /* BratuJacobi (problems/bratu3d.hpp:104-120) */
     NUMA_GPU_PRECOND_BURGERS_MG = 3, /* BurgersMGProvider (problems/burgers2d.hpp:220-246) */
-    NUMA_GPU_PRECOND_LEARNED = 4     /* extension: FP32 V-cycle + learned coarse correction (FGMRES) */
+    NUMA_GPU_PRECOND_LEARNED = 4,    /* extension: FP32 V-cycle + learned coarse correction (FGMRES) */
+    NUMA_GPU_PRECOND_BRUSS_JACOBI = 5, /* BrusselatorJacobi (problems/brusselator1d.hpp:194-222) */
+    NUMA_GPU_PRECOND_BRUSS_MG = 6      /* extension: periodic coupled-block multigrid of Brusselator2D */
 } numa_gpu_precond_kind;
 
 /* ---------------------------------------------------------------- parameter / result structs */
+
+/* Parameters of the periodic 2D Brusselator step (reaction terms of problems/brusselator1d.hpp:4-10). */
+typedef struct numa_brusselator2d_params {
+    double A, B;   /* reaction constants                               (1, 3.4) */
+    double Du, Dv; /* diffusion coefficients of u and v                (0.002, 0.002) */
+    double dt;     /* implicit-Euler step                              (0.01) */
+} numa_brusselator2d_params;
 
 /* KrylovParams (methods/krylov_newton.hpp:24-38), field for field, plus GPU extensions whose
  * zero value is the reference behaviour. */
@@ -150,6 +159,9 @@ typedef struct numa_gpu_provider numa_gpu_provider;
 typedef struct numa_gpu_krylov_space numa_gpu_krylov_space;
 typedef struct numa_gpu_burgers2d numa_gpu_burgers2d;
 typedef struct numa_gpu_hmg2d numa_gpu_hmg2d;
+typedef struct numa_gpu_brusselator1d numa_gpu_brusselator1d;
+typedef struct numa_gpu_brusselator2d numa_gpu_brusselator2d;
+typedef struct numa_gpu_bmg2d numa_gpu_bmg2d;
 typedef struct numa_gpu_learned numa_gpu_learned;
 
 /* ---------------------------------------------------------------- library / context */
@@ -376,6 +388,77 @@ int numa_gpu_provider_create_learned(numa_gpu_ctx* ctx, size_t n, numa_gpu_learn
                                      numa_gpu_provider** out);
 /* Network applications and fallbacks of a learned provider since its creation. */
 int numa_gpu_provider_learned_stats(numa_gpu_provider* p, size_t* applies, size_t* fallbacks);
+
+/* ---------------------------------------------------------------- Brusselator1DStep */
+/* Brusselator1DStep(n, dt) (problems/brusselator1d.hpp:22-45): one implicit-Euler step of the 1D
+ * Brusselator, A = 1, B = 3, alpha = 1/50, Dirichlet u = 1, v = 3; N = 2n, w = (u, v). */
+int numa_gpu_brusselator1d_create(numa_gpu_ctx* ctx, size_t n, double dt, numa_gpu_brusselator1d** out);
+int numa_gpu_brusselator1d_destroy(numa_gpu_brusselator1d* op);
+int numa_gpu_brusselator1d_size(const numa_gpu_brusselator1d* op, size_t* N);
+/* out = previous time level u = 1 + sin(2 pi x), v = 3     Brusselator1DStep::previous (:44) */
+int numa_gpu_brusselator1d_previous(numa_gpu_brusselator1d* op, numa_gpu_vec* out);
+/* out = F(w)                                               Brusselator1DStep::eval (:47-69) */
+int numa_gpu_brusselator1d_eval(numa_gpu_brusselator1d* op, const numa_gpu_vec* w, numa_gpu_vec* out);
+/* out = F'(w) d   mode ANALYTIC: jvp (:71-98); FD: jvp_fd */
+int numa_gpu_brusselator1d_jvp(numa_gpu_brusselator1d* op, const numa_gpu_vec* w, const numa_gpu_vec* d,
+                               numa_gpu_vec* out, int mode);
+/* out = F''(w)[d,d] mode ANALYTIC: d2 (:100-118); FD: d2_fd */
+int numa_gpu_brusselator1d_d2(numa_gpu_brusselator1d* op, const numa_gpu_vec* w, const numa_gpu_vec* d,
+                              numa_gpu_vec* out, int mode);
+/* The drivers on a Brusselator1DStep (CHEB_REC sets p->recycle). */
+int numa_gpu_brusselator1d_solve(numa_gpu_brusselator1d* op, int method, numa_gpu_vec* x,
+                                 const numa_krylov_params* p, numa_gpu_provider* provider,
+                                 numa_krylov_result* result);
+/* BrusselatorJacobi{op} (:194-222): 2x2 point blocks at the Newton iterate. */
+int numa_gpu_provider_create_brusselator_jacobi(numa_gpu_brusselator1d* op, numa_gpu_provider** out);
+/* Host buffers: x0[2n] (NULL = previous(), run_campaign's natural start) -> x_out[2n];
+ * precond_kind NONE or BRUSS_JACOBI. */
+int numa_gpu_solve_brusselator1d_host(numa_gpu_ctx* ctx, size_t n, double dt, int method, int precond_kind,
+                                      const numa_krylov_params* p, const double* x0, double* x_out,
+                                      numa_krylov_result* result);
+
+/* ---------------------------------------------------------------- Brusselator2D (periodic) */
+/* Implicit-Euler step of the 2-species Brusselator on an n x n periodic grid of the unit square
+ * (h = 1/n), the reaction terms of brusselator1d.hpp:4-10 with parameters A, B, D_u, D_v, dt:
+ * F(w) = (w - w_prev)/dt - diag(D_u, D_v) Lap_h w - (A + u^2 v - (B+1) u, B u - u^2 v);
+ * N = 2 n^2, w = (u, v) component-major, row-major planes.  The previous level starts at zero. */
+int numa_gpu_brusselator2d_create(numa_gpu_ctx* ctx, size_t n, const numa_brusselator2d_params* p,
+                                  numa_gpu_brusselator2d** out);
+int numa_gpu_brusselator2d_destroy(numa_gpu_brusselator2d* op);
+int numa_gpu_brusselator2d_size(const numa_gpu_brusselator2d* op, size_t* N);
+int numa_gpu_brusselator2d_set_previous(numa_gpu_brusselator2d* op, const numa_gpu_vec* w);
+int numa_gpu_brusselator2d_eval(numa_gpu_brusselator2d* op, const numa_gpu_vec* w, numa_gpu_vec* out);
+int numa_gpu_brusselator2d_jvp(numa_gpu_brusselator2d* op, const numa_gpu_vec* w, const numa_gpu_vec* d,
+                               numa_gpu_vec* out, int mode);
+int numa_gpu_brusselator2d_d2(numa_gpu_brusselator2d* op, const numa_gpu_vec* w, const numa_gpu_vec* d,
+                              numa_gpu_vec* out, int mode);
+/* One nonlinear solve from x with the current previous level. */
+int numa_gpu_brusselator2d_solve(numa_gpu_brusselator2d* op, int method, numa_gpu_vec* x,
+                                 const numa_krylov_params* p, numa_gpu_provider* provider,
+                                 numa_krylov_result* result);
+/* `steps` implicit-Euler steps: each takes the state x as the previous level and the Newton start
+ * and leaves its solution in x; results[steps] (may be NULL). */
+int numa_gpu_brusselator2d_advance(numa_gpu_brusselator2d* op, int method, size_t steps, numa_gpu_vec* x,
+                                   const numa_krylov_params* p, numa_gpu_provider* provider,
+                                   numa_krylov_result* results);
+/* Coupled-block periodic multigrid V(pre, post) bound at each Newton iterate; precision FP64 or FP32. */
+int numa_gpu_provider_create_brusselator_mg(numa_gpu_brusselator2d* op, int precision, int pre, int post,
+                                            numa_gpu_provider** out);
+/* Host buffers: x0[2n^2] -> x_out[2n^2] after `steps` steps; precond_kind NONE or BRUSS_MG with
+ * V(2,2) in mg_precision.  Operator, provider and state are kept in the context between calls. */
+int numa_gpu_brusselator2d_advance_host(numa_gpu_ctx* ctx, size_t n, const numa_brusselator2d_params* p,
+                                        size_t steps, int method, int precond_kind, int mg_precision,
+                                        const numa_krylov_params* kp, const double* x0, double* x_out,
+                                        numa_krylov_result* results);
+/* The multigrid alone: levels halve an even n while the coarse n is even and >= 4. */
+int numa_gpu_bmg2d_create(numa_gpu_ctx* ctx, size_t n, const numa_brusselator2d_params* p, int precision, int pre,
+                          int post, numa_gpu_bmg2d** out);
+int numa_gpu_bmg2d_destroy(numa_gpu_bmg2d* mg);
+int numa_gpu_bmg2d_levels(const numa_gpu_bmg2d* mg, size_t* levels);
+/* blocks K(w) of the Jacobian at the state w[2 n^2] */
+int numa_gpu_bmg2d_set_state(numa_gpu_bmg2d* mg, const numa_gpu_vec* w);
+/* z = V-cycle(r) */
+int numa_gpu_bmg2d_apply(numa_gpu_bmg2d* mg, const numa_gpu_vec* r, numa_gpu_vec* z);
 
 /* ---------------------------------------------------------------- batched solves */
 /* No counterpart in the reference.  Solves Bratu3D(inst[i].n, inst[i].lambda) from u0 = 0 for every

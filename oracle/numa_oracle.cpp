@@ -25,6 +25,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <memory>
 #include <stdexcept>
@@ -636,6 +637,354 @@ struct BurgersOp {
     }
 };
 
+// ---------------------------------------------------------------- Brusselator1DStep (problems/brusselator1d.hpp)
+// One implicit-Euler step of the 1D Brusselator, w = (u, v) on n interior points each, Dirichlet
+// u = A = 1, v = B = 3, alpha = 1/50, previous state u = 1 + sin(2 pi x), v = 3
+// (brusselator1d.hpp:22-45).  Expressions are written in the reference's order of operations.
+struct Bruss1D {
+    static constexpr double A = 1.0, B = 3.0, alpha = 1.0 / 50.0;
+    std::size_t n;
+    double dt, h, h2inv;
+    DVec prev;
+
+    Bruss1D(std::size_t n_, double dt_) : n(n_), dt(dt_), h(1.0 / (static_cast<double>(n_) + 1.0)) {
+        if (n == 0 || !(dt > 0.0) || !std::isfinite(dt)) throw std::invalid_argument("Brusselator1DStep: n, dt");
+        h2inv = 1.0 / (h * h);
+        prev.assign(2 * n, 0.0);
+        const double pi = std::acos(-1.0);
+        for (std::size_t i = 0; i < n; ++i) {
+            const double x = (static_cast<double>(i) + 1.0) * h;
+            prev[i] = 1.0 + std::sin(2.0 * pi * x);
+            prev[n + i] = 3.0;
+        }
+    }
+    std::size_t size() const { return 2 * n; }
+    // boundary values u = 1, v = 3 for the state (:144-149), zero for a direction (:151-154)
+    double val(const DVec& w, std::size_t c, long i) const {
+        if (i < 0 || i >= static_cast<long>(n)) return c == 0 ? 1.0 : 3.0;
+        return w[c * n + static_cast<std::size_t>(i)];
+    }
+    double dir(const DVec& d, std::size_t c, long i) const {
+        if (i < 0 || i >= static_cast<long>(n)) return 0.0;
+        return d[c * n + static_cast<std::size_t>(i)];
+    }
+    // (:47-69)
+    void eval(const DVec& w, DVec& out) const {
+        out.assign(size(), 0.0);
+        const double invdt = 1.0 / dt;
+#pragma omp parallel for schedule(static) if (n > 4096)
+        for (long i = 0; i < static_cast<long>(n); ++i) {
+            const std::size_t q = static_cast<std::size_t>(i);
+            const double u = w[q], v = w[n + q];
+            const double lu = (val(w, 0, i - 1) - 2.0 * u + val(w, 0, i + 1)) * h2inv;
+            const double lv = (val(w, 1, i - 1) - 2.0 * v + val(w, 1, i + 1)) * h2inv;
+            out[q] = (u - prev[q]) * invdt - alpha * lu - A - u * u * v + (B + 1.0) * u;
+            out[n + q] = (v - prev[n + q]) * invdt - alpha * lv - B * u + u * u * v;
+        }
+    }
+    // (:71-98)
+    void jvp(const DVec& w, const DVec& d, DVec& out) const {
+        out.assign(size(), 0.0);
+        const double invdt = 1.0 / dt;
+#pragma omp parallel for schedule(static) if (n > 4096)
+        for (long i = 0; i < static_cast<long>(n); ++i) {
+            const std::size_t q = static_cast<std::size_t>(i);
+            const double u = w[q], v = w[n + q], du = d[q], dv = d[n + q];
+            const double ldu = (dir(d, 0, i - 1) - 2.0 * du + dir(d, 0, i + 1)) * h2inv;
+            const double ldv = (dir(d, 1, i - 1) - 2.0 * dv + dir(d, 1, i + 1)) * h2inv;
+            out[q] = invdt * du - alpha * ldu - (2.0 * u * v) * du - u * u * dv + (B + 1.0) * du;
+            out[n + q] = invdt * dv - alpha * ldv - B * du + (2.0 * u * v) * du + u * u * dv;
+        }
+    }
+    // (:100-118)
+    void d2(const DVec& w, const DVec& d, DVec& out) const {
+        out.assign(size(), 0.0);
+        for (std::size_t i = 0; i < n; ++i) {
+            const double u = w[i], v = w[n + i], du = d[i], dv = d[n + i];
+            const double q = 2.0 * v * du * du + 4.0 * u * du * dv;
+            out[i] = -q;
+            out[n + i] = q;
+        }
+    }
+    // 2x2 point blocks of the Jacobian without the off-diagonal diffusion (:120-141)
+    void blocks(const DVec& w, DVec& a11, DVec& a12, DVec& a21, DVec& a22) const {
+        a11.resize(n);
+        a12.resize(n);
+        a21.resize(n);
+        a22.resize(n);
+        const double base = 1.0 / dt + 2.0 * alpha * h2inv;
+        for (std::size_t i = 0; i < n; ++i) {
+            const double u = w[i], v = w[n + i];
+            a11[i] = base - 2.0 * u * v + (B + 1.0);
+            a12[i] = -u * u;
+            a21[i] = -B + 2.0 * u * v;
+            a22[i] = base + u * u;
+        }
+    }
+};
+
+// BrusselatorJacobi::Bound: z = block^-1 r per point, z = r where the determinant is not finite
+// or below 1e-14 in magnitude (brusselator1d.hpp:194-222).
+static void bruss_block_apply(const DVec& a11, const DVec& a12, const DVec& a21, const DVec& a22, const DVec& r,
+                              DVec& z) {
+    const std::size_t n = a11.size();
+    z.assign(2 * n, 0.0);
+    for (std::size_t i = 0; i < n; ++i) {
+        const double det = a11[i] * a22[i] - a12[i] * a21[i];
+        if (!std::isfinite(det) || std::abs(det) < 1e-14) {
+            z[i] = r[i];
+            z[n + i] = r[n + i];
+            continue;
+        }
+        z[i] = (a22[i] * r[i] - a12[i] * r[n + i]) / det;
+        z[n + i] = (-a21[i] * r[i] + a11[i] * r[n + i]) / det;
+    }
+}
+
+// ---------------------------------------------------------------- Brusselator2D (periodic, this project's)
+// Implicit-Euler step of the 2-species Brusselator on an n x n periodic grid of the unit square
+// (h = 1/n): the reaction terms of brusselator1d.hpp:47-98 with parameters A, B, D_u, D_v, dt and
+// the 5-point Laplacian ((W + E) + S) + N - 4c.  w = (u, v) component-major, row-major planes.
+// The reference has no 2D Brusselator: this restatement is the checker of the GPU form only.
+struct Bruss2DParams {
+    double A, B, Du, Dv, dt;
+};
+
+struct Bruss2D {
+    std::size_t n;
+    Bruss2DParams P;
+    double h2inv;
+    DVec prev;
+
+    Bruss2D(std::size_t n_, const Bruss2DParams& p, const double* prev_) : n(n_), P(p) {
+        if (n < 3 || !(P.dt > 0.0) || !(P.Du >= 0.0) || !(P.Dv >= 0.0)) throw std::invalid_argument("Brusselator2D");
+        h2inv = static_cast<double>(n) * static_cast<double>(n);
+        prev.assign(prev_, prev_ + 2 * n * n);
+    }
+    std::size_t size() const { return 2 * n * n; }
+    std::size_t up(std::size_t i) const { return i + 1 == n ? 0 : i + 1; }
+    std::size_t dn(std::size_t i) const { return i == 0 ? n - 1 : i - 1; }
+    double lap(const double* a, std::size_t i, std::size_t j) const {
+        const double c = a[i * n + j];
+        return ((((a[i * n + dn(j)] + a[i * n + up(j)]) + a[dn(i) * n + j]) + a[up(i) * n + j]) - 4.0 * c) * h2inv;
+    }
+    void eval(const DVec& w, DVec& out) const {
+        const std::size_t nn = n * n;
+        const double invdt = 1.0 / P.dt;
+        out.assign(size(), 0.0);
+#pragma omp parallel for schedule(static) if (nn > 4096)
+        for (long ii = 0; ii < static_cast<long>(n); ++ii)
+            for (std::size_t j = 0; j < n; ++j) {
+                const std::size_t i = static_cast<std::size_t>(ii), p = i * n + j;
+                const double u = w[p], v = w[nn + p];
+                const double lu = lap(w.data(), i, j), lv = lap(w.data() + nn, i, j);
+                out[p] = (u - prev[p]) * invdt - P.Du * lu - P.A - u * u * v + (P.B + 1.0) * u;
+                out[nn + p] = (v - prev[nn + p]) * invdt - P.Dv * lv - P.B * u + u * u * v;
+            }
+    }
+    void jvp(const DVec& w, const DVec& d, DVec& out) const {
+        const std::size_t nn = n * n;
+        const double invdt = 1.0 / P.dt;
+        out.assign(size(), 0.0);
+#pragma omp parallel for schedule(static) if (nn > 4096)
+        for (long ii = 0; ii < static_cast<long>(n); ++ii)
+            for (std::size_t j = 0; j < n; ++j) {
+                const std::size_t i = static_cast<std::size_t>(ii), p = i * n + j;
+                const double u = w[p], v = w[nn + p], du = d[p], dv = d[nn + p];
+                const double ldu = lap(d.data(), i, j), ldv = lap(d.data() + nn, i, j);
+                out[p] = invdt * du - P.Du * ldu - (2.0 * u * v) * du - u * u * dv + (P.B + 1.0) * du;
+                out[nn + p] = invdt * dv - P.Dv * ldv - P.B * du + (2.0 * u * v) * du + u * u * dv;
+            }
+    }
+    void d2(const DVec& w, const DVec& d, DVec& out) const {
+        const std::size_t nn = n * n;
+        out.assign(size(), 0.0);
+        for (std::size_t p = 0; p < nn; ++p) {
+            const double u = w[p], v = w[nn + p], du = d[p], dv = d[nn + p];
+            const double q = 2.0 * v * du * du + 4.0 * u * du * dv;
+            out[p] = -q;
+            out[nn + p] = q;
+        }
+    }
+};
+
+// Periodic geometric multigrid for the coupled 2x2 block K(x) - diag(D_u, D_v) Lap_h of the
+// Brusselator2D Jacobian (this project's design; the reference's only Brusselator
+// preconditioner is the point-block Jacobi above).  Levels halve n while the coarse n is even
+// and >= 4; K = [[1/dt + B + 1 - 2uv, -u^2], [2uv - B, 1/dt + u^2]] at the fine level from the
+// Newton iterate, full-weighting restricted to the coarse levels; red-black point-block
+// Gauss-Seidel (colour (i+j)&1), pre-smoothing colours 0,1, post-smoothing 1,0; residual and
+// full weighting (9-point, periodic), bilinear periodic prolongation added; the coarsest level
+// takes 30 sweeps from zero.
+class BrussMG2D {
+public:
+    struct Level {
+        std::size_t n;
+        double su, sv;
+        DVec xu, xv, bu, bv, k11, k12, k21, k22;
+    };
+
+    BrussMG2D(std::size_t n, const Bruss2DParams& p, int pre = 2, int post = 2) : P_(p), pre_(pre), post_(post) {
+        if (n < 4 || n % 2 != 0) throw std::invalid_argument("BrussMG2D needs an even n >= 4");
+        std::size_t m = n;
+        for (;;) {
+            Level L;
+            L.n = m;
+            L.su = P_.Du * (static_cast<double>(m) * static_cast<double>(m));
+            L.sv = P_.Dv * (static_cast<double>(m) * static_cast<double>(m));
+            const std::size_t mm = m * m;
+            for (DVec* a : {&L.xu, &L.xv, &L.bu, &L.bv, &L.k11, &L.k12, &L.k21, &L.k22}) a->assign(mm, 0.0);
+            levels_.push_back(std::move(L));
+            if (m % 4 != 0 || m / 2 < 4) break;
+            m /= 2;
+        }
+    }
+    std::size_t levels() const { return levels_.size(); }
+
+    // K at the fine level from w = (u, v), restricted to every coarser level.
+    void set_state(const DVec& w) {
+        Level& F = levels_[0];
+        const std::size_t nn = F.n * F.n;
+        const double c1 = 1.0 / P_.dt + (P_.B + 1.0), c2 = 1.0 / P_.dt;
+        for (std::size_t p = 0; p < nn; ++p) {
+            const double u = w[p], v = w[nn + p];
+            F.k11[p] = c1 - (2.0 * u) * v;
+            F.k12[p] = -(u * u);
+            F.k21[p] = (2.0 * u) * v - P_.B;
+            F.k22[p] = c2 + u * u;
+        }
+        for (std::size_t l = 0; l + 1 < levels_.size(); ++l) {
+            Level& f = levels_[l];
+            Level& c = levels_[l + 1];
+            fw(f.n, f.k11, c.k11);
+            fw(f.n, f.k12, c.k12);
+            fw(f.n, f.k21, c.k21);
+            fw(f.n, f.k22, c.k22);
+        }
+    }
+
+    void apply(const DVec& r, DVec& z) {
+        Level& F = levels_[0];
+        const std::size_t nn = F.n * F.n;
+        std::copy(r.begin(), r.begin() + nn, F.bu.begin());
+        std::copy(r.begin() + nn, r.begin() + 2 * nn, F.bv.begin());
+        cycle(0);
+        z.resize(2 * nn);
+        std::copy(F.xu.begin(), F.xu.end(), z.begin());
+        std::copy(F.xv.begin(), F.xv.end(), z.begin() + nn);
+    }
+
+    // ((4c + 2((W + E) + (S + N))) + (((SW + SE) + NW) + NE)) / 16 at fine (2I, 2J), periodic.
+    static void fw(std::size_t nf, const DVec& f, DVec& c) {
+        const std::size_t nc = nf / 2;
+        for (std::size_t I = 0; I < nc; ++I)
+            for (std::size_t J = 0; J < nc; ++J) {
+                const std::size_t i = 2 * I, j = 2 * J;
+                const std::size_t im = i == 0 ? nf - 1 : i - 1, ip = i + 1, jm = j == 0 ? nf - 1 : j - 1, jp = j + 1;
+                const double ctr = f[i * nf + j];
+                const double edge = (f[i * nf + jm] + f[i * nf + jp]) + (f[im * nf + j] + f[ip * nf + j]);
+                const double corner = ((f[im * nf + jm] + f[im * nf + jp]) + f[ip * nf + jm]) + f[ip * nf + jp];
+                c[I * nc + J] = ((4.0 * ctr + 2.0 * edge) + corner) * 0.0625;
+            }
+    }
+
+private:
+    static double nsum(const DVec& a, std::size_t n, std::size_t i, std::size_t j) {
+        const std::size_t im = i == 0 ? n - 1 : i - 1, ip = i + 1 == n ? 0 : i + 1;
+        const std::size_t jm = j == 0 ? n - 1 : j - 1, jp = j + 1 == n ? 0 : j + 1;
+        return ((a[i * n + jm] + a[i * n + jp]) + a[im * n + j]) + a[ip * n + j];
+    }
+    void smooth(Level& L, int colour) {
+        const std::size_t n = L.n;
+        for (std::size_t i = 0; i < n; ++i)
+            for (std::size_t j = (i + colour) & 1; j < n; j += 2) {
+                const std::size_t p = i * n + j;
+                const double ru = L.bu[p] + L.su * nsum(L.xu, n, i, j);
+                const double rv = L.bv[p] + L.sv * nsum(L.xv, n, i, j);
+                const double m11 = L.k11[p] + 4.0 * L.su, m22 = L.k22[p] + 4.0 * L.sv;
+                const double det = m11 * m22 - L.k12[p] * L.k21[p];
+                L.xu[p] = (m22 * ru - L.k12[p] * rv) / det;
+                L.xv[p] = (m11 * rv - L.k21[p] * ru) / det;
+            }
+    }
+    void cycle(std::size_t l) {
+        Level& L = levels_[l];
+        std::fill(L.xu.begin(), L.xu.end(), 0.0);
+        std::fill(L.xv.begin(), L.xv.end(), 0.0);
+        if (l + 1 == levels_.size()) {
+            for (int s = 0; s < 30; ++s) {
+                smooth(L, 0);
+                smooth(L, 1);
+            }
+            return;
+        }
+        for (int s = 0; s < pre_; ++s) {
+            smooth(L, 0);
+            smooth(L, 1);
+        }
+        const std::size_t n = L.n, nn = n * n;
+        DVec ru(nn), rv(nn);
+        for (std::size_t i = 0; i < n; ++i)
+            for (std::size_t j = 0; j < n; ++j) {
+                const std::size_t p = i * n + j;
+                const double u = L.xu[p], v = L.xv[p];
+                ru[p] = L.bu[p] - ((L.k11[p] * u + L.k12[p] * v) + L.su * (4.0 * u - nsum(L.xu, n, i, j)));
+                rv[p] = L.bv[p] - ((L.k21[p] * u + L.k22[p] * v) + L.sv * (4.0 * v - nsum(L.xv, n, i, j)));
+            }
+        Level& C = levels_[l + 1];
+        fw(n, ru, C.bu);
+        fw(n, rv, C.bv);
+        cycle(l + 1);
+        prolong_add(C.n, C.xu, L.xu);
+        prolong_add(C.n, C.xv, L.xv);
+        for (int s = 0; s < post_; ++s) {
+            smooth(L, 1);
+            smooth(L, 0);
+        }
+    }
+    // fine (2I, 2J) += c; (2I+1, 2J) += (c + c_{I+1}) / 2; (2I, 2J+1) += (c + c_{J+1}) / 2;
+    // (2I+1, 2J+1) += (((c + c_{I+1}) + c_{J+1}) + c_{I+1,J+1}) / 4, periodic.
+    static void prolong_add(std::size_t nc, const DVec& c, DVec& f) {
+        const std::size_t nf = 2 * nc;
+        for (std::size_t I = 0; I < nc; ++I)
+            for (std::size_t J = 0; J < nc; ++J) {
+                const std::size_t I1 = I + 1 == nc ? 0 : I + 1, J1 = J + 1 == nc ? 0 : J + 1;
+                const double c00 = c[I * nc + J], c10 = c[I1 * nc + J], c01 = c[I * nc + J1], c11 = c[I1 * nc + J1];
+                f[(2 * I) * nf + 2 * J] += c00;
+                f[(2 * I + 1) * nf + 2 * J] += 0.5 * (c00 + c10);
+                f[(2 * I) * nf + 2 * J + 1] += 0.5 * (c00 + c01);
+                f[(2 * I + 1) * nf + 2 * J + 1] += 0.25 * (((c00 + c10) + c01) + c11);
+            }
+    }
+
+    Bruss2DParams P_;
+    int pre_, post_;
+    std::vector<Level> levels_;
+};
+
+template <class F>
+struct GenericOp {
+    const F& f;
+    int jvp_mode, d2_mode;
+    Timers* timers;
+    std::size_t size() const { return f.size(); }
+    void eval(const DVec& x, DVec& out) const {
+        auto t0 = Clock::now();
+        f.eval(x, out);
+        timers->t_F += seconds_since(t0);
+    }
+    void jvp(const DVec& x, const DVec& v, DVec& out) const {
+        auto t0 = Clock::now();
+        if (jvp_mode == 1) jvp_fd(f, x, v, out); else f.jvp(x, v, out);
+        timers->t_JVP += seconds_since(t0);
+    }
+    void d2(const DVec& x, const DVec& v, DVec& out) const {
+        auto t0 = Clock::now();
+        if (d2_mode == 1) d2_fd(f, x, v, out); else f.d2(x, v, out);
+        timers->t_D2 += seconds_since(t0);
+    }
+};
+
 // ---------------------------------------------------------------- preconditioner providers
 constexpr int kBurgersMG = 3;
 
@@ -646,18 +995,26 @@ struct Provider {
     const Bratu* f = nullptr;
     std::shared_ptr<PoissonMG> mg;
     std::shared_ptr<HelmholtzMG2D> hmg;  // BurgersMGProvider (burgers2d.hpp:220-246)
+    const Bruss1D* bf = nullptr;         // BrusselatorJacobi (brusselator1d.hpp:194-222)
+    std::shared_ptr<BrussMG2D> bmg;      // Brusselator2D coupled-block multigrid
     std::size_t nn = 0;
-    DVec diag;
+    DVec diag, a11, a12, a21, a22;
     Timers* timers = nullptr;
 
     void make(const DVec& x) {
         auto t0 = Clock::now();
         if (kind == NUMA_GPU_PRECOND_JACOBI) f->jacobi_diag(x, diag);
+        if (kind == NUMA_GPU_PRECOND_BRUSS_JACOBI) bf->blocks(x, a11, a12, a21, a22);
+        if (kind == NUMA_GPU_PRECOND_BRUSS_MG) bmg->set_state(x);
         if (timers) timers->t_setup += seconds_since(t0);
     }
     void operator()(const DVec& r, DVec& z) const {
         auto t0 = Clock::now();
-        if (kind == NUMA_GPU_PRECOND_POISSON_MG) {
+        if (kind == NUMA_GPU_PRECOND_BRUSS_JACOBI) {
+            bruss_block_apply(a11, a12, a21, a22, r, z);
+        } else if (kind == NUMA_GPU_PRECOND_BRUSS_MG) {
+            bmg->apply(r, z);
+        } else if (kind == NUMA_GPU_PRECOND_POISSON_MG) {
             mg->apply(r, z);
         } else if (kind == kBurgersMG) {
             DVec ru(r.begin(), r.begin() + nn), rv(r.begin() + nn, r.end()), zu, zv;
@@ -1077,6 +1434,46 @@ static Params to_params(const numa_krylov_params* cp) {
     return p;
 }
 
+// Runs a driver on a Brusselator operator and fills the C result (bench-style timers included).
+static int bruss_solve(int method, Params p, const std::function<Result(int, Params&, Timers&)>& run,
+                       double* x_out, numa_krylov_result* res) {
+    auto t_start = Clock::now();
+    Timers t;
+    if (method == NUMA_GPU_METHOD_CHEB_REC) p.recycle = true;
+    if (method < NUMA_GPU_METHOD_NK || method > NUMA_GPU_METHOD_TF2018) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    Result r = run(method, p, t);
+    if (x_out) std::memcpy(x_out, r.x.data(), r.x.size() * sizeof(double));
+    if (res) {
+        std::memset(res, 0, sizeof(*res));
+        res->converged = r.converged ? 1 : 0;
+        res->iters = r.iters;
+        res->n_F = r.n_F;
+        res->n_JVP = r.n_JVP;
+        res->n_D2 = r.n_D2;
+        res->n_lin_iters = r.n_lin_iters;
+        res->n_lin_failures = r.n_lin_failures;
+        res->n_prec = r.n_prec;
+        res->res0 = r.res0;
+        res->res = r.res;
+        res->t_F = t.t_F;
+        res->t_JVP = t.t_JVP;
+        res->t_D2 = t.t_D2;
+        res->t_prec = t.t_prec;
+        res->t_setup_dynamic = t.t_setup;
+        res->t_total = seconds_since(t_start);
+    }
+    return 0;
+}
+
+template <class Op>
+static Result run_method(int method, const Op& op, const DVec& x0, const Params& p, Provider& pc) {
+    switch (method) {
+        case NUMA_GPU_METHOD_NK: return newton_krylov(op, x0, p, pc);
+        case NUMA_GPU_METHOD_TF2018: return tf_chebyshev_2018(op, x0, p, pc);
+        default: return chebyshev_inexact(op, x0, p, pc);
+    }
+}
+
 }  // namespace oracle
 
 // ============================================================================ C API (ctypes)
@@ -1423,6 +1820,149 @@ int oracle_solve_burgers2d(size_t n, double nu, double dt, double amp, int metho
             res->t_total = seconds_since(t_start);
         }
         return 0;
+    } catch (const std::invalid_argument&) {
+        return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    }
+}
+
+// ---- Brusselator1DStep and Brusselator2D
+int oracle_bruss1d_previous(size_t n, double dt, double* out) {
+    try {
+        Bruss1D f(n, dt);
+        std::memcpy(out, f.prev.data(), f.size() * sizeof(double));
+        return 0;
+    } catch (const std::invalid_argument&) {
+        return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    }
+}
+
+int oracle_bruss1d_eval(size_t n, double dt, const double* w, double* out) {
+    Bruss1D f(n, dt);
+    DVec W(w, w + f.size()), O;
+    f.eval(W, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+    return 0;
+}
+
+int oracle_bruss1d_jvp(size_t n, double dt, const double* w, const double* d, double* out, int mode) {
+    Bruss1D f(n, dt);
+    DVec W(w, w + f.size()), D(d, d + f.size()), O;
+    if (mode == 1) jvp_fd(f, W, D, O); else f.jvp(W, D, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+    return 0;
+}
+
+int oracle_bruss1d_d2(size_t n, double dt, const double* w, const double* d, double* out, int mode) {
+    Bruss1D f(n, dt);
+    DVec W(w, w + f.size()), D(d, d + f.size()), O;
+    if (mode == 1) d2_fd(f, W, D, O); else f.d2(W, D, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+    return 0;
+}
+
+// BrusselatorJacobi made at w and applied to r.
+int oracle_bruss1d_jacobi_apply(size_t n, double dt, const double* w, const double* r, double* z) {
+    Bruss1D f(n, dt);
+    DVec W(w, w + f.size()), R(r, r + f.size()), a11, a12, a21, a22, Z;
+    f.blocks(W, a11, a12, a21, a22);
+    bruss_block_apply(a11, a12, a21, a22, R, Z);
+    std::memcpy(z, Z.data(), Z.size() * sizeof(double));
+    return 0;
+}
+
+// Brusselator1DStep(n, dt) from x0 (null: the previous state, run_campaign's natural start) with
+// NoPrecond or BrusselatorJacobi.
+int oracle_solve_bruss1d(size_t n, double dt, int method, int precond_kind, const numa_krylov_params* cp,
+                         const double* x0, double* x_out, numa_krylov_result* res) {
+    try {
+        Bruss1D f(n, dt);
+        if (precond_kind != NUMA_GPU_PRECOND_NONE && precond_kind != NUMA_GPU_PRECOND_BRUSS_JACOBI)
+            return NUMA_GPU_ERR_INVALID_ARGUMENT;
+        const DVec X0 = x0 ? DVec(x0, x0 + f.size()) : f.prev;
+        return bruss_solve(method, to_params(cp), [&](int m, Params& p, Timers& t) {
+            GenericOp<Bruss1D> op{f, cp ? cp->jvp_mode : 0, cp ? cp->d2_mode : 0, &t};
+            Provider pc;
+            pc.timers = &t;
+            pc.kind = precond_kind;
+            pc.bf = &f;
+            return run_method(m, op, X0, p, pc);
+        }, x_out, res);
+    } catch (const std::invalid_argument&) {
+        return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    }
+}
+
+// prm = {A, B, D_u, D_v, dt}
+static Bruss2DParams bruss2d_params(const double* prm) { return Bruss2DParams{prm[0], prm[1], prm[2], prm[3], prm[4]}; }
+
+int oracle_bruss2d_eval(size_t n, const double* prm, const double* prev, const double* w, double* out) {
+    Bruss2D f(n, bruss2d_params(prm), prev);
+    DVec W(w, w + f.size()), O;
+    f.eval(W, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+    return 0;
+}
+
+int oracle_bruss2d_jvp(size_t n, const double* prm, const double* prev, const double* w, const double* d,
+                       double* out, int mode) {
+    Bruss2D f(n, bruss2d_params(prm), prev);
+    DVec W(w, w + f.size()), D(d, d + f.size()), O;
+    if (mode == 1) jvp_fd(f, W, D, O); else f.jvp(W, D, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+    return 0;
+}
+
+int oracle_bruss2d_d2(size_t n, const double* prm, const double* prev, const double* w, const double* d,
+                      double* out, int mode) {
+    Bruss2D f(n, bruss2d_params(prm), prev);
+    DVec W(w, w + f.size()), D(d, d + f.size()), O;
+    if (mode == 1) d2_fd(f, W, D, O); else f.d2(W, D, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+    return 0;
+}
+
+int oracle_bmg2d_levels(size_t n) {
+    try {
+        BrussMG2D mg(n, Bruss2DParams{1.0, 1.0, 1.0, 1.0, 1.0});
+        return static_cast<int>(mg.levels());
+    } catch (const std::invalid_argument&) {
+        return -1;
+    }
+}
+
+// One V-cycle of the coupled-block multigrid set at the state w, applied to r.
+int oracle_bmg2d_apply(size_t n, const double* prm, const double* w, int pre, int post, const double* r, double* z) {
+    try {
+        BrussMG2D mg(n, bruss2d_params(prm), pre, post);
+        DVec W(w, w + 2 * n * n), R(r, r + 2 * n * n), Z;
+        mg.set_state(W);
+        mg.apply(R, Z);
+        std::memcpy(z, Z.data(), Z.size() * sizeof(double));
+        return 0;
+    } catch (const std::invalid_argument&) {
+        return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    }
+}
+
+// One implicit-Euler step of Brusselator2D from the previous state prev, Newton start x0 (null:
+// prev), with NoPrecond or the coupled-block multigrid.
+int oracle_solve_bruss2d(size_t n, const double* prm, const double* prev, int method, int precond_kind,
+                         const numa_krylov_params* cp, const double* x0, double* x_out, numa_krylov_result* res) {
+    try {
+        Bruss2D f(n, bruss2d_params(prm), prev);
+        if (precond_kind != NUMA_GPU_PRECOND_NONE && precond_kind != NUMA_GPU_PRECOND_BRUSS_MG)
+            return NUMA_GPU_ERR_INVALID_ARGUMENT;
+        const DVec X0 = x0 ? DVec(x0, x0 + f.size()) : f.prev;
+        std::shared_ptr<BrussMG2D> mg;
+        if (precond_kind == NUMA_GPU_PRECOND_BRUSS_MG) mg = std::make_shared<BrussMG2D>(n, f.P);
+        return bruss_solve(method, to_params(cp), [&](int m, Params& p, Timers& t) {
+            GenericOp<Bruss2D> op{f, cp ? cp->jvp_mode : 0, cp ? cp->d2_mode : 0, &t};
+            Provider pc;
+            pc.timers = &t;
+            pc.kind = precond_kind;
+            pc.bmg = mg;
+            return run_method(m, op, X0, p, pc);
+        }, x_out, res);
     } catch (const std::invalid_argument&) {
         return NUMA_GPU_ERR_INVALID_ARGUMENT;
     }

@@ -122,7 +122,21 @@ class Oracle:
         self._happly = fn("hmg2d_apply", [sz, dbl, dbl, i32, i32, F64P, F64P], i32)
         self._bsolve = fn("solve_burgers2d", [sz, dbl, dbl, dbl, i32, i32, C.POINTER(KrylovParams), F64P, F64P,
                                               C.POINTER(KrylovResult)], i32)
+        self._r1prev = fn("bruss1d_previous", [sz, dbl, F64P], i32)
+        self._r1eval = fn("bruss1d_eval", [sz, dbl, F64P, F64P], i32)
+        self._r1jvp = fn("bruss1d_jvp", [sz, dbl, F64P, F64P, F64P, i32], i32)
+        self._r1d2 = fn("bruss1d_d2", [sz, dbl, F64P, F64P, F64P, i32], i32)
+        self._r1jac = fn("bruss1d_jacobi_apply", [sz, dbl, F64P, F64P, F64P], i32)
+        self._r1solve = fn("solve_bruss1d", [sz, dbl, i32, i32, C.POINTER(KrylovParams), F64P, F64P,
+                                             C.POINTER(KrylovResult)], i32)
         if prefix == "oracle_":
+            self._r2eval = fn("bruss2d_eval", [sz, F64P, F64P, F64P, F64P], i32)
+            self._r2jvp = fn("bruss2d_jvp", [sz, F64P, F64P, F64P, F64P, F64P, i32], i32)
+            self._r2d2 = fn("bruss2d_d2", [sz, F64P, F64P, F64P, F64P, F64P, i32], i32)
+            self._bmglev = fn("bmg2d_levels", [sz], i32)
+            self._bmgapply = fn("bmg2d_apply", [sz, F64P, F64P, i32, i32, F64P, F64P], i32)
+            self._r2solve = fn("solve_bruss2d", [sz, F64P, F64P, i32, i32, C.POINTER(KrylovParams), F64P, F64P,
+                                                 C.POINTER(KrylovResult)], i32)
             self._smooth = fn("mg_smooth", [sz, dbl, F64P, F64P, i32])
             self._resid = fn("mg_residual", [sz, dbl, F64P, F64P, F64P])
             self._restrict = fn("mg_restrict", [sz, F64P, F64P])
@@ -276,6 +290,94 @@ class Oracle:
                           _ptr(x), C.byref(res))
         if rc != 0:
             raise ValueError(f"Burgers2D solve failed with status {rc}")
+        return x, struct_dict(res)
+
+    # ---- Brusselator1DStep (problems/brusselator1d.hpp) and BrusselatorJacobi
+    def bruss1d_previous(self, n, dt):
+        out = np.empty(2 * n)
+        if self._r1prev(n, dt, _ptr(out)) != 0:
+            raise ValueError("Brusselator1DStep: invalid n or dt")
+        return out
+
+    def bruss1d_eval(self, n, dt, w):
+        w = _f64(w)
+        out = np.empty(2 * n)
+        self._r1eval(n, dt, _ptr(w), _ptr(out))
+        return out
+
+    def bruss1d_jvp(self, n, dt, w, d, mode=0):
+        w, d = _f64(w), _f64(d)
+        out = np.empty(2 * n)
+        self._r1jvp(n, dt, _ptr(w), _ptr(d), _ptr(out), mode)
+        return out
+
+    def bruss1d_d2(self, n, dt, w, d, mode=0):
+        w, d = _f64(w), _f64(d)
+        out = np.empty(2 * n)
+        self._r1d2(n, dt, _ptr(w), _ptr(d), _ptr(out), mode)
+        return out
+
+    def bruss1d_jacobi_apply(self, n, dt, w, r):
+        w, r = _f64(w), _f64(r)
+        z = np.empty(2 * n)
+        self._r1jac(n, dt, _ptr(w), _ptr(r), _ptr(z))
+        return z
+
+    def solve_bruss1d(self, n, dt, method="nk", precond="jacobi", params=None, x0=None):
+        """x0 None: the previous state (run_campaign's natural start)."""
+        p = params if params is not None else default_params()
+        x = np.empty(2 * n)
+        res = KrylovResult()
+        kind = 5 if precond == "jacobi" else 0
+        x0p = None if x0 is None else _ptr(_f64(x0))
+        rc = self._r1solve(n, dt, METHODS[method], kind, C.byref(p), x0p, _ptr(x), C.byref(res))
+        if rc != 0:
+            raise ValueError(f"Brusselator1D solve failed with status {rc}")
+        return x, struct_dict(res)
+
+    # ---- Brusselator2D (periodic) and its coupled-block multigrid (this project's; no reference)
+    @staticmethod
+    def _prm(prm):
+        return _f64([prm["A"], prm["B"], prm["Du"], prm["Dv"], prm["dt"]])
+
+    def bruss2d_eval(self, n, prm, prev, w):
+        pr, prev, w = self._prm(prm), _f64(prev), _f64(w)
+        out = np.empty(2 * n * n)
+        self._r2eval(n, _ptr(pr), _ptr(prev), _ptr(w), _ptr(out))
+        return out
+
+    def bruss2d_jvp(self, n, prm, prev, w, d, mode=0):
+        pr, prev, w, d = self._prm(prm), _f64(prev), _f64(w), _f64(d)
+        out = np.empty(2 * n * n)
+        self._r2jvp(n, _ptr(pr), _ptr(prev), _ptr(w), _ptr(d), _ptr(out), mode)
+        return out
+
+    def bruss2d_d2(self, n, prm, prev, w, d, mode=0):
+        pr, prev, w, d = self._prm(prm), _f64(prev), _f64(w), _f64(d)
+        out = np.empty(2 * n * n)
+        self._r2d2(n, _ptr(pr), _ptr(prev), _ptr(w), _ptr(d), _ptr(out), mode)
+        return out
+
+    def bmg2d_levels(self, n):
+        return self._bmglev(n)
+
+    def bmg2d_apply(self, n, prm, w, r, pre=2, post=2):
+        pr, w, r = self._prm(prm), _f64(w), _f64(r)
+        z = np.empty(2 * n * n)
+        if self._bmgapply(n, _ptr(pr), _ptr(w), pre, post, _ptr(r), _ptr(z)) != 0:
+            raise ValueError("BrussMG2D needs an even n >= 4")
+        return z
+
+    def solve_bruss2d(self, n, prm, prev, method="nk", precond="mg", params=None, x0=None):
+        p = params if params is not None else default_params()
+        pr, prev = self._prm(prm), _f64(prev)
+        x = np.empty(2 * n * n)
+        res = KrylovResult()
+        kind = 6 if precond == "mg" else 0
+        x0p = None if x0 is None else _ptr(_f64(x0))
+        rc = self._r2solve(n, _ptr(pr), _ptr(prev), METHODS[method], kind, C.byref(p), x0p, _ptr(x), C.byref(res))
+        if rc != 0:
+            raise ValueError(f"Brusselator2D solve failed with status {rc}")
         return x, struct_dict(res)
 
     def forcing(self, params, k, rnorm, rprev, eta_prev, res0):

@@ -16,6 +16,7 @@
 #include <numa/methods/tf_chebyshev_2018.hpp>
 #include <numa/operators/operator.hpp>
 #include <numa/problems/bratu3d.hpp>
+#include <numa/problems/brusselator1d.hpp>
 #include <numa/problems/burgers2d.hpp>
 #include <numa/linalg/helmholtz_mg2d.hpp>
 
@@ -299,6 +300,88 @@ int ref_solve_burgers2d(size_t n, double nu, double dt, double amp, int method, 
     DVec X0(x0, x0 + f.size());
     KrylovResult r = precond_kind == NUMA_GPU_PRECOND_POISSON_MG ? run(method, op, X0, p, BurgersMGProvider(n, nu, dt))
                                                                  : run(method, op, X0, p, NoPrecond{});
+    if (x_out) std::memcpy(x_out, r.x.data(), r.x.size() * sizeof(double));
+    if (res) {
+        std::memset(res, 0, sizeof(*res));
+        res->converged = r.converged;
+        res->iters = r.iters;
+        res->n_F = r.n_F;
+        res->n_JVP = r.n_JVP;
+        res->n_D2 = r.n_D2;
+        res->n_lin_iters = r.n_lin_iters;
+        res->n_lin_failures = r.n_lin_failures;
+        res->n_prec = r.n_prec;
+        res->res0 = r.res0;
+        res->res = r.res;
+    }
+    return 0;
+}
+
+// ---- Brusselator1DStep and BrusselatorJacobi (problems/brusselator1d.hpp)
+int ref_bruss1d_previous(size_t n, double dt, double* out) {
+    Brusselator1DStep f(n, dt);
+    std::memcpy(out, f.previous().data(), f.size() * sizeof(double));
+    return 0;
+}
+
+int ref_bruss1d_eval(size_t n, double dt, const double* w, double* out) {
+    Brusselator1DStep f(n, dt);
+    DVec W(w, w + f.size()), O;
+    f.eval(W, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+    return 0;
+}
+
+int ref_bruss1d_jvp(size_t n, double dt, const double* w, const double* d, double* out, int mode) {
+    Brusselator1DStep f(n, dt);
+    DVec W(w, w + f.size()), D(d, d + f.size()), O;
+    if (mode == 1) jvp_fd(f, W, D, O); else f.jvp(W, D, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+    return 0;
+}
+
+int ref_bruss1d_d2(size_t n, double dt, const double* w, const double* d, double* out, int mode) {
+    Brusselator1DStep f(n, dt);
+    DVec W(w, w + f.size()), D(d, d + f.size()), O;
+    if (mode == 1) d2_fd(f, W, D, O); else f.d2(W, D, O);
+    std::memcpy(out, O.data(), O.size() * sizeof(double));
+    return 0;
+}
+
+int ref_bruss1d_jacobi_apply(size_t n, double dt, const double* w, const double* r, double* z) {
+    Brusselator1DStep f(n, dt);
+    BrusselatorJacobi pc{f};
+    DVec W(w, w + f.size()), R(r, r + f.size()), Z;
+    auto bound = pc.make(W);
+    bound(R, Z);
+    std::memcpy(z, Z.data(), Z.size() * sizeof(double));
+    return 0;
+}
+
+namespace {
+struct FdBruss {
+    const Brusselator1DStep& f;
+    int jvp_mode, d2_mode;
+    std::size_t size() const { return f.size(); }
+    void eval(const DVec& x, DVec& out) const { f.eval(x, out); }
+    void jvp(const DVec& x, const DVec& v, DVec& out) const {
+        if (jvp_mode == 1) jvp_fd(f, x, v, out); else f.jvp(x, v, out);
+    }
+    void d2(const DVec& x, const DVec& v, DVec& out) const {
+        if (d2_mode == 1) d2_fd(f, x, v, out); else f.d2(x, v, out);
+    }
+};
+}  // namespace
+
+// From x0 (null: previous(), run_campaign.cpp's natural start) with NoPrecond or BrusselatorJacobi.
+int ref_solve_bruss1d(size_t n, double dt, int method, int precond_kind, const numa_krylov_params* cp,
+                      const double* x0, double* x_out, numa_krylov_result* res) {
+    Brusselator1DStep f(n, dt);
+    FdBruss op{f, cp ? cp->jvp_mode : 0, cp ? cp->d2_mode : 0};
+    const KrylovParams p = to_params(cp);
+    const DVec X0 = x0 ? DVec(x0, x0 + f.size()) : f.previous();
+    KrylovResult r = precond_kind == NUMA_GPU_PRECOND_BRUSS_JACOBI ? run(method, op, X0, p, BrusselatorJacobi{f})
+                                                                   : run(method, op, X0, p, NoPrecond{});
     if (x_out) std::memcpy(x_out, r.x.data(), r.x.size() * sizeof(double));
     if (res) {
         std::memset(res, 0, sizeof(*res));

@@ -2,7 +2,7 @@
 
 Run from the repository root, where the reference is present:
 
-    OMP_NUM_THREADS=1 python tests/golden/make_golden.py
+    OMP_NUM_THREADS=1 python tests/golden/make_golden.py [--brusselator]
 
 (one thread: OpenMP's reduction order is not fixed across runs with more threads, and the
 reference's published calibration runs used one thread).
@@ -205,5 +205,63 @@ def main() -> None:
     print(len(out_counts), "solves,", len(vectors), "vectors,", len(rows), "calibration rows")
 
 
+def brusselator_main() -> None:
+    """Brusselator1DStep / BrusselatorJacobi (problems/brusselator1d.hpp) fixtures:
+
+    * ``reference_brusselator.npz`` — the previous state, F, J v, F'' (analytic and finite
+      difference) and a BrusselatorJacobi application on the reference test's point
+      (tests/test_brusselator.cpp:13-19, :37-53), n = 31, dt = 0.01;
+    * ``reference_brusselator.json`` — every method with and without BrusselatorJacobi from the
+      previous state at n = 31, dt = 0.01, rtol 1e-9, GMRES(30), 200 iterations (the test's
+      configuration, :55-67), and at n = 127, dt = 0.016 with the calibration campaign's parameters;
+    * ``c1_brusselator_jacobi.json`` — the reference's published Brusselator calibration rows
+      (experiments/c1/amendment01/calibration_combined.csv, repetition 1), read, not recomputed.
+    """
+    build_ref(force=True)
+    ref = Oracle.reference()
+    n, dt = 31, 0.01
+    prev = ref.bruss1d_previous(n, dt)
+    idx = np.arange(2 * n, dtype=np.float64)
+    x = prev + 0.05 * np.sin(0.31 * idx + 0.4)
+    d = 0.4 * np.sin(0.31 * idx + 1.2)
+    vec = {"prev": prev, "x": x, "d": d, "eval_prev": ref.bruss1d_eval(n, dt, prev), "eval_x": ref.bruss1d_eval(n, dt, x)}
+    for mode, tag in ((0, ""), (1, "_fd")):
+        vec[f"jvp{tag}"] = ref.bruss1d_jvp(n, dt, x, d, mode)
+        vec[f"d2{tag}"] = ref.bruss1d_d2(n, dt, x, d, mode)
+    vec["jacobi_x_d"] = ref.bruss1d_jacobi_apply(n, dt, x, d)
+    solves = []
+    cases = [(31, 0.01, default_params(rtol_nl=1e-9, gmres_restart=30, gmres_max_iters=200), "test"),
+             (127, 0.016, default_params(rtol_nl=1e-8, eta_init=0.25, gmres_restart=30, gmres_max_iters=200),
+              "calibration")]
+    for cn, cdt, p, tag in cases:
+        for method in ("nk", "cheb", "rec", "tf2018"):
+            for precond in ("jacobi", "none"):
+                xs, res = ref.solve_bruss1d(cn, cdt, method, precond, p)
+                solves.append(dict(tag=tag, n=cn, dt=cdt, method=method, precond=precond, params=params_dict(p),
+                                   result={k: res[k] for k in ("converged", "iters", "n_F", "n_JVP", "n_D2",
+                                                               "n_lin_iters", "n_lin_failures", "n_prec", "res0",
+                                                               "res")},
+                                   solution=solution_stats(xs)))
+                if precond == "jacobi":
+                    vec[f"x_{tag}_{method}"] = xs
+    (HERE / "reference_brusselator.json").write_text(json.dumps({"solves": solves}, indent=1))
+    np.savez_compressed(HERE / "reference_brusselator.npz", **vec)
+    rows = []
+    with open(CALIBRATION_CSV) as fh:
+        for r in csv.DictReader(fh):
+            if r["problem"] != "brusselator" or r["repetition"] != "1":
+                continue
+            rows.append({k: r[k] for k in (
+                "n", "param", "method", "precond", "internal_candidate_id", "success", "nonlinear_iters", "n_F",
+                "n_JVP", "n_D2", "n_lin", "n_lin_failures", "n_prec", "residual_rel", "rtol", "max_nl", "eta_init",
+                "eta_max", "gamma", "alpha", "eta2_factor", "eta2_max", "restart", "maxlin")})
+    (HERE / "c1_brusselator_jacobi.json").write_text(json.dumps(rows, indent=0))
+    print(len(solves), "Brusselator solves,", len(vec), "vectors,", len(rows), "calibration rows")
+
+
 if __name__ == "__main__":
-    main()
+    if "--brusselator" in sys.argv:
+        brusselator_main()
+    else:
+        main()
+        brusselator_main()
