@@ -62,9 +62,10 @@ def parse_args(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-solves leg")
+    ap.add_argument("--no-brusselator", action="store_true", help="skip the 2D Brusselator leg")
     ap.add_argument("--cpu-sample-n", type=int, default=127)
     ap.add_argument("--cpu-reps", type=int, default=2)
-    ap.add_argument("--kernel-case", choices=["none", "vcycle", "solve", "conv"], default="none",
+    ap.add_argument("--kernel-case", choices=["none", "vcycle", "solve", "conv", "bruss"], default="none",
                     help="profiling driver: run only this small case (for ncu)")
     return ap.parse_args(argv)
 
@@ -348,6 +349,12 @@ def run_ours(args) -> int:
                     "identical batches is timed (the first sets every worker up)",
         }
 
+    # 2D Brusselator: 2048^2 periodic, 2 species, 20 implicit-Euler steps, NK + FGMRES(40) with the
+    # FP32 coupled-block multigrid (FP64 outer), beside the all-FP64 form
+    bruss = None
+    if not args.no_brusselator and dist.rank == 0:
+        bruss = brusselator_leg(G, ctx, stream, torch)
+
     # end to end through the host-buffer entry point, pinned buffers
     h_in = torch.zeros(N, dtype=torch.float64, pin_memory=True).numpy()
     h_out = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
@@ -433,6 +440,7 @@ def run_ours(args) -> int:
                                        "preconditioner"},
             "learned_mixed": learned_summary(learned, fp64_sec, x_head if args.path == "fp64" else x_other),
             "batched": batched,
+            "brusselator2d": bruss,
             "clocks": clk.summary(),
             "e2e": {"value": e2e_sec, "unit": "s", "h2d_bytes_per_step": N * 8, "d2h_bytes_per_step": N * 8,
                     "api": "numa_gpu_solve_bratu3d_host, pinned host buffers"},
@@ -444,6 +452,83 @@ def run_ours(args) -> int:
         print(json.dumps(line), flush=True)
     dist.close()
     return 0
+
+
+def brusselator_leg(G, ctx, stream, torch, n: int = 2048, steps: int = 20) -> dict:
+    """Twenty implicit-Euler steps of the periodic 2-species Brusselator at 2048^2 (A = 1, B = 3.4,
+    D = 0.002, dt = 0.01, seeded initial state): device-resident (CUDA events) and end to end
+    through numa_gpu_brusselator2d_advance_host with pinned buffers; the CPU restatement times one
+    step at 512^2 on the host cores, scaled by the unknowns and the step count."""
+    prm = G.brusselator_params()
+    N = 2 * n * n
+    x0 = G.brusselator2d_initial(n)
+    op = G.Brusselator2D(ctx, n, prm)
+    # rtol 1e-6 per step: once the initial noise has decayed (step ~14) a step starts from
+    # ||F|| ~ 1, while ||F|| cannot fall below ~sqrt(N) 4 D h^-2 ulp(u) / 2 ~ 1e-8 at 2048^2 (an
+    # FP64 state rounded to the ulp moves F by that much), so 1e-8 is out of reach there
+    kp = dict(rtol_nl=1e-6, gmres_restart=40, gmres_max_iters=400)
+    legs = {"mixed": (G.Provider.brusselator_mg(op, G.FP32),
+                      G.default_params(flexible=1, jvp_precision=G.FP32, orth=G.CGS1, **kp)),
+            "fp64": (G.Provider.brusselator_mg(op, G.FP64), G.default_params(**kp))}
+    x0d = ctx.from_numpy(x0)
+    x = ctx.vec(N)
+    out = {}
+    for name, (pc, p) in legs.items():
+        x.copy_from(x0d)
+        op.advance(x, 1, "nk", p, pc)  # warm: workspaces, multigrid graph
+        x.copy_from(x0d)
+        ctx.sync()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        res = op.advance(x, steps, "nk", p, pc)
+        ev1.record(stream)
+        ev1.synchronize()
+        out[name] = {"s": ev0.elapsed_time(ev1) * 1e-3, "x": x.numpy(), "res": res}
+    mixed, fp64 = out["mixed"], out["fp64"]
+    h_in = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+    h_out = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+    h_in[:] = x0
+    t0 = time.perf_counter()
+    _, res_h = G.brusselator2d_advance_host(ctx, n, h_in, steps, prm, "nk", "mg", G.FP32, legs["mixed"][1], h_out)
+    e2e = time.perf_counter() - t0
+    # one step at 512^2 on the host cores (the CPU restatement, FP64 multigrid, same parameters)
+    from oracle.oracle_lib import Oracle, default_params as oparams
+    o = Oracle()
+    cores = o.max_threads()
+    o.set_threads(cores)
+    ns = 512
+    xs = G.brusselator2d_initial(ns)
+    t0 = time.perf_counter()
+    _, rcpu = o.solve_bruss2d(ns, dict(A=prm.A, B=prm.B, Du=prm.Du, Dv=prm.Dv, dt=prm.dt), xs, "nk", "mg",
+                              oparams(**kp))
+    t_cpu = time.perf_counter() - t0
+    scale = (n * n) / (ns * ns) * steps
+    agg = lambda rs, k: sum(r[k] for r in rs)  # noqa: E731
+    return {
+        "workload": f"Brusselator2D {n}^2 periodic, 2 species, A=1 B=3.4 D_u=D_v=0.002, implicit Euler dt=0.01 x "
+                    f"{steps} steps, NK + FGMRES(40) + coupled-block multigrid V(2,2) (FP32, with FP32 Jacobian "
+                    "products and one-pass classical Gram-Schmidt; FP64 residual, updates and Arnoldi "
+                    "coefficients), rtol 1e-6 per step; initial "
+                    "u = 1 + 0.01 N(0,1), v = 3.4 + 0.01 N(0,1) (numpy PCG64, seed 20261203)",
+        "unknowns": N, "steps": steps,
+        "mixed_s": mixed["s"], "fp64_s": fp64["s"], "ratio": fp64["s"] / mixed["s"],
+        "ms_per_step_mixed": mixed["s"] / steps * 1e3,
+        "rel_err_mixed_vs_fp64": float(np.linalg.norm(mixed["x"] - fp64["x"]) / np.linalg.norm(fp64["x"])),
+        "all_converged": all(r["converged"] == 1 for r in mixed["res"] + fp64["res"] + res_h),
+        "not_converged": [[leg, k, r["iters"], r["res"] / r["res0"] if r["res0"] else 0.0]
+                          for leg, rs in (("mixed", mixed["res"]), ("fp64", fp64["res"]), ("host", res_h))
+                          for k, r in enumerate(rs) if r["converged"] != 1],
+        "counts_mixed": {k: agg(mixed["res"], k) for k in ("iters", "n_JVP", "n_lin_iters", "n_prec")},
+        "counts_fp64": {k: agg(fp64["res"], k) for k in ("iters", "n_JVP", "n_lin_iters", "n_prec")},
+        "e2e": {"value": e2e, "unit": "s", "h2d_bytes": N * 8, "d2h_bytes": N * 8,
+                "api": "numa_gpu_brusselator2d_advance_host, pinned host buffers"},
+        "cpu_baseline": {"value": t_cpu * scale, "unit": "s", "cores": cores, "kind": "port",
+                         "sample": f"one NK step at {ns}^2 (FP64 multigrid), {t_cpu:.3f} s, scaled by "
+                                   f"{n}^2/{ns}^2 x {steps} steps = {scale:.0f}; counts "
+                                   f"{rcpu['iters']}/{rcpu['n_JVP']}/{rcpu['n_prec']}"},
+        "note": "no reference implementation of this configuration exists (the reference's Brusselator is 1D): "
+                "the oracle is this project's CPU restatement",
+    }
 
 
 def learned_summary(learned, fp64_sec, x_fp64):
@@ -489,6 +574,16 @@ def run_kernel_case(G, ctx, args) -> int:
         for _ in range(max(1, args.steps)):
             G.diag_conv3d(ctx, nc, xin, w)
         print(json.dumps({"kernel_case": "conv", "n": nc, "launches": ctx.kernel_launches()}))
+        return 0
+    if args.kernel_case == "bruss":
+        # implicit-Euler steps of the 2D Brusselator at n^2 (FP32 coupled multigrid inside FGMRES(40))
+        op = G.Brusselator2D(ctx, n, G.brusselator_params())
+        pc = G.Provider.brusselator_mg(op, G.FP32)
+        x = ctx.from_numpy(G.brusselator2d_initial(n))
+        op.advance(x, max(1, args.steps), "nk", G.default_params(rtol_nl=1e-6, gmres_restart=40, gmres_max_iters=400,
+                                                                  flexible=1, jvp_precision=G.FP32, orth=G.CGS1), pc)
+        ctx.sync()
+        print(json.dumps({"kernel_case": "bruss", "n": n, "launches": ctx.kernel_launches()}))
         return 0
     if args.kernel_case == "vcycle":
         for prec in (G.FP64, G.FP32):

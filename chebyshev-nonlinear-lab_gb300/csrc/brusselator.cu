@@ -106,19 +106,24 @@ __global__ void __launch_bounds__(256) k_b1_block_apply(const double* __restrict
 // ============================================================================== Brusselator2D
 struct B2Geom {
     int n;
-    double h2inv, invdt, A, B, Du, Dv;
+    double invdt, A, B, Bp1, c1, duh, dvh;  // 1/dt, A, B, B + 1, 1/dt + (B + 1), D_u h^-2, D_v h^-2
 };
 
+// ((W - c) + (E - c)) + ((S - c) + (N - c)) on the periodic grid: for a smooth state every
+// difference of neighbours is exact, so F keeps no rounding floor of order eps * D h^-2 (the form
+// Sum - 4c would cancel values near 1 before the multiplication by D h^-2).
 __device__ __forceinline__ double lap5(const double* __restrict__ a, int n, int i, int j, double c) {
     const int jm = j == 0 ? n - 1 : j - 1, jp = j + 1 == n ? 0 : j + 1;
     const int im = i == 0 ? n - 1 : i - 1, ip = i + 1 == n ? 0 : i + 1;
     const size_t r = (size_t)i * n;
-    return (((a[r + jm] + a[r + jp]) + a[(size_t)im * n + j]) + a[(size_t)ip * n + j]) - 4.0 * c;
+    return ((a[r + jm] - c) + (a[r + jp] - c)) + ((a[(size_t)im * n + j] - c) + (a[(size_t)ip * n + j] - c));
 }
 
-// F(w) = (w - w_prev)/dt - D Lap_h w - reaction, the reference's 1D expressions on the periodic
-// 5-point stencil; optionally ||F||.  Blocks of 32 x 8 stride over rows, so the grid has at
-// most kMaxRedBlocks blocks.
+// F(w) = (w - w_prev)/dt - diag(D_u, D_v) h^-2 L w - reaction, as FMA chains (25 FP64
+// instructions a point: the kernel is bound by the FP64 pipe, not by HBM):
+//   F_u = fma(B+1, u, fma(-u^2, v, fma(-D_u h^-2, L u, fma(u - u_prev, 1/dt, -A))))
+//   F_v = fma(u^2, v, fma(-B, u, fma(-D_v h^-2, L v, (v - v_prev) / dt)));
+// optionally ||F||.  Blocks of 32 x 8 stride over rows, so the grid has at most kMaxRedBlocks blocks.
 template <bool NORM>
 __global__ void __launch_bounds__(256) k_b2_eval(const double* __restrict__ w, const double* __restrict__ prev,
                                                  double* __restrict__ out, B2Geom G, RedArgs red, double* norm_out) {
@@ -131,11 +136,11 @@ __global__ void __launch_bounds__(256) k_b2_eval(const double* __restrict__ w, c
     if (j < n) {
         for (int i = blockIdx.y * 8 + threadIdx.y; i < n; i += gridDim.y * 8) {
             const size_t p = (size_t)i * n + j;
-            const double u = wu[p], v = wv[p];
-            const double lu = lap5(wu, n, i, j, u) * G.h2inv;
-            const double lv = lap5(wv, n, i, j, v) * G.h2inv;
-            const double fu = (u - prev[p]) * G.invdt - G.Du * lu - G.A - u * u * v + (G.B + 1.0) * u;
-            const double fv = (v - prev[nn + p]) * G.invdt - G.Dv * lv - G.B * u + u * u * v;
+            const double u = wu[p], v = wv[p], uu = u * u;
+            const double lu = lap5(wu, n, i, j, u), lv = lap5(wv, n, i, j, v);
+            const double fu =
+                __fma_rn(G.Bp1, u, __fma_rn(-uu, v, __fma_rn(-G.duh, lu, __fma_rn(u - prev[p], G.invdt, -G.A))));
+            const double fv = __fma_rn(uu, v, __fma_rn(-G.B, u, __fma_rn(-G.dvh, lv, (v - prev[nn + p]) * G.invdt)));
             out[p] = fu;
             out[nn + p] = fv;
             if (NORM) acc[0] = __fma_rn(fv, fv, __fma_rn(fu, fu, acc[0]));
@@ -148,6 +153,8 @@ __global__ void __launch_bounds__(256) k_b2_eval(const double* __restrict__ w, c
     }
 }
 
+// J d with the point block [[c1 - 2uv, -u^2], [2uv - B, 1/dt + u^2]]:
+//   (J d)_u = fma(-u^2, dv, fma(-D_u h^-2, L du, a11 du)),  (J d)_v = fma(a22, dv, fma(a21, du, -D_v h^-2 L dv)).
 __global__ void __launch_bounds__(256) k_b2_jvp(const double* __restrict__ w, const double* __restrict__ d,
                                                 double* __restrict__ out, B2Geom G) {
     const int n = G.n;
@@ -157,11 +164,58 @@ __global__ void __launch_bounds__(256) k_b2_jvp(const double* __restrict__ w, co
     for (int i = blockIdx.y * 8 + threadIdx.y; i < n; i += gridDim.y * 8) {
         const size_t p = (size_t)i * n + j;
         const double u = w[p], v = w[nn + p], du = d[p], dv = d[nn + p];
-        const double ldu = lap5(d, n, i, j, du) * G.h2inv;
-        const double ldv = lap5(d + nn, n, i, j, dv) * G.h2inv;
-        out[p] = G.invdt * du - G.Du * ldu - (2.0 * u * v) * du - u * u * dv + (G.B + 1.0) * du;
-        out[nn + p] = G.invdt * dv - G.Dv * ldv - G.B * du + (2.0 * u * v) * du + u * u * dv;
+        const double lu = lap5(d, n, i, j, du), lv = lap5(d + nn, n, i, j, dv);
+        const double u2 = 2.0 * u, uu = u * u;
+        const double a11 = __fma_rn(-u2, v, G.c1), a21 = __fma_rn(u2, v, -G.B), a22 = G.invdt + uu;
+        out[p] = __fma_rn(-uu, dv, __fma_rn(-G.duh, lu, a11 * du));
+        out[nn + p] = __fma_rn(a22, dv, __fma_rn(a21, du, -G.dvh * lv));
     }
+}
+
+// The FP32 Jacobian product's coefficients at the iterate: (2uv, u^2) per point.
+__global__ void __launch_bounds__(256) k_b2_coef32(const double* __restrict__ w, size_t nn, float2* __restrict__ c) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nn) return;
+    const double u = w[p], v = w[nn + p];
+    c[p] = make_float2(f64_to_f32((2.0 * u) * v), f64_to_f32(u * u));
+}
+
+struct B2Geom32 {
+    int n;
+    float invdt, B, c1, duh, dvh;
+};
+
+// J d in FP32 arithmetic (FP64 in and out): a 32 x 8 tile of both components with its one-point
+// periodic halo is rounded to FP32 once per point (integer-pipe conversion) into shared memory.
+__global__ void __launch_bounds__(256) k_b2_jvp32(const float2* __restrict__ coef, const double* __restrict__ d,
+                                                  double* __restrict__ out, B2Geom32 G) {
+    constexpr int TX = 32, TY = 8;
+    __shared__ float tu[TY + 2][TX + 3], tv[TY + 2][TX + 3];
+    const int n = G.n;
+    const size_t nn = (size_t)n * n;
+    const int i0 = blockIdx.y * TY, j0 = blockIdx.x * TX;
+    const int tid = threadIdx.y * TX + threadIdx.x;
+    for (int idx = tid; idx < (TY + 2) * (TX + 2); idx += TX * TY) {
+        const int a = idx / (TX + 2), b = idx - a * (TX + 2);
+        const int gi = (i0 - 1 + a + n) % n, gj = (j0 - 1 + b + n) % n;
+        const size_t q = (size_t)gi * n + gj;
+        tu[a][b] = f64_to_f32(d[q]);
+        tv[a][b] = f64_to_f32(d[nn + q]);
+    }
+    __syncthreads();
+    const int i = i0 + threadIdx.y, j = j0 + threadIdx.x;
+    if (i >= n || j >= n) return;
+    const int a = threadIdx.y + 1, b = threadIdx.x + 1;
+    const float du = tu[a][b], dv = tv[a][b];
+    const float lu = ((tu[a][b - 1] - du) + (tu[a][b + 1] - du)) + ((tu[a - 1][b] - du) + (tu[a + 1][b] - du));
+    const float lv = ((tv[a][b - 1] - dv) + (tv[a][b + 1] - dv)) + ((tv[a - 1][b] - dv) + (tv[a + 1][b] - dv));
+    const size_t p = (size_t)i * n + j;
+    const float2 c = coef[p];
+    const float a11 = G.c1 - c.x, a21 = c.x - G.B, a22 = G.invdt + c.y;
+    const float ou = __fmaf_rn(-c.y, dv, __fmaf_rn(-G.duh, lu, a11 * du));
+    const float ov = __fmaf_rn(a22, dv, __fmaf_rn(a21, du, -G.dvh * lv));
+    out[p] = f32_to_f64(ou);
+    out[nn + p] = f32_to_f64(ov);
 }
 
 dim3 b2_grid(int n) {
@@ -290,9 +344,30 @@ __global__ void __launch_bounds__(256) k_bmg_pass(T* __restrict__ X, T* __restri
     }
 }
 
-// Residual r = b - (K x - diag(s) (S - 4x)) on the finest-level points that a 16 x 16 tile of
-// coarse points covers (33 x 33, periodic), kept in shared memory, then 9-point full weighting
-// ((4c + 2((W + E) + (S + N))) + (((SW + SE) + NW) + NE)) / 16 into the coarse right-hand side.
+// Residual r = b - (K x - diag(s) (S - 4x)) of one level at point (i, j).
+template <class T>
+__device__ __forceinline__ void resid_at(const T* X, const T* Bv, const T* __restrict__ K, int n, int i, int j, T su,
+                                         T sv, T& ru, T& rv) {
+    const size_t p = (size_t)i * n + j;
+    const auto x = ld2(X, p);
+    const auto bb = ld2(Bv, p);
+    const Blk<T> k = load_blk(K, p);
+    T Su, Sv;
+    nbr_sums(X, n, i, j, Su, Sv);
+    ru = bb.x - ((k.k11 * x.x + k.k12 * x.y) + su * (T(4) * x.x - Su));
+    rv = bb.y - ((k.k21 * x.x + k.k22 * x.y) + sv * (T(4) * x.y - Sv));
+}
+
+// 9-point full weighting ((4c + 2((W + E) + (S + N))) + (((SW + SE) + NW) + NE)) / 16; S is row i-1.
+template <class T>
+__device__ __forceinline__ T fw9(T c, T w, T e, T s, T n, T sw, T se, T nw, T ne) {
+    const T edge = (w + e) + (s + n);
+    const T corner = ((sw + se) + nw) + ne;
+    return ((T(4) * c + T(2) * edge) + corner) * T(0.0625);
+}
+
+// Residual of the finest-level points that a 16 x 16 tile of coarse points covers (33 x 33,
+// periodic), kept in shared memory, then full weighting into the coarse right-hand side.
 template <class T>
 __global__ void __launch_bounds__(256) k_bmg_restrict(const T* __restrict__ X, const T* __restrict__ Bv,
                                                       const T* __restrict__ K, LvlArgs L, T* __restrict__ Bc) {
@@ -305,35 +380,22 @@ __global__ void __launch_bounds__(256) k_bmg_restrict(const T* __restrict__ X, c
     for (int idx = tid; idx < FS * FS; idx += TS * TS) {
         const int a = idx / FS, b = idx - a * FS;
         const int fi = (2 * I0 - 1 + a + nf) % nf, fj = (2 * J0 - 1 + b + nf) % nf;
-        const size_t p = (size_t)fi * nf + fj;
-        const auto x = ld2(X, p);
-        const auto bb = ld2(Bv, p);
-        const Blk<T> k = load_blk(K, p);
-        T Su, Sv;
-        nbr_sums(X, nf, fi, fj, Su, Sv);
-        su_s[a][b] = bb.x - ((k.k11 * x.x + k.k12 * x.y) + su * (T(4) * x.x - Su));
-        sv_s[a][b] = bb.y - ((k.k21 * x.x + k.k22 * x.y) + sv * (T(4) * x.y - Sv));
+        resid_at(X, Bv, K, nf, fi, fj, su, sv, su_s[a][b], sv_s[a][b]);
     }
     __syncthreads();
     const int I = I0 + threadIdx.y, J = J0 + threadIdx.x;
     if (I >= nc || J >= nc) return;
     const int a = 2 * threadIdx.y + 1, b = 2 * threadIdx.x + 1;
     auto fw = [a, b](const T (*f)[FS + 1]) {
-        const T ctr = f[a][b];
-        const T edge = (f[a][b - 1] + f[a][b + 1]) + (f[a - 1][b] + f[a + 1][b]);
-        const T corner = ((f[a - 1][b - 1] + f[a - 1][b + 1]) + f[a + 1][b - 1]) + f[a + 1][b + 1];
-        return ((T(4) * ctr + T(2) * edge) + corner) * T(0.0625);
+        return fw9(f[a][b], f[a][b - 1], f[a][b + 1], f[a - 1][b], f[a + 1][b], f[a - 1][b - 1], f[a - 1][b + 1],
+                   f[a + 1][b - 1], f[a + 1][b + 1]);
     };
     st2(Bc, (size_t)I * nc + J, fw(su_s), fw(sv_s));
 }
 
-// x_fine += bilinear periodic interpolation of x_coarse; thread per coarse point (I, J) owns
-// fine (2I + {0,1}, 2J + {0,1}).
+// x_fine += bilinear periodic interpolation of x_coarse at the fine points (2I + {0,1}, 2J + {0,1}).
 template <class T>
-__global__ void __launch_bounds__(256) k_bmg_prolong(const T* __restrict__ Xc, int nc, T* __restrict__ Xf) {
-    const int J = blockIdx.x * 32 + threadIdx.x;
-    const int I = blockIdx.y * 8 + threadIdx.y;
-    if (I >= nc || J >= nc) return;
+__device__ __forceinline__ void prolong_point(const T* Xc, int nc, int I, int J, T* Xf) {
     const int I1 = I + 1 == nc ? 0 : I + 1, J1 = J + 1 == nc ? 0 : J + 1;
     const auto c00 = ld2(Xc, (size_t)I * nc + J), c10 = ld2(Xc, (size_t)I1 * nc + J);
     const auto c01 = ld2(Xc, (size_t)I * nc + J1), c11 = ld2(Xc, (size_t)I1 * nc + J1);
@@ -347,6 +409,14 @@ __global__ void __launch_bounds__(256) k_bmg_prolong(const T* __restrict__ Xc, i
     add(f10, T(0.5) * (c00.x + c10.x), T(0.5) * (c00.y + c10.y));
     add(f00 + 1, T(0.5) * (c00.x + c01.x), T(0.5) * (c00.y + c01.y));
     add(f10 + 1, T(0.25) * (((c00.x + c10.x) + c01.x) + c11.x), T(0.25) * (((c00.y + c10.y) + c01.y) + c11.y));
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_bmg_prolong(const T* __restrict__ Xc, int nc, T* __restrict__ Xf) {
+    const int J = blockIdx.x * 32 + threadIdx.x;
+    const int I = blockIdx.y * 8 + threadIdx.y;
+    if (I >= nc || J >= nc) return;
+    prolong_point(Xc, nc, I, J, Xf);
 }
 
 // The coarsest level in one block: x = 0, then `sweeps` red-black sweeps (colour 0, 1).
@@ -374,18 +444,183 @@ __global__ void __launch_bounds__(1024) k_bmg_coarsest(T* __restrict__ X, const 
     }
 }
 
-// K at the finest level from the FP64 state: [[1/dt + B + 1 - 2uv, -u^2], [2uv - B, 1/dt + u^2]].
+// Levels with n <= 64 below a finer level, as one block: every tail level's pairs x and b live in
+// shared memory (blocks K are read through L1), and the block runs their whole V-cycle — the same
+// per-point arithmetic as the level kernels, so the result is the same to the bit.  desc[k]
+// describes tail level k (k = 0 the finest of them): its n, the offset of its x in the shared
+// buffer (b follows at offset + 2 n^2), s_u, s_v and its blocks.
+struct TailLvl {
+    int n, off;
+    double su, sv;
+    const void* K;
+};
+
+template <class T>
+__global__ void __launch_bounds__(512, 1) k_bmg_tail(const TailLvl* __restrict__ desc, int count, int pre, int post,
+                                                     int sweeps, const T* __restrict__ Bin, T* __restrict__ Xout) {
+    extern __shared__ __align__(16) unsigned char bmg_smem[];
+    T* base = reinterpret_cast<T*>(bmg_smem);
+    // Levels with n <= 8 (at most 32 points of a colour) are run by warp 0 alone, separated by
+    // __syncwarp instead of block barriers; `kw` is the first of them (count if none).
+    int kw = count;
+    for (int k = 0; k < count; ++k)
+        if (desc[k].n <= 8) {
+            kw = k;
+            break;
+        }
+    const bool warp0 = threadIdx.x < 32;
+    // one colour pass of level k by threads [0, nt); then the barrier of that group
+    auto pass = [&](int k, int colour, bool first) {
+        const bool small = k >= kw;
+        const int tid = threadIdx.x, nt = small ? 32 : blockDim.x;
+        const TailLvl L = desc[k];
+        const int n = L.n, half = n / 2;
+        T* X = base + L.off;
+        const T* Bv = X + 2 * n * n;
+        const T* K = static_cast<const T*>(L.K);
+        const T su = (T)L.su, sv = (T)L.sv, su4 = (T)(4.0 * L.su), sv4 = (T)(4.0 * L.sv);
+        for (int idx = tid; idx < n * half; idx += nt) {
+            const int i = idx / half, jj = idx - i * half;
+            const int j = 2 * jj + ((i + colour) & 1), jo = 2 * jj + 1 - ((i + colour) & 1);
+            const size_t p = (size_t)i * n + j;
+            const auto b = ld2(Bv, p);
+            T Su = T(0), Sv = T(0), u, v;
+            if (!first) nbr_sums(X, n, i, j, Su, Sv);
+            block_update(load_blk(K, p), su, sv, su4, sv4, b.x, b.y, Su, Sv, u, v);
+            st2(X, p, u, v);
+            if (first) st2(X, (size_t)i * n + jo, T(0), T(0));
+        }
+        if (small) __syncwarp();
+        else __syncthreads();
+    };
+    // residual of level k, full-weighted into the right-hand side of level k + 1
+    auto restrict_to = [&](int k) {
+        const bool small = k + 1 >= kw && k >= kw;
+        const int tid = threadIdx.x, nt = small ? 32 : blockDim.x;
+        const TailLvl L = desc[k], C = desc[k + 1];
+        const int nf = L.n, nc = C.n;
+        const T* X = base + L.off;
+        const T* Bv = X + 2 * nf * nf;
+        const T* K = static_cast<const T*>(L.K);
+        T* Bc = base + C.off + 2 * nc * nc;
+        const T su = (T)L.su, sv = (T)L.sv;
+        for (int idx = tid; idx < nc * nc; idx += nt) {
+            const int I = idx / nc, J = idx - I * nc;
+            const int i = 2 * I, j = 2 * J;
+            const int im = i == 0 ? nf - 1 : i - 1, ip = i + 1, jm = j == 0 ? nf - 1 : j - 1, jp = j + 1;
+            // fw9's sums in its order, accumulated as the residuals are formed (fewer live registers)
+            T cu, cv, au, av, bu, bv;
+            resid_at(X, Bv, K, nf, i, j, su, sv, cu, cv);
+            resid_at(X, Bv, K, nf, i, jm, su, sv, au, av);
+            resid_at(X, Bv, K, nf, i, jp, su, sv, bu, bv);
+            const T weu = au + bu, wev = av + bv;
+            resid_at(X, Bv, K, nf, im, j, su, sv, au, av);
+            resid_at(X, Bv, K, nf, ip, j, su, sv, bu, bv);
+            const T edgeu = weu + (au + bu), edgev = wev + (av + bv);
+            resid_at(X, Bv, K, nf, im, jm, su, sv, au, av);
+            resid_at(X, Bv, K, nf, im, jp, su, sv, bu, bv);
+            T coru = au + bu, corv = av + bv;
+            resid_at(X, Bv, K, nf, ip, jm, su, sv, au, av);
+            coru = coru + au;
+            corv = corv + av;
+            resid_at(X, Bv, K, nf, ip, jp, su, sv, au, av);
+            coru = coru + au;
+            corv = corv + av;
+            st2(Bc, (size_t)idx, ((T(4) * cu + T(2) * edgeu) + coru) * T(0.0625),
+                ((T(4) * cv + T(2) * edgev) + corv) * T(0.0625));
+        }
+        if (small) __syncwarp();
+        else __syncthreads();
+    };
+    auto prolong_from = [&](int k) {  // level k + 1 into level k
+        const bool small = k >= kw;
+        const int tid = threadIdx.x, nt = small ? 32 : blockDim.x;
+        const int nc = desc[k + 1].n;
+        const T* Xc = base + desc[k + 1].off;
+        T* Xf = base + desc[k].off;
+        for (int idx = tid; idx < nc * nc; idx += nt) prolong_point(Xc, nc, idx / nc, idx % nc, Xf);
+        if (small) __syncwarp();
+        else __syncthreads();
+    };
+    auto down = [&](int k) {
+        pass(k, 0, true);
+        pass(k, 1, false);
+        for (int s = 1; s < pre; ++s) {
+            pass(k, 0, false);
+            pass(k, 1, false);
+        }
+        restrict_to(k);
+    };
+    auto up = [&](int k) {
+        prolong_from(k);
+        for (int s = 0; s < post; ++s) {
+            pass(k, 1, false);
+            pass(k, 0, false);
+        }
+    };
+    auto coarsest = [&]() {
+        const int kc = count - 1, n = desc[kc].n;
+        const bool small = kc >= kw;
+        const int tid = threadIdx.x, nt = small ? 32 : blockDim.x;
+        T* X = base + desc[kc].off;
+        for (int q = tid; q < 2 * n * n; q += nt) X[q] = T(0);
+        if (small) __syncwarp();
+        else __syncthreads();
+        for (int s = 0; s < sweeps; ++s) {
+            pass(kc, 0, false);
+            pass(kc, 1, false);
+        }
+    };
+    {
+        const int n0 = desc[0].n;
+        T* B0 = base + desc[0].off + 2 * n0 * n0;
+        for (int q = threadIdx.x; q < 2 * n0 * n0; q += blockDim.x) B0[q] = Bin[q];
+    }
+    __syncthreads();
+    // block-wide levels down to kw (restricting into kw last)
+    for (int k = 0; k + 1 < count && k < kw; ++k) down(k);
+    if (kw < count) {
+        // the warp-sized levels: the rest of the V-cycle from level kw down and back up, warp 0 only
+        if (warp0) {
+            for (int k = kw; k + 1 < count; ++k) down(k);
+            coarsest();
+            for (int k = count - 2; k >= kw; --k) up(k);
+        }
+        __syncthreads();
+    } else {
+        coarsest();
+    }
+    for (int k = (kw < count - 1 ? kw : count - 1) - 1; k >= 0; --k) up(k);
+    const int n0 = desc[0].n;
+    const T* X0 = base + desc[0].off;
+    for (int q = threadIdx.x; q < 2 * n0 * n0; q += blockDim.x) Xout[q] = X0[q];
+}
+
+// K at the finest level from the FP64 state: [[1/dt + B + 1 - 2uv, -u^2], [2uv - B, 1/dt + u^2]];
+// in FP64 for the FP64 multigrid, in FP32 from the rounded state for the FP32 one (a preconditioner
+// needs no more, and FP64 arithmetic would bound the kernel).
+__device__ __forceinline__ void kfine_point(double u, double v, double c1, double c2, double B, Blk<double>& k) {
+    k.k11 = c1 - (2.0 * u) * v;
+    k.k12 = -(u * u);
+    k.k21 = (2.0 * u) * v - B;
+    k.k22 = c2 + u * u;
+}
+__device__ __forceinline__ void kfine_point(double u, double v, double c1, double c2, double B, Blk<float>& k) {
+    const float u32 = f64_to_f32(u), v32 = f64_to_f32(v);
+    const float uv2 = (2.0f * u32) * v32, uu = u32 * u32;
+    k.k11 = (float)c1 - uv2;
+    k.k12 = -uu;
+    k.k21 = uv2 - (float)B;
+    k.k22 = (float)c2 + uu;
+}
+
 template <class T>
 __global__ void __launch_bounds__(256) k_bmg_kfine(const double* __restrict__ w, size_t nn, double c1, double c2,
                                                    double B, T* __restrict__ K) {
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nn) return;
-    const double u = w[p], v = w[nn + p];
     Blk<T> k;
-    k.k11 = (T)(c1 - (2.0 * u) * v);
-    k.k12 = (T)(-(u * u));
-    k.k21 = (T)((2.0 * u) * v - B);
-    k.k22 = (T)(c2 + u * u);
+    kfine_point(w[p], w[nn + p], c1, c2, B, k);
     store_blk(K, p, k);
 }
 
@@ -432,6 +667,7 @@ __global__ void k_bmg_out(const T* __restrict__ X, size_t nn, double* __restrict
 
 constexpr int kBmgCoarsestSweeps = 30;
 constexpr int kBmgOneBlockPoints = 4096;
+constexpr int kBmgTailMaxN = 64;  // levels this small (below the finest) run in the one-block tail
 
 }  // namespace
 
@@ -531,12 +767,14 @@ Brusselator2D::Brusselator2D(Context& ctx, size_t n, const numa_brusselator2d_pa
 static B2Geom b2_geom(size_t n, const numa_brusselator2d_params& P) {
     B2Geom G;
     G.n = (int)n;
-    G.h2inv = static_cast<double>(n) * static_cast<double>(n);
+    const double h2inv = static_cast<double>(n) * static_cast<double>(n);
     G.invdt = 1.0 / P.dt;
     G.A = P.A;
     G.B = P.B;
-    G.Du = P.Du;
-    G.Dv = P.Dv;
+    G.Bp1 = P.B + 1.0;
+    G.c1 = G.invdt + (P.B + 1.0);
+    G.duh = P.Du * h2inv;
+    G.dvh = P.Dv * h2inv;
     return G;
 }
 
@@ -550,6 +788,32 @@ void Brusselator2D::eval(const double* x, double* out, double*, double* norm_out
         k_b2_eval<false><<<grid, dim3(32, 8), 0, ctx_.stream>>>(x, prev_.p, out, b2_geom(n_, P_), ctx_.red, nullptr);
     ctx_.count_launch();
     ctx_.check_launch("Brusselator2D eval");
+}
+
+void Brusselator2D::bind(const double* x, const double*, int precision) {
+    bound_x_ = x;
+    bound_precision_ = precision;
+    if (precision == NUMA_GPU_FP32) {
+        const size_t nn = n_ * n_;
+        coef32_.resize(nn);  // one float2 per point
+        k_b2_coef32<<<(unsigned)((nn + 255) / 256), 256, 0, ctx_.stream>>>(x, nn,
+                                                                          reinterpret_cast<float2*>(coef32_.p));
+        ctx_.count_launch();
+        ctx_.check_launch("Brusselator2D bind");
+    }
+}
+
+void Brusselator2D::jvp_bound(const double* v, double* out) {
+    if (bound_precision_ != NUMA_GPU_FP32) {
+        jvp_at(bound_x_, v, out);
+        return;
+    }
+    const B2Geom G = b2_geom(n_, P_);
+    const B2Geom32 G32{(int)n_, (float)G.invdt, (float)G.B, (float)G.c1, (float)G.duh, (float)G.dvh};
+    const dim3 grid((unsigned)((n_ + 31) / 32), (unsigned)((n_ + 7) / 8));
+    k_b2_jvp32<<<grid, dim3(32, 8), 0, ctx_.stream>>>(reinterpret_cast<const float2*>(coef32_.p), v, out, G32);
+    ctx_.count_launch();
+    ctx_.check_launch("Brusselator2D jvp32");
 }
 
 void Brusselator2D::jvp_at(const double* x, const double* v, double* out) {
@@ -595,6 +859,34 @@ BrussMG2D::BrussMG2D(Context& ctx, size_t n, const numa_brusselator2d_params& p,
         levels_.push_back(std::move(L));
         if (m % 4 != 0 || m / 2 < 4) break;
         m /= 2;
+    }
+    // levels below the finest with n <= 64 run as one block (at most 4 (64^2 + 32^2 + ...) values,
+    // 175 KB of shared memory in FP64)
+    for (size_t l = 1; l < levels_.size(); ++l)
+        if (levels_[l]->n <= kBmgTailMaxN) {
+            tail_first_ = (int)l;
+            break;
+        }
+    if (tail_first_ > 0) {
+        std::vector<TailLvl> d;
+        size_t off = 0;
+        for (size_t l = (size_t)tail_first_; l < levels_.size(); ++l) {
+            const Level& L = *levels_[l];
+            d.push_back(TailLvl{L.n, (int)off, L.su, L.sv, L.k.p});
+            off += 4 * (size_t)L.n * L.n;
+        }
+        tail_count_ = (int)d.size();
+        tail_smem_ = off * esz;
+        tail_desc_.resize((d.size() * sizeof(TailLvl) + 7) / 8);
+        NUMA_CUDA(cudaMemcpyAsync(tail_desc_.p, d.data(), d.size() * sizeof(TailLvl), cudaMemcpyHostToDevice,
+                                  ctx_.stream));
+        ctx_.sync();
+        if (precision == NUMA_GPU_FP64)
+            NUMA_CUDA(cudaFuncSetAttribute(k_bmg_tail<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)tail_smem_));
+        else
+            NUMA_CUDA(cudaFuncSetAttribute(k_bmg_tail<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)tail_smem_));
     }
 }
 
@@ -644,6 +936,12 @@ void BrussMG2D::cycle(size_t l) {
     const dim3 blk(32, 8);
     const dim3 pgrid((unsigned)((n / 2 + 31) / 32), (unsigned)((n + 7) / 8));
     const size_t nn = (size_t)n * n;
+    if ((int)l == tail_first_) {
+        k_bmg_tail<T><<<1, 512, tail_smem_, s>>>(reinterpret_cast<const TailLvl*>(tail_desc_.p), tail_count_, pre_,
+                                                  post_, kBmgCoarsestSweeps, Bv, X);
+        ctx_.count_launch();
+        return;
+    }
     if (coarsest) {
         if (finest) {
             k_bmg_in<T><<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(r0_, nn, Bv);

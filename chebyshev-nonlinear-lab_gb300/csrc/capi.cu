@@ -209,7 +209,20 @@ void op_derivative(NonlinearOp& f, bool second, const double* x, const double* v
         c.sync();
         return;
     }
-    need(mode == NUMA_GPU_DERIV_ANALYTIC, NUMA_GPU_ERR_INVALID_ARGUMENT, "unknown derivative mode");
+    need(mode == NUMA_GPU_DERIV_ANALYTIC || (mode == NUMA_GPU_DERIV_ANALYTIC_FP32 && !second),
+         NUMA_GPU_ERR_INVALID_ARGUMENT, "unknown derivative mode");
+    if (mode == NUMA_GPU_DERIV_ANALYTIC_FP32) {
+        // the product the drivers use with jvp_precision = FP32 (FP64 where an operator has no FP32 form)
+        f.prepare_cache(NUMA_GPU_FP32);  // before sizing: the FP32 form may keep more in the cache
+        DeviceArray<double> cache(f.cache_size());
+        DeviceArray<double> tmp(f.cache_size() ? N : 0);
+        if (f.cache_size()) f.eval(x, tmp.p, cache.p, nullptr);
+        f.bind(x, cache.p, NUMA_GPU_FP32);
+        f.jvp_bound(v, out);
+        f.prepare_cache(NUMA_GPU_FP64);
+        c.sync();
+        return;
+    }
     if (!second) {
         f.jvp_at(x, v, out);
         return;

@@ -205,16 +205,18 @@ public:
     void set_previous(const double* w);
     size_t cache_size() const override { return 0; }
     void eval(const double* x, double* out, double* cache, double* norm_out) override;
-    void bind(const double* x, const double*, int) override { bound_x_ = x; }
-    void jvp_bound(const double* v, double* out) override { jvp_at(bound_x_, v, out); }
+    // FP32 binding: the coefficients (2uv, u^2) of the iterate in FP32; products in FP32 arithmetic
+    void bind(const double* x, const double*, int precision) override;
+    void jvp_bound(const double* v, double* out) override;
     void jvp_at(const double* x, const double* v, double* out) override;
     void d2(const double* x, const double* cache, const double* v, double* out) override;
 
 private:
     size_t n_;
     numa_brusselator2d_params P_;
-    DeviceArray<double> prev_;
+    DeviceArray<double> prev_, coef32_;
     const double* bound_x_ = nullptr;
+    int bound_precision_ = NUMA_GPU_FP64;
 };
 
 // Periodic geometric multigrid V(pre, post) for the coupled 2x2-block Jacobian of Brusselator2D,
@@ -246,6 +248,10 @@ private:
     double* z0_ = nullptr;
     cudaGraphExec_t coarse_exec_ = nullptr;
     uint64_t coarse_kernels_ = 0;
+    int tail_first_ = -1;          // first level of the one-block tail (-1: none)
+    int tail_count_ = 0;
+    size_t tail_smem_ = 0;         // its shared memory in bytes
+    DeviceArray<double> tail_desc_;  // its level descriptors
 };
 
 // ------------------------------------------------------------------------------ PoissonMG

@@ -54,7 +54,8 @@ typedef enum numa_gpu_precision {
 typedef enum numa_gpu_deriv_mode {
     NUMA_GPU_DERIV_ANALYTIC = 0,     /* Bratu3D::jvp / Bratu3D::d2 (problems/bratu3d.hpp:33-56) */
     NUMA_GPU_DERIV_FD = 1,           /* jvp_fd / d2_fd (operators/operator.hpp:100-134) */
-    NUMA_GPU_DERIV_ANALYTIC_FP32 = 2 /* extension, jvp only: the analytic product in FP32 arithmetic */
+    NUMA_GPU_DERIV_ANALYTIC_FP32 = 2 /* extension, jvp only: the analytic product in FP32 arithmetic
+                                        (Bratu3D, Brusselator2D; FP64 for operators without one) */
 } numa_gpu_deriv_mode;
 
 /* Arnoldi orthogonalisation. */

@@ -8,7 +8,8 @@ across machines), solves with counts within +-1 and solutions within 1e-12.
 The periodic 2D Brusselator and its coupled-block multigrid against the CPU restatement (no
 reference code exists for them: parity unpinned): F, J v, F'' and the FP64 V-cycle bit for bit,
 every driver's counts within +-1 and solution within 1e-12; the FP32 V-cycle within FP32 rounding
-of the FP64 one, and the mixed solve (FP32 multigrid inside FGMRES) within 1e-8 of the FP64 solve.
+of the FP64 one, and the mixed solve (FP32 multigrid and FP32 Jacobian products inside FGMRES)
+within 1e-8 of the FP64 solve.
 At the full 2048^2 size, size-independent properties: the steady state is a fixed point of the
 time stepping, and a periodic translation of the initial state by a multiple of the coarsest
 spacing translates the solution.
@@ -155,6 +156,8 @@ def test_bruss2d_pointwise_bit_exact(gpu, oracle, n):
     assert np.array_equal(out.numpy(), oracle.bruss2d_d2(n, PRM, prev, w, d))
     op.jvp(wv, dv, out, G.FD)
     assert rel_err(out.numpy(), oracle.bruss2d_jvp(n, PRM, prev, w, d, 1)) < 1e-8
+    op.jvp(wv, dv, out, G.ANALYTIC_FP32)  # the mixed path's product: FP32 arithmetic
+    assert rel_err(out.numpy(), oracle.bruss2d_jvp(n, PRM, prev, w, d)) < 1e-5
     op.d2(wv, dv, out, G.FD)
     assert rel_err(out.numpy(), oracle.bruss2d_d2(n, PRM, prev, w, d, 1)) < 1e-5
 
@@ -227,7 +230,7 @@ def test_bruss2d_mixed_and_advance(gpu, oracle):
     assert len(res) == steps and all(r["converged"] == 1 for r in res)
     assert rel_err(x.numpy(), xo) < 1e-12
     xm, resm = G.brusselator2d_advance_host(gpu, n, x0, steps, mg_precision=G.FP32,
-                                            kparams=G.default_params(flexible=1, **kp))
+                                            kparams=G.default_params(flexible=1, jvp_precision=G.FP32, **kp))
     assert all(r["converged"] == 1 for r in resm)
     assert rel_err(xm, xo) < 1e-8
     # the state moved (the homogeneous state is unstable for B > 1 + A^2)
@@ -241,7 +244,7 @@ def test_bruss2d_full_size_properties(gpu):
     G = _G()
     n = 2048
     nn = n * n
-    kp = G.default_params(rtol_nl=1e-10, gmres_restart=40, gmres_max_iters=400, flexible=1)
+    kp = G.default_params(rtol_nl=1e-10, gmres_restart=40, gmres_max_iters=400, flexible=1, jvp_precision=G.FP32)
     ss = np.concatenate([np.full(nn, 1.0), np.full(nn, 3.4)])
     xs, rs = G.brusselator2d_advance_host(gpu, n, ss, 2, kparams=kp)
     assert np.array_equal(xs, ss) and all(r["iters"] == 0 for r in rs)
