@@ -491,6 +491,23 @@ def brusselator_leg(G, ctx, stream, torch, n: int = 2048, steps: int = 20) -> di
     t0 = time.perf_counter()
     _, res_h = G.brusselator2d_advance_host(ctx, n, h_in, steps, prm, "nk", "mg", G.FP32, legs["mixed"][1], h_out)
     e2e = time.perf_counter() - t0
+    # roofline of the dominant multigrid kernel: one FP32 colour pass on the 2048^2 level; algorithmic
+    # bytes per grid point: the other colour's pairs (4), the own colour's right-hand side (4) and
+    # blocks (8) read, its pairs written (4)
+    mg = G.BrussMG2D(ctx, n, prm, G.FP32)
+    mg.set_state(x0d)
+    ms_pass = mg.time_pass(40)
+    pass_bytes = 20.0 * n * n
+    peaks = json.loads(PEAKS_FILE.read_text()) if PEAKS_FILE.exists() else {}
+    hbm_peak = float(peaks.get("hbm_gbs", FALLBACK_HBM_GBS))
+    prof = ROOT / "profiles" / "k_bmg_pass_fp32_2048.json"
+    traffic = json.loads(prof.read_text()).get("dram_bytes_per_launch") if prof.exists() else None
+    achieved = pass_bytes / (ms_pass * 1e-3) / 1e9
+    roofline = {"kernel": f"k_bmg_pass<float> colour pass, {n}^2", "bound": "hbm", "achieved": achieved,
+                "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                "ms_per_launch": ms_pass, "algorithmic_bytes": pass_bytes,
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback"}
+    mg.close()
     # one step at 512^2 on the host cores (the CPU restatement, FP64 multigrid, same parameters)
     from oracle.oracle_lib import Oracle, default_params as oparams
     o = Oracle()
@@ -526,6 +543,7 @@ def brusselator_leg(G, ctx, stream, torch, n: int = 2048, steps: int = 20) -> di
                          "sample": f"one NK step at {ns}^2 (FP64 multigrid), {t_cpu:.3f} s, scaled by "
                                    f"{n}^2/{ns}^2 x {steps} steps = {scale:.0f}; counts "
                                    f"{rcpu['iters']}/{rcpu['n_JVP']}/{rcpu['n_prec']}"},
+        "roofline": roofline,
         "note": "no reference implementation of this configuration exists (the reference's Brusselator is 1D): "
                 "the oracle is this project's CPU restatement",
     }

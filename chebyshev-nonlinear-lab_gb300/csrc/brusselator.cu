@@ -172,12 +172,12 @@ __global__ void __launch_bounds__(256) k_b2_jvp(const double* __restrict__ w, co
     }
 }
 
-// The FP32 Jacobian product's coefficients at the iterate: (2uv, u^2) per point.
+// The FP32 Jacobian product's coefficients at the iterate: (2uv, u^2) per point, in FP32 arithmetic.
 __global__ void __launch_bounds__(256) k_b2_coef32(const double* __restrict__ w, size_t nn, float2* __restrict__ c) {
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nn) return;
-    const double u = w[p], v = w[nn + p];
-    c[p] = make_float2(f64_to_f32((2.0 * u) * v), f64_to_f32(u * u));
+    const float u = f64_to_f32(w[p]), v = f64_to_f32(w[nn + p]);  // FP32 from the rounded state
+    c[p] = make_float2((2.0f * u) * v, u * u);
 }
 
 struct B2Geom32 {
@@ -244,6 +244,16 @@ __device__ __forceinline__ Blk<double> load_blk(const double* __restrict__ K, si
     const double2 b = __ldg(reinterpret_cast<const double2*>(K) + 2 * p + 1);
     return {a.x, a.y, b.x, b.y};
 }
+// the same from shared memory (no read-only-cache path)
+__device__ __forceinline__ Blk<float> load_blk_s(const float* K, size_t p) {
+    const float4 q = reinterpret_cast<const float4*>(K)[p];
+    return {q.x, q.y, q.z, q.w};
+}
+__device__ __forceinline__ Blk<double> load_blk_s(const double* K, size_t p) {
+    const double2 a = reinterpret_cast<const double2*>(K)[2 * p];
+    const double2 b = reinterpret_cast<const double2*>(K)[2 * p + 1];
+    return {a.x, a.y, b.x, b.y};
+}
 __device__ __forceinline__ void store_blk(float* K, size_t p, const Blk<float>& k) {
     reinterpret_cast<float4*>(K)[p] = make_float4(k.k11, k.k12, k.k21, k.k22);
 }
@@ -277,10 +287,21 @@ __device__ __forceinline__ void block_update(const Blk<T>& k, T su, T sv, T su4,
     v = (m11 * rv - k.k21 * ru) / det;
 }
 
+// One level's constants in the multigrid's precision, formed on the host: a kernel converting
+// doubles per thread would spend GB300's narrow FP64 pipe on it (a few FP64 instructions per
+// thread bound a one-point-per-thread FP32 pass).
+template <class T>
 struct LvlArgs {
     int n;
-    double su, sv;
+    T su, sv, su4, sv4;  // s_u = D_u h^-2, s_v, 4 s_u, 4 s_v
 };
+
+// FP64 <-> T without the FP64 pipe for T = float (integer-path conversions, same rounding).
+template <class T> __device__ __forceinline__ T from_f64(double x);
+template <> __device__ __forceinline__ float from_f64<float>(double x) { return f64_to_f32(x); }
+template <> __device__ __forceinline__ double from_f64<double>(double x) { return x; }
+__device__ __forceinline__ double to_f64(float x) { return f32_to_f64(x); }
+__device__ __forceinline__ double to_f64(double x) { return x; }
 
 template <class T>
 __device__ __forceinline__ void nbr_sums(const T* __restrict__ X, int n, int i, int j, T& Su, T& Sv) {
@@ -302,23 +323,23 @@ enum { kBPassNormal = 0, kBPassFirst = 1, kBPassLast = 2 };
 //  Last (finest level, colour 0, the cycle's final pass): also writes z (FP64 planes) for both points.
 template <class T, int MODE>
 __global__ void __launch_bounds__(256) k_bmg_pass(T* __restrict__ X, T* __restrict__ Bv, const T* __restrict__ K,
-                                                  LvlArgs L, int colour, const double* __restrict__ r64,
+                                                  LvlArgs<T> L, int colour, const double* __restrict__ r64,
                                                   double* __restrict__ z64) {
     const int n = L.n;
     const int jj = blockIdx.x * 32 + threadIdx.x;
     const int i = blockIdx.y * 8 + threadIdx.y;
     if (i >= n || 2 * jj >= n) return;
-    const T su = (T)L.su, sv = (T)L.sv, su4 = (T)(4.0 * L.su), sv4 = (T)(4.0 * L.sv);
+    const T su = L.su, sv = L.sv, su4 = L.su4, sv4 = L.sv4;
     const int j = 2 * jj + ((i + colour) & 1);
     const int jo = 2 * jj + 1 - ((i + colour) & 1);
     const size_t p = (size_t)i * n + j, po = (size_t)i * n + jo;
     const size_t nn = (size_t)n * n;
     T bu, bv;
     if (MODE == kBPassFirst && r64) {
-        bu = (T)r64[p];
-        bv = (T)r64[nn + p];
+        bu = from_f64<T>(r64[p]);
+        bv = from_f64<T>(r64[nn + p]);
         st2(Bv, p, bu, bv);
-        st2(Bv, po, (T)r64[po], (T)r64[nn + po]);
+        st2(Bv, po, from_f64<T>(r64[po]), from_f64<T>(r64[nn + po]));
     } else {
         const auto b = ld2(Bv, p);
         bu = b.x;
@@ -337,21 +358,21 @@ __global__ void __launch_bounds__(256) k_bmg_pass(T* __restrict__ X, T* __restri
     if (MODE == kBPassFirst) st2(X, po, T(0), T(0));
     if (MODE == kBPassLast) {
         const auto o = ld2(X, po);
-        z64[p] = (double)u;
-        z64[nn + p] = (double)v;
-        z64[po] = (double)o.x;
-        z64[nn + po] = (double)o.y;
+        z64[p] = to_f64(u);
+        z64[nn + p] = to_f64(v);
+        z64[po] = to_f64(o.x);
+        z64[nn + po] = to_f64(o.y);
     }
 }
 
 // Residual r = b - (K x - diag(s) (S - 4x)) of one level at point (i, j).
-template <class T>
-__device__ __forceinline__ void resid_at(const T* X, const T* Bv, const T* __restrict__ K, int n, int i, int j, T su,
-                                         T sv, T& ru, T& rv) {
+template <class T, bool SMEM_K = false>
+__device__ __forceinline__ void resid_at(const T* X, const T* Bv, const T* K, int n, int i, int j, T su, T sv, T& ru,
+                                         T& rv) {
     const size_t p = (size_t)i * n + j;
     const auto x = ld2(X, p);
     const auto bb = ld2(Bv, p);
-    const Blk<T> k = load_blk(K, p);
+    const Blk<T> k = SMEM_K ? load_blk_s(K, p) : load_blk(K, p);
     T Su, Sv;
     nbr_sums(X, n, i, j, Su, Sv);
     ru = bb.x - ((k.k11 * x.x + k.k12 * x.y) + su * (T(4) * x.x - Su));
@@ -370,13 +391,13 @@ __device__ __forceinline__ T fw9(T c, T w, T e, T s, T n, T sw, T se, T nw, T ne
 // periodic), kept in shared memory, then full weighting into the coarse right-hand side.
 template <class T>
 __global__ void __launch_bounds__(256) k_bmg_restrict(const T* __restrict__ X, const T* __restrict__ Bv,
-                                                      const T* __restrict__ K, LvlArgs L, T* __restrict__ Bc) {
+                                                      const T* __restrict__ K, LvlArgs<T> L, T* __restrict__ Bc) {
     constexpr int TS = 16, FS = 2 * TS + 1;
     __shared__ T su_s[FS][FS + 1], sv_s[FS][FS + 1];
     const int nf = L.n, nc = nf / 2;
     const int I0 = blockIdx.y * TS, J0 = blockIdx.x * TS;
     const int tid = threadIdx.y * TS + threadIdx.x;
-    const T su = (T)L.su, sv = (T)L.sv;
+    const T su = L.su, sv = L.sv;
     for (int idx = tid; idx < FS * FS; idx += TS * TS) {
         const int a = idx / FS, b = idx - a * FS;
         const int fi = (2 * I0 - 1 + a + nf) % nf, fj = (2 * J0 - 1 + b + nf) % nf;
@@ -422,10 +443,10 @@ __global__ void __launch_bounds__(256) k_bmg_prolong(const T* __restrict__ Xc, i
 // The coarsest level in one block: x = 0, then `sweeps` red-black sweeps (colour 0, 1).
 template <class T>
 __global__ void __launch_bounds__(1024) k_bmg_coarsest(T* __restrict__ X, const T* __restrict__ Bv,
-                                                       const T* __restrict__ K, LvlArgs L, int sweeps) {
+                                                       const T* __restrict__ K, LvlArgs<T> L, int sweeps) {
     const int n = L.n;
     const int nn = n * n;
-    const T su = (T)L.su, sv = (T)L.sv, su4 = (T)(4.0 * L.su), sv4 = (T)(4.0 * L.sv);
+    const T su = L.su, sv = L.sv, su4 = L.su4, sv4 = L.sv4;
     for (int p = threadIdx.x; p < nn; p += blockDim.x) st2(X, p, T(0), T(0));
     __syncthreads();
     for (int s = 0; s < sweeps; ++s) {
@@ -444,16 +465,21 @@ __global__ void __launch_bounds__(1024) k_bmg_coarsest(T* __restrict__ X, const 
     }
 }
 
-// Levels with n <= 64 below a finer level, as one block: every tail level's pairs x and b live in
-// shared memory (blocks K are read through L1), and the block runs their whole V-cycle — the same
-// per-point arithmetic as the level kernels, so the result is the same to the bit.  desc[k]
-// describes tail level k (k = 0 the finest of them): its n, the offset of its x in the shared
-// buffer (b follows at offset + 2 n^2), s_u, s_v and its blocks.
+// The small levels below the finest (n <= 64 in FP32, n <= 32 in FP64) as one block: every tail
+// level's pairs x, b and blocks K live in shared memory (8 n^2 values a level, at most 175 KB), and
+// the block runs their whole V-cycle — the same per-point arithmetic as the level kernels, so the
+// result is the same to the bit.  desc[k] describes tail level k (k = 0 the finest of them): its
+// n, the offset of its x in the shared buffer (b follows at offset + 2 n^2, K at offset + 4 n^2),
+// s_u, s_v and its blocks in global memory (copied in at the start).
 struct TailLvl {
     int n, off;
-    double su, sv;
     const void* K;
+    LvlArgs<double> d;  // the level's constants in FP64 and in FP32 (formed on the host: one SM's
+    LvlArgs<float> f;   // FP64 pipe would take tens of microseconds to convert them per pass)
 };
+template <class T> __device__ __forceinline__ const LvlArgs<T>& tail_args(const TailLvl& L);
+template <> __device__ __forceinline__ const LvlArgs<double>& tail_args<double>(const TailLvl& L) { return L.d; }
+template <> __device__ __forceinline__ const LvlArgs<float>& tail_args<float>(const TailLvl& L) { return L.f; }
 
 template <class T>
 __global__ void __launch_bounds__(512, 1) k_bmg_tail(const TailLvl* __restrict__ desc, int count, int pre, int post,
@@ -477,8 +503,9 @@ __global__ void __launch_bounds__(512, 1) k_bmg_tail(const TailLvl* __restrict__
         const int n = L.n, half = n / 2;
         T* X = base + L.off;
         const T* Bv = X + 2 * n * n;
-        const T* K = static_cast<const T*>(L.K);
-        const T su = (T)L.su, sv = (T)L.sv, su4 = (T)(4.0 * L.su), sv4 = (T)(4.0 * L.sv);
+        const T* K = X + 4 * n * n;
+        const LvlArgs<T>& A = tail_args<T>(L);
+        const T su = A.su, sv = A.sv, su4 = A.su4, sv4 = A.sv4;
         for (int idx = tid; idx < n * half; idx += nt) {
             const int i = idx / half, jj = idx - i * half;
             const int j = 2 * jj + ((i + colour) & 1), jo = 2 * jj + 1 - ((i + colour) & 1);
@@ -486,7 +513,7 @@ __global__ void __launch_bounds__(512, 1) k_bmg_tail(const TailLvl* __restrict__
             const auto b = ld2(Bv, p);
             T Su = T(0), Sv = T(0), u, v;
             if (!first) nbr_sums(X, n, i, j, Su, Sv);
-            block_update(load_blk(K, p), su, sv, su4, sv4, b.x, b.y, Su, Sv, u, v);
+            block_update(load_blk_s(K, p), su, sv, su4, sv4, b.x, b.y, Su, Sv, u, v);
             st2(X, p, u, v);
             if (first) st2(X, (size_t)i * n + jo, T(0), T(0));
         }
@@ -501,29 +528,29 @@ __global__ void __launch_bounds__(512, 1) k_bmg_tail(const TailLvl* __restrict__
         const int nf = L.n, nc = C.n;
         const T* X = base + L.off;
         const T* Bv = X + 2 * nf * nf;
-        const T* K = static_cast<const T*>(L.K);
+        const T* K = X + 4 * nf * nf;
         T* Bc = base + C.off + 2 * nc * nc;
-        const T su = (T)L.su, sv = (T)L.sv;
+        const T su = tail_args<T>(L).su, sv = tail_args<T>(L).sv;
         for (int idx = tid; idx < nc * nc; idx += nt) {
             const int I = idx / nc, J = idx - I * nc;
             const int i = 2 * I, j = 2 * J;
             const int im = i == 0 ? nf - 1 : i - 1, ip = i + 1, jm = j == 0 ? nf - 1 : j - 1, jp = j + 1;
             // fw9's sums in its order, accumulated as the residuals are formed (fewer live registers)
             T cu, cv, au, av, bu, bv;
-            resid_at(X, Bv, K, nf, i, j, su, sv, cu, cv);
-            resid_at(X, Bv, K, nf, i, jm, su, sv, au, av);
-            resid_at(X, Bv, K, nf, i, jp, su, sv, bu, bv);
+            resid_at<T, true>(X, Bv, K, nf, i, j, su, sv, cu, cv);
+            resid_at<T, true>(X, Bv, K, nf, i, jm, su, sv, au, av);
+            resid_at<T, true>(X, Bv, K, nf, i, jp, su, sv, bu, bv);
             const T weu = au + bu, wev = av + bv;
-            resid_at(X, Bv, K, nf, im, j, su, sv, au, av);
-            resid_at(X, Bv, K, nf, ip, j, su, sv, bu, bv);
+            resid_at<T, true>(X, Bv, K, nf, im, j, su, sv, au, av);
+            resid_at<T, true>(X, Bv, K, nf, ip, j, su, sv, bu, bv);
             const T edgeu = weu + (au + bu), edgev = wev + (av + bv);
-            resid_at(X, Bv, K, nf, im, jm, su, sv, au, av);
-            resid_at(X, Bv, K, nf, im, jp, su, sv, bu, bv);
+            resid_at<T, true>(X, Bv, K, nf, im, jm, su, sv, au, av);
+            resid_at<T, true>(X, Bv, K, nf, im, jp, su, sv, bu, bv);
             T coru = au + bu, corv = av + bv;
-            resid_at(X, Bv, K, nf, ip, jm, su, sv, au, av);
+            resid_at<T, true>(X, Bv, K, nf, ip, jm, su, sv, au, av);
             coru = coru + au;
             corv = corv + av;
-            resid_at(X, Bv, K, nf, ip, jp, su, sv, au, av);
+            resid_at<T, true>(X, Bv, K, nf, ip, jp, su, sv, au, av);
             coru = coru + au;
             corv = corv + av;
             st2(Bc, (size_t)idx, ((T(4) * cu + T(2) * edgeu) + coru) * T(0.0625),
@@ -575,6 +602,13 @@ __global__ void __launch_bounds__(512, 1) k_bmg_tail(const TailLvl* __restrict__
         const int n0 = desc[0].n;
         T* B0 = base + desc[0].off + 2 * n0 * n0;
         for (int q = threadIdx.x; q < 2 * n0 * n0; q += blockDim.x) B0[q] = Bin[q];
+        for (int k = 0; k < count; ++k) {
+            const int nk = desc[k].n;
+            const float4* src = static_cast<const float4*>(desc[k].K);
+            float4* dst = reinterpret_cast<float4*>(base + desc[k].off + 4 * nk * nk);
+            const int n16 = (int)(4 * (size_t)nk * nk * sizeof(T) / 16);
+            for (int q = threadIdx.x; q < n16; q += blockDim.x) dst[q] = __ldg(src + q);
+        }
     }
     __syncthreads();
     // block-wide levels down to kw (restricting into kw last)
@@ -605,18 +639,19 @@ __device__ __forceinline__ void kfine_point(double u, double v, double c1, doubl
     k.k21 = (2.0 * u) * v - B;
     k.k22 = c2 + u * u;
 }
-__device__ __forceinline__ void kfine_point(double u, double v, double c1, double c2, double B, Blk<float>& k) {
+__device__ __forceinline__ void kfine_point(double u, double v, float c1, float c2, float B, Blk<float>& k) {
     const float u32 = f64_to_f32(u), v32 = f64_to_f32(v);
     const float uv2 = (2.0f * u32) * v32, uu = u32 * u32;
-    k.k11 = (float)c1 - uv2;
+    k.k11 = c1 - uv2;
     k.k12 = -uu;
-    k.k21 = uv2 - (float)B;
-    k.k22 = (float)c2 + uu;
+    k.k21 = uv2 - B;
+    k.k22 = c2 + uu;
 }
 
+// c1 = 1/dt + (B + 1), c2 = 1/dt and B in the multigrid's precision (rounded on the host)
 template <class T>
-__global__ void __launch_bounds__(256) k_bmg_kfine(const double* __restrict__ w, size_t nn, double c1, double c2,
-                                                   double B, T* __restrict__ K) {
+__global__ void __launch_bounds__(256) k_bmg_kfine(const double* __restrict__ w, size_t nn, T c1, T c2, T B,
+                                                   T* __restrict__ K) {
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nn) return;
     Blk<T> k;
@@ -653,21 +688,21 @@ __global__ void __launch_bounds__(256) k_bmg_krestrict(const T* __restrict__ Kf,
 template <class T>
 __global__ void k_bmg_in(const double* __restrict__ r, size_t nn, T* __restrict__ B) {
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < nn) st2(B, p, (T)r[p], (T)r[nn + p]);
+    if (p < nn) st2(B, p, from_f64<T>(r[p]), from_f64<T>(r[nn + p]));
 }
 template <class T>
 __global__ void k_bmg_out(const T* __restrict__ X, size_t nn, double* __restrict__ z) {
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p < nn) {
         const auto x = ld2(X, p);
-        z[p] = (double)x.x;
-        z[nn + p] = (double)x.y;
+        z[p] = to_f64(x.x);
+        z[nn + p] = to_f64(x.y);
     }
 }
 
 constexpr int kBmgCoarsestSweeps = 30;
 constexpr int kBmgOneBlockPoints = 4096;
-constexpr int kBmgTailMaxN = 64;  // levels this small (below the finest) run in the one-block tail
+constexpr int kBmgTailMaxN = 64;  // levels this small (below the finest; half in FP64) run in the one-block tail
 
 }  // namespace
 
@@ -860,10 +895,11 @@ BrussMG2D::BrussMG2D(Context& ctx, size_t n, const numa_brusselator2d_params& p,
         if (m % 4 != 0 || m / 2 < 4) break;
         m /= 2;
     }
-    // levels below the finest with n <= 64 run as one block (at most 4 (64^2 + 32^2 + ...) values,
-    // 175 KB of shared memory in FP64)
+    // levels below the finest with n <= 64 (FP32) or n <= 32 (FP64) run as one block: x, b and K,
+    // 8 (64^2 + 32^2 + ...) values, at most 175 KB of shared memory
+    const int tail_max_n = precision == NUMA_GPU_FP64 ? kBmgTailMaxN / 2 : kBmgTailMaxN;
     for (size_t l = 1; l < levels_.size(); ++l)
-        if (levels_[l]->n <= kBmgTailMaxN) {
+        if (levels_[l]->n <= tail_max_n) {
             tail_first_ = (int)l;
             break;
         }
@@ -872,8 +908,10 @@ BrussMG2D::BrussMG2D(Context& ctx, size_t n, const numa_brusselator2d_params& p,
         size_t off = 0;
         for (size_t l = (size_t)tail_first_; l < levels_.size(); ++l) {
             const Level& L = *levels_[l];
-            d.push_back(TailLvl{L.n, (int)off, L.su, L.sv, L.k.p});
-            off += 4 * (size_t)L.n * L.n;
+            d.push_back(TailLvl{L.n, (int)off, L.k.p, LvlArgs<double>{L.n, L.su, L.sv, 4.0 * L.su, 4.0 * L.sv},
+                                LvlArgs<float>{L.n, (float)L.su, (float)L.sv, (float)(4.0 * L.su),
+                                               (float)(4.0 * L.sv)}});
+            off += 8 * (size_t)L.n * L.n;
         }
         tail_count_ = (int)d.size();
         tail_smem_ = off * esz;
@@ -881,12 +919,9 @@ BrussMG2D::BrussMG2D(Context& ctx, size_t n, const numa_brusselator2d_params& p,
         NUMA_CUDA(cudaMemcpyAsync(tail_desc_.p, d.data(), d.size() * sizeof(TailLvl), cudaMemcpyHostToDevice,
                                   ctx_.stream));
         ctx_.sync();
-        if (precision == NUMA_GPU_FP64)
-            NUMA_CUDA(cudaFuncSetAttribute(k_bmg_tail<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)tail_smem_));
-        else
-            NUMA_CUDA(cudaFuncSetAttribute(k_bmg_tail<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)tail_smem_));
+        const int lim = precision == NUMA_GPU_FP64 ? set_dynamic_smem_limit(ctx_, k_bmg_tail<double>)
+                                                   : set_dynamic_smem_limit(ctx_, k_bmg_tail<float>);
+        if (tail_smem_ > (size_t)lim) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "BrussMG2D tail exceeds shared memory");
     }
 }
 
@@ -900,13 +935,15 @@ static T* tp(DeviceArray<double>& a) {
 }
 
 void BrussMG2D::set_state(const double* w) {
+    state_set_ = true;
     const size_t nn = n0_ * n0_;
     const double c1 = 1.0 / P_.dt + (P_.B + 1.0), c2 = 1.0 / P_.dt;
     const unsigned g = (unsigned)((nn + 255) / 256);
     if (precision_ == NUMA_GPU_FP64)
         k_bmg_kfine<double><<<g, 256, 0, ctx_.stream>>>(w, nn, c1, c2, P_.B, tp<double>(levels_[0]->k));
     else
-        k_bmg_kfine<float><<<g, 256, 0, ctx_.stream>>>(w, nn, c1, c2, P_.B, tp<float>(levels_[0]->k));
+        k_bmg_kfine<float><<<g, 256, 0, ctx_.stream>>>(w, nn, (float)c1, (float)c2, (float)P_.B,
+                                                       tp<float>(levels_[0]->k));
     ctx_.count_launch();
     for (size_t l = 0; l + 1 < levels_.size(); ++l) {
         const int nc = levels_[l + 1]->n;
@@ -932,7 +969,7 @@ void BrussMG2D::cycle(size_t l) {
     T* X = tp<T>(L.x);
     T* Bv = tp<T>(L.b);
     const T* K = tp<T>(L.k);
-    const LvlArgs A{n, L.su, L.sv};
+    const LvlArgs<T> A{n, (T)L.su, (T)L.sv, (T)(4.0 * L.su), (T)(4.0 * L.sv)};
     const dim3 blk(32, 8);
     const dim3 pgrid((unsigned)((n / 2 + 31) / 32), (unsigned)((n + 7) / 8));
     const size_t nn = (size_t)n * n;
@@ -1021,6 +1058,46 @@ void BrussMG2D::coarse_cycle() {
     }
     NUMA_CUDA(cudaGraphLaunch(coarse_exec_, ctx_.stream));
     ctx_.count_launch(static_cast<unsigned>(coarse_kernels_));
+}
+
+// Average duration of one colour pass on the finest level (the V-cycle's dominant kernel), over
+// reps back-to-back launches timed with CUDA events on the context's stream; the blocks must have
+// been set.
+double BrussMG2D::time_finest_pass(int reps) {
+    if (!state_set_) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "BrussMG2D: set_state before timing");
+    Level& L = *levels_[0];
+    const int n = L.n;
+    const LvlArgs<double> A64{n, L.su, L.sv, 4.0 * L.su, 4.0 * L.sv};
+    const LvlArgs<float> A32{n, (float)L.su, (float)L.sv, (float)(4.0 * L.su), (float)(4.0 * L.sv)};
+    const dim3 blk(32, 8), pgrid((unsigned)((n / 2 + 31) / 32), (unsigned)((n + 7) / 8));
+    const size_t esz = precision_ == NUMA_GPU_FP64 ? 8 : 4;
+    NUMA_CUDA(cudaMemsetAsync(L.x.p, 0, 2 * (size_t)n * n * esz, ctx_.stream));
+    NUMA_CUDA(cudaMemsetAsync(L.b.p, 0, 2 * (size_t)n * n * esz, ctx_.stream));
+    cudaEvent_t a, b;
+    NUMA_CUDA(cudaEventCreate(&a));
+    NUMA_CUDA(cudaEventCreate(&b));
+    auto launch = [&](int colour) {
+        if (precision_ == NUMA_GPU_FP64)
+            k_bmg_pass<double, kBPassNormal><<<pgrid, blk, 0, ctx_.stream>>>(tp<double>(L.x), tp<double>(L.b),
+                                                                             tp<double>(L.k), A64, colour, nullptr,
+                                                                             nullptr);
+        else
+            k_bmg_pass<float, kBPassNormal><<<pgrid, blk, 0, ctx_.stream>>>(tp<float>(L.x), tp<float>(L.b),
+                                                                            tp<float>(L.k), A32, colour, nullptr,
+                                                                            nullptr);
+    };
+    launch(0);
+    NUMA_CUDA(cudaEventRecord(a, ctx_.stream));
+    for (int r = 0; r < reps; ++r) launch(r & 1);
+    NUMA_CUDA(cudaEventRecord(b, ctx_.stream));
+    NUMA_CUDA(cudaEventSynchronize(b));
+    float ms = 0.f;
+    NUMA_CUDA(cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    ctx_.count_launch(reps + 1);
+    ctx_.check_launch("BrussMG2D time_finest_pass");
+    return reps > 0 ? ms / reps : 0.0;
 }
 
 void BrussMG2D::apply(const double* r, double* z) {

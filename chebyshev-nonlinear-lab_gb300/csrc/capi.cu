@@ -1626,6 +1626,11 @@ int numa_gpu_provider_learned_stats(numa_gpu_provider* p, size_t* applies, size_
     });
 }
 
+int numa_gpu_diag_time_bmg2d_pass(numa_gpu_bmg2d* mg, int reps, double* ms_per_pass) {
+    if (!mg || !ms_per_pass || reps < 1) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(mg->ctx, [&] { *ms_per_pass = mg->impl->time_finest_pass(reps); });
+}
+
 int numa_gpu_diag_time_smoother(numa_gpu_mg* mg, int reps, double* ms_per_pass) {
     if (!mg || !ms_per_pass || reps < 1) return NUMA_GPU_ERR_INVALID_ARGUMENT;
     return guard(mg->ctx, [&] { *ms_per_pass = mg->impl->time_finest_pass(reps); });

@@ -290,6 +290,21 @@ struct Context {
     void count_launch(unsigned n = 1) { launches += n; }
     void check_launch(const char* what);
 };
+// Largest dynamic shared memory a block may opt in to on the context's device (bytes).
+int smem_optin_limit(Context& ctx);
+
+// Sets a kernel's dynamic shared-memory limit to the most the device allows beside the kernel's
+// static shared memory, and returns it.  The attribute belongs to the kernel, not to one caller:
+// a fixed value lets hierarchies and grids of any size share the kernel (a caller setting its own
+// need would lower the limit under another's launch).
+template <class K>
+int set_dynamic_smem_limit(Context& ctx, K* kernel) {
+    cudaFuncAttributes a;
+    NUMA_CUDA(cudaFuncGetAttributes(&a, kernel));
+    const int lim = smem_optin_limit(ctx) - (int)a.sharedSizeBytes;
+    NUMA_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+    return lim;
+}
 
 // Device scalar slots with fixed roles.
 enum ScalarSlot : int {

@@ -15,6 +15,12 @@ void throw_cuda(cudaError_t e, const char* what, const char* file, int line) {
     throw Status(NUMA_GPU_ERR_CUDA, buf);
 }
 
+int smem_optin_limit(Context& ctx) {
+    int v = 0;
+    NUMA_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx.device));
+    return v;
+}
+
 std::recursive_mutex& alloc_capture_mutex() {
     static std::recursive_mutex m;
     return m;

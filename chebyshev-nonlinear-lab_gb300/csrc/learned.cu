@@ -52,8 +52,8 @@ template <int CIN, int COUT, bool OUT32>
 void launch_conv(Context& ctx, const VoxGrid& g, const uint4* in, const uint4* wg, const float* bias, uint4* out,
                  float* out32, int relu, unsigned* err) {
     const size_t smem = conv_smem_bytes<CIN, COUT>(g);
-    NUMA_CUDA(cudaFuncSetAttribute(k_conv3d_tc<CIN, COUT, OUT32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
+    const int lim = set_dynamic_smem_limit(ctx, k_conv3d_tc<CIN, COUT, OUT32>);
+    if (smem > (size_t)lim) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "convolution tile exceeds shared memory");
     const int grid = std::max(1, std::min(g.tiles, 2 * ctx.sm_count));
     k_conv3d_tc<CIN, COUT, OUT32><<<grid, 128, smem, ctx.stream>>>(in, wg, bias, out, out32, g, relu, err);
     ctx.count_launch();

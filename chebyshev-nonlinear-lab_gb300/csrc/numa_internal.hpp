@@ -233,6 +233,8 @@ public:
     void set_state(const double* w);
     // z = V-cycle(r), FP64 planes in and out
     void apply(const double* r, double* z);
+    // ms of one finest-level colour pass (CUDA events, reps back-to-back launches)
+    double time_finest_pass(int reps);
     struct Level;
 
 private:
@@ -248,6 +250,7 @@ private:
     double* z0_ = nullptr;
     cudaGraphExec_t coarse_exec_ = nullptr;
     uint64_t coarse_kernels_ = 0;
+    bool state_set_ = false;
     int tail_first_ = -1;          // first level of the one-block tail (-1: none)
     int tail_count_ = 0;
     size_t tail_smem_ = 0;         // its shared memory in bytes

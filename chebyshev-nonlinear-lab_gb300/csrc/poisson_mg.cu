@@ -114,10 +114,9 @@ PoissonMG::PoissonMG(Context& ctx, size_t n, int pre, int post, int precision, i
             for (size_t m = l; m < levels_.size(); ++m) elems += 3 * (size_t)levels_[m]->n * levels_[m]->n * levels_[m]->n;
             elems += (size_t)levels_[l]->n * levels_[l]->n * levels_[l]->n;
             tail_smem_ = elems * sizeof(float);
-            NUMA_CUDA(cudaFuncSetAttribute(k_mg_tail<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)tail_smem_));
-            NUMA_CUDA(cudaFuncSetAttribute(k_mg_tail<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)tail_smem_));
+            const int lim = std::min(set_dynamic_smem_limit(ctx_, k_mg_tail<float, true>),
+                                     set_dynamic_smem_limit(ctx_, k_mg_tail<float, false>));
+            if (tail_smem_ > (size_t)lim) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "PoissonMG tail exceeds shared memory");
             tail_l_ = l;
             break;
         }

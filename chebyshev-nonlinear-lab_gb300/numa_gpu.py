@@ -220,6 +220,7 @@ SIGNATURES = {
     "numa_gpu_mg_apply_noalloc": ([_SZ, _I, _I, _P, _P, _P], _I),
     "numa_gpu_diag_fp64_peak": ([_P, _F64P], _I),
     "numa_gpu_diag_time_smoother": ([_P, _I, _F64P], _I),
+    "numa_gpu_diag_time_bmg2d_pass": ([_P, _I, _F64P], _I),
     "numa_gpu_diag_exp": ([_P, _P, _P], _I),
     "numa_gpu_diag_conv3d": ([_P, _SZ, _I, _I, _I, _F32P, _F32P, _F32P, _F32P], _I),
     "numa_gpu_solve_batch": ([_I, C.POINTER(BatchInstance), _SZ, _I, _I, C.POINTER(KrylovParams), _I,
@@ -612,6 +613,12 @@ class BrussMG2D(_Handle):
 
     def apply(self, r: Vec, z: Vec):
         self.ctx.check(self.lib.numa_gpu_bmg2d_apply(self.h, r.h, z.h), "bmg2d_apply")
+
+    def time_pass(self, reps: int = 20) -> float:
+        """ms of one finest-level colour pass (after set_state)."""
+        v = C.c_double()
+        self.ctx.check(self.lib.numa_gpu_diag_time_bmg2d_pass(self.h, reps, C.byref(v)), "diag_time_bmg2d_pass")
+        return v.value
 
 
 def brusselator2d_initial(n: int, A: float = 1.0, B: float = 3.4, seed: int = 20261203) -> np.ndarray:

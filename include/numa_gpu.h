@@ -515,6 +515,8 @@ int numa_gpu_diag_fp64_peak(numa_gpu_ctx* ctx, double* tflops);
 /* Average duration in ms of one red-black Gauss-Seidel colour pass on the finest level of mg
  * (the V-cycle's dominant kernel), over reps back-to-back launches timed with CUDA events. */
 int numa_gpu_diag_time_smoother(numa_gpu_mg* mg, int reps, double* ms_per_pass);
+/* The same for the finest level of a Brusselator2D multigrid (its blocks must have been set). */
+int numa_gpu_diag_time_bmg2d_pass(numa_gpu_bmg2d* mg, int reps, double* ms_per_pass);
 /* out = e^x as the residual kernels compute it (Tang's table-driven method, FP64); cuda_ref
  * (may be NULL) = CUDA's exp(x).  For accuracy checks of the exponential. */
 int numa_gpu_diag_exp(const numa_gpu_vec* x, numa_gpu_vec* out, numa_gpu_vec* cuda_ref);
