@@ -133,7 +133,11 @@ __global__ void __launch_bounds__(BX* BY) k_jvp(const double* __restrict__ cx, c
 // plane of the tile with a 1-point halo; three plane slots roll along i.  Software-pipelined:
 // the raw values of plane i+2 and the coefficient of plane i+1 are loaded into registers while
 // plane i is computed, so the loads' latency overlaps the arithmetic.
-__global__ void __launch_bounds__(BX* BY) k_jvp32(const float* __restrict__ c32, const double* __restrict__ v,
+__device__ __forceinline__ float to_f32(double x) { return f64_to_f32(x); }
+__device__ __forceinline__ float to_f32(float x) { return x; }
+
+template <class VT>
+__global__ void __launch_bounds__(BX* BY) k_jvp32(const float* __restrict__ c32, const VT* __restrict__ v,
                                                   double* __restrict__ out, int n, int ichunk, float h2inv) {
     constexpr int TW = BX + 2, TH = BY + 2, TE = TW * TH;  // 34 x 10 tile, 340 values
     constexpr int PER = (TE + BX * BY - 1) / (BX * BY);    // values per thread and plane (2)
@@ -154,11 +158,11 @@ __global__ void __launch_bounds__(BX* BY) k_jvp32(const float* __restrict__ c32,
         pos[q] = e < TE ? e : -1;
         off[q] = (e < TE && jj >= 0 && jj < n && kk >= 0 && kk < n) ? jj * n + kk : -1;
     }
-    double raw[PER];
+    VT raw[PER];
     auto issue = [&](int p) {
 #pragma unroll
         for (int q = 0; q < PER; ++q) {
-            raw[q] = 0.0;
+            raw[q] = VT(0);
             if (p >= 0 && p < n && off[q] >= 0) raw[q] = v[(size_t)p * plane + off[q]];
         }
     };
@@ -166,7 +170,7 @@ __global__ void __launch_bounds__(BX* BY) k_jvp32(const float* __restrict__ c32,
         float* T = &S[(p + 3) % 3][0][0];
 #pragma unroll
         for (int q = 0; q < PER; ++q)
-            if (pos[q] >= 0) T[pos[q]] = f64_to_f32(raw[q]);
+            if (pos[q] >= 0) T[pos[q]] = to_f32(raw[q]);
     };
     const bool inside = k < n && j < n;
     const size_t col = (size_t)j * n + k;
@@ -252,6 +256,14 @@ void Bratu3D::bind(const double*, const double* cache, int precision) {
     }
 }
 
+void Bratu3D::jvp_bound32(const float* v32, double* out) {
+    if (bound_precision_ != NUMA_GPU_FP32) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Bratu3D: no FP32 product bound");
+    March m = march_shape((int)n_, false);
+    k_jvp32<float><<<m.grid, dim3(BX, BY), 0, ctx_.stream>>>(bound_c32_, v32, out, (int)n_, m.ichunk, (float)h2inv_);
+    ctx_.count_launch();
+    ctx_.check_launch("bratu3d jvp32 (fp32 input)");
+}
+
 void Bratu3D::jvp_bound(const double* v, double* out) {
     if (bound_precision_ == NUMA_GPU_FP32) jvp_c32(bound_c32_, v, out);
     else jvp_c(bound_c_, v, out);
@@ -295,7 +307,7 @@ void Bratu3D::jvp_c(const double* c, const double* v, double* out) {
 
 void Bratu3D::jvp_c32(const float* c32, const double* v, double* out) {
     March m = march_shape((int)n_, false);
-    k_jvp32<<<m.grid, dim3(BX, BY), 0, ctx_.stream>>>(c32, v, out, (int)n_, m.ichunk, (float)h2inv_);
+    k_jvp32<double><<<m.grid, dim3(BX, BY), 0, ctx_.stream>>>(c32, v, out, (int)n_, m.ichunk, (float)h2inv_);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d jvp32");
 }
@@ -304,7 +316,7 @@ void Bratu3D::jvp_c32(const float* c32, const double* v, double* out) {
 // that hold the coefficient themselves (the learned preconditioner).
 void bratu_jvp32(Context& ctx, int n, double h2inv, const float* c32, const double* v, double* out) {
     March m = march_shape(n, false);
-    k_jvp32<<<m.grid, dim3(BX, BY), 0, ctx.stream>>>(c32, v, out, n, m.ichunk, (float)h2inv);
+    k_jvp32<double><<<m.grid, dim3(BX, BY), 0, ctx.stream>>>(c32, v, out, n, m.ichunk, (float)h2inv);
     ctx.count_launch();
     ctx.check_launch("bratu jvp32");
 }

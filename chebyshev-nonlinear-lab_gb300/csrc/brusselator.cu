@@ -185,9 +185,14 @@ struct B2Geom32 {
     float invdt, B, c1, duh, dvh;
 };
 
-// J d in FP32 arithmetic (FP64 in and out): a 32 x 8 tile of both components with its one-point
-// periodic halo is rounded to FP32 once per point (integer-pipe conversion) into shared memory.
-__global__ void __launch_bounds__(256) k_b2_jvp32(const float2* __restrict__ coef, const double* __restrict__ d,
+__device__ __forceinline__ float to_f32(double x) { return f64_to_f32(x); }
+__device__ __forceinline__ float to_f32(float x) { return x; }
+
+// J d in FP32 arithmetic (FP64 out; d in FP64 or already in FP32): a 32 x 8 tile of both components
+// with its one-point periodic halo is rounded to FP32 once per point (integer-pipe conversion) into
+// shared memory.
+template <class VT>
+__global__ void __launch_bounds__(256) k_b2_jvp32(const float2* __restrict__ coef, const VT* __restrict__ d,
                                                   double* __restrict__ out, B2Geom32 G) {
     constexpr int TX = 32, TY = 8;
     __shared__ float tu[TY + 2][TX + 3], tv[TY + 2][TX + 3];
@@ -199,8 +204,8 @@ __global__ void __launch_bounds__(256) k_b2_jvp32(const float2* __restrict__ coe
         const int a = idx / (TX + 2), b = idx - a * (TX + 2);
         const int gi = (i0 - 1 + a + n) % n, gj = (j0 - 1 + b + n) % n;
         const size_t q = (size_t)gi * n + gj;
-        tu[a][b] = f64_to_f32(d[q]);
-        tv[a][b] = f64_to_f32(d[nn + q]);
+        tu[a][b] = to_f32(d[q]);
+        tv[a][b] = to_f32(d[nn + q]);
     }
     __syncthreads();
     const int i = i0 + threadIdx.y, j = j0 + threadIdx.x;
@@ -320,11 +325,12 @@ enum { kBPassNormal = 0, kBPassFirst = 1, kBPassLast = 2 };
 //  Normal: x_c updated from the other colour.
 //  First (colour 0, x = 0 before the pass): x_0 = block^-1 b (neighbour sums are zeros), x_1 = 0;
 //    on the finest level the right-hand side is read from r (FP64 planes) and stored as b.
-//  Last (finest level, colour 0, the cycle's final pass): also writes z (FP64 planes) for both points.
+//  Last (finest level, colour 0, the cycle's final pass): also writes z (FP64 planes) for both points,
+//    or, for an FP32 consumer, the same values as FP32 planes z32.
 template <class T, int MODE>
 __global__ void __launch_bounds__(256) k_bmg_pass(T* __restrict__ X, T* __restrict__ Bv, const T* __restrict__ K,
                                                   LvlArgs<T> L, int colour, const double* __restrict__ r64,
-                                                  double* __restrict__ z64) {
+                                                  double* __restrict__ z64, float* __restrict__ z32 = nullptr) {
     const int n = L.n;
     const int jj = blockIdx.x * 32 + threadIdx.x;
     const int i = blockIdx.y * 8 + threadIdx.y;
@@ -358,10 +364,20 @@ __global__ void __launch_bounds__(256) k_bmg_pass(T* __restrict__ X, T* __restri
     if (MODE == kBPassFirst) st2(X, po, T(0), T(0));
     if (MODE == kBPassLast) {
         const auto o = ld2(X, po);
-        z64[p] = to_f64(u);
-        z64[nn + p] = to_f64(v);
-        z64[po] = to_f64(o.x);
-        z64[nn + po] = to_f64(o.y);
+        if (z64) {
+            z64[p] = to_f64(u);
+            z64[nn + p] = to_f64(v);
+            z64[po] = to_f64(o.x);
+            z64[nn + po] = to_f64(o.y);
+        }
+        if constexpr (sizeof(T) == 4) {
+            if (z32) {  // or the values unwidened, for an FP32 consumer
+                z32[p] = u;
+                z32[nn + p] = v;
+                z32[po] = o.x;
+                z32[nn + po] = o.y;
+            }
+        }
     }
 }
 
@@ -846,9 +862,22 @@ void Brusselator2D::jvp_bound(const double* v, double* out) {
     const B2Geom G = b2_geom(n_, P_);
     const B2Geom32 G32{(int)n_, (float)G.invdt, (float)G.B, (float)G.c1, (float)G.duh, (float)G.dvh};
     const dim3 grid((unsigned)((n_ + 31) / 32), (unsigned)((n_ + 7) / 8));
-    k_b2_jvp32<<<grid, dim3(32, 8), 0, ctx_.stream>>>(reinterpret_cast<const float2*>(coef32_.p), v, out, G32);
+    k_b2_jvp32<double><<<grid, dim3(32, 8), 0, ctx_.stream>>>(reinterpret_cast<const float2*>(coef32_.p), v, out,
+                                                              G32);
     ctx_.count_launch();
     ctx_.check_launch("Brusselator2D jvp32");
+}
+
+void Brusselator2D::jvp_bound32(const float* v32, double* out) {
+    if (bound_precision_ != NUMA_GPU_FP32)
+        throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Brusselator2D: no FP32 product bound");
+    const B2Geom G = b2_geom(n_, P_);
+    const B2Geom32 G32{(int)n_, (float)G.invdt, (float)G.B, (float)G.c1, (float)G.duh, (float)G.dvh};
+    const dim3 grid((unsigned)((n_ + 31) / 32), (unsigned)((n_ + 7) / 8));
+    k_b2_jvp32<float><<<grid, dim3(32, 8), 0, ctx_.stream>>>(reinterpret_cast<const float2*>(coef32_.p), v32, out,
+                                                             G32);
+    ctx_.count_launch();
+    ctx_.check_launch("Brusselator2D jvp32 (fp32 input)");
 }
 
 void Brusselator2D::jvp_at(const double* x, const double* v, double* out) {
@@ -1025,7 +1054,7 @@ void BrussMG2D::cycle(size_t l) {
     for (int k = 0; k < post_; ++k) {
         k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 1, nullptr, nullptr);
         if (finest && k + 1 == post_)
-            k_bmg_pass<T, kBPassLast><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 0, nullptr, z0_);
+            k_bmg_pass<T, kBPassLast><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 0, nullptr, z0_, z32_);
         else
             k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 0, nullptr, nullptr);
         ctx_.count_launch(2);
@@ -1100,6 +1129,18 @@ double BrussMG2D::time_finest_pass(int reps) {
     return reps > 0 ? ms / reps : 0.0;
 }
 
+void BrussMG2D::apply32(const double* r, float* z32) {
+    if (!supports_out32()) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "BrussMG2D: no FP32 output for this hierarchy");
+    z32_ = z32;
+    try {
+        apply(r, nullptr);
+    } catch (...) {
+        z32_ = nullptr;
+        throw;
+    }
+    z32_ = nullptr;
+}
+
 void BrussMG2D::apply(const double* r, double* z) {
     const size_t N = size();
     // the finest pass reads r while the last one writes z: an aliased call goes through a copy
@@ -1124,6 +1165,9 @@ public:
         : mg_(ctx, n, p, precision, pre, post) {}
     void make(const double* x, const double*) override { mg_.set_state(x); }
     void apply(const double* r, double* z) override { mg_.apply(r, z); }
+    // the FP32 cycle can hand its result over unwidened
+    bool has_apply32() const override { return mg_.supports_out32(); }
+    void apply32(const double* r, float* z32) override { mg_.apply32(r, z32); }
     int kind() const override { return NUMA_GPU_PRECOND_BRUSS_MG; }
 
 private:

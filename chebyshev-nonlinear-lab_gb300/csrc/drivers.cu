@@ -39,6 +39,9 @@ public:
         : mg_(ctx, n, pre, post, precision, max_levels) {}
     void make(const double*, const double*) override {}  // PoissonMGProvider::make ignores x
     void apply(const double* r, double* z) override { mg_.apply(r, z); }
+    // the FP32 cycle can hand its result over unwidened
+    bool has_apply32() const override { return mg_.supports_out32(); }
+    void apply32(const double* r, float* z32) override { mg_.apply32(r, z32); }
     int kind() const override { return NUMA_GPU_PRECOND_POISSON_MG; }
     PoissonMG& mg() { return mg_; }
 
@@ -159,6 +162,11 @@ public:
         if (mode_ == NUMA_GPU_DERIV_FD) f_.jvp_fd(x_, fx_, xnorm_, v, out);
         else f_.jvp_bound(v, out);
     }
+    bool has_apply32() const override { return mode_ != NUMA_GPU_DERIV_FD && f_.has_jvp32(); }
+    void apply32(const float* v32, double* out) override {
+        Timers::Scope s(&t_, kT_JVP);
+        f_.jvp_bound32(v32, out);
+    }
 
 private:
     NonlinearOp& f_;
@@ -175,6 +183,11 @@ public:
         p_->apply(r, z);
     }
     void progress(size_t iters, double rel_res) override { p_->progress(iters, rel_res); }
+    bool has_apply32() const override { return p_->has_apply32(); }
+    void apply32(const double* r, float* z32) override {
+        Timers::Scope s(&t_, kT_PREC);
+        p_->apply32(r, z32);
+    }
 
 private:
     Provider* p_;

@@ -171,8 +171,13 @@ __global__ void k_combine(const double* __restrict__ base, const double* __restr
     }
 }
 
-// x += sum_i coef[i] V_i in one pass (the flexible update; x is read and written in place)
-__global__ void k_combine_add(const double* __restrict__ V, size_t ldv, int cnt, const double* __restrict__ coef,
+__device__ __forceinline__ double widen(double v) { return v; }
+__device__ __forceinline__ double widen(float v) { return f32_to_f64(v); }
+
+// x += sum_i coef[i] V_i in one pass (the flexible update; x is read and written in place); V in
+// FP64, or in FP32 widened exactly (the same sums as from the widened vectors)
+template <class VT>
+__global__ void k_combine_add(const VT* __restrict__ V, size_t ldv, int cnt, const double* __restrict__ coef,
                               double* x, size_t N) {
     extern __shared__ double cs[];
     for (int r = threadIdx.x; r < cnt; r += blockDim.x) cs[r] = coef[r];
@@ -180,7 +185,7 @@ __global__ void k_combine_add(const double* __restrict__ V, size_t ldv, int cnt,
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) {
         double t = x[i];
-        for (int r = 0; r < cnt; ++r) t = __fma_rn(cs[r], V[(size_t)r * ldv + i], t);
+        for (int r = 0; r < cnt; ++r) t = __fma_rn(cs[r], widen(V[(size_t)r * ldv + i]), t);
         x[i] = t;
     }
 }
@@ -281,8 +286,12 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
         return res;
     }
     if (o.zero_guess) dev_fill(ctx_, x, 0.0, N);
+    // FP32 preconditioner output into an FP32 product: the preconditioned vectors are kept in FP32
+    // (exactly the values the FP64 path would widen), halving their writes and reads
+    const bool z32 = M && M->has_apply32() && A.has_apply32();
     V_.resize((m + 1) * N);
-    Z_.resize(m * N);
+    if (z32) Z32_.resize(m * N);
+    else Z_.resize(m * N);
     w_.resize(N);
     r_.resize(N);
     std::vector<std::vector<double>> H(m + 1, std::vector<double>(m, 0.0));
@@ -327,10 +336,17 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
         while (k < m && res.iters < o.max_iters) {
             const size_t j = k;
             const double* vj = j == 0 ? v0 : V_.p + j * N;
-            double* zj = Z_.p + j * N;
-            precond_apply(M, vj, zj);
-            ++res.precs;
-            A.apply(zj, w_.p);
+            if (z32) {
+                float* zj = Z32_.p + j * N;
+                M->apply32(vj, zj);
+                ++res.precs;
+                A.apply32(zj, w_.p);
+            } else {
+                double* zj = Z_.p + j * N;
+                precond_apply(M, vj, zj);
+                ++res.precs;
+                A.apply(zj, w_.p);
+            }
             ++res.matvecs;
             const int cnt = (int)(j + 1);
             launch_cgs<0>(ctx_, cnt, w_.p, v0, V_.p, N, nullptr, nullptr, sl, nullptr, nullptr);
@@ -375,7 +391,8 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
         double* yh = pin_.get(m);
         for (size_t jj = 0; jj < k; ++jj) yh[jj] = y[jj] * sig[jj];
         NUMA_CUDA(cudaMemcpyAsync(ydev, yh, k * sizeof(double), cudaMemcpyHostToDevice, ctx_.stream));
-        k_combine_add<<<eg, 256, k * sizeof(double), ctx_.stream>>>(Z_.p, N, (int)k, ydev, x, N);
+        if (z32) k_combine_add<float><<<eg, 256, k * sizeof(double), ctx_.stream>>>(Z32_.p, N, (int)k, ydev, x, N);
+        else k_combine_add<double><<<eg, 256, k * sizeof(double), ctx_.stream>>>(Z_.p, N, (int)k, ydev, x, N);
         ctx_.count_launch();
         ctx_.check_launch("gmres update (lazy)");
         if (res.rel_res <= o.rtol) {

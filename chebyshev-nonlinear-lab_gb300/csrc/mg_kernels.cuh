@@ -224,13 +224,14 @@ enum SplitPass { kPassFull = 0, kPassFirst = 1, kPassLastZ = 2 };
 // pointers (they never overlap).
 //   kPassFirst: x is zero before the pass, x = bs / 6.
 //   kPassLastZ: the final pass of the cycle: x is not stored; z (FP64, natural layout) receives
-//               both members of the pair (the other member holds its value from the previous pass).
+//               both members of the pair (the other member holds its value from the previous pass),
+//               or z32 (FP32) the same values unwidened, for consumers that work in FP32.
 //   NN > 0: the grid size is a compile-time constant, so every neighbour offset is an immediate of
 //           the load instruction (one add per point forms the base m + c).
 template <int MODE, int ICH, int NN>
 __global__ void __launch_bounds__(BX* BY) k_pass_split(float* __restrict__ own, const float* __restrict__ oth,
                                                        const float* __restrict__ bown, double* __restrict__ z,
-                                                       Split g, int c) {
+                                                       Split g, int c, float* __restrict__ z32 = nullptr) {
     const int kk = blockIdx.x * BX + threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
     const int n = NN > 0 ? NN : g.n;
@@ -267,7 +268,11 @@ __global__ void __launch_bounds__(BX* BY) k_pass_split(float* __restrict__ own, 
         const int m = L >> 1;
         if (MODE == kPassLastZ) {
             const int ko = k ^ 1;
-            if (ko < n) z[L - k + ko] = f32_to_f64(ko > k ? v_kp[s] : v_km[s]);
+            if (ko < n) {
+                const float vo = ko > k ? v_kp[s] : v_km[s];
+                if (z) z[L - k + ko] = f32_to_f64(vo);
+                if (z32) z32[L - k + ko] = vo;
+            }
         }
         if (k < n) {
             float v;
@@ -283,15 +288,20 @@ __global__ void __launch_bounds__(BX* BY) k_pass_split(float* __restrict__ own, 
                 acc = acc + ((k + 1 < n) ? v_kp[s] : 0.0f);
                 v = div6(acc);
             }
-            if (MODE == kPassLastZ) z[L] = f32_to_f64(v);
-            else own[m] = v;
+            if (MODE == kPassLastZ) {
+                if (z) z[L] = f32_to_f64(v);
+                if (z32) z32[L] = v;
+            } else {
+                own[m] = v;
+            }
         }
     }
 }
 
 // Launches one colour pass on a split level: planes per thread 4 above 63 points, else 1.
 template <int MODE>
-inline void launch_pass_split(float* x, const float* bs, double* z, const Split& g, int c, cudaStream_t st) {
+inline void launch_pass_split(float* x, const float* bs, double* z, const Split& g, int c, cudaStream_t st,
+                              float* z32 = nullptr) {
     float* own = x + (c ? g.half : 0);
     const float* oth = x + (c ? 0 : g.half);
     const float* bown = bs + (c ? g.half : 0);
@@ -299,12 +309,12 @@ inline void launch_pass_split(float* x, const float* bs, double* z, const Split&
     const dim3 blk(BX, BY);
     if (n >= 64) {
         const dim3 grid(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, (n + 3) / 4);
-        if (n == 255) k_pass_split<MODE, 4, 255><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c);
-        else if (n == 127) k_pass_split<MODE, 4, 127><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c);
-        else k_pass_split<MODE, 4, 0><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c);
+        if (n == 255) k_pass_split<MODE, 4, 255><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c, z32);
+        else if (n == 127) k_pass_split<MODE, 4, 127><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c, z32);
+        else k_pass_split<MODE, 4, 0><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c, z32);
     } else {
         const dim3 grid(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n);
-        k_pass_split<MODE, 1, 0><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c);
+        k_pass_split<MODE, 1, 0><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c, z32);
     }
 }
 

@@ -62,6 +62,12 @@ public:
     }
     // out = F''(x)[v, v] at an iterate with its cache.
     virtual void d2(const double* x, const double* cache, const double* v, double* out) = 0;
+    // The bound product in FP32 from an FP32 v, where bind() selected an FP32 form (has_jvp32).
+    virtual bool has_jvp32() const { return false; }
+    virtual void jvp_bound32(const float* v32, double* out) {
+        (void)v32;
+        (void)out;
+    }
 
     // Finite-difference forms of operators/operator.hpp:101-134 over eval.  f0 = F(x) must be
     // supplied (the same vector the reference recomputes inside the call); xnorm = ||x|| as a
@@ -100,6 +106,8 @@ public:
     void eval(const double* x, double* out, double* cache, double* norm_out) override;
     void bind(const double* x, const double* cache, int precision) override;
     void jvp_bound(const double* v, double* out) override;
+    bool has_jvp32() const override { return bound_precision_ == NUMA_GPU_FP32; }
+    void jvp_bound32(const float* v32, double* out) override;
     void jvp_at(const double* x, const double* v, double* out) override { jvp_x(x, v, out); }
     void jvp_cached(const double*, const double* cache, const double* v, double* out) override {
         jvp_c(cache, v, out);
@@ -208,6 +216,8 @@ public:
     // FP32 binding: the coefficients (2uv, u^2) of the iterate in FP32; products in FP32 arithmetic
     void bind(const double* x, const double*, int precision) override;
     void jvp_bound(const double* v, double* out) override;
+    bool has_jvp32() const override { return bound_precision_ == NUMA_GPU_FP32; }
+    void jvp_bound32(const float* v32, double* out) override;
     void jvp_at(const double* x, const double* v, double* out) override;
     void d2(const double* x, const double* cache, const double* v, double* out) override;
 
@@ -233,6 +243,9 @@ public:
     void set_state(const double* w);
     // z = V-cycle(r), FP64 planes in and out
     void apply(const double* r, double* z);
+    // z32 = V-cycle(r) in FP32 only, for an FP32 hierarchy with more than one level.
+    bool supports_out32() const { return precision_ == NUMA_GPU_FP32 && levels_.size() > 1; }
+    void apply32(const double* r, float* z32);
     // ms of one finest-level colour pass (CUDA events, reps back-to-back launches)
     double time_finest_pass(int reps);
     struct Level;
@@ -248,6 +261,7 @@ private:
     DeviceArray<double> alias_;
     const double* r0_ = nullptr;
     double* z0_ = nullptr;
+    float* z32_ = nullptr;
     cudaGraphExec_t coarse_exec_ = nullptr;
     uint64_t coarse_kernels_ = 0;
     bool state_set_ = false;
@@ -267,6 +281,9 @@ public:
     int precision() const { return precision_; }
     // z = V-cycle(r); r and z are FP64 device vectors of size n^3 (poisson_mg.hpp:69-80).
     void apply(const double* r, double* z);
+    // z32 = V-cycle(r) in FP32 only (the values apply() widens into z), where supports_out32().
+    bool supports_out32() const;
+    void apply32(const double* r, float* z32);
     // Diagnostic: average time (ms) of one red-black colour pass on the finest level, timed with
     // CUDA events over `reps` back-to-back passes on the context stream.
     double time_finest_pass(int reps);
@@ -297,6 +314,7 @@ private:
     size_t N0_;
     int pre_, post_, precision_;
     std::vector<std::unique_ptr<Level>> levels_;
+    float* z32_out_ = nullptr;        // FP32 output of the current apply32
     DeviceArray<double> scratch_r_;   // residual of the level being restricted (FP64 or FP32 bytes)
     DeviceArray<double> alias_b_;     // copy of r when r and z alias
 };
@@ -339,6 +357,12 @@ public:
         (void)iters;
         (void)rel_res;
     }
+    // z32 = M r in FP32 only (the values apply() would widen into z), where has_apply32().
+    virtual bool has_apply32() const { return false; }
+    virtual void apply32(const double* r, float* z32) {
+        (void)r;
+        (void)z32;
+    }
 };
 
 std::unique_ptr<Provider> make_identity_provider(Context& ctx, size_t N);
@@ -374,10 +398,22 @@ struct KrylovSpace {
 struct LinearOp {
     virtual ~LinearOp() = default;
     virtual void apply(const double* v, double* out) = 0;
+    // out = A v from an FP32 v, where A has an FP32 form.
+    virtual bool has_apply32() const { return false; }
+    virtual void apply32(const float* v32, double* out) {
+        (void)v32;
+        (void)out;
+    }
 };
 struct Precond {
     virtual ~Precond() = default;
     virtual void apply(const double* r, double* z) = 0;
+    // z32 = M r in FP32 only, where M has an FP32 output.
+    virtual bool has_apply32() const { return false; }
+    virtual void apply32(const double* r, float* z32) {
+        (void)r;
+        (void)z32;
+    }
     // Called by GMRES after each Arnoldi step with the iteration count of the solve and the relative
     // residual estimate (a preconditioner may change strategy on stagnation, as FGMRES allows).
     virtual void progress(size_t iters, double rel_res) {
@@ -417,6 +453,7 @@ private:
     Context& ctx_;
     size_t N_;
     DeviceArray<double> V_, Z_, w_, r_, comb_, z_, rrec_;
+    DeviceArray<float> Z32_;  // FGMRES preconditioned vectors in FP32 (FP32 preconditioner and product)
     PinnedBuf pin_;
 };
 

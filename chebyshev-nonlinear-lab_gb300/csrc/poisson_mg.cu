@@ -293,7 +293,8 @@ void PoissonMG::cycle32(size_t l) {
         if (split) {
             if (first && fused_first) return;  // already written by the producer of b
             if (first) launch_pass_split<kPassFirst>(x, bs, nullptr, g, colour, s);
-            else if (last && z) launch_pass_split<kPassLastZ>(x, bs, z, g, colour, s);
+            else if (last && (z || (finest && z32_out_)))
+                launch_pass_split<kPassLastZ>(x, bs, z, g, colour, s, finest ? z32_out_ : nullptr);
             else launch_pass_split<kPassFull>(x, bs, nullptr, g, colour, s);
         } else {
             if (first) k_rbgs<float, true, false><<<cgrid, blk, 0, s>>>(x, bs, nullptr, n, colour);
@@ -360,6 +361,24 @@ void PoissonMG::cycle32(size_t l) {
     for (int sw = 0; sw < post_; ++sw) sweep(1, false, sw == post_ - 1);
     if (z && post_ == 0) out_z();
     ctx_.check_launch("mg cycle (fp32)");
+}
+
+// The FP32 cycle's finest level ends with a split pass that writes the output (odd n, a coarser
+// level, post-smoothing): it can write z32 instead of z.
+bool PoissonMG::supports_out32() const {
+    return precision_ == NUMA_GPU_FP32 && (levels_[0]->n & 1) && levels_.size() > 1 && post_ > 0 && tail_l_ != 0;
+}
+
+void PoissonMG::apply32(const double* r, float* z32) {
+    if (!supports_out32()) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "PoissonMG: no FP32 output for this hierarchy");
+    z32_out_ = z32;
+    try {
+        apply(r, nullptr);
+    } catch (...) {
+        z32_out_ = nullptr;
+        throw;
+    }
+    z32_out_ = nullptr;
 }
 
 void PoissonMG::apply(const double* r, double* z) {
