@@ -35,6 +35,8 @@ struct B1Geom {
 // F(w) (brusselator1d.hpp:47-69): boundary values u = 1, v = 3 outside the grid.
 __global__ void __launch_bounds__(256) k_b1_eval(const double* __restrict__ w, const double* __restrict__ prev,
                                                  double* __restrict__ out, B1Geom G) {
+    pdl_wait();
+    pdl_trigger();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = G.n;
     if (i >= n) return;
@@ -50,6 +52,8 @@ __global__ void __launch_bounds__(256) k_b1_eval(const double* __restrict__ w, c
 // F'(w) d (:71-98): a direction is zero outside the grid.
 __global__ void __launch_bounds__(256) k_b1_jvp(const double* __restrict__ w, const double* __restrict__ d,
                                                 double* __restrict__ out, B1Geom G) {
+    pdl_wait();
+    pdl_trigger();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = G.n;
     if (i >= n) return;
@@ -65,6 +69,8 @@ __global__ void __launch_bounds__(256) k_b1_jvp(const double* __restrict__ w, co
 // F''(w)[d, d] = (-q, q), q = 2 v du^2 + 4 u du dv (:100-118).  Also the 2D operator's (any plane size).
 __global__ void __launch_bounds__(256) k_bruss_d2(const double* __restrict__ w, const double* __restrict__ d,
                                                   double* __restrict__ out, size_t m) {
+    pdl_wait();
+    pdl_trigger();
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     const double u = w[i], v = w[m + i], du = d[i], dv = d[m + i];
@@ -75,6 +81,8 @@ __global__ void __launch_bounds__(256) k_bruss_d2(const double* __restrict__ w, 
 
 // The 2x2 point blocks without the off-diagonal diffusion (:120-141), one plane each.
 __global__ void __launch_bounds__(256) k_b1_blocks(const double* __restrict__ w, double* __restrict__ a, B1Geom G) {
+    pdl_wait();
+    pdl_trigger();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = G.n;
     if (i >= n) return;
@@ -89,6 +97,8 @@ __global__ void __launch_bounds__(256) k_b1_blocks(const double* __restrict__ w,
 // finite or below 1e-14 in magnitude.
 __global__ void __launch_bounds__(256) k_b1_block_apply(const double* __restrict__ a, const double* __restrict__ r,
                                                         double* __restrict__ z, int n) {
+    pdl_wait();
+    pdl_trigger();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double a11 = a[i], a12 = a[n + i], a21 = a[2 * n + i], a22 = a[3 * n + i];
@@ -127,6 +137,8 @@ __device__ __forceinline__ double lap5(const double* __restrict__ a, int n, int 
 template <bool NORM>
 __global__ void __launch_bounds__(256) k_b2_eval(const double* __restrict__ w, const double* __restrict__ prev,
                                                  double* __restrict__ out, B2Geom G, RedArgs red, double* norm_out) {
+    pdl_wait();
+    pdl_trigger();
     const int n = G.n;
     const size_t nn = (size_t)n * n;
     const int j = blockIdx.x * 32 + threadIdx.x;
@@ -157,6 +169,8 @@ __global__ void __launch_bounds__(256) k_b2_eval(const double* __restrict__ w, c
 //   (J d)_u = fma(-u^2, dv, fma(-D_u h^-2, L du, a11 du)),  (J d)_v = fma(a22, dv, fma(a21, du, -D_v h^-2 L dv)).
 __global__ void __launch_bounds__(256) k_b2_jvp(const double* __restrict__ w, const double* __restrict__ d,
                                                 double* __restrict__ out, B2Geom G) {
+    pdl_wait();
+    pdl_trigger();
     const int n = G.n;
     const size_t nn = (size_t)n * n;
     const int j = blockIdx.x * 32 + threadIdx.x;
@@ -174,6 +188,8 @@ __global__ void __launch_bounds__(256) k_b2_jvp(const double* __restrict__ w, co
 
 // The FP32 Jacobian product's coefficients at the iterate: (2uv, u^2) per point, in FP32 arithmetic.
 __global__ void __launch_bounds__(256) k_b2_coef32(const double* __restrict__ w, size_t nn, float2* __restrict__ c) {
+    pdl_wait();
+    pdl_trigger();
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nn) return;
     const float u = f64_to_f32(w[p]), v = f64_to_f32(w[nn + p]);  // FP32 from the rounded state
@@ -194,6 +210,8 @@ __device__ __forceinline__ float to_f32(float x) { return x; }
 template <class VT>
 __global__ void __launch_bounds__(256) k_b2_jvp32(const float2* __restrict__ coef, const VT* __restrict__ d,
                                                   double* __restrict__ out, B2Geom32 G) {
+    pdl_wait();
+    pdl_trigger();
     constexpr int TX = 32, TY = 8;
     __shared__ float tu[TY + 2][TX + 3], tv[TY + 2][TX + 3];
     const int n = G.n;
@@ -331,6 +349,8 @@ template <class T, int MODE>
 __global__ void __launch_bounds__(256) k_bmg_pass(T* __restrict__ X, T* __restrict__ Bv, const T* __restrict__ K,
                                                   LvlArgs<T> L, int colour, const double* __restrict__ r64,
                                                   double* __restrict__ z64, float* __restrict__ z32 = nullptr) {
+    pdl_wait();
+    pdl_trigger();
     const int n = L.n;
     const int jj = blockIdx.x * 32 + threadIdx.x;
     const int i = blockIdx.y * 8 + threadIdx.y;
@@ -408,6 +428,8 @@ __device__ __forceinline__ T fw9(T c, T w, T e, T s, T n, T sw, T se, T nw, T ne
 template <class T>
 __global__ void __launch_bounds__(256) k_bmg_restrict(const T* __restrict__ X, const T* __restrict__ Bv,
                                                       const T* __restrict__ K, LvlArgs<T> L, T* __restrict__ Bc) {
+    pdl_wait();
+    pdl_trigger();
     constexpr int TS = 16, FS = 2 * TS + 1;
     __shared__ T su_s[FS][FS + 1], sv_s[FS][FS + 1];
     const int nf = L.n, nc = nf / 2;
@@ -450,6 +472,8 @@ __device__ __forceinline__ void prolong_point(const T* Xc, int nc, int I, int J,
 
 template <class T>
 __global__ void __launch_bounds__(256) k_bmg_prolong(const T* __restrict__ Xc, int nc, T* __restrict__ Xf) {
+    pdl_wait();
+    pdl_trigger();
     const int J = blockIdx.x * 32 + threadIdx.x;
     const int I = blockIdx.y * 8 + threadIdx.y;
     if (I >= nc || J >= nc) return;
@@ -460,6 +484,8 @@ __global__ void __launch_bounds__(256) k_bmg_prolong(const T* __restrict__ Xc, i
 template <class T>
 __global__ void __launch_bounds__(1024) k_bmg_coarsest(T* __restrict__ X, const T* __restrict__ Bv,
                                                        const T* __restrict__ K, LvlArgs<T> L, int sweeps) {
+    pdl_wait();
+    pdl_trigger();
     const int n = L.n;
     const int nn = n * n;
     const T su = L.su, sv = L.sv, su4 = L.su4, sv4 = L.sv4;
@@ -500,6 +526,8 @@ template <> __device__ __forceinline__ const LvlArgs<float>& tail_args<float>(co
 template <class T>
 __global__ void __launch_bounds__(512, 1) k_bmg_tail(const TailLvl* __restrict__ desc, int count, int pre, int post,
                                                      int sweeps, const T* __restrict__ Bin, T* __restrict__ Xout) {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ __align__(16) unsigned char bmg_smem[];
     T* base = reinterpret_cast<T*>(bmg_smem);
     // Levels with n <= 8 (at most 32 points of a colour) are run by warp 0 alone, separated by
@@ -668,6 +696,8 @@ __device__ __forceinline__ void kfine_point(double u, double v, float c1, float 
 template <class T>
 __global__ void __launch_bounds__(256) k_bmg_kfine(const double* __restrict__ w, size_t nn, T c1, T c2, T B,
                                                    T* __restrict__ K) {
+    pdl_wait();
+    pdl_trigger();
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nn) return;
     Blk<T> k;
@@ -678,6 +708,8 @@ __global__ void __launch_bounds__(256) k_bmg_kfine(const double* __restrict__ w,
 // Full weighting of the four block components to the next coarser level.
 template <class T>
 __global__ void __launch_bounds__(256) k_bmg_krestrict(const T* __restrict__ Kf, int nf, T* __restrict__ Kc) {
+    pdl_wait();
+    pdl_trigger();
     const int nc = nf / 2;
     const int J = blockIdx.x * 32 + threadIdx.x;
     const int I = blockIdx.y * 8 + threadIdx.y;
@@ -703,11 +735,15 @@ __global__ void __launch_bounds__(256) k_bmg_krestrict(const T* __restrict__ Kf,
 // FP64 planes <-> interleaved level pairs (used only when the finest level is also the coarsest).
 template <class T>
 __global__ void k_bmg_in(const double* __restrict__ r, size_t nn, T* __restrict__ B) {
+    pdl_wait();
+    pdl_trigger();
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p < nn) st2(B, p, from_f64<T>(r[p]), from_f64<T>(r[nn + p]));
 }
 template <class T>
 __global__ void k_bmg_out(const T* __restrict__ X, size_t nn, double* __restrict__ z) {
+    pdl_wait();
+    pdl_trigger();
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p < nn) {
         const auto x = ld2(X, p);
@@ -755,32 +791,32 @@ static B1Geom b1_geom(size_t n, double dt, double h2inv) {
 }
 
 void Brusselator1D::eval(const double* x, double* out, double*, double* norm_out) {
-    k_b1_eval<<<(unsigned)((n_ + 255) / 256), 256, 0, ctx_.stream>>>(x, prev_.p, out, b1_geom(n_, dt_, h2inv_));
+    launch_pdl(k_b1_eval, (unsigned)((n_ + 255) / 256), 256, 0, ctx_.stream, x, prev_.p, out, b1_geom(n_, dt_, h2inv_));
     ctx_.count_launch();
     ctx_.check_launch("Brusselator1D eval");
     if (norm_out) dev_norm2(ctx_, out, size(), norm_out);
 }
 
 void Brusselator1D::jvp_at(const double* x, const double* v, double* out) {
-    k_b1_jvp<<<(unsigned)((n_ + 255) / 256), 256, 0, ctx_.stream>>>(x, v, out, b1_geom(n_, dt_, h2inv_));
+    launch_pdl(k_b1_jvp, (unsigned)((n_ + 255) / 256), 256, 0, ctx_.stream, x, v, out, b1_geom(n_, dt_, h2inv_));
     ctx_.count_launch();
     ctx_.check_launch("Brusselator1D jvp");
 }
 
 void Brusselator1D::d2(const double* x, const double*, const double* v, double* out) {
-    k_bruss_d2<<<(unsigned)((n_ + 255) / 256), 256, 0, ctx_.stream>>>(x, v, out, n_);
+    launch_pdl(k_bruss_d2, (unsigned)((n_ + 255) / 256), 256, 0, ctx_.stream, x, v, out, n_);
     ctx_.count_launch();
     ctx_.check_launch("Brusselator1D d2");
 }
 
 void Brusselator1D::blocks(const double* x, double* a) {
-    k_b1_blocks<<<(unsigned)((n_ + 255) / 256), 256, 0, ctx_.stream>>>(x, a, b1_geom(n_, dt_, h2inv_));
+    launch_pdl(k_b1_blocks, (unsigned)((n_ + 255) / 256), 256, 0, ctx_.stream, x, a, b1_geom(n_, dt_, h2inv_));
     ctx_.count_launch();
     ctx_.check_launch("Brusselator1D blocks");
 }
 
 void brusselator_block_apply(Context& ctx, const double* a, const double* r, double* z, size_t n) {
-    k_b1_block_apply<<<(unsigned)((n + 255) / 256), 256, 0, ctx.stream>>>(a, r, z, (int)n);
+    launch_pdl(k_b1_block_apply, (unsigned)((n + 255) / 256), 256, 0, ctx.stream, a, r, z, (int)n);
     ctx.count_launch();
     ctx.check_launch("BrusselatorJacobi apply");
 }
@@ -834,9 +870,9 @@ void Brusselator2D::set_previous(const double* w) { dev_copy(ctx_, w, prev_.p, s
 void Brusselator2D::eval(const double* x, double* out, double*, double* norm_out) {
     const dim3 grid = b2_grid((int)n_);
     if (norm_out)
-        k_b2_eval<true><<<grid, dim3(32, 8), 0, ctx_.stream>>>(x, prev_.p, out, b2_geom(n_, P_), ctx_.red, norm_out);
+        launch_pdl(k_b2_eval<true>, grid, dim3(32, 8), 0, ctx_.stream, x, prev_.p, out, b2_geom(n_, P_), ctx_.red, norm_out);
     else
-        k_b2_eval<false><<<grid, dim3(32, 8), 0, ctx_.stream>>>(x, prev_.p, out, b2_geom(n_, P_), ctx_.red, nullptr);
+        launch_pdl(k_b2_eval<false>, grid, dim3(32, 8), 0, ctx_.stream, x, prev_.p, out, b2_geom(n_, P_), ctx_.red, nullptr);
     ctx_.count_launch();
     ctx_.check_launch("Brusselator2D eval");
 }
@@ -847,7 +883,7 @@ void Brusselator2D::bind(const double* x, const double*, int precision) {
     if (precision == NUMA_GPU_FP32) {
         const size_t nn = n_ * n_;
         coef32_.resize(nn);  // one float2 per point
-        k_b2_coef32<<<(unsigned)((nn + 255) / 256), 256, 0, ctx_.stream>>>(x, nn,
+        launch_pdl(k_b2_coef32, (unsigned)((nn + 255) / 256), 256, 0, ctx_.stream, x, nn,
                                                                           reinterpret_cast<float2*>(coef32_.p));
         ctx_.count_launch();
         ctx_.check_launch("Brusselator2D bind");
@@ -862,7 +898,7 @@ void Brusselator2D::jvp_bound(const double* v, double* out) {
     const B2Geom G = b2_geom(n_, P_);
     const B2Geom32 G32{(int)n_, (float)G.invdt, (float)G.B, (float)G.c1, (float)G.duh, (float)G.dvh};
     const dim3 grid((unsigned)((n_ + 31) / 32), (unsigned)((n_ + 7) / 8));
-    k_b2_jvp32<double><<<grid, dim3(32, 8), 0, ctx_.stream>>>(reinterpret_cast<const float2*>(coef32_.p), v, out,
+    launch_pdl(k_b2_jvp32<double>, grid, dim3(32, 8), 0, ctx_.stream, reinterpret_cast<const float2*>(coef32_.p), v, out,
                                                               G32);
     ctx_.count_launch();
     ctx_.check_launch("Brusselator2D jvp32");
@@ -874,21 +910,21 @@ void Brusselator2D::jvp_bound32(const float* v32, double* out) {
     const B2Geom G = b2_geom(n_, P_);
     const B2Geom32 G32{(int)n_, (float)G.invdt, (float)G.B, (float)G.c1, (float)G.duh, (float)G.dvh};
     const dim3 grid((unsigned)((n_ + 31) / 32), (unsigned)((n_ + 7) / 8));
-    k_b2_jvp32<float><<<grid, dim3(32, 8), 0, ctx_.stream>>>(reinterpret_cast<const float2*>(coef32_.p), v32, out,
+    launch_pdl(k_b2_jvp32<float>, grid, dim3(32, 8), 0, ctx_.stream, reinterpret_cast<const float2*>(coef32_.p), v32, out,
                                                              G32);
     ctx_.count_launch();
     ctx_.check_launch("Brusselator2D jvp32 (fp32 input)");
 }
 
 void Brusselator2D::jvp_at(const double* x, const double* v, double* out) {
-    k_b2_jvp<<<b2_grid((int)n_), dim3(32, 8), 0, ctx_.stream>>>(x, v, out, b2_geom(n_, P_));
+    launch_pdl(k_b2_jvp, b2_grid((int)n_), dim3(32, 8), 0, ctx_.stream, x, v, out, b2_geom(n_, P_));
     ctx_.count_launch();
     ctx_.check_launch("Brusselator2D jvp");
 }
 
 void Brusselator2D::d2(const double* x, const double*, const double* v, double* out) {
     const size_t nn = n_ * n_;
-    k_bruss_d2<<<(unsigned)((nn + 255) / 256), 256, 0, ctx_.stream>>>(x, v, out, nn);
+    launch_pdl(k_bruss_d2, (unsigned)((nn + 255) / 256), 256, 0, ctx_.stream, x, v, out, nn);
     ctx_.count_launch();
     ctx_.check_launch("Brusselator2D d2");
 }
@@ -969,19 +1005,19 @@ void BrussMG2D::set_state(const double* w) {
     const double c1 = 1.0 / P_.dt + (P_.B + 1.0), c2 = 1.0 / P_.dt;
     const unsigned g = (unsigned)((nn + 255) / 256);
     if (precision_ == NUMA_GPU_FP64)
-        k_bmg_kfine<double><<<g, 256, 0, ctx_.stream>>>(w, nn, c1, c2, P_.B, tp<double>(levels_[0]->k));
+        launch_pdl(k_bmg_kfine<double>, g, 256, 0, ctx_.stream, w, nn, c1, c2, P_.B, tp<double>(levels_[0]->k));
     else
-        k_bmg_kfine<float><<<g, 256, 0, ctx_.stream>>>(w, nn, (float)c1, (float)c2, (float)P_.B,
+        launch_pdl(k_bmg_kfine<float>, g, 256, 0, ctx_.stream, w, nn, (float)c1, (float)c2, (float)P_.B,
                                                        tp<float>(levels_[0]->k));
     ctx_.count_launch();
     for (size_t l = 0; l + 1 < levels_.size(); ++l) {
         const int nc = levels_[l + 1]->n;
         const dim3 grid((unsigned)((nc + 31) / 32), (unsigned)((nc + 7) / 8));
         if (precision_ == NUMA_GPU_FP64)
-            k_bmg_krestrict<double><<<grid, dim3(32, 8), 0, ctx_.stream>>>(tp<double>(levels_[l]->k), levels_[l]->n,
+            launch_pdl(k_bmg_krestrict<double>, grid, dim3(32, 8), 0, ctx_.stream, tp<double>(levels_[l]->k), levels_[l]->n,
                                                                           tp<double>(levels_[l + 1]->k));
         else
-            k_bmg_krestrict<float><<<grid, dim3(32, 8), 0, ctx_.stream>>>(tp<float>(levels_[l]->k), levels_[l]->n,
+            launch_pdl(k_bmg_krestrict<float>, grid, dim3(32, 8), 0, ctx_.stream, tp<float>(levels_[l]->k), levels_[l]->n,
                                                                          tp<float>(levels_[l + 1]->k));
         ctx_.count_launch();
     }
@@ -1003,60 +1039,60 @@ void BrussMG2D::cycle(size_t l) {
     const dim3 pgrid((unsigned)((n / 2 + 31) / 32), (unsigned)((n + 7) / 8));
     const size_t nn = (size_t)n * n;
     if ((int)l == tail_first_) {
-        k_bmg_tail<T><<<1, 512, tail_smem_, s>>>(reinterpret_cast<const TailLvl*>(tail_desc_.p), tail_count_, pre_,
+        launch_pdl(k_bmg_tail<T>, 1, 512, tail_smem_, s, reinterpret_cast<const TailLvl*>(tail_desc_.p), tail_count_, pre_,
                                                   post_, kBmgCoarsestSweeps, Bv, X);
         ctx_.count_launch();
         return;
     }
     if (coarsest) {
         if (finest) {
-            k_bmg_in<T><<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(r0_, nn, Bv);
+            launch_pdl(k_bmg_in<T>, (unsigned)((nn + 255) / 256), 256, 0, s, r0_, nn, Bv);
             ctx_.count_launch();
         }
         if (nn <= (size_t)kBmgOneBlockPoints) {
-            k_bmg_coarsest<T><<<1, 1024, 0, s>>>(X, Bv, K, A, kBmgCoarsestSweeps);
+            launch_pdl(k_bmg_coarsest<T>, 1, 1024, 0, s, X, Bv, K, A, kBmgCoarsestSweeps);
             ctx_.count_launch();
         } else {
-            k_bmg_pass<T, kBPassFirst><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 0, nullptr, nullptr);
-            k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 1, nullptr, nullptr);
+            launch_pdl(k_bmg_pass<T, kBPassFirst>, pgrid, blk, 0, s, X, Bv, K, A, 0, nullptr, nullptr, nullptr);
+            launch_pdl(k_bmg_pass<T, kBPassNormal>, pgrid, blk, 0, s, X, Bv, K, A, 1, nullptr, nullptr, nullptr);
             ctx_.count_launch(2);
             for (int k = 1; k < kBmgCoarsestSweeps; ++k) {
-                k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 0, nullptr, nullptr);
-                k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 1, nullptr, nullptr);
+                launch_pdl(k_bmg_pass<T, kBPassNormal>, pgrid, blk, 0, s, X, Bv, K, A, 0, nullptr, nullptr, nullptr);
+                launch_pdl(k_bmg_pass<T, kBPassNormal>, pgrid, blk, 0, s, X, Bv, K, A, 1, nullptr, nullptr, nullptr);
                 ctx_.count_launch(2);
             }
         }
         if (finest) {
-            k_bmg_out<T><<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(X, nn, z0_);
+            launch_pdl(k_bmg_out<T>, (unsigned)((nn + 255) / 256), 256, 0, s, X, nn, z0_);
             ctx_.count_launch();
         }
         return;
     }
     // pre-smoothing: colours 0, 1; the first pass starts from x = 0
-    k_bmg_pass<T, kBPassFirst><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 0, finest ? r0_ : nullptr, nullptr);
-    k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 1, nullptr, nullptr);
+    launch_pdl(k_bmg_pass<T, kBPassFirst>, pgrid, blk, 0, s, X, Bv, K, A, 0, finest ? r0_ : nullptr, nullptr, nullptr);
+    launch_pdl(k_bmg_pass<T, kBPassNormal>, pgrid, blk, 0, s, X, Bv, K, A, 1, nullptr, nullptr, nullptr);
     ctx_.count_launch(2);
     for (int k = 1; k < pre_; ++k) {
-        k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 0, nullptr, nullptr);
-        k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 1, nullptr, nullptr);
+        launch_pdl(k_bmg_pass<T, kBPassNormal>, pgrid, blk, 0, s, X, Bv, K, A, 0, nullptr, nullptr, nullptr);
+        launch_pdl(k_bmg_pass<T, kBPassNormal>, pgrid, blk, 0, s, X, Bv, K, A, 1, nullptr, nullptr, nullptr);
         ctx_.count_launch(2);
     }
     Level& C = *levels_[l + 1];
     const int nc = C.n;
-    k_bmg_restrict<T><<<dim3((unsigned)((nc + 15) / 16), (unsigned)((nc + 15) / 16)), dim3(16, 16), 0, s>>>(
+    launch_pdl(k_bmg_restrict<T>, dim3((unsigned)((nc + 15) / 16), (unsigned)((nc + 15) / 16)), dim3(16, 16), 0, s, 
         X, Bv, K, A, tp<T>(C.b));
     ctx_.count_launch();
     if (finest) coarse_cycle();
     else cycle<T>(l + 1);
-    k_bmg_prolong<T><<<dim3((unsigned)((nc + 31) / 32), (unsigned)((nc + 7) / 8)), blk, 0, s>>>(tp<T>(C.x), nc, X);
+    launch_pdl(k_bmg_prolong<T>, dim3((unsigned)((nc + 31) / 32), (unsigned)((nc + 7) / 8)), blk, 0, s, tp<T>(C.x), nc, X);
     ctx_.count_launch();
     // post-smoothing: colours 1, 0; the very last pass of the finest level writes z
     for (int k = 0; k < post_; ++k) {
-        k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 1, nullptr, nullptr);
+        launch_pdl(k_bmg_pass<T, kBPassNormal>, pgrid, blk, 0, s, X, Bv, K, A, 1, nullptr, nullptr, nullptr);
         if (finest && k + 1 == post_)
-            k_bmg_pass<T, kBPassLast><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 0, nullptr, z0_, z32_);
+            launch_pdl(k_bmg_pass<T, kBPassLast>, pgrid, blk, 0, s, X, Bv, K, A, 0, nullptr, z0_, z32_);
         else
-            k_bmg_pass<T, kBPassNormal><<<pgrid, blk, 0, s>>>(X, Bv, K, A, 0, nullptr, nullptr);
+            launch_pdl(k_bmg_pass<T, kBPassNormal>, pgrid, blk, 0, s, X, Bv, K, A, 0, nullptr, nullptr, nullptr);
         ctx_.count_launch(2);
     }
 }
@@ -1107,13 +1143,11 @@ double BrussMG2D::time_finest_pass(int reps) {
     NUMA_CUDA(cudaEventCreate(&b));
     auto launch = [&](int colour) {
         if (precision_ == NUMA_GPU_FP64)
-            k_bmg_pass<double, kBPassNormal><<<pgrid, blk, 0, ctx_.stream>>>(tp<double>(L.x), tp<double>(L.b),
-                                                                             tp<double>(L.k), A64, colour, nullptr,
-                                                                             nullptr);
+            launch_pdl(k_bmg_pass<double, kBPassNormal>, pgrid, blk, 0, ctx_.stream, tp<double>(L.x),
+                       tp<double>(L.b), tp<double>(L.k), A64, colour, nullptr, nullptr, nullptr);
         else
-            k_bmg_pass<float, kBPassNormal><<<pgrid, blk, 0, ctx_.stream>>>(tp<float>(L.x), tp<float>(L.b),
-                                                                            tp<float>(L.k), A32, colour, nullptr,
-                                                                            nullptr);
+            launch_pdl(k_bmg_pass<float, kBPassNormal>, pgrid, blk, 0, ctx_.stream, tp<float>(L.x), tp<float>(L.b),
+                       tp<float>(L.k), A32, colour, nullptr, nullptr, nullptr);
     };
     launch(0);
     NUMA_CUDA(cudaEventRecord(a, ctx_.stream));

@@ -15,6 +15,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <mutex>
+#include <utility>
 #include <stdexcept>
 #include <string>
 
@@ -290,6 +291,31 @@ struct Context {
     void count_launch(unsigned n = 1) { launches += n; }
     void check_launch(const char* what);
 };
+// Programmatic dependent launch.  A kernel launched by launch_pdl may be scheduled while its
+// predecessor on the stream is still running; it must call pdl_wait() before it touches memory
+// (griddepcontrol.wait returns once every prerequisite grid has completed and its writes are
+// visible).  pdl_trigger() lets this grid's own dependents be scheduled once all its CTAs have
+// issued it; they still wait for its completion.  Both are no-ops in a kernel launched normally.
+// In a chain of small kernels (the coarse levels of a V-cycle) this hides the launch latency
+// between consecutive kernels, on a stream or inside a captured graph.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <class... KArgs, class... Args>
+void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    NUMA_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
+}
+
 // Largest dynamic shared memory a block may opt in to on the context's device (bytes).
 int smem_optin_limit(Context& ctx);
 

@@ -19,6 +19,8 @@ template <class T> __device__ __forceinline__ T zero() { return T(0); }
 template <class T, bool FIRST, bool OUT_Z>
 __global__ void __launch_bounds__(BX* BY) k_rbgs(T* __restrict__ x, const T* __restrict__ bs, double* __restrict__ z,
                                                  int n, int colour) {
+    pdl_wait();
+    pdl_trigger();
     const int kk = blockIdx.x * BX + threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
     const int i = blockIdx.z;
@@ -48,6 +50,8 @@ __global__ void __launch_bounds__(BX* BY) k_rbgs(T* __restrict__ x, const T* __r
 template <class T>
 __global__ void __launch_bounds__(BX* BY) k_residual(const T* __restrict__ x, const T* __restrict__ b,
                                                      T* __restrict__ r, int n, int ichunk, T h2inv) {
+    pdl_wait();
+    pdl_trigger();
     const int k = blockIdx.x * BX + threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
     const int i0 = blockIdx.z * ichunk;
@@ -83,6 +87,8 @@ __device__ __forceinline__ float fma_t(float a, float b, float c) { return __fma
 template <class T>
 __global__ void __launch_bounds__(BX* BY) k_restrict(const T* __restrict__ rf, T* __restrict__ bc,
                                                      T* __restrict__ bsc, int nf, int nc, double inv_c) {
+    pdl_wait();
+    pdl_trigger();
     const int K = blockIdx.x * BX + threadIdx.x;
     const int J = blockIdx.y * BY + threadIdx.y;
     const int I = blockIdx.z;
@@ -130,6 +136,8 @@ __device__ __forceinline__ int interp(int f, int nc, int (&idx)[2]) {
 // products are powers of two, so w * xc is exact and the FMA equals the reference's sum.
 template <class T, bool COLOUR0_ONLY>
 __global__ void __launch_bounds__(BX* BY) k_prolong(const T* __restrict__ xc, T* __restrict__ xf, int nc, int nf) {
+    pdl_wait();
+    pdl_trigger();
     const int t = blockIdx.x * BX + threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
     const int i = blockIdx.z;
@@ -153,6 +161,8 @@ __global__ void __launch_bounds__(BX* BY) k_prolong(const T* __restrict__ xc, T*
 
 // bs = r * inv at the finest FP64 level.
 __global__ void k_scale_in64(const double* __restrict__ r, double* __restrict__ bs, double inv, size_t N) {
+    pdl_wait();
+    pdl_trigger();
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) bs[p] = r[p] * inv;
 }
@@ -161,6 +171,8 @@ __global__ void k_scale_in64(const double* __restrict__ r, double* __restrict__ 
 // arithmetic: no FP64 instruction).
 __global__ void k_scale_in32(const double* __restrict__ r, float* __restrict__ b, float* __restrict__ bs, float inv,
                              size_t N) {
+    pdl_wait();
+    pdl_trigger();
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) {
         const float v = f64_to_f32(r[p]);
@@ -170,6 +182,8 @@ __global__ void k_scale_in32(const double* __restrict__ r, float* __restrict__ b
 }
 
 __global__ void k_to64(const float* __restrict__ x, double* __restrict__ z, size_t N) {
+    pdl_wait();
+    pdl_trigger();
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) z[p] = f32_to_f64(x[p]);
 }
@@ -177,6 +191,8 @@ __global__ void k_to64(const float* __restrict__ x, double* __restrict__ z, size
 // Coarsest level with one point: x = b / (6 h^-2) (poisson_mg.hpp:267-269).
 template <class T>
 __global__ void k_single(const T* __restrict__ b, T* __restrict__ x, double* __restrict__ z, double six_h2inv) {
+    pdl_wait();
+    pdl_trigger();
     const T v = (T)((double)b[0] / six_h2inv);
     x[0] = v;
     if (z) z[0] = (double)v;
@@ -232,6 +248,8 @@ template <int MODE, int ICH, int NN>
 __global__ void __launch_bounds__(BX* BY) k_pass_split(float* __restrict__ own, const float* __restrict__ oth,
                                                        const float* __restrict__ bown, double* __restrict__ z,
                                                        Split g, int c, float* __restrict__ z32 = nullptr) {
+    pdl_wait();
+    pdl_trigger();
     const int kk = blockIdx.x * BX + threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
     const int n = NN > 0 ? NN : g.n;
@@ -309,12 +327,12 @@ inline void launch_pass_split(float* x, const float* bs, double* z, const Split&
     const dim3 blk(BX, BY);
     if (n >= 64) {
         const dim3 grid(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, (n + 3) / 4);
-        if (n == 255) k_pass_split<MODE, 4, 255><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c, z32);
-        else if (n == 127) k_pass_split<MODE, 4, 127><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c, z32);
-        else k_pass_split<MODE, 4, 0><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c, z32);
+        if (n == 255) launch_pdl(k_pass_split<MODE, 4, 255>, grid, blk, 0, st, own, oth, bown, z, g, c, z32);
+        else if (n == 127) launch_pdl(k_pass_split<MODE, 4, 127>, grid, blk, 0, st, own, oth, bown, z, g, c, z32);
+        else launch_pdl(k_pass_split<MODE, 4, 0>, grid, blk, 0, st, own, oth, bown, z, g, c, z32);
     } else {
         const dim3 grid(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n);
-        k_pass_split<MODE, 1, 0><<<grid, blk, 0, st>>>(own, oth, bown, z, g, c, z32);
+        launch_pdl(k_pass_split<MODE, 1, 0>, grid, blk, 0, st, own, oth, bown, z, g, c, z32);
     }
 }
 
@@ -326,6 +344,8 @@ inline void launch_pass_split(float* x, const float* bs, double* z, const Split&
 template <int ICH>
 __global__ void __launch_bounds__(BX* BY) k_residual_split(const float* __restrict__ x, const float* __restrict__ b,
                                                            float* __restrict__ r, Split g, float h2inv) {
+    pdl_wait();
+    pdl_trigger();
     const int kk = blockIdx.x * BX + threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
     const int n = g.n;
@@ -397,6 +417,8 @@ template <bool FIRST_X>
 __global__ void __launch_bounds__(BX* BY) k_restrict_split(const float* __restrict__ rf, float* __restrict__ bc,
                                                            float* __restrict__ bsc, float* __restrict__ xc, int nf,
                                                            int nc, int halfc, float inv_c) {
+    pdl_wait();
+    pdl_trigger();
     const int K = blockIdx.x * BX + threadIdx.x;
     const int J = blockIdx.y * BY + threadIdx.y;
     const int I = blockIdx.z;
@@ -464,6 +486,8 @@ __device__ __forceinline__ void prolong_point(const float (&X)[2][2][2], const b
 template <bool SPLIT_C, bool ALL>
 __global__ void __launch_bounds__(BX* BY) k_prolong_split(const float* __restrict__ xc, float* __restrict__ xf,
                                                           int nc, int halfc, int nf, int halff) {
+    pdl_wait();
+    pdl_trigger();
     const int K = blockIdx.x * BX + threadIdx.x;
     const int J = blockIdx.y * BY + threadIdx.y;
     const int I = blockIdx.z;
@@ -502,6 +526,8 @@ __global__ void __launch_bounds__(BX* BY) k_prolong_split(const float* __restric
 template <bool WRITE_X>
 __global__ void k_scale_in32_split(const double* __restrict__ r, float* __restrict__ b, float* __restrict__ bs,
                                    float* __restrict__ x, float inv, int N, int half) {
+    pdl_wait();
+    pdl_trigger();
     const int stride = gridDim.x * blockDim.x;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < half; t += stride) {
         const int L = 2 * t;
@@ -520,6 +546,8 @@ __global__ void k_scale_in32_split(const double* __restrict__ r, float* __restri
 
 // z (FP64, natural) = x (FP32, split)
 __global__ void k_to64_split(const float* __restrict__ x, double* __restrict__ z, int N, int half) {
+    pdl_wait();
+    pdl_trigger();
     const int stride = gridDim.x * blockDim.x;
     for (int L = blockIdx.x * blockDim.x + threadIdx.x; L < N; L += stride) z[L] = f32_to_f64(x[split_at(L, half)]);
 }
@@ -636,6 +664,8 @@ __device__ void tail_prolong(const T* __restrict__ xc, T* __restrict__ xf, int n
 template <class T, bool SPLIT_IO>
 __global__ void __launch_bounds__(512) k_mg_tail(const T* __restrict__ b_g, const T* __restrict__ bs_g,
                                                  T* __restrict__ x_g, TailParams tp) {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ __align__(16) unsigned char tail_smem[];
     T* base = reinterpret_cast<T*>(tail_smem);
     T *X[kMaxTail], *B[kMaxTail], *BS[kMaxTail];

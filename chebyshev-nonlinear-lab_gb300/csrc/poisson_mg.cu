@@ -138,8 +138,8 @@ void PoissonMG::launch_tail32() {
     tp.post = post_;
     const bool split = (L.n & 1) != 0;
     tp.half = split ? make_split(L.n).half : 0;
-    if (split) k_mg_tail<float, true><<<1, 512, tail_smem_, ctx_.stream>>>(L.b32.p, L.bs32.p, L.xs, tp);
-    else k_mg_tail<float, false><<<1, 512, tail_smem_, ctx_.stream>>>(L.b32.p, L.bs32.p, L.xs, tp);
+    if (split) launch_pdl(k_mg_tail<float, true>, 1, 512, tail_smem_, ctx_.stream, L.b32.p, L.bs32.p, L.xs, tp);
+    else launch_pdl(k_mg_tail<float, false>, 1, 512, tail_smem_, ctx_.stream, L.b32.p, L.bs32.p, L.xs, tp);
     ctx_.count_launch();
     L.cur32 = L.xs;
     ctx_.check_launch("mg tail (fp32)");
@@ -191,10 +191,10 @@ void PoissonMG::cycle(size_t l) {
     const dim3 cgrid(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n);
 
     auto pass = [&](int colour, bool first, bool outz) {
-        if (first && outz) k_rbgs<T, true, true><<<cgrid, blk, 0, s>>>(x, bs, z, n, colour);
-        else if (first) k_rbgs<T, true, false><<<cgrid, blk, 0, s>>>(x, bs, nullptr, n, colour);
-        else if (outz) k_rbgs<T, false, true><<<cgrid, blk, 0, s>>>(x, bs, z, n, colour);
-        else k_rbgs<T, false, false><<<cgrid, blk, 0, s>>>(x, bs, nullptr, n, colour);
+        if (first && outz) launch_pdl(k_rbgs<T, true, true>, cgrid, blk, 0, s, x, bs, z, n, colour);
+        else if (first) launch_pdl(k_rbgs<T, true, false>, cgrid, blk, 0, s, x, bs, nullptr, n, colour);
+        else if (outz) launch_pdl(k_rbgs<T, false, true>, cgrid, blk, 0, s, x, bs, z, n, colour);
+        else launch_pdl(k_rbgs<T, false, false>, cgrid, blk, 0, s, x, bs, nullptr, n, colour);
         ctx_.count_launch();
     };
     // order 0: colour 0 then 1; order 1: colour 1 then 0 (poisson_mg.hpp:103-106)
@@ -206,7 +206,7 @@ void PoissonMG::cycle(size_t l) {
 
     if (l + 1 == levels_.size()) {
         if (n == 1) {
-            k_single<T><<<1, 1, 0, s>>>(b, x, z, 6.0 * L.h2inv);
+            launch_pdl(k_single<T>, 1, 1, 0, s, b, x, z, 6.0 * L.h2inv);
             ctx_.count_launch();
         } else {
             for (int sw = 0; sw < 30; ++sw) sweep(sw % 2, sw == 0, z != nullptr && sw == 29);
@@ -222,14 +222,14 @@ void PoissonMG::cycle(size_t l) {
     {
         const int ichunk = n >= 64 ? 8 : 1;
         const dim3 g((n + BX - 1) / BX, (n + BY - 1) / BY, (n + ichunk - 1) / ichunk);
-        k_residual<T><<<g, blk, 0, s>>>(x, b, r, n, ichunk, (T)L.h2inv);
+        launch_pdl(k_residual<T>, g, blk, 0, s, x, b, r, n, ichunk, (T)L.h2inv);
         ctx_.count_launch();
     }
     Level& C = *levels_[l + 1];
     const int nc = C.n;
     {
         const dim3 g((nc + BX - 1) / BX, (nc + BY - 1) / BY, nc);
-        k_restrict<T><<<g, blk, 0, s>>>(r, bp<T>(C), bsp<T>(C), n, nc, C.inv);
+        launch_pdl(k_restrict<T>, g, blk, 0, s, r, bp<T>(C), bsp<T>(C), n, nc, C.inv);
         ctx_.count_launch();
     }
     ctx_.check_launch("mg restrict");
@@ -237,15 +237,15 @@ void PoissonMG::cycle(size_t l) {
     else cycle<T>(l + 1);
     if (post_ > 0) {
         const dim3 g(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n);
-        k_prolong<T, true><<<g, blk, 0, s>>>(xp<T>(C), x, nc, n);
+        launch_pdl(k_prolong<T, true>, g, blk, 0, s, xp<T>(C), x, nc, n);
     } else {
         const dim3 g((n + BX - 1) / BX, (n + BY - 1) / BY, n);
-        k_prolong<T, false><<<g, blk, 0, s>>>(xp<T>(C), x, nc, n);
+        launch_pdl(k_prolong<T, false>, g, blk, 0, s, xp<T>(C), x, nc, n);
     }
     ctx_.count_launch();
     for (int sw = 0; sw < post_; ++sw) sweep(1, false, z != nullptr && sw == post_ - 1);
     if (z != nullptr && post_ == 0) {
-        k_to64<<<ew_grid(ctx_, Nl), 256, 0, s>>>(reinterpret_cast<const float*>(x), z, Nl);
+        launch_pdl(k_to64, ew_grid(ctx_, Nl), 256, 0, s, reinterpret_cast<const float*>(x), z, Nl);
         ctx_.count_launch();
     }
     ctx_.check_launch("mg cycle");
@@ -297,8 +297,8 @@ void PoissonMG::cycle32(size_t l) {
                 launch_pass_split<kPassLastZ>(x, bs, z, g, colour, s, finest ? z32_out_ : nullptr);
             else launch_pass_split<kPassFull>(x, bs, nullptr, g, colour, s);
         } else {
-            if (first) k_rbgs<float, true, false><<<cgrid, blk, 0, s>>>(x, bs, nullptr, n, colour);
-            else k_rbgs<float, false, false><<<cgrid, blk, 0, s>>>(x, bs, nullptr, n, colour);
+            if (first) launch_pdl(k_rbgs<float, true, false>, cgrid, blk, 0, s, x, bs, nullptr, n, colour);
+            else launch_pdl(k_rbgs<float, false, false>, cgrid, blk, 0, s, x, bs, nullptr, n, colour);
         }
         ctx_.count_launch();
     };
@@ -309,14 +309,14 @@ void PoissonMG::cycle32(size_t l) {
     };
     // z from x when no pass wrote it
     auto out_z = [&]() {
-        if (split) k_to64_split<<<ew_grid(ctx_, Nl), 256, 0, s>>>(x, z, (int)Nl, g.half);
-        else k_to64<<<ew_grid(ctx_, Nl), 256, 0, s>>>(x, z, Nl);
+        if (split) launch_pdl(k_to64_split, ew_grid(ctx_, Nl), 256, 0, s, x, z, (int)Nl, g.half);
+        else launch_pdl(k_to64, ew_grid(ctx_, Nl), 256, 0, s, x, z, Nl);
         ctx_.count_launch();
     };
     L.cur32 = x;
     if (l + 1 == levels_.size()) {
         if (n == 1) {
-            k_single<float><<<1, 1, 0, s>>>(b, x, z, 6.0 * L.h2inv);
+            launch_pdl(k_single<float>, 1, 1, 0, s, b, x, z, 6.0 * L.h2inv);
             ctx_.count_launch();
         } else {
             for (int sw = 0; sw < 30; ++sw) sweep(sw % 2, sw == 0, sw == 29);
@@ -331,8 +331,8 @@ void PoissonMG::cycle32(size_t l) {
     float* r = reinterpret_cast<float*>(scratch_r_.p);
     {
         const dim3 rgd(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, (n + ich - 1) / ich);
-        if (ich == 4) k_residual_split<4><<<rgd, blk, 0, s>>>(x, b, r, g, (float)L.h2inv);
-        else k_residual_split<1><<<rgd, blk, 0, s>>>(x, b, r, g, (float)L.h2inv);
+        if (ich == 4) launch_pdl(k_residual_split<4>, rgd, blk, 0, s, x, b, r, g, (float)L.h2inv);
+        else launch_pdl(k_residual_split<1>, rgd, blk, 0, s, x, b, r, g, (float)L.h2inv);
         ctx_.count_launch();
     }
     Level& C = *levels_[l + 1];
@@ -341,21 +341,21 @@ void PoissonMG::cycle32(size_t l) {
     const Split gc = make_split(nc);
     const dim3 rg((nc + BX - 1) / BX, (nc + BY - 1) / BY, nc);
     if (csplit && first_fused32(l + 1))
-        k_restrict_split<true><<<rg, blk, 0, s>>>(r, C.b32.p, C.bs32.p, C.xs, n, nc, gc.half, (float)C.inv);
+        launch_pdl(k_restrict_split<true>, rg, blk, 0, s, r, C.b32.p, C.bs32.p, C.xs, n, nc, gc.half, (float)C.inv);
     else if (csplit)
-        k_restrict_split<false><<<rg, blk, 0, s>>>(r, C.b32.p, C.bs32.p, C.xs, n, nc, gc.half, (float)C.inv);
+        launch_pdl(k_restrict_split<false>, rg, blk, 0, s, r, C.b32.p, C.bs32.p, C.xs, n, nc, gc.half, (float)C.inv);
     else
-        k_restrict<float><<<rg, blk, 0, s>>>(r, C.b32.p, C.bs32.p, n, nc, C.inv);
+        launch_pdl(k_restrict<float>, rg, blk, 0, s, r, C.b32.p, C.bs32.p, n, nc, C.inv);
     ctx_.count_launch();
     if (l == 0) coarse_cycle();
     else cycle32(l + 1);
     const dim3 cg((nc + 1 + BX - 1) / BX, (nc + 1 + BY - 1) / BY, nc + 1);
     if (post_ > 0) {
-        if (csplit) k_prolong_split<true, false><<<cg, blk, 0, s>>>(C.cur32, x, nc, gc.half, n, g.half);
-        else k_prolong_split<false, false><<<cg, blk, 0, s>>>(C.cur32, x, nc, gc.half, n, g.half);
+        if (csplit) launch_pdl(k_prolong_split<true, false>, cg, blk, 0, s, C.cur32, x, nc, gc.half, n, g.half);
+        else launch_pdl(k_prolong_split<false, false>, cg, blk, 0, s, C.cur32, x, nc, gc.half, n, g.half);
     } else {
-        if (csplit) k_prolong_split<true, true><<<cg, blk, 0, s>>>(C.cur32, x, nc, gc.half, n, g.half);
-        else k_prolong_split<false, true><<<cg, blk, 0, s>>>(C.cur32, x, nc, gc.half, n, g.half);
+        if (csplit) launch_pdl(k_prolong_split<true, true>, cg, blk, 0, s, C.cur32, x, nc, gc.half, n, g.half);
+        else launch_pdl(k_prolong_split<false, true>, cg, blk, 0, s, C.cur32, x, nc, gc.half, n, g.half);
     }
     ctx_.count_launch();
     for (int sw = 0; sw < post_; ++sw) sweep(1, false, sw == post_ - 1);
@@ -391,7 +391,7 @@ void PoissonMG::apply(const double* r, double* z) {
             dev_copy(ctx_, r, alias_b_.p, N);
             b = alias_b_.p;
         }
-        k_scale_in64<<<ew_grid(ctx_, N), 256, 0, ctx_.stream>>>(b, L0.bs64.p, L0.inv, N);
+        launch_pdl(k_scale_in64, ew_grid(ctx_, N), 256, 0, ctx_.stream, b, L0.bs64.p, L0.inv, N);
         ctx_.count_launch();
         x0_ = z;
         b0_ = b;
@@ -403,13 +403,13 @@ void PoissonMG::apply(const double* r, double* z) {
             const Split g = make_split(L0.n);
             const unsigned grid = ew_grid(ctx_, (size_t)g.half);
             if (first_fused32(0))
-                k_scale_in32_split<true><<<grid, 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, L0.xs,
+                launch_pdl(k_scale_in32_split<true>, grid, 256, 0, ctx_.stream, r, L0.b32.p, L0.bs32.p, L0.xs,
                                                                         (float)L0.inv, (int)N, g.half);
             else
-                k_scale_in32_split<false><<<grid, 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, L0.xs,
+                launch_pdl(k_scale_in32_split<false>, grid, 256, 0, ctx_.stream, r, L0.b32.p, L0.bs32.p, L0.xs,
                                                                          (float)L0.inv, (int)N, g.half);
         } else {
-            k_scale_in32<<<ew_grid(ctx_, N), 256, 0, ctx_.stream>>>(r, L0.b32.p, L0.bs32.p, (float)L0.inv, N);
+            launch_pdl(k_scale_in32, ew_grid(ctx_, N), 256, 0, ctx_.stream, r, L0.b32.p, L0.bs32.p, (float)L0.inv, N);
         }
         ctx_.count_launch();
         z0_ = z;
@@ -434,10 +434,10 @@ double PoissonMG::time_finest_pass(int reps) {
         DeviceArray<double> x(N);
         NUMA_CUDA(cudaMemsetAsync(x.p, 0, N * sizeof(double), ctx_.stream));
         NUMA_CUDA(cudaMemsetAsync(L0.bs64.p, 0, N * sizeof(double), ctx_.stream));
-        k_rbgs<double, false, false><<<cgrid, blk, 0, ctx_.stream>>>(x.p, L0.bs64.p, nullptr, n, 0);
+        launch_pdl(k_rbgs<double, false, false>, cgrid, blk, 0, ctx_.stream, x.p, L0.bs64.p, nullptr, n, 0);
         NUMA_CUDA(cudaEventRecord(a, ctx_.stream));
         for (int r = 0; r < reps; ++r)
-            k_rbgs<double, false, false><<<cgrid, blk, 0, ctx_.stream>>>(x.p, L0.bs64.p, nullptr, n, r & 1);
+            launch_pdl(k_rbgs<double, false, false>, cgrid, blk, 0, ctx_.stream, x.p, L0.bs64.p, nullptr, n, r & 1);
         NUMA_CUDA(cudaEventRecord(b, ctx_.stream));
         NUMA_CUDA(cudaEventSynchronize(b));
     } else {
