@@ -66,6 +66,8 @@ template <bool WRITE_C, bool NORM, bool C32>
 __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, double* __restrict__ F,
                                                  double* __restrict__ c_out, float* __restrict__ c32_out, int n,
                                                  int ichunk, double lam, double h2inv, RedArgs red, double* norm_out) {
+    pdl_wait();
+    pdl_trigger();
     const int k = blockIdx.x * BX + threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
     const int i0 = blockIdx.z * ichunk;
@@ -99,6 +101,8 @@ __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, d
 
 // c = lambda e^u
 __global__ void k_coef(const double* __restrict__ u, double* __restrict__ c, size_t N, double lam) {
+    pdl_wait();
+    pdl_trigger();
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) c[p] = lam * exp_tang(u[p]);
 }
@@ -108,6 +112,8 @@ template <bool FROM_X>
 __global__ void __launch_bounds__(BX* BY) k_jvp(const double* __restrict__ cx, const double* __restrict__ v,
                                                 double* __restrict__ out, int n, int ichunk, double lam,
                                                 double h2inv) {
+    pdl_wait();
+    pdl_trigger();
     const int k = blockIdx.x * BX + threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
     const int i0 = blockIdx.z * ichunk;
@@ -139,6 +145,8 @@ __device__ __forceinline__ float to_f32(float x) { return x; }
 template <class VT>
 __global__ void __launch_bounds__(BX* BY) k_jvp32(const float* __restrict__ c32, const VT* __restrict__ v,
                                                   double* __restrict__ out, int n, int ichunk, float h2inv) {
+    pdl_wait();
+    pdl_trigger();
     constexpr int TW = BX + 2, TH = BY + 2, TE = TW * TH;  // 34 x 10 tile, 340 values
     constexpr int PER = (TE + BX * BY - 1) / (BX * BY);    // values per thread and plane (2)
     __shared__ float S[3][TH][TW];
@@ -206,12 +214,16 @@ __global__ void __launch_bounds__(BX* BY) k_jvp32(const float* __restrict__ c32,
 
 // c32 = RN32(c) (integer conversion)
 __global__ void k_coef32(const double* __restrict__ c, float* __restrict__ c32, size_t N) {
+    pdl_wait();
+    pdl_trigger();
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) c32[i] = f64_to_f32(c[i]);
 }
 
 // out = -c v v  (bratu3d.hpp:52: -lambda * exp(u) * v * v, evaluated left to right)
 __global__ void k_d2(const double* __restrict__ c, const double* __restrict__ v, double* __restrict__ out, size_t N) {
+    pdl_wait();
+    pdl_trigger();
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) {
         const double vv = v[p];
@@ -221,6 +233,8 @@ __global__ void k_d2(const double* __restrict__ c, const double* __restrict__ v,
 
 // d = 6 h^-2 - c
 __global__ void k_jacobi_diag(const double* __restrict__ c, double* __restrict__ d, size_t N, double six_h2inv) {
+    pdl_wait();
+    pdl_trigger();
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) d[p] = six_h2inv - c[p];
 }
@@ -259,7 +273,7 @@ void Bratu3D::bind(const double*, const double* cache, int precision) {
 void Bratu3D::jvp_bound32(const float* v32, double* out) {
     if (bound_precision_ != NUMA_GPU_FP32) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Bratu3D: no FP32 product bound");
     March m = march_shape((int)n_, false);
-    k_jvp32<float><<<m.grid, dim3(BX, BY), 0, ctx_.stream>>>(bound_c32_, v32, out, (int)n_, m.ichunk, (float)h2inv_);
+    launch_pdl(k_jvp32<float>, m.grid, dim3(BX, BY), 0, ctx_.stream, bound_c32_, v32, out, (int)n_, m.ichunk, (float)h2inv_);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d jvp32 (fp32 input)");
 }
@@ -277,37 +291,37 @@ void Bratu3D::eval(const double* x, double* out, double* c_out, double* norm_out
     float* c32 = (c_out && mixed_cache_) ? reinterpret_cast<float*>(c_out + N_) : nullptr;
     const double lam = lambda_, h2 = h2inv_;
     if (c32 && norm)
-        k_eval<true, true, true><<<m.grid, blk, 0, ctx_.stream>>>(x, out, c_out, c32, n, m.ichunk, lam, h2, ctx_.red, norm_out);
+        launch_pdl(k_eval<true, true, true>, m.grid, blk, 0, ctx_.stream, x, out, c_out, c32, n, m.ichunk, lam, h2, ctx_.red, norm_out);
     else if (c32)
-        k_eval<true, false, true><<<m.grid, blk, 0, ctx_.stream>>>(x, out, c_out, c32, n, m.ichunk, lam, h2, ctx_.red, nullptr);
+        launch_pdl(k_eval<true, false, true>, m.grid, blk, 0, ctx_.stream, x, out, c_out, c32, n, m.ichunk, lam, h2, ctx_.red, nullptr);
     else if (c_out && norm)
-        k_eval<true, true, false><<<m.grid, blk, 0, ctx_.stream>>>(x, out, c_out, nullptr, n, m.ichunk, lam, h2, ctx_.red, norm_out);
+        launch_pdl(k_eval<true, true, false>, m.grid, blk, 0, ctx_.stream, x, out, c_out, nullptr, n, m.ichunk, lam, h2, ctx_.red, norm_out);
     else if (c_out)
-        k_eval<true, false, false><<<m.grid, blk, 0, ctx_.stream>>>(x, out, c_out, nullptr, n, m.ichunk, lam, h2, ctx_.red, nullptr);
+        launch_pdl(k_eval<true, false, false>, m.grid, blk, 0, ctx_.stream, x, out, c_out, nullptr, n, m.ichunk, lam, h2, ctx_.red, nullptr);
     else if (norm)
-        k_eval<false, true, false><<<m.grid, blk, 0, ctx_.stream>>>(x, out, nullptr, nullptr, n, m.ichunk, lam, h2, ctx_.red, norm_out);
+        launch_pdl(k_eval<false, true, false>, m.grid, blk, 0, ctx_.stream, x, out, nullptr, nullptr, n, m.ichunk, lam, h2, ctx_.red, norm_out);
     else
-        k_eval<false, false, false><<<m.grid, blk, 0, ctx_.stream>>>(x, out, nullptr, nullptr, n, m.ichunk, lam, h2, ctx_.red, nullptr);
+        launch_pdl(k_eval<false, false, false>, m.grid, blk, 0, ctx_.stream, x, out, nullptr, nullptr, n, m.ichunk, lam, h2, ctx_.red, nullptr);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d eval");
 }
 
 void Bratu3D::coef(const double* x, double* c) {
-    k_coef<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(x, c, N_, lambda_);
+    launch_pdl(k_coef, ew_grid(ctx_, N_), 256, 0, ctx_.stream, x, c, N_, lambda_);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d coef");
 }
 
 void Bratu3D::jvp_c(const double* c, const double* v, double* out) {
     March m = march_shape((int)n_, false);
-    k_jvp<false><<<m.grid, dim3(BX, BY), 0, ctx_.stream>>>(c, v, out, (int)n_, m.ichunk, lambda_, h2inv_);
+    launch_pdl(k_jvp<false>, m.grid, dim3(BX, BY), 0, ctx_.stream, c, v, out, (int)n_, m.ichunk, lambda_, h2inv_);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d jvp");
 }
 
 void Bratu3D::jvp_c32(const float* c32, const double* v, double* out) {
     March m = march_shape((int)n_, false);
-    k_jvp32<double><<<m.grid, dim3(BX, BY), 0, ctx_.stream>>>(c32, v, out, (int)n_, m.ichunk, (float)h2inv_);
+    launch_pdl(k_jvp32<double>, m.grid, dim3(BX, BY), 0, ctx_.stream, c32, v, out, (int)n_, m.ichunk, (float)h2inv_);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d jvp32");
 }
@@ -316,37 +330,37 @@ void Bratu3D::jvp_c32(const float* c32, const double* v, double* out) {
 // that hold the coefficient themselves (the learned preconditioner).
 void bratu_jvp32(Context& ctx, int n, double h2inv, const float* c32, const double* v, double* out) {
     March m = march_shape(n, false);
-    k_jvp32<double><<<m.grid, dim3(BX, BY), 0, ctx.stream>>>(c32, v, out, n, m.ichunk, (float)h2inv);
+    launch_pdl(k_jvp32<double>, m.grid, dim3(BX, BY), 0, ctx.stream, c32, v, out, n, m.ichunk, (float)h2inv);
     ctx.count_launch();
     ctx.check_launch("bratu jvp32");
 }
 
 void bratu_coef32(Context& ctx, const double* c, float* c32, size_t N) {
-    k_coef32<<<ew_grid(ctx, N), 256, 0, ctx.stream>>>(c, c32, N);
+    launch_pdl(k_coef32, ew_grid(ctx, N), 256, 0, ctx.stream, c, c32, N);
     ctx.count_launch();
 }
 
 void Bratu3D::coef32(const double* c, float* c32) {
-    k_coef32<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(c, c32, N_);
+    launch_pdl(k_coef32, ew_grid(ctx_, N_), 256, 0, ctx_.stream, c, c32, N_);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d coef32");
 }
 
 void Bratu3D::jvp_x(const double* x, const double* v, double* out) {
     March m = march_shape((int)n_, false);
-    k_jvp<true><<<m.grid, dim3(BX, BY), 0, ctx_.stream>>>(x, v, out, (int)n_, m.ichunk, lambda_, h2inv_);
+    launch_pdl(k_jvp<true>, m.grid, dim3(BX, BY), 0, ctx_.stream, x, v, out, (int)n_, m.ichunk, lambda_, h2inv_);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d jvp(x)");
 }
 
 void Bratu3D::d2_c(const double* c, const double* v, double* out) {
-    k_d2<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(c, v, out, N_);
+    launch_pdl(k_d2, ew_grid(ctx_, N_), 256, 0, ctx_.stream, c, v, out, N_);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d d2");
 }
 
 void Bratu3D::jacobi_diag_c(const double* c, double* d) {
-    k_jacobi_diag<<<ew_grid(ctx_, N_), 256, 0, ctx_.stream>>>(c, d, N_, 6.0 * h2inv_);
+    launch_pdl(k_jacobi_diag, ew_grid(ctx_, N_), 256, 0, ctx_.stream, c, d, N_, 6.0 * h2inv_);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d jacobi_diag");
 }

@@ -98,6 +98,8 @@ struct StoreSqrt {
 template <class Fin>
 __global__ void __launch_bounds__(kRedThreads) k_dot(const double* __restrict__ a, const double* __restrict__ b,
                                                      size_t N, RedArgs red, Fin fin) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double sm[1][32];
     double s[1] = {0.0};
     const size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -108,18 +110,24 @@ __global__ void __launch_bounds__(kRedThreads) k_dot(const double* __restrict__ 
 }
 
 __global__ void k_axpy(double a, const double* __restrict__ x, double* __restrict__ y, size_t N) {
+    pdl_wait();
+    pdl_trigger();
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride)
         y[i] = y[i] + a * x[i];
 }
 
 __global__ void k_fill(double* __restrict__ y, double v, size_t N) {
+    pdl_wait();
+    pdl_trigger();
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) y[i] = v;
 }
 
 __global__ void k_newton_step(const double* __restrict__ x, const double* __restrict__ z, double lam,
                               double* __restrict__ xn, size_t N) {
+    pdl_wait();
+    pdl_trigger();
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride)
         xn[i] = x[i] - lam * z[i];
@@ -127,12 +135,16 @@ __global__ void k_newton_step(const double* __restrict__ x, const double* __rest
 
 __global__ void k_cheb_step(const double* __restrict__ x, const double* __restrict__ z,
                             const double* __restrict__ u, double* __restrict__ xn, size_t N) {
+    pdl_wait();
+    pdl_trigger();
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride)
         xn[i] = x[i] - z[i] - 0.5 * u[i];
 }
 
 __global__ void k_scale(double* __restrict__ y, double a, size_t N) {
+    pdl_wait();
+    pdl_trigger();
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) y[i] = a * y[i];
 }
@@ -147,20 +159,20 @@ static unsigned elementwise_grid(const Context& ctx, size_t N) {
 }
 
 void dev_dot(Context& ctx, const double* a, const double* b, size_t N, double* out) {
-    k_dot<<<ctx.red_grid(N), kRedThreads, 0, ctx.stream>>>(a, b, N, ctx.red, StoreSum{out});
+    launch_pdl(k_dot<StoreSum>, ctx.red_grid(N), kRedThreads, 0, ctx.stream, a, b, N, ctx.red, StoreSum{out});
     ctx.count_launch();
     ctx.check_launch("dot");
 }
 
 void dev_norm2(Context& ctx, const double* a, size_t N, double* out) {
-    k_dot<<<ctx.red_grid(N), kRedThreads, 0, ctx.stream>>>(a, a, N, ctx.red, StoreSqrt{out});
+    launch_pdl(k_dot<StoreSqrt>, ctx.red_grid(N), kRedThreads, 0, ctx.stream, a, a, N, ctx.red, StoreSqrt{out});
     ctx.count_launch();
     ctx.check_launch("norm2");
 }
 
 void dev_axpy(Context& ctx, double a, const double* x, double* y, size_t N) {
     if (N == 0) return;
-    k_axpy<<<elementwise_grid(ctx, N), 256, 0, ctx.stream>>>(a, x, y, N);
+    launch_pdl(k_axpy, elementwise_grid(ctx, N), 256, 0, ctx.stream, a, x, y, N);
     ctx.count_launch();
     ctx.check_launch("axpy");
 }
@@ -171,7 +183,7 @@ void dev_fill(Context& ctx, double* y, double value, size_t N) {
         NUMA_CUDA(cudaMemsetAsync(y, 0, N * sizeof(double), ctx.stream));
         return;
     }
-    k_fill<<<elementwise_grid(ctx, N), 256, 0, ctx.stream>>>(y, value, N);
+    launch_pdl(k_fill, elementwise_grid(ctx, N), 256, 0, ctx.stream, y, value, N);
     ctx.count_launch();
     ctx.check_launch("fill");
 }
@@ -182,19 +194,19 @@ void dev_copy(Context& ctx, const double* src, double* dst, size_t N) {
 }
 
 void dev_newton_step(Context& ctx, const double* x, const double* z, double lam, double* xn, size_t N) {
-    k_newton_step<<<elementwise_grid(ctx, N), 256, 0, ctx.stream>>>(x, z, lam, xn, N);
+    launch_pdl(k_newton_step, elementwise_grid(ctx, N), 256, 0, ctx.stream, x, z, lam, xn, N);
     ctx.count_launch();
     ctx.check_launch("newton_step");
 }
 
 void dev_cheb_step(Context& ctx, const double* x, const double* z, const double* u, double* xn, size_t N) {
-    k_cheb_step<<<elementwise_grid(ctx, N), 256, 0, ctx.stream>>>(x, z, u, xn, N);
+    launch_pdl(k_cheb_step, elementwise_grid(ctx, N), 256, 0, ctx.stream, x, z, u, xn, N);
     ctx.count_launch();
     ctx.check_launch("cheb_step");
 }
 
 void dev_scale_inplace(Context& ctx, double* y, double a, size_t N) {
-    k_scale<<<elementwise_grid(ctx, N), 256, 0, ctx.stream>>>(y, a, N);
+    launch_pdl(k_scale, elementwise_grid(ctx, N), 256, 0, ctx.stream, y, a, N);
     ctx.count_launch();
     ctx.check_launch("scale");
 }

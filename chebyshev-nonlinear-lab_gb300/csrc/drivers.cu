@@ -51,6 +51,8 @@ private:
 
 __global__ void k_jacobi_apply(const double* __restrict__ r, const double* __restrict__ d, double* __restrict__ z,
                                size_t N) {
+    pdl_wait();
+    pdl_trigger();
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) z[i] = r[i] / d[i];
 }
@@ -70,7 +72,7 @@ public:
         Context& ctx = op_.ctx();
         const size_t N = op_.size();
         size_t g = (N + 255) / 256, cap = (size_t)ctx.sm_count * 16;
-        k_jacobi_apply<<<(unsigned)std::max<size_t>(1, std::min(g, cap)), 256, 0, ctx.stream>>>(r, d_.p, z, N);
+        launch_pdl(k_jacobi_apply, (unsigned)std::max<size_t>(1, std::min(g, cap)), 256, 0, ctx.stream, r, d_.p, z, N);
         ctx.count_launch();
         ctx.check_launch("jacobi apply");
     }
@@ -197,6 +199,8 @@ private:
 // (j1 - j0) / h  (tf_chebyshev_2018.hpp:46-48)
 __global__ void k_quot(const double* __restrict__ a, const double* __restrict__ b, double h, double* __restrict__ out,
                        size_t N) {
+    pdl_wait();
+    pdl_trigger();
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) out[i] = (a[i] - b[i]) / h;
 }
@@ -542,7 +546,7 @@ void tf_chebyshev_2018(NonlinearOp& f, double* x0, const KrylovParams& p, Provid
             }
         }
         out.n_JVP += 2;
-        k_quot<<<ew_grid(ctx, N), 256, 0, ctx.stream>>>(j1, j0, h, S.w.p, N);
+        launch_pdl(k_quot, ew_grid(ctx, N), 256, 0, ctx.stream, j1, j0, h, S.w.p, N);
         ctx.count_launch();
         dev_scale_inplace(ctx, S.w.p, -0.5, N);
         const GmresResult g2 = S.gmres.solve(J, Mp, S.w.p, S.u.p, gmres_opts(p, eta2));

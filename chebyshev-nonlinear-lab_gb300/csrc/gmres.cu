@@ -38,6 +38,8 @@ template <bool HAS_PREV, bool NORM, class Fin>
 __global__ void __launch_bounds__(kRedThreads) k_mgs(double* __restrict__ w, const double* __restrict__ Vprev,
                                                      const double* __restrict__ hprev,
                                                      const double* __restrict__ Vcur, size_t N, RedArgs red, Fin fin) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double sm[1][32];
     double s[1] = {0.0};
     const double a = HAS_PREV ? -(*hprev) : 0.0;
@@ -77,6 +79,8 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs(const double* w, const doub
                                                      const double* __restrict__ hin, const double* __restrict__ sig2,
                                                      size_t N, RedArgs red, double* __restrict__ hout, double* wout,
                                                      double* __restrict__ sig2_out) {
+    pdl_wait();
+    pdl_trigger();
     constexpr int R = MODE == 2 ? 1 : CNT;
     __shared__ double sm[R][32];
     double hs[CNT];
@@ -121,7 +125,7 @@ bool launch_cgs(Context& ctx, int cnt, const double* w, const double* v0, const 
     switch (cnt) {
 #define NUMA_CGS_CASE(K)                                                                                       \
     case K:                                                                                                    \
-        k_cgs<K, MODE><<<g, kRedThreads, 0, ctx.stream>>>(w, v0, V, N, hin, sig2, N, ctx.red, hout, wout,   \
+        launch_pdl(k_cgs<K, MODE>, g, kRedThreads, 0, ctx.stream, w, v0, V, N, hin, sig2, N, ctx.red, hout, wout,   \
                                                           sig2_out);                                         \
         break;
         NUMA_CGS_CASE(1)
@@ -144,6 +148,8 @@ bool launch_cgs(Context& ctx, int cnt, const double* w, const double* v0, const 
 // division (within 1.5 ulp of it; the basis vectors already differ from the reference's in the
 // last bits through the order of the inner-product sums).
 __global__ void k_div(const double* __restrict__ src, double d, double rd, double* __restrict__ dst, size_t N) {
+    pdl_wait();
+    pdl_trigger();
     (void)d;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) dst[i] = src[i] * rd;
@@ -151,6 +157,8 @@ __global__ void k_div(const double* __restrict__ src, double d, double rd, doubl
 
 // r = b - w (gmres.hpp:116)
 __global__ void k_sub(const double* __restrict__ b, const double* __restrict__ w, double* __restrict__ r, size_t N) {
+    pdl_wait();
+    pdl_trigger();
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) r[i] = b[i] - w[i];
 }
@@ -160,6 +168,8 @@ __global__ void k_sub(const double* __restrict__ b, const double* __restrict__ w
 // term fused into one FMA.
 __global__ void k_combine(const double* __restrict__ base, const double* __restrict__ V, size_t ldv, int cnt,
                           const double* __restrict__ coef, double* __restrict__ out, size_t N) {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ double cs[];
     for (int r = threadIdx.x; r < cnt; r += blockDim.x) cs[r] = coef[r];
     __syncthreads();
@@ -179,6 +189,8 @@ __device__ __forceinline__ double widen(float v) { return f32_to_f64(v); }
 template <class VT>
 __global__ void k_combine_add(const VT* __restrict__ V, size_t ldv, int cnt, const double* __restrict__ coef,
                               double* x, size_t N) {
+    pdl_wait();
+    pdl_trigger();
     extern __shared__ double cs[];
     for (int r = threadIdx.x; r < cnt; r += blockDim.x) cs[r] = coef[r];
     __syncthreads();
@@ -191,7 +203,11 @@ __global__ void k_combine_add(const VT* __restrict__ V, size_t ldv, int cnt, con
 }
 
 // *out = v (one device scalar from a host value, stream-ordered)
-__global__ void k_set_scalar(double* __restrict__ out, double v) { *out = v; }
+__global__ void k_set_scalar(double* __restrict__ out, double v) {
+    pdl_wait();
+    pdl_trigger();
+    *out = v;
+}
 
 unsigned ew_grid(const Context& ctx, size_t N) {
     size_t want = (N + 255) / 256;
@@ -215,14 +231,14 @@ void Gmres::arnoldi_mgs(size_t j, double* w) {
     const size_t N = N_;
     const unsigned g = ctx_.red_grid(N);
     const double* V = V_.p;
-    k_mgs<false, false><<<g, kRedThreads, 0, ctx_.stream>>>(w, nullptr, nullptr, V, N, ctx_.red, StoreAt{hcol});
+    launch_pdl(k_mgs<false, false, StoreAt>, g, kRedThreads, 0, ctx_.stream, w, nullptr, nullptr, V, N, ctx_.red, StoreAt{hcol});
     ctx_.count_launch();
     for (size_t i = 1; i <= j; ++i) {
-        k_mgs<true, false><<<g, kRedThreads, 0, ctx_.stream>>>(w, V + (i - 1) * N, hcol + (i - 1), V + i * N, N,
+        launch_pdl(k_mgs<true, false, StoreAt>, g, kRedThreads, 0, ctx_.stream, w, V + (i - 1) * N, hcol + (i - 1), V + i * N, N,
                                                               ctx_.red, StoreAt{hcol + i});
         ctx_.count_launch();
     }
-    k_mgs<true, true><<<g, kRedThreads, 0, ctx_.stream>>>(w, V + j * N, hcol + j, nullptr, N, ctx_.red,
+    launch_pdl(k_mgs<true, true, StoreSqrtAt>, g, kRedThreads, 0, ctx_.stream, w, V + j * N, hcol + j, nullptr, N, ctx_.red,
                                                          StoreSqrtAt{hcol + j + 1});
     ctx_.count_launch();
     ctx_.check_launch("arnoldi mgs");
@@ -316,7 +332,7 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
         } else {
             A.apply(x, w_.p);
             ++res.matvecs;
-            k_sub<<<eg, 256, 0, ctx_.stream>>>(b, w_.p, r_.p, N);
+            launch_pdl(k_sub, eg, 256, 0, ctx_.stream, b, w_.p, r_.p, N);
             ctx_.count_launch();
             v0 = r_.p;
             dev_norm2(ctx_, v0, N, sl);
@@ -327,7 +343,7 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
             res.converged = true;
             break;
         }
-        k_set_scalar<<<1, 1, 0, ctx_.stream>>>(sig2, 1.0 / (beta * beta));
+        launch_pdl(k_set_scalar, 1, 1, 0, ctx_.stream, sig2, 1.0 / (beta * beta));
         ctx_.count_launch();
         sig[0] = 1.0 / beta;
         std::fill(g.begin(), g.end(), 0.0);
@@ -391,8 +407,8 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
         double* yh = pin_.get(m);
         for (size_t jj = 0; jj < k; ++jj) yh[jj] = y[jj] * sig[jj];
         NUMA_CUDA(cudaMemcpyAsync(ydev, yh, k * sizeof(double), cudaMemcpyHostToDevice, ctx_.stream));
-        if (z32) k_combine_add<float><<<eg, 256, k * sizeof(double), ctx_.stream>>>(Z32_.p, N, (int)k, ydev, x, N);
-        else k_combine_add<double><<<eg, 256, k * sizeof(double), ctx_.stream>>>(Z_.p, N, (int)k, ydev, x, N);
+        if (z32) launch_pdl(k_combine_add<float>, eg, 256, k * sizeof(double), ctx_.stream, Z32_.p, N, (int)k, ydev, x, N);
+        else launch_pdl(k_combine_add<double>, eg, 256, k * sizeof(double), ctx_.stream, Z_.p, N, (int)k, ydev, x, N);
         ctx_.count_launch();
         ctx_.check_launch("gmres update (lazy)");
         if (res.rel_res <= o.rtol) {
@@ -462,7 +478,7 @@ GmresResult Gmres::solve(LinearOp& A, Precond* M, const double* b, double* x, co
         } else {
             A.apply(x, w_.p);
             ++res.matvecs;
-            k_sub<<<eg, 256, 0, ctx_.stream>>>(b, w_.p, r_.p, N);
+            launch_pdl(k_sub, eg, 256, 0, ctx_.stream, b, w_.p, r_.p, N);
             ctx_.count_launch();
             rv = r_.p;
         }
@@ -475,7 +491,7 @@ GmresResult Gmres::solve(LinearOp& A, Precond* M, const double* b, double* x, co
             break;
         }
         for (auto& row : Hraw) std::fill(row.begin(), row.end(), 0.0);
-        k_div<<<eg, 256, 0, ctx_.stream>>>(rv, beta, 1.0 / beta, V_.p, N);
+        launch_pdl(k_div, eg, 256, 0, ctx_.stream, rv, beta, 1.0 / beta, V_.p, N);
         ctx_.count_launch();
         std::fill(g.begin(), g.end(), 0.0);
         g[0] = beta;
@@ -504,7 +520,7 @@ GmresResult Gmres::solve(LinearOp& A, Precond* M, const double* b, double* x, co
             for (size_t i = 0; i <= j + 1; ++i) H[i][j] = col[i];
             double* vnext = V_.p + (j + 1) * N;
             if (H[j + 1][j] > 0.0) {
-                k_div<<<eg, 256, 0, ctx_.stream>>>(w_.p, H[j + 1][j], 1.0 / H[j + 1][j], vnext, N);
+                launch_pdl(k_div, eg, 256, 0, ctx_.stream, w_.p, H[j + 1][j], 1.0 / H[j + 1][j], vnext, N);
                 ctx_.count_launch();
             } else {
                 dev_fill(ctx_, vnext, 0.0, N);
@@ -547,11 +563,11 @@ GmresResult Gmres::solve(LinearOp& A, Precond* M, const double* b, double* x, co
         std::memcpy(yh, y.data(), k * sizeof(double));
         NUMA_CUDA(cudaMemcpyAsync(ydev, yh, k * sizeof(double), cudaMemcpyHostToDevice, ctx_.stream));
         if (o.flexible) {
-            k_combine<<<eg, 256, k * sizeof(double), ctx_.stream>>>(nullptr, Z_.p, N, (int)k, ydev, comb_.p, N);
+            launch_pdl(k_combine, eg, 256, k * sizeof(double), ctx_.stream, nullptr, Z_.p, N, (int)k, ydev, comb_.p, N);
             ctx_.count_launch();
             dev_axpy(ctx_, 1.0, comb_.p, x, N);
         } else {
-            k_combine<<<eg, 256, k * sizeof(double), ctx_.stream>>>(nullptr, V_.p, N, (int)k, ydev, comb_.p, N);
+            launch_pdl(k_combine, eg, 256, k * sizeof(double), ctx_.stream, nullptr, V_.p, N, (int)k, ydev, comb_.p, N);
             ctx_.count_launch();
             precond_apply(M, comb_.p, z_.p);
             ++res.precs;
@@ -638,9 +654,9 @@ GmresResult Gmres::solve_recycled(LinearOp& A, Precond* M, const double* b, doub
     rrec_.resize(N);
     comb_.resize(N);
     const unsigned eg = ew_grid(ctx_, N);
-    k_combine<<<eg, 256, (k + 1) * sizeof(double), ctx_.stream>>>(b, sp.V.p, N, (int)(k + 1), cdev, rrec_.p, N);
+    launch_pdl(k_combine, eg, 256, (k + 1) * sizeof(double), ctx_.stream, b, sp.V.p, N, (int)(k + 1), cdev, rrec_.p, N);
     // comb = sum_{j<k} y_j V_j; x = M comb (gmres.hpp:312-317)
-    k_combine<<<eg, 256, k * sizeof(double), ctx_.stream>>>(nullptr, sp.V.p, N, (int)k, cdev + k + 1, comb_.p, N);
+    launch_pdl(k_combine, eg, 256, k * sizeof(double), ctx_.stream, nullptr, sp.V.p, N, (int)k, cdev + k + 1, comb_.p, N);
     ctx_.count_launch(2);
     NUMA_CUDA(cudaStreamSynchronize(ctx_.stream));
     precond_apply(M, comb_.p, x);
