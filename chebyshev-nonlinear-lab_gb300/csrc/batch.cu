@@ -34,6 +34,33 @@ struct BatchWorker {
 BatchExecutor::BatchExecutor(int device, int workers) : device_(device) {
     const int nw = std::max(1, workers);
     for (int w = 0; w < nw; ++w) workers_.push_back(std::make_unique<BatchWorker>(device));
+    active_ = nw;
+}
+
+void BatchExecutor::set_active(int w) {
+    if (w < 1 || w > (int)workers_.size()) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "worker count out of range");
+    active_ = w;
+}
+
+int BatchExecutor::autotune(const numa_batch_instance* inst, size_t count, int method, int mg_precision,
+                            const numa_krylov_params* params, const int* candidates, int ncand, double* seconds) {
+    if (ncand < 1 || !candidates) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "no candidate worker counts");
+    std::vector<numa_batch_result> res(count);
+    int best = -1;
+    double best_t = 0.0;
+    for (int c = 0; c < ncand; ++c) {
+        set_active(candidates[c]);
+        double t = 0.0;
+        solve(inst, count, method, mg_precision, params, res.data(), &t);  // sets the workers up
+        solve(inst, count, method, mg_precision, params, res.data(), &t);
+        if (seconds) seconds[c] = t;
+        if (best < 0 || t < best_t) {
+            best = candidates[c];
+            best_t = t;
+        }
+    }
+    set_active(best);
+    return best;
 }
 
 BatchExecutor::~BatchExecutor() = default;
@@ -106,7 +133,7 @@ void BatchExecutor::solve(const numa_batch_instance* inst, size_t count, int met
             }
         }
     };
-    const size_t nw = std::min(workers_.size(), std::max<size_t>(count, 1));
+    const size_t nw = std::min((size_t)active_, std::max<size_t>(count, 1));
     std::vector<std::thread> threads;
     threads.reserve(nw);
     for (size_t w = 0; w < nw; ++w) threads.emplace_back(work, std::ref(*workers_[w]));

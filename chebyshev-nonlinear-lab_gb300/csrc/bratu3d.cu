@@ -212,6 +212,42 @@ __global__ void __launch_bounds__(BX* BY) k_jvp32(const float* __restrict__ c32,
     }
 }
 
+// The FP32 product from an FP32 v (the V-cycle's output): no conversion, so no shared-memory tile —
+// a (k, j) column marches in i holding planes i-1, i, i+1 in registers, and the neighbours in j and k
+// come through L1.  The arithmetic is k_jvp32's, operation for operation (same results).
+__global__ void __launch_bounds__(BX* BY) k_jvp32f(const float* __restrict__ c32, const float* __restrict__ v,
+                                                   double* __restrict__ out, int n, int ichunk, float h2inv) {
+    pdl_wait();
+    pdl_trigger();
+    const int k = blockIdx.x * BX + threadIdx.x;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    if (k >= n || j >= n) return;
+    const int i0 = blockIdx.z * ichunk;
+    const int i1 = min(i0 + ichunk, n);
+    const size_t plane = (size_t)n * n;
+    const size_t col = (size_t)j * n + k;
+    const bool jlo = j > 0, jhi = j + 1 < n, klo = k > 0, khi = k + 1 < n;
+    float below = i0 > 0 ? v[(size_t)(i0 - 1) * plane + col] : 0.0f;
+    float cur = i0 < i1 ? v[(size_t)i0 * plane + col] : 0.0f;
+    for (int i = i0; i < i1; ++i) {
+        const size_t p = (size_t)i * plane + col;
+        const float above = (i + 1 < n) ? v[p + plane] : 0.0f;
+        const float jm = jlo ? v[p - n] : 0.0f, jp = jhi ? v[p + n] : 0.0f;
+        const float km = klo ? v[p - 1] : 0.0f, kp = khi ? v[p + 1] : 0.0f;
+        const float cc = c32[p];
+        float s = 6.0f * cur;
+        s = s - below;
+        s = s - above;
+        s = s - jm;
+        s = s - jp;
+        s = s - km;
+        s = s - kp;
+        out[p] = f32_to_f64(h2inv * s - cc * cur);
+        below = cur;
+        cur = above;
+    }
+}
+
 // c32 = RN32(c) (integer conversion)
 __global__ void k_coef32(const double* __restrict__ c, float* __restrict__ c32, size_t N) {
     pdl_wait();
@@ -273,7 +309,7 @@ void Bratu3D::bind(const double*, const double* cache, int precision) {
 void Bratu3D::jvp_bound32(const float* v32, double* out) {
     if (bound_precision_ != NUMA_GPU_FP32) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Bratu3D: no FP32 product bound");
     March m = march_shape((int)n_, false);
-    launch_pdl(k_jvp32<float>, m.grid, dim3(BX, BY), 0, ctx_.stream, bound_c32_, v32, out, (int)n_, m.ichunk, (float)h2inv_);
+    launch_pdl(k_jvp32f, m.grid, dim3(BX, BY), 0, ctx_.stream, bound_c32_, v32, out, (int)n_, m.ichunk, (float)h2inv_);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d jvp32 (fp32 input)");
 }

@@ -1455,6 +1455,40 @@ int numa_gpu_batch_create(int device, int workers, numa_gpu_batch** out) {
     }
 }
 
+int numa_gpu_batch_set_workers(numa_gpu_batch* b, int workers) {
+    if (!b) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    try {
+        b->impl->set_active(workers);
+        return NUMA_GPU_OK;
+    } catch (const Status& s) {
+        set_batch_error(s.what());
+        return s.code;
+    }
+}
+
+int numa_gpu_batch_autotune(numa_gpu_batch* b, const numa_batch_instance* inst, size_t count, int method,
+                            int mg_precision, const numa_krylov_params* p, const int* candidates, int ncand,
+                            int* chosen, double* seconds) {
+    if (!b || !inst || !count || !candidates || ncand < 1 || !chosen) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    if (method < NUMA_GPU_METHOD_NK || method > NUMA_GPU_METHOD_TF2018) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    if (mg_precision != NUMA_GPU_FP64 && mg_precision != NUMA_GPU_FP32) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    for (size_t i = 0; i < count; ++i)
+        if (inst[i].n == 0 || inst[i].n > 1290) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    for (int c = 0; c < ncand; ++c)
+        if (candidates[c] < 1 || candidates[c] > b->impl->workers()) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    set_batch_error("");
+    try {
+        *chosen = b->impl->autotune(inst, count, method, mg_precision, p, candidates, ncand, seconds);
+        return NUMA_GPU_OK;
+    } catch (const Status& s) {
+        set_batch_error(s.what());
+        return s.code;
+    } catch (const std::exception& e) {
+        set_batch_error(e.what());
+        return NUMA_GPU_ERR_CUDA;
+    }
+}
+
 int numa_gpu_batch_destroy(numa_gpu_batch* b) {
     delete b;
     return NUMA_GPU_OK;

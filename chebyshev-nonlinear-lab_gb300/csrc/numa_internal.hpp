@@ -512,11 +512,19 @@ public:
     BatchExecutor(int device, int workers);
     ~BatchExecutor();
     int workers() const { return (int)workers_.size(); }
+    // how many of the workers a batch uses (1 ... workers())
+    int active() const { return active_; }
+    void set_active(int w);
     void solve(const numa_batch_instance* inst, size_t count, int method, int mg_precision,
                const numa_krylov_params* params, numa_batch_result* results, double* wall_seconds);
+    // The schedule autotuner: for each candidate worker count, one untimed batch (sets the workers
+    // up) and one timed batch of these instances; keeps the fastest as the active count and returns it.
+    int autotune(const numa_batch_instance* inst, size_t count, int method, int mg_precision,
+                 const numa_krylov_params* params, const int* candidates, int ncand, double* seconds);
 
 private:
     int device_;
+    int active_;
     std::vector<std::unique_ptr<BatchWorker>> workers_;
 };
 

@@ -228,6 +228,9 @@ SIGNATURES = {
     "numa_gpu_batch_last_error": ([], C.c_char_p),
     "numa_gpu_batch_create": ([_I, _I, _PP], _I),
     "numa_gpu_batch_destroy": ([_P], _I),
+    "numa_gpu_batch_set_workers": ([_P, _I], _I),
+    "numa_gpu_batch_autotune": ([_P, C.POINTER(BatchInstance), _SZ, _I, _I, C.POINTER(KrylovParams),
+                                 C.POINTER(_I), _I, C.POINTER(_I), _F64P], _I),
     "numa_gpu_batch_solve": ([_P, C.POINTER(BatchInstance), _SZ, _I, _I, C.POINTER(KrylovParams),
                               C.POINTER(BatchResult), _F64P], _I),
     "numa_gpu_learned_create": ([_P, _SZ, C.c_uint64, _PP], _I),
@@ -1128,6 +1131,26 @@ class BatchExecutor:
             self.close()
         except Exception:
             pass
+
+    def set_workers(self, workers: int):
+        rc = self.lib.numa_gpu_batch_set_workers(self.h, workers)
+        if rc != OK:
+            raise NumaGPUError(rc, "numa_gpu_batch_set_workers", self.lib.numa_gpu_batch_last_error().decode())
+
+    def autotune(self, instances, candidates=(4, 8, 16, 24, 32), method: str = "nk", mg_precision: int = FP32,
+                 params: KrylovParams | None = None) -> tuple[int, dict]:
+        """Picks the worker count (the schedule) that runs these instances fastest; returns it and the
+        seconds of every candidate."""
+        arr = (BatchInstance * len(instances))(*[BatchInstance(int(n), float(lam)) for n, lam in instances])
+        cand = (C.c_int * len(candidates))(*candidates)
+        secs = (C.c_double * len(candidates))()
+        chosen = C.c_int()
+        p = params if params is not None else default_params()
+        rc = self.lib.numa_gpu_batch_autotune(self.h, arr, len(instances), METHODS[method], mg_precision, C.byref(p),
+                                              cand, len(candidates), C.byref(chosen), secs)
+        if rc != OK:
+            raise NumaGPUError(rc, "numa_gpu_batch_autotune", self.lib.numa_gpu_batch_last_error().decode())
+        return chosen.value, {int(c): float(t) for c, t in zip(candidates, secs)}
 
     def solve(self, instances, method: str = "nk", mg_precision: int = FP32,
               params: KrylovParams | None = None) -> tuple[list[dict], float]:

@@ -485,6 +485,14 @@ int numa_gpu_solve_batch(int device, const numa_batch_instance* inst, size_t cou
 typedef struct numa_gpu_batch numa_gpu_batch;
 int numa_gpu_batch_create(int device, int workers, numa_gpu_batch** out);
 int numa_gpu_batch_destroy(numa_gpu_batch* b);
+/* How many of the executor's workers a batch uses (1 ... the count given at creation). */
+int numa_gpu_batch_set_workers(numa_gpu_batch* b, int workers);
+/* Schedule autotuner: for each candidate worker count, one untimed and one timed batch of these
+ * instances; the fastest becomes the executor's worker count (*chosen); seconds[c] (may be NULL)
+ * the timed batch of candidate c. */
+int numa_gpu_batch_autotune(numa_gpu_batch* b, const numa_batch_instance* inst, size_t count, int method,
+                            int mg_precision, const numa_krylov_params* p, const int* candidates, int ncand,
+                            int* chosen, double* seconds);
 int numa_gpu_batch_solve(numa_gpu_batch* b, const numa_batch_instance* inst, size_t count, int method,
                          int mg_precision, const numa_krylov_params* p, numa_batch_result* results,
                          double* wall_seconds);

@@ -61,3 +61,28 @@ def test_batch_executor_reuses_state_across_batches(gpu):
             assert all(r["converged"] == 1 for r in got), method
     finally:
         ex.close()
+
+
+def test_batch_autotune(gpu):
+    """The schedule autotuner tries each worker count on the batch, keeps the fastest, and the
+    executor then solves with it; counts do not depend on the schedule."""
+    G = _G()
+    inst = [(15, 2.0), (31, 5.5), (15, 6.0), (23, 1.0), (31, 3.3), (23, 4.4)]
+    p = G.default_params(rtol_nl=1e-10, gmres_restart=30, flexible=1, jvp_precision=G.FP32, orth=G.CGS1)
+    keys = ("converged", "iters", "n_F", "n_JVP", "n_lin_iters", "n_prec")
+    ex = G.BatchExecutor(workers=4)
+    try:
+        chosen, tune = ex.autotune(inst, (1, 2, 4), "nk", G.FP32, p)
+        assert chosen in (1, 2, 4) and set(tune) == {1, 2, 4} and all(t > 0 for t in tune.values())
+        assert tune[chosen] == min(tune.values())
+        got, _ = ex.solve(inst, "nk", G.FP32, p)
+        ex.set_workers(1)
+        one, _ = ex.solve(inst, "nk", G.FP32, p)
+        for a, b in zip(got, one):
+            assert all(a[k] == b[k] for k in keys)
+        with pytest.raises(G.NumaGPUError):
+            ex.set_workers(5)
+        with pytest.raises(G.NumaGPUError):
+            ex.autotune(inst, (8,), "nk", G.FP32, p)
+    finally:
+        ex.close()
