@@ -12,8 +12,10 @@
 //
 // Layouts.  Operator vectors are the reference's: w = (u, v) component-major, each plane
 // row-major (i * n + j).  Inside BrussMG2D every level keeps (u, v) interleaved per point (one
-// 8-byte FP32 or 16-byte FP64 pair), and the 2x2 block (k11, k12, k21, k22) per point (16 or
-// 32 bytes), so a point-block update is one vector load of each.
+// 8-byte FP32 or 16-byte FP64 pair) and the 2x2 block (k11, k12, k21, k22) per point (16 or 32
+// bytes), so a point-block update is one vector load of each; the points are stored colour-split
+// (each colour's points together, row-major), so a colour pass reads and writes only the cache
+// lines of the colours it touches.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -326,12 +328,21 @@ template <> __device__ __forceinline__ double from_f64<double>(double x) { retur
 __device__ __forceinline__ double to_f64(float x) { return f32_to_f64(x); }
 __device__ __forceinline__ double to_f64(double x) { return x; }
 
+// Storage index of point (i, j) of an n x n level (n even): colour-split, each colour's points in
+// row-major order, colour (i + j) & 1 first-half / second-half — a colour pass then reads and
+// writes only whole cache lines of the colours it touches.  The four neighbours of a point are all
+// of the other colour, in its rows i and i +- 1 at column index j/2 or j/2 +- 1.
+__device__ __forceinline__ size_t pidx(int n, int i, int j) {
+    const int half = n >> 1;
+    return (size_t)((i + j) & 1) * ((size_t)n * half) + (size_t)i * half + (j >> 1);
+}
+
 template <class T>
 __device__ __forceinline__ void nbr_sums(const T* __restrict__ X, int n, int i, int j, T& Su, T& Sv) {
     const int jm = j == 0 ? n - 1 : j - 1, jp = j + 1 == n ? 0 : j + 1;
     const int im = i == 0 ? n - 1 : i - 1, ip = i + 1 == n ? 0 : i + 1;
-    const size_t r = (size_t)i * n;
-    const auto w = ld2(X, r + jm), e = ld2(X, r + jp), s = ld2(X, (size_t)im * n + j), nn = ld2(X, (size_t)ip * n + j);
+    const auto w = ld2(X, pidx(n, i, jm)), e = ld2(X, pidx(n, i, jp)), s = ld2(X, pidx(n, im, j)),
+               nn = ld2(X, pidx(n, ip, j));
     Su = ((w.x + e.x) + s.x) + nn.x;
     Sv = ((w.y + e.y) + s.y) + nn.y;
 }
@@ -339,7 +350,8 @@ __device__ __forceinline__ void nbr_sums(const T* __restrict__ X, int n, int i, 
 enum { kBPassNormal = 0, kBPassFirst = 1, kBPassLast = 2 };
 
 // One colour of red-black point-block Gauss-Seidel on one level.  Thread (jj, i) owns the pair
-// of row i's points 2jj and 2jj + 1 (one of each colour) and updates the one of this colour.
+// of row i's points 2jj and 2jj + 1 (one of each colour) and updates the one of this colour; a warp
+// covers 32 consecutive points of one colour.
 //  Normal: x_c updated from the other colour.
 //  First (colour 0, x = 0 before the pass): x_0 = block^-1 b (neighbour sums are zeros), x_1 = 0;
 //    on the finest level the right-hand side is read from r (FP64 planes) and stored as b.
@@ -358,14 +370,15 @@ __global__ void __launch_bounds__(256) k_bmg_pass(T* __restrict__ X, T* __restri
     const T su = L.su, sv = L.sv, su4 = L.su4, sv4 = L.sv4;
     const int j = 2 * jj + ((i + colour) & 1);
     const int jo = 2 * jj + 1 - ((i + colour) & 1);
-    const size_t p = (size_t)i * n + j, po = (size_t)i * n + jo;
+    const size_t p = pidx(n, i, j), po = pidx(n, i, jo);                // level storage
+    const size_t pn = (size_t)i * n + j, pon = (size_t)i * n + jo;      // r and z: natural planes
     const size_t nn = (size_t)n * n;
     T bu, bv;
     if (MODE == kBPassFirst && r64) {
-        bu = from_f64<T>(r64[p]);
-        bv = from_f64<T>(r64[nn + p]);
+        bu = from_f64<T>(r64[pn]);
+        bv = from_f64<T>(r64[nn + pn]);
         st2(Bv, p, bu, bv);
-        st2(Bv, po, from_f64<T>(r64[po]), from_f64<T>(r64[nn + po]));
+        st2(Bv, po, from_f64<T>(r64[pon]), from_f64<T>(r64[nn + pon]));
     } else {
         const auto b = ld2(Bv, p);
         bu = b.x;
@@ -385,17 +398,17 @@ __global__ void __launch_bounds__(256) k_bmg_pass(T* __restrict__ X, T* __restri
     if (MODE == kBPassLast) {
         const auto o = ld2(X, po);
         if (z64) {
-            z64[p] = to_f64(u);
-            z64[nn + p] = to_f64(v);
-            z64[po] = to_f64(o.x);
-            z64[nn + po] = to_f64(o.y);
+            z64[pn] = to_f64(u);
+            z64[nn + pn] = to_f64(v);
+            z64[pon] = to_f64(o.x);
+            z64[nn + pon] = to_f64(o.y);
         }
         if constexpr (sizeof(T) == 4) {
             if (z32) {  // or the values unwidened, for an FP32 consumer
-                z32[p] = u;
-                z32[nn + p] = v;
-                z32[po] = o.x;
-                z32[nn + po] = o.y;
+                z32[pn] = u;
+                z32[nn + pn] = v;
+                z32[pon] = o.x;
+                z32[nn + pon] = o.y;
             }
         }
     }
@@ -405,7 +418,7 @@ __global__ void __launch_bounds__(256) k_bmg_pass(T* __restrict__ X, T* __restri
 template <class T, bool SMEM_K = false>
 __device__ __forceinline__ void resid_at(const T* X, const T* Bv, const T* K, int n, int i, int j, T su, T sv, T& ru,
                                          T& rv) {
-    const size_t p = (size_t)i * n + j;
+    const size_t p = pidx(n, i, j);
     const auto x = ld2(X, p);
     const auto bb = ld2(Bv, p);
     const Blk<T> k = SMEM_K ? load_blk_s(K, p) : load_blk(K, p);
@@ -449,25 +462,26 @@ __global__ void __launch_bounds__(256) k_bmg_restrict(const T* __restrict__ X, c
         return fw9(f[a][b], f[a][b - 1], f[a][b + 1], f[a - 1][b], f[a + 1][b], f[a - 1][b - 1], f[a - 1][b + 1],
                    f[a + 1][b - 1], f[a + 1][b + 1]);
     };
-    st2(Bc, (size_t)I * nc + J, fw(su_s), fw(sv_s));
+    st2(Bc, pidx(nc, I, J), fw(su_s), fw(sv_s));
 }
 
 // x_fine += bilinear periodic interpolation of x_coarse at the fine points (2I + {0,1}, 2J + {0,1}).
 template <class T>
 __device__ __forceinline__ void prolong_point(const T* Xc, int nc, int I, int J, T* Xf) {
     const int I1 = I + 1 == nc ? 0 : I + 1, J1 = J + 1 == nc ? 0 : J + 1;
-    const auto c00 = ld2(Xc, (size_t)I * nc + J), c10 = ld2(Xc, (size_t)I1 * nc + J);
-    const auto c01 = ld2(Xc, (size_t)I * nc + J1), c11 = ld2(Xc, (size_t)I1 * nc + J1);
+    const auto c00 = ld2(Xc, pidx(nc, I, J)), c10 = ld2(Xc, pidx(nc, I1, J));
+    const auto c01 = ld2(Xc, pidx(nc, I, J1)), c11 = ld2(Xc, pidx(nc, I1, J1));
     const int nf = 2 * nc;
-    const size_t f00 = (size_t)(2 * I) * nf + 2 * J, f10 = f00 + nf;
+    const size_t f00 = pidx(nf, 2 * I, 2 * J), f10 = pidx(nf, 2 * I + 1, 2 * J);
+    const size_t f01 = pidx(nf, 2 * I, 2 * J + 1), f11 = pidx(nf, 2 * I + 1, 2 * J + 1);
     auto add = [Xf](size_t p, T du, T dv) {
         const auto x = ld2(Xf, p);
         st2(Xf, p, x.x + du, x.y + dv);
     };
     add(f00, c00.x, c00.y);
     add(f10, T(0.5) * (c00.x + c10.x), T(0.5) * (c00.y + c10.y));
-    add(f00 + 1, T(0.5) * (c00.x + c01.x), T(0.5) * (c00.y + c01.y));
-    add(f10 + 1, T(0.25) * (((c00.x + c10.x) + c01.x) + c11.x), T(0.25) * (((c00.y + c10.y) + c01.y) + c11.y));
+    add(f01, T(0.5) * (c00.x + c01.x), T(0.5) * (c00.y + c01.y));
+    add(f11, T(0.25) * (((c00.x + c10.x) + c01.x) + c11.x), T(0.25) * (((c00.y + c10.y) + c01.y) + c11.y));
 }
 
 template <class T>
@@ -496,11 +510,12 @@ __global__ void __launch_bounds__(1024) k_bmg_coarsest(T* __restrict__ X, const 
             for (int p = threadIdx.x; p < nn; p += blockDim.x) {
                 const int i = p / n, j = p - i * n;
                 if (((i + j) & 1) != c) continue;
+                const size_t q = pidx(n, i, j);
                 T Su, Sv, u, v;
                 nbr_sums(X, n, i, j, Su, Sv);
-                const auto b = ld2(Bv, p);
-                block_update(load_blk(K, p), su, sv, su4, sv4, b.x, b.y, Su, Sv, u, v);
-                st2(X, p, u, v);
+                const auto b = ld2(Bv, q);
+                block_update(load_blk(K, q), su, sv, su4, sv4, b.x, b.y, Su, Sv, u, v);
+                st2(X, q, u, v);
             }
             __syncthreads();
         }
@@ -553,13 +568,13 @@ __global__ void __launch_bounds__(512, 1) k_bmg_tail(const TailLvl* __restrict__
         for (int idx = tid; idx < n * half; idx += nt) {
             const int i = idx / half, jj = idx - i * half;
             const int j = 2 * jj + ((i + colour) & 1), jo = 2 * jj + 1 - ((i + colour) & 1);
-            const size_t p = (size_t)i * n + j;
+            const size_t p = pidx(n, i, j);
             const auto b = ld2(Bv, p);
             T Su = T(0), Sv = T(0), u, v;
             if (!first) nbr_sums(X, n, i, j, Su, Sv);
             block_update(load_blk_s(K, p), su, sv, su4, sv4, b.x, b.y, Su, Sv, u, v);
             st2(X, p, u, v);
-            if (first) st2(X, (size_t)i * n + jo, T(0), T(0));
+            if (first) st2(X, pidx(n, i, jo), T(0), T(0));
         }
         if (small) __syncwarp();
         else __syncthreads();
@@ -597,7 +612,7 @@ __global__ void __launch_bounds__(512, 1) k_bmg_tail(const TailLvl* __restrict__
             resid_at<T, true>(X, Bv, K, nf, ip, jp, su, sv, au, av);
             coru = coru + au;
             corv = corv + av;
-            st2(Bc, (size_t)idx, ((T(4) * cu + T(2) * edgeu) + coru) * T(0.0625),
+            st2(Bc, pidx(nc, I, J), ((T(4) * cu + T(2) * edgeu) + coru) * T(0.0625),
                 ((T(4) * cv + T(2) * edgev) + corv) * T(0.0625));
         }
         if (small) __syncwarp();
@@ -694,15 +709,17 @@ __device__ __forceinline__ void kfine_point(double u, double v, float c1, float 
 
 // c1 = 1/dt + (B + 1), c2 = 1/dt and B in the multigrid's precision (rounded on the host)
 template <class T>
-__global__ void __launch_bounds__(256) k_bmg_kfine(const double* __restrict__ w, size_t nn, T c1, T c2, T B,
+__global__ void __launch_bounds__(256) k_bmg_kfine(const double* __restrict__ w, int n, T c1, T c2, T B,
                                                    T* __restrict__ K) {
     pdl_wait();
     pdl_trigger();
+    const size_t nn = (size_t)n * n;
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nn) return;
+    const int i = (int)(p / n), j = (int)(p - (size_t)i * n);
     Blk<T> k;
     kfine_point(w[p], w[nn + p], c1, c2, B, k);
-    store_blk(K, p, k);
+    store_blk(K, pidx(n, i, j), k);
 }
 
 // Full weighting of the four block components to the next coarser level.
@@ -716,7 +733,7 @@ __global__ void __launch_bounds__(256) k_bmg_krestrict(const T* __restrict__ Kf,
     if (I >= nc || J >= nc) return;
     const int i = 2 * I, j = 2 * J;
     const int im = i == 0 ? nf - 1 : i - 1, ip = i + 1, jm = j == 0 ? nf - 1 : j - 1, jp = j + 1;
-    auto at = [Kf, nf](int a, int b) { return load_blk(Kf, (size_t)a * nf + b); };
+    auto at = [Kf, nf](int a, int b) { return load_blk(Kf, pidx(nf, a, b)); };
     const Blk<T> c = at(i, j), w = at(i, jm), e = at(i, jp), s = at(im, j), nth = at(ip, j);
     const Blk<T> sw = at(im, jm), se = at(im, jp), nw = at(ip, jm), ne = at(ip, jp);
     auto fw = [](T ctr, T w_, T e_, T s_, T n_, T sw_, T se_, T nw_, T ne_) {
@@ -729,27 +746,31 @@ __global__ void __launch_bounds__(256) k_bmg_krestrict(const T* __restrict__ Kf,
     o.k12 = fw(c.k12, w.k12, e.k12, s.k12, nth.k12, sw.k12, se.k12, nw.k12, ne.k12);
     o.k21 = fw(c.k21, w.k21, e.k21, s.k21, nth.k21, sw.k21, se.k21, nw.k21, ne.k21);
     o.k22 = fw(c.k22, w.k22, e.k22, s.k22, nth.k22, sw.k22, se.k22, nw.k22, ne.k22);
-    store_blk(Kc, (size_t)I * nc + J, o);
+    store_blk(Kc, pidx(nc, I, J), o);
 }
 
 // FP64 planes <-> interleaved level pairs (used only when the finest level is also the coarsest).
 template <class T>
-__global__ void k_bmg_in(const double* __restrict__ r, size_t nn, T* __restrict__ B) {
+__global__ void k_bmg_in(const double* __restrict__ r, int n, T* __restrict__ B) {
     pdl_wait();
     pdl_trigger();
+    const size_t nn = (size_t)n * n;
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < nn) st2(B, p, from_f64<T>(r[p]), from_f64<T>(r[nn + p]));
+    if (p >= nn) return;
+    const int i = (int)(p / n), j = (int)(p - (size_t)i * n);
+    st2(B, pidx(n, i, j), from_f64<T>(r[p]), from_f64<T>(r[nn + p]));
 }
 template <class T>
-__global__ void k_bmg_out(const T* __restrict__ X, size_t nn, double* __restrict__ z) {
+__global__ void k_bmg_out(const T* __restrict__ X, int n, double* __restrict__ z) {
     pdl_wait();
     pdl_trigger();
+    const size_t nn = (size_t)n * n;
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < nn) {
-        const auto x = ld2(X, p);
-        z[p] = to_f64(x.x);
-        z[nn + p] = to_f64(x.y);
-    }
+    if (p >= nn) return;
+    const int i = (int)(p / n), j = (int)(p - (size_t)i * n);
+    const auto x = ld2(X, pidx(n, i, j));
+    z[p] = to_f64(x.x);
+    z[nn + p] = to_f64(x.y);
 }
 
 constexpr int kBmgCoarsestSweeps = 30;
@@ -1005,9 +1026,9 @@ void BrussMG2D::set_state(const double* w) {
     const double c1 = 1.0 / P_.dt + (P_.B + 1.0), c2 = 1.0 / P_.dt;
     const unsigned g = (unsigned)((nn + 255) / 256);
     if (precision_ == NUMA_GPU_FP64)
-        launch_pdl(k_bmg_kfine<double>, g, 256, 0, ctx_.stream, w, nn, c1, c2, P_.B, tp<double>(levels_[0]->k));
+        launch_pdl(k_bmg_kfine<double>, g, 256, 0, ctx_.stream, w, (int)n0_, c1, c2, P_.B, tp<double>(levels_[0]->k));
     else
-        launch_pdl(k_bmg_kfine<float>, g, 256, 0, ctx_.stream, w, nn, (float)c1, (float)c2, (float)P_.B,
+        launch_pdl(k_bmg_kfine<float>, g, 256, 0, ctx_.stream, w, (int)n0_, (float)c1, (float)c2, (float)P_.B,
                                                        tp<float>(levels_[0]->k));
     ctx_.count_launch();
     for (size_t l = 0; l + 1 < levels_.size(); ++l) {
@@ -1046,7 +1067,7 @@ void BrussMG2D::cycle(size_t l) {
     }
     if (coarsest) {
         if (finest) {
-            launch_pdl(k_bmg_in<T>, (unsigned)((nn + 255) / 256), 256, 0, s, r0_, nn, Bv);
+            launch_pdl(k_bmg_in<T>, (unsigned)((nn + 255) / 256), 256, 0, s, r0_, n, Bv);
             ctx_.count_launch();
         }
         if (nn <= (size_t)kBmgOneBlockPoints) {
@@ -1063,7 +1084,7 @@ void BrussMG2D::cycle(size_t l) {
             }
         }
         if (finest) {
-            launch_pdl(k_bmg_out<T>, (unsigned)((nn + 255) / 256), 256, 0, s, X, nn, z0_);
+            launch_pdl(k_bmg_out<T>, (unsigned)((nn + 255) / 256), 256, 0, s, X, n, z0_);
             ctx_.count_launch();
         }
         return;
