@@ -250,6 +250,31 @@ dim3 b2_grid(int n) {
     return dim3(gx, gy);
 }
 
+// The same product from an FP32 d (the multigrid's output): no conversion, so no shared-memory
+// tile — neighbours come through L1; the arithmetic is k_b2_jvp32's, operation for operation.
+__global__ void __launch_bounds__(256) k_b2_jvp32f(const float2* __restrict__ coef, const float* __restrict__ d,
+                                                   double* __restrict__ out, B2Geom32 G) {
+    pdl_wait();
+    pdl_trigger();
+    const int n = G.n;
+    const size_t nn = (size_t)n * n;
+    const int j = blockIdx.x * 32 + threadIdx.x;
+    if (j >= n) return;
+    const int jm = j == 0 ? n - 1 : j - 1, jp = j + 1 == n ? 0 : j + 1;
+    for (int i = blockIdx.y * 8 + threadIdx.y; i < n; i += gridDim.y * 8) {
+        const int im = i == 0 ? n - 1 : i - 1, ip = i + 1 == n ? 0 : i + 1;
+        const size_t r = (size_t)i * n, p = r + j;
+        const float du = d[p], dv = d[nn + p];
+        const float lu = ((d[r + jm] - du) + (d[r + jp] - du)) + ((d[(size_t)im * n + j] - du) + (d[(size_t)ip * n + j] - du));
+        const float* e = d + nn;
+        const float lv = ((e[r + jm] - dv) + (e[r + jp] - dv)) + ((e[(size_t)im * n + j] - dv) + (e[(size_t)ip * n + j] - dv));
+        const float2 c = coef[p];
+        const float a11 = G.c1 - c.x, a21 = c.x - G.B, a22 = G.invdt + c.y;
+        out[p] = f32_to_f64(__fmaf_rn(-c.y, dv, __fmaf_rn(-G.duh, lu, a11 * du)));
+        out[nn + p] = f32_to_f64(__fmaf_rn(a22, dv, __fmaf_rn(a21, du, -G.dvh * lv)));
+    }
+}
+
 // ============================================================================== BrussMG2D kernels
 template <class T> struct P2;
 template <> struct P2<float> { using t = float2; };
@@ -930,9 +955,8 @@ void Brusselator2D::jvp_bound32(const float* v32, double* out) {
         throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Brusselator2D: no FP32 product bound");
     const B2Geom G = b2_geom(n_, P_);
     const B2Geom32 G32{(int)n_, (float)G.invdt, (float)G.B, (float)G.c1, (float)G.duh, (float)G.dvh};
-    const dim3 grid((unsigned)((n_ + 31) / 32), (unsigned)((n_ + 7) / 8));
-    launch_pdl(k_b2_jvp32<float>, grid, dim3(32, 8), 0, ctx_.stream, reinterpret_cast<const float2*>(coef32_.p), v32, out,
-                                                             G32);
+    launch_pdl(k_b2_jvp32f, b2_grid((int)n_), dim3(32, 8), 0, ctx_.stream, reinterpret_cast<const float2*>(coef32_.p),
+               v32, out, G32);
     ctx_.count_launch();
     ctx_.check_launch("Brusselator2D jvp32 (fp32 input)");
 }
