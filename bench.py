@@ -305,6 +305,20 @@ def run_ours(args) -> int:
                                    stream)
     x_other = x.numpy() if dist.rank == 0 else None
 
+    # the inexact Chebyshev method (chebyshev_inexact, two linear solves and F'' per step) on both paths
+    sec_c64, res_c64, _ = timed_solves(G, ctx, op, pc64, x, u0, "cheb", params_for(G, "fp64"), 2, 1, dist, stream)
+    x_c64 = x.numpy() if dist.rank == 0 else None
+    sec_c32, res_c32, _ = timed_solves(G, ctx, op, pc32, x, u0, "cheb", params_for(G, "mixed"), 2, 1, dist, stream)
+    x_c32 = x.numpy() if dist.rank == 0 else None
+    ckeys = ("iters", "n_F", "n_JVP", "n_D2", "n_lin_iters", "n_prec", "converged")
+    cheb = {"plain_fp64_s": sec_c64, "mixed_s": sec_c32, "ratio": sec_c64 / sec_c32,
+            "counts_fp64": {k: res_c64[k] for k in ckeys}, "counts_mixed": {k: res_c32[k] for k in ckeys},
+            "rel_err_between_paths": (float(np.linalg.norm(x_c32 - x_c64) / np.linalg.norm(x_c64))
+                                      if dist.rank == 0 else None),
+            "note": "chebyshev_inexact (J z = F, J w = F''[z, z], trial x - z - w/2, analytic F''), same "
+                    "configuration and preconditioners as the headline; mixed = FGMRES with the FP32 V-cycle and "
+                    "FP32 J v for both linear solves"}
+
     # the learned preconditioner beside the V-cycle inside FGMRES (trained here, on this GPU, from
     # GMG-preconditioned solves of this grid at seeded lambda; lambda of the bench is held out)
     learned = None
@@ -439,6 +453,7 @@ def run_ours(args) -> int:
                                "note": "mixed = FP32 V-cycle + FP32 Jacobian products inside FGMRES(30) with one-pass "
                                        "classical Gram-Schmidt, FP64 residual / updates / Arnoldi; no learned "
                                        "preconditioner"},
+            "chebyshev": cheb,
             "learned_mixed": learned_summary(learned, fp64_sec, x_head if args.path == "fp64" else x_other),
             "batched": batched,
             "brusselator2d": bruss,
