@@ -101,6 +101,18 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int lim
     return false;
 }
 
+// Bulk copy by the tensor memory accelerator (non-tensor form): `bytes` (a multiple of 16) from
+// global src to shared dst (both 16-byte aligned), counted as transaction bytes on mbarrier bar.
+__device__ __forceinline__ void tma_bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+// One arrival on bar that also expects `bytes` of transactions before the phase can complete.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -136,16 +148,16 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
     return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-// Shared memory of k_conv3d_tc: resident weights, then the three spans.
+// Shared memory of k_conv3d_tc: resident weights, then two buffers of the three spans.
 template <int CIN, int COUT>
 __host__ __device__ constexpr size_t conv_weight_bytes() {
     return (size_t)27 * (CIN / 16) * 2 * COUT * 16;
 }
-// Weights plus the three spans: two CTAs fit on an SM at every supported shape (<= 105 KB each),
-// so one CTA's copies overlap the other's MMAs and epilogue.
+// Weights plus two span buffers (<= 153 KB at the largest supported shape): the spans of the next
+// tile are copied by the TMA into one buffer while the MMAs of this tile read the other.
 template <int CIN, int COUT>
 inline size_t conv_smem_bytes(const VoxGrid& g) {
-    return conv_weight_bytes<CIN, COUT>() + (size_t)3 * (CIN / 8) * g.span * 16;
+    return conv_weight_bytes<CIN, COUT>() + (size_t)2 * 3 * (CIN / 8) * g.span * 16;
 }
 
 constexpr int kConvWaitLimit = 1 << 22;
@@ -163,15 +175,21 @@ __global__ void __launch_bounds__(128) k_conv3d_tc(const uint4* __restrict__ in,
     constexpr int KC = CIN / 16, PL = CIN / 8;
     constexpr uint32_t kCols = 32;
     extern __shared__ __align__(128) unsigned char conv_smem[];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar;     // MMA completion
+    __shared__ __align__(8) uint64_t lbar[2];  // span copies of buffer 0 / 1
     __shared__ uint32_t tmem_slot;
     uint4* w_s = reinterpret_cast<uint4*>(conv_smem);
     uint4* a_s = reinterpret_cast<uint4*>(conv_smem + conv_weight_bytes<CIN, COUT>());
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int bufsz = 3 * PL * g.span;  // uint4 per span buffer
 
     for (int e = tid; e < (int)(conv_weight_bytes<CIN, COUT>() / 16); e += 128) w_s[e] = wg[e];
     if (warp == 0) tmem_alloc(&tmem_slot, kCols);
-    if (tid == 0) mbar_init(smem_addr(&mbar), 1);
+    if (tid == 0) {
+        mbar_init(smem_addr(&mbar), 1);
+        mbar_init(smem_addr(&lbar[0]), 1);
+        mbar_init(smem_addr(&lbar[1]), 1);
+    }
     fence_proxy_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -181,21 +199,42 @@ __global__ void __launch_bounds__(128) k_conv3d_tc(const uint4* __restrict__ in,
     constexpr uint32_t idesc = umma_idesc_bf16(128, COUT);
     bool ok = true;
 
+    // Thread 0: the 3 * PL spans of tile t into buffer b, one bulk copy each (a span is g.span
+    // consecutive 16-byte rows of one 8-channel plane), completing on lbar[b].
+    auto issue = [&](int t, int b) {
+        const uint32_t lb = smem_addr(&lbar[b]);
+        mbar_arrive_expect_tx(lb, (uint32_t)bufsz * 16u);
+        const int start = g.pp + 128 * t;  // padded row of tile row 0
+        for (int dz = 0; dz < 3; ++dz)
+            for (int p = 0; p < PL; ++p) {
+                const int q0 = start + (dz - 1) * g.pp - g.np - 1;
+                tma_bulk_g2s(smem_addr(a_s + (size_t)b * bufsz + (size_t)(dz * PL + p) * g.span),
+                             in + (size_t)p * g.rows + g.front + q0, (uint32_t)g.span * 16u, lb);
+            }
+    };
+    if (tid == 0 && (int)blockIdx.x < g.tiles) issue(blockIdx.x, 0);
+    bool prefetched = false;   // a copy into the other buffer is in flight
+    bool mma_issued = false;   // this iteration's MMAs were issued
+
     int it = 0;
     for (int t = blockIdx.x; t < g.tiles; t += gridDim.x, ++it) {
         const int start = g.pp + 128 * t;  // padded row of tile row 0
-        const int total = 3 * PL * g.span;
-        for (int e = tid; e < total; e += 128) {
-            const int r = e % g.span, rest = e / g.span, p = rest % PL, dz = rest / PL;
-            const int q = start + (dz - 1) * g.pp - g.np - 1 + r;
-            a_s[e] = in[(size_t)p * g.rows + g.front + q];
+        const int b = it & 1;
+        // the next tile's spans into the other buffer (its last MMAs were waited for below)
+        prefetched = t + (int)gridDim.x < g.tiles;
+        if (tid == 0 && prefetched) issue(t + gridDim.x, b ^ 1);
+        // this tile's spans (every thread waits, bounded; the block gives up together)
+        const int landed = mbar_wait(smem_addr(&lbar[b]), (uint32_t)((it >> 1) & 1), kConvWaitLimit) ? 1 : 0;
+        if (!__syncthreads_and(landed)) {
+            ok = false;
+            if (tid == 0) atomicOr(err, 1u);
+            break;
         }
-        fence_proxy_async_smem();
-        __syncthreads();
+        mma_issued = true;
         if (tid == 0) {
             tc_fence_after();
             uint32_t acc = 0;
-            const uint32_t a0 = smem_addr(a_s), w0 = smem_addr(w_s);
+            const uint32_t a0 = smem_addr(a_s + (size_t)b * bufsz), w0 = smem_addr(w_s);
 #pragma unroll 1
             for (int tap = 0; tap < 27; ++tap) {
                 const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
@@ -217,6 +256,7 @@ __global__ void __launch_bounds__(128) k_conv3d_tc(const uint4* __restrict__ in,
             if (tid == 0) atomicOr(err, 1u);
             break;
         }
+        mma_issued = false;
         tc_fence_after();
         float v[COUT];
 #pragma unroll
@@ -254,7 +294,13 @@ __global__ void __launch_bounds__(128) k_conv3d_tc(const uint4* __restrict__ in,
         tc_fence_before();
         __syncthreads();
     }
-    (void)ok;
+    if (!ok && tid == 0) {
+        // a block that gave up drains its copies and MMAs still in flight (bounded) before its shared
+        // and tensor memory are released
+        mbar_wait(smem_addr(&lbar[it & 1]), (uint32_t)((it >> 1) & 1), kConvWaitLimit);
+        if (prefetched) mbar_wait(smem_addr(&lbar[(it + 1) & 1]), (uint32_t)(((it + 1) >> 1) & 1), kConvWaitLimit);
+        if (mma_issued) mbar_wait(bar, (uint32_t)(it & 1), kConvWaitLimit);
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
