@@ -65,7 +65,7 @@ def parse_args(argv=None):
     ap.add_argument("--no-brusselator", action="store_true", help="skip the 2D Brusselator leg")
     ap.add_argument("--cpu-sample-n", type=int, default=127)
     ap.add_argument("--cpu-reps", type=int, default=2)
-    ap.add_argument("--kernel-case", choices=["none", "vcycle", "solve", "conv", "bruss"], default="none",
+    ap.add_argument("--kernel-case", choices=["none", "vcycle", "solve", "conv", "bruss", "stencils"], default="none",
                     help="profiling driver: run only this small case (for ncu)")
     return ap.parse_args(argv)
 
@@ -608,6 +608,30 @@ def run_kernel_case(G, ctx, args) -> int:
         for _ in range(max(1, args.steps)):
             G.diag_conv3d(ctx, nc, xin, w)
         print(json.dumps({"kernel_case": "conv", "n": nc, "launches": ctx.kernel_launches()}))
+        return 0
+    if args.kernel_case == "stencils":
+        # the finite-difference and second-difference products of Bratu3D at n^3, and the 5-point
+        # Burgers2D stencils with one HelmholtzMG2D V-cycle at 511^2
+        op = G.Bratu3D(ctx, n, args.lam)
+        xv = ctx.from_numpy(0.3 * np.sin(0.37 * np.arange(N) + 0.5))
+        vv = ctx.from_numpy(np.sin(0.37 * np.arange(N) + 0.5))
+        out = ctx.vec(N)
+        op.jvp(xv, vv, out, G.FD)
+        op.d2(xv, vv, out, G.ANALYTIC)
+        op.d2(xv, vv, out, G.FD)
+        nb = 511
+        bop = G.Burgers2D(ctx, nb, 0.05, 0.1, 1.0)
+        w = ctx.from_numpy(0.5 * np.sin(0.37 * np.arange(2 * nb * nb) + 0.5))
+        d = ctx.from_numpy(0.7 * np.sin(0.37 * np.arange(2 * nb * nb) + 1.1))
+        bo = ctx.vec(2 * nb * nb)
+        bop.eval(w, bo)
+        bop.jvp(w, d, bo)
+        hmg = G.HelmholtzMG2D(ctx, nb, 10.0, 0.05)
+        r = ctx.from_numpy(np.sin(0.37 * np.arange(nb * nb) + 0.5))
+        z = ctx.vec(nb * nb)
+        hmg(r, z)
+        ctx.sync()
+        print(json.dumps({"kernel_case": "stencils", "n": n, "launches": ctx.kernel_launches()}))
         return 0
     if args.kernel_case == "bruss":
         # implicit-Euler steps of the 2D Brusselator at n^2 (FP32 coupled multigrid inside FGMRES(40))

@@ -1562,6 +1562,15 @@ int numa_gpu_diag_exp(const numa_gpu_vec* x, numa_gpu_vec* out, numa_gpu_vec* cu
     });
 }
 
+int numa_gpu_diag_div(const numa_gpu_vec* a, double b, numa_gpu_vec* out) {
+    if (!a || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(a->ctx, [&] {
+        same_ctx(a->ctx, out);
+        need(out->n == a->n, NUMA_GPU_ERR_SIZE_MISMATCH, "output length differs");
+        diag_div(*a->ctx->impl, a->d, b, out->d, a->n);
+    });
+}
+
 int numa_gpu_diag_conv3d(numa_gpu_ctx* ctx, size_t n, int cin, int cout, int adjoint, const float* x,
                          const float* w, const float* bias, float* y) {
     if (!ctx || !x || !w || !y) return NUMA_GPU_ERR_INVALID_ARGUMENT;

@@ -181,6 +181,27 @@ __device__ __forceinline__ double f32_to_f64(float f) {
     return (double)f;  // subnormal, infinity, NaN
 }
 
+// RN(a / b) from y = RN(1/b), for many a divided by one b (Markstein's correction): q = RN(a y) is
+// within one ulp of a/b, r = a - b q is exact by FMA, and RN(q + r y) is the correctly rounded
+// quotient.  That needs a, q and y well inside the normal range (r ~ 2^-52 a must not underflow):
+// outside [2^-960, 2^1001) — zeros, subnormals, infinities, NaN — the IEEE division runs instead.
+// Three FP64 instructions instead of a full division.
+__device__ __forceinline__ unsigned fp64_biased_exp(double v) {
+    return ((unsigned)__double2hiint(v) >> 20) & 0x7FFu;
+}
+// y for div_by_recip: RN(1/b), or 0 (every quotient then takes the IEEE division) when b is outside
+// [2^-960, 2^960].
+__device__ __forceinline__ double recip_for_div(double b) {
+    return fp64_biased_exp(b) - 63u <= 1920u ? __ddiv_rn(1.0, b) : 0.0;
+}
+__device__ __forceinline__ double div_by_recip(double a, double b, double y) {
+    const double q = __dmul_rn(a, y);
+    const double r = __fma_rn(-q, b, a);
+    const double q2 = __fma_rn(r, y, q);
+    if (fp64_biased_exp(a) - 63u > 1960u || fp64_biased_exp(q2) - 63u > 1960u) return __ddiv_rn(a, b);
+    return q2;
+}
+
 // ------------------------------------------------------------------------------------------
 // e^x by Tang's table-driven method (P. T. P. Tang, "Table-driven implementation of the
 // exponential function in IEEE floating-point arithmetic", ACM TOMS 15(2):144-157, 1989):
@@ -341,6 +362,8 @@ enum ScalarSlot : int {
     kSlotFdRh = 17,
     kSlotFdZero = 18,
     kSlotFdXnorm = 19,
+    kSlotFdInvH = 20,     // RN(1/h) and RN(1/h^2) for the quotients
+    kSlotFdInvHH = 21,
     kSlotGmresH = 64,     // Hessenberg column, m + 2 entries
     kSlotGmresH2 = 320,   // CGS2 second-pass coefficients, up to 8
     kSlotGmresY = 400,    // least-squares solution y, m entries

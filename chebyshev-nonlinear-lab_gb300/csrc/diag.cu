@@ -36,7 +36,22 @@ __global__ void k_exp_pair(const double* __restrict__ x, double* __restrict__ ou
     }
 }
 
+// out = a / b through the finite-difference quotients' reciprocal form
+__global__ void k_div_recip(const double* __restrict__ a, double b, double* __restrict__ out, size_t N) {
+    const double y = recip_for_div(b);
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride)
+        out[p] = div_by_recip(a[p], b, y);
+}
+
 }  // namespace
+
+void diag_div(Context& ctx, const double* a, double b, double* out, size_t N) {
+    size_t g = (N + 255) / 256, cap = (size_t)ctx.sm_count * 16;
+    k_div_recip<<<(unsigned)std::max<size_t>(1, std::min(g, cap)), 256, 0, ctx.stream>>>(a, b, out, N);
+    ctx.count_launch();
+    ctx.check_launch("diag div");
+}
 
 void diag_exp(Context& ctx, const double* x, double* out, double* ref, size_t N) {
     size_t g = (N + 255) / 256, cap = (size_t)ctx.sm_count * 16;

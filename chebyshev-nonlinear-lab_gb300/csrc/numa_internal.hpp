@@ -482,6 +482,7 @@ KrylovParams params_from_c(const numa_krylov_params* p);
 double diag_fp64_peak_tflops(Context& ctx);
 // out = the library's e^x (exp_tang) of x; ref (optional) = CUDA's exp(x).
 void diag_exp(Context& ctx, const double* x, double* out, double* ref, size_t N);
+void diag_div(Context& ctx, const double* a, double b, double* out, size_t N);
 // One tensor-core 3x3x3 convolution from host buffers (learned.cu): y = conv(x, W) + b, FP32
 // channel-last in and out, BF16 operands; flip = the adjoint convolution (gradient with respect to
 // the input, W of shape [27][cin][cout] used as [27][cout][cin] with the taps reversed).

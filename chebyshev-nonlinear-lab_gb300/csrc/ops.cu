@@ -13,7 +13,7 @@ namespace {
 // ||v|| and the finite-difference step h = scale (1 + ||x||) / ||v|| on the device; a zero
 // direction raises the flag that makes the quotient kernels write zeros (operator.hpp:105-106).
 __global__ void __launch_bounds__(kRedThreads) k_fd_step(const double* __restrict__ v, size_t N, RedArgs red,
-                                                         double scale, double* slots /* h, 1/h, zero, xnorm */) {
+                                                         double scale, double* slots /* h, h^2, zero, xnorm, RN(1/h), RN(1/h^2) */) {
     __shared__ double sm[1][32];
     double s[1] = {0.0};
     const size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -25,11 +25,15 @@ __global__ void __launch_bounds__(kRedThreads) k_fd_step(const double* __restric
             slots[0] = 0.0;
             slots[1] = 0.0;
             slots[2] = 1.0;
+            slots[4] = 0.0;
+            slots[5] = 0.0;
         } else {
             const double h = __ddiv_rn(scale * (1.0 + slots[3]), nv);
             slots[0] = h;
             slots[1] = h * h;
             slots[2] = 0.0;
+            slots[4] = recip_for_div(h);          // kSlotFdInvH
+            slots[5] = recip_for_div(slots[1]);   // kSlotFdInvHH
         }
     });
 }
@@ -42,24 +46,24 @@ __global__ void k_fd_shift(const double* __restrict__ x, const double* __restric
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride) xp[p] = x[p] + a * v[p];
 }
 
-// out = (f1 - f0) / h  (operator.hpp:113)
+// out = (f1 - f0) / h  (operator.hpp:113); the correctly rounded quotient from RN(1/h)
 __global__ void k_fd_quot(const double* __restrict__ f1, const double* __restrict__ f0,
                           const double* __restrict__ slots, double* __restrict__ out, size_t N) {
-    const double h = slots[0];
+    const double h = slots[0], rh = slots[4];
     const bool zero = slots[2] != 0.0;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride)
-        out[p] = zero ? 0.0 : __ddiv_rn(f1[p] - f0[p], h);
+        out[p] = zero ? 0.0 : div_by_recip(f1[p] - f0[p], h, rh);
 }
 
-// out = (fp - 2 f0 + fm) / (h h)  (operator.hpp:132-133)
+// out = (fp - 2 f0 + fm) / (h h)  (operator.hpp:132-133); the correctly rounded quotient from RN(1/h^2)
 __global__ void k_fd2_quot(const double* __restrict__ fp, const double* __restrict__ f0, const double* __restrict__ fm,
                            const double* __restrict__ slots, double* __restrict__ out, size_t N) {
-    const double hh = slots[1];
+    const double hh = slots[1], rhh = slots[5];
     const bool zero = slots[2] != 0.0;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < N; p += stride)
-        out[p] = zero ? 0.0 : __ddiv_rn(fp[p] - 2.0 * f0[p] + fm[p], hh);
+        out[p] = zero ? 0.0 : div_by_recip(fp[p] - 2.0 * f0[p] + fm[p], hh, rhh);
 }
 
 unsigned ew_grid(const Context& ctx, size_t N) {

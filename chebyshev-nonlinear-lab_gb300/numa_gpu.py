@@ -222,6 +222,7 @@ SIGNATURES = {
     "numa_gpu_diag_time_smoother": ([_P, _I, _F64P], _I),
     "numa_gpu_diag_time_bmg2d_pass": ([_P, _I, _F64P], _I),
     "numa_gpu_diag_exp": ([_P, _P, _P], _I),
+    "numa_gpu_diag_div": ([_P, C.c_double, _P], _I),
     "numa_gpu_diag_conv3d": ([_P, _SZ, _I, _I, _I, _F32P, _F32P, _F32P, _F32P], _I),
     "numa_gpu_solve_batch": ([_I, C.POINTER(BatchInstance), _SZ, _I, _I, C.POINTER(KrylovParams), _I,
                               C.POINTER(BatchResult), _F64P], _I),
@@ -960,6 +961,11 @@ def mg_apply_noalloc(n: int, r: Vec, z: Vec, pre: int = 2, post: int = 2, stream
 def diag_exp(x: "Vec", out: "Vec", cuda_ref: "Vec | None" = None):
     """out = the library's FP64 e^x (table-driven, as in the residual kernels); cuda_ref = CUDA's exp."""
     x.ctx.check(x.lib.numa_gpu_diag_exp(x.h, out.h, cuda_ref.h if cuda_ref is not None else None), "diag_exp")
+
+
+def diag_div(a: "Vec", b: float, out: "Vec"):
+    """out = a / b through the finite-difference quotients' reciprocal form (correctly rounded)."""
+    a.ctx.check(a.lib.numa_gpu_diag_div(a.h, float(b), out.h), "diag_div")
 
 
 def diag_conv3d(ctx: Context, n: int, x: np.ndarray, w: np.ndarray, bias: np.ndarray | None = None,

@@ -528,6 +528,9 @@ int numa_gpu_diag_time_bmg2d_pass(numa_gpu_bmg2d* mg, int reps, double* ms_per_p
 /* out = e^x as the residual kernels compute it (Tang's table-driven method, FP64); cuda_ref
  * (may be NULL) = CUDA's exp(x).  For accuracy checks of the exponential. */
 int numa_gpu_diag_exp(const numa_gpu_vec* x, numa_gpu_vec* out, numa_gpu_vec* cuda_ref);
+/* out = a / b as the finite-difference quotients compute it: from RN(1/b) with Markstein's
+ * correction, the IEEE division outside the safe exponent range.  out may alias a. */
+int numa_gpu_diag_div(const numa_gpu_vec* a, double b, numa_gpu_vec* out);
 /* One 3x3x3 convolution of the learned preconditioner on the tensor cores (tcgen05, BF16 operands,
  * FP32 accumulation), host buffers in and out, zero padding: y[v][co] = bias[co] +
  * sum_{tap, ci} x[v + tap][ci] w[tap][ci][co] on an n^3 grid (n <= 63), x channel-last [n^3][cin],

@@ -220,3 +220,33 @@ def test_exp_table_driven(gpu):
     special = ~fin
     assert np.array_equal(got[special], cuda[special], equal_nan=True)
     assert np.all(got[x == 0.0] == 1.0)
+
+
+def test_fd_quotient_division_correctly_rounded(gpu):
+    """The finite-difference quotients divide by h (or h^2) through RN(1/h) and Markstein's
+    correction: every quotient must equal the IEEE division bit for bit, for step sizes of the
+    operators' range and for arbitrary divisors, including significands of all ones, zeros,
+    subnormals, huge values, infinities and NaN."""
+    import numa_gpu as G
+    rng = np.random.default_rng(77)
+    M = 400_000
+    a = np.concatenate([
+        rng.standard_normal(M) * 10.0 ** rng.uniform(-30, 30, M),
+        rng.uniform(-1, 1, M) * 2.0 ** rng.integers(-1074, 1023, M),
+        np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, -5e-324, 2.2250738585072014e-308,
+                  1.7976931348623157e308, -1.7976931348623157e308, 1.0, np.nextafter(2.0, 0)]),
+    ])
+    av, out = gpu.from_numpy(a), gpu.vec(a.size)
+    divisors = [1.4901161193847656e-08, 2.2204460492503131e-16, 3.7e-9, 1.2e-17, np.nextafter(2.0, 0),
+                -np.nextafter(1.0, 0), 3.0, 0.1, 1e-300, 1e300, 2.0 ** -960, 2.0 ** 960, 5e-324, 0.0,
+                np.inf, np.nan]
+    divisors += list(rng.uniform(1, 2, 6) * 2.0 ** rng.integers(-1000, 1000, 6))
+    with np.errstate(all="ignore"):
+        for b in divisors:
+            G.diag_div(av, b, out)
+            want = a / b
+            got = out.numpy()
+            assert np.array_equal(got.view(np.int64), want.view(np.int64)) or \
+                np.array_equal(got, want, equal_nan=True), b
+            bad = (got.view(np.int64) != want.view(np.int64)) & ~(np.isnan(got) & np.isnan(want))
+            assert not bad.any(), (b, a[bad][:4], got[bad][:4], want[bad][:4])
