@@ -204,69 +204,53 @@ __device__ __forceinline__ double div_by_recip(double a, double b, double y) {
 
 // ------------------------------------------------------------------------------------------
 // e^x by Tang's table-driven method (P. T. P. Tang, "Table-driven implementation of the
-// exponential function in IEEE floating-point arithmetic", ACM TOMS 15(2):144-157, 1989):
-//   x = (32 M + j) ln2/32 + r, |r| <= ln2/64,   e^x = 2^M * 2^(j/32) * e^r,
-// with 2^(j/32) from a 32-entry table held as hi + lo (hi = RN(2^(j/32)), lo = RN(2^(j/32) - hi))
-// and e^r - 1 = r + r^2 (1/2! + r (1/3! + r (1/4! + r (1/5! + r / 6!)))) (Taylor; truncation below
-// 2e-18).  ln2/32 is split as L1 + L2 and N = round(32 x / ln2) comes from the 1.5 * 2^52
-// shifter, so the reduction is exact to ~1e-21; the result is within ~0.54 ulp of e^x (Tang's
-// bound).  Twelve FP64 instructions, against the FP64 pipe that bounds the residual kernels;
-// the table index, 2^M and the range test are integer work.  |x| >= 708 (overflow, results near
-// or below the smallest normal, infinities, NaN) is left to exp().
-// Table: 2^(j/32), j = 0..31, computed at 60 significant digits.
-__device__ const double2 kExp2Frac[32] = {
-    {0x1.0000000000000p+0, 0x0.0p+0},
-    {0x1.059b0d3158574p+0, 0x1.d73e2a475b465p-55},
-    {0x1.0b5586cf9890fp+0, 0x1.8a62e4adc610bp-54},
-    {0x1.11301d0125b51p+0, -0x1.6c51039449b3ap-54},
-    {0x1.172b83c7d517bp+0, -0x1.19041b9d78a76p-55},
-    {0x1.1d4873168b9aap+0, 0x1.e016e00a2643cp-54},
-    {0x1.2387a6e756238p+0, 0x1.9b07eb6c70573p-54},
-    {0x1.29e9df51fdee1p+0, 0x1.612e8afad1255p-55},
-    {0x1.306fe0a31b715p+0, 0x1.6f46ad23182e4p-55},
-    {0x1.371a7373aa9cbp+0, -0x1.63aeabf42eae2p-54},
-    {0x1.3dea64c123422p+0, 0x1.ada0911f09ebcp-55},
-    {0x1.44e086061892dp+0, 0x1.89b7a04ef80d0p-59},
-    {0x1.4bfdad5362a27p+0, 0x1.d4397afec42e2p-56},
-    {0x1.5342b569d4f82p+0, -0x1.07abe1db13cadp-55},
-    {0x1.5ab07dd485429p+0, 0x1.6324c054647adp-54},
-    {0x1.6247eb03a5585p+0, -0x1.383c17e40b497p-54},
-    {0x1.6a09e667f3bcdp+0, -0x1.bdd3413b26456p-54},
-    {0x1.71f75e8ec5f74p+0, -0x1.16e4786887a99p-55},
-    {0x1.7a11473eb0187p+0, -0x1.41577ee04992fp-55},
-    {0x1.82589994cce13p+0, -0x1.d4c1dd41532d8p-54},
-    {0x1.8ace5422aa0dbp+0, 0x1.6e9f156864b27p-54},
-    {0x1.93737b0cdc5e5p+0, -0x1.75fc781b57ebcp-57},
-    {0x1.9c49182a3f090p+0, 0x1.c7c46b071f2bep-56},
-    {0x1.a5503b23e255dp+0, -0x1.d2f6edb8d41e1p-54},
-    {0x1.ae89f995ad3adp+0, 0x1.7a1cd345dcc81p-54},
-    {0x1.b7f76f2fb5e47p+0, -0x1.5584f7e54ac3bp-56},
-    {0x1.c199bdd85529cp+0, 0x1.11065895048ddp-55},
-    {0x1.cb720dcef9069p+0, 0x1.503cbd1e949dbp-56},
-    {0x1.d5818dcfba487p+0, 0x1.2ed02d75b3707p-55},
-    {0x1.dfc97337b9b5fp+0, -0x1.1a5cd4f184b5cp-54},
-    {0x1.ea4afa2a490dap+0, -0x1.e9c23179c2893p-54},
-    {0x1.f50765b6e4540p+0, 0x1.9d3e12dd8a18bp-54},
-};
+// exponential function in IEEE floating-point arithmetic", ACM TOMS 15(2):144-157, 1989), with a
+// 256-entry table and the work that needs no FP64 moved to the FP32 and integer pipes (on this
+// GPU the FP64 pipe issues about 2 instructions per clock per SM against 128 FP32 ones):
+//   x = (256 M + j) ln2/256 + r,   e^x = 2^M * 2^(j/256) * e^r,   |r| <= ~ln2/512,
+// with 2^(j/256) = T_hi + T_lo from exp2_table.cuh (gen_exp2_table.py).
+//  * N = 256 M + j = round(256 x / ln2) is formed in FP32 from x truncated to FP32 (near a tie it
+//    may be the other neighbour, which only widens |r| a little) and turned into the FP64 value
+//    N exactly through the 1.5 * 2^52 shifter.
+//  * ln2/256 = L1 + L2: r1 = RN(x - N L1) in FP64 (one FMA); the small part N L2 (< 6e-14) is
+//    folded into the table's low word in FP32, to first order: T_lo - T_hi N L2 (1 + r).
+//  * e^r1 - 1 = r1 + r1^2 (1/2 + r1 (1/6 + r1 s)), s = 1/24 + r1/120 in FP32 (it scales r1^4 <
+//    4e-12, so its FP32 rounding stays below 1e-19); truncation below 1e-20.
+//  * y = T_hi + (T_hi (e^r1 - 1) + (T_lo - T_hi N L2 (1 + r))) in [0.99, 2.01], then 2^M by adding
+//    M to the exponent field: for |x| < 708 the result is normal.
+// Eight FP64 instructions (Tang's error analysis applies: within ~0.54 ulp).  |x| >= 708
+// (overflow, results near or below the smallest normal, infinities, NaN) is left to exp().
+#include "exp2_table.cuh"
 
 __device__ __forceinline__ double exp_tang(double x) {
-    if ((__double2hiint(x) & 0x7FFFFFFF) >= 0x40862000) return exp(x);  // |x| >= 708, inf, NaN
-    const double shift = 0x1.8p52;
-    const double t = __fma_rn(x, 0x1.71547652b82fep+5, shift);  // 32/ln2
-    const double nd = __dsub_rn(t, shift);                       // N = round(32 x / ln2), exact
-    const int N = __double2loint(t);
-    double r = __fma_rn(-nd, 0x1.62e42fefa39efp-6, x);  // L1 = RN(ln2/32)
-    r = __fma_rn(-nd, 0x1.abc9e3b39803fp-61, r);         // L2 = RN(ln2/32 - L1)
-    double q = __fma_rn(r, 0x1.6c16c16c16c17p-10, 0x1.1111111111111p-7);
-    q = __fma_rn(r, q, 0x1.5555555555555p-5);
-    q = __fma_rn(r, q, 0x1.5555555555555p-3);
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned ax = hi & 0x7FFFFFFFu;
+    if (ax >= 0x40862000u) return exp(x);  // |x| >= 708, inf, NaN
+    // x truncated to FP32 (exponent re-biased by 896; below 2^-126 it is taken as zero)
+    const float xf = ax > 0x38000000u ? __uint_as_float((hi & 0x80000000u) | ((ax - 0x38000000u) << 3) | (lo >> 29))
+                                      : 0.0f;
+    const float tf = __fmaf_rn(xf, kExpInvL, 0x1.8p23f);
+    const int N = (int)(__float_as_uint(tf) - 0x4B400000u);  // round(256 x / ln2), |N| < 2^18
+    const float nf = __fsub_rn(tf, 0x1.8p23f);
+    const double nd = __dsub_rn(__hiloint2double(0x43380000 + (N >> 31), N), 0x1.8p52);
+    const double r = __fma_rn(-nd, kExpL1, x);
+    const float rf = __fmaf_rn(-nf, kExpL1f, xf);  // r to within ~1e-4 (x up to 708), enough for s and the fold
+    const float sf = __fmaf_rn(rf, 0x1.111112p-7f, 0x1.555556p-5f);  // 1/120, 1/24
+    const double s = __hiloint2double((int)(((__float_as_uint(sf) & 0x7FFFFFFFu) >> 3) + (896u << 20)),
+                                      (int)(__float_as_uint(sf) << 29));  // exact widening, sf in (0.04, 0.05)
+    double q = __fma_rn(r, s, 0x1.5555555555555p-3);  // 1/6
     q = __fma_rn(r, q, 0.5);
-    const double p = __fma_rn(__dmul_rn(r, r), q, r);  // e^r - 1
-    const double2 T = __ldg(&kExp2Frac[N & 31]);
-    const double y = __dadd_rn(T.x, __fma_rn(T.x, p, T.y));  // 2^(j/32) e^r, in [0.98, 2.03]
-    // y * 2^M, M = floor(N / 32), by adding M to the exponent field: for |x| < 708 the result is
-    // a normal number
-    return __hiloint2double(__double2hiint(y) + (N >> 5) * (1 << 20), __double2loint(y));
+    const double p = __fma_rn(__dmul_rn(r, r), q, r);  // e^r1 - 1
+    const int jj = N & 255;
+    const double2 T = __ldg(&kExp2Frac[jj]);
+    const float2 Tf = __ldg(&kExp2FracF[jj]);
+    const float cf = __fmaf_rn(-__fmul_rn(Tf.x, __fmul_rn(nf, kExpL2f)), 1.0f + rf, Tf.y);
+    const unsigned cb = __float_as_uint(cf);
+    const double c = (cb & 0x7F800000u) ? __hiloint2double((int)((cb & 0x80000000u) | (((cb & 0x7FFFFFFFu) >> 3) + (896u << 20))),
+                                                           (int)(cb << 29))
+                                        : 0.0;  // exact widening; FP32 zeros and subnormals (< 1.2e-38) as 0
+    const double y = __dadd_rn(T.x, __fma_rn(T.x, p, c));
+    return __hiloint2double(__double2hiint(y) + (N >> 8) * (1 << 20), __double2loint(y));
 }
 
 // ------------------------------------------------------------------------------------------
