@@ -214,9 +214,11 @@ __global__ void __launch_bounds__(BX* BY) k_jvp32(const float* __restrict__ c32,
 
 // The FP32 product from an FP32 v (the V-cycle's output): no conversion, so no shared-memory tile —
 // a (k, j) column marches in i holding planes i-1, i, i+1 in registers, and the neighbours in j and k
-// come through L1.  The arithmetic is k_jvp32's, operation for operation (same results).
+// come through L1.  The arithmetic is k_jvp32's, operation for operation (same results); OT = float
+// stores the FP32 result as it is, OT = double widens it.
+template <class OT>
 __global__ void __launch_bounds__(BX* BY) k_jvp32f(const float* __restrict__ c32, const float* __restrict__ v,
-                                                   double* __restrict__ out, int n, int ichunk, float h2inv) {
+                                                   OT* __restrict__ out, int n, int ichunk, float h2inv) {
     pdl_wait();
     pdl_trigger();
     const int k = blockIdx.x * BX + threadIdx.x;
@@ -242,7 +244,9 @@ __global__ void __launch_bounds__(BX* BY) k_jvp32f(const float* __restrict__ c32
         s = s - jp;
         s = s - km;
         s = s - kp;
-        out[p] = f32_to_f64(h2inv * s - cc * cur);
+        const float r = h2inv * s - cc * cur;
+        if constexpr (sizeof(OT) == 4) out[p] = r;
+        else out[p] = f32_to_f64(r);
         below = cur;
         cur = above;
     }
@@ -309,9 +313,19 @@ void Bratu3D::bind(const double*, const double* cache, int precision) {
 void Bratu3D::jvp_bound32(const float* v32, double* out) {
     if (bound_precision_ != NUMA_GPU_FP32) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Bratu3D: no FP32 product bound");
     March m = march_shape((int)n_, false);
-    launch_pdl(k_jvp32f, m.grid, dim3(BX, BY), 0, ctx_.stream, bound_c32_, v32, out, (int)n_, m.ichunk, (float)h2inv_);
+    launch_pdl(k_jvp32f<double>, m.grid, dim3(BX, BY), 0, ctx_.stream, bound_c32_, v32, out, (int)n_, m.ichunk,
+               (float)h2inv_);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d jvp32 (fp32 input)");
+}
+
+void Bratu3D::jvp_bound32f(const float* v32, float* out32) {
+    if (bound_precision_ != NUMA_GPU_FP32) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Bratu3D: no FP32 product bound");
+    March m = march_shape((int)n_, false);
+    launch_pdl(k_jvp32f<float>, m.grid, dim3(BX, BY), 0, ctx_.stream, bound_c32_, v32, out32, (int)n_, m.ichunk,
+               (float)h2inv_);
+    ctx_.count_launch();
+    ctx_.check_launch("bratu3d jvp32 (fp32 input and output)");
 }
 
 void Bratu3D::jvp_bound(const double* v, double* out) {

@@ -169,6 +169,8 @@ __device__ __forceinline__ float f64_to_f32(double d) {
     return __double2float_rn(d);  // float subnormals, infinities and NaN: the hardware conversion
 }
 
+__device__ __forceinline__ float f64_to_f32(float f) { return f; }
+
 __device__ __forceinline__ double f32_to_f64(float f) {
     const unsigned b = __float_as_uint(f);
     const unsigned ef = (b >> 23) & 0xFFu;
@@ -180,6 +182,46 @@ __device__ __forceinline__ double f32_to_f64(float f) {
     if ((b & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
     return (double)f;  // subnormal, infinity, NaN
 }
+
+// ------------------------------------------------------------------------------------------
+// Double-FP32 arithmetic (T. J. Dekker, "A floating-point technique for extending the available
+// precision", Numer. Math. 18:224-242, 1971; D. E. Knuth, TAOCP vol. 2, 4.2.2): a value held as
+// hi + lo in two FP32 numbers, about 48 significant bits, on the FP32 pipe.  Used where FP32 data
+// needs products and sums beyond FP32 precision without spending FP64 instructions.
+struct DF {
+    float hi, lo;
+};
+// s + e = a + b exactly (Knuth's two-sum; no ordering of |a|, |b| needed)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// acc += a b: the product is exact as p + pe (FMA), p enters hi through two-sum and the two error
+// terms gather in lo (over the hundred-odd terms a thread sums, lo stays far below hi)
+__device__ __forceinline__ void df_mac(DF& acc, float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float pe = __fmaf_rn(a, b, -p);
+    float s, e;
+    two_sum(acc.hi, p, s, e);
+    acc.hi = s;
+    acc.lo = __fadd_rn(acc.lo, __fadd_rn(e, pe));
+}
+// acc += (c.hi + c.lo) b: c.hi b exact as above, c.lo b (a 2^-24-relative term) in one rounding
+__device__ __forceinline__ void df_mac(DF& acc, DF c, float b) {
+    const float p = __fmul_rn(c.hi, b);
+    const float pe = __fmaf_rn(c.hi, b, -p);
+    float s, e;
+    two_sum(acc.hi, p, s, e);
+    acc.hi = s;
+    acc.lo = __fadd_rn(acc.lo, __fadd_rn(e, __fmaf_rn(c.lo, b, pe)));
+}
+// An FP64 scalar split as hi = RN32(d), lo = RN32(d - hi) (once per thread, not per element)
+__device__ __forceinline__ DF df_split(double d) {
+    const float hi = __double2float_rn(d);
+    return DF{hi, __double2float_rn(__dsub_rn(d, (double)hi))};
+}
+__device__ __forceinline__ double df_to_f64(DF a) { return __dadd_rn(f32_to_f64(a.hi), f32_to_f64(a.lo)); }
 
 // RN(a / b) from y = RN(1/b), for many a divided by one b (Markstein's correction): q = RN(a y) is
 // within one ulp of a/b, r = a - b q is exact by FMA, and RN(q + r y) is the correctly rounded
@@ -353,6 +395,7 @@ enum ScalarSlot : int {
     kSlotGmresY = 400,    // least-squares solution y, m entries
     kSlotGmresCoef = 700, // recycled-solve coefficients, 2k + 1 entries
     kSlotGmresSig2 = 1250, // lazily normalised basis: 1 / norm^2 of each vector, m + 1 entries
+    kSlotGmresSig = 1270,  // FP32 basis: 1 / norm of each vector, m + 1 entries
 };
 
 // Pinned host staging for small vectors moving to the device.

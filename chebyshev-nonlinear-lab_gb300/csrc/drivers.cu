@@ -42,6 +42,8 @@ public:
     // the FP32 cycle can hand its result over unwidened
     bool has_apply32() const override { return mg_.supports_out32(); }
     void apply32(const double* r, float* z32) override { mg_.apply32(r, z32); }
+    bool has_apply32f() const override { return mg_.supports_out32(); }
+    void apply32f(const float* r32, float* z32) override { mg_.apply32f(r32, z32); }
     int kind() const override { return NUMA_GPU_PRECOND_POISSON_MG; }
     PoissonMG& mg() { return mg_; }
 
@@ -169,6 +171,11 @@ public:
         Timers::Scope s(&t_, kT_JVP);
         f_.jvp_bound32(v32, out);
     }
+    bool has_apply32f() const override { return mode_ != NUMA_GPU_DERIV_FD && f_.has_jvp32f(); }
+    void apply32f(const float* v32, float* out32) override {
+        Timers::Scope s(&t_, kT_JVP);
+        f_.jvp_bound32f(v32, out32);
+    }
 
 private:
     NonlinearOp& f_;
@@ -189,6 +196,11 @@ public:
     void apply32(const double* r, float* z32) override {
         Timers::Scope s(&t_, kT_PREC);
         p_->apply32(r, z32);
+    }
+    bool has_apply32f() const override { return p_->has_apply32f(); }
+    void apply32f(const float* r32, float* z32) override {
+        Timers::Scope s(&t_, kT_PREC);
+        p_->apply32f(r32, z32);
     }
 
 private:

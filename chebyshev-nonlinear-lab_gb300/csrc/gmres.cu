@@ -66,6 +66,9 @@ struct StoreVec {
     }
 };
 
+__device__ __forceinline__ double widen(double v) { return v; }
+__device__ __forceinline__ double widen(float v) { return f32_to_f64(v); }
+
 // Fused classical Gram-Schmidt passes over CNT basis vectors (CNT a compile-time count, so the CNT
 // partial sums stay in registers through the two-level reduction).  The vectors are v0 (r = 0) and
 // V + r ldv (r >= 1), so a first vector can live outside the basis array.
@@ -181,9 +184,6 @@ __global__ void k_combine(const double* __restrict__ base, const double* __restr
     }
 }
 
-__device__ __forceinline__ double widen(double v) { return v; }
-__device__ __forceinline__ double widen(float v) { return f32_to_f64(v); }
-
 // x += sum_i coef[i] V_i in one pass (the flexible update; x is read and written in place); V in
 // FP64, or in FP32 widened exactly (the same sums as from the widened vectors)
 template <class VT>
@@ -202,12 +202,134 @@ __global__ void k_combine_add(const VT* __restrict__ V, size_t ldv, int cnt, con
     }
 }
 
+// ---- the FP32 basis (flexible GMRES with the FP32 hand-off and a loose linear tolerance).  The
+// basis vectors u_j are FP32 and scaled to norms near 1; sigma_j = 1/||u_j|| (sig) and sigma_j^2
+// (sig2) are device scalars.  Inner products and updates run in double-FP32 arithmetic on the
+// FP32 pipe, so these passes are bound by HBM, not by the FP64 pipe.
+
+// u0 = RN32(s * src): the first basis vector, normalised by s = 1/||src||
+__global__ void k_to32_scaled(const double* __restrict__ src, double s, float* __restrict__ dst, size_t N) {
+    pdl_wait();
+    pdl_trigger();
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride)
+        dst[i] = f64_to_f32(__dmul_rn(src[i], s));
+}
+
+// MODE 0: h[r] = <w, u_r> for r < CNT.
+// MODE 2: u_out = RN32(sigma_j (w - sum_r h[r] sigma_r^2 u_r)) (the orthogonalised w, scaled by the
+//         previous vector's 1/norm so that the stored vectors keep norms near 1 in FP32 range),
+//         then hout[0] = ||u_out||, sig2[j+1] = 1/||u_out||^2, sig[j+1] = 1/||u_out||.
+// Sums per thread in double-FP32, converted to FP64 for the block and grid reduction.
+template <int CNT, int MODE>
+__global__ void __launch_bounds__(kRedThreads) k_cgs_df(const float* __restrict__ w, const float* __restrict__ U,
+                                                        size_t ldu, const double* __restrict__ hin, double* sig2,
+                                                        double* sig, int j, size_t N, RedArgs red,
+                                                        double* __restrict__ hout, float* __restrict__ uout) {
+    pdl_wait();
+    pdl_trigger();
+    constexpr int R = MODE == 2 ? 1 : CNT;
+    __shared__ double sm[R][32];
+    DF cw{0.0f, 0.0f}, c[CNT];
+    if (MODE == 2) {
+        const double sj = sig[j];
+        cw = df_split(sj);
+#pragma unroll
+        for (int r = 0; r < CNT; ++r) c[r] = df_split(-(sj * hin[r] * sig2[r]));
+    }
+    DF acc[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[r] = DF{0.0f, 0.0f};
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) {
+        const float wi = w[i];
+        if (MODE == 2) {
+            DF t{0.0f, 0.0f};
+            df_mac(t, cw, wi);
+#pragma unroll
+            for (int r = 0; r < CNT; ++r) df_mac(t, c[r], U[(size_t)r * ldu + i]);
+            const float u = __fadd_rn(t.hi, t.lo);
+            uout[i] = u;
+            df_mac(acc[0], u, u);
+        } else {
+#pragma unroll
+            for (int r = 0; r < CNT; ++r) df_mac(acc[r], wi, U[(size_t)r * ldu + i]);
+        }
+    }
+    double s[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) s[r] = df_to_f64(acc[r]);
+    block_sum<R>(s, sm);
+    grid_reduce_finish<R>(s, red, [hout, sig2, sig, j] __device__(const double(&t)[R]) {
+        if (MODE == 2) {
+            const double nrm = __dsqrt_rn(t[0]);
+            hout[0] = nrm;
+            sig2[j + 1] = t[0] > 0.0 ? 1.0 / t[0] : 0.0;
+            sig[j + 1] = nrm > 0.0 ? 1.0 / nrm : 0.0;
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) hout[r] = t[r];
+        }
+    });
+}
+
+// x += scale * sum_r coef[r] Z_r with FP32 Z and |coef| <= 1 (the host normalises them by scale):
+// the sum in double-FP32, then one FMA into x (two FP64 instructions a point)
+__global__ void k_combine_add_df(const float* __restrict__ Z, size_t ldz, int cnt, const double* __restrict__ coef,
+                                 double scale, double* x, size_t N) {
+    pdl_wait();
+    pdl_trigger();
+    extern __shared__ float cf[];  // cnt (hi, lo) pairs
+    for (int r = threadIdx.x; r < cnt; r += blockDim.x) {
+        const DF c = df_split(coef[r]);
+        cf[2 * r] = c.hi;
+        cf[2 * r + 1] = c.lo;
+    }
+    __syncthreads();
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) {
+        DF t{0.0f, 0.0f};
+        for (int r = 0; r < cnt; ++r) df_mac(t, DF{cf[2 * r], cf[2 * r + 1]}, Z[(size_t)r * ldz + i]);
+        x[i] = __fma_rn(scale, df_to_f64(t), x[i]);
+    }
+}
+
+// Launches k_cgs_df<cnt, MODE>; false when cnt is above the largest compiled count.
+template <int MODE>
+bool launch_cgs_df(Context& ctx, int cnt, const float* w, const float* U, size_t N, const double* hin, double* sig2,
+                   double* sig, int j, double* hout, float* uout) {
+    const unsigned g = ctx.red_grid(N);
+    switch (cnt) {
+#define NUMA_CGS_DF_CASE(K)                                                                                  \
+    case K:                                                                                                  \
+        launch_pdl(k_cgs_df<K, MODE>, g, kRedThreads, 0, ctx.stream, w, U, N, hin, sig2, sig, j, N, ctx.red, hout, \
+                   uout);                                                                                    \
+        break;
+        NUMA_CGS_DF_CASE(1)
+        NUMA_CGS_DF_CASE(2)
+        NUMA_CGS_DF_CASE(3)
+        NUMA_CGS_DF_CASE(4)
+        NUMA_CGS_DF_CASE(5)
+        NUMA_CGS_DF_CASE(6)
+        NUMA_CGS_DF_CASE(7)
+        NUMA_CGS_DF_CASE(8)
+#undef NUMA_CGS_DF_CASE
+        default:
+            return false;
+    }
+    ctx.count_launch();
+    return true;
+}
+
 // *out = v (one device scalar from a host value, stream-ordered)
 __global__ void k_set_scalar(double* __restrict__ out, double v) {
     pdl_wait();
     pdl_trigger();
     *out = v;
 }
+
+// Smallest linear tolerance for which FGMRES keeps its basis in FP32 (the FP32 hand-off only).
+constexpr double kV32MinRtol = 1e-5;
 
 unsigned ew_grid(const Context& ctx, size_t N) {
     size_t want = (N + 255) / 256;
@@ -305,7 +427,20 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
     // FP32 preconditioner output into an FP32 product: the preconditioned vectors are kept in FP32
     // (exactly the values the FP64 path would widen), halving their writes and reads
     const bool z32 = M && M->has_apply32() && A.has_apply32();
-    V_.resize((m + 1) * N);
+    // ... and, with a linear tolerance far above FP32 rounding (an inexact-Newton forcing term) and an
+    // operator whose FP32 product can be stored as it is, the whole Arnoldi process runs on FP32
+    // vectors: the basis u_0 = RN32(r / ||r||), u_1, ... and w = A z_j.  Rounding a stored vector
+    // perturbs the Arnoldi relation A Z = V H by 6e-8 relative, which bounds the attainable linear
+    // residual near that; inner products, updates and the solution update are computed in
+    // double-FP32 and reduced in FP64, and the Hessenberg matrix and least squares stay FP64.
+    const bool v32 = z32 && M->has_apply32f() && A.has_apply32f() && o.rtol >= kV32MinRtol;
+    double* sigd = ctx_.scalar(kSlotGmresSig);
+    if (v32) {
+        V32_.resize((m + 1) * N);
+        W32_.resize(N);
+    } else {
+        V_.resize((m + 1) * N);
+    }
     if (z32) Z32_.resize(m * N);
     else Z_.resize(m * N);
     w_.resize(N);
@@ -343,16 +478,29 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
             res.converged = true;
             break;
         }
-        launch_pdl(k_set_scalar, 1, 1, 0, ctx_.stream, sig2, 1.0 / (beta * beta));
-        ctx_.count_launch();
-        sig[0] = 1.0 / beta;
+        if (v32) {
+            launch_pdl(k_to32_scaled, eg, 256, 0, ctx_.stream, v0, 1.0 / beta, V32_.p, N);
+            launch_pdl(k_set_scalar, 1, 1, 0, ctx_.stream, sig2, 1.0);
+            launch_pdl(k_set_scalar, 1, 1, 0, ctx_.stream, sigd, 1.0);
+            ctx_.count_launch(3);
+            sig[0] = 1.0;
+        } else {
+            launch_pdl(k_set_scalar, 1, 1, 0, ctx_.stream, sig2, 1.0 / (beta * beta));
+            ctx_.count_launch();
+            sig[0] = 1.0 / beta;
+        }
         std::fill(g.begin(), g.end(), 0.0);
         g[0] = beta;
         size_t k = 0;
         while (k < m && res.iters < o.max_iters) {
             const size_t j = k;
-            const double* vj = j == 0 ? v0 : V_.p + j * N;
-            if (z32) {
+            const double* vj = v32 ? nullptr : (j == 0 ? v0 : V_.p + j * N);
+            if (v32) {
+                float* zj = Z32_.p + j * N;
+                M->apply32f(V32_.p + j * N, zj);
+                ++res.precs;
+                A.apply32f(zj, W32_.p);
+            } else if (z32) {
                 float* zj = Z32_.p + j * N;
                 M->apply32(vj, zj);
                 ++res.precs;
@@ -365,12 +513,19 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
             }
             ++res.matvecs;
             const int cnt = (int)(j + 1);
-            launch_cgs<0>(ctx_, cnt, w_.p, v0, V_.p, N, nullptr, nullptr, sl, nullptr, nullptr);
-            launch_cgs<2>(ctx_, cnt, w_.p, v0, V_.p, N, sl, sig2, sl + j + 1, V_.p + (j + 1) * N, sig2 + j + 1);
+            if (v32) {
+                launch_cgs_df<0>(ctx_, cnt, W32_.p, V32_.p, N, nullptr, sig2, sigd, (int)j, sl, nullptr);
+                launch_cgs_df<2>(ctx_, cnt, W32_.p, V32_.p, N, sl, sig2, sigd, (int)j, sl + j + 1,
+                                 V32_.p + (j + 1) * N);
+            } else {
+                launch_cgs<0>(ctx_, cnt, w_.p, v0, V_.p, N, nullptr, nullptr, sl, nullptr, nullptr);
+                launch_cgs<2>(ctx_, cnt, w_.p, v0, V_.p, N, sl, sig2, sl + j + 1, V_.p + (j + 1) * N,
+                                      sig2 + j + 1);
+            }
             ctx_.check_launch("arnoldi (lazy cgs1)");
             ctx_.fetch(sl, (int)(j + 2), col.data());
             for (size_t i = 0; i <= j; ++i) H[i][j] = sig[j] * sig[i] * col[i];
-            H[j + 1][j] = sig[j] * col[j + 1];
+            H[j + 1][j] = v32 ? col[j + 1] : sig[j] * col[j + 1];  // the FP32 u_{j+1} carries sigma_j
             sig[j + 1] = col[j + 1] > 0.0 ? 1.0 / col[j + 1] : 0.0;
             for (size_t i = 0; i < j; ++i) {
                 const double t = cs[i] * H[i][j] + sn[i] * H[i + 1][j];
@@ -406,8 +561,17 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
         }
         double* yh = pin_.get(m);
         for (size_t jj = 0; jj < k; ++jj) yh[jj] = y[jj] * sig[jj];
+        double scale = 0.0;
+        if (v32) {
+            for (size_t jj = 0; jj < k; ++jj) scale = std::max(scale, std::abs(yh[jj]));
+            if (scale > 0.0)
+                for (size_t jj = 0; jj < k; ++jj) yh[jj] /= scale;
+        }
         NUMA_CUDA(cudaMemcpyAsync(ydev, yh, k * sizeof(double), cudaMemcpyHostToDevice, ctx_.stream));
-        if (z32) launch_pdl(k_combine_add<float>, eg, 256, k * sizeof(double), ctx_.stream, Z32_.p, N, (int)k, ydev, x, N);
+        if (v32)
+            launch_pdl(k_combine_add_df, eg, 256, 2 * k * sizeof(float), ctx_.stream, Z32_.p, N, (int)k, ydev, scale,
+                       x, N);
+        else if (z32) launch_pdl(k_combine_add<float>, eg, 256, k * sizeof(double), ctx_.stream, Z32_.p, N, (int)k, ydev, x, N);
         else launch_pdl(k_combine_add<double>, eg, 256, k * sizeof(double), ctx_.stream, Z_.p, N, (int)k, ydev, x, N);
         ctx_.count_launch();
         ctx_.check_launch("gmres update (lazy)");

@@ -169,7 +169,9 @@ __global__ void k_scale_in64(const double* __restrict__ r, double* __restrict__ 
 
 // b32 = RN32(r), bs32 = RN32(b32 * RN32(inv)) at the finest FP32 level (conversions in integer
 // arithmetic: no FP64 instruction).
-__global__ void k_scale_in32(const double* __restrict__ r, float* __restrict__ b, float* __restrict__ bs, float inv,
+// RT = double (an FP64 right-hand side, rounded here) or float (already FP32: copied as is)
+template <class RT>
+__global__ void k_scale_in32(const RT* __restrict__ r, float* __restrict__ b, float* __restrict__ bs, float inv,
                              size_t N) {
     pdl_wait();
     pdl_trigger();
@@ -523,8 +525,8 @@ __global__ void __launch_bounds__(BX* BY) k_prolong_split(const float* __restric
 // b32 = RN32(r), bs32 = RN32(b32 * inv) into the split layout at the finest level; WRITE_X: also
 // the cycle's first smoothing pass (colour 0 from x = 0: x = bs / 6).  Thread t handles the
 // natural pair L = 2t (colour 0, index t) and L = 2t + 1 (colour 1, index half + t).
-template <bool WRITE_X>
-__global__ void k_scale_in32_split(const double* __restrict__ r, float* __restrict__ b, float* __restrict__ bs,
+template <bool WRITE_X, class RT>
+__global__ void k_scale_in32_split(const RT* __restrict__ r, float* __restrict__ b, float* __restrict__ bs,
                                    float* __restrict__ x, float inv, int N, int half) {
     pdl_wait();
     pdl_trigger();

@@ -68,6 +68,12 @@ public:
         (void)v32;
         (void)out;
     }
+    // The same product stored in FP32 (its arithmetic is FP32 already), where has_jvp32f().
+    virtual bool has_jvp32f() const { return false; }
+    virtual void jvp_bound32f(const float* v32, float* out32) {
+        (void)v32;
+        (void)out32;
+    }
 
     // Finite-difference forms of operators/operator.hpp:101-134 over eval.  f0 = F(x) must be
     // supplied (the same vector the reference recomputes inside the call); xnorm = ||x|| as a
@@ -108,6 +114,8 @@ public:
     void jvp_bound(const double* v, double* out) override;
     bool has_jvp32() const override { return bound_precision_ == NUMA_GPU_FP32; }
     void jvp_bound32(const float* v32, double* out) override;
+    bool has_jvp32f() const override { return bound_precision_ == NUMA_GPU_FP32; }
+    void jvp_bound32f(const float* v32, float* out32) override;
     void jvp_at(const double* x, const double* v, double* out) override { jvp_x(x, v, out); }
     void jvp_cached(const double*, const double* cache, const double* v, double* out) override {
         jvp_c(cache, v, out);
@@ -284,6 +292,8 @@ public:
     // z32 = V-cycle(r) in FP32 only (the values apply() widens into z), where supports_out32().
     bool supports_out32() const;
     void apply32(const double* r, float* z32);
+    // The same from an FP32 right-hand side (an FP32 Krylov basis vector), read as it is.
+    void apply32f(const float* r32, float* z32);
     // Diagnostic: average time (ms) of one red-black colour pass on the finest level, timed with
     // CUDA events over `reps` back-to-back passes on the context stream.
     double time_finest_pass(int reps);
@@ -315,6 +325,7 @@ private:
     int pre_, post_, precision_;
     std::vector<std::unique_ptr<Level>> levels_;
     float* z32_out_ = nullptr;        // FP32 output of the current apply32
+    const float* in32_ = nullptr;     // FP32 right-hand side of the current apply32f
     DeviceArray<double> scratch_r_;   // residual of the level being restricted (FP64 or FP32 bytes)
     DeviceArray<double> alias_b_;     // copy of r when r and z alias
 };
@@ -363,6 +374,12 @@ public:
         (void)r;
         (void)z32;
     }
+    // z32 = M r32 from an FP32 r, where has_apply32f().
+    virtual bool has_apply32f() const { return false; }
+    virtual void apply32f(const float* r32, float* z32) {
+        (void)r32;
+        (void)z32;
+    }
 };
 
 std::unique_ptr<Provider> make_identity_provider(Context& ctx, size_t N);
@@ -404,6 +421,12 @@ struct LinearOp {
         (void)v32;
         (void)out;
     }
+    // out32 = A v32 stored in FP32, where has_apply32f().
+    virtual bool has_apply32f() const { return false; }
+    virtual void apply32f(const float* v32, float* out32) {
+        (void)v32;
+        (void)out32;
+    }
 };
 struct Precond {
     virtual ~Precond() = default;
@@ -412,6 +435,12 @@ struct Precond {
     virtual bool has_apply32() const { return false; }
     virtual void apply32(const double* r, float* z32) {
         (void)r;
+        (void)z32;
+    }
+    // z32 = M r32 from an FP32 r (an FP32 Krylov basis vector), where has_apply32f().
+    virtual bool has_apply32f() const { return false; }
+    virtual void apply32f(const float* r32, float* z32) {
+        (void)r32;
         (void)z32;
     }
     // Called by GMRES after each Arnoldi step with the iteration count of the solve and the relative
@@ -454,6 +483,8 @@ private:
     size_t N_;
     DeviceArray<double> V_, Z_, w_, r_, comb_, z_, rrec_;
     DeviceArray<float> Z32_;  // FGMRES preconditioned vectors in FP32 (FP32 preconditioner and product)
+    DeviceArray<float> V32_;  // FGMRES basis in FP32 (FP32 hand-off, loose linear tolerance)
+    DeviceArray<float> W32_;  // its A z_j in FP32
     PinnedBuf pin_;
 };
 

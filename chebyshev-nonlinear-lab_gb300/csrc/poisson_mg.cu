@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cstring>
 #include <limits>
+#include <type_traits>
 
 #include "mg_kernels.cuh"
 
@@ -381,6 +382,21 @@ void PoissonMG::apply32(const double* r, float* z32) {
     z32_out_ = nullptr;
 }
 
+void PoissonMG::apply32f(const float* r32, float* z32) {
+    if (!supports_out32()) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "PoissonMG: no FP32 output for this hierarchy");
+    z32_out_ = z32;
+    in32_ = r32;
+    try {
+        apply(nullptr, nullptr);
+    } catch (...) {
+        z32_out_ = nullptr;
+        in32_ = nullptr;
+        throw;
+    }
+    z32_out_ = nullptr;
+    in32_ = nullptr;
+}
+
 void PoissonMG::apply(const double* r, double* z) {
     Level& L0 = *levels_[0];
     const size_t N = N0_;
@@ -399,18 +415,24 @@ void PoissonMG::apply(const double* r, double* z) {
         z0_ = nullptr;
         cycle<double>(0);
     } else {
-        if (L0.n & 1) {
-            const Split g = make_split(L0.n);
-            const unsigned grid = ew_grid(ctx_, (size_t)g.half);
-            if (first_fused32(0))
-                launch_pdl(k_scale_in32_split<true>, grid, 256, 0, ctx_.stream, r, L0.b32.p, L0.bs32.p, L0.xs,
-                                                                        (float)L0.inv, (int)N, g.half);
-            else
-                launch_pdl(k_scale_in32_split<false>, grid, 256, 0, ctx_.stream, r, L0.b32.p, L0.bs32.p, L0.xs,
-                                                                         (float)L0.inv, (int)N, g.half);
-        } else {
-            launch_pdl(k_scale_in32, ew_grid(ctx_, N), 256, 0, ctx_.stream, r, L0.b32.p, L0.bs32.p, (float)L0.inv, N);
-        }
+        auto scale_in = [&](auto rin) {
+            using RT = std::remove_cv_t<std::remove_pointer_t<decltype(rin)>>;
+            if (L0.n & 1) {
+                const Split g = make_split(L0.n);
+                const unsigned grid = ew_grid(ctx_, (size_t)g.half);
+                if (first_fused32(0))
+                    launch_pdl(k_scale_in32_split<true, RT>, grid, 256, 0, ctx_.stream, rin, L0.b32.p, L0.bs32.p,
+                               L0.xs, (float)L0.inv, (int)N, g.half);
+                else
+                    launch_pdl(k_scale_in32_split<false, RT>, grid, 256, 0, ctx_.stream, rin, L0.b32.p, L0.bs32.p,
+                               L0.xs, (float)L0.inv, (int)N, g.half);
+            } else {
+                launch_pdl(k_scale_in32<RT>, ew_grid(ctx_, N), 256, 0, ctx_.stream, rin, L0.b32.p, L0.bs32.p,
+                           (float)L0.inv, N);
+            }
+        };
+        if (in32_) scale_in(in32_);
+        else scale_in(r);
         ctx_.count_launch();
         z0_ = z;
         cycle32(0);
