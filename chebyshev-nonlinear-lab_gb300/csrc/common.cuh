@@ -150,6 +150,12 @@ __device__ __forceinline__ double div_by(double a, double d, double rd) {
 // instructions issue on the (slow) FP64 pipe; these use only integer instructions and give the
 // same results: round-to-nearest-even from the IEEE-754 bit fields, with the rare cases (float
 // subnormals, NaN) handed to the hardware instruction.
+// The hardware conversions for the rare operands (float subnormals, infinities, NaN) sit in calls
+// that are not inlined, so the compiler branches around them instead of predicating them: a
+// conversion involving FP64 issues on the FP64 pipe, which would otherwise be paid by every element.
+static __device__ __noinline__ float f64_to_f32_rare(double d) { return __double2float_rn(d); }
+static __device__ __noinline__ double f32_to_f64_rare(float f) { return (double)f; }
+
 __device__ __forceinline__ float f64_to_f32(double d) {
     const unsigned hi = (unsigned)__double2hiint(d);
     const unsigned lo = (unsigned)__double2loint(d);
@@ -166,7 +172,7 @@ __device__ __forceinline__ float f64_to_f32(double d) {
     }
     if (e == 0 || ef <= -25) return __uint_as_float(sign);  // zero, or too small for a float subnormal
     if (ef >= 255 && e != 0x7FF) return __uint_as_float(sign | 0x7F800000u);
-    return __double2float_rn(d);  // float subnormals, infinities and NaN: the hardware conversion
+    return f64_to_f32_rare(d);  // float subnormals, infinities and NaN: the hardware conversion
 }
 
 __device__ __forceinline__ float f64_to_f32(float f) { return f; }
@@ -180,7 +186,7 @@ __device__ __forceinline__ double f32_to_f64(float f) {
         return __hiloint2double((int)hi, (int)lo);
     }
     if ((b & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
-    return (double)f;  // subnormal, infinity, NaN
+    return f32_to_f64_rare(f);  // subnormal, infinity, NaN
 }
 
 // ------------------------------------------------------------------------------------------

@@ -133,6 +133,15 @@ __global__ void k_newton_step(const double* __restrict__ x, const double* __rest
         xn[i] = x[i] - lam * z[i];
 }
 
+// xn = x - z: the full step (lam = 1, where lam z = z exactly), one FP64 instruction a point
+__global__ void k_newton_full_step(const double* __restrict__ x, const double* __restrict__ z, double* __restrict__ xn,
+                                   size_t N) {
+    pdl_wait();
+    pdl_trigger();
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) xn[i] = x[i] - z[i];
+}
+
 __global__ void k_cheb_step(const double* __restrict__ x, const double* __restrict__ z,
                             const double* __restrict__ u, double* __restrict__ xn, size_t N) {
     pdl_wait();
@@ -194,7 +203,8 @@ void dev_copy(Context& ctx, const double* src, double* dst, size_t N) {
 }
 
 void dev_newton_step(Context& ctx, const double* x, const double* z, double lam, double* xn, size_t N) {
-    launch_pdl(k_newton_step, elementwise_grid(ctx, N), 256, 0, ctx.stream, x, z, lam, xn, N);
+    if (lam == 1.0) launch_pdl(k_newton_full_step, elementwise_grid(ctx, N), 256, 0, ctx.stream, x, z, xn, N);
+    else launch_pdl(k_newton_step, elementwise_grid(ctx, N), 256, 0, ctx.stream, x, z, lam, xn, N);
     ctx.count_launch();
     ctx.check_launch("newton_step");
 }

@@ -273,25 +273,50 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs_df(const float* __restrict_
     });
 }
 
-// x += scale * sum_r coef[r] Z_r with FP32 Z and |coef| <= 1 (the host normalises them by scale):
-// the sum in double-FP32, then one FMA into x (two FP64 instructions a point)
-__global__ void k_combine_add_df(const float* __restrict__ Z, size_t ldz, int cnt, const double* __restrict__ coef,
-                                 double scale, double* x, size_t N) {
+// x += scale * sum_r coef[r] Z_r (ASSIGN: x = scale * sum_r coef[r] Z_r, x not read) with FP32 Z and
+// |coef| <= 1 (the host normalises them by scale): the sum in double-FP32, then one FMA (or multiply)
+// into x — two FP64 instructions a point
+template <int CNT, bool ASSIGN>
+__global__ void k_combine_df(const float* __restrict__ Z, size_t ldz, const double* __restrict__ coef, double scale,
+                             double* x, size_t N) {
     pdl_wait();
     pdl_trigger();
-    extern __shared__ float cf[];  // cnt (hi, lo) pairs
-    for (int r = threadIdx.x; r < cnt; r += blockDim.x) {
-        const DF c = df_split(coef[r]);
-        cf[2 * r] = c.hi;
-        cf[2 * r + 1] = c.lo;
-    }
+    __shared__ DF cs[CNT];
+    if (threadIdx.x < CNT) cs[threadIdx.x] = df_split(coef[threadIdx.x]);
     __syncthreads();
+    DF c[CNT];
+#pragma unroll
+    for (int r = 0; r < CNT; ++r) c[r] = cs[r];
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) {
         DF t{0.0f, 0.0f};
-        for (int r = 0; r < cnt; ++r) df_mac(t, DF{cf[2 * r], cf[2 * r + 1]}, Z[(size_t)r * ldz + i]);
-        x[i] = __fma_rn(scale, df_to_f64(t), x[i]);
+#pragma unroll
+        for (int r = 0; r < CNT; ++r) df_mac(t, c[r], Z[(size_t)r * ldz + i]);
+        x[i] = ASSIGN ? __dmul_rn(scale, df_to_f64(t)) : __fma_rn(scale, df_to_f64(t), x[i]);
     }
+}
+
+template <bool ASSIGN>
+void launch_combine_df(Context& ctx, unsigned grid, int cnt, const float* Z, size_t N, const double* coef, double scale,
+                       double* x) {
+    switch (cnt) {
+#define NUMA_COMBINE_DF_CASE(K)                                                                               \
+    case K:                                                                                                   \
+        launch_pdl(k_combine_df<K, ASSIGN>, grid, 256, 0, ctx.stream, Z, N, coef, scale, x, N);                 \
+        break;
+        NUMA_COMBINE_DF_CASE(1)
+        NUMA_COMBINE_DF_CASE(2)
+        NUMA_COMBINE_DF_CASE(3)
+        NUMA_COMBINE_DF_CASE(4)
+        NUMA_COMBINE_DF_CASE(5)
+        NUMA_COMBINE_DF_CASE(6)
+        NUMA_COMBINE_DF_CASE(7)
+        NUMA_COMBINE_DF_CASE(8)
+#undef NUMA_COMBINE_DF_CASE
+        default:
+            throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "gmres: basis count above the compiled combine kernels");
+    }
+    ctx.count_launch();
 }
 
 // Launches k_cgs_df<cnt, MODE>; false when cnt is above the largest compiled count.
@@ -423,7 +448,13 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
         res.rel_res = 1.0;
         return res;
     }
-    if (o.zero_guess) dev_fill(ctx_, x, 0.0, N);
+    // a zero first guess is written by the first solution update itself (x = Z y, x not read); any
+    // earlier exit or use of x fills it first
+    bool x_zero_pending = o.zero_guess;
+    auto settle_x = [&] {
+        if (x_zero_pending) dev_fill(ctx_, x, 0.0, N);
+        x_zero_pending = false;
+    };
     // FP32 preconditioner output into an FP32 product: the preconditioned vectors are kept in FP32
     // (exactly the values the FP64 path would widen), halving their writes and reads
     const bool z32 = M && M->has_apply32() && A.has_apply32();
@@ -465,6 +496,7 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
             first = false;
             beta = bnorm;
         } else {
+            settle_x();
             A.apply(x, w_.p);
             ++res.matvecs;
             launch_pdl(k_sub, eg, 256, 0, ctx_.stream, b, w_.p, r_.p, N);
@@ -476,6 +508,7 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
         res.rel_res = beta / bnorm;
         if (res.rel_res <= o.rtol) {
             res.converged = true;
+            settle_x();
             break;
         }
         if (v32) {
@@ -535,6 +568,7 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
             const double den = std::hypot(H[j][j], H[j + 1][j]);
             if (!(den > 0.0) || !std::isfinite(den)) {
                 res.breakdown = true;
+                settle_x();
                 return res;
             }
             cs[j] = H[j][j] / den;
@@ -553,6 +587,7 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
             const double piv = H[ii][ii];
             if (!(std::abs(piv) > 0.0) || !std::isfinite(piv)) {
                 res.breakdown = true;
+                settle_x();
                 return res;
             }
             double t = g[ii];
@@ -568,18 +603,23 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
                 for (size_t jj = 0; jj < k; ++jj) yh[jj] /= scale;
         }
         NUMA_CUDA(cudaMemcpyAsync(ydev, yh, k * sizeof(double), cudaMemcpyHostToDevice, ctx_.stream));
-        if (v32)
-            launch_pdl(k_combine_add_df, eg, 256, 2 * k * sizeof(float), ctx_.stream, Z32_.p, N, (int)k, ydev, scale,
-                       x, N);
-        else if (z32) launch_pdl(k_combine_add<float>, eg, 256, k * sizeof(double), ctx_.stream, Z32_.p, N, (int)k, ydev, x, N);
-        else launch_pdl(k_combine_add<double>, eg, 256, k * sizeof(double), ctx_.stream, Z_.p, N, (int)k, ydev, x, N);
-        ctx_.count_launch();
+        if (v32) {
+            if (x_zero_pending) launch_combine_df<true>(ctx_, eg, (int)k, Z32_.p, N, ydev, scale, x);
+            else launch_combine_df<false>(ctx_, eg, (int)k, Z32_.p, N, ydev, scale, x);
+            x_zero_pending = false;
+        } else {
+            settle_x();
+            if (z32) launch_pdl(k_combine_add<float>, eg, 256, k * sizeof(double), ctx_.stream, Z32_.p, N, (int)k, ydev, x, N);
+            else launch_pdl(k_combine_add<double>, eg, 256, k * sizeof(double), ctx_.stream, Z_.p, N, (int)k, ydev, x, N);
+            ctx_.count_launch();
+        }
         ctx_.check_launch("gmres update (lazy)");
         if (res.rel_res <= o.rtol) {
             res.converged = true;
             break;
         }
     }
+    settle_x();
     return res;
 }
 
