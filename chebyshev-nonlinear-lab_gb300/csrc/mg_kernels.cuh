@@ -414,7 +414,8 @@ __global__ void __launch_bounds__(BX* BY) k_residual_split(const float* __restri
 // Restriction from a natural-layout fine residual into a split coarse level (odd nc): the
 // 27-point sum of k_restrict in the same order, b and b h^2 stored split.  FIRST_X: also the
 // coarse level's first smoothing pass (colour 0 from x = 0: x = bs / 6), which the cycle then
-// skips.
+// skips.  Split levels come in pairs nf = 2 nc + 1, so all 27 fine points exist: no bounds tests,
+// and the 27 loads are issued ahead of the FMA chain.
 template <bool FIRST_X>
 __global__ void __launch_bounds__(BX* BY) k_restrict_split(const float* __restrict__ rf, float* __restrict__ bc,
                                                            float* __restrict__ bsc, float* __restrict__ xc, int nf,
@@ -426,24 +427,24 @@ __global__ void __launch_bounds__(BX* BY) k_restrict_split(const float* __restri
     const int I = blockIdx.z;
     if (K >= nc || J >= nc) return;
     const float w[3] = {0.25f, 0.5f, 0.25f};
-    float acc = 0.0f;
+    float v[27];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const int fi = 2 * I + a;
-        if (fi >= nf) continue;
+    for (int a = 0; a < 3; ++a)
 #pragma unroll
         for (int bb = 0; bb < 3; ++bb) {
-            const int fj = 2 * J + bb;
-            if (fj >= nf) continue;
-            const float wab = w[a] * w[bb];
-            const float* row = rf + (fi * nf + fj) * nf + 2 * K;
+            const float* row = rf + ((2 * I + a) * nf + 2 * J + bb) * nf + 2 * K;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                if (2 * K + c >= nf) continue;
-                acc = __fmaf_rn(wab * w[c], row[c], acc);
-            }
+            for (int c = 0; c < 3; ++c) v[(a * 3 + bb) * 3 + c] = row[c];
         }
-    }
+    float acc = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb) {
+            const float wab = w[a] * w[bb];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) acc = __fmaf_rn(wab * w[c], v[(a * 3 + bb) * 3 + c], acc);
+        }
     const int Lc = (I * nc + J) * nc + K;
     const int q = split_at(Lc, halfc);
     const float bsv = acc * inv_c;

@@ -286,7 +286,6 @@ void PoissonMG::cycle32(size_t l) {
     const float* bs = L.bs32.p;
     const dim3 blk(BX, BY);
     const Split g = make_split(n);
-    const int ich = n >= 64 ? 4 : 1;
     const dim3 cgrid(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n);
     const bool fused_first = first_fused32(l);
     // pass(colour, first, last): last = the final pass of the cycle on the finest level
@@ -330,15 +329,15 @@ void PoissonMG::cycle32(size_t l) {
     for (int sw = 0; sw < pre_; ++sw) sweep(0, sw == 0, false);
     if (pre_ == 0) NUMA_CUDA(cudaMemsetAsync(x, 0, Nl * sizeof(float), s));
     float* r = reinterpret_cast<float*>(scratch_r_.p);
-    {
-        const dim3 rgd(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, (n + ich - 1) / ich);
-        if (ich == 4) launch_pdl(k_residual_split<4>, rgd, blk, 0, s, x, b, r, g, (float)L.h2inv);
-        else launch_pdl(k_residual_split<1>, rgd, blk, 0, s, x, b, r, g, (float)L.h2inv);
-        ctx_.count_launch();
-    }
     Level& C = *levels_[l + 1];
     const int nc = C.n;
     const bool csplit = (nc & 1) != 0;
+    {
+        // one plane a thread: 31 registers and full occupancy (a four-plane march took 80)
+        const dim3 rgd(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n);
+        launch_pdl(k_residual_split<1>, rgd, blk, 0, s, x, b, r, g, (float)L.h2inv);
+        ctx_.count_launch();
+    }
     const Split gc = make_split(nc);
     const dim3 rg((nc + BX - 1) / BX, (nc + BY - 1) / BY, nc);
     if (csplit && first_fused32(l + 1))
