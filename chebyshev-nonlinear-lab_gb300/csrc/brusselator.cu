@@ -251,9 +251,11 @@ dim3 b2_grid(int n) {
 }
 
 // The same product from an FP32 d (the multigrid's output): no conversion, so no shared-memory
-// tile — neighbours come through L1; the arithmetic is k_b2_jvp32's, operation for operation.
+// tile — neighbours come through L1; the arithmetic is k_b2_jvp32's, operation for operation.  OT =
+// float stores the FP32 result as it is, OT = double widens it.
+template <class OT>
 __global__ void __launch_bounds__(256) k_b2_jvp32f(const float2* __restrict__ coef, const float* __restrict__ d,
-                                                   double* __restrict__ out, B2Geom32 G) {
+                                                   OT* __restrict__ out, B2Geom32 G) {
     pdl_wait();
     pdl_trigger();
     const int n = G.n;
@@ -270,8 +272,15 @@ __global__ void __launch_bounds__(256) k_b2_jvp32f(const float2* __restrict__ co
         const float lv = ((e[r + jm] - dv) + (e[r + jp] - dv)) + ((e[(size_t)im * n + j] - dv) + (e[(size_t)ip * n + j] - dv));
         const float2 c = coef[p];
         const float a11 = G.c1 - c.x, a21 = c.x - G.B, a22 = G.invdt + c.y;
-        out[p] = f32_to_f64(__fmaf_rn(-c.y, dv, __fmaf_rn(-G.duh, lu, a11 * du)));
-        out[nn + p] = f32_to_f64(__fmaf_rn(a22, dv, __fmaf_rn(a21, du, -G.dvh * lv)));
+        const float ru = __fmaf_rn(-c.y, dv, __fmaf_rn(-G.duh, lu, a11 * du));
+        const float rv = __fmaf_rn(a22, dv, __fmaf_rn(a21, du, -G.dvh * lv));
+        if constexpr (sizeof(OT) == 4) {
+            out[p] = ru;
+            out[nn + p] = rv;
+        } else {
+            out[p] = f32_to_f64(ru);
+            out[nn + p] = f32_to_f64(rv);
+        }
     }
 }
 
@@ -350,6 +359,12 @@ struct LvlArgs {
 template <class T> __device__ __forceinline__ T from_f64(double x);
 template <> __device__ __forceinline__ float from_f64<float>(double x) { return f64_to_f32(x); }
 template <> __device__ __forceinline__ double from_f64<double>(double x) { return x; }
+// a right-hand side read as FP64 or as FP32 into the level type
+template <class T> __device__ __forceinline__ T from_in(double x) { return from_f64<T>(x); }
+template <class T> __device__ __forceinline__ T from_in(float x) {
+    if constexpr (sizeof(T) == 4) return x;
+    else return f32_to_f64(x);
+}
 __device__ __forceinline__ double to_f64(float x) { return f32_to_f64(x); }
 __device__ __forceinline__ double to_f64(double x) { return x; }
 
@@ -382,9 +397,9 @@ enum { kBPassNormal = 0, kBPassFirst = 1, kBPassLast = 2 };
 //    on the finest level the right-hand side is read from r (FP64 planes) and stored as b.
 //  Last (finest level, colour 0, the cycle's final pass): also writes z (FP64 planes) for both points,
 //    or, for an FP32 consumer, the same values as FP32 planes z32.
-template <class T, int MODE>
+template <class T, int MODE, class RT = double>
 __global__ void __launch_bounds__(256) k_bmg_pass(T* __restrict__ X, T* __restrict__ Bv, const T* __restrict__ K,
-                                                  LvlArgs<T> L, int colour, const double* __restrict__ r64,
+                                                  LvlArgs<T> L, int colour, const RT* __restrict__ r64,
                                                   double* __restrict__ z64, float* __restrict__ z32 = nullptr) {
     pdl_wait();
     pdl_trigger();
@@ -400,10 +415,10 @@ __global__ void __launch_bounds__(256) k_bmg_pass(T* __restrict__ X, T* __restri
     const size_t nn = (size_t)n * n;
     T bu, bv;
     if (MODE == kBPassFirst && r64) {
-        bu = from_f64<T>(r64[pn]);
-        bv = from_f64<T>(r64[nn + pn]);
+        bu = from_in<T>(r64[pn]);
+        bv = from_in<T>(r64[nn + pn]);
         st2(Bv, p, bu, bv);
-        st2(Bv, po, from_f64<T>(r64[pon]), from_f64<T>(r64[nn + pon]));
+        st2(Bv, po, from_in<T>(r64[pon]), from_in<T>(r64[nn + pon]));
     } else {
         const auto b = ld2(Bv, p);
         bu = b.x;
@@ -775,15 +790,15 @@ __global__ void __launch_bounds__(256) k_bmg_krestrict(const T* __restrict__ Kf,
 }
 
 // FP64 planes <-> interleaved level pairs (used only when the finest level is also the coarsest).
-template <class T>
-__global__ void k_bmg_in(const double* __restrict__ r, int n, T* __restrict__ B) {
+template <class T, class RT = double>
+__global__ void k_bmg_in(const RT* __restrict__ r, int n, T* __restrict__ B) {
     pdl_wait();
     pdl_trigger();
     const size_t nn = (size_t)n * n;
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nn) return;
     const int i = (int)(p / n), j = (int)(p - (size_t)i * n);
-    st2(B, pidx(n, i, j), from_f64<T>(r[p]), from_f64<T>(r[nn + p]));
+    st2(B, pidx(n, i, j), from_in<T>(r[p]), from_in<T>(r[nn + p]));
 }
 template <class T>
 __global__ void k_bmg_out(const T* __restrict__ X, int n, double* __restrict__ z) {
@@ -955,10 +970,21 @@ void Brusselator2D::jvp_bound32(const float* v32, double* out) {
         throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Brusselator2D: no FP32 product bound");
     const B2Geom G = b2_geom(n_, P_);
     const B2Geom32 G32{(int)n_, (float)G.invdt, (float)G.B, (float)G.c1, (float)G.duh, (float)G.dvh};
-    launch_pdl(k_b2_jvp32f, b2_grid((int)n_), dim3(32, 8), 0, ctx_.stream, reinterpret_cast<const float2*>(coef32_.p),
-               v32, out, G32);
+    launch_pdl(k_b2_jvp32f<double>, b2_grid((int)n_), dim3(32, 8), 0, ctx_.stream,
+               reinterpret_cast<const float2*>(coef32_.p), v32, out, G32);
     ctx_.count_launch();
     ctx_.check_launch("Brusselator2D jvp32 (fp32 input)");
+}
+
+void Brusselator2D::jvp_bound32f(const float* v32, float* out32) {
+    if (bound_precision_ != NUMA_GPU_FP32)
+        throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Brusselator2D: no FP32 product bound");
+    const B2Geom G = b2_geom(n_, P_);
+    const B2Geom32 G32{(int)n_, (float)G.invdt, (float)G.B, (float)G.c1, (float)G.duh, (float)G.dvh};
+    launch_pdl(k_b2_jvp32f<float>, b2_grid((int)n_), dim3(32, 8), 0, ctx_.stream,
+               reinterpret_cast<const float2*>(coef32_.p), v32, out32, G32);
+    ctx_.count_launch();
+    ctx_.check_launch("Brusselator2D jvp32 (fp32 input and output)");
 }
 
 void Brusselator2D::jvp_at(const double* x, const double* v, double* out) {
@@ -1091,7 +1117,8 @@ void BrussMG2D::cycle(size_t l) {
     }
     if (coarsest) {
         if (finest) {
-            launch_pdl(k_bmg_in<T>, (unsigned)((nn + 255) / 256), 256, 0, s, r0_, n, Bv);
+            if (r32_) launch_pdl(k_bmg_in<T, float>, (unsigned)((nn + 255) / 256), 256, 0, s, r32_, n, Bv);
+            else launch_pdl(k_bmg_in<T>, (unsigned)((nn + 255) / 256), 256, 0, s, r0_, n, Bv);
             ctx_.count_launch();
         }
         if (nn <= (size_t)kBmgOneBlockPoints) {
@@ -1114,7 +1141,11 @@ void BrussMG2D::cycle(size_t l) {
         return;
     }
     // pre-smoothing: colours 0, 1; the first pass starts from x = 0
-    launch_pdl(k_bmg_pass<T, kBPassFirst>, pgrid, blk, 0, s, X, Bv, K, A, 0, finest ? r0_ : nullptr, nullptr, nullptr);
+    if (finest && r32_)
+        launch_pdl(k_bmg_pass<T, kBPassFirst, float>, pgrid, blk, 0, s, X, Bv, K, A, 0, r32_, nullptr, nullptr);
+    else
+        launch_pdl(k_bmg_pass<T, kBPassFirst>, pgrid, blk, 0, s, X, Bv, K, A, 0, finest ? r0_ : nullptr, nullptr,
+                   nullptr);
     launch_pdl(k_bmg_pass<T, kBPassNormal>, pgrid, blk, 0, s, X, Bv, K, A, 1, nullptr, nullptr, nullptr);
     ctx_.count_launch(2);
     for (int k = 1; k < pre_; ++k) {
@@ -1220,6 +1251,24 @@ void BrussMG2D::apply32(const double* r, float* z32) {
     z32_ = nullptr;
 }
 
+void BrussMG2D::apply32f(const float* r32, float* z32) {
+    if (!supports_out32()) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "BrussMG2D: no FP32 output for this hierarchy");
+    r0_ = nullptr;
+    r32_ = r32;
+    z0_ = nullptr;
+    z32_ = z32;
+    try {
+        cycle<float>(0);
+    } catch (...) {
+        r32_ = nullptr;
+        z32_ = nullptr;
+        throw;
+    }
+    r32_ = nullptr;
+    z32_ = nullptr;
+    ctx_.check_launch("BrussMG2D apply32f");
+}
+
 void BrussMG2D::apply(const double* r, double* z) {
     const size_t N = size();
     // the finest pass reads r while the last one writes z: an aliased call goes through a copy
@@ -1247,6 +1296,8 @@ public:
     // the FP32 cycle can hand its result over unwidened
     bool has_apply32() const override { return mg_.supports_out32(); }
     void apply32(const double* r, float* z32) override { mg_.apply32(r, z32); }
+    bool has_apply32f() const override { return mg_.supports_out32(); }
+    void apply32f(const float* r32, float* z32) override { mg_.apply32f(r32, z32); }
     int kind() const override { return NUMA_GPU_PRECOND_BRUSS_MG; }
 
 private:

@@ -226,6 +226,8 @@ public:
     void jvp_bound(const double* v, double* out) override;
     bool has_jvp32() const override { return bound_precision_ == NUMA_GPU_FP32; }
     void jvp_bound32(const float* v32, double* out) override;
+    bool has_jvp32f() const override { return bound_precision_ == NUMA_GPU_FP32; }
+    void jvp_bound32f(const float* v32, float* out32) override;
     void jvp_at(const double* x, const double* v, double* out) override;
     void d2(const double* x, const double* cache, const double* v, double* out) override;
 
@@ -254,6 +256,8 @@ public:
     // z32 = V-cycle(r) in FP32 only, for an FP32 hierarchy with more than one level.
     bool supports_out32() const { return precision_ == NUMA_GPU_FP32 && levels_.size() > 1; }
     void apply32(const double* r, float* z32);
+    // The same from an FP32 right-hand side (an FP32 Krylov basis vector), read as it is.
+    void apply32f(const float* r32, float* z32);
     // ms of one finest-level colour pass (CUDA events, reps back-to-back launches)
     double time_finest_pass(int reps);
     struct Level;
@@ -268,6 +272,7 @@ private:
     std::vector<std::unique_ptr<Level>> levels_;
     DeviceArray<double> alias_;
     const double* r0_ = nullptr;
+    const float* r32_ = nullptr;  // FP32 right-hand side of the current apply32f
     double* z0_ = nullptr;
     float* z32_ = nullptr;
     cudaGraphExec_t coarse_exec_ = nullptr;
