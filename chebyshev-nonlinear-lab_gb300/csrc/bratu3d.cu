@@ -61,10 +61,12 @@ __device__ __forceinline__ double lap_sum(const double* __restrict__ v, size_t p
 
 // F = h^-2 (6u - sum) - lambda e^u; optionally c = lambda e^u and ||F||.  The last step is one FMA
 // (F differs from the reference's two roundings by at most half an ulp, as e^u already may).
-// C32: also c32 = RN32(c) (the mixed path's FP32 Jacobian coefficient, integer conversion).
+// C32: also c32 = RN32(c) (the mixed path's FP32 Jacobian coefficient) and f32 = RN32(F) (the
+// first FP32 Krylov vector of the next linear solve), integer conversions.
 template <bool WRITE_C, bool NORM, bool C32>
 __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, double* __restrict__ F,
-                                                 double* __restrict__ c_out, float* __restrict__ c32_out, int n,
+                                                 double* __restrict__ c_out, float* __restrict__ c32_out,
+                                                 float* __restrict__ f32_out, int n,
                                                  int ichunk, double lam, double h2inv, RedArgs red, double* norm_out) {
     pdl_wait();
     pdl_trigger();
@@ -85,7 +87,10 @@ __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, d
             const double f = __fma_rn(h2inv, s, -e);  // h^-2 s - e with one rounding
             F[p] = f;
             if (WRITE_C) c_out[p] = e;
-            if (C32) c32_out[p] = f64_to_f32(e);
+            if (C32) {
+                c32_out[p] = f64_to_f32(e);
+                f32_out[p] = f64_to_f32(f);
+            }
             if (NORM) acc[0] = __fma_rn(f, f, acc[0]);
             below = cur;
             cur = above;
@@ -339,19 +344,20 @@ void Bratu3D::eval(const double* x, double* out, double* c_out, double* norm_out
     March m = march_shape(n, norm);
     dim3 blk(BX, BY);
     float* c32 = (c_out && mixed_cache_) ? reinterpret_cast<float*>(c_out + N_) : nullptr;
+    float* f32 = c32 ? reinterpret_cast<float*>(c_out + N_ + (N_ + 1) / 2) : nullptr;
     const double lam = lambda_, h2 = h2inv_;
     if (c32 && norm)
-        launch_pdl(k_eval<true, true, true>, m.grid, blk, 0, ctx_.stream, x, out, c_out, c32, n, m.ichunk, lam, h2, ctx_.red, norm_out);
+        launch_pdl(k_eval<true, true, true>, m.grid, blk, 0, ctx_.stream, x, out, c_out, c32, f32, n, m.ichunk, lam, h2, ctx_.red, norm_out);
     else if (c32)
-        launch_pdl(k_eval<true, false, true>, m.grid, blk, 0, ctx_.stream, x, out, c_out, c32, n, m.ichunk, lam, h2, ctx_.red, nullptr);
+        launch_pdl(k_eval<true, false, true>, m.grid, blk, 0, ctx_.stream, x, out, c_out, c32, f32, n, m.ichunk, lam, h2, ctx_.red, nullptr);
     else if (c_out && norm)
-        launch_pdl(k_eval<true, true, false>, m.grid, blk, 0, ctx_.stream, x, out, c_out, nullptr, n, m.ichunk, lam, h2, ctx_.red, norm_out);
+        launch_pdl(k_eval<true, true, false>, m.grid, blk, 0, ctx_.stream, x, out, c_out, nullptr, nullptr, n, m.ichunk, lam, h2, ctx_.red, norm_out);
     else if (c_out)
-        launch_pdl(k_eval<true, false, false>, m.grid, blk, 0, ctx_.stream, x, out, c_out, nullptr, n, m.ichunk, lam, h2, ctx_.red, nullptr);
+        launch_pdl(k_eval<true, false, false>, m.grid, blk, 0, ctx_.stream, x, out, c_out, nullptr, nullptr, n, m.ichunk, lam, h2, ctx_.red, nullptr);
     else if (norm)
-        launch_pdl(k_eval<false, true, false>, m.grid, blk, 0, ctx_.stream, x, out, nullptr, nullptr, n, m.ichunk, lam, h2, ctx_.red, norm_out);
+        launch_pdl(k_eval<false, true, false>, m.grid, blk, 0, ctx_.stream, x, out, nullptr, nullptr, nullptr, n, m.ichunk, lam, h2, ctx_.red, norm_out);
     else
-        launch_pdl(k_eval<false, false, false>, m.grid, blk, 0, ctx_.stream, x, out, nullptr, nullptr, n, m.ichunk, lam, h2, ctx_.red, nullptr);
+        launch_pdl(k_eval<false, false, false>, m.grid, blk, 0, ctx_.stream, x, out, nullptr, nullptr, nullptr, n, m.ichunk, lam, h2, ctx_.red, nullptr);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d eval");
 }

@@ -261,6 +261,10 @@ struct SolveState {
         cn = nc ? cb.p : nullptr;
     }
     // F(xn) with its coefficient and norm; returns ||F(xn)||.
+    // RN32(F(x)) where the operator keeps it beside its FP32 Jacobian data (the FP32 hand-off)
+    const float* f32() const {
+        return p.jvp_precision == NUMA_GPU_FP32 && p.jvp_mode == NUMA_GPU_DERIV_ANALYTIC ? f.f32_of_cache(cx) : nullptr;
+    }
     double eval_trial() {
         {
             Timers::Scope s(&timers, kT_F);
@@ -291,9 +295,10 @@ struct SolveState {
     }
 };
 
-GmresOptions gmres_opts(const KrylovParams& p, double rtol, double bnorm = -1.0) {
+GmresOptions gmres_opts(const KrylovParams& p, double rtol, double bnorm = -1.0, const float* b32 = nullptr) {
     GmresOptions o;
     o.bnorm = bnorm;
+    o.b32 = b32;
     o.rtol = rtol;
     o.restart = p.restart;
     o.max_iters = p.max_iters;
@@ -382,7 +387,7 @@ void newton_krylov(NonlinearOp& f, double* x0, const KrylovParams& p, Provider* 
         }
         const double eta = forcing(p, k, rnorm, rprev, eta_prev, out.res0);
         S.bind(J, pc);
-        const GmresResult g = S.gmres.solve(J, Mp, S.Fx, S.z.p, gmres_opts(p, eta, rnorm));
+        const GmresResult g = S.gmres.solve(J, Mp, S.Fx, S.z.p, gmres_opts(p, eta, rnorm, S.f32()));
         add_lin(out, g);
         if (g.breakdown) break;
         double lam = 1.0;
@@ -442,7 +447,7 @@ void chebyshev_inexact(NonlinearOp& f, double* x0, const KrylovParams& p, Provid
         S.bind(J, pc);
         space.clear();
         const GmresResult g1 =
-            S.gmres.solve(J, Mp, S.Fx, S.z.p, gmres_opts(p, eta1, rnorm), p.recycle ? &space : nullptr);
+            S.gmres.solve(J, Mp, S.Fx, S.z.p, gmres_opts(p, eta1, rnorm, S.f32()), p.recycle ? &space : nullptr);
         add_lin(out, g1);
         if (g1.breakdown) break;
         {
@@ -526,7 +531,7 @@ void tf_chebyshev_2018(NonlinearOp& f, double* x0, const KrylovParams& p, Provid
         const double eta1 = std::clamp(std::min(1e-8, rnorm * rnorm), 2.0 * eps, 1e-8);
         const double eta2 = std::clamp(std::min(1e-8, rnorm), 2.0 * eps, 1e-8);
         S.bind(J, pc);
-        const GmresResult g1 = S.gmres.solve(J, Mp, S.Fx, S.z.p, gmres_opts(p, eta1, rnorm));
+        const GmresResult g1 = S.gmres.solve(J, Mp, S.Fx, S.z.p, gmres_opts(p, eta1, rnorm, S.f32()));
         add_lin(out, g1);
         if (!g1.converged) break;
         if (g1.breakdown) break;

@@ -222,8 +222,9 @@ __global__ void k_to32_scaled(const double* __restrict__ src, double s, float* _
 //         then hout[0] = ||u_out||, sig2[j+1] = 1/||u_out||^2, sig[j+1] = 1/||u_out||.
 // Sums per thread in double-FP32, converted to FP64 for the block and grid reduction.
 template <int CNT, int MODE>
-__global__ void __launch_bounds__(kRedThreads) k_cgs_df(const float* __restrict__ w, const float* __restrict__ U,
-                                                        size_t ldu, const double* __restrict__ hin, double* sig2,
+__global__ void __launch_bounds__(kRedThreads) k_cgs_df(const float* __restrict__ w, const float* __restrict__ u0,
+                                                        const float* __restrict__ U, size_t ldu,
+                                                        const double* __restrict__ hin, double* sig2,
                                                         double* sig, int j, size_t N, RedArgs red,
                                                         double* __restrict__ hout, float* __restrict__ uout) {
     pdl_wait();
@@ -247,13 +248,13 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs_df(const float* __restrict_
             DF t{0.0f, 0.0f};
             df_mac(t, cw, wi);
 #pragma unroll
-            for (int r = 0; r < CNT; ++r) df_mac(t, c[r], U[(size_t)r * ldu + i]);
+            for (int r = 0; r < CNT; ++r) df_mac(t, c[r], r == 0 ? u0[i] : U[(size_t)r * ldu + i]);
             const float u = __fadd_rn(t.hi, t.lo);
             uout[i] = u;
             df_mac(acc[0], u, u);
         } else {
 #pragma unroll
-            for (int r = 0; r < CNT; ++r) df_mac(acc[r], wi, U[(size_t)r * ldu + i]);
+            for (int r = 0; r < CNT; ++r) df_mac(acc[r], wi, r == 0 ? u0[i] : U[(size_t)r * ldu + i]);
         }
     }
     double s[R];
@@ -321,13 +322,13 @@ void launch_combine_df(Context& ctx, unsigned grid, int cnt, const float* Z, siz
 
 // Launches k_cgs_df<cnt, MODE>; false when cnt is above the largest compiled count.
 template <int MODE>
-bool launch_cgs_df(Context& ctx, int cnt, const float* w, const float* U, size_t N, const double* hin, double* sig2,
-                   double* sig, int j, double* hout, float* uout) {
+bool launch_cgs_df(Context& ctx, int cnt, const float* w, const float* u0, const float* U, size_t N, const double* hin,
+                   double* sig2, double* sig, int j, double* hout, float* uout) {
     const unsigned g = ctx.red_grid(N);
     switch (cnt) {
 #define NUMA_CGS_DF_CASE(K)                                                                                  \
     case K:                                                                                                  \
-        launch_pdl(k_cgs_df<K, MODE>, g, kRedThreads, 0, ctx.stream, w, U, N, hin, sig2, sig, j, N, ctx.red, hout, \
+        launch_pdl(k_cgs_df<K, MODE>, g, kRedThreads, 0, ctx.stream, w, u0, U, N, hin, sig2, sig, j, N, ctx.red, hout, \
                    uout);                                                                                    \
         break;
         NUMA_CGS_DF_CASE(1)
@@ -484,6 +485,7 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
     const unsigned eg = ew_grid(ctx_, N);
     while (res.iters < o.max_iters) {
         const double* v0;
+        const float* v0_32 = nullptr;  // RN32(v0) from the caller, used as it is
         double beta;
         if (given) {
             v0 = r_init;
@@ -495,6 +497,9 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
             v0 = b;
             first = false;
             beta = bnorm;
+            // elements of order beta / sqrt(N): far from FP32's range limits for the double-FP32 products
+            const double typ = beta / std::sqrt((double)N);
+            if (o.b32 && typ > 1e-15 && typ < 1e15) v0_32 = o.b32;
         } else {
             settle_x();
             A.apply(x, w_.p);
@@ -511,7 +516,13 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
             settle_x();
             break;
         }
-        if (v32) {
+        if (v32 && v0_32) {
+            // u_0 = RN32(b) as the caller stored it, sigma_0 = 1/||b||: no conversion pass
+            launch_pdl(k_set_scalar, 1, 1, 0, ctx_.stream, sig2, 1.0 / (beta * beta));
+            launch_pdl(k_set_scalar, 1, 1, 0, ctx_.stream, sigd, 1.0 / beta);
+            ctx_.count_launch(2);
+            sig[0] = 1.0 / beta;
+        } else if (v32) {
             launch_pdl(k_to32_scaled, eg, 256, 0, ctx_.stream, v0, 1.0 / beta, V32_.p, N);
             launch_pdl(k_set_scalar, 1, 1, 0, ctx_.stream, sig2, 1.0);
             launch_pdl(k_set_scalar, 1, 1, 0, ctx_.stream, sigd, 1.0);
@@ -524,13 +535,14 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
         }
         std::fill(g.begin(), g.end(), 0.0);
         g[0] = beta;
+        const float* u0 = v0_32 ? v0_32 : V32_.p;  // the FP32 basis' first vector
         size_t k = 0;
         while (k < m && res.iters < o.max_iters) {
             const size_t j = k;
             const double* vj = v32 ? nullptr : (j == 0 ? v0 : V_.p + j * N);
             if (v32) {
                 float* zj = Z32_.p + j * N;
-                M->apply32f(V32_.p + j * N, zj);
+                M->apply32f(j == 0 ? u0 : V32_.p + j * N, zj);
                 ++res.precs;
                 A.apply32f(zj, W32_.p);
             } else if (z32) {
@@ -547,8 +559,8 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
             ++res.matvecs;
             const int cnt = (int)(j + 1);
             if (v32) {
-                launch_cgs_df<0>(ctx_, cnt, W32_.p, V32_.p, N, nullptr, sig2, sigd, (int)j, sl, nullptr);
-                launch_cgs_df<2>(ctx_, cnt, W32_.p, V32_.p, N, sl, sig2, sigd, (int)j, sl + j + 1,
+                launch_cgs_df<0>(ctx_, cnt, W32_.p, u0, V32_.p, N, nullptr, sig2, sigd, (int)j, sl, nullptr);
+                launch_cgs_df<2>(ctx_, cnt, W32_.p, u0, V32_.p, N, sl, sig2, sigd, (int)j, sl + j + 1,
                                  V32_.p + (j + 1) * N);
             } else {
                 launch_cgs<0>(ctx_, cnt, w_.p, v0, V_.p, N, nullptr, nullptr, sl, nullptr, nullptr);

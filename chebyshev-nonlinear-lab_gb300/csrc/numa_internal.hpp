@@ -46,6 +46,11 @@ public:
     // Announces the precision the Jacobian products of the coming solve will use, before any
     // evaluation (an operator may then keep what that precision needs in the cache).
     virtual void prepare_cache(int precision) { (void)precision; }
+    // RN32(F) written by the evaluation that filled cache, where the operator keeps it (else null)
+    virtual const float* f32_of_cache(const double* cache) const {
+        (void)cache;
+        return nullptr;
+    }
     // out = F(x); cache := the Jacobian data at x (when cache_size() > 0); norm_out := ||F(x)||
     // as a device scalar (optional).
     virtual void eval(const double* x, double* out, double* cache, double* norm_out) = 0;
@@ -107,7 +112,11 @@ public:
 
     // NonlinearOp: the cache of an iterate x is c = lambda e^x; for FP32 products it also holds
     // RN32(c) (N floats after the N doubles), written by the evaluation itself.
-    size_t cache_size() const override { return mixed_cache_ ? N_ + (N_ + 1) / 2 : N_; }
+    // mixed cache: c (FP64), then RN32(c) and RN32(F) (N floats each)
+    size_t cache_size() const override { return mixed_cache_ ? N_ + 2 * ((N_ + 1) / 2) : N_; }
+    const float* f32_of_cache(const double* cache) const override {
+        return mixed_cache_ && cache ? reinterpret_cast<const float*>(cache + N_ + (N_ + 1) / 2) : nullptr;
+    }
     void prepare_cache(int precision) override { mixed_cache_ = precision == NUMA_GPU_FP32; }
     void eval(const double* x, double* out, double* cache, double* norm_out) override;
     void bind(const double* x, const double* cache, int precision) override;
@@ -464,6 +473,7 @@ struct GmresOptions {
     int orth = NUMA_GPU_ORTH_MGS;
     bool flexible = false;
     double bnorm = -1.0;  // ||b|| when the caller knows it (>= 0), used by the flexible CGS1 solver
+    const float* b32 = nullptr;  // RN32(b) when the caller has it (the FP32 Arnoldi basis starts from it)
 };
 
 class Gmres {
