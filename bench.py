@@ -8,13 +8,14 @@ with every vector resident in HBM.  Inputs are synthetic and deterministic (u0 =
 
     python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--path fp64|mixed]
 
-Printed JSON line: value = seconds per solve of the headline path (plain FP64 drop-in by
-default), e2e = the same through numa_gpu_solve_bratu3d_host with pinned host buffers (host to
-device copy of u0 and device to host copy of the solution inside the timed region), "mixed" =
-the FP32-V-cycle / FP32-Jacobian / FGMRES variant timed in the same run with its error against
-the FP64 solution, roofline = the V-cycle's dominant kernel (red-black Gauss-Seidel colour
-pass), cpu_baseline = the oracle port (the reference's algorithm restated in C++ with the
-reference's OpenMP layout) on the host cores.
+Printed JSON line: value = seconds per solve of the headline path (the mixed path by default:
+FP32 V-cycle and FP32 Jacobian products inside FGMRES, FP64 residual and outer iteration; --path
+fp64 makes the plain FP64 drop-in the headline), e2e = the same through
+numa_gpu_solve_bratu3d_host with pinned host buffers (host to device copy of u0 and device to
+host copy of the solution inside the timed region), mixed_vs_plain = the other path timed in the
+same run with the error between the two solutions, roofline = the V-cycle's dominant kernel (the
+finest colour pass), cpu_baseline = the oracle port (the reference's algorithm restated in C++
+with the reference's OpenMP layout) on the host cores.
 
 --impl reference times the reference's CPU implementation of the same solve (the oracle port:
 the reference's own build cannot travel to the GPU host) on all host cores; each step is a
@@ -119,7 +120,7 @@ class Dist:
 
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
-    """nvidia-smi clock / throttle samples every 200 ms while the timed region runs."""
+    """nvidia-smi clock / throttle samples every 50 ms while the timed region runs."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -135,9 +136,14 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # nvidia-smi's start-up (driver and NVML initialisation) happens before the timed region:
+            # wait for its first sample (at most 5 s)
+            t0 = time.time()
+            while not self.lines and self.proc.poll() is None and time.time() - t0 < 5.0:
+                time.sleep(0.01)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
