@@ -172,6 +172,24 @@ def test_mixed_path_with_cgs1(gpu):
     assert rel_err(xm.numpy(), x64.numpy()) < 1e-8
 
 
+def test_mixed_fp32_basis_against_fp64_basis(gpu):
+    """The mixed path keeps its Arnoldi basis in FP32 (double-FP32 inner products and updates) when
+    the forcing term is >= 1e-5, and in FP64 below; capping the forcing terms at 1e-6 runs the FP64
+    basis throughout.  Both converge to the same tolerance, their solutions within 1e-8."""
+    G = _G()
+    n, lam = 63, 6.0
+    op = G.Bratu3D(gpu, n, lam)
+    base = dict(rtol_nl=1e-10, gmres_restart=30, flexible=1, jvp_precision=G.FP32, orth=G.CGS1)
+    xa, xb = gpu.vec(n ** 3), gpu.vec(n ** 3)
+    ra = G.newton_krylov(op, xa, G.default_params(**base), G.Provider.poisson_mg(gpu, n, precision=G.FP32))
+    rb = G.newton_krylov(op, xb, G.default_params(eta_init=1e-6, eta_max=1e-6, **base),
+                         G.Provider.poisson_mg(gpu, n, precision=G.FP32))
+    assert ra["converged"] and rb["converged"]
+    assert ra["res"] <= 1e-10 * ra["res0"] and rb["res"] <= 1e-10 * rb["res0"]
+    assert rb["n_lin_iters"] > ra["n_lin_iters"]  # the tight forcing really changed the linear solves
+    assert rel_err(xa.numpy(), xb.numpy()) < 1e-8
+
+
 def test_fgmres_fp32_preconditioner(gpu):
     """Flexible GMRES with the FP32 V-cycle reaches the same tolerance; no extra precond."""
     G = _G()
