@@ -665,7 +665,7 @@ __device__ void tail_prolong(const T* __restrict__ xc, T* __restrict__ xf, int n
 }
 
 template <class T, bool SPLIT_IO>
-__global__ void __launch_bounds__(512) k_mg_tail(const T* __restrict__ b_g, const T* __restrict__ bs_g,
+__global__ void __launch_bounds__(1024) k_mg_tail(const T* __restrict__ b_g, const T* __restrict__ bs_g,
                                                  T* __restrict__ x_g, TailParams tp) {
     pdl_wait();
     pdl_trigger();

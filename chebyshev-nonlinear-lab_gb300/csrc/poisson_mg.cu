@@ -139,8 +139,8 @@ void PoissonMG::launch_tail32() {
     tp.post = post_;
     const bool split = (L.n & 1) != 0;
     tp.half = split ? make_split(L.n).half : 0;
-    if (split) launch_pdl(k_mg_tail<float, true>, 1, 512, tail_smem_, ctx_.stream, L.b32.p, L.bs32.p, L.xs, tp);
-    else launch_pdl(k_mg_tail<float, false>, 1, 512, tail_smem_, ctx_.stream, L.b32.p, L.bs32.p, L.xs, tp);
+    if (split) launch_pdl(k_mg_tail<float, true>, 1, 1024, tail_smem_, ctx_.stream, L.b32.p, L.bs32.p, L.xs, tp);
+    else launch_pdl(k_mg_tail<float, false>, 1, 1024, tail_smem_, ctx_.stream, L.b32.p, L.bs32.p, L.xs, tp);
     ctx_.count_launch();
     L.cur32 = L.xs;
     ctx_.check_launch("mg tail (fp32)");
