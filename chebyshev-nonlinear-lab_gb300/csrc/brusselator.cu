@@ -606,8 +606,11 @@ template <class T> __device__ __forceinline__ const LvlArgs<T>& tail_args(const 
 template <> __device__ __forceinline__ const LvlArgs<double>& tail_args<double>(const TailLvl& L) { return L.d; }
 template <> __device__ __forceinline__ const LvlArgs<float>& tail_args<float>(const TailLvl& L) { return L.f; }
 
+// threads of the one-CTA tail: 1024 in FP32 (64 registers, no spills), 512 in FP64 (which would spill at 1024)
 template <class T>
-__global__ void __launch_bounds__(512, 1) k_bmg_tail(const TailLvl* __restrict__ desc, int count, int pre, int post,
+constexpr int kBmgTailThreads = sizeof(T) == 4 ? 1024 : 512;
+template <class T>
+__global__ void __launch_bounds__(kBmgTailThreads<T>, 1) k_bmg_tail(const TailLvl* __restrict__ desc, int count, int pre, int post,
                                                      int sweeps, const T* __restrict__ Bin, T* __restrict__ Xout) {
     pdl_wait();
     pdl_trigger();
@@ -1139,7 +1142,7 @@ void BrussMG2D::cycle(size_t l) {
     const dim3 pgrid((unsigned)((n / 2 + 31) / 32), (unsigned)((n + 7) / 8));
     const size_t nn = (size_t)n * n;
     if ((int)l == tail_first_) {
-        launch_pdl(k_bmg_tail<T>, 1, 512, tail_smem_, s, reinterpret_cast<const TailLvl*>(tail_desc_.p), tail_count_, pre_,
+        launch_pdl(k_bmg_tail<T>, 1, kBmgTailThreads<T>, tail_smem_, s, reinterpret_cast<const TailLvl*>(tail_desc_.p), tail_count_, pre_,
                                                   post_, kBmgCoarsestSweeps, Bv, X);
         ctx_.count_launch();
         return;
