@@ -481,6 +481,28 @@ __device__ __forceinline__ void prolong_point(const float (&X)[2][2][2], const b
     *e = *e + acc;
 }
 
+// The same correction without the update: returns the weighted sum for fine point (A, B, C) of the cell.
+template <int A, int B, int C>
+__device__ __forceinline__ float prolong_sum(const float (&X)[2][2][2], const bool (&pi)[2], const bool (&pj)[2],
+                                             const bool (&pk)[2]) {
+    const float w = (A ? 1.0f : 0.5f) * (B ? 1.0f : 0.5f) * (C ? 1.0f : 0.5f);
+    float acc = 0.0f;
+#pragma unroll
+    for (int di = A; di < 2; ++di) {
+        if (!pi[di]) continue;
+#pragma unroll
+        for (int dj = B; dj < 2; ++dj) {
+            if (!pj[dj]) continue;
+#pragma unroll
+            for (int dk = C; dk < 2; ++dk) {
+                if (!pk[dk]) continue;
+                acc = __fmaf_rn(w, X[di][dj][dk], acc);
+            }
+        }
+    }
+    return acc;
+}
+
 // Fine x += trilinear interpolation of coarse x (k_prolong's arithmetic) on a split fine level.
 // A thread owns the coarse cell (I, J, K), I, J, K in [0, nc], i.e. the fine points
 // (2I + a, 2J + b, 2K + c), a, b, c in {0, 1}, inside the grid; it loads the eight coarse values
@@ -511,11 +533,27 @@ __global__ void __launch_bounds__(BX* BY) k_prolong_split(const float* __restric
                 X[di][dj][dk] = v;
             }
     const bool ia = I < nc, jb = J < nc, kc = K < nc;  // fine index 2I + 1 inside the grid
+    if (!ALL) {
+        // the four colour-0 points: their fine values are loaded before any is stored (the compiler
+        // cannot tell the four addresses apart, and would otherwise wait out each load in turn)
+        const int L0 = ((2 * I) * nf + 2 * J) * nf + 2 * K;
+        float* e0 = xf + split_at(L0, halff);
+        float* e1 = xf + split_at(L0 + nf + 1, halff);       // (0, 1, 1)
+        float* e2 = xf + split_at(L0 + nf * nf + 1, halff);  // (1, 0, 1)
+        float* e3 = xf + split_at(L0 + nf * nf + nf, halff); // (1, 1, 0)
+        const bool h1 = jb && kc, h2 = ia && kc, h3 = ia && jb;
+        const float v0 = *e0, v1 = h1 ? *e1 : 0.0f, v2 = h2 ? *e2 : 0.0f, v3 = h3 ? *e3 : 0.0f;
+        *e0 = v0 + prolong_sum<0, 0, 0>(X, pi, pj, pk);
+        if (h1) *e1 = v1 + prolong_sum<0, 1, 1>(X, pi, pj, pk);
+        if (h2) *e2 = v2 + prolong_sum<1, 0, 1>(X, pi, pj, pk);
+        if (h3) *e3 = v3 + prolong_sum<1, 1, 0>(X, pi, pj, pk);
+        return;
+    }
     prolong_point<0, 0, 0>(X, pi, pj, pk, xf, I, J, K, nf, halff);
     if (jb && kc) prolong_point<0, 1, 1>(X, pi, pj, pk, xf, I, J, K, nf, halff);
     if (ia && kc) prolong_point<1, 0, 1>(X, pi, pj, pk, xf, I, J, K, nf, halff);
     if (ia && jb) prolong_point<1, 1, 0>(X, pi, pj, pk, xf, I, J, K, nf, halff);
-    if (ALL) {
+    {
         if (kc) prolong_point<0, 0, 1>(X, pi, pj, pk, xf, I, J, K, nf, halff);
         if (jb) prolong_point<0, 1, 0>(X, pi, pj, pk, xf, I, J, K, nf, halff);
         if (ia) prolong_point<1, 0, 0>(X, pi, pj, pk, xf, I, J, K, nf, halff);
