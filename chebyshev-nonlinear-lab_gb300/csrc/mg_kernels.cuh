@@ -146,14 +146,14 @@ __global__ void __launch_bounds__(BX* BY) k_prolong(const T* __restrict__ xc, T*
     if (k >= nf) return;
     int ci[2], cj[2], ck[2];
     const int ni = interp(i, nc, ci), nj = interp(j, nc, cj), nk = interp(k, nc, ck);
-    const T wi = (ni == 1 && (i & 1)) ? T(1) : T(0.5);
-    const T wj = (nj == 1 && (j & 1)) ? T(1) : T(0.5);
-    const T wk = (nk == 1 && (k & 1)) ? T(1) : T(0.5);
+    // w = wi wj wk, each 1 (odd index) or 1/2: the power of two 2^-halves, picked without FP64 work
+    const int halves = !(ni == 1 && (i & 1)) + !(nj == 1 && (j & 1)) + !(nk == 1 && (k & 1));
+    const T w = halves == 0 ? T(1) : (halves == 1 ? T(0.5) : (halves == 2 ? T(0.25) : T(0.125)));
     T acc = zero<T>();
     for (int a = 0; a < ni; ++a)
         for (int b = 0; b < nj; ++b) {
             const T* row = xc + ((size_t)ci[a] * nc + cj[b]) * nc;
-            for (int c = 0; c < nk; ++c) acc = fma_t(wi * wj * wk, row[ck[c]], acc);
+            for (int c = 0; c < nk; ++c) acc = fma_t(w, row[ck[c]], acc);
         }
     const size_t p = ((size_t)i * nf + j) * nf + k;
     xf[p] = xf[p] + acc;
