@@ -542,14 +542,13 @@ __device__ __forceinline__ void prolong_point(const T* Xc, int nc, int I, int J,
     const int nf = 2 * nc;
     const size_t f00 = pidx(nf, 2 * I, 2 * J), f10 = pidx(nf, 2 * I + 1, 2 * J);
     const size_t f01 = pidx(nf, 2 * I, 2 * J + 1), f11 = pidx(nf, 2 * I + 1, 2 * J + 1);
-    auto add = [Xf](size_t p, T du, T dv) {
-        const auto x = ld2(Xf, p);
-        st2(Xf, p, x.x + du, x.y + dv);
-    };
-    add(f00, c00.x, c00.y);
-    add(f10, T(0.5) * (c00.x + c10.x), T(0.5) * (c00.y + c10.y));
-    add(f01, T(0.5) * (c00.x + c01.x), T(0.5) * (c00.y + c01.y));
-    add(f11, T(0.25) * (((c00.x + c10.x) + c01.x) + c11.x), T(0.25) * (((c00.y + c10.y) + c01.y) + c11.y));
+    // the four fine pairs are loaded before any is stored (the compiler cannot tell the addresses apart)
+    const auto x00 = ld2(Xf, f00), x10 = ld2(Xf, f10), x01 = ld2(Xf, f01), x11 = ld2(Xf, f11);
+    st2(Xf, f00, x00.x + c00.x, x00.y + c00.y);
+    st2(Xf, f10, x10.x + T(0.5) * (c00.x + c10.x), x10.y + T(0.5) * (c00.y + c10.y));
+    st2(Xf, f01, x01.x + T(0.5) * (c00.x + c01.x), x01.y + T(0.5) * (c00.y + c01.y));
+    st2(Xf, f11, x11.x + T(0.25) * (((c00.x + c10.x) + c01.x) + c11.x),
+        x11.y + T(0.25) * (((c00.y + c10.y) + c01.y) + c11.y));
 }
 
 template <class T>
