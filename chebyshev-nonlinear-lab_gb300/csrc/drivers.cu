@@ -387,13 +387,16 @@ void newton_krylov(NonlinearOp& f, double* x0, const KrylovParams& p, Provider* 
         }
         const double eta = forcing(p, k, rnorm, rprev, eta_prev, out.res0);
         S.bind(J, pc);
-        const GmresResult g = S.gmres.solve(J, Mp, S.Fx, S.z.p, gmres_opts(p, eta, rnorm, S.f32()));
+        GmresOptions go = gmres_opts(p, eta, rnorm, S.f32());
+        go.x_base = S.x;  // the solution update may form the full step xn = x - z in the same pass
+        go.x_step = S.xn;
+        const GmresResult g = S.gmres.solve(J, Mp, S.Fx, S.z.p, go);
         add_lin(out, g);
         if (g.breakdown) break;
         double lam = 1.0;
         bool ok = false;
         while (lam >= p.min_lambda) {
-            dev_newton_step(S.ctx, S.x, S.z.p, lam, S.xn, N);
+            if (!(lam == 1.0 && g.stepped)) dev_newton_step(S.ctx, S.x, S.z.p, lam, S.xn, N);
             const double fn = S.eval_trial();
             ++out.n_F;
             if (fn <= (1.0 - p.armijo * lam) * rnorm) {

@@ -277,9 +277,11 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs_df(const float* __restrict_
 // x += scale * sum_r coef[r] Z_r (ASSIGN: x = scale * sum_r coef[r] Z_r, x not read) with FP32 Z and
 // |coef| <= 1 (the host normalises them by scale): the sum in double-FP32, then one FMA (or multiply)
 // into x — two FP64 instructions a point
-template <int CNT, bool ASSIGN>
+// STEP (with ASSIGN): also xs = xb - x, the full Newton step from the value just stored.
+template <int CNT, bool ASSIGN, bool STEP = false>
 __global__ void k_combine_df(const float* __restrict__ Z, size_t ldz, const double* __restrict__ coef, double scale,
-                             double* x, size_t N) {
+                             double* x, size_t N, const double* __restrict__ xb = nullptr,
+                             double* __restrict__ xs = nullptr) {
     pdl_wait();
     pdl_trigger();
     __shared__ DF cs[CNT];
@@ -293,17 +295,19 @@ __global__ void k_combine_df(const float* __restrict__ Z, size_t ldz, const doub
         DF t{0.0f, 0.0f};
 #pragma unroll
         for (int r = 0; r < CNT; ++r) df_mac(t, c[r], Z[(size_t)r * ldz + i]);
-        x[i] = ASSIGN ? __dmul_rn(scale, df_to_f64(t)) : __fma_rn(scale, df_to_f64(t), x[i]);
+        const double v = ASSIGN ? __dmul_rn(scale, df_to_f64(t)) : __fma_rn(scale, df_to_f64(t), x[i]);
+        x[i] = v;
+        if (STEP) xs[i] = xb[i] - v;
     }
 }
 
-template <bool ASSIGN>
+template <bool ASSIGN, bool STEP = false>
 void launch_combine_df(Context& ctx, unsigned grid, int cnt, const float* Z, size_t N, const double* coef, double scale,
-                       double* x) {
+                       double* x, const double* xb = nullptr, double* xs = nullptr) {
     switch (cnt) {
 #define NUMA_COMBINE_DF_CASE(K)                                                                               \
     case K:                                                                                                   \
-        launch_pdl(k_combine_df<K, ASSIGN>, grid, 256, 0, ctx.stream, Z, N, coef, scale, x, N);                 \
+        launch_pdl(k_combine_df<K, ASSIGN, STEP>, grid, 256, 0, ctx.stream, Z, N, coef, scale, x, N, xb, xs);   \
         break;
         NUMA_COMBINE_DF_CASE(1)
         NUMA_COMBINE_DF_CASE(2)
@@ -616,8 +620,14 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
         }
         NUMA_CUDA(cudaMemcpyAsync(ydev, yh, k * sizeof(double), cudaMemcpyHostToDevice, ctx_.stream));
         if (v32) {
-            if (x_zero_pending) launch_combine_df<true>(ctx_, eg, (int)k, Z32_.p, N, ydev, scale, x);
-            else launch_combine_df<false>(ctx_, eg, (int)k, Z32_.p, N, ydev, scale, x);
+            if (x_zero_pending && o.x_step) {
+                launch_combine_df<true, true>(ctx_, eg, (int)k, Z32_.p, N, ydev, scale, x, o.x_base, o.x_step);
+                res.stepped = true;
+            } else {
+                if (x_zero_pending) launch_combine_df<true>(ctx_, eg, (int)k, Z32_.p, N, ydev, scale, x);
+                else launch_combine_df<false>(ctx_, eg, (int)k, Z32_.p, N, ydev, scale, x);
+                res.stepped = false;  // a later update: the step written before no longer matches x
+            }
             x_zero_pending = false;
         } else {
             settle_x();

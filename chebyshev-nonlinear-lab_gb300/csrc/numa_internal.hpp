@@ -414,6 +414,7 @@ struct GmresResult {
     size_t iters = 0, matvecs = 0, precs = 0;
     double rel_res = 0.0;
     bool converged = false, breakdown = false;
+    bool stepped = false;  // GmresOptions::x_step holds x_base - x for the returned x
 };
 
 // Arnoldi basis of the last cycle (gmres.hpp:25-35).  V holds (at least) k+1 device vectors.
@@ -474,6 +475,10 @@ struct GmresOptions {
     bool flexible = false;
     double bnorm = -1.0;  // ||b|| when the caller knows it (>= 0), used by the flexible CGS1 solver
     const float* b32 = nullptr;  // RN32(b) when the caller has it (the FP32 Arnoldi basis starts from it)
+    // When given (a Newton driver): the solution update also writes x_step = x_base - x, the full
+    // Newton step, and reports it in GmresResult::stepped if that update was the solve's last
+    const double* x_base = nullptr;
+    double* x_step = nullptr;
 };
 
 class Gmres {
