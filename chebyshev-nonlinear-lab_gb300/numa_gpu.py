@@ -12,6 +12,7 @@ call that needs a GPU raises ``NumaGPUError`` when there is none.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import os
 import weakref
@@ -290,6 +291,21 @@ def _f64(a) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
+# Contexts still open when the interpreter exits are closed (their objects first) by an exit hook, which
+# runs before the CUDA runtime is torn down: finalisers left to module teardown could otherwise free
+# device memory after it.
+_live_contexts: "weakref.WeakSet" = weakref.WeakSet()  # contexts and batch executors
+
+
+@atexit.register
+def _close_live_contexts():
+    for ctx in list(_live_contexts):
+        try:
+            ctx.close()
+        except Exception:
+            pass
+
+
 class Context:
     """One device and one stream (numa_gpu_ctx)."""
 
@@ -301,6 +317,7 @@ class Context:
             raise NumaGPUError(rc, "numa_gpu_ctx_create")
         self.h = h
         self._children = weakref.WeakSet()
+        _live_contexts.add(self)
 
     def _adopt(self, obj):
         """Objects created on this context are closed before it (whatever the order of garbage collection)."""
@@ -1126,6 +1143,7 @@ class BatchExecutor:
         if rc != OK:
             raise NumaGPUError(rc, "numa_gpu_batch_create", self.lib.numa_gpu_batch_last_error().decode())
         self.h = h
+        _live_contexts.add(self)  # closed at exit like a context (it owns worker contexts)
 
     def close(self):
         if self.h:
