@@ -67,12 +67,13 @@ template <bool WRITE_C, bool NORM, bool C32>
 __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, double* __restrict__ F,
                                                  double* __restrict__ c_out, float* __restrict__ c32_out,
                                                  float* __restrict__ f32_out, int n,
-                                                 int ichunk, double lam, double h2inv, RedArgs red, double* norm_out) {
+                                                 int ichunk, double lam, double h2inv, RedArgs red, double* norm_out,
+                                                 int zoff = 0, int norm_raw = 0) {
     pdl_wait();
     pdl_trigger();
     const int k = blockIdx.x * BX + threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
-    const int i0 = blockIdx.z * ichunk;
+    const int i0 = (blockIdx.z + zoff) * ichunk;  // zoff: the first plane chunk of a piece
     const int i1 = min(i0 + ichunk, n);
     const size_t plane = (size_t)n * n;
     double acc[1] = {0.0};
@@ -100,7 +101,9 @@ __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, d
     if (NORM) {
         __shared__ double sm[1][32];
         block_sum<1>(acc, sm);
-        grid_reduce_finish<1>(acc, red, [norm_out] __device__(const double(&t)[1]) { *norm_out = __dsqrt_rn(t[0]); });
+        grid_reduce_finish<1>(acc, red, [norm_out, norm_raw] __device__(const double(&t)[1]) {
+            *norm_out = norm_raw ? t[0] : __dsqrt_rn(t[0]);  // raw: a piece's sum of squares
+        });
     }
 }
 
@@ -339,27 +342,68 @@ void Bratu3D::jvp_bound(const double* v, double* out) {
 }
 
 void Bratu3D::eval(const double* x, double* out, double* c_out, double* norm_out) {
+    const March m = march_shape((int)n_, norm_out != nullptr);
+    eval_launch(x, out, c_out, norm_out, m.grid, m.ichunk, 0, 0);
+}
+
+// One launch of k_eval over the plane chunks [zoff, zoff + grid.z) (of ichunk planes each).
+void Bratu3D::eval_launch(const double* x, double* out, double* c_out, double* norm_out, dim3 grid, int ichunk,
+                          int zoff, int norm_raw) {
     const int n = (int)n_;
     const bool norm = norm_out != nullptr;
-    March m = march_shape(n, norm);
-    dim3 blk(BX, BY);
+    const dim3 blk(BX, BY);
     float* c32 = (c_out && mixed_cache_) ? reinterpret_cast<float*>(c_out + N_) : nullptr;
     float* f32 = c32 ? reinterpret_cast<float*>(c_out + N_ + (N_ + 1) / 2) : nullptr;
     const double lam = lambda_, h2 = h2inv_;
+    const RedArgs red = ctx_.red;
     if (c32 && norm)
-        launch_pdl(k_eval<true, true, true>, m.grid, blk, 0, ctx_.stream, x, out, c_out, c32, f32, n, m.ichunk, lam, h2, ctx_.red, norm_out);
+        launch_pdl(k_eval<true, true, true>, grid, blk, 0, ctx_.stream, x, out, c_out, c32, f32, n, ichunk, lam, h2, red,
+                   norm_out, zoff, norm_raw);
     else if (c32)
-        launch_pdl(k_eval<true, false, true>, m.grid, blk, 0, ctx_.stream, x, out, c_out, c32, f32, n, m.ichunk, lam, h2, ctx_.red, nullptr);
+        launch_pdl(k_eval<true, false, true>, grid, blk, 0, ctx_.stream, x, out, c_out, c32, f32, n, ichunk, lam, h2, red,
+                   nullptr, zoff, norm_raw);
     else if (c_out && norm)
-        launch_pdl(k_eval<true, true, false>, m.grid, blk, 0, ctx_.stream, x, out, c_out, nullptr, nullptr, n, m.ichunk, lam, h2, ctx_.red, norm_out);
+        launch_pdl(k_eval<true, true, false>, grid, blk, 0, ctx_.stream, x, out, c_out, nullptr, nullptr, n, ichunk, lam,
+                   h2, red, norm_out, zoff, norm_raw);
     else if (c_out)
-        launch_pdl(k_eval<true, false, false>, m.grid, blk, 0, ctx_.stream, x, out, c_out, nullptr, nullptr, n, m.ichunk, lam, h2, ctx_.red, nullptr);
+        launch_pdl(k_eval<true, false, false>, grid, blk, 0, ctx_.stream, x, out, c_out, nullptr, nullptr, n, ichunk, lam,
+                   h2, red, nullptr, zoff, norm_raw);
     else if (norm)
-        launch_pdl(k_eval<false, true, false>, m.grid, blk, 0, ctx_.stream, x, out, nullptr, nullptr, nullptr, n, m.ichunk, lam, h2, ctx_.red, norm_out);
+        launch_pdl(k_eval<false, true, false>, grid, blk, 0, ctx_.stream, x, out, nullptr, nullptr, nullptr, n, ichunk,
+                   lam, h2, red, norm_out, zoff, norm_raw);
     else
-        launch_pdl(k_eval<false, false, false>, m.grid, blk, 0, ctx_.stream, x, out, nullptr, nullptr, nullptr, n, m.ichunk, lam, h2, ctx_.red, nullptr);
+        launch_pdl(k_eval<false, false, false>, grid, blk, 0, ctx_.stream, x, out, nullptr, nullptr, nullptr, n, ichunk,
+                   lam, h2, red, nullptr, zoff, norm_raw);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d eval");
+}
+
+// Pieces of the evaluation for an upload that overlaps it: the plane chunks of the fused-norm grid
+// shared out into up to kEvalPieces runs of whole chunks.
+int Bratu3D::eval_pieces() const {
+    const March m = march_shape((int)n_, true);
+    return (int)std::min<unsigned>(kEvalPieces, m.grid.z);
+}
+
+size_t Bratu3D::eval_piece_begin(int c) const {
+    const March m = march_shape((int)n_, true);
+    const int K = eval_pieces();
+    const size_t plane0 = std::min<size_t>((size_t)(c * (int)m.grid.z / K) * m.ichunk, n_);
+    return plane0 * n_ * n_;
+}
+
+size_t Bratu3D::eval_piece_need(int c) const {
+    const March m = march_shape((int)n_, true);
+    const int K = eval_pieces();
+    const size_t plane1 = std::min<size_t>((size_t)((c + 1) * (int)m.grid.z / K) * m.ichunk, n_);
+    return std::min(plane1 + 1, n_) * n_ * n_;  // its planes and the next one (the stencil's i + 1)
+}
+
+void Bratu3D::eval_piece(const double* x, double* out, double* cache, int c, double* sumsq) {
+    const March m = march_shape((int)n_, true);
+    const int K = eval_pieces();
+    const int z0 = c * (int)m.grid.z / K, z1 = (c + 1) * (int)m.grid.z / K;
+    eval_launch(x, out, cache, sumsq, dim3(m.grid.x, m.grid.y, (unsigned)(z1 - z0)), m.ichunk, z0, 1);
 }
 
 void Bratu3D::coef(const double* x, double* c) {

@@ -67,6 +67,7 @@ struct CtxExtras {
     std::unique_ptr<Bratu3D> host_op;
     std::unique_ptr<Provider> host_pc;
     DeviceArray<double> host_x;
+    std::unique_ptr<HostUpload> host_up;  // the staged upload of a pinned x0 (Newton–Krylov)
     size_t host_n = 0;
     double host_lambda = 0.0;
     int host_kind = -1, host_prec = -1;
@@ -916,10 +917,24 @@ int numa_gpu_solve_bratu3d_host(numa_gpu_ctx* ctx, size_t n, double lambda, int 
         }
         const size_t N = n * n * n;
         e.host_x.resize(N);
-        NUMA_CUDA(cudaMemcpyAsync(e.host_x.p, x0, N * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        // a pinned x0 goes up in pieces that overlap the first evaluation; any other x0 up front
+        cudaPointerAttributes pa{};
+        const bool pinned = method == NUMA_GPU_METHOD_NK && cudaPointerGetAttributes(&pa, x0) == cudaSuccess &&
+                            pa.type == cudaMemoryTypeHost;
+        cudaGetLastError();  // clears the error older runtimes report for an unregistered pointer
+        if (pinned && !e.host_up) {
+            auto up = std::make_unique<HostUpload>();
+            NUMA_CUDA(cudaStreamCreateWithFlags(&up->copy, cudaStreamNonBlocking));
+            NUMA_CUDA(cudaEventCreateWithFlags(&up->start, cudaEventDisableTiming));
+            for (cudaEvent_t& ev : up->done) NUMA_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            e.host_up = std::move(up);
+        }
+        if (pinned) e.host_up->host = x0;
+        else NUMA_CUDA(cudaMemcpyAsync(e.host_x.p, x0, N * sizeof(double), cudaMemcpyHostToDevice, c.stream));
         KrylovParams kp = params_from_c(p);
         Provider* pc = e.host_pc.get();
-        if (method == NUMA_GPU_METHOD_NK) newton_krylov(*e.host_op, e.host_x.p, kp, pc, *result);
+        if (method == NUMA_GPU_METHOD_NK)
+            newton_krylov(*e.host_op, e.host_x.p, kp, pc, *result, pinned ? e.host_up.get() : nullptr);
         else if (method == NUMA_GPU_METHOD_TF2018) tf_chebyshev_2018(*e.host_op, e.host_x.p, kp, pc, *result);
         else {
             if (method == NUMA_GPU_METHOD_CHEB_REC) kp.recycle = true;

@@ -400,6 +400,7 @@ enum ScalarSlot : int {
     kSlotFdXnorm = 19,
     kSlotFdInvH = 20,     // RN(1/h) and RN(1/h^2) for the quotients
     kSlotFdInvHH = 21,
+    kSlotPieceSums = 24,  // sums of squares of an evaluation's pieces, 8 entries
     kSlotGmresH = 64,     // Hessenberg column, m + 2 entries
     kSlotGmresH2 = 320,   // CGS2 second-pass coefficients, up to 8
     kSlotGmresY = 400,    // least-squares solution y, m entries

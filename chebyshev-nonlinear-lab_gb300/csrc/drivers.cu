@@ -364,7 +364,17 @@ double forcing(const KrylovParams& p, size_t k, double rnorm, double rprev, doub
 
 // ------------------------------------------------------------------------------ newton_krylov
 // krylov_newton.hpp:69-114
-void newton_krylov(NonlinearOp& f, double* x0, const KrylovParams& p, Provider* pc, numa_krylov_result& out) {
+// *out = sqrt(sum of the K pieces' sums of squares), summed in piece order
+__global__ void k_sum_sqrt(const double* __restrict__ parts, int K, double* __restrict__ out) {
+    pdl_wait();
+    pdl_trigger();
+    double s = 0.0;
+    for (int c = 0; c < K; ++c) s += parts[c];
+    *out = __dsqrt_rn(s);
+}
+
+void newton_krylov(NonlinearOp& f, double* x0, const KrylovParams& p, Provider* pc, numa_krylov_result& out,
+                   const HostUpload* up) {
     const auto t0 = std::chrono::steady_clock::now();
     std::memset(&out, 0, sizeof(out));
     SolveState S(f, p, x0);
@@ -374,7 +384,34 @@ void newton_krylov(NonlinearOp& f, double* x0, const KrylovParams& p, Provider* 
     const size_t N = S.N;
     {
         Timers::Scope s(&S.timers, kT_F);
-        f.eval(S.x, S.Fx, S.cx, S.ctx.scalar(kSlotNormF));
+        const int K = up ? f.eval_pieces() : 0;
+        if (up && K == 0) {
+            NUMA_CUDA(cudaMemcpyAsync(S.x, up->host, N * sizeof(double), cudaMemcpyHostToDevice, S.ctx.stream));
+        }
+        if (K > 0) {
+            // the pieces of x0 go up on the copy stream while the evaluation runs on those already there
+            NUMA_CUDA(cudaEventRecord(up->start, S.ctx.stream));
+            NUMA_CUDA(cudaStreamWaitEvent(up->copy, up->start, 0));
+            for (int c = 0; c < K; ++c) {
+                const size_t b0 = f.eval_piece_begin(c), b1 = c + 1 < K ? f.eval_piece_begin(c + 1) : N;
+                NUMA_CUDA(cudaMemcpyAsync(S.x + b0, up->host + b0, (b1 - b0) * sizeof(double), cudaMemcpyHostToDevice,
+                                          up->copy));
+                NUMA_CUDA(cudaEventRecord(up->done[c], up->copy));
+            }
+            double* sums = S.ctx.scalar(kSlotPieceSums);
+            for (int c = 0; c < K; ++c) {
+                const size_t need = f.eval_piece_need(c);
+                int last = c;  // the last piece whose upload the evaluation of piece c reads
+                while (last + 1 < K && f.eval_piece_begin(last + 1) < need) ++last;
+                NUMA_CUDA(cudaStreamWaitEvent(S.ctx.stream, up->done[last], 0));
+                f.eval_piece(S.x, S.Fx, S.cx, c, sums + c);
+            }
+            launch_pdl(k_sum_sqrt, 1, 1, 0, S.ctx.stream, (const double*)sums, K, S.ctx.scalar(kSlotNormF));
+            S.ctx.count_launch();
+            S.ctx.check_launch("newton_krylov staged evaluation");
+        } else {
+            f.eval(S.x, S.Fx, S.cx, S.ctx.scalar(kSlotNormF));
+        }
     }
     ++out.n_F;
     double rnorm = S.ctx.fetch1(S.ctx.scalar(kSlotNormF));

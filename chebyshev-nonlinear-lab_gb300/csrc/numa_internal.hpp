@@ -46,6 +46,26 @@ public:
     // Announces the precision the Jacobian products of the coming solve will use, before any
     // evaluation (an operator may then keep what that precision needs in the cache).
     virtual void prepare_cache(int precision) { (void)precision; }
+    // The evaluation in pieces along the slowest index, so that an upload of x can overlap it:
+    // piece c writes the outputs from element eval_piece_begin(c) on (up to the next piece's begin),
+    // reads x below eval_piece_need(c), and stores the raw sum of squares of its F values at *sumsq.
+    // eval_pieces() = 0: not available.
+    virtual int eval_pieces() const { return 0; }
+    virtual size_t eval_piece_begin(int c) const {
+        (void)c;
+        return 0;
+    }
+    virtual size_t eval_piece_need(int c) const {
+        (void)c;
+        return size();
+    }
+    virtual void eval_piece(const double* x, double* out, double* cache, int c, double* sumsq) {
+        (void)x;
+        (void)out;
+        (void)cache;
+        (void)c;
+        (void)sumsq;
+    }
     // RN32(F) written by the evaluation that filled cache, where the operator keeps it (else null)
     virtual const float* f32_of_cache(const double* cache) const {
         (void)cache;
@@ -119,6 +139,10 @@ public:
     }
     void prepare_cache(int precision) override { mixed_cache_ = precision == NUMA_GPU_FP32; }
     void eval(const double* x, double* out, double* cache, double* norm_out) override;
+    int eval_pieces() const override;
+    size_t eval_piece_begin(int c) const override;
+    size_t eval_piece_need(int c) const override;
+    void eval_piece(const double* x, double* out, double* cache, int c, double* sumsq) override;
     void bind(const double* x, const double* cache, int precision) override;
     void jvp_bound(const double* v, double* out) override;
     bool has_jvp32() const override { return bound_precision_ == NUMA_GPU_FP32; }
@@ -155,6 +179,8 @@ private:
     int bound_precision_ = NUMA_GPU_FP64;
     bool mixed_cache_ = false;
     DeviceArray<float> c32_;
+    void eval_launch(const double* x, double* out, double* c_out, double* norm_out, dim3 grid, int ichunk, int zoff,
+                     int norm_raw);
 };
 
 void bratu_jvp32(Context& ctx, int n, double h2inv, const float* c32, const double* v, double* out);
@@ -581,7 +607,23 @@ private:
 };
 
 // x holds x0 on entry and the final iterate on return.
-void newton_krylov(NonlinearOp& f, double* x, const KrylovParams& p, Provider* pc, numa_krylov_result& out);
+constexpr int kEvalPieces = 8;  // most pieces of an evaluation overlapped with an upload
+// An initial point still in (pinned) host memory: newton_krylov uploads it in pieces on `copy` while the
+// first evaluation runs on the pieces already there.
+struct HostUpload {
+    const double* host = nullptr;
+    cudaStream_t copy = nullptr;
+    cudaEvent_t start = nullptr;
+    cudaEvent_t done[kEvalPieces] = {};
+    ~HostUpload() {
+        for (cudaEvent_t e : done)
+            if (e) cudaEventDestroy(e);
+        if (start) cudaEventDestroy(start);
+        if (copy) cudaStreamDestroy(copy);
+    }
+};
+void newton_krylov(NonlinearOp& f, double* x, const KrylovParams& p, Provider* pc, numa_krylov_result& out,
+                   const HostUpload* up = nullptr);
 void chebyshev_inexact(NonlinearOp& f, double* x, const KrylovParams& p, Provider* pc, numa_krylov_result& out);
 void tf_chebyshev_2018(NonlinearOp& f, double* x, const KrylovParams& p, Provider* pc, numa_krylov_result& out);
 

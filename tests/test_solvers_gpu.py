@@ -302,6 +302,31 @@ def test_host_buffer_api_matches_device_api(gpu):
     assert np.array_equal(xd, xh)
 
 
+@pytest.mark.parametrize("n,mixed", [(31, False), (63, True)])
+def test_host_api_staged_upload_of_pinned_start(gpu, n, mixed):
+    """A pinned x0 is uploaded in plane pieces that overlap the first residual evaluation; the
+    solve matches the device-buffer entry point (same counts, same solution to rounding: only the
+    order in which the first ||F|| is summed differs)."""
+    torch = pytest.importorskip("torch")
+    G = _G()
+    params = dict(rtol_nl=1e-10, gmres_restart=30)
+    if mixed:
+        params.update(flexible=1, jvp_precision=1)
+    mg = 1 if mixed else 0
+    x0 = 0.05 * make_point(n ** 3, 1.0)
+    xd, rd = gpu_solve(gpu, n, 6.0, "nk", "mg", params, x0=x0, mg_precision=mg)
+    h_in = torch.from_numpy(x0).pin_memory().numpy()
+    h_out = torch.empty(n ** 3, dtype=torch.float64, pin_memory=True).numpy()
+    for _ in range(2):  # the second call reuses the cached copy stream and events
+        h_out[:] = np.nan
+        xh, rh = G.solve_bratu3d_host(gpu, n, 6.0, h_in, out=h_out, method="nk", precond="mg",
+                                      mg_precision=mg, params=gpu_params(G, params))
+        assert rd["converged"] and rh["converged"]
+        assert all(rd[k] == rh[k] for k in COUNTS)
+        assert rel_err(xh, xd) < 1e-12
+        assert abs(rh["res0"] - rd["res0"]) <= 1e-13 * rd["res0"]
+
+
 def test_mixed_precision_error_vs_fp64(gpu):
     """FP32 V-cycle + FP32 Jacobian products inside FGMRES, FP64 outer: converges to the same
     tolerance, solution within 1e-8 of the FP64 path."""
