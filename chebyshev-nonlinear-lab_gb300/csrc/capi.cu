@@ -917,30 +917,41 @@ int numa_gpu_solve_bratu3d_host(numa_gpu_ctx* ctx, size_t n, double lambda, int 
         }
         const size_t N = n * n * n;
         e.host_x.resize(N);
-        // a pinned x0 goes up in pieces that overlap the first evaluation; any other x0 up front
-        cudaPointerAttributes pa{};
-        const bool pinned = method == NUMA_GPU_METHOD_NK && cudaPointerGetAttributes(&pa, x0) == cudaSuccess &&
-                            pa.type == cudaMemoryTypeHost;
-        cudaGetLastError();  // clears the error older runtimes report for an unregistered pointer
-        if (pinned && !e.host_up) {
+        // Newton–Krylov with pinned buffers overlaps the transfers with residual evaluations: x0 goes up in
+        // pieces under the first one, the predicted last iterate comes down under its own
+        const auto is_pinned = [](const void* ptr) {
+            cudaPointerAttributes pa{};
+            const bool pinned = cudaPointerGetAttributes(&pa, ptr) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+            cudaGetLastError();  // clears the error older runtimes report for an unregistered pointer
+            return pinned;
+        };
+        const bool nk = method == NUMA_GPU_METHOD_NK;
+        const bool pin_in = nk && is_pinned(x0), pin_out = nk && is_pinned(x_out);
+        if ((pin_in || pin_out) && !e.host_up) {
             auto up = std::make_unique<HostUpload>();
             NUMA_CUDA(cudaStreamCreateWithFlags(&up->copy, cudaStreamNonBlocking));
-            NUMA_CUDA(cudaEventCreateWithFlags(&up->start, cudaEventDisableTiming));
+            for (cudaEvent_t* ev : {&up->start, &up->fetch_start, &up->fetch_done})
+                NUMA_CUDA(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
             for (cudaEvent_t& ev : up->done) NUMA_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
             e.host_up = std::move(up);
         }
-        if (pinned) e.host_up->host = x0;
-        else NUMA_CUDA(cudaMemcpyAsync(e.host_x.p, x0, N * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        HostUpload* up = pin_in || pin_out ? e.host_up.get() : nullptr;
+        if (up) {
+            up->host = pin_in ? x0 : nullptr;
+            up->host_out = pin_out ? x_out : nullptr;
+            up->fetched = false;
+        }
+        if (!pin_in) NUMA_CUDA(cudaMemcpyAsync(e.host_x.p, x0, N * sizeof(double), cudaMemcpyHostToDevice, c.stream));
         KrylovParams kp = params_from_c(p);
         Provider* pc = e.host_pc.get();
-        if (method == NUMA_GPU_METHOD_NK)
-            newton_krylov(*e.host_op, e.host_x.p, kp, pc, *result, pinned ? e.host_up.get() : nullptr);
+        if (nk) newton_krylov(*e.host_op, e.host_x.p, kp, pc, *result, up);
         else if (method == NUMA_GPU_METHOD_TF2018) tf_chebyshev_2018(*e.host_op, e.host_x.p, kp, pc, *result);
         else {
             if (method == NUMA_GPU_METHOD_CHEB_REC) kp.recycle = true;
             chebyshev_inexact(*e.host_op, e.host_x.p, kp, pc, *result);
         }
-        NUMA_CUDA(cudaMemcpyAsync(x_out, e.host_x.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        if (up && up->fetched) NUMA_CUDA(cudaEventSynchronize(up->fetch_done));
+        else NUMA_CUDA(cudaMemcpyAsync(x_out, e.host_x.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
         c.sync();
     });
     result->status = rc;

@@ -374,7 +374,7 @@ __global__ void k_sum_sqrt(const double* __restrict__ parts, int K, double* __re
 }
 
 void newton_krylov(NonlinearOp& f, double* x0, const KrylovParams& p, Provider* pc, numa_krylov_result& out,
-                   const HostUpload* up) {
+                   HostUpload* up) {
     const auto t0 = std::chrono::steady_clock::now();
     std::memset(&out, 0, sizeof(out));
     SolveState S(f, p, x0);
@@ -384,8 +384,8 @@ void newton_krylov(NonlinearOp& f, double* x0, const KrylovParams& p, Provider* 
     const size_t N = S.N;
     {
         Timers::Scope s(&S.timers, kT_F);
-        const int K = up ? f.eval_pieces() : 0;
-        if (up && K == 0) {
+        const int K = up && up->host ? f.eval_pieces() : 0;
+        if (up && up->host && K == 0) {
             NUMA_CUDA(cudaMemcpyAsync(S.x, up->host, N * sizeof(double), cudaMemcpyHostToDevice, S.ctx.stream));
         }
         if (K > 0) {
@@ -417,11 +417,13 @@ void newton_krylov(NonlinearOp& f, double* x0, const KrylovParams& p, Provider* 
     double rnorm = S.ctx.fetch1(S.ctx.scalar(kSlotNormF));
     out.res0 = rnorm;
     double rprev = rnorm, eta_prev = p.eta_init;
+    const double* fetched = nullptr;  // the device iterate last downloaded to up->host_out
     for (size_t k = 0; k < p.max_nl; ++k) {
         if (rnorm <= p.rtol_nl * out.res0) {
             out.converged = 1;
             break;
         }
+        fetched = nullptr;  // this iteration's step overwrites the other buffer, the next one this one
         const double eta = forcing(p, k, rnorm, rprev, eta_prev, out.res0);
         S.bind(J, pc);
         GmresOptions go = gmres_opts(p, eta, rnorm, S.f32());
@@ -434,14 +436,25 @@ void newton_krylov(NonlinearOp& f, double* x0, const KrylovParams& p, Provider* 
         bool ok = false;
         while (lam >= p.min_lambda) {
             if (!(lam == 1.0 && g.stepped)) dev_newton_step(S.ctx, S.x, S.z.p, lam, S.xn, N);
+            // the linear model predicts the full step converges: download it while its residual is evaluated
+            const bool fetch = up && up->host_out && lam == 1.0 && g.rel_res * rnorm <= p.rtol_nl * out.res0;
+            if (fetch) {
+                NUMA_CUDA(cudaEventRecord(up->fetch_start, S.ctx.stream));
+                NUMA_CUDA(cudaStreamWaitEvent(up->copy, up->fetch_start, 0));
+                NUMA_CUDA(cudaMemcpyAsync(up->host_out, S.xn, N * sizeof(double), cudaMemcpyDeviceToHost, up->copy));
+                NUMA_CUDA(cudaEventRecord(up->fetch_done, up->copy));
+                fetched = S.xn;
+            }
             const double fn = S.eval_trial();
             ++out.n_F;
+            if (fetch) NUMA_CUDA(cudaStreamWaitEvent(S.ctx.stream, up->fetch_done, 0));  // before xn is written again
             if (fn <= (1.0 - p.armijo * lam) * rnorm) {
                 ok = true;
                 rprev = rnorm;
                 rnorm = fn;
                 break;
             }
+            fetched = nullptr;
             lam *= 0.5;
         }
         if (!ok) break;
@@ -451,6 +464,7 @@ void newton_krylov(NonlinearOp& f, double* x0, const KrylovParams& p, Provider* 
     }
     if (rnorm <= p.rtol_nl * out.res0) out.converged = 1;
     out.res = rnorm;
+    if (up) up->fetched = fetched != nullptr && fetched == S.x;  // the returned iterate is the one downloaded
     S.finish();
     S.timers.collect(out);
     out.t_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -608,22 +608,28 @@ private:
 
 // x holds x0 on entry and the final iterate on return.
 constexpr int kEvalPieces = 8;  // most pieces of an evaluation overlapped with an upload
-// An initial point still in (pinned) host memory: newton_krylov uploads it in pieces on `copy` while the
-// first evaluation runs on the pieces already there.
+// Pinned host buffers of a Newton solve.  `host` (the initial point) goes up in pieces on `copy` while the
+// first evaluation runs on the pieces already there.  `host_out`, when set, receives a trial point the
+// linear model predicts to be the last while its residual is evaluated; `fetched` reports that the
+// returned solution is that copy (otherwise the caller downloads it).
 struct HostUpload {
     const double* host = nullptr;
+    double* host_out = nullptr;
+    bool fetched = false;
     cudaStream_t copy = nullptr;
     cudaEvent_t start = nullptr;
     cudaEvent_t done[kEvalPieces] = {};
+    cudaEvent_t fetch_start = nullptr, fetch_done = nullptr;
     ~HostUpload() {
         for (cudaEvent_t e : done)
             if (e) cudaEventDestroy(e);
-        if (start) cudaEventDestroy(start);
+        for (cudaEvent_t e : {start, fetch_start, fetch_done})
+            if (e) cudaEventDestroy(e);
         if (copy) cudaStreamDestroy(copy);
     }
 };
 void newton_krylov(NonlinearOp& f, double* x, const KrylovParams& p, Provider* pc, numa_krylov_result& out,
-                   const HostUpload* up = nullptr);
+                   HostUpload* up = nullptr);
 void chebyshev_inexact(NonlinearOp& f, double* x, const KrylovParams& p, Provider* pc, numa_krylov_result& out);
 void tf_chebyshev_2018(NonlinearOp& f, double* x, const KrylovParams& p, Provider* pc, numa_krylov_result& out);
 

@@ -302,11 +302,12 @@ def test_host_buffer_api_matches_device_api(gpu):
     assert np.array_equal(xd, xh)
 
 
-@pytest.mark.parametrize("n,mixed", [(31, False), (63, True)])
-def test_host_api_staged_upload_of_pinned_start(gpu, n, mixed):
-    """A pinned x0 is uploaded in plane pieces that overlap the first residual evaluation; the
-    solve matches the device-buffer entry point (same counts, same solution to rounding: only the
-    order in which the first ||F|| is summed differs)."""
+@pytest.mark.parametrize("n,mixed,pin_in", [(31, False, True), (63, True, True), (31, False, False)])
+def test_host_api_staged_upload_of_pinned_start(gpu, n, mixed, pin_in):
+    """A pinned x0 is uploaded in plane pieces that overlap the first residual evaluation, and the
+    iterate predicted to be the last is downloaded to a pinned output while its residual is
+    evaluated; the solve matches the device-buffer entry point (same counts, same solution to
+    rounding: only the order in which the first ||F|| is summed differs)."""
     torch = pytest.importorskip("torch")
     G = _G()
     params = dict(rtol_nl=1e-10, gmres_restart=30)
@@ -315,7 +316,7 @@ def test_host_api_staged_upload_of_pinned_start(gpu, n, mixed):
     mg = 1 if mixed else 0
     x0 = 0.05 * make_point(n ** 3, 1.0)
     xd, rd = gpu_solve(gpu, n, 6.0, "nk", "mg", params, x0=x0, mg_precision=mg)
-    h_in = torch.from_numpy(x0).pin_memory().numpy()
+    h_in = torch.from_numpy(x0).pin_memory().numpy() if pin_in else x0.copy()
     h_out = torch.empty(n ** 3, dtype=torch.float64, pin_memory=True).numpy()
     for _ in range(2):  # the second call reuses the cached copy stream and events
         h_out[:] = np.nan
