@@ -220,6 +220,25 @@ __global__ void __launch_bounds__(BX* BY) k_jvp32(const float* __restrict__ c32,
     }
 }
 
+// One point of k_jvp32f: h^-2 (6 v - the six neighbours, i-1, i+1, j-1, j+1, k-1, k+1) - c v.
+__device__ __forceinline__ float jvp32_point(float below, float cur, float above, float jm, float jp, float km,
+                                             float kp, float cc, float h2inv) {
+    float s = 6.0f * cur;
+    s = s - below;
+    s = s - above;
+    s = s - jm;
+    s = s - jp;
+    s = s - km;
+    s = s - kp;
+    return h2inv * s - cc * cur;
+}
+
+template <class OT>
+__device__ __forceinline__ void jvp32_store(OT* __restrict__ out, size_t p, float r) {
+    if constexpr (sizeof(OT) == 4) out[p] = r;
+    else out[p] = f32_to_f64(r);
+}
+
 // The FP32 product from an FP32 v (the V-cycle's output): no conversion, so no shared-memory tile —
 // a (k, j) column marches in i holding planes i-1, i, i+1 in registers, and the neighbours in j and k
 // come through L1.  The arithmetic is k_jvp32's, operation for operation (same results); OT = float
@@ -239,24 +258,28 @@ __global__ void __launch_bounds__(BX* BY) k_jvp32f(const float* __restrict__ c32
     const bool jlo = j > 0, jhi = j + 1 < n, klo = k > 0, khi = k + 1 < n;
     float below = i0 > 0 ? v[(size_t)(i0 - 1) * plane + col] : 0.0f;
     float cur = i0 < i1 ? v[(size_t)i0 * plane + col] : 0.0f;
-    for (int i = i0; i < i1; ++i) {
+    int i = i0;
+    // two planes a step, all their loads issued before either store: twice the bytes in flight
+    for (; i + 1 < i1; i += 2) {
+        const size_t p = (size_t)i * plane + col, q = p + plane;
+        const float a1 = v[q];  // i + 1 < i1 <= n
+        const float a2 = (i + 2 < n) ? v[q + plane] : 0.0f;
+        const float jm0 = jlo ? v[p - n] : 0.0f, jp0 = jhi ? v[p + n] : 0.0f;
+        const float km0 = klo ? v[p - 1] : 0.0f, kp0 = khi ? v[p + 1] : 0.0f;
+        const float jm1 = jlo ? v[q - n] : 0.0f, jp1 = jhi ? v[q + n] : 0.0f;
+        const float km1 = klo ? v[q - 1] : 0.0f, kp1 = khi ? v[q + 1] : 0.0f;
+        const float c0 = c32[p], c1 = c32[q];
+        jvp32_store(out, p, jvp32_point(below, cur, a1, jm0, jp0, km0, kp0, c0, h2inv));
+        jvp32_store(out, q, jvp32_point(cur, a1, a2, jm1, jp1, km1, kp1, c1, h2inv));
+        below = a1;
+        cur = a2;
+    }
+    if (i < i1) {
         const size_t p = (size_t)i * plane + col;
         const float above = (i + 1 < n) ? v[p + plane] : 0.0f;
         const float jm = jlo ? v[p - n] : 0.0f, jp = jhi ? v[p + n] : 0.0f;
         const float km = klo ? v[p - 1] : 0.0f, kp = khi ? v[p + 1] : 0.0f;
-        const float cc = c32[p];
-        float s = 6.0f * cur;
-        s = s - below;
-        s = s - above;
-        s = s - jm;
-        s = s - jp;
-        s = s - km;
-        s = s - kp;
-        const float r = h2inv * s - cc * cur;
-        if constexpr (sizeof(OT) == 4) out[p] = r;
-        else out[p] = f32_to_f64(r);
-        below = cur;
-        cur = above;
+        jvp32_store(out, p, jvp32_point(below, cur, above, jm, jp, km, kp, c32[p], h2inv));
     }
 }
 
