@@ -4,6 +4,7 @@
 // copy of the kernels it launches.
 #pragma once
 
+#include <type_traits>
 #include "numa_internal.hpp"
 
 namespace numa::gpu {
@@ -611,8 +612,11 @@ struct TailParams {
     int half;                    // split geometry of level lb (SPLIT_IO)
 };
 
-template <class T>
-__device__ void tail_pass(T* __restrict__ x, const T* __restrict__ bs, int n, int c, bool first) {
+// NC > 0: the level's n as a compile-time constant (the index divisions become multiplications);
+// 0: the runtime n_rt.
+template <class T, int NC>
+__device__ void tail_pass(T* __restrict__ x, const T* __restrict__ bs, int n_rt, int c, bool first) {
+    const int n = NC ? NC : n_rt;
     const int np = (n + 1) / 2, total = n * n * np, P = n * n;
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
         const int kk = t % np, row = t / np, j = row % n, i = row / n;
@@ -637,8 +641,10 @@ __device__ void tail_pass(T* __restrict__ x, const T* __restrict__ bs, int n, in
     __syncthreads();
 }
 
-template <class T>
-__device__ void tail_residual(const T* __restrict__ x, const T* __restrict__ b, T* __restrict__ r, int n, T h2inv) {
+template <class T, int NC>
+__device__ void tail_residual(const T* __restrict__ x, const T* __restrict__ b, T* __restrict__ r, int n_rt,
+                              T h2inv) {
+    const int n = NC ? NC : n_rt;
     const int N = n * n * n, P = n * n;
     for (int p = threadIdx.x; p < N; p += blockDim.x) {
         const int k = p % n, j = (p / n) % n, i = p / P;
@@ -654,9 +660,10 @@ __device__ void tail_residual(const T* __restrict__ x, const T* __restrict__ b, 
     __syncthreads();
 }
 
-template <class T>
-__device__ void tail_restrict(const T* __restrict__ rf, T* __restrict__ bc, T* __restrict__ bsc, int nf, int nc,
-                              T inv_c) {
+template <class T, int NF>  // NF > 0: nf = NF and nc = (NF - 1) / 2 at compile time
+__device__ void tail_restrict(const T* __restrict__ rf, T* __restrict__ bc, T* __restrict__ bsc, int nf_rt,
+                              int nc_rt, T inv_c) {
+    const int nf = NF ? NF : nf_rt, nc = NF ? (NF - 1) / 2 : nc_rt;
     const int Nc = nc * nc * nc;
     const T w[3] = {T(0.25), T(0.5), T(0.25)};
     for (int q = threadIdx.x; q < Nc; q += blockDim.x) {
@@ -682,8 +689,9 @@ __device__ void tail_restrict(const T* __restrict__ rf, T* __restrict__ bc, T* _
     __syncthreads();
 }
 
-template <class T>
-__device__ void tail_prolong(const T* __restrict__ xc, T* __restrict__ xf, int nc, int nf, bool colour0_only) {
+template <class T, int NF>  // NF > 0: nf = NF and nc = (NF - 1) / 2 at compile time
+__device__ void tail_prolong(const T* __restrict__ xc, T* __restrict__ xf, int nc_rt, int nf_rt, bool colour0_only) {
+    const int nf = NF ? NF : nf_rt, nc = NF ? (NF - 1) / 2 : nc_rt;
     const int Nf = nf * nf * nf;
     for (int p = threadIdx.x; p < Nf; p += blockDim.x) {
         const int k = p % nf, j = (p / nf) % nf, i = p / (nf * nf);
@@ -700,6 +708,17 @@ __device__ void tail_prolong(const T* __restrict__ xc, T* __restrict__ xf, int n
         xf[p] = xf[p] + acc;
     }
     __syncthreads();
+}
+
+// Calls f with n as a compile-time constant for the tail's usual sizes (odd chains 15, 7, 3), else
+// with 0 (runtime n).  A constant is used only where the next level is (n - 1) / 2.
+template <class F>
+__device__ __forceinline__ void with_tail_n(int n, int n_next, F&& f) {
+    const bool chain = n_next == (n - 1) / 2;
+    if (n == 15 && chain) f(std::integral_constant<int, 15>{});
+    else if (n == 7 && chain) f(std::integral_constant<int, 7>{});
+    else if (n == 3 && chain) f(std::integral_constant<int, 3>{});
+    else f(std::integral_constant<int, 0>{});
 }
 
 template <class T, bool SPLIT_IO>
@@ -731,16 +750,19 @@ __global__ void __launch_bounds__(1024) k_mg_tail(const T* __restrict__ b_g, con
     const int last = tp.levels - 1;
     for (int l = 0; l < last; ++l) {  // down: pre-smoothing, residual, restriction
         const int n = tp.n[l];
-        for (int sw = 0; sw < tp.pre; ++sw) {
-            tail_pass<T>(X[l], BS[l], n, 0, sw == 0);
-            tail_pass<T>(X[l], BS[l], n, 1, false);
-        }
-        if (tp.pre == 0) {
-            for (int p = threadIdx.x; p < n * n * n; p += blockDim.x) X[l][p] = zero<T>();
-            __syncthreads();
-        }
-        tail_residual<T>(X[l], B[l], R, n, (T)tp.h2inv[l]);
-        tail_restrict<T>(R, B[l + 1], BS[l + 1], n, tp.n[l + 1], (T)tp.inv[l + 1]);
+        with_tail_n(n, tp.n[l + 1], [&](auto nc) {
+            constexpr int NC = decltype(nc)::value;
+            for (int sw = 0; sw < tp.pre; ++sw) {
+                tail_pass<T, NC>(X[l], BS[l], n, 0, sw == 0);
+                tail_pass<T, NC>(X[l], BS[l], n, 1, false);
+            }
+            if (tp.pre == 0) {
+                for (int p = threadIdx.x; p < n * n * n; p += blockDim.x) X[l][p] = zero<T>();
+                __syncthreads();
+            }
+            tail_residual<T, NC>(X[l], B[l], R, n, (T)tp.h2inv[l]);
+            tail_restrict<T, NC>(R, B[l + 1], BS[l + 1], n, tp.n[l + 1], (T)tp.inv[l + 1]);
+        });
     }
     {  // coarsest
         const int n = tp.n[last];
@@ -750,18 +772,21 @@ __global__ void __launch_bounds__(1024) k_mg_tail(const T* __restrict__ b_g, con
         } else {
             for (int sw = 0; sw < 30; ++sw) {
                 const int c0 = (sw % 2 == 0) ? 0 : 1;
-                tail_pass<T>(X[last], BS[last], n, c0, sw == 0);
-                tail_pass<T>(X[last], BS[last], n, 1 - c0, false);
+                tail_pass<T, 0>(X[last], BS[last], n, c0, sw == 0);
+                tail_pass<T, 0>(X[last], BS[last], n, 1 - c0, false);
             }
         }
     }
     for (int l = last - 1; l >= 0; --l) {  // up: prolongation, post-smoothing
         const int n = tp.n[l];
-        tail_prolong<T>(X[l + 1], X[l], tp.n[l + 1], n, tp.post > 0);
-        for (int sw = 0; sw < tp.post; ++sw) {
-            tail_pass<T>(X[l], BS[l], n, 1, false);
-            tail_pass<T>(X[l], BS[l], n, 0, false);
-        }
+        with_tail_n(n, tp.n[l + 1], [&](auto nc) {
+            constexpr int NC = decltype(nc)::value;
+            tail_prolong<T, NC>(X[l + 1], X[l], tp.n[l + 1], n, tp.post > 0);
+            for (int sw = 0; sw < tp.post; ++sw) {
+                tail_pass<T, NC>(X[l], BS[l], n, 1, false);
+                tail_pass<T, NC>(X[l], BS[l], n, 0, false);
+            }
+        });
     }
     {
         const int n = tp.n[0], N = n * n * n;
