@@ -341,75 +341,79 @@ inline void launch_pass_split(float* x, const float* bs, double* z, const Split&
 
 // r (natural layout) = b - h^-2 (6x - sum of neighbours) with x and b split: the order of
 // k_residual (6x, then - i-1, - i+1, - j-1, - j+1, - k-1, - k+1).  A thread owns the k-pair
-// {2kk, 2kk+1} of row j (colours cA and 1 - cA) and marches over ICH planes; as in k_pass_split the
-// padded arrays let every load be issued unconditionally, and selects replace the neighbours
-// outside the grid by +0.0.
-template <int ICH>
+// {2kk, 2kk+1} of row j (colours cA and 1 - cA) in the two planes {i0, i0 + 1}; the i-neighbours
+// inside the pair come from the other plane's registers (x(i0 + 1) is plane 1's own x, x(i0)
+// plane 0's).  As in k_pass_split the padded arrays let every load be issued unconditionally (a
+// plane past the grid reads plane 0's addresses), and selects replace the neighbours outside the
+// grid by +0.0.
+__device__ __forceinline__ void residual_pair(float* __restrict__ r, int LA, bool hasB, bool ilo, bool ihi, bool jlo,
+                                              bool jhi, bool kloA, bool khiB, float xa, float xb, float ba, float bb,
+                                              float a_im, float a_ip, float a_jm, float a_jp, float a_km, float b_im,
+                                              float b_ip, float b_jm, float b_jp, float b_kp, float h2inv) {
+    const float xbv = hasB ? xb : 0.0f;
+    {
+        float t = 6.0f * xa;
+        t = t - (ilo ? a_im : 0.0f);
+        t = t - (ihi ? a_ip : 0.0f);
+        t = t - (jlo ? a_jm : 0.0f);
+        t = t - (jhi ? a_jp : 0.0f);
+        t = t - (kloA ? a_km : 0.0f);
+        t = t - xbv;
+        r[LA] = ba - h2inv * t;
+    }
+    if (hasB) {
+        float t = 6.0f * xbv;
+        t = t - (ilo ? b_im : 0.0f);
+        t = t - (ihi ? b_ip : 0.0f);
+        t = t - (jlo ? b_jm : 0.0f);
+        t = t - (jhi ? b_jp : 0.0f);
+        t = t - xa;
+        t = t - (khiB ? b_kp : 0.0f);
+        r[LA + 1] = bb - h2inv * t;
+    }
+}
+
 __global__ void __launch_bounds__(BX* BY) k_residual_split(const float* __restrict__ x, const float* __restrict__ b,
-                                                           float* __restrict__ r, Split g, float h2inv) {
+                                                            float* __restrict__ r, Split g, float h2inv) {
     pdl_wait();
     pdl_trigger();
     const int kk = blockIdx.x * BX + threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
     const int n = g.n;
     if (j >= n || 2 * kk >= n) return;
-    const int i0 = blockIdx.z * ICH;
+    const int i0 = blockIdx.z * 2;
     const int P = n * n;
     const bool jlo = j > 0, jhi = j + 1 < n, hasB = 2 * kk + 1 < n, kloA = kk > 0, khiB = 2 * kk + 2 < n;
+    const bool two = i0 + 1 < n;
     const int LA0 = (i0 * n + j) * n + 2 * kk;
-    float xa[ICH], xb[ICH], ba[ICH], bb[ICH];
-    float a_im[ICH], a_ip[ICH], a_jm[ICH], a_jp[ICH], a_km[ICH];
-    float b_im[ICH], b_ip[ICH], b_jm[ICH], b_jp[ICH], b_kp[ICH];
-#pragma unroll
-    for (int s = 0; s < ICH; ++s) {
-        const int cA = (i0 + s + j) & 1, cB = cA ^ 1;
-        const int LA = (i0 + s < n) ? LA0 + s * P : 0;  // planes past the grid load harmlessly
-        const int mA = LA >> 1, mB = (LA + 1) >> 1;
-        const float* ownA = x + (cA ? g.half : 0);  // colour cA = B's other colour
-        const float* othA = x + (cA ? 0 : g.half);  // colour cB = A's other colour
-        xa[s] = ownA[mA];
-        xb[s] = othA[mA + cA];
-        ba[s] = b[(cA ? g.half : 0) + mA];
-        bb[s] = b[(cB ? g.half : 0) + mB];
-        a_im[s] = othA[mA + cA - g.hP - 1];
-        a_ip[s] = othA[mA + cA + g.hP];
-        a_jm[s] = othA[mA + cA - g.hn - 1];
-        a_jp[s] = othA[mA + cA + g.hn];
-        a_km[s] = othA[mA + cA - 1];
-        b_im[s] = ownA[mB + cB - g.hP - 1];
-        b_ip[s] = ownA[mB + cB + g.hP];
-        b_jm[s] = ownA[mB + cB - g.hn - 1];
-        b_jp[s] = ownA[mB + cB + g.hn];
-        b_kp[s] = ownA[mB + cB];
-    }
-#pragma unroll
-    for (int s = 0; s < ICH; ++s) {
-        const int i = i0 + s;
-        if (i >= n) break;
-        const bool ilo = i > 0, ihi = i + 1 < n;
-        const int LA = LA0 + s * P;
-        const float xbv = hasB ? xb[s] : 0.0f;
-        {
-            float t = 6.0f * xa[s];
-            t = t - (ilo ? a_im[s] : 0.0f);
-            t = t - (ihi ? a_ip[s] : 0.0f);
-            t = t - (jlo ? a_jm[s] : 0.0f);
-            t = t - (jhi ? a_jp[s] : 0.0f);
-            t = t - (kloA ? a_km[s] : 0.0f);
-            t = t - xbv;
-            r[LA] = ba[s] - h2inv * t;
-        }
-        if (hasB) {
-            float t = 6.0f * xbv;
-            t = t - (ilo ? b_im[s] : 0.0f);
-            t = t - (ihi ? b_ip[s] : 0.0f);
-            t = t - (jlo ? b_jm[s] : 0.0f);
-            t = t - (jhi ? b_jp[s] : 0.0f);
-            t = t - xa[s];
-            t = t - (khiB ? b_kp[s] : 0.0f);
-            r[LA + 1] = bb[s] - h2inv * t;
-        }
-    }
+    const int LA1 = two ? LA0 + P : 0;  // a plane past the grid loads harmlessly
+    // plane 0
+    const int cA0 = (i0 + j) & 1, cB0 = cA0 ^ 1;
+    const int mA0 = LA0 >> 1, mB0 = (LA0 + 1) >> 1;
+    const float* own0 = x + (cA0 ? g.half : 0);
+    const float* oth0 = x + (cA0 ? 0 : g.half);
+    const float xa0 = own0[mA0], xb0 = oth0[mA0 + cA0];
+    const float ba0 = b[(cA0 ? g.half : 0) + mA0], bb0 = b[(cB0 ? g.half : 0) + mB0];
+    const float a_im0 = oth0[mA0 + cA0 - g.hP - 1], a_jm0 = oth0[mA0 + cA0 - g.hn - 1], a_jp0 = oth0[mA0 + cA0 + g.hn];
+    const float a_km0 = oth0[mA0 + cA0 - 1];
+    const float b_im0 = own0[mB0 + cB0 - g.hP - 1], b_jm0 = own0[mB0 + cB0 - g.hn - 1], b_jp0 = own0[mB0 + cB0 + g.hn];
+    const float b_kp0 = own0[mB0 + cB0];
+    // plane 1 (colours swapped)
+    const int cA1 = cB0, cB1 = cA0;
+    const int mA1 = LA1 >> 1, mB1 = (LA1 + 1) >> 1;
+    const float* own1 = x + (cA1 ? g.half : 0);
+    const float* oth1 = x + (cA1 ? 0 : g.half);
+    const float xa1 = own1[mA1], xb1 = oth1[mA1 + cA1];
+    const float ba1 = b[(cA1 ? g.half : 0) + mA1], bb1 = b[(cB1 ? g.half : 0) + mB1];
+    const float a_ip1 = oth1[mA1 + cA1 + g.hP], a_jm1 = oth1[mA1 + cA1 - g.hn - 1], a_jp1 = oth1[mA1 + cA1 + g.hn];
+    const float a_km1 = oth1[mA1 + cA1 - 1];
+    const float b_ip1 = own1[mB1 + cB1 + g.hP], b_jm1 = own1[mB1 + cB1 - g.hn - 1], b_jp1 = own1[mB1 + cB1 + g.hn];
+    const float b_kp1 = own1[mB1 + cB1];
+    residual_pair(r, LA0, hasB, i0 > 0, two, jlo, jhi, kloA, khiB, xa0, xb0, ba0, bb0, a_im0, xa1, a_jm0, a_jp0, a_km0,
+                  b_im0, xb1, b_jm0, b_jp0, b_kp0, h2inv);
+    if (two)
+        residual_pair(r, LA1, hasB, true, i0 + 2 < n, jlo, jhi, kloA, khiB, xa1, xb1, ba1, bb1, xa0, a_ip1, a_jm1,
+                      a_jp1, a_km1, xb0, b_ip1, b_jm1, b_jp1, b_kp1, h2inv);
 }
 
 // Restriction from a natural-layout fine residual into a split coarse level (odd nc): the

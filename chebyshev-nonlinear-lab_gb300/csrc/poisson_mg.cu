@@ -333,9 +333,10 @@ void PoissonMG::cycle32(size_t l) {
     const int nc = C.n;
     const bool csplit = (nc & 1) != 0;
     {
-        // one plane a thread: 31 registers and full occupancy (a four-plane march took 80)
-        const dim3 rgd(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n);
-        launch_pdl(k_residual_split<1>, rgd, blk, 0, s, x, b, r, g, (float)L.h2inv);
+        // two planes a thread sharing their i-neighbours (a four-plane march without the sharing took 80
+        // registers)
+        const dim3 rgd(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, (n + 1) / 2);
+        launch_pdl(k_residual_split, rgd, blk, 0, s, x, b, r, g, (float)L.h2inv);
         ctx_.count_launch();
     }
     const Split gc = make_split(nc);
