@@ -327,7 +327,10 @@ int numa_gpu_burgers2d_solve(numa_gpu_burgers2d* op, int method, numa_gpu_vec* x
 
 /* One call from host buffers to host buffers: Bratu3D(n, lambda), provider of precond_kind
  * (MG with pre = post = 2 and mg_precision), method of numa_gpu_method, x0[n^3] -> x_out[n^3].
- * The shape of apps/smoke_bratu.cpp:125-148 and apps/run_campaign.cpp:344-390. */
+ * The shape of apps/smoke_bratu.cpp:125-148 and apps/run_campaign.cpp:344-390.  With
+ * NUMA_GPU_METHOD_NK and page-locked buffers the transfers overlap the solve: a pinned x0 goes up
+ * in plane pieces under the first residual evaluation, and the iterate predicted to be the last is
+ * copied to a pinned x_out while its residual is evaluated.  Results do not depend on it. */
 int numa_gpu_solve_bratu3d_host(numa_gpu_ctx* ctx, size_t n, double lambda, int method,
                                 int precond_kind, int mg_precision, const numa_krylov_params* p,
                                 const double* x0, double* x_out, numa_krylov_result* result);
