@@ -2,25 +2,32 @@
 """Bratu3D 255^3 time to ||F||/||F0|| <= 1e-10 on one GB300 (the path's headline metric).
 
 One step = one full Newton-Krylov solve of -Lap_h u - lambda e^u = 0 on the 255^3 interior grid
-(16,581,375 unknowns), lambda = 6, u0 = 0, GMRES(30) right-preconditioned by the geometric
-multigrid V(2,2) on 8 levels, Eisenstat-Walker forcing, rtol 1e-10 — through the library's C ABI
-with every vector resident in HBM.  Inputs are synthetic and deterministic (u0 = 0).
+(16,581,375 unknowns), lambda = 6, u0 = 0, Eisenstat-Walker forcing, rtol 1e-10, multigrid
+V(2,2) on the full 8-level hierarchy, through the library's C ABI with every vector resident in
+HBM.  Inputs are synthetic and deterministic (u0 = 0).
 
     python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--path fp64|mixed]
 
-Printed JSON line: value = seconds per solve of the headline path (the mixed path by default:
-FP32 V-cycle and FP32 Jacobian products inside FGMRES, FP64 residual and outer iteration; --path
-fp64 makes the plain FP64 drop-in the headline), e2e = the same through
-numa_gpu_solve_bratu3d_host with pinned host buffers (host to device copy of u0 and device to
-host copy of the solution inside the timed region), mixed_vs_plain = the other path timed in the
-same run with the error between the two solutions, roofline = the V-cycle's dominant kernel (the
-finest colour pass), cpu_baseline = the oracle port (the reference's algorithm restated in C++
-with the reference's OpenMP layout) on the host cores.
+Paths.  mixed (the headline, default): flexible GMRES(30) whose cycles run to 30 steps, classical
+Gram-Schmidt (one pass by default, --orth cgs2 for two) on lazily normalised basis vectors (an
+FP32 basis in double-FP32 arithmetic while the forcing term is >= 1e-5), FP32 V-cycle and FP32
+Jacobian products; FP64 residual, Newton update, Arnoldi coefficients and Hessenberg least
+squares.  fp64 (the drop-in): the reference's right-preconditioned GMRES(30) with modified
+Gram-Schmidt, FP64 V-cycle and FP64 Jacobian products.
 
---impl reference times the reference's CPU implementation of the same solve (the oracle port:
-the reference's own build cannot travel to the GPU host) on all host cores; each step is a
-127^3 solve whose time is scaled by N(255)/N(127) (the work of every primitive is linear in N
-and the counts are mesh-independent: 5 Newton steps, 12 JVPs, 17 V-cycles at 31^3 ... 255^3).
+Printed JSON line: value = seconds per solve of the headline path (CUDA events, vectors resident),
+e2e = the same through numa_gpu_solve_bratu3d_host with pinned host buffers (host to device copy
+of u0 and device to host copy of the solution inside the timed region), e2e_fp64 = the plain FP64
+drop-in through the same call, mixed_vs_plain = the other path timed in the same run with the
+error between the two solutions, roofline = the dominant kernel (the residual evaluation, with its
+HBM and FP64-pipe fractions) beside the V-cycle's colour pass, cpu_baseline = the reference's
+algorithm on the host cores at 255^3 itself (all cores and one thread).
+
+--impl reference times the reference's CPU implementation of the same 255^3 solve on all host
+cores: the reference's own build where it was compiled (oracle/_ref), else the oracle port (the
+reference's algorithm restated in C++ with the reference's OpenMP layout), W warm-up and K timed
+solves (fewer if they would not end within --ref-budget seconds; the line then says so), plus one
+single-thread solve.
 
 Multi-GPU: the path does not shard across GPUs (replicas only): with N ranks each GPU solves its
 own instance; value is the max over ranks of the time per step.
@@ -66,9 +73,13 @@ def parse_args(argv=None):
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-solves leg")
     ap.add_argument("--no-brusselator", action="store_true", help="skip the 2D Brusselator leg")
-    ap.add_argument("--cpu-sample-n", type=int, default=127)
-    ap.add_argument("--cpu-reps", type=int, default=2)
-    ap.add_argument("--kernel-case", choices=["none", "vcycle", "solve", "conv", "bruss", "stencils"], default="none",
+    ap.add_argument("--orth", choices=["cgs1", "cgs2"], default="cgs1",
+                    help="Gram-Schmidt form of the mixed path's FGMRES")
+    ap.add_argument("--cpu-reps", type=int, default=2, help="all-core CPU solves of the cpu_baseline leg")
+    ap.add_argument("--ref-budget", type=float, default=270.0,
+                    help="seconds the reference arm may spend on its warm-up and timed solves")
+    ap.add_argument("--kernel-case", choices=["none", "vcycle", "solve", "conv", "bruss", "stencils", "eval"],
+                    default="none",
                     help="profiling driver: run only this small case (for ncu)")
     return ap.parse_args(argv)
 
@@ -197,75 +208,138 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-# ------------------------------------------------------------------ CPU side (oracle port)
-def cpu_solve_time(n: int, lam: float, method: str, reps: int) -> tuple[float, int, dict]:
-    """Median seconds of `reps` oracle-port solves at n^3 on all host threads."""
-    from oracle.oracle_lib import Oracle, default_params
-    o = Oracle()
+# ------------------------------------------------------------------ CPU side (the reference's algorithm)
+def cpu_solver():
+    """(solve function, kind, Oracle for thread control): the reference's own build where it was
+    compiled here (oracle/_ref), else the oracle port."""
+    from oracle.oracle_lib import Oracle
+    port = Oracle()
+    ref = None
+    try:
+        ref = Oracle.reference()
+    except OSError:
+        ref = None
+    if ref is not None:
+        return ref.solve, "reference", port
+    return port.solve, "port", port
+
+
+def cpu_params():
+    from oracle.oracle_lib import default_params
+    return default_params(rtol_nl=1e-10, gmres_restart=30)
+
+
+def cpu_solve_times(n: int, lam: float, method: str, reps: int) -> dict:
+    """Median seconds of `reps` solves at n^3 on all host cores and of one single-thread solve."""
+    solve, kind, ctl = cpu_solver()
     cores = os.cpu_count() or 1
-    o.set_threads(cores)
-    p = default_params(rtol_nl=1e-10, gmres_restart=30)
-    times, res = [], {}
-    for _ in range(reps):
-        t0 = time.perf_counter()
-        _, res = o.solve(n, lam, method, "mg", p)
-        times.append(time.perf_counter() - t0)
-    return float(np.median(times)), cores, res
+    p = cpu_params()
+    out = {"kind": kind, "cores": cores}
+    for threads, r in ((cores, reps), (1, 1)):
+        ctl.set_threads(threads)
+        times, res = [], {}
+        for _ in range(r):
+            t0 = time.perf_counter()
+            _, res = solve(n, lam, method, "mg", p)
+            times.append(time.perf_counter() - t0)
+        out[threads] = (float(np.median(times)), len(times), res)
+    ctl.set_threads(cores)
+    return out
+
+
+def host_cpu_model() -> str:
+    try:
+        for line in subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.TimeoutExpired):
+        pass
+    return "unknown"
 
 
 def run_reference(args) -> int:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0  # replicas of the CPU reference are not run: rank 0 alone reports
-    n_s = args.cpu_sample_n
-    scale = (args.n ** 3) / (n_s ** 3)
-    from oracle.oracle_lib import Oracle, default_params
-    o = Oracle()
+    solve, kind, ctl = cpu_solver()
     cores = os.cpu_count() or 1
-    o.set_threads(cores)
-    p = default_params(rtol_nl=1e-10, gmres_restart=30)
+    ctl.set_threads(cores)
+    p = cpu_params()
+    n = args.n
+    t_start = time.perf_counter()
+    times, res = [], {}
+    warm_done = 0
     for _ in range(args.warmup):
-        o.solve(n_s, args.lam, args.method, "mg", p)
-    times = []
-    res = {}
-    for _ in range(args.steps):
         t0 = time.perf_counter()
-        _, res = o.solve(n_s, args.lam, args.method, "mg", p)
+        solve(n, args.lam, args.method, "mg", p)
+        times.append(time.perf_counter() - t0)  # the first solve sizes the budget
+        warm_done += 1
+        if (time.perf_counter() - t_start) + times[0] * (args.steps + 1) > args.ref_budget:
+            break
+    times = []
+    for _ in range(args.steps):
+        if times and (time.perf_counter() - t_start) + float(np.mean(times)) > args.ref_budget:
+            break
+        t0 = time.perf_counter()
+        _, res = solve(n, args.lam, args.method, "mg", p)
         times.append(time.perf_counter() - t0)
-    per = float(np.mean(times)) * scale
-    sample = (f"{args.method} solve at {n_s}^3 (lambda={args.lam}, rtol 1e-10, GMRES(30), MG V(2,2)) per step, "
-              f"mean of {args.steps}, scaled by N({args.n})/N({n_s}) = {scale:.4f}; counts "
-              f"{res.get('iters')}/{res.get('n_JVP')}/{res.get('n_prec')} (iters/JVP/prec)")
+    per = float(np.mean(times))
+    ctl.set_threads(1)
+    t0 = time.perf_counter()
+    _, res1 = solve(n, args.lam, args.method, "mg", p)
+    one = time.perf_counter() - t0
+    ctl.set_threads(cores)
+    sample = (f"{args.method} solve at {n}^3 itself (lambda={args.lam}, u0 = 0, rtol 1e-10, GMRES(30), MG V(2,2)), "
+              f"{warm_done} warm-up and {len(times)} timed solves on {cores} threads ({host_cpu_model()}), mean; "
+              f"counts {res.get('iters')}/{res.get('n_JVP')}/{res.get('n_prec')} (iters/JVP/prec); "
+              f"{'the reference built from its own headers' if kind == 'reference' else 'the oracle port (the reference build cannot travel to this host)'}")
     line = {
-        "impl": "reference", "metric": METRIC, "value": per, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (u0 = 0)",
-        "config": workload_config(args, "fp64"),
-        "cpu_baseline": {"value": per, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
+        "impl": "reference", "metric": METRIC, "value": per, "unit": "s", "n_gpus": args.gpus,
+        "steps": len(times), "warmup": warm_done, "ms_per_step": per * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (u0 = 0)",
+        "config": workload_config(args, "fp64", None),
+        "cpu_baseline": {"value": per, "unit": "s", "cores": cores, "kind": kind, "sample": sample,
+                         "single_thread": {"value": one, "unit": "s", "cores": 1,
+                                           "counts": [res1.get("iters"), res1.get("n_JVP"), res1.get("n_prec")]}},
         "e2e": {"value": per, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if len(times) < args.steps or warm_done < args.warmup:
+        line["steps_requested"] = args.steps
+        line["warmup_requested"] = args.warmup
+        line["note"] = f"solves capped by --ref-budget {args.ref_budget:.0f} s"
     print(json.dumps(line), flush=True)
     return 0
 
 
-def workload_config(args, path: str) -> dict:
+def workload_config(args, path: str, levels: int | None) -> dict:
+    lv = f"{levels} levels" if levels else "the full hierarchy"
+    if path == "mixed":
+        orth = "two-pass (CGS2)" if args.orth == "cgs2" else "one-pass (CGS1)"
+        solver = (f"FGMRES(30) (cycles up to 30 steps; {orth} classical Gram-Schmidt on lazily normalised basis "
+                  f"vectors, FP32 basis in double-FP32 arithmetic while the forcing term is >= 1e-5) right-"
+                  f"preconditioned by the FP32 GMG V(2,2) ({lv}), FP32 Jacobian products; FP64 residual, Newton "
+                  f"update, Arnoldi coefficients and least squares")
+    else:
+        solver = (f"GMRES(30) with modified Gram-Schmidt (the reference's) right-preconditioned by the FP64 GMG "
+                  f"V(2,2) ({lv}), FP64 Jacobian products")
     return {
-        "workload": f"Bratu3D {args.n}^3 lambda={args.lam} u0=0, {args.method.upper()} + GMRES(30) right-preconditioned "
-                    f"by GMG V(2,2) (8 levels), Eisenstat-Walker forcing, stop at ||F||/||F0|| <= 1e-10",
+        "workload": f"Bratu3D {args.n}^3 lambda={args.lam} u0=0, {args.method.upper()} (Eisenstat-Walker forcing) + "
+                    f"{solver}, stop at ||F||/||F0|| <= 1e-10",
         "n": args.n, "unknowns": args.n ** 3, "lambda": args.lam, "method": args.method, "path": path,
-        "precond": "PoissonMG V(2,2) red-black Gauss-Seidel", "gmres_restart": 30, "rtol_nl": 1e-10,
+        "precond": f"PoissonMG V(2,2) red-black Gauss-Seidel, {lv}", "gmres_restart": 30, "rtol_nl": 1e-10,
+        "orth": args.orth if path == "mixed" else "mgs",
         "jvp": "analytic (Bratu3D::jvp)",
         "l2": "inputs larger than L2: one vector is 133 MB and the solve's working set ~6 GB vs 129 MB L2",
     }
 
 
 # ------------------------------------------------------------------ our arm
-def params_for(G, path: str):
+def params_for(G, path: str, orth: str = "cgs1"):
     p = G.default_params(rtol_nl=1e-10, gmres_restart=30)
     if path == "mixed":
         p.flexible = 1
         p.jvp_precision = G.FP32
-        p.orth = G.CGS1
+        p.orth = G.CGS2 if orth == "cgs2" else G.CGS1
     return p
 
 
@@ -312,7 +386,10 @@ def run_ours(args) -> int:
     u0 = ctx.vec(N).fill(0.0)
     x = ctx.vec(N)
 
-    heads = {"fp64": (pc64, params_for(G, "fp64")), "mixed": (pc32, params_for(G, "mixed"))}
+    heads = {"fp64": (pc64, params_for(G, "fp64")), "mixed": (pc32, params_for(G, "mixed", args.orth))}
+    mg_probe = G.PoissonMG(ctx, n)
+    levels = mg_probe.levels()
+    mg_probe.close()
     pc, prm = heads[args.path]
     with ClockSampler(dev) as clk:
         sec, res, launches = timed_solves(G, ctx, op, pc, x, u0, args.method, prm, args.steps, args.warmup, dist,
@@ -329,7 +406,8 @@ def run_ours(args) -> int:
     # the inexact Chebyshev method (chebyshev_inexact, two linear solves and F'' per step) on both paths
     sec_c64, res_c64, _ = timed_solves(G, ctx, op, pc64, x, u0, "cheb", params_for(G, "fp64"), 2, 1, dist, stream)
     x_c64 = x.numpy() if dist.rank == 0 else None
-    sec_c32, res_c32, _ = timed_solves(G, ctx, op, pc32, x, u0, "cheb", params_for(G, "mixed"), 2, 1, dist, stream)
+    sec_c32, res_c32, _ = timed_solves(G, ctx, op, pc32, x, u0, "cheb", params_for(G, "mixed", args.orth), 2, 1, dist,
+                                       stream)
     x_c32 = x.numpy() if dist.rank == 0 else None
     ckeys = ("iters", "n_F", "n_JVP", "n_D2", "n_lin_iters", "n_prec", "converged")
     cheb = {"plain_fp64_s": sec_c64, "mixed_s": sec_c32, "ratio": sec_c64 / sec_c32,
@@ -349,7 +427,7 @@ def run_ours(args) -> int:
             trep = net.train(n, instances=4, states=3, rhs_per_state=2, krylov_per_state=8, epochs=8, batch=4,
                              lr=2e-3, seed=11)
             pcl = G.Provider.learned(ctx, n, net, stall=0.9)
-            sec_l, res_l, _ = timed_solves(G, ctx, op, pcl, x, u0, args.method, params_for(G, "mixed"),
+            sec_l, res_l, _ = timed_solves(G, ctx, op, pcl, x, u0, args.method, params_for(G, "mixed", args.orth),
                                            max(1, args.steps // 2), 1, dist, stream)
             x_l = x.numpy() if dist.rank == 0 else None
             applies, fallbacks = pcl.learned_stats()
@@ -361,9 +439,8 @@ def run_ours(args) -> int:
     # batched solves: 128 instances, n from {31, 63, 127}, lambda ~ U[1, 6.5] (seeded), mixed path
     batched = None
     if not args.no_batch and dist.rank == 0:
-        rng = np.random.default_rng(42)
-        inst = [(int(nn), float(lm)) for nn, lm in zip(rng.choice([31, 63, 127], 128), rng.uniform(1.0, 6.5, 128))]
-        pb = params_for(G, "mixed")
+        inst = G.batch_config_instances(128, seed=42)
+        pb = params_for(G, "mixed", args.orth)
         ex = G.BatchExecutor(workers=32, device=dev)
         # the schedule (concurrent workers, each with its own stream) is autotuned on this batch
         chosen, tune = ex.autotune(inst, (4, 8, 16, 24, 32), "nk", G.FP32, pb)
@@ -377,7 +454,9 @@ def run_ours(args) -> int:
             "autotune_s": tune,
             "one_worker_solves_per_s": len(inst) / wall1,
             "all_converged": all(r["converged"] == 1 for r in rb),
-            "iters_range": [min(r["iters"] for r in rb), max(r["iters"] for r in rb)],
+            "per_instance": {"n": [nn for nn, _ in inst], "lambda": [round(lm, 6) for _, lm in inst],
+                             "iters": [r["iters"] for r in rb], "n_JVP": [r["n_JVP"] for r in rb],
+                             "n_prec": [r["n_prec"] for r in rb], "converged": [r["converged"] for r in rb]},
             "lin_iters_total": sum(r["n_lin_iters"] for r in rb),
             "note": "mixed NK (FGMRES(30), FP32 V-cycle and J v), u0 = 0, rtol 1e-10; host workers with one "
                     "stream each, operators, hierarchies and workspaces kept between batches; the worker count is "
@@ -391,22 +470,28 @@ def run_ours(args) -> int:
     if not args.no_brusselator and dist.rank == 0:
         bruss = brusselator_leg(G, ctx, stream, torch)
 
-    # end to end through the host-buffer entry point, pinned buffers
+    # end to end through the host-buffer entry point, pinned buffers: the headline path, then the
+    # plain FP64 drop-in through the same call
     h_in = torch.zeros(N, dtype=torch.float64, pin_memory=True).numpy()
     h_out = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
     mgp = G.FP64 if args.path == "fp64" else G.FP32
-    for _ in range(2):  # warm: allocations, the host entry's operator, hierarchy and captured graphs
-        G.solve_bratu3d_host(ctx, n, args.lam, h_in, h_out, args.method, "mg", mgp, prm)
-    e2e_steps = max(1, args.steps)
-    dist.barrier()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with quiet_gc():
-        ev0.record(stream)
-        for _ in range(e2e_steps):
-            G.solve_bratu3d_host(ctx, n, args.lam, h_in, h_out, args.method, "mg", mgp, prm)
-        ev1.record(stream)
-        ev1.synchronize()
-    e2e_sec = dist.max(ev0.elapsed_time(ev1) * 1e-3 / e2e_steps)
+
+    def e2e_leg(mg_prec, prm_e, steps):
+        for _ in range(2):  # warm: allocations, the host entry's operator, hierarchy and captured graphs
+            G.solve_bratu3d_host(ctx, n, args.lam, h_in, h_out, args.method, "mg", mg_prec, prm_e)
+        dist.barrier()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with quiet_gc():
+            ev0.record(stream)
+            for _ in range(steps):
+                G.solve_bratu3d_host(ctx, n, args.lam, h_in, h_out, args.method, "mg", mg_prec, prm_e)
+            ev1.record(stream)
+            ev1.synchronize()
+        return dist.max(ev0.elapsed_time(ev1) * 1e-3 / steps), h_out.copy()
+
+    e2e_sec, x_e2e = e2e_leg(mgp, prm, max(1, args.steps))
+    other_mgp = G.FP32 if mgp == G.FP64 else G.FP64
+    e2e_other, _ = e2e_leg(other_mgp, prmo, max(1, args.steps // 2))
 
     # per-primitive breakdown of one solve of each path (CUDA-event timers inside the library)
     breakdown = {}
@@ -417,7 +502,11 @@ def run_ours(args) -> int:
         ctx.set_timing(False)
         breakdown[name] = {k: rb[k] for k in ("t_F", "t_JVP", "t_prec", "t_setup_dynamic", "t_total")}
 
-    # roofline of the dominant kernel: the finest-level red-black colour pass
+    # roofline: the dominant kernel of the headline solve (the residual evaluation, FP64-pipe bound)
+    # and the V-cycle's dominant kernel (the finest-level red-black colour pass)
+    x.copy_from(u0)
+    G.solve(op, x, args.method, prm, pc)
+    ms_eval = op.time_eval(x, G.FP32 if mgp == G.FP32 else G.FP64, 20)
     mg_head = G.PoissonMG(ctx, n, precision=mgp)
     ms_pass = mg_head.time_smoother(20)
     fp64_peak = ctx.fp64_peak_tflops()
@@ -426,40 +515,53 @@ def run_ours(args) -> int:
     if dist.rank == 0:
         peaks = json.loads(PEAKS_FILE.read_text()) if PEAKS_FILE.exists() else {}
         hbm_peak = float(peaks.get("hbm_gbs", FALLBACK_HBM_GBS))
+        peak_source = "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback"
         eb = 8 if mgp == G.FP64 else 4
-        # algorithmic bytes of the dominant kernel, one red-black colour pass: the own-colour
-        # right-hand side (N/2) and the other-colour neighbours (N/2) read once, the own-colour
-        # values (N/2) written once
+        # the residual evaluation: algorithmic 16 B a point (u read, F written once); the drivers'
+        # cache adds c = lambda e^u (8 B) and, on the mixed path, RN32(c) and RN32(F) (4 + 4 B).
+        # FP64 instructions a point from ncu (k_eval_fp64_pipe_255.md): 15
+        eval_bytes = 16.0 * N
+        eval_moved = (32.0 if mgp == G.FP32 else 24.0) * N
+        eval_dp_per_pt = 15
+        ach_eval = eval_bytes / (ms_eval * 1e-3) / 1e9
+        dp_rate = eval_dp_per_pt * N / (ms_eval * 1e-3) / 1e12
+        # one red-black colour pass: the own-colour right-hand side (N/2) and the other-colour
+        # neighbours (N/2) read once, the own-colour values (N/2) written once
         pass_bytes = 3 * (N / 2) * eb
         achieved = pass_bytes / (ms_pass * 1e-3) / 1e9
-        # FP64 instructions of one pass: per updated point 6 adds + 3 for the division by 6
-        # (one multiply, two FMAs); the FP64 pipe issues one such instruction per lane-cycle,
-        # so its instruction peak is the measured FMA peak (2 flops each) / 2
-        pass_instr = 9 * (N / 2)
-        traffic = load_profile_traffic(mgp)
+        prof = load_profile(ROOT / "profiles" / ("k_eval_fp32cache_255.json" if mgp == G.FP32 else
+                                                 "k_eval_fp64cache_255.json"))
         roofline = {
-            "kernel": (f"k_rbgs<double> colour pass, {n}^3" if mgp == G.FP64 else
-                       f"k_pass_split colour pass (FP32, colour-split layout), {n}^3"),
-            "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-            "traffic": traffic, "ms_per_launch": ms_pass,
-            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback",
+            "kernel": f"k_eval (FP64 residual F, its norm and the drivers' cache), {n}^3",
+            "bound": "hbm", "achieved": ach_eval, "peak": hbm_peak, "unit": "GB/s", "frac": ach_eval / hbm_peak,
+            "traffic": prof.get("dram_bytes_per_launch"), "ms_per_launch": ms_eval,
+            "algorithmic_bytes": eval_bytes, "bytes_written_and_read": eval_moved,
+            "peak_source": peak_source,
+            "fp64_pipe": {
+                "achieved_tinstr_per_s": dp_rate, "peak_tinstr_per_s": fp64_peak / 2,
+                "peak_fma_tflops_measured": fp64_peak, "frac": dp_rate / (fp64_peak / 2),
+                "dp_instr_per_point": eval_dp_per_pt,
+                "note": "the bound that holds: FP64 arithmetic (e^u and the 7-point sum, 15 DP instructions a "
+                        "point) against the FMA-chain peak measured live; HBM would allow ~16x the rate",
+            },
+            "vcycle_colour_pass": {
+                "kernel": (f"k_rbgs<double> colour pass, {n}^3" if mgp == G.FP64 else
+                           f"k_pass_split colour pass (FP32, colour-split layout), {n}^3"),
+                "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "traffic": load_profile_traffic(mgp), "ms_per_launch": ms_pass, "algorithmic_bytes": pass_bytes,
+            },
         }
-        if mgp == G.FP64:
-            rate = pass_instr / (ms_pass * 1e-3) / 1e12
-            roofline["fp64_pipe"] = {
-                "achieved_tinstr_per_s": rate, "peak_tinstr_per_s": fp64_peak / 2,
-                "peak_fma_tflops_measured": fp64_peak, "frac": rate / (fp64_peak / 2),
-                "note": "FP64 arithmetic, not HBM, bounds the FP64 kernels on this GPU: DP instructions "
-                        "per second vs the FMA-chain peak measured live",
-            }
         cpu = None
         if not args.no_cpu_baseline:
-            t_cpu, cores, rcpu = cpu_solve_time(args.cpu_sample_n, args.lam, args.method, args.cpu_reps)
-            scale = N / args.cpu_sample_n ** 3
-            cpu = {"value": t_cpu * scale, "unit": "s", "cores": cores, "kind": "port",
-                   "sample": f"{args.method} solve at {args.cpu_sample_n}^3 (same lambda/rtol/GMRES/MG), median of "
-                             f"{args.cpu_reps}, scaled by N({n})/N({args.cpu_sample_n}) = {scale:.4f}; counts "
-                             f"{rcpu.get('iters')}/{rcpu.get('n_JVP')}/{rcpu.get('n_prec')}"}
+            ct = cpu_solve_times(n, args.lam, args.method, args.cpu_reps)
+            cores = ct["cores"]
+            t_all, reps_all, rcpu = ct[cores]
+            t_one, _, _ = ct[1]
+            cpu = {"value": t_all, "unit": "s", "cores": cores, "kind": ct["kind"],
+                   "sample": f"{args.method} solve at {n}^3 itself (same lambda / rtol / GMRES(30) / MG V(2,2), "
+                             f"plain FP64), median of {reps_all} on {cores} threads ({host_cpu_model()}); counts "
+                             f"{rcpu.get('iters')}/{rcpu.get('n_JVP')}/{rcpu.get('n_prec')}",
+                   "single_thread": {"value": t_one, "unit": "s", "cores": 1}}
         err = float(np.linalg.norm(x_other - x_head) / np.linalg.norm(x_head))
         fp64_sec = sec if args.path == "fp64" else sec_o
         mixed_sec = sec_o if args.path == "fp64" else sec
@@ -467,7 +569,7 @@ def run_ours(args) -> int:
             "metric": METRIC, "value": sec, "unit": "s", "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.path == "fp64" else "f64+f32",
-            "data": "synthetic (u0 = 0, deterministic)", "config": workload_config(args, args.path),
+            "data": "synthetic (u0 = 0, deterministic)", "config": workload_config(args, args.path, levels),
             "counts": {k: res[k] for k in ("iters", "n_F", "n_JVP", "n_D2", "n_lin_iters", "n_prec", "converged")},
             "res_rel": res["res"] / res["res0"],
             "mixed_vs_plain": {"plain_fp64_s": fp64_sec, "mixed_s": mixed_sec, "ratio": fp64_sec / mixed_sec,
@@ -482,7 +584,12 @@ def run_ours(args) -> int:
             "brusselator2d": bruss,
             "clocks": clk.summary(),
             "e2e": {"value": e2e_sec, "unit": "s", "h2d_bytes_per_step": N * 8, "d2h_bytes_per_step": N * 8,
-                    "api": "numa_gpu_solve_bratu3d_host, pinned host buffers"},
+                    "api": "numa_gpu_solve_bratu3d_host, pinned host buffers",
+                    "rel_err_vs_device_path": float(np.linalg.norm(x_e2e - x_head) / np.linalg.norm(x_head))},
+            ("e2e_mixed" if args.path == "fp64" else "e2e_fp64"): {
+                "value": e2e_other, "unit": "s", "h2d_bytes_per_step": N * 8, "d2h_bytes_per_step": N * 8,
+                "api": "numa_gpu_solve_bratu3d_host, pinned host buffers",
+                "path": "mixed" if args.path == "fp64" else "plain FP64 drop-in (GMRES(30) MGS, FP64 V-cycle)"},
             "gpu_launches": launches,
             "breakdown_s": breakdown,
             "roofline": roofline,
@@ -614,6 +721,14 @@ def learned_summary(learned, fp64_sec, x_fp64):
     }
 
 
+def load_profile(f: Path) -> dict:
+    """A committed ncu summary (JSON beside its .md), or {} when absent."""
+    try:
+        return json.loads(f.read_text()) if f.exists() else {}
+    except ValueError:
+        return {}
+
+
 def load_profile_traffic(mgp) -> float | None:
     """DRAM bytes per launch of the colour pass from the committed ncu summary, if present."""
     f = ROOT / "profiles" / ("k_rbgs_fp64_255.json" if mgp == 0 else "k_pass_split_fp32_255.json")
@@ -637,6 +752,14 @@ def run_kernel_case(G, ctx, args) -> int:
         for _ in range(max(1, args.steps)):
             G.diag_conv3d(ctx, nc, xin, w)
         print(json.dumps({"kernel_case": "conv", "n": nc, "launches": ctx.kernel_launches()}))
+        return 0
+    if args.kernel_case == "eval":
+        # the residual evaluation with the mixed path's cache, on a smooth iterate of the solve's size
+        op = G.Bratu3D(ctx, n, args.lam)
+        i = np.arange(N, dtype=np.float64)
+        xv = ctx.from_numpy(0.4 * np.sin(np.pi * (i % n + 1) / (n + 1)))
+        ms = op.time_eval(xv, G.FP32 if args.path == "mixed" else G.FP64, max(1, args.steps))
+        print(json.dumps({"kernel_case": "eval", "n": n, "ms_per_eval": ms, "launches": ctx.kernel_launches()}))
         return 0
     if args.kernel_case == "stencils":
         # the finite-difference and second-difference products of Bratu3D at n^3, and the 5-point

@@ -369,6 +369,27 @@ void Bratu3D::eval(const double* x, double* out, double* c_out, double* norm_out
     eval_launch(x, out, c_out, norm_out, m.grid, m.ichunk, 0, 0);
 }
 
+double Bratu3D::time_eval(const double* x, int precision, int reps) {
+    const bool keep = mixed_cache_;
+    prepare_cache(precision);
+    DeviceArray<double> out(N_), cache(cache_size());
+    double* nrm = ctx_.scalar(kSlotTmp0);
+    cudaEvent_t a, b;
+    NUMA_CUDA(cudaEventCreate(&a));
+    NUMA_CUDA(cudaEventCreate(&b));
+    eval(x, out.p, cache.p, nrm);
+    NUMA_CUDA(cudaEventRecord(a, ctx_.stream));
+    for (int r = 0; r < reps; ++r) eval(x, out.p, cache.p, nrm);
+    NUMA_CUDA(cudaEventRecord(b, ctx_.stream));
+    NUMA_CUDA(cudaEventSynchronize(b));
+    float ms = 0.f;
+    NUMA_CUDA(cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    mixed_cache_ = keep;
+    return reps > 0 ? ms / reps : 0.0;
+}
+
 // One launch of k_eval over the plane chunks [zoff, zoff + grid.z) (of ichunk planes each).
 void Bratu3D::eval_launch(const double* x, double* out, double* c_out, double* norm_out, dim3 grid, int ichunk,
                           int zoff, int norm_raw) {

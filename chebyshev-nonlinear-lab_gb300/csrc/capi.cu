@@ -157,19 +157,34 @@ struct CallbackPrec : Precond {
 };
 
 // Jacobian of a Bratu3D at a fixed point.
+// The Bratu3D Jacobian at a point as a linear operator: analytic (FP64), analytic in FP32 arithmetic
+// (bound as the mixed drivers bind it, with the FP32 product forms FGMRES uses), or by finite
+// differences.
 struct BratuJacOp : LinearOp {
     Bratu3D& f;
     int mode;
     const double *x, *c, *fx, *xnorm;
     BratuJacOp(Bratu3D& f_, int m) : f(f_), mode(m), x(nullptr), c(nullptr), fx(nullptr), xnorm(nullptr) {}
+    ~BratuJacOp() override {
+        if (mode == NUMA_GPU_DERIV_ANALYTIC_FP32) f.prepare_cache(NUMA_GPU_FP64);
+    }
     void apply(const double* v, double* out) override {
         if (mode == NUMA_GPU_DERIV_FD) f.jvp_fd(x, fx, xnorm, v, out);
+        else if (mode == NUMA_GPU_DERIV_ANALYTIC_FP32) f.jvp_bound(v, out);
         else f.jvp_c(c, v, out);
     }
+    bool has_apply32() const override { return mode == NUMA_GPU_DERIV_ANALYTIC_FP32 && f.has_jvp32(); }
+    void apply32(const float* v32, double* out) override { f.jvp_bound32(v32, out); }
+    bool has_apply32f() const override { return mode == NUMA_GPU_DERIV_ANALYTIC_FP32 && f.has_jvp32f(); }
+    void apply32f(const float* v32, float* out32) override { f.jvp_bound32f(v32, out32); }
 };
 struct ProviderPrec : Precond {
     Provider* p;
     void apply(const double* r, double* z) override { p->apply(r, z); }
+    bool has_apply32() const override { return p->has_apply32(); }
+    void apply32(const double* r, float* z32) override { p->apply32(r, z32); }
+    bool has_apply32f() const override { return p->has_apply32f(); }
+    void apply32f(const float* r32, float* z32) override { p->apply32f(r32, z32); }
 };
 
 // Checks a driver's vector and provider against an operator of size N.
@@ -772,6 +787,13 @@ static void bratu_jac_setup(numa_gpu_bratu3d* op, const numa_gpu_vec* xpt, int j
         dev_norm2(c, xpt->d, N, c.scalar(kSlotTmp1));
         J.fx = buf.p;
         J.xnorm = c.scalar(kSlotTmp1);
+    } else if (jvp_mode == NUMA_GPU_DERIV_ANALYTIC_FP32) {
+        // bound as the mixed drivers bind it: the cache of the evaluation at xpt (c, RN32(c), RN32(F))
+        f.prepare_cache(NUMA_GPU_FP32);
+        buf.resize(f.cache_size() + N);
+        f.eval(xpt->d, buf.p + f.cache_size(), buf.p, nullptr);
+        f.bind(xpt->d, buf.p, NUMA_GPU_FP32);
+        J.c = buf.p;
     } else {
         need(jvp_mode == NUMA_GPU_DERIV_ANALYTIC, NUMA_GPU_ERR_INVALID_ARGUMENT, "unknown derivative mode");
         buf.resize(N);
@@ -1703,6 +1725,16 @@ int numa_gpu_diag_time_bmg2d_pass(numa_gpu_bmg2d* mg, int reps, double* ms_per_p
 int numa_gpu_diag_time_smoother(numa_gpu_mg* mg, int reps, double* ms_per_pass) {
     if (!mg || !ms_per_pass || reps < 1) return NUMA_GPU_ERR_INVALID_ARGUMENT;
     return guard(mg->ctx, [&] { *ms_per_pass = mg->impl->time_finest_pass(reps); });
+}
+
+int numa_gpu_diag_time_eval(numa_gpu_bratu3d* op, const numa_gpu_vec* x, int precision, int reps, double* ms_per_eval) {
+    if (!op || !ms_per_eval || reps < 1) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    if (precision != NUMA_GPU_FP64 && precision != NUMA_GPU_FP32) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(op->ctx, [&] {
+        same_ctx(op->ctx, x);
+        sized(x, op->impl->size());
+        *ms_per_eval = op->impl->time_eval(x->d, precision, reps);
+    });
 }
 
 }  // extern "C"

@@ -401,12 +401,12 @@ enum ScalarSlot : int {
     kSlotFdInvH = 20,     // RN(1/h) and RN(1/h^2) for the quotients
     kSlotFdInvHH = 21,
     kSlotPieceSums = 24,  // sums of squares of an evaluation's pieces, 8 entries
-    kSlotGmresH = 64,     // Hessenberg column, m + 2 entries
-    kSlotGmresH2 = 320,   // CGS2 second-pass coefficients, up to 8
-    kSlotGmresY = 400,    // least-squares solution y, m entries
-    kSlotGmresCoef = 700, // recycled-solve coefficients, 2k + 1 entries
-    kSlotGmresSig2 = 1250, // lazily normalised basis: 1 / norm^2 of each vector, m + 1 entries
-    kSlotGmresSig = 1270,  // FP32 basis: 1 / norm of each vector, m + 1 entries
+    kSlotGmresH = 64,      // Hessenberg column, m + 2 entries (m <= kMaxRestart)
+    kSlotGmresH2 = 320,    // CGS2 second-pass coefficients, m + 1 entries
+    kSlotGmresY = 640,     // least-squares solution y, m entries
+    kSlotGmresCoef = 900,  // recycled-solve coefficients, 2k + 1 entries
+    kSlotGmresSig2 = 1408, // lazily normalised basis: 1 / norm^2 of each vector, m + 1 entries
+    kSlotGmresSig = 1664,  // FP32 basis: 1 / norm of each vector, m + 1 entries
 };
 
 // Pinned host staging for small vectors moving to the device.

@@ -10,7 +10,12 @@
 //    axpy w -= h_{i-1} V_{i-1} (one FMA) with the next inner product <w, V_i>; the last one fuses
 //    the final axpy with ||w||.  2(j+1)+1 FP64 operations per point, j+2 launches per step.
 //  * CGS2: h = V^T w; w -= V h fused with h' = V^T w; w -= V h' fused with ||w||; H = h + h'.
-//    Three passes over the basis, 4(j+1)+1 FP64 operations per point; for j+1 <= 16.
+//    Three passes over the basis, 4(j+1)+1 FP64 operations per point.
+//  * CGS1: h = V^T w; w -= V h fused with ||w|| (2j + 5 vector passes).
+// The fused classical Gram-Schmidt kernels keep one partial sum per basis vector in registers, for
+// at most kCgsBlock vectors a pass; a longer basis is taken in blocks (updates of the earlier
+// blocks chained through the output vector, dots of the earlier blocks after the last update),
+// so a cycle runs to the restart length the caller asked for.
 // On this GPU FP64 arithmetic, not bandwidth, bounds these kernels, so MGS is the cheaper of
 // the two; CGS2 issues fewer launches and is the better-conditioned choice.
 #include <algorithm>
@@ -22,7 +27,7 @@
 namespace numa::gpu {
 namespace {
 
-constexpr int kMaxCgs = 8;  // largest basis count of the fused classical Gram-Schmidt kernels
+constexpr int kCgsBlock = 8;  // basis vectors per fused classical Gram-Schmidt pass
 
 struct StoreAt {
     double* out;
@@ -73,9 +78,11 @@ __device__ __forceinline__ double widen(float v) { return f32_to_f64(v); }
 // partial sums stay in registers through the two-level reduction).  The vectors are v0 (r = 0) and
 // V + r ldv (r >= 1), so a first vector can live outside the basis array.
 // MODE 0: h[r] = <w, v_r>.
-// MODE 1: wout = w - sum_r hin[r] v_r, then h[r] = <wout, v_r>.
-// MODE 2: wout = w - sum_r hin[r] sig2[r] v_r (sig2 = 1 when null), then h[0] = ||wout|| and, when
-//         sig2_out is given, *sig2_out = 1 / ||wout||^2 (0 for a zero vector).
+// MODE 1: wout = w - sum_r hin[r] sig2[r] v_r (sig2 = 1 when null), then h[r] = <wout, v_r>.
+// MODE 2: the same wout, then h[0] = ||wout|| and, when sig2_out is given, *sig2_out = 1 / ||wout||^2
+//         (0 for a zero vector).
+// MODE 3: the same wout and no reduction (the earlier blocks of a basis longer than kCgsBlock).
+// w and wout may be the same array (each element is read before it is written, by one thread).
 template <int CNT, int MODE>
 __global__ void __launch_bounds__(kRedThreads) k_cgs(const double* w, const double* __restrict__ v0,
                                                      const double* __restrict__ V, size_t ldv,
@@ -102,27 +109,29 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs(const double* w, const doub
         }
         if (MODE == 2) {
             s[0] = __fma_rn(wi, wi, s[0]);
-        } else {
+        } else if (MODE != 3) {
 #pragma unroll
             for (int r = 0; r < CNT; ++r) s[r] = __fma_rn(wi, r == 0 ? v0[i] : V[(size_t)r * ldv + i], s[r]);
         }
     }
-    block_sum<R>(s, sm);
-    grid_reduce_finish<R>(s, red, [hout, sig2_out] __device__(const double(&t)[R]) {
-        if (MODE == 2) {
-            const double nrm = __dsqrt_rn(t[0]);
-            hout[0] = nrm;
-            if (sig2_out) *sig2_out = t[0] > 0.0 ? 1.0 / t[0] : 0.0;
-        } else {
+    if constexpr (MODE != 3) {
+        block_sum<R>(s, sm);
+        grid_reduce_finish<R>(s, red, [hout, sig2_out] __device__(const double(&t)[R]) {
+            if (MODE == 2) {
+                const double nrm = __dsqrt_rn(t[0]);
+                hout[0] = nrm;
+                if (sig2_out) *sig2_out = t[0] > 0.0 ? 1.0 / t[0] : 0.0;
+            } else {
 #pragma unroll
-            for (int r = 0; r < R; ++r) hout[r] = t[r];
-        }
-    });
+                for (int r = 0; r < R; ++r) hout[r] = t[r];
+            }
+        });
+    }
 }
 
-// Launches k_cgs<cnt, MODE>; false when cnt is above the largest compiled count.
+// Launches k_cgs<cnt, MODE> for 1 <= cnt <= kCgsBlock.
 template <int MODE>
-bool launch_cgs(Context& ctx, int cnt, const double* w, const double* v0, const double* V, size_t N,
+void launch_cgs(Context& ctx, int cnt, const double* w, const double* v0, const double* V, size_t N,
                 const double* hin, const double* sig2, double* hout, double* wout, double* sig2_out) {
     const unsigned g = ctx.red_grid(N);
     switch (cnt) {
@@ -141,10 +150,41 @@ bool launch_cgs(Context& ctx, int cnt, const double* w, const double* v0, const 
         NUMA_CGS_CASE(8)
 #undef NUMA_CGS_CASE
         default:
-            return false;
+            throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "gmres: Gram-Schmidt block count outside 1..8");
     }
     ctx.count_launch();
-    return true;
+}
+
+// h[r] = <w, v_r> for r < cnt (v_0 = v0, v_r = V + r N): one fused pass per block of kCgsBlock.
+void cgs_dots(Context& ctx, int cnt, const double* w, const double* v0, const double* V, size_t N, double* h,
+              int upto = -1) {
+    const int lim = upto < 0 ? cnt : upto;
+    for (int b0 = 0; b0 < lim; b0 += kCgsBlock) {
+        const int c = std::min(kCgsBlock, lim - b0);
+        launch_cgs<0>(ctx, c, w, b0 == 0 ? v0 : V + (size_t)b0 * N, V + (size_t)b0 * N, N, nullptr, nullptr, h + b0,
+                      nullptr, nullptr);
+    }
+}
+
+// wout = w - sum_{r < cnt} hin[r] sig2[r] v_r (sig2 = 1 when null), then FIN = 2: hout[0] = ||wout||
+// (and *sig2_out), or FIN = 1: hout[r] = <wout, v_r> for every r < cnt.  The earlier blocks update
+// wout in place without a reduction; the last block fuses its update with the finish, and with
+// FIN = 1 the dots of the earlier blocks follow on the finished wout.
+template <int FIN>
+void cgs_update(Context& ctx, int cnt, const double* w, const double* v0, const double* V, size_t N,
+                const double* hin, const double* sig2, double* hout, double* wout, double* sig2_out) {
+    const int nb = (cnt + kCgsBlock - 1) / kCgsBlock;
+    const double* src = w;
+    for (int bi = 0; bi < nb; ++bi) {
+        const int b0 = bi * kCgsBlock, c = std::min(kCgsBlock, cnt - b0);
+        const double* bv0 = b0 == 0 ? v0 : V + (size_t)b0 * N;
+        const double* bV = V + (size_t)b0 * N;
+        const double* bs = sig2 ? sig2 + b0 : nullptr;
+        if (bi + 1 < nb) launch_cgs<3>(ctx, c, src, bv0, bV, N, hin + b0, bs, nullptr, wout, nullptr);
+        else launch_cgs<FIN>(ctx, c, src, bv0, bV, N, hin + b0, bs, FIN == 1 ? hout + b0 : hout, wout, sig2_out);
+        src = wout;
+    }
+    if (FIN == 1 && nb > 1) cgs_dots(ctx, cnt, wout, v0, V, N, hout, (nb - 1) * kCgsBlock);
 }
 
 // dst = src / d (gmres.hpp:128, :149) as src * RN(1/d): one FP64 instruction instead of a
@@ -217,61 +257,85 @@ __global__ void k_to32_scaled(const double* __restrict__ src, double s, float* _
 }
 
 // MODE 0: h[r] = <w, u_r> for r < CNT.
-// MODE 2: u_out = RN32(sigma_j (w - sum_r h[r] sigma_r^2 u_r)) (the orthogonalised w, scaled by the
-//         previous vector's 1/norm so that the stored vectors keep norms near 1 in FP32 range),
-//         then hout[0] = ||u_out||, sig2[j+1] = 1/||u_out||^2, sig[j+1] = 1/||u_out||.
-// Sums per thread in double-FP32, converted to FP64 for the block and grid reduction.
+// MODE 1: u = RN32(a (w - sum_r h[r] s2[r] u_r)) into uout (a = *ascale, or 1 when null), then
+//         h[r] = <u, u_r> (the second pass of CGS2).
+// MODE 2: the same u into uout, then hout[0] = ||u||, sig2[j+1] = 1/||u||^2, sig[j+1] = 1/||u||.
+// MODE 3: the double-FP32 partial sum a w - sum_r a h[r] s2[r] u_r into part_out, no reduction (the
+//         earlier blocks of a basis longer than kCgsBlock).
+// With part_in given, MODES 1-3 start from that partial sum instead of a w.  In MODE 2 (CGS1, the
+// second pass of CGS2 with a = sigma_j) the stored vectors keep norms near 1 in FP32 range.  Sums per
+// thread in double-FP32, converted to FP64 for the block and grid reduction.  w and uout may be the
+// same array, and so may part_in and part_out (each element is read before it is written, by one
+// thread).
 template <int CNT, int MODE>
-__global__ void __launch_bounds__(kRedThreads) k_cgs_df(const float* __restrict__ w, const float* __restrict__ u0,
-                                                        const float* __restrict__ U, size_t ldu,
-                                                        const double* __restrict__ hin, double* sig2,
-                                                        double* sig, int j, size_t N, RedArgs red,
-                                                        double* __restrict__ hout, float* __restrict__ uout) {
+__global__ void __launch_bounds__(kRedThreads) k_cgs_df(const float* w, const float2* part_in,
+                                                        const float* __restrict__ u0, const float* __restrict__ U,
+                                                        size_t ldu, const double* __restrict__ hin,
+                                                        const double* __restrict__ s2c,
+                                                        const double* __restrict__ ascale, double* sig2, double* sig,
+                                                        int j, size_t N, RedArgs red, double* __restrict__ hout,
+                                                        float* uout, float2* part_out) {
     pdl_wait();
     pdl_trigger();
     constexpr int R = MODE == 2 ? 1 : CNT;
     __shared__ double sm[R][32];
     DF cw{0.0f, 0.0f}, c[CNT];
-    if (MODE == 2) {
-        const double sj = sig[j];
-        cw = df_split(sj);
+    if (MODE != 0) {
+        const double a = ascale ? *ascale : 1.0;
+        cw = df_split(a);
 #pragma unroll
-        for (int r = 0; r < CNT; ++r) c[r] = df_split(-(sj * hin[r] * sig2[r]));
+        for (int r = 0; r < CNT; ++r) c[r] = df_split(-(a * hin[r] * s2c[r]));
     }
     DF acc[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) acc[r] = DF{0.0f, 0.0f};
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) {
-        const float wi = w[i];
-        if (MODE == 2) {
-            DF t{0.0f, 0.0f};
-            df_mac(t, cw, wi);
-#pragma unroll
-            for (int r = 0; r < CNT; ++r) df_mac(t, c[r], r == 0 ? u0[i] : U[(size_t)r * ldu + i]);
-            const float u = __fadd_rn(t.hi, t.lo);
-            uout[i] = u;
-            df_mac(acc[0], u, u);
-        } else {
+        if (MODE == 0) {
+            const float wi = w[i];
 #pragma unroll
             for (int r = 0; r < CNT; ++r) df_mac(acc[r], wi, r == 0 ? u0[i] : U[(size_t)r * ldu + i]);
+        } else {
+            DF t{0.0f, 0.0f};
+            if (part_in) {
+                const float2 p = part_in[i];
+                t = DF{p.x, p.y};
+            } else {
+                df_mac(t, cw, w[i]);
+            }
+#pragma unroll
+            for (int r = 0; r < CNT; ++r) df_mac(t, c[r], r == 0 ? u0[i] : U[(size_t)r * ldu + i]);
+            if (MODE == 3) {
+                part_out[i] = make_float2(t.hi, t.lo);
+            } else {
+                const float u = __fadd_rn(t.hi, t.lo);
+                uout[i] = u;
+                if (MODE == 2) {
+                    df_mac(acc[0], u, u);
+                } else {
+#pragma unroll
+                    for (int r = 0; r < CNT; ++r) df_mac(acc[r], u, r == 0 ? u0[i] : U[(size_t)r * ldu + i]);
+                }
+            }
         }
     }
-    double s[R];
+    if constexpr (MODE != 3) {
+        double s[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) s[r] = df_to_f64(acc[r]);
-    block_sum<R>(s, sm);
-    grid_reduce_finish<R>(s, red, [hout, sig2, sig, j] __device__(const double(&t)[R]) {
-        if (MODE == 2) {
-            const double nrm = __dsqrt_rn(t[0]);
-            hout[0] = nrm;
-            sig2[j + 1] = t[0] > 0.0 ? 1.0 / t[0] : 0.0;
-            sig[j + 1] = nrm > 0.0 ? 1.0 / nrm : 0.0;
-        } else {
+        for (int r = 0; r < R; ++r) s[r] = df_to_f64(acc[r]);
+        block_sum<R>(s, sm);
+        grid_reduce_finish<R>(s, red, [hout, sig2, sig, j] __device__(const double(&t)[R]) {
+            if (MODE == 2) {
+                const double nrm = __dsqrt_rn(t[0]);
+                hout[0] = nrm;
+                sig2[j + 1] = t[0] > 0.0 ? 1.0 / t[0] : 0.0;
+                sig[j + 1] = nrm > 0.0 ? 1.0 / nrm : 0.0;
+            } else {
 #pragma unroll
-            for (int r = 0; r < R; ++r) hout[r] = t[r];
-        }
-    });
+                for (int r = 0; r < R; ++r) hout[r] = t[r];
+            }
+        });
+    }
 }
 
 // x += scale * sum_r coef[r] Z_r (ASSIGN: x = scale * sum_r coef[r] Z_r, x not read) with FP32 Z and
@@ -324,16 +388,17 @@ void launch_combine_df(Context& ctx, unsigned grid, int cnt, const float* Z, siz
     ctx.count_launch();
 }
 
-// Launches k_cgs_df<cnt, MODE>; false when cnt is above the largest compiled count.
+// Launches k_cgs_df<cnt, MODE> for 1 <= cnt <= kCgsBlock.
 template <int MODE>
-bool launch_cgs_df(Context& ctx, int cnt, const float* w, const float* u0, const float* U, size_t N, const double* hin,
-                   double* sig2, double* sig, int j, double* hout, float* uout) {
+void launch_cgs_df(Context& ctx, int cnt, const float* w, const float2* part_in, const float* u0, const float* U,
+                   size_t N, const double* hin, const double* s2c, const double* ascale, double* sig2, double* sig,
+                   int j, double* hout, float* uout, float2* part_out) {
     const unsigned g = ctx.red_grid(N);
     switch (cnt) {
 #define NUMA_CGS_DF_CASE(K)                                                                                  \
     case K:                                                                                                  \
-        launch_pdl(k_cgs_df<K, MODE>, g, kRedThreads, 0, ctx.stream, w, u0, U, N, hin, sig2, sig, j, N, ctx.red, hout, \
-                   uout);                                                                                    \
+        launch_pdl(k_cgs_df<K, MODE>, g, kRedThreads, 0, ctx.stream, w, part_in, u0, U, N, hin, s2c, ascale, sig2, \
+                   sig, j, N, ctx.red, hout, uout, part_out);                                                \
         break;
         NUMA_CGS_DF_CASE(1)
         NUMA_CGS_DF_CASE(2)
@@ -345,10 +410,43 @@ bool launch_cgs_df(Context& ctx, int cnt, const float* w, const float* u0, const
         NUMA_CGS_DF_CASE(8)
 #undef NUMA_CGS_DF_CASE
         default:
-            return false;
+            throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "gmres: Gram-Schmidt block count outside 1..8");
     }
     ctx.count_launch();
-    return true;
+}
+
+// The FP32-basis forms of cgs_dots / cgs_update (u_0 = u0, u_r = U + r N).  cgs_update_df forms
+// u = RN32(a (w - sum_r hin[r] s2[r] u_r)) into uout with FIN = 2 (norm and the sigma slots of j + 1)
+// or FIN = 1 (h[r] = <u, u_r>); a basis longer than kCgsBlock chains its earlier blocks through the
+// double-FP32 partial sums in part (2 floats a point).
+void cgs_dots_df(Context& ctx, int cnt, const float* w, const float* u0, const float* U, size_t N, double* h,
+                 int upto = -1) {
+    const int lim = upto < 0 ? cnt : upto;
+    for (int b0 = 0; b0 < lim; b0 += kCgsBlock) {
+        const int c = std::min(kCgsBlock, lim - b0);
+        launch_cgs_df<0>(ctx, c, w, nullptr, b0 == 0 ? u0 : U + (size_t)b0 * N, U + (size_t)b0 * N, N, nullptr,
+                         nullptr, nullptr, nullptr, nullptr, 0, h + b0, nullptr, nullptr);
+    }
+}
+
+template <int FIN>
+void cgs_update_df(Context& ctx, int cnt, const float* w, const float* u0, const float* U, size_t N,
+                   const double* hin, const double* s2, const double* ascale, double* sig2, double* sig, int j,
+                   double* hout, float* uout, float2* part) {
+    const int nb = (cnt + kCgsBlock - 1) / kCgsBlock;
+    for (int bi = 0; bi < nb; ++bi) {
+        const int b0 = bi * kCgsBlock, c = std::min(kCgsBlock, cnt - b0);
+        const float* bu0 = b0 == 0 ? u0 : U + (size_t)b0 * N;
+        const float* bU = U + (size_t)b0 * N;
+        const float2* pin = bi == 0 ? nullptr : part;
+        if (bi + 1 < nb)
+            launch_cgs_df<3>(ctx, c, w, pin, bu0, bU, N, hin + b0, s2 + b0, ascale, sig2, sig, j, nullptr, nullptr,
+                             part);
+        else
+            launch_cgs_df<FIN>(ctx, c, w, pin, bu0, bU, N, hin + b0, s2 + b0, ascale, sig2, sig, j,
+                               FIN == 1 ? hout + b0 : hout, uout, nullptr);
+    }
+    if (FIN == 1 && nb > 1) cgs_dots_df(ctx, cnt, uout, u0, U, N, hout, (nb - 1) * kCgsBlock);
 }
 
 // *out = v (one device scalar from a host value, stream-ordered)
@@ -401,9 +499,9 @@ void Gmres::arnoldi_cgs2(size_t j, double* w) {
     double* h2 = ctx_.scalar(kSlotGmresH2);
     const size_t N = N_;
     const int cnt = (int)(j + 1);
-    launch_cgs<0>(ctx_, cnt, w, V_.p, V_.p, N, nullptr, nullptr, hcol, nullptr, nullptr);
-    launch_cgs<1>(ctx_, cnt, w, V_.p, V_.p, N, hcol, nullptr, h2, w, nullptr);
-    launch_cgs<2>(ctx_, cnt, w, V_.p, V_.p, N, h2, nullptr, hcol + j + 1, w, nullptr);
+    cgs_dots(ctx_, cnt, w, V_.p, V_.p, N, hcol);
+    cgs_update<1>(ctx_, cnt, w, V_.p, V_.p, N, hcol, nullptr, h2, w, nullptr);
+    cgs_update<2>(ctx_, cnt, w, V_.p, V_.p, N, h2, nullptr, hcol + j + 1, w, nullptr);
     ctx_.check_launch("arnoldi cgs2");
     // H = h + h' is formed on the host after the column is read (see solve).
 }
@@ -415,22 +513,26 @@ void Gmres::arnoldi_cgs1(size_t j, double* w) {
     double* hcol = ctx_.scalar(kSlotGmresH);
     const size_t N = N_;
     const int cnt = (int)(j + 1);
-    launch_cgs<0>(ctx_, cnt, w, V_.p, V_.p, N, nullptr, nullptr, hcol, nullptr, nullptr);
-    launch_cgs<2>(ctx_, cnt, w, V_.p, V_.p, N, hcol, nullptr, hcol + j + 1, w, nullptr);
+    cgs_dots(ctx_, cnt, w, V_.p, V_.p, N, hcol);
+    cgs_update<2>(ctx_, cnt, w, V_.p, V_.p, N, hcol, nullptr, hcol + j + 1, w, nullptr);
     ctx_.check_launch("arnoldi cgs1");
 }
 
-// Flexible GMRES with one-pass classical Gram-Schmidt and lazily normalised basis vectors: the
-// basis keeps v~_j = w~ as the update pass writes it, with sigma_j = 1/||v~_j|| (sigma_j^2 on the
-// device, sigma_j on the host), so no pass divides a vector.  The preconditioned vectors are
-// z_j := sigma_j M(v~_j) (FGMRES admits any z_j), A z_j = sigma_j A M(v~_j), and the Hessenberg
-// entries and the final coefficients carry the sigmas: h_ij = sigma_j sigma_i <A M(v~_j), v~_i>,
-// h_{j+1,j} = sigma_j ||w~||, x += sum_j (y_j sigma_j) M(v~_j).  The first basis vector is the
-// right-hand side (or residual) itself, read in place.  Cycles are at most kMaxCgs steps long.
+// Flexible GMRES with classical Gram-Schmidt (one pass, CGS1, or two, CGS2) and lazily normalised
+// basis vectors: the basis keeps v~_j = w~ as the update pass writes it, with sigma_j = 1/||v~_j||
+// (sigma_j^2 on the device, sigma_j on the host), so no pass divides a vector.  The preconditioned
+// vectors are z_j := sigma_j M(v~_j) (FGMRES admits any z_j), A z_j = sigma_j A M(v~_j), and the
+// Hessenberg entries and the final coefficients carry the sigmas: h_ij = sigma_j sigma_i
+// <A M(v~_j), v~_i> (CGS2: plus the second pass' coefficients), h_{j+1,j} = sigma_j ||w~||,
+// x += sum_j (y_j sigma_j) M(v~_j).  The first basis vector is the right-hand side (or residual)
+// itself, read in place.  Cycles run to the restart length (the Gram-Schmidt passes take a long
+// basis in blocks).
 GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* x, const GmresOptions& o,
                               const double* r_init) {
     const size_t N = N_;
-    const size_t m = std::min(o.restart, (size_t)kMaxCgs);
+    const size_t m = o.restart;
+    if (m > kMaxRestart) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "GMRES restart larger than 250 is not supported");
+    const bool two_pass = o.orth == NUMA_GPU_ORTH_CGS2;
     GmresResult res;
     double* sl = ctx_.scalar(kSlotGmresH);
     double* sig2 = ctx_.scalar(kSlotGmresSig2);
@@ -474,6 +576,7 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
     if (v32) {
         V32_.resize((m + 1) * N);
         W32_.resize(N);
+        if (m + 1 > (size_t)kCgsBlock) P32_.resize(2 * N);  // double-FP32 partial sums of a long basis
     } else {
         V_.resize((m + 1) * N);
     }
@@ -482,8 +585,10 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
     w_.resize(N);
     r_.resize(N);
     std::vector<std::vector<double>> H(m + 1, std::vector<double>(m, 0.0));
-    std::vector<double> cs(m), sn(m), g(m + 1), y(m), col(m + 2), sig(m + 1);
+    std::vector<double> cs(m), sn(m), g(m + 1), y(m), col(m + 2), col2(m + 1), sig(m + 1);
     double* ydev = ctx_.scalar(kSlotGmresY);
+    double* h2 = ctx_.scalar(kSlotGmresH2);
+    float2* part = v32 && m + 1 > (size_t)kCgsBlock ? reinterpret_cast<float2*>(P32_.p) : nullptr;
     bool given = r_init != nullptr;
     bool first = o.zero_guess;
     const unsigned eg = ew_grid(ctx_, N);
@@ -562,18 +667,34 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
             }
             ++res.matvecs;
             const int cnt = (int)(j + 1);
-            if (v32) {
-                launch_cgs_df<0>(ctx_, cnt, W32_.p, u0, V32_.p, N, nullptr, sig2, sigd, (int)j, sl, nullptr);
-                launch_cgs_df<2>(ctx_, cnt, W32_.p, u0, V32_.p, N, sl, sig2, sigd, (int)j, sl + j + 1,
-                                 V32_.p + (j + 1) * N);
+            float* unext = v32 ? V32_.p + (j + 1) * N : nullptr;
+            if (v32 && !two_pass) {
+                cgs_dots_df(ctx_, cnt, W32_.p, u0, V32_.p, N, sl);
+                cgs_update_df<2>(ctx_, cnt, W32_.p, u0, V32_.p, N, sl, sig2, sigd + j, sig2, sigd, (int)j, sl + j + 1,
+                                 unext, part);
+            } else if (v32) {
+                // w' = RN32(sigma_j (w - sum c_r sigma_r^2 u_r)) into the next slot with c'_r = <w', u_r>, then
+                // u_{j+1} = RN32(w' - sum c'_r sigma_r^2 u_r) in place
+                cgs_dots_df(ctx_, cnt, W32_.p, u0, V32_.p, N, sl);
+                cgs_update_df<1>(ctx_, cnt, W32_.p, u0, V32_.p, N, sl, sig2, sigd + j, sig2, sigd, (int)j, h2, unext,
+                                 part);
+                cgs_update_df<2>(ctx_, cnt, unext, u0, V32_.p, N, h2, sig2, nullptr, sig2, sigd, (int)j, sl + j + 1,
+                                 unext, part);
+            } else if (!two_pass) {
+                cgs_dots(ctx_, cnt, w_.p, v0, V_.p, N, sl);
+                cgs_update<2>(ctx_, cnt, w_.p, v0, V_.p, N, sl, sig2, sl + j + 1, V_.p + (j + 1) * N, sig2 + j + 1);
             } else {
-                launch_cgs<0>(ctx_, cnt, w_.p, v0, V_.p, N, nullptr, nullptr, sl, nullptr, nullptr);
-                launch_cgs<2>(ctx_, cnt, w_.p, v0, V_.p, N, sl, sig2, sl + j + 1, V_.p + (j + 1) * N,
-                                      sig2 + j + 1);
+                cgs_dots(ctx_, cnt, w_.p, v0, V_.p, N, sl);
+                cgs_update<1>(ctx_, cnt, w_.p, v0, V_.p, N, sl, sig2, h2, w_.p, nullptr);
+                cgs_update<2>(ctx_, cnt, w_.p, v0, V_.p, N, h2, sig2, sl + j + 1, V_.p + (j + 1) * N, sig2 + j + 1);
             }
-            ctx_.check_launch("arnoldi (lazy cgs1)");
+            ctx_.check_launch("arnoldi (lazy cgs)");
             ctx_.fetch(sl, (int)(j + 2), col.data());
+            if (two_pass) ctx_.fetch(h2, (int)(j + 1), col2.data());
             for (size_t i = 0; i <= j; ++i) H[i][j] = sig[j] * sig[i] * col[i];
+            // the second pass' coefficients: on sigma_j w~ (FP32 basis) or on w~ itself
+            if (two_pass)
+                for (size_t i = 0; i <= j; ++i) H[i][j] += v32 ? sig[i] * col2[i] : sig[j] * sig[i] * col2[i];
             H[j + 1][j] = v32 ? col[j + 1] : sig[j] * col[j + 1];  // the FP32 u_{j+1} carries sigma_j
             sig[j + 1] = col[j + 1] > 0.0 ? 1.0 / col[j + 1] : 0.0;
             for (size_t i = 0; i < j; ++i) {
@@ -647,7 +768,8 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
 
 GmresResult Gmres::solve(LinearOp& A, Precond* M, const double* b, double* x, const GmresOptions& o,
                          KrylovSpace* save, const double* r_init) {
-    if (o.flexible && o.orth == NUMA_GPU_ORTH_CGS1 && !save) return solve_lazy(A, M, b, x, o, r_init);
+    if (o.flexible && (o.orth == NUMA_GPU_ORTH_CGS1 || o.orth == NUMA_GPU_ORTH_CGS2) && !save)
+        return solve_lazy(A, M, b, x, o, r_init);
     const size_t N = N_;
     const size_t m = o.restart;
     GmresResult res;
@@ -731,12 +853,12 @@ GmresResult Gmres::solve(LinearOp& A, Precond* M, const double* b, double* x, co
             ++res.precs;
             A.apply(zj, w_.p);
             ++res.matvecs;
-            if (cgs2 && j + 1 <= (size_t)kMaxCgs) {
+            if (cgs2) {
                 arnoldi_cgs2(j, w_.p);
                 ctx_.fetch(sl, (int)(j + 2), col.data());
                 ctx_.fetch(ctx_.scalar(kSlotGmresH2), (int)(j + 1), col2.data());
                 for (size_t i = 0; i <= j; ++i) col[i] += col2[i];
-            } else if (cgs1 && j + 1 <= (size_t)kMaxCgs) {
+            } else if (cgs1) {
                 arnoldi_cgs1(j, w_.p);
                 ctx_.fetch(sl, (int)(j + 2), col.data());
             } else {

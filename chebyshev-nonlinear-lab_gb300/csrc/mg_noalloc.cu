@@ -1,23 +1,28 @@
 // mg_noalloc.cu — a V-cycle entry point that allocates no memory.
 //
-// Some callers cannot call cudaMalloc when they need the preconditioner: code running while a
-// stream is being captured into a CUDA graph (allocation is not allowed there), a solver
-// callback in another library (for example a shell preconditioner invoked inside a foreign
-// Krylov loop) that must not allocate on every application, and programs that reserve their
-// whole device-memory budget up front.  numa_gpu_mg_apply_noalloc serves them: it runs the same
-// FP64 V-cycle as numa_gpu_mg_apply, with the same kernels in the same order (so the result is
-// bit-identical), but every work array lives in one static device array of 4.8 MB
-// (NUMA_GPU_NOALLOC_MAX_DOUBLES doubles), enough for grids up to 63^3.  Each GPU that loads this
-// library holds that array until the process exits.
+// Some callers cannot call cudaMalloc when they need the preconditioner: a solver callback in
+// another library (for example a shell preconditioner invoked inside a foreign Krylov loop)
+// that must not allocate or free on every application (cudaMalloc and cudaFree can synchronise
+// the device and so stall that library's pipeline), and programs that reserve their whole
+// device-memory budget up front and must not grow it.  numa_gpu_mg_apply_noalloc serves them: it
+// runs the same FP64 V-cycle as numa_gpu_mg_apply, with the same kernels in the same order (so
+// the result is bit-identical), but every work array lives in one static device array of
+// 4.8 MB (NUMA_GPU_NOALLOC_MAX_DOUBLES doubles), enough for grids up to 63^3.  Each GPU that
+// loads this library holds that array until the process exits.
 //
 // Set-up: the first call on a device, with that device current, resolves the array's device
-// address with cudaGetSymbolAddress (that may load the module); make that first call before
-// any stream capture.  Later calls only launch kernels.
+// address with cudaGetSymbolAddress (that may load the module) and keeps it for that device;
+// make that first call before any stream capture.  Later calls only launch kernels.  The kept
+// address belongs to the device's primary context: after cudaDeviceReset, or with another
+// context made current on the device, it is stale, and this entry point must not be used there.
 //
 // Sharing: every call uses the same array and leaves its contents behind.  The V-cycle writes
 // every value before it reads it, except the level iterates when pre = 0, which are cleared
 // with cudaMemsetAsync.  Calls that can overlap on the GPU (unordered streams) race on the
 // array: order them, or use numa_gpu_mg_apply with separate hierarchies.
+//
+// Errors: a CUDA error already pending when the call starts is returned as NUMA_GPU_ERR_CUDA
+// and left pending (cudaPeekAtLastError), so the caller still sees its own earlier failure.
 #include <cstring>
 #include <mutex>
 
@@ -72,8 +77,9 @@ size_t layout(size_t n, NaLevel* lv, int& nlev) {
     return used <= NUMA_GPU_NOALLOC_MAX_DOUBLES ? used : 0;
 }
 
-// The FP64 V-cycle of PoissonMG::cycle<double> on the static layout.
-void na_cycle(NaLevel* lv, int nlev, int l, double* resid, int pre, int post, cudaStream_t s) {
+// The FP64 V-cycle of PoissonMG::cycle<double> on the static layout.  Returns the first
+// failing enqueue's status (cudaSuccess when every launch and the memset were accepted).
+cudaError_t na_cycle(NaLevel* lv, int nlev, int l, double* resid, int pre, int post, cudaStream_t s) {
     NaLevel& L = lv[l];
     const int n = L.n;
     const dim3 blk(BX, BY);
@@ -91,10 +97,13 @@ void na_cycle(NaLevel* lv, int nlev, int l, double* resid, int pre, int post, cu
         if (n == 1) k_single<double><<<1, 1, 0, s>>>(L.b, L.x, nullptr, 6.0 * L.h2inv);
         else
             for (int sw = 0; sw < 30; ++sw) sweep(sw % 2, sw == 0);
-        return;
+        return cudaPeekAtLastError();
     }
     for (int sw = 0; sw < pre; ++sw) sweep(0, sw == 0);
-    if (pre == 0) cudaMemsetAsync(L.x, 0, (size_t)n * n * n * sizeof(double), s);
+    if (pre == 0) {
+        const cudaError_t e = cudaMemsetAsync(L.x, 0, (size_t)n * n * n * sizeof(double), s);
+        if (e != cudaSuccess) return e;
+    }
     {
         const int ichunk = n >= 64 ? 8 : 1;
         const dim3 g((n + BX - 1) / BX, (n + BY - 1) / BY, (n + ichunk - 1) / ichunk);
@@ -103,12 +112,14 @@ void na_cycle(NaLevel* lv, int nlev, int l, double* resid, int pre, int post, cu
     NaLevel& C = lv[l + 1];
     const int nc = C.n;
     k_restrict<double><<<dim3((nc + BX - 1) / BX, (nc + BY - 1) / BY, nc), blk, 0, s>>>(resid, C.b, C.bs, n, nc, C.inv);
-    na_cycle(lv, nlev, l + 1, resid, pre, post, s);
+    const cudaError_t ec = na_cycle(lv, nlev, l + 1, resid, pre, post, s);
+    if (ec != cudaSuccess) return ec;
     if (post > 0)
         k_prolong<double, true><<<dim3(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, n), blk, 0, s>>>(C.x, L.x, nc, n);
     else
         k_prolong<double, false><<<dim3((n + BX - 1) / BX, (n + BY - 1) / BY, n), blk, 0, s>>>(C.x, L.x, nc, n);
     for (int sw = 0; sw < post; ++sw) sweep(1, false);
+    return cudaPeekAtLastError();
 }
 
 }  // namespace
@@ -122,12 +133,15 @@ extern "C" int numa_gpu_mg_apply_noalloc(size_t n, int pre, int post, const doub
     NaLevel lv[16];
     int nlev = 0;
     if (layout(n, lv, nlev) == 0) return NUMA_GPU_ERR_TOO_LARGE;
+    // an error left by an earlier call of the caller's is reported, not consumed
+    if (cudaPeekAtLastError() != cudaSuccess) return NUMA_GPU_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
         return NUMA_GPU_ERR_NO_DEVICE;
     }
     if (dev < 0 || dev >= kMaxDevices) return NUMA_GPU_ERR_NOT_SUPPORTED;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
     double* base = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_mu);
@@ -149,13 +163,16 @@ extern "C" int numa_gpu_mg_apply_noalloc(size_t n, int pre, int post, const doub
     }
     const size_t N0 = n * n * n;
     double* resid = base + N0;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     // finest level: smooth in z, read r in place, b*h^2 into the array (poisson_mg.hpp:76-79)
     lv[0].x = z;
     lv[0].b = const_cast<double*>(r);
     const unsigned g = static_cast<unsigned>((N0 + 255) / 256 < 4096 ? (N0 + 255) / 256 : 4096);
     k_scale_in64<<<g, 256, 0, s>>>(r, lv[0].bs, lv[0].inv, N0);
-    na_cycle(lv, nlev, 0, resid, pre, post, s);
-    const cudaError_t e = cudaGetLastError();
-    return e == cudaSuccess ? NUMA_GPU_OK : NUMA_GPU_ERR_CUDA;
+    const cudaError_t e0 = cudaPeekAtLastError();
+    const cudaError_t e = e0 != cudaSuccess ? e0 : na_cycle(lv, nlev, 0, resid, pre, post, s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();  // this call's own launch error: reported through the status
+        return NUMA_GPU_ERR_CUDA;
+    }
+    return NUMA_GPU_OK;
 }

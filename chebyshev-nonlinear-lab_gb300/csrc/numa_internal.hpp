@@ -170,6 +170,9 @@ public:
     void d2_c(const double* c, const double* v, double* out);
     // d = 6 h^-2 - c (bratu3d.hpp:59-69).
     void jacobi_diag_c(const double* c, double* d);
+    // Average ms of one residual evaluation with its fused norm and the cache the drivers keep
+    // (c = lambda e^x; with precision FP32 also RN32(c) and RN32(F)), reps launches back to back.
+    double time_eval(const double* x, int precision, int reps);
 
 private:
     size_t n_, N_;
@@ -531,6 +534,7 @@ private:
     DeviceArray<float> Z32_;  // FGMRES preconditioned vectors in FP32 (FP32 preconditioner and product)
     DeviceArray<float> V32_;  // FGMRES basis in FP32 (FP32 hand-off, loose linear tolerance)
     DeviceArray<float> W32_;  // its A z_j in FP32
+    DeviceArray<float> P32_;  // double-FP32 partial sums of a Gram-Schmidt update over a long FP32 basis
     PinnedBuf pin_;
 };
 

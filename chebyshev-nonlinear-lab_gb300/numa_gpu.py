@@ -221,6 +221,7 @@ SIGNATURES = {
     "numa_gpu_mg_apply_noalloc": ([_SZ, _I, _I, _P, _P, _P], _I),
     "numa_gpu_diag_fp64_peak": ([_P, _F64P], _I),
     "numa_gpu_diag_time_smoother": ([_P, _I, _F64P], _I),
+    "numa_gpu_diag_time_eval": ([_P, _P, _I, _I, _F64P], _I),
     "numa_gpu_diag_time_bmg2d_pass": ([_P, _I, _F64P], _I),
     "numa_gpu_diag_exp": ([_P, _P, _P], _I),
     "numa_gpu_diag_div": ([_P, C.c_double, _P], _I),
@@ -481,6 +482,12 @@ class Bratu3D:
     def jacobi_diag(self, x: Vec, d: Vec):
         self.ctx.check(self.lib.numa_gpu_bratu3d_jacobi_diag(self.h, x.h, d.h), "bratu3d_jacobi_diag")
 
+    def time_eval(self, x: Vec, precision: int = FP64, reps: int = 20) -> float:
+        """Average ms of one residual evaluation with its fused norm and cache (diagnostic)."""
+        v = C.c_double()
+        self.ctx.check(self.lib.numa_gpu_diag_time_eval(self.h, x.h, precision, reps, C.byref(v)), "diag_time_eval")
+        return v.value
+
 
 class Burgers2D:
     """Burgers2D(n, nu, dt, amplitude) (problems/burgers2d.hpp:23-52) on the GPU; N = 2 n^2."""
@@ -640,6 +647,17 @@ class BrussMG2D(_Handle):
         v = C.c_double()
         self.ctx.check(self.lib.numa_gpu_diag_time_bmg2d_pass(self.h, reps, C.byref(v)), "diag_time_bmg2d_pass")
         return v.value
+
+
+def batch_config_instances(count: int = 128, seed: int = 42, sizes=(31, 63, 127),
+                           lam_range=(1.0, 6.5)) -> list[tuple[int, float]]:
+    """The batched configuration's instance table: `count` Bratu3D instances (n, lambda), n drawn
+    uniformly from `sizes` and lambda ~ U[lam_range] from numpy's PCG64 stream of `seed` (all n
+    first, then all lambda)."""
+    rng = np.random.default_rng(seed)
+    ns = rng.choice(list(sizes), count)
+    lams = rng.uniform(lam_range[0], lam_range[1], count)
+    return [(int(n), float(lm)) for n, lm in zip(ns, lams)]
 
 
 def brusselator2d_initial(n: int, A: float = 1.0, B: float = 3.4, seed: int = 20261203) -> np.ndarray:

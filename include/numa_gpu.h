@@ -504,18 +504,21 @@ const char* numa_gpu_batch_last_error(void);
 
 /* ---------------------------------------------------------------- V-cycle without allocation */
 /* No counterpart in the reference.  For callers that cannot allocate device memory when they
- * apply the preconditioner (while a stream is being captured into a CUDA graph, inside another
- * library's solver callback, under a device-memory budget fixed up front): one FP64 V-cycle
- * z = M^-1 r of PoissonMG(n, pre, post) on grids up to 63^3, bit-identical to
- * numa_gpu_mg_apply, with every work array in one static device array of
- * NUMA_GPU_NOALLOC_MAX_DOUBLES doubles (4.8 MB, held by each GPU that loads the library until
- * the process exits).  r and z are distinct device arrays of n^3 doubles on the current device;
- * the work is enqueued on `stream` (a cudaStream_t, NULL for the default stream) and the call
- * returns without waiting.  It calls no cudaMalloc, cudaFree or allocating library routine.
- * The first call on each device, with that device current, resolves the array's address with
- * cudaGetSymbolAddress: make it before any stream capture.  Every call shares the array, so
- * calls that may run concurrently on the GPU race: order them on one stream.  Returns
- * NUMA_GPU_ERR_TOO_LARGE when the hierarchy of n does not fit the array. */
+ * apply the preconditioner: another library's solver callback that must not allocate or free on
+ * every application (cudaMalloc / cudaFree can synchronise the device), or a program whose
+ * device-memory budget is fixed up front.  One FP64 V-cycle z = M^-1 r of PoissonMG(n, pre, post)
+ * on grids up to 63^3, bit-identical to numa_gpu_mg_apply, with every work array in one static
+ * device array of NUMA_GPU_NOALLOC_MAX_DOUBLES doubles (4.8 MB, held by each GPU that loads the
+ * library until the process exits).  r and z are distinct device arrays of n^3 doubles on the
+ * current device; the work is enqueued on `stream` (a cudaStream_t, NULL for the default stream)
+ * and the call returns without waiting.  It calls no cudaMalloc, cudaFree or allocating library
+ * routine.  The first call on each device, with that device current, resolves the array's
+ * address with cudaGetSymbolAddress and keeps it: make it before any stream capture.  The kept
+ * address belongs to the device's primary context; after cudaDeviceReset, or with another
+ * context current on the device, do not call this entry point.  Every call shares the array,
+ * so calls that may run concurrently on the GPU race: order them on one stream.  Returns
+ * NUMA_GPU_ERR_TOO_LARGE when the hierarchy of n does not fit the array, and NUMA_GPU_ERR_CUDA,
+ * leaving the error pending, when a CUDA error was already pending on entry. */
 #define NUMA_GPU_NOALLOC_MAX_DOUBLES 600832
 int numa_gpu_mg_apply_noalloc(size_t n, int pre, int post, const double* r, double* z, void* stream);
 
@@ -526,6 +529,11 @@ int numa_gpu_diag_fp64_peak(numa_gpu_ctx* ctx, double* tflops);
 /* Average duration in ms of one red-black Gauss-Seidel colour pass on the finest level of mg
  * (the V-cycle's dominant kernel), over reps back-to-back launches timed with CUDA events. */
 int numa_gpu_diag_time_smoother(numa_gpu_mg* mg, int reps, double* ms_per_pass);
+/* Average duration in ms of one Bratu3D residual evaluation F(x) with its fused norm and the cache
+ * the nonlinear drivers keep (c = lambda e^x; precision NUMA_GPU_FP32 adds RN32(c) and RN32(F), as
+ * on the mixed path), over reps back-to-back launches timed with CUDA events. */
+int numa_gpu_diag_time_eval(numa_gpu_bratu3d* op, const numa_gpu_vec* x, int precision, int reps,
+                            double* ms_per_eval);
 /* The same for the finest level of a Brusselator2D multigrid (its blocks must have been set). */
 int numa_gpu_diag_time_bmg2d_pass(numa_gpu_bmg2d* mg, int reps, double* ms_per_pass);
 /* out = e^x as the residual kernels compute it (Tang's table-driven method, FP64); cuda_ref

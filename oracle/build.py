@@ -3,8 +3,9 @@
 * ``oracle/_build/liboracle.so`` — the CPU restatement (numa_oracle.cpp), g++ + OpenMP,
   floating-point contraction off.  Built wherever the tests or bench.py's CPU baseline run.
 * ``oracle/_ref/libnuma_ref.so`` — ref_driver.cpp compiled against the reference's own headers
-  where they lie (``REFERENCE_ROOT``, default /root/reference/include).  Built only where the
-  reference is present; it generates the golden fixtures under tests/golden/.
+  where they lie: the reference checkout named by the environment variable ``NUMA_REFERENCE_ROOT``,
+  or else a checkout called ``reference`` beside this repository's directory.  Built only where
+  the reference is present; it generates the golden fixtures under tests/golden/.
 
 Run ``python oracle/build.py`` to build both.
 """
@@ -20,7 +21,19 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
-REFERENCE_INCLUDE = Path(os.environ.get("NUMA_REFERENCE_INCLUDE", "/root/reference/include"))
+
+
+def reference_root() -> Path | None:
+    """The reference checkout: $NUMA_REFERENCE_ROOT, else ``../reference`` beside this repository.
+
+    None when neither holds the reference's headers (as on a machine that only runs the tests)."""
+    env = os.environ.get("NUMA_REFERENCE_ROOT")
+    cands = [Path(env)] if env else [ROOT.parent / "reference"]
+    for c in cands:
+        if (c / "include" / "numa" / "problems" / "bratu3d.hpp").is_file():
+            return c
+    return None
+
 
 COMMON = ["-O3", "-DNDEBUG", "-std=c++20", "-fopenmp", "-fPIC", "-shared"]
 
@@ -48,7 +61,7 @@ def build_oracle(force: bool = False) -> Path:
 
 
 def reference_available() -> bool:
-    return (REFERENCE_INCLUDE / "numa" / "problems" / "bratu3d.hpp").is_file()
+    return reference_root() is not None
 
 
 def build_ref(force: bool = False) -> Path | None:
@@ -57,13 +70,14 @@ def build_ref(force: bool = False) -> Path | None:
     Flags follow the reference's Release build (CMakeLists.txt: -O3, C++20, OpenMP with
     NUMA_HAS_OPENMP=1, no -march), so x86-64 code has no FMA contraction, like the oracle.
     """
-    if not reference_available():
+    root = reference_root()
+    if root is None:
         return None
     REF_OUT.mkdir(exist_ok=True)
     out = REF_OUT / "libnuma_ref.so"
     srcs = [HERE / "ref_driver.cpp", ROOT / "include" / "numa_gpu.h"]
     if force or _stale(out, srcs):
-        cmd = [_cxx(), *COMMON, "-DNUMA_HAS_OPENMP=1", f"-I{REFERENCE_INCLUDE}",
+        cmd = [_cxx(), *COMMON, "-DNUMA_HAS_OPENMP=1", f"-I{root / 'include'}",
                str(HERE / "ref_driver.cpp"), "-o", str(out)]
         subprocess.run(cmd, check=True)
     return out

@@ -1,7 +1,8 @@
 // The reference's own nonlinear drivers and GMRES (namespace numa::op), instantiated unchanged
-// with the GPU operator and preconditioner of numa/gpu/numa_gpu.hpp.  This translation unit is
-// compiled where the reference headers are present (tests/test_cpp_adaptor.py); each operator
-// call then moves its vectors to and from the GPU.
+// with the GPU operator and preconditioner of numa/gpu/numa_gpu.hpp.  This program is compiled
+// and linked against libnuma_gpu.so where the reference headers are present
+// (tests/test_cpp_adaptor.py); run on a GPU host, each operator call moves its vectors to and
+// from the GPU.
 #include <numa/linalg/gmres.hpp>
 #include <numa/methods/krylov_newton.hpp>
 #include <numa/methods/tf_chebyshev_2018.hpp>

@@ -2,7 +2,7 @@
 
 Run from the repository root, where the reference is present:
 
-    OMP_NUM_THREADS=1 python tests/golden/make_golden.py [--brusselator]
+    OMP_NUM_THREADS=1 python tests/golden/make_golden.py [--brusselator | --large]
 
 (one thread: OpenMP's reduction order is not fixed across runs with more threads, and the
 reference's published calibration runs used one thread).
@@ -36,10 +36,12 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
 sys.path.insert(0, str(ROOT))
 
-from oracle.build import build_ref  # noqa: E402
+from oracle.build import build_ref, reference_root  # noqa: E402
 from oracle.oracle_lib import Oracle, default_params, make_point  # noqa: E402
 
-REFERENCE_ROOT = Path("/root/reference")
+REFERENCE_ROOT = reference_root()  # $NUMA_REFERENCE_ROOT, or ../reference beside the repository
+if REFERENCE_ROOT is None:
+    raise SystemExit("the reference checkout was not found: set NUMA_REFERENCE_ROOT")
 CALIBRATION_CSV = REFERENCE_ROOT / "experiments/c1/amendment01/calibration_combined.csv"
 
 
@@ -259,8 +261,69 @@ def brusselator_main() -> None:
     print(len(solves), "Brusselator solves,", len(vec), "vectors,", len(rows), "calibration rows")
 
 
+def strided_sample(N: int, target: int) -> np.ndarray:
+    """Deterministic sample indices of an N-vector: every stride-th point from stride/2, stride odd
+    and about N/target (an odd stride does not alias with the power-of-two-plus-one grid lines)."""
+    stride = max(1, N // target) | 1
+    return np.arange(stride // 2, N, stride, dtype=np.int64)
+
+
+def large_main() -> None:
+    """Fixtures at the sizes the benchmark runs (the reference's headers compiled here, one thread):
+
+    * ``reference_large.json`` / ``reference_large.npz`` — Bratu3D lambda = 6, u0 = 0, rtol 1e-10,
+      GMRES(30), PoissonMG V(2,2) on the full hierarchy: at 255^3 Newton-Krylov, inexact Chebyshev
+      and Chebyshev with Krylov recycling; at 127^3 Newton-Krylov and inexact Chebyshev.  Counts,
+      residuals, solution statistics and a strided sample of ~16k solution values with its indices;
+    * ``reference_batch.json`` / ``reference_batch.npz`` — every instance of the batched
+      configuration (128 instances, n from {31, 63, 127}, lambda ~ U[1, 6.5], numpy PCG64 seed 42;
+      numa_gpu.batch_config_instances), each solved alone by Newton-Krylov with the same settings,
+      as the reference's campaign runner loops over instances (apps/run_campaign.cpp:344-475):
+      counts, residuals, statistics and a strided sample of ~512 values per instance.
+    """
+    sys.path.insert(0, str(ROOT / "chebyshev-nonlinear-lab_gb300"))
+    from numa_gpu import batch_config_instances
+    if build_ref() is None:
+        raise SystemExit("reference headers not found")
+    ref = Oracle.reference()
+    north = dict(rtol_nl=1e-10, gmres_restart=30)
+    keys = ("converged", "iters", "n_F", "n_JVP", "n_D2", "n_lin_iters", "n_lin_failures", "n_prec", "res0", "res")
+    large, lvec = [], {}
+    for n, methods in ((127, ("nk", "cheb")), (255, ("nk", "cheb", "rec"))):
+        N = n ** 3
+        idx = strided_sample(N, 16384)
+        lvec[f"idx_n{n}"] = idx
+        for method in methods:
+            p = default_params(**north)
+            x, res = ref.solve(n, 6.0, method, "mg", p)
+            large.append(dict(n=n, lam=6.0, method=method, precond="mg", params=params_dict(p),
+                              result={k: res[k] for k in keys}, solution=solution_stats(x)))
+            lvec[f"x_n{n}_{method}"] = x[idx]
+            print("large", n, method, res["iters"], res["n_JVP"], res["n_prec"], flush=True)
+    (HERE / "reference_large.json").write_text(json.dumps(large, indent=1))
+    np.savez_compressed(HERE / "reference_large.npz", **lvec)
+
+    inst = batch_config_instances()
+    batch, bvec = [], {}
+    for i, (n, lam) in enumerate(inst):
+        p = default_params(**north)
+        x, res = ref.solve(n, lam, "nk", "mg", p)
+        idx = strided_sample(n ** 3, 512)
+        batch.append(dict(index=i, n=n, lam=lam, method="nk", precond="mg", result={k: res[k] for k in keys},
+                          solution=solution_stats(x), sample_count=int(idx.size)))
+        bvec[f"x_{i}"] = x[idx]
+        print("batch", i, n, round(lam, 4), res["iters"], res["n_JVP"], res["n_prec"], flush=True)
+    (HERE / "reference_batch.json").write_text(json.dumps({"seed": 42, "params": params_dict(default_params(**north)),
+                                                           "instances": batch}, indent=1))
+    np.savez_compressed(HERE / "reference_batch.npz", **bvec)
+
+
 if __name__ == "__main__":
-    if "--brusselator" in sys.argv:
+    if os.environ.get("OMP_NUM_THREADS") != "1":
+        raise SystemExit("run with OMP_NUM_THREADS=1")
+    if "--large" in sys.argv:
+        large_main()
+    elif "--brusselator" in sys.argv:
         brusselator_main()
     else:
         main()

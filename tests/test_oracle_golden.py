@@ -146,3 +146,37 @@ def test_c1_calibration_n31(oracle, c1_rows):
         want = tuple(int(r[k]) for k in ("nonlinear_iters", "n_F", "n_JVP", "n_D2", "n_lin", "n_prec"))
         assert got == want, (r["param"], r["method"], r["internal_candidate_id"])
         assert res["res"] / res["res0"] == pytest.approx(float(r["residual_rel"]), rel=1e-3)
+
+
+# ------------------------------------------------------------------ the benchmark's sizes
+def test_oracle_matches_reference_at_127(oracle):
+    """The oracle port at 127^3 (lambda = 6, rtol 1e-10, GMRES(30), MG V(2,2)) against the reference's
+    own run (tests/golden/reference_large.*): equal counts, solution to 1e-12 at the sampled points.
+    (The 255^3 fixtures pin the GPU path in tests/test_parity_large_gpu.py; the oracle takes ~10 s
+    there on one thread, too long for this suite.)"""
+    import json
+
+    from conftest import GOLDEN
+    cases = {(c["n"], c["method"]): c for c in json.loads((GOLDEN / "reference_large.json").read_text())}
+    vec = np.load(GOLDEN / "reference_large.npz")
+    c = cases[(127, "nk")]
+    x, r = oracle.solve(127, c["lam"], "nk", "mg", default_params(rtol_nl=1e-10, gmres_restart=30))
+    assert all(r[k] == c["result"][k] for k in COUNT_KEYS)
+    idx = vec["idx_n127"]
+    assert rel_err(x[idx], vec["x_n127_nk"]) < 1e-12
+    assert float(x.max()) == pytest.approx(c["solution"]["max"], rel=1e-12)
+
+
+def test_batch_fixture_instance_table():
+    """The batched configuration's instance table (numa_gpu.batch_config_instances: 128 instances,
+    n from {31, 63, 127}, lambda ~ U[1, 6.5], seed 42) is the one the reference solved for
+    tests/golden/reference_batch.*, and every instance there converged."""
+    import json
+
+    import numa_gpu
+    from conftest import GOLDEN
+    fx = json.loads((GOLDEN / "reference_batch.json").read_text())
+    table = numa_gpu.batch_config_instances(128, seed=42)
+    assert [(e["n"], e["lam"]) for e in fx["instances"]] == table
+    assert all(e["result"]["converged"] == 1 for e in fx["instances"])
+    assert {n for n, _ in table} == {31, 63, 127}

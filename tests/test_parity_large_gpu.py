@@ -1,0 +1,113 @@
+"""Parity at the benchmark's sizes, against the reference itself.
+
+The fixtures tests/golden/reference_large.{json,npz} were made by the reference's own headers
+compiled here (tests/golden/make_golden.py --large, one thread): Bratu3D, lambda = 6, u0 = 0,
+rtol 1e-10, GMRES(30), PoissonMG V(2,2) on the full hierarchy, at 255^3 (Newton-Krylov, inexact
+Chebyshev, Chebyshev with Krylov recycling) and 127^3 (Newton-Krylov, inexact Chebyshev).  Each
+records the counts, the residuals, the solution's sum / l2 / max / min and ~16k solution values at
+fixed strided indices.
+
+* The plain FP64 path (the drop-in) must give the reference's counts within +-1 and its solution
+  within 1e-12 relative (reductions are not bit-exact, so not bit for bit).
+* The mixed path (FP32 V-cycle and FP32 Jacobian products inside FGMRES, FP64 residual, updates
+  and Arnoldi coefficients) and the learned preconditioner must reach the same tolerance with the
+  Newton count within +-1, and their solutions must lie within 1e-8 of the reference's.
+"""
+from __future__ import annotations
+
+import json
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+COUNTS = ("iters", "n_F", "n_JVP", "n_D2", "n_lin_iters", "n_lin_failures", "n_prec")
+
+
+def _G():
+    import numa_gpu
+    return numa_gpu
+
+
+@pytest.fixture(scope="module")
+def large():
+    cases = json.loads((GOLDEN / "reference_large.json").read_text())
+    vec = dict(np.load(GOLDEN / "reference_large.npz"))
+    return {(c["n"], c["method"]): c for c in cases}, vec
+
+
+def _params(G, c, mixed: bool, orth=None):
+    p = G.default_params()
+    for k, v in c["params"].items():
+        setattr(p, k, v)
+    if mixed:
+        p.flexible = 1
+        p.jvp_precision = G.FP32
+        p.orth = G.CGS1 if orth is None else orth
+    return p
+
+
+def _check_solution(x, c, vec, tol):
+    n, method = c["n"], c["method"]
+    idx = vec[f"idx_n{n}"]
+    want = vec[f"x_n{n}_{method}"]
+    got = x[idx]
+    assert np.linalg.norm(got - want) <= tol * np.linalg.norm(want), (n, method)
+    st = c["solution"]
+    assert float(x.max()) == pytest.approx(st["max"], rel=tol)
+    assert float(np.linalg.norm(x)) == pytest.approx(st["l2"], rel=tol)
+    assert float(x.sum()) == pytest.approx(st["sum"], rel=tol)
+    assert float(x.min()) == pytest.approx(st["min"], rel=tol, abs=tol * st["max"])
+
+
+@pytest.mark.parametrize("n,method", [(255, "nk"), (255, "cheb"), (255, "rec"), (127, "nk"), (127, "cheb")])
+def test_fp64_path_matches_reference(gpu, large, n, method):
+    G = _G()
+    cases, vec = large
+    c = cases[(n, method)]
+    op = G.Bratu3D(gpu, n, c["lam"])
+    pc = G.Provider.poisson_mg(gpu, n)
+    x = gpu.vec(n ** 3).fill(0.0)
+    r = G.solve(op, x, method, _params(G, c, False), pc)
+    ref = c["result"]
+    assert r["converged"] == ref["converged"] == 1
+    assert all(abs(int(r[k]) - int(ref[k])) <= 1 for k in COUNTS), (r, ref)
+    assert r["res"] <= 1e-10 * r["res0"]
+    assert r["res0"] == pytest.approx(ref["res0"], rel=1e-12)
+    _check_solution(x.numpy(), c, vec, 1e-12)
+
+
+@pytest.mark.parametrize("n,method,orth", [(255, "nk", "CGS1"), (255, "nk", "CGS2"), (255, "cheb", "CGS1"),
+                                           (127, "nk", "CGS1")])
+def test_mixed_path_within_1e8_of_reference(gpu, large, n, method, orth):
+    G = _G()
+    cases, vec = large
+    c = cases[(n, method)]
+    op = G.Bratu3D(gpu, n, c["lam"])
+    pc = G.Provider.poisson_mg(gpu, n, precision=G.FP32)
+    x = gpu.vec(n ** 3).fill(0.0)
+    r = G.solve(op, x, method, _params(G, c, True, getattr(G, orth)), pc)
+    assert r["converged"] == 1 and r["res"] <= 1e-10 * r["res0"]
+    assert abs(int(r["iters"]) - int(c["result"]["iters"])) <= 1
+    _check_solution(x.numpy(), c, vec, 1e-8)
+
+
+def test_learned_path_within_1e8_of_reference(gpu, large):
+    """The learned preconditioner beside the FP32 V-cycle inside FGMRES (a small network trained
+    here, on seeded lambda other than 6): the 255^3 solution within 1e-8 of the reference's."""
+    G = _G()
+    cases, vec = large
+    n = 255
+    c = cases[(n, "nk")]
+    net = G.LearnedNet(gpu, 31, seed=3)
+    net.train(n, instances=2, states=2, rhs_per_state=1, krylov_per_state=4, epochs=2, batch=4, lr=2e-3, seed=11)
+    pcl = G.Provider.learned(gpu, n, net, stall=0.9)
+    op = G.Bratu3D(gpu, n, c["lam"])
+    x = gpu.vec(n ** 3).fill(0.0)
+    r = G.solve(op, x, "nk", _params(G, c, True), pcl)
+    assert r["converged"] == 1 and r["res"] <= 1e-10 * r["res0"]
+    assert abs(int(r["iters"]) - int(c["result"]["iters"])) <= 1
+    _check_solution(x.numpy(), c, vec, 1e-8)

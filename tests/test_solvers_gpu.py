@@ -158,6 +158,64 @@ def test_cgs2_matches_mgs(gpu):
     assert rel_err(xa.numpy(), xc.numpy()) < 1e-9
 
 
+@pytest.mark.parametrize("orth", ["CGS1", "CGS2"])
+def test_fgmres_long_cycles_match_reference(gpu, ref_counts, orth):
+    """FGMRES cycles run to the restart length asked for (30 here), past the 8 basis vectors one fused
+    Gram-Schmidt pass holds: the Jacobi-preconditioned 31^3 solves of the published calibration
+    (tuning t01: rtol 1e-8, eta0 0.25, GMRES(30), 200 linear iterations), whose linear solves take
+    up to 30 iterations a cycle, run as flexible GMRES with lazily normalised classical
+    Gram-Schmidt on the FP64 basis and give the reference's counts (+-1) and solution."""
+    G = _G()
+    cases = [c for c in ref_counts if c["tag"] == "c1_t01_n31" and c["method"] in ("nk", "cheb")]
+    assert cases
+    for c in cases:
+        params = dict(c["params"])
+        params.update(flexible=1, orth=getattr(G, orth))
+        x, r = gpu_solve(gpu, c["n"], c["lam"], c["method"], "jacobi", params)
+        ref = c["result"]
+        assert r["converged"] == ref["converged"] == 1
+        # linear solves of more than 8 iterations a cycle happened
+        assert r["n_lin_iters"] > 8 * r["iters"], (c["method"], r["n_lin_iters"])
+        assert all(abs(int(r[k]) - int(ref[k])) <= 1 for k in ("iters", "n_F", "n_D2")), (c["method"], r, ref)
+        assert abs(int(r["n_lin_iters"]) - int(ref["n_lin_iters"])) <= max(2, ref["n_lin_iters"] // 50), (r, ref)
+        assert x.max() == pytest.approx(c["solution"]["max"], rel=1e-8)
+        assert np.linalg.norm(x) == pytest.approx(c["solution"]["l2"], rel=1e-8)
+
+
+@pytest.mark.parametrize("orth", ["CGS1", "CGS2"])
+def test_fp32_basis_long_cycles(gpu, orth):
+    """The FP32 Arnoldi basis (double-FP32 Gram-Schmidt passes) over cycles longer than one fused
+    pass: GMRES(30) to 1e-5 on the Jacobian of Bratu3D at u = 0 with a large lambda, an indefinite
+    system (dozens of eigenvalues of -Lap_h lie below lambda) that the FP32 V-cycle leaves for GMRES
+    to resolve over many iterations; the first lambda of 150, 250, 400 whose FP64 solve takes more
+    than 8 iterations is used.  The true FP64 residual of the answer meets the tolerance (within the
+    FP32 basis' 6e-8 rounding of the Arnoldi relation) and the iteration count is the FP64 basis'
+    within 20 %."""
+    G = _G()
+    n = 31
+    N = n ** 3
+    xpt = gpu.vec(N)
+    b = gpu.from_numpy(make_point(N, 1.0))
+    pc32 = G.Provider.poisson_mg(gpu, n, precision=G.FP32)
+    pc64 = G.Provider.poisson_mg(gpu, n)
+    for lam in (150.0, 250.0, 400.0):
+        op = G.Bratu3D(gpu, n, lam)
+        x64 = gpu.vec(N)
+        g64 = G.gmres_bratu3d(op, xpt, b, x64, 1e-5, 30, 600, provider=pc64, orth=G.MGS)
+        if g64["converged"] and g64["iters"] > 8:
+            break
+    assert g64["converged"] and g64["iters"] > 8, g64
+    x32 = gpu.vec(N)
+    g32 = G.gmres_bratu3d(op, xpt, b, x32, 1e-5, 30, 600, provider=pc32, jvp_mode=G.ANALYTIC_FP32,
+                          orth=getattr(G, orth), flexible=True)
+    assert g32["converged"], (lam, g32, g64)
+    assert abs(g32["iters"] - g64["iters"]) <= max(2, g64["iters"] // 5), (lam, g32, g64)
+    Ax = gpu.vec(N)
+    op.jvp(xpt, x32, Ax)
+    Ax.axpy(-1.0, b)
+    assert Ax.norm2() <= 1.05e-5 * b.norm2()
+
+
 def test_mixed_path_with_cgs1(gpu):
     """The mixed path as the benchmark runs it (FGMRES, FP32 V-cycle and J v, one-pass classical
     Gram-Schmidt) against the FP64 drop-in: same Newton count, solution within 1e-8."""

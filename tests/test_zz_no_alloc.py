@@ -1,7 +1,7 @@
 """The V-cycle entry point that allocates nothing (numa_gpu_mg_apply_noalloc).
 
 It exists for callers that cannot allocate device memory when they apply the preconditioner:
-code running while a stream is captured into a CUDA graph, another library's solver callback,
+another library's solver callback that must not allocate or free on every application, and
 programs with a device-memory budget fixed up front.  These tests call it through the C ABI and
 hold it to the existing entry point numa_gpu_mg_apply: the FP64 V-cycle has no reductions, so
 the two must agree bit for bit (the tolerance the V-cycle tests use), on two calls in a row.
