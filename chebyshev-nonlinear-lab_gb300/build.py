@@ -29,9 +29,9 @@ NVCC_FLAGS = [
 ]
 SOURCES = [
     "context.cu", "bratu3d.cu", "ops.cu", "poisson_mg.cu", "hmg2d.cu", "brusselator.cu", "gmres.cu", "drivers.cu", "capi.cu", "diag.cu",
-    "mg_noalloc.cu", "learned.cu", "learned_net.cu", "batch.cu",
+    "mg_noalloc.cu", "learned.cu", "learned_net.cu", "batch.cu", "batch_solver.cu",
 ]
-HEADERS = ["common.cuh", "numa_internal.hpp", "mg_kernels.cuh", "learned_conv.cuh"]
+HEADERS = ["common.cuh", "numa_internal.hpp", "mg_kernels.cuh", "learned_conv.cuh", "batch_kernels.cuh"]
 
 
 def nvcc() -> str:

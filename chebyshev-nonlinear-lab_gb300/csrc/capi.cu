@@ -1722,6 +1722,65 @@ int numa_gpu_diag_time_bmg2d_pass(numa_gpu_bmg2d* mg, int reps, double* ms_per_p
     return guard(mg->ctx, [&] { *ms_per_pass = mg->impl->time_finest_pass(reps); });
 }
 
+struct numa_gpu_bsolver {
+    numa_gpu_ctx* ctx;
+    std::unique_ptr<BatchSolver> impl;
+};
+
+int numa_gpu_bsolver_create(numa_gpu_ctx* ctx, const numa_batch_instance* inst, size_t count,
+                            const numa_krylov_params* p, numa_gpu_bsolver** out) {
+    if (!ctx || !out || !inst || count == 0) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        auto h = std::make_unique<numa_gpu_bsolver>();
+        h->ctx = ctx;
+        h->impl = std::make_unique<BatchSolver>(*ctx->impl, inst, count, params_from_c(p));
+        *out = h.release();
+    });
+}
+
+int numa_gpu_bsolver_destroy(numa_gpu_bsolver* s) {
+    if (!s) return NUMA_GPU_OK;
+    numa_gpu_ctx* ctx = s->ctx;
+    return guard(ctx, [&] { delete s; });
+}
+
+int numa_gpu_bsolver_solve(numa_gpu_bsolver* s, double* x_out, numa_batch_result* results, double* seconds) {
+    if (!s || !results) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(s->ctx, [&] { s->impl->solve(x_out, results, seconds); });
+}
+
+int numa_gpu_bsolver_get_tuning(const numa_gpu_bsolver* s, numa_batch_tuning* t) {
+    if (!s || !t) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    std::memset(t, 0, sizeof(*t));
+    const BatchTuning b = s->impl->tuning();
+    t->planes = b.planes;
+    t->elems_per_block = b.elems_per_block;
+    return NUMA_GPU_OK;
+}
+
+int numa_gpu_bsolver_set_tuning(numa_gpu_bsolver* s, const numa_batch_tuning* t) {
+    if (!s || !t || t->planes < 1 || t->elems_per_block < 1) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(s->ctx, [&] { s->impl->set_tuning(BatchTuning{t->planes, t->elems_per_block}); });
+}
+
+int numa_gpu_bsolver_autotune(numa_gpu_bsolver* s, const int* planes, int np, const int* elems, int ne,
+                              numa_batch_tuning* chosen, double* seconds) {
+    if (!s || !planes || !elems || np < 1 || ne < 1) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    for (int a = 0; a < np; ++a)
+        if (planes[a] < 1) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    for (int b = 0; b < ne; ++b)
+        if (elems[b] < 1) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(s->ctx, [&] {
+        const BatchTuning b = s->impl->autotune(planes, np, elems, ne, seconds);
+        if (chosen) {
+            std::memset(chosen, 0, sizeof(*chosen));
+            chosen->planes = b.planes;
+            chosen->elems_per_block = b.elems_per_block;
+        }
+    });
+}
+
 int numa_gpu_diag_time_smoother(numa_gpu_mg* mg, int reps, double* ms_per_pass) {
     if (!mg || !ms_per_pass || reps < 1) return NUMA_GPU_ERR_INVALID_ARGUMENT;
     return guard(mg->ctx, [&] { *ms_per_pass = mg->impl->time_finest_pass(reps); });

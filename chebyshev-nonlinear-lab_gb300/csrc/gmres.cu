@@ -365,9 +365,9 @@ __global__ void k_combine_df(const float* __restrict__ Z, size_t ldz, const doub
     }
 }
 
-template <bool ASSIGN, bool STEP = false>
-void launch_combine_df(Context& ctx, unsigned grid, int cnt, const float* Z, size_t N, const double* coef, double scale,
-                       double* x, const double* xb = nullptr, double* xs = nullptr) {
+template <bool ASSIGN, bool STEP>
+void launch_combine_df_block(Context& ctx, unsigned grid, int cnt, const float* Z, size_t N, const double* coef,
+                             double scale, double* x, const double* xb, double* xs) {
     switch (cnt) {
 #define NUMA_COMBINE_DF_CASE(K)                                                                               \
     case K:                                                                                                   \
@@ -383,9 +383,26 @@ void launch_combine_df(Context& ctx, unsigned grid, int cnt, const float* Z, siz
         NUMA_COMBINE_DF_CASE(8)
 #undef NUMA_COMBINE_DF_CASE
         default:
-            throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "gmres: basis count above the compiled combine kernels");
+            throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "gmres: combine block count outside 1..8");
     }
     ctx.count_launch();
+}
+
+// x (+)= scale sum_{r<cnt} coef_r Z_r in blocks of kCgsBlock vectors: the first block assigns (ASSIGN)
+// or adds, later blocks add, and the last also writes the full step (STEP).
+template <bool ASSIGN, bool STEP = false>
+void launch_combine_df(Context& ctx, unsigned grid, int cnt, const float* Z, size_t N, const double* coef, double scale,
+                       double* x, const double* xb = nullptr, double* xs = nullptr) {
+    for (int b0 = 0; b0 < cnt; b0 += kCgsBlock) {
+        const int c = std::min(kCgsBlock, cnt - b0);
+        const bool first = b0 == 0, last = b0 + c >= cnt;
+        const float* Zb = Z + (size_t)b0 * N;
+        const double* cb = coef + b0;
+        if (first && last) launch_combine_df_block<ASSIGN, STEP>(ctx, grid, c, Zb, N, cb, scale, x, xb, xs);
+        else if (first) launch_combine_df_block<ASSIGN, false>(ctx, grid, c, Zb, N, cb, scale, x, xb, xs);
+        else if (last) launch_combine_df_block<false, STEP>(ctx, grid, c, Zb, N, cb, scale, x, xb, xs);
+        else launch_combine_df_block<false, false>(ctx, grid, c, Zb, N, cb, scale, x, xb, xs);
+    }
 }
 
 // Launches k_cgs_df<cnt, MODE> for 1 <= cnt <= kCgsBlock.

@@ -247,17 +247,17 @@ enum SplitPass { kPassFull = 0, kPassFirst = 1, kPassLastZ = 2 };
 //               or z32 (FP32) the same values unwidened, for consumers that work in FP32.
 //   NN > 0: the grid size is a compile-time constant, so every neighbour offset is an immediate of
 //           the load instruction (one add per point forms the base m + c).
+// The body takes its block coordinates as arguments, so that the batched form (below) can run it
+// on one grid of a pool.
 template <int MODE, int ICH, int NN>
-__global__ void __launch_bounds__(BX* BY) k_pass_split(float* __restrict__ own, const float* __restrict__ oth,
-                                                       const float* __restrict__ bown, double* __restrict__ z,
-                                                       Split g, int c, float* __restrict__ z32 = nullptr) {
-    pdl_wait();
-    pdl_trigger();
-    const int kk = blockIdx.x * BX + threadIdx.x;
-    const int j = blockIdx.y * BY + threadIdx.y;
+__device__ __forceinline__ void pass_split_body(float* __restrict__ own, const float* __restrict__ oth,
+                                                const float* __restrict__ bown, double* __restrict__ z, Split g,
+                                                int c, float* __restrict__ z32, int bx, int by, int bz) {
+    const int kk = bx * BX + threadIdx.x;
+    const int j = by * BY + threadIdx.y;
     const int n = NN > 0 ? NN : g.n;
     if (j >= n || 2 * kk >= n) return;
-    const int i0 = blockIdx.z * ICH;
+    const int i0 = bz * ICH;
     const int P = n * n;
     const int hn = NN > 0 ? (NN - 1) / 2 : g.hn, hP = NN > 0 ? (NN * NN - 1) / 2 : g.hP;
     const bool jlo = j > 0, jhi = j + 1 < n;
@@ -319,6 +319,15 @@ __global__ void __launch_bounds__(BX* BY) k_pass_split(float* __restrict__ own, 
     }
 }
 
+template <int MODE, int ICH, int NN>
+__global__ void __launch_bounds__(BX* BY) k_pass_split(float* __restrict__ own, const float* __restrict__ oth,
+                                                       const float* __restrict__ bown, double* __restrict__ z,
+                                                       Split g, int c, float* __restrict__ z32 = nullptr) {
+    pdl_wait();
+    pdl_trigger();
+    pass_split_body<MODE, ICH, NN>(own, oth, bown, z, g, c, z32, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
 // Launches one colour pass on a split level: planes per thread 4 above 63 points, else 1.
 template <int MODE>
 inline void launch_pass_split(float* x, const float* bs, double* z, const Split& g, int c, cudaStream_t st,
@@ -373,15 +382,14 @@ __device__ __forceinline__ void residual_pair(float* __restrict__ r, int LA, boo
     }
 }
 
-__global__ void __launch_bounds__(BX* BY) k_residual_split(const float* __restrict__ x, const float* __restrict__ b,
-                                                            float* __restrict__ r, Split g, float h2inv) {
-    pdl_wait();
-    pdl_trigger();
-    const int kk = blockIdx.x * BX + threadIdx.x;
-    const int j = blockIdx.y * BY + threadIdx.y;
+__device__ __forceinline__ void residual_split_body(const float* __restrict__ x, const float* __restrict__ b,
+                                                    float* __restrict__ r, Split g, float h2inv, int bx, int by,
+                                                    int bz) {
+    const int kk = bx * BX + threadIdx.x;
+    const int j = by * BY + threadIdx.y;
     const int n = g.n;
     if (j >= n || 2 * kk >= n) return;
-    const int i0 = blockIdx.z * 2;
+    const int i0 = bz * 2;
     const int P = n * n;
     const bool jlo = j > 0, jhi = j + 1 < n, hasB = 2 * kk + 1 < n, kloA = kk > 0, khiB = 2 * kk + 2 < n;
     const bool two = i0 + 1 < n;
@@ -416,20 +424,25 @@ __global__ void __launch_bounds__(BX* BY) k_residual_split(const float* __restri
                       a_jp1, a_km1, xb0, b_ip1, b_jm1, b_jp1, b_kp1, h2inv);
 }
 
+__global__ void __launch_bounds__(BX* BY) k_residual_split(const float* __restrict__ x, const float* __restrict__ b,
+                                                            float* __restrict__ r, Split g, float h2inv) {
+    pdl_wait();
+    pdl_trigger();
+    residual_split_body(x, b, r, g, h2inv, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
 // Restriction from a natural-layout fine residual into a split coarse level (odd nc): the
 // 27-point sum of k_restrict in the same order, b and b h^2 stored split.  FIRST_X: also the
 // coarse level's first smoothing pass (colour 0 from x = 0: x = bs / 6), which the cycle then
 // skips.  Split levels come in pairs nf = 2 nc + 1, so all 27 fine points exist: no bounds tests,
 // and the 27 loads are issued ahead of the FMA chain.
 template <bool FIRST_X>
-__global__ void __launch_bounds__(BX* BY) k_restrict_split(const float* __restrict__ rf, float* __restrict__ bc,
-                                                           float* __restrict__ bsc, float* __restrict__ xc, int nf,
-                                                           int nc, int halfc, float inv_c) {
-    pdl_wait();
-    pdl_trigger();
-    const int K = blockIdx.x * BX + threadIdx.x;
-    const int J = blockIdx.y * BY + threadIdx.y;
-    const int I = blockIdx.z;
+__device__ __forceinline__ void restrict_split_body(const float* __restrict__ rf, float* __restrict__ bc,
+                                                    float* __restrict__ bsc, float* __restrict__ xc, int nf, int nc,
+                                                    int halfc, float inv_c, int bx, int by, int bz) {
+    const int K = bx * BX + threadIdx.x;
+    const int J = by * BY + threadIdx.y;
+    const int I = bz;
     if (K >= nc || J >= nc) return;
     const float w[3] = {0.25f, 0.5f, 0.25f};
     float v[27];
@@ -456,6 +469,15 @@ __global__ void __launch_bounds__(BX* BY) k_restrict_split(const float* __restri
     bc[q] = acc;
     bsc[q] = bsv;
     if (FIRST_X && !(Lc & 1)) xc[q] = div6(bsv);
+}
+
+template <bool FIRST_X>
+__global__ void __launch_bounds__(BX* BY) k_restrict_split(const float* __restrict__ rf, float* __restrict__ bc,
+                                                           float* __restrict__ bsc, float* __restrict__ xc, int nf,
+                                                           int nc, int halfc, float inv_c) {
+    pdl_wait();
+    pdl_trigger();
+    restrict_split_body<FIRST_X>(rf, bc, bsc, xc, nf, nc, halfc, inv_c, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // One fine point of a prolongation cell: x_f += sum over the present coarse neighbours (in the
@@ -514,13 +536,11 @@ __device__ __forceinline__ float prolong_sum(const float (&X)[2][2][2], const bo
 // around the cell once.  ALL = false: only the colour-0 fine points ((a + b + c) even), the only
 // ones the first post-smoothing pass reads.  The coarse level is split (odd nc) or natural.
 template <bool SPLIT_C, bool ALL>
-__global__ void __launch_bounds__(BX* BY) k_prolong_split(const float* __restrict__ xc, float* __restrict__ xf,
-                                                          int nc, int halfc, int nf, int halff) {
-    pdl_wait();
-    pdl_trigger();
-    const int K = blockIdx.x * BX + threadIdx.x;
-    const int J = blockIdx.y * BY + threadIdx.y;
-    const int I = blockIdx.z;
+__device__ __forceinline__ void prolong_split_body(const float* __restrict__ xc, float* __restrict__ xf, int nc,
+                                                   int halfc, int nf, int halff, int bx, int by, int bz) {
+    const int K = bx * BX + threadIdx.x;
+    const int J = by * BY + threadIdx.y;
+    const int I = bz;
     if (K > nc || J > nc) return;
     const bool pi[2] = {I >= 1, I < nc}, pj[2] = {J >= 1, J < nc}, pk[2] = {K >= 1, K < nc};
     float X[2][2][2];
@@ -564,6 +584,14 @@ __global__ void __launch_bounds__(BX* BY) k_prolong_split(const float* __restric
         if (ia) prolong_point<1, 0, 0>(X, pi, pj, pk, xf, I, J, K, nf, halff);
         if (ia && jb && kc) prolong_point<1, 1, 1>(X, pi, pj, pk, xf, I, J, K, nf, halff);
     }
+}
+
+template <bool SPLIT_C, bool ALL>
+__global__ void __launch_bounds__(BX* BY) k_prolong_split(const float* __restrict__ xc, float* __restrict__ xf,
+                                                          int nc, int halfc, int nf, int halff) {
+    pdl_wait();
+    pdl_trigger();
+    prolong_split_body<SPLIT_C, ALL>(xc, xf, nc, halfc, nf, halff, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // b32 = RN32(r), bs32 = RN32(b32 * inv) into the split layout at the finest level; WRITE_X: also
@@ -726,10 +754,8 @@ __device__ __forceinline__ void with_tail_n(int n, int n_next, F&& f) {
 }
 
 template <class T, bool SPLIT_IO>
-__global__ void __launch_bounds__(1024) k_mg_tail(const T* __restrict__ b_g, const T* __restrict__ bs_g,
-                                                 T* __restrict__ x_g, TailParams tp) {
-    pdl_wait();
-    pdl_trigger();
+__device__ __forceinline__ void mg_tail_body(const T* __restrict__ b_g, const T* __restrict__ bs_g,
+                                             T* __restrict__ x_g, const TailParams& tp) {
     extern __shared__ __align__(16) unsigned char tail_smem[];
     T* base = reinterpret_cast<T*>(tail_smem);
     T *X[kMaxTail], *B[kMaxTail], *BS[kMaxTail];
@@ -796,6 +822,14 @@ __global__ void __launch_bounds__(1024) k_mg_tail(const T* __restrict__ b_g, con
         const int n = tp.n[0], N = n * n * n;
         for (int p = threadIdx.x; p < N; p += blockDim.x) x_g[SPLIT_IO ? split_at(p, tp.half) : p] = X[0][p];
     }
+}
+
+template <class T, bool SPLIT_IO>
+__global__ void __launch_bounds__(1024) k_mg_tail(const T* __restrict__ b_g, const T* __restrict__ bs_g,
+                                                 T* __restrict__ x_g, TailParams tp) {
+    pdl_wait();
+    pdl_trigger();
+    mg_tail_body<T, SPLIT_IO>(b_g, bs_g, x_g, tp);
 }
 
 }  // namespace

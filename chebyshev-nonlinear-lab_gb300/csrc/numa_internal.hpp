@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstddef>
 #include <cstdint>
+#include <functional>
 #include <memory>
 #include <vector>
 
@@ -608,6 +609,35 @@ private:
     int device_;
     int active_;
     std::vector<std::unique_ptr<BatchWorker>> workers_;
+};
+
+// Tile shapes of the batched solver's kernels (batch_solver.cu), picked by its autotuner:
+// planes a thread marches in the residual and Jacobian stencils, elements a block of the
+// element-wise passes (Gram-Schmidt, solution update, line-search step) covers.
+struct BatchTuning {
+    int planes = 8;
+    int elems_per_block = 16384;
+};
+
+// Many Bratu3D instances of uneven size (n = 2^k - 1, 31 ... 1023) and lambda solved together by
+// the mixed Newton-Krylov path, one launch per operation over a packed instance table.
+class BatchSolver {
+public:
+    BatchSolver(Context& ctx, const numa_batch_instance* inst, size_t count, const KrylovParams& p);
+    ~BatchSolver();
+    // u0 = 0 for every instance; x_out (may be null): the solutions, packed in the caller's order.
+    void solve(double* x_out, numa_batch_result* results, double* seconds);
+    size_t instances() const;
+    size_t total_unknowns() const;
+    BatchTuning tuning() const;
+    void set_tuning(const BatchTuning& t);
+    // One warm and one timed batch for every (planes[a], elems[b]) pair; keeps and returns the fastest.
+    BatchTuning autotune(const int* planes, int np, const int* elems, int ne, double* seconds);
+
+    struct Impl;
+
+private:
+    std::unique_ptr<Impl> impl_;
 };
 
 // x holds x0 on entry and the final iterate on return.

@@ -82,6 +82,11 @@ class BatchResult(C.Structure):
                 ("seconds", C.c_double)]
 
 
+class BatchTuning(C.Structure):
+    """numa_batch_tuning: tile shapes of the batched solver."""
+    _fields_ = [("planes", C.c_int32), ("elems_per_block", C.c_int32), ("reserved", C.c_int32 * 6)]
+
+
 class KrylovResult(C.Structure):
     """numa_krylov_result: KrylovResult (krylov_newton.hpp:40-49) plus timers."""
     _fields_ = [
@@ -246,6 +251,13 @@ SIGNATURES = {
     "numa_gpu_learned_train": ([_P, C.POINTER(LearnedTrainParams), C.POINTER(LearnedTrainReport)], _I),
     "numa_gpu_provider_create_learned": ([_P, _SZ, _P, _D, _PP], _I),
     "numa_gpu_provider_learned_stats": ([_P, C.POINTER(_SZ), C.POINTER(_SZ)], _I),
+    "numa_gpu_bsolver_create": ([_P, C.POINTER(BatchInstance), _SZ, C.POINTER(KrylovParams), _PP], _I),
+    "numa_gpu_bsolver_destroy": ([_P], _I),
+    "numa_gpu_bsolver_solve": ([_P, _F64P, C.POINTER(BatchResult), _F64P], _I),
+    "numa_gpu_bsolver_get_tuning": ([_P, C.POINTER(BatchTuning)], _I),
+    "numa_gpu_bsolver_set_tuning": ([_P, C.POINTER(BatchTuning)], _I),
+    "numa_gpu_bsolver_autotune": ([_P, C.POINTER(C.c_int), _I, C.POINTER(C.c_int), _I, C.POINTER(BatchTuning),
+                                   _F64P], _I),
 }
 
 _lib = None
@@ -1205,3 +1217,88 @@ class BatchExecutor:
         if rc != OK:
             raise NumaGPUError(rc, "numa_gpu_batch_solve", self.lib.numa_gpu_batch_last_error().decode())
         return [to_dict(r) for r in res], wall.value
+
+
+class BatchSolver:
+    """numa_gpu_bsolver_*: many Bratu3D instances (n = 2^k - 1, 31 ... 1023) solved together by the
+    mixed Newton-Krylov path, one launch per operation over all of them, scalar decisions on the
+    device, Arnoldi steps and line-search trials as captured CUDA graphs."""
+
+    def __init__(self, ctx: Context, instances, params: KrylovParams | None = None):
+        self.ctx, self.lib = ctx, ctx.lib
+        self.instances = [(int(n), float(lam)) for n, lam in instances]
+        arr = (BatchInstance * len(self.instances))(*[BatchInstance(n, lam) for n, lam in self.instances])
+        p = params if params is not None else default_params()
+        h = C.c_void_p()
+        ctx.check(self.lib.numa_gpu_bsolver_create(ctx.h, arr, len(self.instances), C.byref(p), C.byref(h)),
+                  "bsolver_create")
+        self.h = h
+        ctx._adopt(self)
+
+    def close(self):
+        if self.h:
+            self.lib.numa_gpu_bsolver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, want_x: bool = False):
+        """Returns (per-instance result dicts, seconds, solutions or None) in the order given."""
+        res = (BatchResult * len(self.instances))()
+        secs = C.c_double()
+        x = None
+        if want_x:
+            x = np.empty(sum(n ** 3 for n, _ in self.instances))
+        self.ctx.check(self.lib.numa_gpu_bsolver_solve(self.h, x.ctypes.data_as(_F64P) if x is not None else None, res,
+                                                       C.byref(secs)), "bsolver_solve")
+        xs = None
+        if x is not None:
+            xs, o = [], 0
+            for n, _ in self.instances:
+                xs.append(x[o:o + n ** 3])
+                o += n ** 3
+        return [to_dict(r) for r in res], secs.value, xs
+
+    def tuning(self) -> dict:
+        t = BatchTuning()
+        self.ctx.check(self.lib.numa_gpu_bsolver_get_tuning(self.h, C.byref(t)), "bsolver_get_tuning")
+        return {"planes": t.planes, "elems_per_block": t.elems_per_block}
+
+    def set_tuning(self, planes: int, elems_per_block: int):
+        t = BatchTuning(planes, elems_per_block)
+        self.ctx.check(self.lib.numa_gpu_bsolver_set_tuning(self.h, C.byref(t)), "bsolver_set_tuning")
+
+    def autotune(self, planes=(2, 4, 8), elems=(8192, 16384, 32768), cache: str | Path | None = None) -> dict:
+        """Picks the fastest tile shapes on this batch (one warm and one timed batch per candidate); with
+        `cache`, a JSON file of earlier choices keyed by the batch's size histogram is read first and
+        updated after tuning."""
+        import json
+        key = None
+        if cache is not None:
+            hist = {}
+            for n, _ in self.instances:
+                hist[n] = hist.get(n, 0) + 1
+            key = ",".join(f"{n}x{c}" for n, c in sorted(hist.items()))
+            path = Path(cache)
+            book = json.loads(path.read_text()) if path.exists() else {}
+            if key in book:
+                self.set_tuning(book[key]["planes"], book[key]["elems_per_block"])
+                return dict(book[key], cached=True)
+        pa = (C.c_int * len(planes))(*planes)
+        ea = (C.c_int * len(elems))(*elems)
+        secs = (C.c_double * (len(planes) * len(elems)))()
+        t = BatchTuning()
+        self.ctx.check(self.lib.numa_gpu_bsolver_autotune(self.h, pa, len(planes), ea, len(elems), C.byref(t), secs),
+                       "bsolver_autotune")
+        out = {"planes": t.planes, "elems_per_block": t.elems_per_block,
+               "seconds": {f"{p}x{e}": float(secs[a * len(elems) + b]) for a, p in enumerate(planes)
+                           for b, e in enumerate(elems)}}
+        if key is not None:
+            book[key] = {"planes": t.planes, "elems_per_block": t.elems_per_block}
+            path.parent.mkdir(parents=True, exist_ok=True)
+            path.write_text(json.dumps(book, indent=1))
+        return out

@@ -502,6 +502,37 @@ int numa_gpu_batch_solve(numa_gpu_batch* b, const numa_batch_instance* inst, siz
 /* Message of the last failing batched call in this process ("" if it succeeded). */
 const char* numa_gpu_batch_last_error(void);
 
+/* Batched solves in one set of launches (no counterpart in the reference, whose campaign runner
+ * solves instances one after another, apps/run_campaign.cpp:344-475): every instance advances
+ * through newton_krylov (methods/krylov_newton.hpp:69-114) in lockstep, FGMRES(restart) with the
+ * mixed path's FP32 basis and one-pass classical Gram-Schmidt, right-preconditioned by the FP32
+ * V(2,2) multigrid cycle, FP32 Jacobian products, FP64 residual, update and least squares.  One
+ * kernel launch per operation covers all instances (a packed instance table; the multigrid levels
+ * of one size from all instances in one launch); every scalar decision (forcing term, Givens
+ * rotations, restart, Armijo line search, convergence) is taken on the device per instance; each
+ * Arnoldi step and each line-search trial is a captured CUDA graph.  Grid sizes n = 2^k - 1 with
+ * 31 <= n <= 1023; u0 = 0.  Created on a context (its stream and device); the packed vectors, the
+ * Krylov basis and the multigrid pools stay allocated until destroy. */
+typedef struct numa_gpu_bsolver numa_gpu_bsolver;
+typedef struct numa_batch_tuning {
+    int32_t planes;          /* planes a thread marches in the residual and Jacobian stencils */
+    int32_t elems_per_block; /* elements a block of the element-wise passes covers */
+    int32_t reserved[6];
+} numa_batch_tuning;
+int numa_gpu_bsolver_create(numa_gpu_ctx* ctx, const numa_batch_instance* inst, size_t count,
+                            const numa_krylov_params* p, numa_gpu_bsolver** out);
+int numa_gpu_bsolver_destroy(numa_gpu_bsolver* s);
+/* Solves every instance from u0 = 0.  results[i] for inst[i]; x_out (may be NULL): host buffer of
+ * sum n_i^3 doubles receiving the solutions packed in the order of inst; seconds (may be NULL):
+ * wall time of the call. */
+int numa_gpu_bsolver_solve(numa_gpu_bsolver* s, double* x_out, numa_batch_result* results, double* seconds);
+int numa_gpu_bsolver_get_tuning(const numa_gpu_bsolver* s, numa_batch_tuning* t);
+int numa_gpu_bsolver_set_tuning(numa_gpu_bsolver* s, const numa_batch_tuning* t);
+/* Tile-shape autotuner: one warm and one timed batch for each (planes[a], elems[b]) pair, the
+ * fastest kept and returned in *chosen; seconds[a * ne + b] (may be NULL) = the timed batch. */
+int numa_gpu_bsolver_autotune(numa_gpu_bsolver* s, const int* planes, int np, const int* elems, int ne,
+                              numa_batch_tuning* chosen, double* seconds);
+
 /* ---------------------------------------------------------------- V-cycle without allocation */
 /* No counterpart in the reference.  For callers that cannot allocate device memory when they
  * apply the preconditioner: another library's solver callback that must not allocate or free on

@@ -50,13 +50,16 @@ def test_reference_arm_other_ranks_do_nothing(capsys, monkeypatch):
     assert capsys.readouterr().out == ""
 
 
-@pytest.mark.parametrize("n", [15])
-def test_reference_arm_prints_line(capsys, monkeypatch, n):
+def test_reference_arm_prints_line(capsys, monkeypatch):
+    """The reference arm solves the configured grid itself (no scaled sample): here 31^3, one timed
+    solve and the single-thread one; the reference's own build where it was compiled, else the port."""
     import json
     import bench
     monkeypatch.delenv("RANK", raising=False)
-    assert bench.main(["--impl", "reference", "--steps", "1", "--warmup", "0", "--n", "31",
-                       "--cpu-sample-n", str(n)]) == 0
+    assert bench.main(["--impl", "reference", "--steps", "1", "--warmup", "0", "--n", "31"]) == 0
     line = json.loads(capsys.readouterr().out.strip())
     assert line["impl"] == "reference" and line["unit"] == "s" and line["higher_is_better"] is False
-    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+    assert line["steps"] == 1 and line["warmup"] == 0 and "steps_requested" not in line
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] in ("port", "reference")
+    assert line["config"]["n"] == 31 and "31^3 itself" in line["cpu_baseline"]["sample"]
+    assert line["cpu_baseline"]["single_thread"]["counts"] == [5, 12, 17]
