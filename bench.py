@@ -78,7 +78,7 @@ def parse_args(argv=None):
     ap.add_argument("--cpu-reps", type=int, default=2, help="all-core CPU solves of the cpu_baseline leg")
     ap.add_argument("--ref-budget", type=float, default=270.0,
                     help="seconds the reference arm may spend on its warm-up and timed solves")
-    ap.add_argument("--kernel-case", choices=["none", "vcycle", "solve", "conv", "bruss", "stencils", "eval"],
+    ap.add_argument("--kernel-case", choices=["none", "vcycle", "solve", "conv", "bruss", "stencils", "eval", "batch"],
                     default="none",
                     help="profiling driver: run only this small case (for ncu)")
     return ap.parse_args(argv)
@@ -774,6 +774,19 @@ def run_kernel_case(G, ctx, args) -> int:
         for _ in range(max(1, args.steps)):
             G.diag_conv3d(ctx, nc, xin, w)
         print(json.dumps({"kernel_case": "conv", "n": nc, "launches": ctx.kernel_launches()}))
+        return 0
+    if args.kernel_case == "batch":
+        # the batched configuration through the batched solver: one warm batch, then args.steps batches
+        inst = G.batch_config_instances(128, seed=42)
+        bs = G.BatchSolver(ctx, inst, params_for(G, "mixed", "cgs1"))
+        bs.solve()
+        t = 0.0
+        for _ in range(max(1, args.steps)):
+            _, secs, _ = bs.solve()
+            t += secs
+        bs.close()
+        print(json.dumps({"kernel_case": "batch", "instances": len(inst), "s_per_batch": t / max(1, args.steps),
+                          "launches": ctx.kernel_launches()}))
         return 0
     if args.kernel_case == "eval":
         # the residual evaluation with the mixed path's cache, on a smooth iterate of the solve's size
