@@ -431,10 +431,42 @@ def run_ours(args) -> int:
                                            max(1, args.steps // 2), 1, dist, stream)
             x_l = x.numpy() if dist.rank == 0 else None
             applies, fallbacks = pcl.learned_stats()
+            # held-out lambda at 127^3: a network trained the same way on that grid's hierarchy
+            held = []
+            if dist.rank == 0:
+                n2 = 127
+                net2 = G.LearnedNet(ctx, 31, seed=3)
+                net2.train(n2, instances=4, states=3, rhs_per_state=2, krylov_per_state=8, epochs=8, batch=4,
+                           lr=2e-3, seed=11)
+                pm2 = G.Provider.poisson_mg(ctx, n2, precision=G.FP32)
+                pl2 = G.Provider.learned(ctx, n2, net2, stall=0.9)
+                x2 = ctx.vec(n2 ** 3)
+                for lam2 in (2.7, 5.3):
+                    op2 = G.Bratu3D(ctx, n2, lam2)
+                    row = {"n": n2, "lambda": lam2}
+                    for tag, pcx in (("mixed", pm2), ("learned", pl2)):
+                        x2.fill(0.0)
+                        rr = G.solve(op2, x2, "nk", params_for(G, "mixed", args.orth), pcx)
+                        row[tag] = [rr["iters"], rr["n_lin_iters"], rr["converged"]]
+                    held.append(row)
             learned = {"s": sec_l, "res": res_l, "x": x_l, "training": trep, "applies": applies,
-                       "fallbacks": fallbacks}
+                       "fallbacks": fallbacks, "held_out": held}
         except G.NumaGPUError as exc:
             learned = {"skipped": str(exc)}
+
+    # the FP32 V-cycle with Jacobian-aware coarse levels (levels n <= 15 solve with -Lap_h - lambda e^u)
+    jac = None
+    if dist.rank == 0:
+        pcj = G.Provider.jacobian_mg(ctx, n)
+        sec_j, res_j, _ = timed_solves(G, ctx, op, pcj, x, u0, args.method, params_for(G, "mixed", args.orth),
+                                       max(1, args.steps // 2), 1, dist, stream)
+        x_j = x.numpy()
+        jac = {"s": sec_j, "counts": {k: res_j[k] for k in ("iters", "n_F", "n_JVP", "n_lin_iters", "n_prec",
+                                                             "converged")},
+               "res_rel": res_j["res"] / res_j["res0"], "x": x_j,
+               "note": "mixed path with the Jacobian-aware coarse levels: the V-cycle's levels n <= 15 solve with "
+                       "-Lap_h - c (c = lambda e^u restricted) instead of -Lap_h; fine levels, FGMRES and the "
+                       "FP32 products as on the mixed path"}
 
     # batched solves: 128 instances, n from {31, 63, 127}, lambda ~ U[1, 6.5] (seeded), mixed path
     batched = None
@@ -557,6 +589,10 @@ def run_ours(args) -> int:
                                        "preconditioner"},
             "chebyshev": cheb,
             "learned_mixed": learned_summary(learned, fp64_sec, x_head if args.path == "fp64" else x_other),
+            "jacobian_coarse": (None if jac is None else dict(
+                {k: v for k, v in jac.items() if k != "x"},
+                rel_err_vs_fp64=float(np.linalg.norm(jac["x"] - (x_head if args.path == "fp64" else x_other)) /
+                                      np.linalg.norm(x_head if args.path == "fp64" else x_other)))),
             "batched": batched,
             "brusselator2d": bruss,
             "clocks": clk.summary(),
@@ -735,6 +771,7 @@ def learned_summary(learned, fp64_sec, x_fp64):
         "counts": {k: r[k] for k in ("iters", "n_JVP", "n_lin_iters", "n_prec", "converged")},
         "rel_err_vs_fp64": float(np.linalg.norm(learned["x"] - x_fp64) / np.linalg.norm(x_fp64)),
         "net_applies": learned["applies"], "fallbacks_to_vcycle": learned["fallbacks"],
+        "held_out_127": learned.get("held_out"),
         "training": {k: learned["training"][k] for k in ("samples", "gen_seconds", "train_seconds", "loss_first",
                                                           "loss_last", "target_ms")},
         "note": "FGMRES(30) preconditioned by the FP32 V-cycle plus a 4-level 3D conv net (BF16, tcgen05) on the "

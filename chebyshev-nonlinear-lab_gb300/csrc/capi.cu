@@ -671,6 +671,18 @@ int numa_gpu_provider_create_poisson_mg(numa_gpu_ctx* ctx, size_t n, int pre, in
     });
 }
 
+int numa_gpu_provider_create_jacobian_mg(numa_gpu_ctx* ctx, size_t n, int pre, int post, numa_gpu_provider** out) {
+    if (!ctx || !out || pre < 0 || post < 1) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        auto h = std::make_unique<numa_gpu_provider>();
+        h->ctx = ctx;
+        h->impl = make_jacobian_mg_provider(*ctx->impl, n, pre, post);
+        h->N = n * n * n;
+        *out = h.release();
+    });
+}
+
 int numa_gpu_provider_create_jacobi(numa_gpu_bratu3d* op, numa_gpu_provider** out) {
     if (!op || !out) return NUMA_GPU_ERR_INVALID_ARGUMENT;
     *out = nullptr;
@@ -1617,6 +1629,12 @@ int numa_gpu_diag_div(const numa_gpu_vec* a, double b, numa_gpu_vec* out) {
         need(out->n == a->n, NUMA_GPU_ERR_SIZE_MISMATCH, "output length differs");
         diag_div(*a->ctx->impl, a->d, b, out->d, a->n);
     });
+}
+
+int numa_gpu_diag_conv3d_wgrad(numa_gpu_ctx* ctx, size_t n, int cin, int cout, const float* x, const float* g,
+                               float* dw, float* db) {
+    if (!ctx || !x || !g || !dw || !db || n == 0 || n > 63) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(ctx, [&] { diag_conv3d_wgrad(*ctx->impl, (int)n, cin, cout, x, g, dw, db); });
 }
 
 int numa_gpu_diag_conv3d(numa_gpu_ctx* ctx, size_t n, int cin, int cout, int adjoint, const float* x,

@@ -51,6 +51,30 @@ private:
     PoissonMG mg_;
 };
 
+// The FP32 V-cycle with Jacobian-aware coarse levels, bound at each iterate: make() restricts the
+// iterate's coefficient c = lambda e^x (the operator's cache) down to the one-CTA tail.
+class JacobianMGProvider : public Provider {
+public:
+    JacobianMGProvider(Context& ctx, size_t n, int pre, int post) : mg_(ctx, n, pre, post, NUMA_GPU_FP32, 0) {
+        if (!mg_.supports_coarse_jacobian() || !mg_.supports_out32())
+            throw Status(NUMA_GPU_ERR_NOT_SUPPORTED,
+                         "Jacobian-aware multigrid: the grid needs an odd hierarchy down to a tail of n <= 15");
+    }
+    void make(const double*, const double* c) override {
+        if (!c) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "Jacobian-aware multigrid: the operator keeps no coefficient");
+        mg_.set_coarse_coefficient(c);
+    }
+    void apply(const double* r, double* z) override { mg_.apply(r, z); }
+    bool has_apply32() const override { return true; }
+    void apply32(const double* r, float* z32) override { mg_.apply32(r, z32); }
+    bool has_apply32f() const override { return true; }
+    void apply32f(const float* r32, float* z32) override { mg_.apply32f(r32, z32); }
+    int kind() const override { return NUMA_GPU_PRECOND_JACOBIAN_MG; }
+
+private:
+    PoissonMG mg_;
+};
+
 __global__ void k_jacobi_apply(const double* __restrict__ r, const double* __restrict__ d, double* __restrict__ z,
                                size_t N) {
     pdl_wait();
@@ -325,6 +349,9 @@ std::unique_ptr<Provider> make_mg_provider(Context& ctx, size_t n, int pre, int 
     return std::make_unique<MGProvider>(ctx, n, pre, post, precision, max_levels);
 }
 std::unique_ptr<Provider> make_jacobi_provider(Bratu3D& op) { return std::make_unique<JacobiProvider>(op); }
+std::unique_ptr<Provider> make_jacobian_mg_provider(Context& ctx, size_t n, int pre, int post) {
+    return std::make_unique<JacobianMGProvider>(ctx, n, pre, post);
+}
 
 KrylovParams params_from_c(const numa_krylov_params* c) {
     KrylovParams p;

@@ -177,61 +177,32 @@ __global__ void k_relu_mask_planes(uint4* __restrict__ g, const uint4* __restric
     }
 }
 
-// dW[tap][ci][co] += sum_v x[v + tap][ci] g[v][co] and (tap 13) db[co] += sum_v g[v][co] over the
-// interior voxels, FP32 on the CUDA cores: each block stages 64 voxels of x (at the tap's offset)
-// and g in shared memory, its threads own (ci, co) pairs, and the block's partial sums go to dW
-// with one atomic add per pair.  Grid: (27 taps, voxel-chunk groups).
-template <int CIN, int COUT>
-__global__ void __launch_bounds__(256) k_conv_dw(const uint4* __restrict__ x, const uint4* __restrict__ g, VoxGrid gr,
-                                                 float* __restrict__ dw, float* __restrict__ db) {
-    constexpr int CH = 64, PAIRS = CIN * COUT, PER = (PAIRS + 255) / 256;
-    __shared__ float xs[CH][CIN + 1];
-    __shared__ float gs[CH][COUT + 1];
-    const int tap = blockIdx.x;
-    const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+// dw[e] += sum over the CTAs c of part[c][e], in CTA order (the tensor-core weight gradient's partials)
+__global__ void k_dw_reduce(const float* __restrict__ part, int nparts, int count, float* __restrict__ dw) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += stride) {
+        float s = 0.0f;
+        for (int c = 0; c < nparts; ++c) s += part[(size_t)c * count + e];
+        dw[e] += s;
+    }
+}
+
+// db[co] += sum over the interior voxels of g[v][co]: one block per output channel, FP32 sums per
+// thread, the block's total in FP64 (deterministic).
+__global__ void __launch_bounds__(256) k_bias_grad(const uint4* __restrict__ g, VoxGrid gr, float* __restrict__ db) {
+    const int co = blockIdx.x, pl = co / 8, q = co % 8;
     const int N = gr.n * gr.n * gr.n;
-    float acc[PER];
-#pragma unroll
-    for (int q = 0; q < PER; ++q) acc[q] = 0.0f;
-    float bacc = 0.0f;
-    for (int v0 = blockIdx.y * CH; v0 < N; v0 += gridDim.y * CH) {
-        __syncthreads();
-        for (int e = threadIdx.x; e < CH * (CIN / 8 + COUT / 8); e += 256) {
-            const int vv = e % CH, pl = e / CH, v = v0 + vv;
-            float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            if (v < N) {
-                const int xx = v % gr.n, yy = (v / gr.n) % gr.n, zz = v / (gr.n * gr.n);
-                if (pl < CIN / 8) unpack8(x[prow(gr, pl, xx + dx, yy + dy, zz + dz)], f);
-                else unpack8(g[prow(gr, pl - CIN / 8, xx, yy, zz)], f);
-            }
-            if (pl < CIN / 8) {
-#pragma unroll
-                for (int q = 0; q < 8; ++q) xs[vv][8 * pl + q] = f[q];
-            } else {
-#pragma unroll
-                for (int q = 0; q < 8; ++q) gs[vv][8 * (pl - CIN / 8) + q] = f[q];
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < PER; ++q) {
-            const int pair = threadIdx.x + 256 * q;
-            if (pair < PAIRS) {
-                const int ci = pair / COUT, co = pair % COUT;
-                float s = acc[q];
-                for (int vv = 0; vv < CH; ++vv) s = __fmaf_rn(xs[vv][ci], gs[vv][co], s);
-                acc[q] = s;
-            }
-        }
-        if (tap == 13 && threadIdx.x < COUT)
-            for (int vv = 0; vv < CH; ++vv) bacc += gs[vv][threadIdx.x];
+    float s = 0.0f;
+    for (int v = threadIdx.x; v < N; v += 256) {
+        const int xx = v % gr.n, yy = (v / gr.n) % gr.n, zz = v / (gr.n * gr.n);
+        float f[8];
+        unpack8(g[prow(gr, pl, xx, yy, zz)], f);
+        s += f[q];
     }
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-        const int pair = threadIdx.x + 256 * q;
-        if (pair < PAIRS) atomicAdd(&dw[(size_t)tap * PAIRS + pair], acc[q]);
-    }
-    if (tap == 13 && threadIdx.x < COUT) atomicAdd(&db[threadIdx.x], bacc);
+    double acc[1] = {(double)s};
+    __shared__ double sm[1][32];
+    block_sum<1>(acc, sm);
+    if (threadIdx.x == 0) db[co] += (float)acc[0];
 }
 
 // 16-channel feature planes: channel 0 = sr r, 1 = sc c, 2 = sz z, 3..15 = 0 (FP32 natural in).
@@ -329,16 +300,33 @@ void planes_relu_mask(Context& ctx, uint4* g, const uint4* y, const VoxGrid& gr,
     ctx.count_launch();
 }
 
-void conv_dw(Context& ctx, const VoxGrid& gr, int cin, int cout, const uint4* x, const uint4* g, float* dw, float* db) {
-    const int N = gr.n * gr.n * gr.n;
-    const int chunks = (N + 63) / 64;
-    const dim3 grid(27, (unsigned)std::max(1, std::min(chunks, 16)));
-    if (cin == 16 && cout == 16) k_conv_dw<16, 16><<<grid, 256, 0, ctx.stream>>>(x, g, gr, dw, db);
-    else if (cin == 16 && cout == 32) k_conv_dw<16, 32><<<grid, 256, 0, ctx.stream>>>(x, g, gr, dw, db);
-    else if (cin == 32 && cout == 16) k_conv_dw<32, 16><<<grid, 256, 0, ctx.stream>>>(x, g, gr, dw, db);
-    else if (cin == 32 && cout == 32) k_conv_dw<32, 32><<<grid, 256, 0, ctx.stream>>>(x, g, gr, dw, db);
+template <int CIN, int COUT>
+void launch_conv_dw(Context& ctx, const VoxGrid& gr, const uint4* x, const uint4* g, float* dw, float* db,
+                    DeviceArray<float>& part, unsigned* err) {
+    const size_t smem = dw_smem_bytes<CIN, COUT>(gr);
+    const int lim = set_dynamic_smem_limit(ctx, k_conv_dw_tc<CIN, COUT>);
+    if (smem > (size_t)lim) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "weight-gradient tile exceeds shared memory");
+    // one CTA per SM at most (512 tensor-memory columns at C_out = 32), each accumulating its tiles
+    const int grid = std::max(1, std::min(gr.tiles, ctx.sm_count));
+    const int count = 27 * CIN * COUT;
+    part.resize((size_t)grid * count);
+    k_conv_dw_tc<CIN, COUT><<<grid, 128, smem, ctx.stream>>>(x, g, gr, part.p, err);
+    k_dw_reduce<<<(count + 255) / 256, 256, 0, ctx.stream>>>(part.p, grid, count, dw);
+    k_bias_grad<<<COUT, 256, 0, ctx.stream>>>(g, gr, db);
+    ctx.count_launch(3);
+}
+
+// dW += the weight gradient (BF16 operands on the tensor cores, FP32 accumulation), db += the bias
+// gradient; part is the caller's scratch for the per-CTA partials, err the mbarrier give-up flag.
+void conv_dw(Context& ctx, const VoxGrid& gr, int cin, int cout, const uint4* x, const uint4* g, float* dw, float* db,
+             DeviceArray<float>& part, unsigned* err) {
+    if (gr.n > 63) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "weight gradient: grid above 63^3");
+    if (cin == 16 && cout == 16) launch_conv_dw<16, 16>(ctx, gr, x, g, dw, db, part, err);
+    else if (cin == 16 && cout == 32) launch_conv_dw<16, 32>(ctx, gr, x, g, dw, db, part, err);
+    else if (cin == 32 && cout == 16) launch_conv_dw<32, 16>(ctx, gr, x, g, dw, db, part, err);
+    else if (cin == 32 && cout == 32) launch_conv_dw<32, 32>(ctx, gr, x, g, dw, db, part, err);
     else throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "weight gradient: channel counts must be 16 or 32");
-    ctx.count_launch();
+    ctx.check_launch("conv_dw_tc");
 }
 
 void planes_features(Context& ctx, const float* r, const float* c, const float* z, const float* scales, uint4* planes,
@@ -397,6 +385,34 @@ void diag_conv3d(Context& ctx, int n, int cin, int cout, int flip, const float* 
     NUMA_CUDA(cudaMemcpyAsync(y_h, y.p, N * co * sizeof(float), cudaMemcpyDeviceToHost, ctx.stream));
     ctx.sync();
     if (herr) throw Status(NUMA_GPU_ERR_CUDA, "tensor-core convolution: an mbarrier wait gave up");
+}
+
+// One layer's weight and bias gradients from host buffers (diagnostic and test entry point):
+// dw[tap][ci][co] = sum_v x[v + tap][ci] g[v][co], db[co] = sum_v g[v][co], x [n^3][cin], g [n^3][cout].
+void diag_conv3d_wgrad(Context& ctx, int n, int cin, int cout, const float* x_h, const float* g_h, float* dw_h,
+                       float* db_h) {
+    if (n < 1) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "grid size must be positive");
+    const VoxGrid g = make_voxgrid(n);
+    const size_t N = (size_t)n * n * n;
+    DeviceArray<float> x(N * cin), gr(N * cout), dw(27 * (size_t)cin * cout), db(cout), part;
+    DeviceArray<uint4> xp((size_t)(cin / 8) * g.rows), gp((size_t)(cout / 8) * g.rows);
+    DeviceArray<unsigned> err(1);
+    NUMA_CUDA(cudaMemsetAsync(xp.p, 0, xp.n * sizeof(uint4), ctx.stream));
+    NUMA_CUDA(cudaMemsetAsync(gp.p, 0, gp.n * sizeof(uint4), ctx.stream));
+    NUMA_CUDA(cudaMemsetAsync(dw.p, 0, dw.n * sizeof(float), ctx.stream));
+    NUMA_CUDA(cudaMemsetAsync(db.p, 0, db.n * sizeof(float), ctx.stream));
+    NUMA_CUDA(cudaMemsetAsync(err.p, 0, sizeof(unsigned), ctx.stream));
+    NUMA_CUDA(cudaMemcpyAsync(x.p, x_h, N * cin * sizeof(float), cudaMemcpyHostToDevice, ctx.stream));
+    NUMA_CUDA(cudaMemcpyAsync(gr.p, g_h, N * cout * sizeof(float), cudaMemcpyHostToDevice, ctx.stream));
+    pack_act(ctx, x.p, xp.p, g, cin);
+    pack_act(ctx, gr.p, gp.p, g, cout);
+    conv_dw(ctx, g, cin, cout, xp.p, gp.p, dw.p, db.p, part, err.p);
+    unsigned herr = 0;
+    NUMA_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx.stream));
+    NUMA_CUDA(cudaMemcpyAsync(dw_h, dw.p, dw.n * sizeof(float), cudaMemcpyDeviceToHost, ctx.stream));
+    NUMA_CUDA(cudaMemcpyAsync(db_h, db.p, db.n * sizeof(float), cudaMemcpyDeviceToHost, ctx.stream));
+    ctx.sync();
+    if (herr) throw Status(NUMA_GPU_ERR_CUDA, "tensor-core weight gradient: an mbarrier wait gave up");
 }
 
 }  // namespace numa::gpu

@@ -67,6 +67,11 @@ __device__ __forceinline__ uint64_t umma_sdesc(uint32_t saddr, uint32_t lbo, uin
 __host__ __device__ constexpr uint32_t umma_idesc_bf16(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
+// The same with A and B both MN-major (the "transpose A / transpose B" bits 15 and 16): A is M x K
+// stored with M contiguous, B is K x N stored with N contiguous.
+__host__ __device__ constexpr uint32_t umma_idesc_bf16_mn(int M, int N) {
+    return umma_idesc_bf16(M, N) | (1u << 15) | (1u << 16);
+}
 
 __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                           uint32_t accumulate) {
@@ -305,6 +310,169 @@ __global__ void __launch_bounds__(128) k_conv3d_tc(const uint4* __restrict__ in,
     __syncthreads();
     tc_fence_after();
     if (warp == 0) tmem_free(tmem, kCols);
+}
+
+// ------------------------------------------------------------------------------ weight gradient
+// dW[tap][ci][co] = sum over the voxels v of x[v + tap][ci] dy[v][co] (the gradient of a layer's
+// weights), as implicit GEMMs on the tensor cores: K runs over voxel rows, and each operand is taken
+// MN-major straight from the plane layout, where a voxel row holds 8 channels in 16 bytes and 8
+// consecutive rows of one plane form a 128-byte core matrix (8 K rows x 8 channels).
+//  * A (M x K): the input's spans of a tile, as the forward kernel copies them (one span of
+//    g.span rows per dz and 8-channel plane, spans back to back).  The span of (dz, plane p) is
+//    8-channel group dz * PL + p, so the three dz taps of one (dy, dx) stack along M with a
+//    uniform group stride (the span bytes, SBO); the (dy, dx) shift is the descriptor's start
+//    address, dy (n+2) + dx rows into the spans.  M = 128 rows: 3 * C_in real ones (48 or 96),
+//    the rest read the following spans and their sums are never read.
+//  * B (K x N): the output gradient's tile of 128 rows, one 2 KB block per 8-channel plane (SBO).
+//  * D: one block of C_out FP32 columns per (dy, dx), 9 blocks, accumulated over every tile the
+//    CTA takes; the halo rows of dy are zero, so tile rows outside the grid add nothing.
+// Double-buffered: the copies of the next tile go in while the MMAs of this tile run, and a
+// buffer is refilled only after the MMAs that read it have completed (commit on an mbarrier).
+// Each CTA writes its partial dW to part[blockIdx.x]; k_dw_reduce adds the partials in CTA order.
+template <int CIN, int COUT>
+struct DwShape {
+    static constexpr int PL = CIN / 8, QL = COUT / 8;
+    static constexpr int GROUPS = 16;                              // M = 128 rows
+    static constexpr int EXTRA = GROUPS - 3 * PL;                  // spans past the second buffer
+    static constexpr uint32_t COLS = 9 * COUT <= 256 ? 256 : 512;  // tensor-memory columns
+};
+template <int CIN, int COUT>
+inline size_t dw_smem_bytes(const VoxGrid& g) {
+    using S = DwShape<CIN, COUT>;
+    return (size_t)(2 * 3 * S::PL + S::EXTRA) * g.span * 16 + (size_t)2 * S::QL * 128 * 16;
+}
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(128) k_conv_dw_tc(const uint4* __restrict__ x, const uint4* __restrict__ dy,
+                                                    VoxGrid g, float* __restrict__ part, unsigned* __restrict__ err) {
+    using S = DwShape<CIN, COUT>;
+    constexpr int PL = S::PL, QL = S::QL;
+    extern __shared__ __align__(128) unsigned char dw_smem[];
+    __shared__ __align__(8) uint64_t mbar[2];  // MMAs of the tile in buffer 0 / 1
+    __shared__ __align__(8) uint64_t lbar[2];  // copies into buffer 0 / 1
+    __shared__ uint32_t tmem_slot;
+    uint4* a_s = reinterpret_cast<uint4*>(dw_smem);
+    uint4* b_s = a_s + (size_t)(2 * 3 * PL + S::EXTRA) * g.span;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int abuf = 3 * PL * g.span;  // uint4 per A buffer
+    const int bbuf = QL * 128;         // uint4 per B buffer
+
+    // the spans past the second buffer are read by the unused rows of M: keep them finite
+    for (int e = tid; e < S::EXTRA * g.span; e += 128) a_s[(size_t)2 * abuf + e] = make_uint4(0u, 0u, 0u, 0u);
+    if (warp == 0) tmem_alloc(&tmem_slot, S::COLS);
+    if (tid == 0) {
+        mbar_init(smem_addr(&mbar[0]), 1);
+        mbar_init(smem_addr(&mbar[1]), 1);
+        mbar_init(smem_addr(&lbar[0]), 1);
+        mbar_init(smem_addr(&lbar[1]), 1);
+    }
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    constexpr uint32_t idesc = umma_idesc_bf16_mn(128, COUT);
+
+    auto issue = [&](int t, int b) {
+        const uint32_t lb = smem_addr(&lbar[b]);
+        mbar_arrive_expect_tx(lb, (uint32_t)(abuf + bbuf) * 16u);
+        const int start = g.pp + 128 * t;
+        for (int dz = 0; dz < 3; ++dz)
+            for (int p = 0; p < PL; ++p) {
+                const int q0 = start + (dz - 1) * g.pp - g.np - 1;
+                tma_bulk_g2s(smem_addr(a_s + (size_t)b * abuf + (size_t)(dz * PL + p) * g.span),
+                             x + (size_t)p * g.rows + g.front + q0, (uint32_t)g.span * 16u, lb);
+            }
+        for (int p = 0; p < QL; ++p)
+            tma_bulk_g2s(smem_addr(b_s + (size_t)b * bbuf + (size_t)p * 128), dy + (size_t)p * g.rows + g.front + start,
+                         128u * 16u, lb);
+    };
+    bool ok = true;
+    int it = 0;
+    int pend[2] = {-1, -1};  // iteration whose MMAs last read buffer 0 / 1 (not yet waited for)
+    if (tid == 0 && (int)blockIdx.x < g.tiles) issue(blockIdx.x, 0);
+    for (int t = blockIdx.x; t < g.tiles; t += gridDim.x, ++it) {
+        const int b = it & 1;
+        const int tn = t + (int)gridDim.x;
+        if (tn < g.tiles) {
+            // the other buffer is refilled once the MMAs that read it (iteration it - 1) are done
+            int free_ok = 1;
+            if (pend[b ^ 1] >= 0) {
+                free_ok = mbar_wait(smem_addr(&mbar[b ^ 1]), (uint32_t)((pend[b ^ 1] >> 1) & 1), kConvWaitLimit) ? 1 : 0;
+                pend[b ^ 1] = -1;
+            }
+            if (!__syncthreads_and(free_ok)) {
+                ok = false;
+                break;
+            }
+            if (tid == 0) issue(tn, b ^ 1);
+        }
+        const int landed = mbar_wait(smem_addr(&lbar[b]), (uint32_t)((it >> 1) & 1), kConvWaitLimit) ? 1 : 0;
+        if (!__syncthreads_and(landed)) {
+            ok = false;
+            break;
+        }
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t a0 = smem_addr(a_s + (size_t)b * abuf), b0 = smem_addr(b_s + (size_t)b * bbuf);
+#pragma unroll 1
+            for (int pr = 0; pr < 9; ++pr) {
+                const int ddy = pr / 3, ddx = pr % 3;
+#pragma unroll
+                for (int kk = 0; kk < 8; ++kk) {
+                    const uint32_t aa = a0 + (uint32_t)((ddy * g.np + ddx + 16 * kk) * 16);
+                    const uint32_t bb = b0 + (uint32_t)(16 * kk * 16);
+                    umma_bf16(tmem + (uint32_t)(pr * COUT), umma_sdesc(aa, 128, (uint32_t)g.span * 16),
+                              umma_sdesc(bb, 128, 128 * 16), idesc, (it > 0 || kk > 0) ? 1u : 0u);
+                }
+            }
+            umma_commit(smem_addr(&mbar[b]));
+        }
+        pend[b] = it;
+    }
+    // the last MMAs (bounded waits; a block that gave up reports it and writes nothing)
+    int done = ok ? 1 : 0;
+    for (int q = 0; q < 2; ++q)
+        if (pend[q] >= 0) {
+            if (!mbar_wait(smem_addr(&mbar[q]), (uint32_t)((pend[q] >> 1) & 1), kConvWaitLimit)) done = 0;
+            pend[q] = -1;
+        }
+    done = __syncthreads_and(done);
+    if (!done) {
+        if (tid == 0) {
+            atomicOr(err, 1u);
+            // copies still in flight into either buffer finish before the shared memory is released
+            mbar_wait(smem_addr(&lbar[it & 1]), (uint32_t)((it >> 1) & 1), kConvWaitLimit);
+            mbar_wait(smem_addr(&lbar[(it + 1) & 1]), (uint32_t)(((it + 1) >> 1) & 1), kConvWaitLimit);
+        }
+    } else if (it > 0) {
+        tc_fence_after();
+        const int m = 32 * warp + lane;  // row of D = this thread's tensor-memory lane
+        const bool real = m < 3 * CIN;
+        const int dz = m / CIN, ci = m % CIN;
+        float* pb = part + (size_t)blockIdx.x * 27 * CIN * COUT;
+#pragma unroll 1
+        for (int pr = 0; pr < 9; ++pr) {
+#pragma unroll
+            for (int c = 0; c < COUT; c += 16) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(pr * COUT + c), v);
+                if (real) {
+                    float* o = pb + ((size_t)(dz * 9 + pr) * CIN + ci) * COUT + c;
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) o[i] = v[i];
+                }
+            }
+        }
+    } else {
+        // no tile: a zero partial
+        float* pb = part + (size_t)blockIdx.x * 27 * CIN * COUT;
+        for (int e = tid; e < 27 * CIN * COUT; e += 128) pb[e] = 0.0f;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_free(tmem, S::COLS);
 }
 
 }  // namespace numa::gpu

@@ -32,7 +32,8 @@ void planes_restrict(Context& ctx, const uint4* fine, uint4* coarse, const VoxGr
 void planes_prolong(Context& ctx, const uint4* coarse, const uint4* add, uint4* out, const VoxGrid& gc,
                     const VoxGrid& gf, int C, float scale, bool accumulate);
 void planes_relu_mask(Context& ctx, uint4* g, const uint4* y, const VoxGrid& gr, int C);
-void conv_dw(Context& ctx, const VoxGrid& gr, int cin, int cout, const uint4* x, const uint4* g, float* dw, float* db);
+void conv_dw(Context& ctx, const VoxGrid& gr, int cin, int cout, const uint4* x, const uint4* g, float* dw, float* db,
+             DeviceArray<float>& part, unsigned* err);
 void planes_features(Context& ctx, const float* r, const float* c, const float* z, const float* scales, uint4* planes,
                      const VoxGrid& gr);
 void planes_loss_grad(Context& ctx, const float* y32, const float* t, uint4* g, const VoxGrid& gr, float* loss);
@@ -99,6 +100,7 @@ private:
     DeviceArray<float> params_, grad_, m_, v_;
     DeviceArray<__nv_bfloat16> wf_[kNumLayers], wb_[kNumLayers];
     DeviceArray<unsigned> err_;
+    DeviceArray<float> dw_part_;  // per-CTA partials of the tensor-core weight gradient
     DeviceArray<float> out32_, gout32_;
     int step_ = 0;
     // activations
@@ -216,7 +218,7 @@ void LearnedNet::conv_adj(int l, const uint4* g, uint4* out) {
 
 void LearnedNet::dw(int l, const uint4* x, const uint4* g) {
     const LayerSpec& L = kLayers[l];
-    conv_dw(ctx_, g_[L.level], L.cin, L.cout, x, g, grad_.p + woff_[l], grad_.p + boff_[l]);
+    conv_dw(ctx_, g_[L.level], L.cin, L.cout, x, g, grad_.p + woff_[l], grad_.p + boff_[l], dw_part_, err_.p);
 }
 
 void LearnedNet::forward(const uint4* in, float* out32) {

@@ -642,12 +642,17 @@ struct TailParams {
     double six_h2inv[kMaxTail];  // 6 h^-2 (single-point solve)
     int pre, post;
     int half;                    // split geometry of level lb (SPLIT_IO)
+    // Jacobian-aware coarse levels (FP32 only): c[l] = the coefficient c of -Lap_h - c on level l
+    // (natural layout, global memory), or null everywhere for the Poisson tail.
+    const float* c[kMaxTail];
 };
 
 // NC > 0: the level's n as a compile-time constant (the index divisions become multiplications);
 // 0: the runtime n_rt.
+// cs (may be null): c h^2 per point: the pass then solves for -Lap_h - c, x = (b h^2 + sum) / (6 - c h^2).
 template <class T, int NC>
-__device__ void tail_pass(T* __restrict__ x, const T* __restrict__ bs, int n_rt, int c, bool first) {
+__device__ void tail_pass(T* __restrict__ x, const T* __restrict__ bs, int n_rt, int c, bool first,
+                          const T* __restrict__ cs = nullptr) {
     const int n = NC ? NC : n_rt;
     const int np = (n + 1) / 2, total = n * n * np, P = n * n;
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
@@ -655,27 +660,24 @@ __device__ void tail_pass(T* __restrict__ x, const T* __restrict__ bs, int n_rt,
         const int k = 2 * kk + ((i + j + c) & 1);
         if (k >= n) continue;
         const int p = (i * n + j) * n + k;
-        T v;
-        if (first) {
-            v = div6(bs[p]);
-        } else {
-            T acc = bs[p];
+        T acc = bs[p];
+        if (!first) {
             acc = acc + ((i > 0) ? x[p - P] : zero<T>());
             acc = acc + ((i + 1 < n) ? x[p + P] : zero<T>());
             acc = acc + ((j > 0) ? x[p - n] : zero<T>());
             acc = acc + ((j + 1 < n) ? x[p + n] : zero<T>());
             acc = acc + ((k > 0) ? x[p - 1] : zero<T>());
             acc = acc + ((k + 1 < n) ? x[p + 1] : zero<T>());
-            v = div6(acc);
         }
-        x[p] = v;
+        x[p] = cs ? acc / (T(6) - cs[p]) : div6(acc);
     }
     __syncthreads();
 }
 
+// cs (may be null): c h^2 per point: r = b - h^-2 (6x - sum - c h^2 x), the residual of -Lap_h - c.
 template <class T, int NC>
 __device__ void tail_residual(const T* __restrict__ x, const T* __restrict__ b, T* __restrict__ r, int n_rt,
-                              T h2inv) {
+                              T h2inv, const T* __restrict__ cs = nullptr) {
     const int n = NC ? NC : n_rt;
     const int N = n * n * n, P = n * n;
     for (int p = threadIdx.x; p < N; p += blockDim.x) {
@@ -687,6 +689,7 @@ __device__ void tail_residual(const T* __restrict__ x, const T* __restrict__ b, 
         s = s - ((j + 1 < n) ? x[p + n] : zero<T>());
         s = s - ((k > 0) ? x[p - 1] : zero<T>());
         s = s - ((k + 1 < n) ? x[p + 1] : zero<T>());
+        if (cs) s = s - cs[p] * x[p];
         r[p] = b[p] - h2inv * s;
     }
     __syncthreads();
@@ -758,7 +761,8 @@ __device__ __forceinline__ void mg_tail_body(const T* __restrict__ b_g, const T*
                                              T* __restrict__ x_g, const TailParams& tp) {
     extern __shared__ __align__(16) unsigned char tail_smem[];
     T* base = reinterpret_cast<T*>(tail_smem);
-    T *X[kMaxTail], *B[kMaxTail], *BS[kMaxTail];
+    T *X[kMaxTail], *B[kMaxTail], *BS[kMaxTail], *CS[kMaxTail];
+    const bool shift = tp.c[0] != nullptr;
     int off = 0;
     for (int l = 0; l < tp.levels; ++l) {
         const int Nl = tp.n[l] * tp.n[l] * tp.n[l];
@@ -768,6 +772,17 @@ __device__ __forceinline__ void mg_tail_body(const T* __restrict__ b_g, const T*
         off += 3 * Nl;
     }
     T* R = base + off;  // residual scratch, the size of level lb
+    off += tp.n[0] * tp.n[0] * tp.n[0];
+    for (int l = 0; l < tp.levels; ++l) {
+        CS[l] = nullptr;
+        if (!shift) continue;
+        // c h^2 of the level (the shift in the units of b h^2)
+        const int Nl = tp.n[l] * tp.n[l] * tp.n[l];
+        CS[l] = base + off;
+        off += Nl;
+        const T inv = (T)tp.inv[l];
+        for (int p = threadIdx.x; p < Nl; p += blockDim.x) CS[l][p] = (T)tp.c[l][p] * inv;
+    }
     {
         const int n = tp.n[0], N = n * n * n;
         for (int p = threadIdx.x; p < N; p += blockDim.x) {
@@ -783,27 +798,30 @@ __device__ __forceinline__ void mg_tail_body(const T* __restrict__ b_g, const T*
         with_tail_n(n, tp.n[l + 1], [&](auto nc) {
             constexpr int NC = decltype(nc)::value;
             for (int sw = 0; sw < tp.pre; ++sw) {
-                tail_pass<T, NC>(X[l], BS[l], n, 0, sw == 0);
-                tail_pass<T, NC>(X[l], BS[l], n, 1, false);
+                tail_pass<T, NC>(X[l], BS[l], n, 0, sw == 0, CS[l]);
+                tail_pass<T, NC>(X[l], BS[l], n, 1, false, CS[l]);
             }
             if (tp.pre == 0) {
                 for (int p = threadIdx.x; p < n * n * n; p += blockDim.x) X[l][p] = zero<T>();
                 __syncthreads();
             }
-            tail_residual<T, NC>(X[l], B[l], R, n, (T)tp.h2inv[l]);
+            tail_residual<T, NC>(X[l], B[l], R, n, (T)tp.h2inv[l], CS[l]);
             tail_restrict<T, NC>(R, B[l + 1], BS[l + 1], n, tp.n[l + 1], (T)tp.inv[l + 1]);
         });
     }
     {  // coarsest
         const int n = tp.n[last];
         if (n == 1) {
-            if (threadIdx.x == 0) X[last][0] = (T)((double)B[last][0] / tp.six_h2inv[last]);
+            if (threadIdx.x == 0) {
+                if (shift) X[last][0] = B[last][0] / ((T)tp.six_h2inv[last] - (T)tp.c[last][0]);
+                else X[last][0] = (T)((double)B[last][0] / tp.six_h2inv[last]);
+            }
             __syncthreads();
         } else {
             for (int sw = 0; sw < 30; ++sw) {
                 const int c0 = (sw % 2 == 0) ? 0 : 1;
-                tail_pass<T, 0>(X[last], BS[last], n, c0, sw == 0);
-                tail_pass<T, 0>(X[last], BS[last], n, 1 - c0, false);
+                tail_pass<T, 0>(X[last], BS[last], n, c0, sw == 0, CS[last]);
+                tail_pass<T, 0>(X[last], BS[last], n, 1 - c0, false, CS[last]);
             }
         }
     }
@@ -813,8 +831,8 @@ __device__ __forceinline__ void mg_tail_body(const T* __restrict__ b_g, const T*
             constexpr int NC = decltype(nc)::value;
             tail_prolong<T, NC>(X[l + 1], X[l], tp.n[l + 1], n, tp.post > 0);
             for (int sw = 0; sw < tp.post; ++sw) {
-                tail_pass<T, NC>(X[l], BS[l], n, 1, false);
-                tail_pass<T, NC>(X[l], BS[l], n, 0, false);
+                tail_pass<T, NC>(X[l], BS[l], n, 1, false, CS[l]);
+                tail_pass<T, NC>(X[l], BS[l], n, 0, false, CS[l]);
             }
         });
     }

@@ -343,6 +343,12 @@ public:
     double time_finest_pass(int reps);
     // FP32 cycle: RN32(r) of the last apply on the finest level and its layout (colour-split when odd).
     const float* fine_b32() const;
+    // Jacobian-aware coarse levels (FP32 cycle with a one-CTA tail): the levels n <= 15 then solve
+    // with -Lap_h - c instead of -Lap_h, c the full-weighting restriction of the fine coefficient c
+    // (for Bratu3D's Jacobian, c = lambda e^u) set by set_coarse_coefficient.
+    bool supports_coarse_jacobian() const { return precision_ == NUMA_GPU_FP32 && tail_l_ != SIZE_MAX; }
+    void set_coarse_coefficient(const double* c_fine);
+    void clear_coarse_coefficient() { coarse_jac_ = false; }
 
     struct Level;
 
@@ -372,6 +378,10 @@ private:
     const float* in32_ = nullptr;     // FP32 right-hand side of the current apply32f
     DeviceArray<double> scratch_r_;   // residual of the level being restricted (FP64 or FP32 bytes)
     DeviceArray<double> alias_b_;     // copy of r when r and z alias
+    bool coarse_jac_ = false;         // the tail solves with the coefficient below
+    bool graph_jac_ = false;          // the mode the coarse-level graph was captured in
+    DeviceArray<float> cl_;           // the restricted coefficient of every level below the finest
+    std::vector<size_t> cl_off_;      // offsets of the levels' coefficients in cl_
 };
 
 // ------------------------------------------------------------------------------ HelmholtzMG2D
@@ -429,6 +439,9 @@ public:
 std::unique_ptr<Provider> make_identity_provider(Context& ctx, size_t N);
 std::unique_ptr<Provider> make_mg_provider(Context& ctx, size_t n, int pre, int post, int precision,
                                            int max_levels);
+// The FP32 V-cycle whose coarse levels (n <= 15) solve with the Jacobian -Lap_h - c of the iterate it
+// is bound at (c from the operator's cache): a preconditioner for Bratu3D's J = -Lap_h - lambda e^u.
+std::unique_ptr<Provider> make_jacobian_mg_provider(Context& ctx, size_t n, int pre, int post);
 std::unique_ptr<Provider> make_jacobi_provider(Bratu3D& op);
 // BurgersMGProvider (problems/burgers2d.hpp:220-246): the HelmholtzMG2D V-cycle of
 // (1/dt) I - nu Lap_h applied to each component.
@@ -568,6 +581,8 @@ void diag_div(Context& ctx, const double* a, double b, double* out, size_t N);
 // One tensor-core 3x3x3 convolution from host buffers (learned.cu): y = conv(x, W) + b, FP32
 // channel-last in and out, BF16 operands; flip = the adjoint convolution (gradient with respect to
 // the input, W of shape [27][cin][cout] used as [27][cout][cin] with the taps reversed).
+void diag_conv3d_wgrad(Context& ctx, int n, int cin, int cout, const float* x_h, const float* g_h, float* dw_h,
+                       float* db_h);
 void diag_conv3d(Context& ctx, int n, int cin, int cout, int flip, const float* x_h, const float* w_h,
                  const float* b_h, float* y_h);
 

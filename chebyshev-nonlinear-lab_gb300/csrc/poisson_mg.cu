@@ -112,7 +112,8 @@ PoissonMG::PoissonMG(Context& ctx, size_t n, int pre, int post, int precision, i
             if (levels_[l]->n > 15) continue;
             if (levels_.size() - l > (size_t)kMaxTail) break;
             size_t elems = 0;
-            for (size_t m = l; m < levels_.size(); ++m) elems += 3 * (size_t)levels_[m]->n * levels_[m]->n * levels_[m]->n;
+            // x, b, b h^2 and (Jacobian-aware tail) c h^2 of each level, and the residual scratch
+            for (size_t m = l; m < levels_.size(); ++m) elems += 4 * (size_t)levels_[m]->n * levels_[m]->n * levels_[m]->n;
             elems += (size_t)levels_[l]->n * levels_[l]->n * levels_[l]->n;
             tail_smem_ = elems * sizeof(float);
             const int lim = std::min(set_dynamic_smem_limit(ctx_, k_mg_tail<float, true>),
@@ -139,6 +140,9 @@ void PoissonMG::launch_tail32() {
     tp.post = post_;
     const bool split = (L.n & 1) != 0;
     tp.half = split ? make_split(L.n).half : 0;
+    for (int m = 0; m < kMaxTail; ++m) tp.c[m] = nullptr;
+    if (coarse_jac_)
+        for (int m = 0; m < tp.levels; ++m) tp.c[m] = cl_.p + cl_off_[tail_l_ + m];
     if (split) launch_pdl(k_mg_tail<float, true>, 1, 1024, tail_smem_, ctx_.stream, L.b32.p, L.bs32.p, L.xs, tp);
     else launch_pdl(k_mg_tail<float, false>, 1, 1024, tail_smem_, ctx_.stream, L.b32.p, L.bs32.p, L.xs, tp);
     ctx_.count_launch();
@@ -151,7 +155,12 @@ PoissonMG::~PoissonMG() {
 }
 
 void PoissonMG::coarse_cycle() {
+    if (coarse_exec_ && graph_jac_ != coarse_jac_) {  // captured in the other tail mode
+        cudaGraphExecDestroy(coarse_exec_);
+        coarse_exec_ = nullptr;
+    }
     if (!coarse_exec_) {
+        graph_jac_ = coarse_jac_;
         // no other thread may allocate or free (and so synchronise the device) during the capture
         std::lock_guard<std::recursive_mutex> lk(alloc_capture_mutex());
         const uint64_t before = ctx_.launches;
@@ -441,6 +450,57 @@ void PoissonMG::apply(const double* r, double* z) {
 }
 
 const float* PoissonMG::fine_b32() const { return levels_[0]->b32.p; }
+
+namespace {
+
+// cc = the full-weighting restriction of a natural-layout coefficient (weights (1/4, 1/2, 1/4) per
+// dimension, summed z outer, y, x inner), FP32 out.
+template <class TI>
+__global__ void k_restrict_coef(const TI* __restrict__ cf, float* __restrict__ cc, int nf, int nc) {
+    pdl_wait();
+    pdl_trigger();
+    const int Nc = nc * nc * nc;
+    const float w[3] = {0.25f, 0.5f, 0.25f};
+    const int stride = gridDim.x * blockDim.x;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < Nc; q += stride) {
+        const int K = q % nc, J = (q / nc) % nc, I = q / (nc * nc);
+        float acc = 0.0f;
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b)
+                for (int c = 0; c < 3; ++c) {
+                    const size_t f = ((size_t)(2 * I + a) * nf + 2 * J + b) * nf + 2 * K + c;
+                    acc = __fmaf_rn(w[a] * w[b] * w[c], (float)cf[f], acc);
+                }
+        cc[q] = acc;
+    }
+}
+
+}  // namespace
+
+void PoissonMG::set_coarse_coefficient(const double* c_fine) {
+    if (!supports_coarse_jacobian())
+        throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "Jacobian-aware coarse levels need the FP32 cycle with a one-CTA tail");
+    if (cl_off_.empty()) {
+        size_t total = 0;
+        cl_off_.assign(levels_.size(), 0);
+        for (size_t l = 1; l < levels_.size(); ++l) {
+            cl_off_[l] = total;
+            total += (size_t)levels_[l]->n * levels_[l]->n * levels_[l]->n;
+        }
+        cl_.resize(total);
+    }
+    for (size_t l = 1; l < levels_.size(); ++l) {
+        const int nf = levels_[l - 1]->n, nc = levels_[l]->n;
+        const size_t Nc = (size_t)nc * nc * nc;
+        const unsigned g = ew_grid(ctx_, Nc);
+        if (l == 1) launch_pdl(k_restrict_coef<double>, g, 256, 0, ctx_.stream, c_fine, cl_.p + cl_off_[1], nf, nc);
+        else launch_pdl(k_restrict_coef<float>, g, 256, 0, ctx_.stream, (const float*)(cl_.p + cl_off_[l - 1]),
+                        cl_.p + cl_off_[l], nf, nc);
+        ctx_.count_launch();
+    }
+    ctx_.check_launch("mg coarse coefficient");
+    coarse_jac_ = true;
+}
 
 double PoissonMG::time_finest_pass(int reps) {
     Level& L0 = *levels_[0];

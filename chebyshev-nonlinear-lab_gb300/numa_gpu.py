@@ -29,7 +29,7 @@ FP64, FP32 = 0, 1
 ANALYTIC, FD, ANALYTIC_FP32 = 0, 1, 2
 MGS, CGS2, CGS1 = 0, 1, 2
 METHODS = {"nk": 0, "cheb": 1, "rec": 2, "tf2018": 3}
-PRECONDS = {"none": 0, "mg": 1, "jacobi": 2, "burgers_mg": 3, "bruss_jacobi": 5, "bruss_mg": 6}
+PRECONDS = {"none": 0, "mg": 1, "jacobi": 2, "burgers_mg": 3, "bruss_jacobi": 5, "bruss_mg": 6, "jacobian_mg": 7}
 
 
 class KrylovParams(C.Structure):
@@ -231,6 +231,7 @@ SIGNATURES = {
     "numa_gpu_diag_exp": ([_P, _P, _P], _I),
     "numa_gpu_diag_div": ([_P, C.c_double, _P], _I),
     "numa_gpu_diag_conv3d": ([_P, _SZ, _I, _I, _I, _F32P, _F32P, _F32P, _F32P], _I),
+    "numa_gpu_diag_conv3d_wgrad": ([_P, _SZ, _I, _I, _F32P, _F32P, _F32P, _F32P], _I),
     "numa_gpu_solve_batch": ([_I, C.POINTER(BatchInstance), _SZ, _I, _I, C.POINTER(KrylovParams), _I,
                               C.POINTER(BatchResult), _F64P], _I),
     "numa_gpu_batch_last_error": ([], C.c_char_p),
@@ -251,6 +252,7 @@ SIGNATURES = {
     "numa_gpu_learned_train": ([_P, C.POINTER(LearnedTrainParams), C.POINTER(LearnedTrainReport)], _I),
     "numa_gpu_provider_create_learned": ([_P, _SZ, _P, _D, _PP], _I),
     "numa_gpu_provider_learned_stats": ([_P, C.POINTER(_SZ), C.POINTER(_SZ)], _I),
+    "numa_gpu_provider_create_jacobian_mg": ([_P, _SZ, _I, _I, _PP], _I),
     "numa_gpu_bsolver_create": ([_P, C.POINTER(BatchInstance), _SZ, C.POINTER(KrylovParams), _PP], _I),
     "numa_gpu_bsolver_destroy": ([_P], _I),
     "numa_gpu_bsolver_solve": ([_P, _F64P, C.POINTER(BatchResult), _F64P], _I),
@@ -834,6 +836,14 @@ class Provider:
         return cls(ctx, h, "mg")
 
     @classmethod
+    def jacobian_mg(cls, ctx: Context, n: int, pre: int = 2, post: int = 2) -> "Provider":
+        """The FP32 V-cycle with Jacobian-aware coarse levels (n <= 15 solve with -Lap_h - lambda e^u)."""
+        h = C.c_void_p()
+        ctx.check(ctx.lib.numa_gpu_provider_create_jacobian_mg(ctx.h, n, pre, post, C.byref(h)),
+                  "provider_jacobian_mg")
+        return cls(ctx, h, "jacobian_mg")
+
+    @classmethod
     def jacobi(cls, op: Bratu3D) -> "Provider":
         h = C.c_void_p()
         op.ctx.check(op.lib.numa_gpu_provider_create_jacobi(op.h, C.byref(h)), "provider_jacobi")
@@ -1029,6 +1039,20 @@ def diag_conv3d(ctx: Context, n: int, x: np.ndarray, w: np.ndarray, bias: np.nda
                                       y.ctypes.data_as(_F32P))
     ctx.check(rc, "diag_conv3d")
     return y
+
+
+def diag_conv3d_wgrad(ctx: Context, n: int, x: np.ndarray, g: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """The tensor-core weight and bias gradients of one 3x3x3 convolution: x [n^3, cin], g [n^3, cout];
+    returns dw [27, cin, cout] and db [cout]."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    g = np.ascontiguousarray(g, dtype=np.float32)
+    cin, cout = int(x.shape[1]), int(g.shape[1])
+    dw = np.empty((27, cin, cout), dtype=np.float32)
+    db = np.empty(cout, dtype=np.float32)
+    rc = ctx.lib.numa_gpu_diag_conv3d_wgrad(ctx.h, n, cin, cout, x.ctypes.data_as(_F32P), g.ctypes.data_as(_F32P),
+                                            dw.ctypes.data_as(_F32P), db.ctypes.data_as(_F32P))
+    ctx.check(rc, "diag_conv3d_wgrad")
+    return dw, db
 
 
 def forcing(params: KrylovParams, k: int, rnorm: float, rprev: float, eta_prev: float, res0: float) -> float:

@@ -81,7 +81,8 @@ typedef enum numa_gpu_precond_kind {
     NUMA_GPU_PRECOND_BURGERS_MG = 3, /* BurgersMGProvider (problems/burgers2d.hpp:220-246) */
     NUMA_GPU_PRECOND_LEARNED = 4,    /* extension: FP32 V-cycle + learned coarse correction (FGMRES) */
     NUMA_GPU_PRECOND_BRUSS_JACOBI = 5, /* BrusselatorJacobi (problems/brusselator1d.hpp:194-222) */
-    NUMA_GPU_PRECOND_BRUSS_MG = 6      /* extension: periodic coupled-block multigrid of Brusselator2D */
+    NUMA_GPU_PRECOND_BRUSS_MG = 6,     /* extension: periodic coupled-block multigrid of Brusselator2D */
+    NUMA_GPU_PRECOND_JACOBIAN_MG = 7   /* extension: FP32 V-cycle with Jacobian-aware coarse levels */
 } numa_gpu_precond_kind;
 
 /* ---------------------------------------------------------------- parameter / result structs */
@@ -262,6 +263,13 @@ int numa_gpu_provider_create_identity(numa_gpu_ctx* ctx, numa_gpu_provider** out
 int numa_gpu_provider_create_poisson_mg(numa_gpu_ctx* ctx, size_t n, int pre, int post, int precision,
                                         numa_gpu_provider** out);
 int numa_gpu_provider_create_jacobi(numa_gpu_bratu3d* op, numa_gpu_provider** out);
+/* No counterpart in the reference (whose PoissonMGProvider, linalg/poisson_mg.hpp:303-320, ignores
+ * the iterate): the FP32 PoissonMG V-cycle whose coarse levels n <= 15 (the one-CTA tail) solve with
+ * the Jacobian -Lap_h - c instead of -Lap_h, c the full-weighting restriction of the Bratu3D
+ * coefficient lambda e^u of the iterate the provider is bound at (make reads the operator's cache).
+ * The fine levels keep the Poisson smoother: the shift matters only for the smooth modes, which the
+ * coarse levels carry.  n = 2^k - 1 >= 31 (an odd hierarchy down to the tail). */
+int numa_gpu_provider_create_jacobian_mg(numa_gpu_ctx* ctx, size_t n, int pre, int post, numa_gpu_provider** out);
 /* BurgersMGProvider(n, nu, dt): HelmholtzMG2D(n, 1/dt, nu) V(2,2) on u and on v. */
 int numa_gpu_provider_create_burgers_mg(numa_gpu_ctx* ctx, size_t n, double nu, double dt,
                                         numa_gpu_provider** out);
@@ -581,6 +589,12 @@ int numa_gpu_diag_div(const numa_gpu_vec* a, double b, numa_gpu_vec* out);
  * x is then [n^3][cout] and y [n^3][cin].  cin, cout in {16, 32}; bias may be NULL. */
 int numa_gpu_diag_conv3d(numa_gpu_ctx* ctx, size_t n, int cin, int cout, int adjoint, const float* x,
                          const float* w, const float* bias, float* y);
+/* The learned preconditioner's weight and bias gradients of one 3x3x3 convolution on the tensor
+ * cores (tcgen05, BF16 operands, FP32 accumulation), host buffers: dw[tap][ci][co] = sum_v
+ * x[v + tap][ci] g[v][co] over the n^3 grid (zero outside), db[co] = sum_v g[v][co]; x [n^3][cin],
+ * g [n^3][cout], n <= 63, cin, cout in {16, 32}. */
+int numa_gpu_diag_conv3d_wgrad(numa_gpu_ctx* ctx, size_t n, int cin, int cout, const float* x, const float* g,
+                               float* dw, float* db);
 
 #ifdef __cplusplus
 } /* extern "C" */

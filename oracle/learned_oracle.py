@@ -41,6 +41,19 @@ def conv3d_adjoint(g: np.ndarray, w: np.ndarray, n: int) -> np.ndarray:
     return conv3d(g, wf, n)
 
 
+def conv3d_wgrad(x: np.ndarray, g: np.ndarray, n: int):
+    """The gradients of conv3d with respect to its weights and bias: dw[tap][ci][co] =
+    sum_v x[v + tap][ci] g[v][co] (x zero outside the grid), db[co] = sum_v g[v][co]; FP64."""
+    ci, co = x.shape[1], g.shape[1]
+    xp = np.zeros((n + 2, n + 2, n + 2, ci))
+    xp[1:-1, 1:-1, 1:-1] = np.asarray(x, dtype=np.float64).reshape(n, n, n, ci)
+    gg = np.asarray(g, dtype=np.float64).reshape(-1, co)
+    gw = np.zeros((27, ci, co))
+    for t, dz, dy, dx in taps():
+        gw[t] = xp[1 + dz:n + 1 + dz, 1 + dy:n + 1 + dy, 1 + dx:n + 1 + dx].reshape(-1, ci).T @ gg
+    return gw, gg.sum(axis=0)
+
+
 # ------------------------------------------------------------------------------ the network
 # (cin, cout, level, relu) of e0a e0b e1a e1b e2a e2b e3a e3b d2 d1 d0a d0b — the layer table of
 # the GPU network (chebyshev-nonlinear-lab_gb300/csrc/learned_net.cu).

@@ -7,7 +7,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from oracle.learned_oracle import bf16, conv3d, conv3d_adjoint
+from oracle.learned_oracle import bf16, conv3d, conv3d_adjoint, conv3d_wgrad
 
 pytestmark = pytest.mark.gpu
 
@@ -41,6 +41,24 @@ def test_conv3d_adjoint_tensor_cores(gpu, n, cin, cout):
     dx = G.diag_conv3d(gpu, n, g, w, adjoint=True)
     ref = conv3d_adjoint(g, w, n)
     assert np.abs(dx - ref).max() / (np.abs(ref).max() + 1e-30) < 1e-5
+
+
+@pytest.mark.parametrize("n", [1, 3, 7, 15, 31, 63])
+@pytest.mark.parametrize("cin,cout", [(16, 16), (16, 32), (32, 16), (32, 32)])
+def test_conv3d_weight_gradient_tensor_cores(gpu, n, cin, cout):
+    """The weight gradient as implicit GEMMs on the tensor cores (MN-major operands straight from the
+    plane layout, the three dz taps stacked along M) against the FP64 sums of the oracle on the same
+    BF16 inputs; the bias gradient beside it."""
+    if n == 63 and (cin, cout) != (32, 32):
+        pytest.skip("63^3 once, at the largest channel counts")
+    G = _G()
+    rng = np.random.default_rng(13 * n + cin + 5 * cout)
+    x = bf16(rng.standard_normal((n ** 3, cin)))
+    g = bf16(rng.standard_normal((n ** 3, cout)))
+    dw, db = G.diag_conv3d_wgrad(gpu, n, x, g)
+    ref_w, ref_b = conv3d_wgrad(x, g, n)
+    assert np.abs(dw - ref_w).max() / (np.abs(ref_w).max() + 1e-30) < 1e-5
+    assert np.abs(db - ref_b).max() / (np.abs(ref_b).max() + 1e-30) < 1e-5
 
 
 def test_network_forward_and_gradient(gpu):
@@ -104,4 +122,22 @@ def test_learned_preconditioner_trains_and_solves(gpu):
     print("plain", r64["iters"], r64["n_lin_iters"], "mixed", rm["iters"], rm["n_lin_iters"], "learned", rl["iters"],
           rl["n_lin_iters"], "net applies", applies, "fallbacks", fallbacks)
     assert rl["converged"] == 1 and applies > 0
+    assert np.linalg.norm(xl - x64) <= 1e-8 * np.linalg.norm(x64)
+
+
+def test_stagnation_falls_back_to_the_vcycle(gpu):
+    """A network that corrects in the wrong direction (an untrained one with its weights scaled
+    up tenfold) makes an FGMRES iteration stall; the provider then hands the rest of that linear
+    solve to the plain V-cycle, and the Newton solve still converges to the FP64 path's solution."""
+    G = _G()
+    n, n0 = 31, 15
+    net = G.LearnedNet(gpu, n0, seed=3)
+    net.set_params(net.get_params() * 10.0)
+    mp = G.default_params(rtol_nl=1e-10, gmres_restart=30, flexible=1, jvp_precision=G.FP32)
+    pl = G.Provider.learned(gpu, n, net, stall=0.9)
+    xl, rl = _solve(G, gpu, n, 4.2, pl, mp)
+    applies, fallbacks = pl.learned_stats()
+    x64, _ = _solve(G, gpu, n, 4.2, G.Provider.poisson_mg(gpu, n), G.default_params(rtol_nl=1e-10, gmres_restart=30))
+    assert fallbacks > 0, (applies, fallbacks)
+    assert rl["converged"] == 1 and rl["res"] <= 1e-10 * rl["res0"]
     assert np.linalg.norm(xl - x64) <= 1e-8 * np.linalg.norm(x64)
