@@ -528,18 +528,22 @@ def run_ours(args) -> int:
         eb = 8 if mgp == G.FP64 else 4
         # the residual evaluation: algorithmic 16 B a point (u read, F written once); the drivers'
         # cache adds c = lambda e^u (8 B) and, on the mixed path, RN32(c) and RN32(F) (4 + 4 B).
-        # FP64 instructions a point from ncu (k_eval_fp64_pipe_255.md): 15
+        # FP64 instructions a point: ncu's count from the committed capture of the mixed path's
+        # evaluation (13.7: the 7-point sum with one FMA, e^u 5 with lambda in the table, F, the norm
+        # and the block reduction); the plain FP64 evaluation has one more (6u and the subtraction)
         eval_bytes = 16.0 * N
         eval_moved = (32.0 if mgp == G.FP32 else 24.0) * N
-        eval_dp_per_pt = 15
+        prof = load_profile(ROOT / "profiles" / "k_eval_fp32cache_255.json")
+        dp_mixed = prof["fp64_thread_instructions"] / prof["points"] if prof.get("points") else 13.7
+        eval_dp_per_pt = dp_mixed if mgp == G.FP32 else dp_mixed + 1.0
+        if mgp != G.FP32:
+            prof = {}
         ach_eval = eval_bytes / (ms_eval * 1e-3) / 1e9
         dp_rate = eval_dp_per_pt * N / (ms_eval * 1e-3) / 1e12
         # one red-black colour pass: the own-colour right-hand side (N/2) and the other-colour
         # neighbours (N/2) read once, the own-colour values (N/2) written once
         pass_bytes = 3 * (N / 2) * eb
         achieved = pass_bytes / (ms_pass * 1e-3) / 1e9
-        prof = load_profile(ROOT / "profiles" / ("k_eval_fp32cache_255.json" if mgp == G.FP32 else
-                                                 "k_eval_fp64cache_255.json"))
         roofline = {
             "kernel": f"k_eval (FP64 residual F, its norm and the drivers' cache), {n}^3",
             "bound": "hbm", "achieved": ach_eval, "peak": hbm_peak, "unit": "GB/s", "frac": ach_eval / hbm_peak,
@@ -550,8 +554,9 @@ def run_ours(args) -> int:
                 "achieved_tinstr_per_s": dp_rate, "peak_tinstr_per_s": fp64_peak / 2,
                 "peak_fma_tflops_measured": fp64_peak, "frac": dp_rate / (fp64_peak / 2),
                 "dp_instr_per_point": eval_dp_per_pt,
-                "note": "the bound that holds: FP64 arithmetic (e^u and the 7-point sum, 15 DP instructions a "
-                        "point) against the FMA-chain peak measured live; HBM would allow ~16x the rate",
+                "note": f"the bound that holds: FP64 arithmetic (e^u and the 7-point sum, {eval_dp_per_pt:.1f} FP64 "
+                        "instructions a point by ncu) against the FMA-chain peak measured live; HBM would allow "
+                        "~14x the rate",
             },
             "vcycle_colour_pass": {
                 "kernel": (f"k_rbgs<double> colour pass, {n}^3" if mgp == G.FP64 else

@@ -62,13 +62,16 @@ __device__ __forceinline__ double lap_sum(const double* __restrict__ v, size_t p
 // F = h^-2 (6u - sum) - lambda e^u; optionally c = lambda e^u and ||F||.  The last step is one FMA
 // (F differs from the reference's two roundings by at most half an ulp, as e^u already may).
 // C32: also c32 = RN32(c) (the mixed path's FP32 Jacobian coefficient) and f32 = RN32(F) (the
-// first FP32 Krylov vector of the next linear solve), integer conversions.
-template <bool WRITE_C, bool NORM, bool C32>
+// first FP32 Krylov vector of the next linear solve), integer conversions; this is the mixed
+// path's evaluation, and it forms 6u - (i-1 neighbour) as one FMA (one rounding fewer than the
+// reference's two).  LT: lambda e^u from the operator's lambda-scaled exp table (lt2, ltf).
+template <bool WRITE_C, bool NORM, bool C32, bool LT>
 __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, double* __restrict__ F,
                                                  double* __restrict__ c_out, float* __restrict__ c32_out,
                                                  float* __restrict__ f32_out, int n,
                                                  int ichunk, double lam, double h2inv, RedArgs red, double* norm_out,
-                                                 int zoff = 0, int norm_raw = 0) {
+                                                 int zoff, int norm_raw, const double2* __restrict__ lt2,
+                                                 const float2* __restrict__ ltf) {
     pdl_wait();
     pdl_trigger();
     const int k = blockIdx.x * BX + threadIdx.x;
@@ -83,8 +86,23 @@ __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, d
         double cur = u[p];
         for (int i = i0; i < i1; ++i) {
             double above;
-            const double s = lap_sum(u, p, plane, n, i, j, k, below, cur, above);
-            const double e = lam * exp_tang(cur);
+            double s;
+            if (C32) {
+                above = (i + 1 < n) ? u[p + plane] : 0.0;
+                const double jm = (j > 0) ? u[p - n] : 0.0;
+                const double jp = (j + 1 < n) ? u[p + n] : 0.0;
+                const double km = (k > 0) ? u[p - 1] : 0.0;
+                const double kp = (k + 1 < n) ? u[p + 1] : 0.0;
+                s = __fma_rn(6.0, cur, -below);
+                s = s - above;
+                s = s - jm;
+                s = s - jp;
+                s = s - km;
+                s = s - kp;
+            } else {
+                s = lap_sum(u, p, plane, n, i, j, k, below, cur, above);
+            }
+            const double e = LT ? lam_exp_tang(cur, lam, lt2, ltf) : lam * exp_tang(cur);
             const double f = __fma_rn(h2inv, s, -e);  // h^-2 s - e with one rounding
             F[p] = f;
             if (WRITE_C) c_out[p] = e;
@@ -105,6 +123,18 @@ __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, d
             *norm_out = norm_raw ? t[0] : __dsqrt_rn(t[0]);  // raw: a piece's sum of squares
         });
     }
+}
+
+// The exp table scaled by lambda: T2[j] = (RN(lambda T_hi), lambda T_hi - RN(lambda T_hi) + lambda T_lo),
+// TF[j] = RN32 of both (the unscaled table is 2^(j/2048) = T_hi + T_lo).
+__global__ void k_lam_table(double lam, double2* __restrict__ T2, float2* __restrict__ TF) {
+    const int jj = blockIdx.x * blockDim.x + threadIdx.x;
+    if (jj >= (1 << kExpTableBits)) return;
+    const double2 T = kExp2Frac[jj];
+    const double hi = __dmul_rn(lam, T.x);
+    const double lo = __dadd_rn(__fma_rn(lam, T.x, -hi), __dmul_rn(lam, T.y));
+    T2[jj] = make_double2(hi, lo);
+    TF[jj] = make_float2(__double2float_rn(hi), __double2float_rn(lo));
 }
 
 // c = lambda e^u
@@ -323,6 +353,20 @@ Bratu3D::Bratu3D(Context& ctx, size_t n, double lambda)
     : NonlinearOp(ctx), n_(n), N_(n * n * n), lambda_(lambda), h2inv_((n + 1.0) * (n + 1.0)) {
     if (n == 0) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Bratu3D needs n > 0");
     if (n > 65535 * 8) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "grid too large");
+    set_lambda(lambda);
+}
+
+// lambda in [2^-10, 2^10]: the evaluation takes lambda e^u from a table scaled by lambda (one FP64
+// multiply a point fewer); otherwise lambda * e^u.
+void Bratu3D::set_lambda(double lambda) {
+    lambda_ = lambda;
+    lt_on_ = lambda >= 0x1p-10 && lambda <= 0x1p10;
+    if (!lt_on_) return;
+    lt2_.resize(1 << kExpTableBits);
+    ltf_.resize(1 << kExpTableBits);
+    k_lam_table<<<(1 << kExpTableBits) / 256, 256, 0, ctx_.stream>>>(lambda, lt2_.p, ltf_.p);
+    ctx_.count_launch();
+    ctx_.check_launch("bratu3d lambda table");
 }
 
 Bratu3D::~Bratu3D() = default;
@@ -400,24 +444,27 @@ void Bratu3D::eval_launch(const double* x, double* out, double* c_out, double* n
     float* f32 = c32 ? reinterpret_cast<float*>(c_out + N_ + (N_ + 1) / 2) : nullptr;
     const double lam = lambda_, h2 = h2inv_;
     const RedArgs red = ctx_.red;
-    if (c32 && norm)
-        launch_pdl(k_eval<true, true, true>, grid, blk, 0, ctx_.stream, x, out, c_out, c32, f32, n, ichunk, lam, h2, red,
-                   norm_out, zoff, norm_raw);
-    else if (c32)
-        launch_pdl(k_eval<true, false, true>, grid, blk, 0, ctx_.stream, x, out, c_out, c32, f32, n, ichunk, lam, h2, red,
-                   nullptr, zoff, norm_raw);
-    else if (c_out && norm)
-        launch_pdl(k_eval<true, true, false>, grid, blk, 0, ctx_.stream, x, out, c_out, nullptr, nullptr, n, ichunk, lam,
-                   h2, red, norm_out, zoff, norm_raw);
-    else if (c_out)
-        launch_pdl(k_eval<true, false, false>, grid, blk, 0, ctx_.stream, x, out, c_out, nullptr, nullptr, n, ichunk, lam,
-                   h2, red, nullptr, zoff, norm_raw);
-    else if (norm)
-        launch_pdl(k_eval<false, true, false>, grid, blk, 0, ctx_.stream, x, out, nullptr, nullptr, nullptr, n, ichunk,
-                   lam, h2, red, norm_out, zoff, norm_raw);
-    else
-        launch_pdl(k_eval<false, false, false>, grid, blk, 0, ctx_.stream, x, out, nullptr, nullptr, nullptr, n, ichunk,
-                   lam, h2, red, nullptr, zoff, norm_raw);
+    const double2* t2 = lt_on_ ? lt2_.p : nullptr;
+    const float2* tf = lt_on_ ? ltf_.p : nullptr;
+    auto go = [&](auto kernel, double* c, float* c32v, float* f32v, double* nrm) {
+        launch_pdl(kernel, grid, blk, 0, ctx_.stream, x, out, c, c32v, f32v, n, ichunk, lam, h2, red, nrm, zoff, norm_raw,
+                   t2, tf);
+    };
+    if (lt_on_) {
+        if (c32 && norm) go(k_eval<true, true, true, true>, c_out, c32, f32, norm_out);
+        else if (c32) go(k_eval<true, false, true, true>, c_out, c32, f32, nullptr);
+        else if (c_out && norm) go(k_eval<true, true, false, true>, c_out, nullptr, nullptr, norm_out);
+        else if (c_out) go(k_eval<true, false, false, true>, c_out, nullptr, nullptr, nullptr);
+        else if (norm) go(k_eval<false, true, false, true>, nullptr, nullptr, nullptr, norm_out);
+        else go(k_eval<false, false, false, true>, nullptr, nullptr, nullptr, nullptr);
+    } else {
+        if (c32 && norm) go(k_eval<true, true, true, false>, c_out, c32, f32, norm_out);
+        else if (c32) go(k_eval<true, false, true, false>, c_out, c32, f32, nullptr);
+        else if (c_out && norm) go(k_eval<true, true, false, false>, c_out, nullptr, nullptr, norm_out);
+        else if (c_out) go(k_eval<true, false, false, false>, c_out, nullptr, nullptr, nullptr);
+        else if (norm) go(k_eval<false, true, false, false>, nullptr, nullptr, nullptr, norm_out);
+        else go(k_eval<false, false, false, false>, nullptr, nullptr, nullptr, nullptr);
+    }
     ctx_.count_launch();
     ctx_.check_launch("bratu3d eval");
 }

@@ -128,8 +128,8 @@ public:
     size_t grid() const { return n_; }
     double lambda() const { return lambda_; }
     double h2inv() const { return h2inv_; }
-    // A new lambda for the same grid (kernels take lambda as a parameter; nothing is cached on it).
-    void set_lambda(double lambda) { lambda_ = lambda; }
+    // A new lambda for the same grid (rebuilds the lambda-scaled exp table on the stream).
+    void set_lambda(double lambda);
 
     // NonlinearOp: the cache of an iterate x is c = lambda e^x; for FP32 products it also holds
     // RN32(c) (N floats after the N doubles), written by the evaluation itself.
@@ -183,6 +183,9 @@ private:
     int bound_precision_ = NUMA_GPU_FP64;
     bool mixed_cache_ = false;
     DeviceArray<float> c32_;
+    bool lt_on_ = false;           // lambda e^u from the lambda-scaled exp table
+    DeviceArray<double2> lt2_;     // its FP64 pairs
+    DeviceArray<float2> ltf_;      // and their RN32
     void eval_launch(const double* x, double* out, double* c_out, double* norm_out, dim3 grid, int ichunk, int zoff,
                      int norm_raw);
 };
