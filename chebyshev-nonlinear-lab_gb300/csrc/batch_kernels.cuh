@@ -176,8 +176,7 @@ __global__ void __launch_bounds__(kBX* kBY) k_beval(const double* __restrict__ x
             const double jp = (j + 1 < n) ? u[p + n] : 0.0;
             const double km = (k > 0) ? u[p - 1] : 0.0;
             const double kp = (k + 1 < n) ? u[p + 1] : 0.0;
-            double s = 6.0 * curv;
-            s = s - below;
+            double s = __fma_rn(6.0, curv, -below);  // as the single-instance mixed evaluation
             s = s - above;
             s = s - jm;
             s = s - jp;

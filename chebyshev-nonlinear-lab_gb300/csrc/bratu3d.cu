@@ -23,11 +23,12 @@ struct March {
     int ichunk;
 };
 
-// Grid of (k tiles, j tiles, i chunks).  Chunks of 8 planes keep ~1M threads in flight at
-// n = 255; the chunk grows when a fused reduction would exceed kMaxRedBlocks partials.
+// Grid of (k tiles, j tiles, i chunks).  Chunks of 8 planes keep ~2M threads at n = 255; a fused
+// reduction takes 16 from n = 128 (its block sum, in FP64, is then shared by twice the points), and
+// more when it would exceed kMaxRedBlocks partials.
 March march_shape(int n, bool reducing) {
     const int kb = (n + BX - 1) / BX, jb = (n + BY - 1) / BY;
-    int ichunk = n >= 64 ? 8 : (n >= 16 ? 4 : 1);
+    int ichunk = n >= 64 ? (reducing && n >= 128 ? 16 : 8) : (n >= 16 ? 4 : 1);
     if (reducing) {
         const long cols = (long)kb * jb;
         const long max_chunks = kMaxRedBlocks / cols;

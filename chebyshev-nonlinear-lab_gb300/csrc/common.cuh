@@ -260,8 +260,8 @@ __device__ __forceinline__ double div_by_recip(double a, double b, double y) {
 //   x = (2048 M + j) ln2/2048 + r,   e^x = 2^M * 2^(j/2048) * e^r,   |r| <= ~ln2/4096 < 1.7e-4,
 // with 2^(j/2048) = T_hi + T_lo from exp2_table.cuh (gen_exp2_table.py).
 //  * N = 2048 M + j = round(2048 x / ln2) is formed in FP32 from x truncated to FP32 (near a tie it
-//    may be the other neighbour, which only widens |r| a little) and turned into the FP64 value
-//    N exactly through the 1.5 * 2^52 shifter.
+//    may be the other neighbour, which only widens |r| a little); the FP32 value N (an integer below
+//    2^22 in magnitude, exact) is widened to FP64 by integer instructions.
 //  * ln2/2048 = L1 + L2: r = RN(x - N L1) in FP64 (one FMA); the small part N L2 (< 3e-14) is
 //    folded into the table's low word in FP32, to first order: - T_hi N L2 (1 + r).
 //  * e^r - 1 = (r + r^2/2) + r^3 (1/6 + r/24) + O(r^5 < 2e-21): r + r^2/2 as one FMA with r/2
@@ -269,7 +269,7 @@ __device__ __forceinline__ double div_by_recip(double a, double b, double y) {
 //    the low word too (their FP32 rounding stays below 1e-19).
 //  * y = T_hi + (T_hi (r + r^2/2) + [T_lo - T_hi N L2 (1 + r) + T_hi r^3 (1/6 + r/24)]) in
 //    [0.99, 2.01], then 2^M by adding M to the exponent field: for |x| < 708 the result is normal.
-// Five FP64 instructions; within 0.505 ulp of e^x over 24M test points (99.9 % correctly rounded).
+// Four FP64 instructions; within 0.505 ulp of e^x over 24M test points (99.9 % correctly rounded).
 // |x| >= 708 (overflow, results near or below the smallest normal, infinities, NaN) is left to exp().
 #include "exp2_table.cuh"
 
@@ -288,8 +288,12 @@ __device__ __forceinline__ double exp_tang_core(double x, const double2* __restr
     const float xf = f64_trunc_f32(x);  // |x| < 708 < 2^127: no overflow
     const float tf = __fmaf_rn(xf, kExpInvL, 0x1.8p23f);
     const int N = (int)(__float_as_uint(tf) - 0x4B400000u);  // round(2048 x / ln2), |N| < 2^22
-    const float nf = __fsub_rn(tf, 0x1.8p23f);
-    const double nd = __dsub_rn(__hiloint2double(0x43380000 + (N >> 31), N), 0x1.8p52);
+    const float nf = __fsub_rn(tf, 0x1.8p23f);  // N exactly (|N| < 2^22)
+    const unsigned nb = __float_as_uint(nf);
+    const double nd = (nb & 0x7FFFFFFFu)  // N in FP64: the exact widening of nf, in integer instructions
+                          ? __hiloint2double((int)((nb & 0x80000000u) | (((nb & 0x7FFFFFFFu) >> 3) + (896u << 20))),
+                                             (int)(nb << 29))
+                          : 0.0;
     const double r = __fma_rn(-nd, kExpL1, x);
     const int rhi = __double2hiint(r), rlo = __double2loint(r);
     const double hr = ((unsigned)rhi & 0x7FF00000u) > 0x00100000u ? __hiloint2double(rhi - 0x00100000, rlo) : 0.0;

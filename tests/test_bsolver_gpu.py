@@ -104,8 +104,10 @@ def test_bsolver_restarted_cycles(gpu):
 
 def test_bsolver_repeatable_and_tuning_independent(gpu, tmp_path):
     """A second solve repeats the first bit for bit (fixed reduction order); other tile shapes give
-    the same counts and solutions within 1e-12; the autotuner keeps the fastest candidate and its
-    cache answers the second call."""
+    the same counts and solutions within 1e-10; the autotuner keeps the fastest candidate and its
+    cache answers the second call.  Another tile shape sums the norms and inner products in another
+    order, which moves FP32 roundings of the basis: measured 1e-14 to 2.3e-12 between shapes, against
+    8e-13 to 1.2e-11 between the mixed path's solution and the FP64 one for these instances."""
     G = _G()
     inst = [(31, 6.0), (63, 3.5), (31, 1.2), (63, 6.5)]
     bs = G.BatchSolver(gpu, inst, _mixed(G))
@@ -119,7 +121,7 @@ def test_bsolver_repeatable_and_tuning_independent(gpu, tmp_path):
         r3, _, x3 = bs.solve(want_x=True)
         keys = ("converged", "iters", "n_F", "n_JVP", "n_lin_iters", "n_prec")
         assert all(all(a[k] == b[k] for k in keys) for a, b in zip(r1, r3))
-        assert all(rel_err(a, b) < 1e-12 for a, b in zip(x3, x1))
+        assert all(rel_err(a, b) < 1e-10 for a, b in zip(x3, x1))
         cache = tmp_path / "tuning.json"
         t = bs.autotune((4, 8), (8192, 16384), cache=cache)
         assert (t["planes"], t["elems_per_block"]) in {(4, 8192), (4, 16384), (8, 8192), (8, 16384)}
