@@ -54,11 +54,14 @@ void launch_conv(Context& ctx, const VoxGrid& g, const uint4* in, const uint4* w
     const size_t smem = conv_smem_bytes<CIN, COUT>(g);
     const int lim = set_dynamic_smem_limit(ctx, k_conv3d_tc<CIN, COUT, OUT32>);
     if (smem > (size_t)lim) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "convolution tile exceeds shared memory");
+    if (OUT32 && (reinterpret_cast<uintptr_t>(out32) & 15u))
+        throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "convolution FP32 output must be 16-byte aligned");
     // persistent CTAs: as many as fit on the GPU at once, each pipelining its tiles
     int per_sm = 0;
-    NUMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3d_tc<CIN, COUT, OUT32>, 128, smem));
+    NUMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3d_tc<CIN, COUT, OUT32>, kConvThreads,
+                                                            smem));
     const int grid = std::max(1, std::min(g.tiles, std::max(1, per_sm) * ctx.sm_count));
-    k_conv3d_tc<CIN, COUT, OUT32><<<grid, 128, smem, ctx.stream>>>(in, wg, bias, out, out32, g, relu, err);
+    k_conv3d_tc<CIN, COUT, OUT32><<<grid, kConvThreads, smem, ctx.stream>>>(in, wg, bias, out, out32, g, relu, err);
     ctx.count_launch();
 }
 

@@ -167,31 +167,58 @@ inline size_t conv_smem_bytes(const VoxGrid& g) {
 
 constexpr int kConvWaitLimit = 1 << 22;
 
+// 8 consecutive FP32 columns of this thread's tensor-memory lane.
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+constexpr int kConvThreads = 256;
+
 // out = act(conv(in) + bias) on the 8-channel plane layout, or (OUT32) FP32 channel-last output of
 // the interior voxels [((z-1) n + y-1) n + x-1][C_out] without activation.
 //   wg: the layer's BF16 weights in the B-operand layout [tap][k16 chunk][half][C_out][8].
 //   err: set to 1 when an mbarrier wait gives up (no tile after that is computed).
+// A persistent CTA of eight warps walks its tiles (128 padded rows each) through a three-stage
+// pipeline: the TMA brings the next tile's spans into one of two buffers, one thread issues the
+// 27 x C_in/16 MMAs of this tile into one of two accumulators in tensor memory, and all eight warps
+// meanwhile drain the previous tile's accumulator (warp w reads tensor-memory lanes 32 (w mod 4) ..
+// + 31, columns of half w / 4).  So the tensor pipe runs the MMAs of tile t while the epilogue of
+// tile t - 1 and the copies of tile t + 1 are in flight.  Every wait is bounded; a block that gives
+// up drains its copies and MMAs in flight (bounded) before its shared and tensor memory are freed.
 template <int CIN, int COUT, bool OUT32>
-__global__ void __launch_bounds__(128) k_conv3d_tc(const uint4* __restrict__ in, const uint4* __restrict__ wg,
-                                                   const float* __restrict__ bias, uint4* __restrict__ out,
-                                                   float* __restrict__ out32, VoxGrid g, int relu,
-                                                   unsigned* __restrict__ err) {
+__global__ void __launch_bounds__(kConvThreads) k_conv3d_tc(const uint4* __restrict__ in, const uint4* __restrict__ wg,
+                                                            const float* __restrict__ bias, uint4* __restrict__ out,
+                                                            float* __restrict__ out32, VoxGrid g, int relu,
+                                                            unsigned* __restrict__ err) {
     static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT >= 16 && COUT <= 32, "channel counts");
     constexpr int KC = CIN / 16, PL = CIN / 8;
-    constexpr uint32_t kCols = 32;
+    constexpr int HALF = COUT / 2;                           // accumulator columns an epilogue warp takes
+    constexpr uint32_t kCols = 2 * COUT <= 32 ? 32 : 64;     // two accumulators of COUT columns
     extern __shared__ __align__(128) unsigned char conv_smem[];
-    __shared__ __align__(8) uint64_t mbar;     // MMA completion
-    __shared__ __align__(8) uint64_t lbar[2];  // span copies of buffer 0 / 1
+    __shared__ __align__(8) uint64_t mbar[2];  // MMAs into accumulator 0 / 1 complete
+    __shared__ __align__(8) uint64_t lbar[2];  // span copies into buffer 0 / 1 complete
     __shared__ uint32_t tmem_slot;
     uint4* w_s = reinterpret_cast<uint4*>(conv_smem);
     uint4* a_s = reinterpret_cast<uint4*>(conv_smem + conv_weight_bytes<CIN, COUT>());
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int quarter = warp & 3, half = warp >> 2;
     const int bufsz = 3 * PL * g.span;  // uint4 per span buffer
 
-    for (int e = tid; e < (int)(conv_weight_bytes<CIN, COUT>() / 16); e += 128) w_s[e] = wg[e];
+    for (int e = tid; e < (int)(conv_weight_bytes<CIN, COUT>() / 16); e += kConvThreads) w_s[e] = wg[e];
+    float bv[HALF];
+#pragma unroll
+    for (int i = 0; i < HALF; ++i) bv[i] = bias ? bias[half * HALF + i] : 0.0f;
     if (warp == 0) tmem_alloc(&tmem_slot, kCols);
     if (tid == 0) {
-        mbar_init(smem_addr(&mbar), 1);
+        mbar_init(smem_addr(&mbar[0]), 1);
+        mbar_init(smem_addr(&mbar[1]), 1);
         mbar_init(smem_addr(&lbar[0]), 1);
         mbar_init(smem_addr(&lbar[1]), 1);
     }
@@ -200,9 +227,7 @@ __global__ void __launch_bounds__(128) k_conv3d_tc(const uint4* __restrict__ in,
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
-    const uint32_t bar = smem_addr(&mbar);
     constexpr uint32_t idesc = umma_idesc_bf16(128, COUT);
-    bool ok = true;
 
     // Thread 0: the 3 * PL spans of tile t into buffer b, one bulk copy each (a span is g.span
     // consecutive 16-byte rows of one 8-channel plane), completing on lbar[b].
@@ -217,25 +242,62 @@ __global__ void __launch_bounds__(128) k_conv3d_tc(const uint4* __restrict__ in,
                              in + (size_t)p * g.rows + g.front + q0, (uint32_t)g.span * 16u, lb);
             }
     };
-    if (tid == 0 && (int)blockIdx.x < g.tiles) issue(blockIdx.x, 0);
-    bool prefetched = false;   // a copy into the other buffer is in flight
-    bool mma_issued = false;   // this iteration's MMAs were issued
-
-    int it = 0;
+    // The epilogue of tile t from accumulator b: this thread's row, HALF columns.
+    auto epilogue = [&](int t, int b) {
+        float v[HALF];
+        const uint32_t ta = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(b * COUT + half * HALF);
+        if constexpr (HALF == 16) {
+            tmem_ld16(ta, v);
+        } else {
+            tmem_ld8(ta, v);
+        }
+        const int q = g.pp + 128 * t + 32 * quarter + lane;
+        const int x = q % g.np, y = (q / g.np) % g.np, z = q / g.pp;
+        if (x < 1 || x > g.n || y < 1 || y > g.n || z < 1 || z > g.n) return;
+        if (OUT32) {
+            float4* o = reinterpret_cast<float4*>(out32 + ((size_t)((z - 1) * g.n + (y - 1)) * g.n + (x - 1)) * COUT +
+                                                  half * HALF);
+#pragma unroll
+            for (int c = 0; c < HALF; c += 4)
+                o[c / 4] = make_float4(v[c] + bv[c], v[c + 1] + bv[c + 1], v[c + 2] + bv[c + 2], v[c + 3] + bv[c + 3]);
+        } else {
+#pragma unroll
+            for (int c8 = 0; c8 < HALF / 8; ++c8) {
+                float w8[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const float s = v[8 * c8 + i] + bv[8 * c8 + i];
+                    w8[i] = (relu && s < 0.0f) ? 0.0f : s;
+                }
+                uint4 pk;
+                pk.x = pack_bf16x2(w8[0], w8[1]);
+                pk.y = pack_bf16x2(w8[2], w8[3]);
+                pk.z = pack_bf16x2(w8[4], w8[5]);
+                pk.w = pack_bf16x2(w8[6], w8[7]);
+                out[(size_t)(half * HALF / 8 + c8) * g.rows + g.front + q] = pk;
+            }
+        }
+    };
+    // copies and MMA batches issued / waited for, per buffer and accumulator (uniform in the block;
+    // scalars, so that they stay in registers)
+    int ls0 = 0, ls1 = 0, lw0 = 0, lw1 = 0, ms0 = 0, ms1 = 0, mw0 = 0, mw1 = 0;
+    if ((int)blockIdx.x < g.tiles) {
+        if (tid == 0) issue(blockIdx.x, 0);
+        ls0 = 1;
+    }
+    bool ok = true;
+    int it = 0, prev_t = -1;
     for (int t = blockIdx.x; t < g.tiles; t += gridDim.x, ++it) {
-        const int start = g.pp + 128 * t;  // padded row of tile row 0
         const int b = it & 1;
-        // the next tile's spans into the other buffer (its last MMAs were waited for below)
-        prefetched = t + (int)gridDim.x < g.tiles;
-        if (tid == 0 && prefetched) issue(t + gridDim.x, b ^ 1);
         // this tile's spans (every thread waits, bounded; the block gives up together)
-        const int landed = mbar_wait(smem_addr(&lbar[b]), (uint32_t)((it >> 1) & 1), kConvWaitLimit) ? 1 : 0;
+        const int lw = b ? lw1 : lw0;
+        const int landed = mbar_wait(smem_addr(&lbar[b]), (uint32_t)(lw & 1), kConvWaitLimit) ? 1 : 0;
         if (!__syncthreads_and(landed)) {
             ok = false;
-            if (tid == 0) atomicOr(err, 1u);
             break;
         }
-        mma_issued = true;
+        if (b) ++lw1; else ++lw0;
+        // its MMAs into accumulator b (free: its last epilogue ended before the barrier below)
         if (tid == 0) {
             tc_fence_after();
             uint32_t acc = 0;
@@ -247,64 +309,57 @@ __global__ void __launch_bounds__(128) k_conv3d_tc(const uint4* __restrict__ in,
                 for (int kc = 0; kc < KC; ++kc) {
                     const uint32_t aa = a0 + (uint32_t)(((dz * PL + 2 * kc) * g.span + dy * g.np + dx) * 16);
                     const uint32_t bb = w0 + (uint32_t)((tap * KC + kc) * 2 * COUT * 16);
-                    umma_bf16(tmem, umma_sdesc(aa, (uint32_t)g.span * 16, 128), umma_sdesc(bb, COUT * 16, 128),
-                              idesc, acc);
+                    umma_bf16(tmem + (uint32_t)(b * COUT), umma_sdesc(aa, (uint32_t)g.span * 16, 128),
+                              umma_sdesc(bb, COUT * 16, 128), idesc, acc);
                     acc = 1;
                 }
             }
-            umma_commit(bar);
+            umma_commit(smem_addr(&mbar[b]));
         }
-        // every thread waits (bounded); the block gives up together, so no barrier is left unmatched
-        const int waited = mbar_wait(bar, (uint32_t)(it & 1), kConvWaitLimit) ? 1 : 0;
-        if (!__syncthreads_and(waited)) {
-            ok = false;
-            if (tid == 0) atomicOr(err, 1u);
-            break;
-        }
-        mma_issued = false;
-        tc_fence_after();
-        float v[COUT];
-#pragma unroll
-        for (int c = 0; c < COUT; c += 16) {
-            float part[16];
-            tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, part);
-#pragma unroll
-            for (int i = 0; i < 16; ++i) v[c + i] = part[i];
-        }
-        const int q = start + 32 * warp + lane;
-        const int x = q % g.np, y = (q / g.np) % g.np, z = q / g.pp;
-        if (x >= 1 && x <= g.n && y >= 1 && y <= g.n && z >= 1 && z <= g.n) {
-            if (OUT32) {
-                float* o = out32 + ((size_t)((z - 1) * g.n + (y - 1)) * g.n + (x - 1)) * COUT;
-#pragma unroll
-                for (int c = 0; c < COUT; ++c) o[c] = v[c] + (bias ? bias[c] : 0.0f);
-            } else {
-#pragma unroll
-                for (int c8 = 0; c8 < COUT / 8; ++c8) {
-                    float w8[8];
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        float s = v[8 * c8 + i] + (bias ? bias[8 * c8 + i] : 0.0f);
-                        w8[i] = (relu && s < 0.0f) ? 0.0f : s;
-                    }
-                    uint4 pk;
-                    pk.x = pack_bf16x2(w8[0], w8[1]);
-                    pk.y = pack_bf16x2(w8[2], w8[3]);
-                    pk.z = pack_bf16x2(w8[4], w8[5]);
-                    pk.w = pack_bf16x2(w8[6], w8[7]);
-                    out[(size_t)c8 * g.rows + g.front + q] = pk;
-                }
+        if (b) ++ms1; else ++ms0;
+        if (it > 0) {
+            // the previous tile's MMAs: their accumulator is then readable and their span buffer free
+            const int mw = b ? mw0 : mw1;  // accumulator b ^ 1
+            const int done = mbar_wait(smem_addr(&mbar[b ^ 1]), (uint32_t)(mw & 1), kConvWaitLimit) ? 1 : 0;
+            if (!__syncthreads_and(done)) {
+                ok = false;
+                break;
             }
+            if (b) ++mw0; else ++mw1;
+        }
+        const int tn = t + (int)gridDim.x;
+        if (tn < g.tiles) {
+            if (tid == 0) issue(tn, b ^ 1);
+            if (b) ++ls0; else ++ls1;
+        }
+        if (it > 0) {
+            tc_fence_after();
+            epilogue(prev_t, b ^ 1);
         }
         tc_fence_before();
-        __syncthreads();
+        __syncthreads();  // the epilogue's reads of accumulator b ^ 1 end before its next MMAs
+        tc_fence_after();
+        prev_t = t;
+    }
+    if (ok && it > 0) {
+        const int bl = (it - 1) & 1;
+        const int mw = bl ? mw1 : mw0;
+        const int done = mbar_wait(smem_addr(&mbar[bl]), (uint32_t)(mw & 1), kConvWaitLimit) ? 1 : 0;
+        if (__syncthreads_and(done)) {
+            if (bl) ++mw1; else ++mw0;
+            tc_fence_after();
+            epilogue(prev_t, bl);
+        } else {
+            ok = false;
+        }
     }
     if (!ok && tid == 0) {
-        // a block that gave up drains its copies and MMAs still in flight (bounded) before its shared
-        // and tensor memory are released
-        mbar_wait(smem_addr(&lbar[it & 1]), (uint32_t)((it >> 1) & 1), kConvWaitLimit);
-        if (prefetched) mbar_wait(smem_addr(&lbar[(it + 1) & 1]), (uint32_t)(((it + 1) >> 1) & 1), kConvWaitLimit);
-        if (mma_issued) mbar_wait(bar, (uint32_t)(it & 1), kConvWaitLimit);
+        atomicOr(err, 1u);
+        // copies and MMAs still in flight finish (bounded) before the shared and tensor memory go
+        if (ls0 > lw0) mbar_wait(smem_addr(&lbar[0]), (uint32_t)(lw0 & 1), kConvWaitLimit);
+        if (ls1 > lw1) mbar_wait(smem_addr(&lbar[1]), (uint32_t)(lw1 & 1), kConvWaitLimit);
+        if (ms0 > mw0) mbar_wait(smem_addr(&mbar[0]), (uint32_t)(mw0 & 1), kConvWaitLimit);
+        if (ms1 > mw1) mbar_wait(smem_addr(&mbar[1]), (uint32_t)(mw1 & 1), kConvWaitLimit);
     }
     tc_fence_before();
     __syncthreads();

@@ -724,6 +724,9 @@ void learned_train(Context& ctx, LearnedNet& net, const numa_learned_train_param
             const double sfac = p.states == 1 ? 1.0 : (double)st / (double)(p.states - 1);
             k_axpby64<<<ew(ctx, N), 256, 0, ctx.stream>>>(u.p, sfac, u.p, 0.0, us.p, N);
             ctx.count_launch();
+            // c holds N doubles: the FP64 cache (the mixed solve above left the operator keeping
+            // RN32(c) and RN32(F) after them, which would write past c)
+            op.prepare_cache(NUMA_GPU_FP64);
             op.eval(us.p, F.p, c.p, nullptr);
             const float* c0 = chain.restrict_nat<double>(c.p, tmp.p);
             bratu_coef32(ctx, c.p, c32.p, N);

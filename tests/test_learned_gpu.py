@@ -125,6 +125,20 @@ def test_learned_preconditioner_trains_and_solves(gpu):
     assert np.linalg.norm(xl - x64) <= 1e-8 * np.linalg.norm(x64)
 
 
+def test_training_is_repeatable(gpu):
+    """The same seeds give the same training data and the same network, bit for bit, run after run in
+    one process (the data come from solves whose kernels and reductions have a fixed order)."""
+    G = _G()
+    runs = []
+    for _ in range(2):
+        net = G.LearnedNet(gpu, 15, seed=3)
+        rep = net.train(31, instances=2, states=2, rhs_per_state=1, krylov_per_state=4, epochs=2, batch=4, lr=2e-3,
+                        seed=11)
+        runs.append((rep["target_ms"], rep["loss_first"], net.get_params()))
+    assert runs[0][0] == runs[1][0]
+    assert np.array_equal(runs[0][2], runs[1][2])
+
+
 def test_stagnation_falls_back_to_the_vcycle(gpu):
     """A network that corrects in the wrong direction (an untrained one with its weights scaled
     up tenfold) makes an FGMRES iteration stall; the provider then hands the rest of that linear
