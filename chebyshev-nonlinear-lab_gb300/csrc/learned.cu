@@ -48,21 +48,30 @@ __global__ void k_pack_w(const float* __restrict__ w, __nv_bfloat16* __restrict_
     }
 }
 
+template <int CIN, int COUT, bool OUT32, int NST>
+void launch_conv_stages(Context& ctx, const VoxGrid& g, const uint4* in, const uint4* wg, const float* bias, uint4* out,
+                        float* out32, int relu, unsigned* err, size_t smem) {
+    // persistent CTAs: as many as fit on the GPU at once, each pipelining its tiles
+    int per_sm = 0;
+    NUMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3d_tc<CIN, COUT, OUT32, NST>, kConvThreads,
+                                                            smem));
+    const int grid = std::max(1, std::min(g.tiles, std::max(1, per_sm) * ctx.sm_count));
+    k_conv3d_tc<CIN, COUT, OUT32, NST><<<grid, kConvThreads, smem, ctx.stream>>>(in, wg, bias, out, out32, g, relu, err);
+    ctx.count_launch();
+}
+
+// Three span buffers where they fit in shared memory, else two.
 template <int CIN, int COUT, bool OUT32>
 void launch_conv(Context& ctx, const VoxGrid& g, const uint4* in, const uint4* wg, const float* bias, uint4* out,
                  float* out32, int relu, unsigned* err) {
-    const size_t smem = conv_smem_bytes<CIN, COUT>(g);
-    const int lim = set_dynamic_smem_limit(ctx, k_conv3d_tc<CIN, COUT, OUT32>);
-    if (smem > (size_t)lim) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "convolution tile exceeds shared memory");
     if (OUT32 && (reinterpret_cast<uintptr_t>(out32) & 15u))
         throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "convolution FP32 output must be 16-byte aligned");
-    // persistent CTAs: as many as fit on the GPU at once, each pipelining its tiles
-    int per_sm = 0;
-    NUMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3d_tc<CIN, COUT, OUT32>, kConvThreads,
-                                                            smem));
-    const int grid = std::max(1, std::min(g.tiles, std::max(1, per_sm) * ctx.sm_count));
-    k_conv3d_tc<CIN, COUT, OUT32><<<grid, kConvThreads, smem, ctx.stream>>>(in, wg, bias, out, out32, g, relu, err);
-    ctx.count_launch();
+    const int lim3 = set_dynamic_smem_limit(ctx, k_conv3d_tc<CIN, COUT, OUT32, 3>);
+    const int lim2 = set_dynamic_smem_limit(ctx, k_conv3d_tc<CIN, COUT, OUT32, 2>);
+    const size_t s3 = conv_smem_bytes<CIN, COUT>(g, 3), s2 = conv_smem_bytes<CIN, COUT>(g, 2);
+    if (s3 <= (size_t)lim3) launch_conv_stages<CIN, COUT, OUT32, 3>(ctx, g, in, wg, bias, out, out32, relu, err, s3);
+    else if (s2 <= (size_t)lim2) launch_conv_stages<CIN, COUT, OUT32, 2>(ctx, g, in, wg, bias, out, out32, relu, err, s2);
+    else throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "convolution tile exceeds shared memory");
 }
 
 __device__ __forceinline__ void unpack8(const uint4 u, float (&f)[8]) {

@@ -158,11 +158,11 @@ template <int CIN, int COUT>
 __host__ __device__ constexpr size_t conv_weight_bytes() {
     return (size_t)27 * (CIN / 16) * 2 * COUT * 16;
 }
-// Weights plus two span buffers (<= 153 KB at the largest supported shape): the spans of the next
-// tile are copied by the TMA into one buffer while the MMAs of this tile read the other.
+// Weights plus `stages` span buffers (three at the largest supported shape: 207 KB): the TMA fills
+// the buffers of the next tiles while the MMAs of this tile read one.
 template <int CIN, int COUT>
-inline size_t conv_smem_bytes(const VoxGrid& g) {
-    return conv_weight_bytes<CIN, COUT>() + (size_t)2 * 3 * (CIN / 8) * g.span * 16;
+inline size_t conv_smem_bytes(const VoxGrid& g, int stages) {
+    return conv_weight_bytes<CIN, COUT>() + (size_t)stages * 3 * (CIN / 8) * g.span * 16;
 }
 
 constexpr int kConvWaitLimit = 1 << 22;
@@ -179,187 +179,192 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
     for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-constexpr int kConvThreads = 256;
+// One arrival on bar.
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+constexpr int kConvEpiWarps = 8;                          // warps that drain the accumulators
+constexpr int kConvThreads = 32 * (kConvEpiWarps + 1);    // and one that feeds the TMA and the tensor cores
 
 // out = act(conv(in) + bias) on the 8-channel plane layout, or (OUT32) FP32 channel-last output of
 // the interior voxels [((z-1) n + y-1) n + x-1][C_out] without activation.
 //   wg: the layer's BF16 weights in the B-operand layout [tap][k16 chunk][half][C_out][8].
 //   err: set to 1 when an mbarrier wait gives up (no tile after that is computed).
-// A persistent CTA of eight warps walks its tiles (128 padded rows each) through a three-stage
-// pipeline: the TMA brings the next tile's spans into one of two buffers, one thread issues the
-// 27 x C_in/16 MMAs of this tile into one of two accumulators in tensor memory, and all eight warps
-// meanwhile drain the previous tile's accumulator (warp w reads tensor-memory lanes 32 (w mod 4) ..
-// + 31, columns of half w / 4).  So the tensor pipe runs the MMAs of tile t while the epilogue of
-// tile t - 1 and the copies of tile t + 1 are in flight.  Every wait is bounded; a block that gives
-// up drains its copies and MMAs in flight (bounded) before its shared and tensor memory are freed.
-template <int CIN, int COUT, bool OUT32>
-__global__ void __launch_bounds__(kConvThreads) k_conv3d_tc(const uint4* __restrict__ in, const uint4* __restrict__ wg,
+// A persistent CTA walks its tiles (128 padded rows each) with its warps specialised and coupled
+// only through mbarriers:
+//  * warp 8, one thread: the TMA copies of each tile's spans into one of NST buffers (lbar), issued
+//    NST - 1 tiles ahead, and the
+//    27 x C_in/16 MMAs of each tile into one of two accumulators in tensor memory, committed to
+//    full[b]; an accumulator is reused once the epilogue warps released it (empty[b]), a span buffer
+//    once the MMAs that read it completed (full[b]);
+//  * warps 0-7: for each tile, wait for its accumulator, read their lanes (warp w: tensor-memory lanes
+//    32 (w mod 4) .. + 31, the columns of half w / 4) into registers, release the accumulator, then
+//    add the bias and store.
+// So the copies of tile t + 1, the MMAs of tile t and the stores of tile t - 1 overlap.  Every wait is
+// bounded; the thread that gives up sets err and waits (bounded) for its copies and MMAs in flight
+// before the shared and tensor memory are freed.
+template <int CIN, int COUT, bool OUT32, int NST>
+__global__ void __launch_bounds__(kConvThreads, 1) k_conv3d_tc(const uint4* __restrict__ in, const uint4* __restrict__ wg,
                                                             const float* __restrict__ bias, uint4* __restrict__ out,
                                                             float* __restrict__ out32, VoxGrid g, int relu,
                                                             unsigned* __restrict__ err) {
     static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT >= 16 && COUT <= 32, "channel counts");
     constexpr int KC = CIN / 16, PL = CIN / 8;
     constexpr int HALF = COUT / 2;                           // accumulator columns an epilogue warp takes
-    constexpr uint32_t kCols = 2 * COUT <= 32 ? 32 : 64;     // two accumulators of COUT columns
+    constexpr int NACC = 2;                                  // accumulators of COUT columns in tensor memory
+    constexpr uint32_t kCols = NACC * COUT <= 32 ? 32 : (NACC * COUT <= 64 ? 64 : 128);
     extern __shared__ __align__(128) unsigned char conv_smem[];
-    __shared__ __align__(8) uint64_t mbar[2];  // MMAs into accumulator 0 / 1 complete
-    __shared__ __align__(8) uint64_t lbar[2];  // span copies into buffer 0 / 1 complete
+    __shared__ __align__(8) uint64_t lbar[NST];    // span copies into buffer 0 .. NST - 1 complete
+    __shared__ __align__(8) uint64_t full[NACC];   // MMAs into accumulator a complete
+    __shared__ __align__(8) uint64_t empty[NACC];  // accumulator a read out by the epilogue warps
     __shared__ uint32_t tmem_slot;
     uint4* w_s = reinterpret_cast<uint4*>(conv_smem);
     uint4* a_s = reinterpret_cast<uint4*>(conv_smem + conv_weight_bytes<CIN, COUT>());
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int quarter = warp & 3, half = warp >> 2;
     const int bufsz = 3 * PL * g.span;  // uint4 per span buffer
+    const int ntile = (int)blockIdx.x < g.tiles ? (g.tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
 
     for (int e = tid; e < (int)(conv_weight_bytes<CIN, COUT>() / 16); e += kConvThreads) w_s[e] = wg[e];
-    float bv[HALF];
-#pragma unroll
-    for (int i = 0; i < HALF; ++i) bv[i] = bias ? bias[half * HALF + i] : 0.0f;
     if (warp == 0) tmem_alloc(&tmem_slot, kCols);
     if (tid == 0) {
-        mbar_init(smem_addr(&mbar[0]), 1);
-        mbar_init(smem_addr(&mbar[1]), 1);
-        mbar_init(smem_addr(&lbar[0]), 1);
-        mbar_init(smem_addr(&lbar[1]), 1);
+        for (int q = 0; q < NST; ++q) mbar_init(smem_addr(&lbar[q]), 1);
+        for (int q = 0; q < NACC; ++q) {
+            mbar_init(smem_addr(&full[q]), 1);
+            mbar_init(smem_addr(&empty[q]), kConvEpiWarps);
+        }
     }
     fence_proxy_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
-    constexpr uint32_t idesc = umma_idesc_bf16(128, COUT);
 
-    // Thread 0: the 3 * PL spans of tile t into buffer b, one bulk copy each (a span is g.span
-    // consecutive 16-byte rows of one 8-channel plane), completing on lbar[b].
-    auto issue = [&](int t, int b) {
-        const uint32_t lb = smem_addr(&lbar[b]);
-        mbar_arrive_expect_tx(lb, (uint32_t)bufsz * 16u);
-        const int start = g.pp + 128 * t;  // padded row of tile row 0
-        for (int dz = 0; dz < 3; ++dz)
-            for (int p = 0; p < PL; ++p) {
-                const int q0 = start + (dz - 1) * g.pp - g.np - 1;
-                tma_bulk_g2s(smem_addr(a_s + (size_t)b * bufsz + (size_t)(dz * PL + p) * g.span),
-                             in + (size_t)p * g.rows + g.front + q0, (uint32_t)g.span * 16u, lb);
-            }
-    };
-    // The epilogue of tile t from accumulator b: this thread's row, HALF columns.
-    auto epilogue = [&](int t, int b) {
-        float v[HALF];
-        const uint32_t ta = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(b * COUT + half * HALF);
-        if constexpr (HALF == 16) {
-            tmem_ld16(ta, v);
-        } else {
-            tmem_ld8(ta, v);
-        }
-        const int q = g.pp + 128 * t + 32 * quarter + lane;
-        const int x = q % g.np, y = (q / g.np) % g.np, z = q / g.pp;
-        if (x < 1 || x > g.n || y < 1 || y > g.n || z < 1 || z > g.n) return;
-        if (OUT32) {
-            float4* o = reinterpret_cast<float4*>(out32 + ((size_t)((z - 1) * g.n + (y - 1)) * g.n + (x - 1)) * COUT +
-                                                  half * HALF);
-#pragma unroll
-            for (int c = 0; c < HALF; c += 4)
-                o[c / 4] = make_float4(v[c] + bv[c], v[c + 1] + bv[c + 1], v[c + 2] + bv[c + 2], v[c + 3] + bv[c + 3]);
-        } else {
-#pragma unroll
-            for (int c8 = 0; c8 < HALF / 8; ++c8) {
-                float w8[8];
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const float s = v[8 * c8 + i] + bv[8 * c8 + i];
-                    w8[i] = (relu && s < 0.0f) ? 0.0f : s;
+    if (warp == kConvEpiWarps) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = umma_idesc_bf16(128, COUT);
+            // the 3 * PL spans of tile number k (of this CTA) into buffer k mod NST, one bulk copy each
+            auto issue = [&](int k) {
+                const int b = k % NST;
+                const uint32_t lb = smem_addr(&lbar[b]);
+                mbar_arrive_expect_tx(lb, (uint32_t)bufsz * 16u);
+                const int start = g.pp + 128 * ((int)blockIdx.x + k * (int)gridDim.x);  // padded row of tile row 0
+                for (int dz = 0; dz < 3; ++dz)
+                    for (int p = 0; p < PL; ++p) {
+                        const int q0 = start + (dz - 1) * g.pp - g.np - 1;
+                        tma_bulk_g2s(smem_addr(a_s + (size_t)b * bufsz + (size_t)(dz * PL + p) * g.span),
+                                     in + (size_t)p * g.rows + g.front + q0, (uint32_t)g.span * 16u, lb);
+                    }
+            };
+            int issued = 0, landed = 0, mmas = 0;  // tiles copied, waited for, given to the tensor cores
+            bool ok = true;
+            while (issued < ntile && issued < NST) issue(issued++);
+            for (int it = 0; it < ntile; ++it) {
+                const int b = it % NACC, sb = it % NST;  // accumulator, span buffer
+                if (!mbar_wait(smem_addr(&lbar[sb]), (uint32_t)((it / NST) & 1), kConvWaitLimit)) {
+                    ok = false;
+                    break;
                 }
-                uint4 pk;
-                pk.x = pack_bf16x2(w8[0], w8[1]);
-                pk.y = pack_bf16x2(w8[2], w8[3]);
-                pk.z = pack_bf16x2(w8[4], w8[5]);
-                pk.w = pack_bf16x2(w8[6], w8[7]);
-                out[(size_t)(half * HALF / 8 + c8) * g.rows + g.front + q] = pk;
-            }
-        }
-    };
-    // copies and MMA batches issued / waited for, per buffer and accumulator (uniform in the block;
-    // scalars, so that they stay in registers)
-    int ls0 = 0, ls1 = 0, lw0 = 0, lw1 = 0, ms0 = 0, ms1 = 0, mw0 = 0, mw1 = 0;
-    if ((int)blockIdx.x < g.tiles) {
-        if (tid == 0) issue(blockIdx.x, 0);
-        ls0 = 1;
-    }
-    bool ok = true;
-    int it = 0, prev_t = -1;
-    for (int t = blockIdx.x; t < g.tiles; t += gridDim.x, ++it) {
-        const int b = it & 1;
-        // this tile's spans (every thread waits, bounded; the block gives up together)
-        const int lw = b ? lw1 : lw0;
-        const int landed = mbar_wait(smem_addr(&lbar[b]), (uint32_t)(lw & 1), kConvWaitLimit) ? 1 : 0;
-        if (!__syncthreads_and(landed)) {
-            ok = false;
-            break;
-        }
-        if (b) ++lw1; else ++lw0;
-        // its MMAs into accumulator b (free: its last epilogue ended before the barrier below)
-        if (tid == 0) {
-            tc_fence_after();
-            uint32_t acc = 0;
-            const uint32_t a0 = smem_addr(a_s + (size_t)b * bufsz), w0 = smem_addr(w_s);
+                ++landed;
+                if (it >= NACC && !mbar_wait(smem_addr(&empty[b]), (uint32_t)(((it - NACC) / NACC) & 1), kConvWaitLimit)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                // the descriptors of tap (dz, dy, dx), chunk kc are the buffer's and the weights' plus
+                // an offset in 16-byte units in the start-address field (shared addresses stay below
+                // 2^18, so the field does not carry)
+                const uint64_t ad0 = umma_sdesc(smem_addr(a_s + (size_t)sb * bufsz), (uint32_t)g.span * 16, 128);
+                const uint64_t bd0 = umma_sdesc(smem_addr(w_s), COUT * 16, 128);
+                const uint32_t td = tmem + (uint32_t)(b * COUT);
+                uint32_t acc = 0;
 #pragma unroll 1
-            for (int tap = 0; tap < 27; ++tap) {
-                const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+                for (int dz = 0; dz < 3; ++dz) {
 #pragma unroll
-                for (int kc = 0; kc < KC; ++kc) {
-                    const uint32_t aa = a0 + (uint32_t)(((dz * PL + 2 * kc) * g.span + dy * g.np + dx) * 16);
-                    const uint32_t bb = w0 + (uint32_t)((tap * KC + kc) * 2 * COUT * 16);
-                    umma_bf16(tmem + (uint32_t)(b * COUT), umma_sdesc(aa, (uint32_t)g.span * 16, 128),
-                              umma_sdesc(bb, COUT * 16, 128), idesc, acc);
-                    acc = 1;
+                    for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+                        for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+                            for (int kc = 0; kc < KC; ++kc) {
+                                const uint32_t ao = (uint32_t)((dz * PL + 2 * kc) * g.span + dy * g.np + dx);
+                                const uint32_t bo = (uint32_t)(((dz * 9 + dy * 3 + dx) * KC + kc) * 2 * COUT);
+                                umma_bf16(td, ad0 + ao, bd0 + bo, idesc, acc);
+                                acc = 1;
+                            }
+                }
+                umma_commit(smem_addr(&full[b]));
+                ++mmas;
+                if (it >= 1 && issued < ntile) {
+                    // the previous tile's span buffer is free once its MMAs are done; tile it + NST - 1
+                    // goes there
+                    if (!mbar_wait(smem_addr(&full[(it - 1) % NACC]), (uint32_t)(((it - 1) / NACC) & 1), kConvWaitLimit)) {
+                        ok = false;
+                        break;
+                    }
+                    issue(issued++);
                 }
             }
-            umma_commit(smem_addr(&mbar[b]));
+            if (!ok) {
+                atomicOr(err, 1u);
+                // copies and MMAs in flight finish (bounded) before the shared and tensor memory go
+                for (int k = landed; k < issued; ++k)
+                    mbar_wait(smem_addr(&lbar[k % NST]), (uint32_t)((k / NST) & 1), kConvWaitLimit);
+                if (mmas > 0)
+                    mbar_wait(smem_addr(&full[(mmas - 1) % NACC]), (uint32_t)(((mmas - 1) / NACC) & 1), kConvWaitLimit);
+            }
         }
-        if (b) ++ms1; else ++ms0;
-        if (it > 0) {
-            // the previous tile's MMAs: their accumulator is then readable and their span buffer free
-            const int mw = b ? mw0 : mw1;  // accumulator b ^ 1
-            const int done = mbar_wait(smem_addr(&mbar[b ^ 1]), (uint32_t)(mw & 1), kConvWaitLimit) ? 1 : 0;
-            if (!__syncthreads_and(done)) {
-                ok = false;
+        __syncwarp();
+    } else {
+        const int quarter = warp & 3, half = warp >> 2;
+        float bv[HALF];
+#pragma unroll
+        for (int i = 0; i < HALF; ++i) bv[i] = bias ? bias[half * HALF + i] : 0.0f;
+        for (int it = 0; it < ntile; ++it) {
+            const int b = it % NACC;
+            // every lane waits (bounded); the warp goes on or gives up as one, converged for the
+            // warp-wide tensor-memory load
+            const int seen = mbar_wait(smem_addr(&full[b]), (uint32_t)((it / NACC) & 1), kConvWaitLimit) ? 1 : 0;
+            if (!__all_sync(0xffffffffu, seen)) {
+                if (lane == 0) atomicOr(err, 1u);
                 break;
             }
-            if (b) ++mw0; else ++mw1;
-        }
-        const int tn = t + (int)gridDim.x;
-        if (tn < g.tiles) {
-            if (tid == 0) issue(tn, b ^ 1);
-            if (b) ++ls0; else ++ls1;
-        }
-        if (it > 0) {
             tc_fence_after();
-            epilogue(prev_t, b ^ 1);
+            float v[HALF];
+            const uint32_t ta = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(b * COUT + half * HALF);
+            if constexpr (HALF == 16) {
+                tmem_ld16(ta, v);
+            } else {
+                tmem_ld8(ta, v);
+            }
+            tc_fence_before();
+            if (lane == 0) mbar_arrive(smem_addr(&empty[b]));
+            const int q = g.pp + 128 * ((int)blockIdx.x + it * (int)gridDim.x) + 32 * quarter + lane;
+            const int x = q % g.np, y = (q / g.np) % g.np, z = q / g.pp;
+            if (x < 1 || x > g.n || y < 1 || y > g.n || z < 1 || z > g.n) continue;
+            if (OUT32) {
+                float4* o = reinterpret_cast<float4*>(out32 + ((size_t)((z - 1) * g.n + (y - 1)) * g.n + (x - 1)) * COUT +
+                                                      half * HALF);
+#pragma unroll
+                for (int c = 0; c < HALF; c += 4)
+                    o[c / 4] = make_float4(v[c] + bv[c], v[c + 1] + bv[c + 1], v[c + 2] + bv[c + 2], v[c + 3] + bv[c + 3]);
+            } else {
+#pragma unroll
+                for (int c8 = 0; c8 < HALF / 8; ++c8) {
+                    float w8[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const float s = v[8 * c8 + i] + bv[8 * c8 + i];
+                        w8[i] = (relu && s < 0.0f) ? 0.0f : s;
+                    }
+                    uint4 pk;
+                    pk.x = pack_bf16x2(w8[0], w8[1]);
+                    pk.y = pack_bf16x2(w8[2], w8[3]);
+                    pk.z = pack_bf16x2(w8[4], w8[5]);
+                    pk.w = pack_bf16x2(w8[6], w8[7]);
+                    out[(size_t)(half * HALF / 8 + c8) * g.rows + g.front + q] = pk;
+                }
+            }
         }
-        tc_fence_before();
-        __syncthreads();  // the epilogue's reads of accumulator b ^ 1 end before its next MMAs
-        tc_fence_after();
-        prev_t = t;
-    }
-    if (ok && it > 0) {
-        const int bl = (it - 1) & 1;
-        const int mw = bl ? mw1 : mw0;
-        const int done = mbar_wait(smem_addr(&mbar[bl]), (uint32_t)(mw & 1), kConvWaitLimit) ? 1 : 0;
-        if (__syncthreads_and(done)) {
-            if (bl) ++mw1; else ++mw0;
-            tc_fence_after();
-            epilogue(prev_t, bl);
-        } else {
-            ok = false;
-        }
-    }
-    if (!ok && tid == 0) {
-        atomicOr(err, 1u);
-        // copies and MMAs still in flight finish (bounded) before the shared and tensor memory go
-        if (ls0 > lw0) mbar_wait(smem_addr(&lbar[0]), (uint32_t)(lw0 & 1), kConvWaitLimit);
-        if (ls1 > lw1) mbar_wait(smem_addr(&lbar[1]), (uint32_t)(lw1 & 1), kConvWaitLimit);
-        if (ms0 > mw0) mbar_wait(smem_addr(&mbar[0]), (uint32_t)(mw0 & 1), kConvWaitLimit);
-        if (ms1 > mw1) mbar_wait(smem_addr(&mbar[1]), (uint32_t)(mw1 & 1), kConvWaitLimit);
     }
     tc_fence_before();
     __syncthreads();
