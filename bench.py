@@ -316,9 +316,12 @@ def workload_config(args, path: str, levels: int | None) -> dict:
     if path == "mixed":
         orth = "two-pass (CGS2)" if args.orth == "cgs2" else "one-pass (CGS1)"
         solver = (f"FGMRES(30) (cycles up to 30 steps; {orth} classical Gram-Schmidt on lazily normalised basis "
-                  f"vectors, FP32 basis in double-FP32 arithmetic while the forcing term is >= 1e-5) right-"
-                  f"preconditioned by the FP32 GMG V(2,2) ({lv}), FP32 Jacobian products; FP64 residual, Newton "
-                  f"update, Arnoldi coefficients and least squares")
+                  f"vectors, FP32 basis in double-FP32 arithmetic while the forcing term is >= 1e-5, FP64 basis "
+                  f"below) right-preconditioned by the FP32 GMG V(2,2) ({lv}; the levels n <= 15 with the "
+                  f"Jacobian -Lap_h - lambda e^u of the iterate), Jacobian products of the FP32 preconditioned "
+                  f"vectors in FP32 arithmetic while the forcing term is >= 1e-5 and to FP64 accuracy "
+                  f"(double-FP32 stencil, FP64 coefficient) below; FP64 residual, Newton update, Arnoldi "
+                  f"coefficients and least squares")
     else:
         solver = (f"GMRES(30) with modified Gram-Schmidt (the reference's) right-preconditioned by the FP64 GMG "
                   f"V(2,2) ({lv}), FP64 Jacobian products")
@@ -326,7 +329,9 @@ def workload_config(args, path: str, levels: int | None) -> dict:
         "workload": f"Bratu3D {args.n}^3 lambda={args.lam} u0=0, {args.method.upper()} (Eisenstat-Walker forcing) + "
                     f"{solver}, stop at ||F||/||F0|| <= 1e-10",
         "n": args.n, "unknowns": args.n ** 3, "lambda": args.lam, "method": args.method, "path": path,
-        "precond": f"PoissonMG V(2,2) red-black Gauss-Seidel, {lv}", "gmres_restart": 30, "rtol_nl": 1e-10,
+        "precond": (f"PoissonMG V(2,2) red-black Gauss-Seidel, {lv}" if path != "mixed" else
+                    f"PoissonMG V(2,2) red-black Gauss-Seidel in FP32, {lv}, Jacobian-aware levels n <= 15"),
+        "gmres_restart": 30, "rtol_nl": 1e-10,
         "orth": args.orth if path == "mixed" else "mgs",
         "jvp": "analytic (Bratu3D::jvp)",
         "l2": "inputs larger than L2: one vector is 133 MB and the solve's working set ~6 GB vs 129 MB L2",
@@ -335,11 +340,14 @@ def workload_config(args, path: str, levels: int | None) -> dict:
 
 # ------------------------------------------------------------------ our arm
 def params_for(G, path: str, orth: str = "cgs1"):
+    """fp64: the reference's GMRES(30) with MGS.  mixed_fp32: FGMRES(30), CGS, FP32 Jacobian products.
+    mixed: the same with products of FP64 accuracy in the linear solves whose tolerance is below 1e-5."""
     p = G.default_params(rtol_nl=1e-10, gmres_restart=30)
-    if path == "mixed":
+    if path in ("mixed", "mixed_fp32"):
         p.flexible = 1
         p.jvp_precision = G.FP32
         p.orth = G.CGS2 if orth == "cgs2" else G.CGS1
+        p.jvp_tight = 1 if path == "mixed" else 0
     return p
 
 
@@ -383,10 +391,11 @@ def run_ours(args) -> int:
     op = G.Bratu3D(ctx, n, args.lam)
     pc64 = G.Provider.poisson_mg(ctx, n, precision=G.FP64)
     pc32 = G.Provider.poisson_mg(ctx, n, precision=G.FP32)
+    pcj = G.Provider.jacobian_mg(ctx, n)
     u0 = ctx.vec(N).fill(0.0)
     x = ctx.vec(N)
 
-    heads = {"fp64": (pc64, params_for(G, "fp64")), "mixed": (pc32, params_for(G, "mixed", args.orth))}
+    heads = {"fp64": (pc64, params_for(G, "fp64")), "mixed": (pcj, params_for(G, "mixed", args.orth))}
     mg_probe = G.PoissonMG(ctx, n)
     levels = mg_probe.levels()
     mg_probe.close()
@@ -406,7 +415,7 @@ def run_ours(args) -> int:
     # the inexact Chebyshev method (chebyshev_inexact, two linear solves and F'' per step) on both paths
     sec_c64, res_c64, _ = timed_solves(G, ctx, op, pc64, x, u0, "cheb", params_for(G, "fp64"), 2, 1, dist, stream)
     x_c64 = x.numpy() if dist.rank == 0 else None
-    sec_c32, res_c32, _ = timed_solves(G, ctx, op, pc32, x, u0, "cheb", params_for(G, "mixed", args.orth), 2, 1, dist,
+    sec_c32, res_c32, _ = timed_solves(G, ctx, op, pcj, x, u0, "cheb", params_for(G, "mixed", args.orth), 2, 1, dist,
                                        stream)
     x_c32 = x.numpy() if dist.rank == 0 else None
     ckeys = ("iters", "n_F", "n_JVP", "n_D2", "n_lin_iters", "n_prec", "converged")
@@ -415,8 +424,9 @@ def run_ours(args) -> int:
             "rel_err_between_paths": (float(np.linalg.norm(x_c32 - x_c64) / np.linalg.norm(x_c64))
                                       if dist.rank == 0 else None),
             "note": "chebyshev_inexact (J z = F, J w = F''[z, z], trial x - z - w/2, analytic F''), same "
-                    "configuration and preconditioners as the headline; mixed = FGMRES with the FP32 V-cycle and "
-                    "FP32 J v for both linear solves"}
+                    "configuration and preconditioners as the headline; mixed = FGMRES with the FP32 V-cycle "
+                    "(Jacobian-aware coarse levels) and FP32 J v, of FP64 accuracy below forcing 1e-5, for both "
+                    "linear solves"}
 
     # the learned preconditioner beside the V-cycle inside FGMRES (trained here, on this GPU, from
     # GMG-preconditioned solves of this grid at seeded lambda; lambda of the bench is held out)
@@ -427,8 +437,9 @@ def run_ours(args) -> int:
             trep = net.train(n, instances=4, states=3, rhs_per_state=2, krylov_per_state=8, epochs=8, batch=4,
                              lr=2e-3, seed=11)
             pcl = G.Provider.learned(ctx, n, net, stall=0.9)
-            sec_l, res_l, _ = timed_solves(G, ctx, op, pcl, x, u0, args.method, params_for(G, "mixed", args.orth),
-                                           max(1, args.steps // 2), 1, dist, stream)
+            sec_l, res_l, _ = timed_solves(G, ctx, op, pcl, x, u0, args.method,
+                                           params_for(G, "mixed_fp32", args.orth), max(1, args.steps // 2), 1, dist,
+                                           stream)
             x_l = x.numpy() if dist.rank == 0 else None
             applies, fallbacks = pcl.learned_stats()
             # held-out lambda at 127^3: a network trained the same way on that grid's hierarchy
@@ -446,7 +457,7 @@ def run_ours(args) -> int:
                     row = {"n": n2, "lambda": lam2}
                     for tag, pcx in (("mixed", pm2), ("learned", pl2)):
                         x2.fill(0.0)
-                        rr = G.solve(op2, x2, "nk", params_for(G, "mixed", args.orth), pcx)
+                        rr = G.solve(op2, x2, "nk", params_for(G, "mixed_fp32", args.orth), pcx)
                         row[tag] = [rr["iters"], rr["n_lin_iters"], rr["converged"]]
                     held.append(row)
             learned = {"s": sec_l, "res": res_l, "x": x_l, "training": trep, "applies": applies,
@@ -454,24 +465,25 @@ def run_ours(args) -> int:
         except G.NumaGPUError as exc:
             learned = {"skipped": str(exc)}
 
-    # the FP32 V-cycle with Jacobian-aware coarse levels (levels n <= 15 solve with -Lap_h - lambda e^u)
-    jac = None
+    # the mixed path's two steps, one at a time: the plain FP32 Poisson V-cycle with FP32 products
+    # throughout, then the Jacobian-aware coarse levels alone (levels n <= 15 with -Lap_h - lambda e^u)
+    steps_mixed = {}
     if dist.rank == 0:
-        pcj = G.Provider.jacobian_mg(ctx, n)
-        sec_j, res_j, _ = timed_solves(G, ctx, op, pcj, x, u0, args.method, params_for(G, "mixed", args.orth),
-                                       max(1, args.steps // 2), 1, dist, stream)
-        x_j = x.numpy()
-        jac = {"s": sec_j, "counts": {k: res_j[k] for k in ("iters", "n_F", "n_JVP", "n_lin_iters", "n_prec",
-                                                             "converged")},
-               "res_rel": res_j["res"] / res_j["res0"], "x": x_j,
-               "note": "mixed path with the Jacobian-aware coarse levels: the V-cycle's levels n <= 15 solve with "
-                       "-Lap_h - c (c = lambda e^u restricted) instead of -Lap_h; fine levels, FGMRES and the "
-                       "FP32 products as on the mixed path"}
+        for tag, pcs, prms, note in (
+                ("poisson_vcycle_fp32_products", pc32, params_for(G, "mixed_fp32", args.orth),
+                 "FP32 Poisson V-cycle (coarse levels -Lap_h), FP32 Jacobian products in every linear solve"),
+                ("jacobian_coarse_fp32_products", pcj, params_for(G, "mixed_fp32", args.orth),
+                 "Jacobian-aware coarse levels, FP32 Jacobian products in every linear solve")):
+            sec_s, res_s, _ = timed_solves(G, ctx, op, pcs, x, u0, args.method, prms, max(1, args.steps // 2), 1,
+                                           dist, stream)
+            steps_mixed[tag] = {"s": sec_s, "x": x.numpy(), "res_rel": res_s["res"] / res_s["res0"], "note": note,
+                                "counts": {k: res_s[k] for k in ("iters", "n_F", "n_JVP", "n_lin_iters", "n_prec",
+                                                                 "converged")}}
 
     # batched solves: 128 instances, n from {31, 63, 127}, lambda ~ U[1, 6.5] (seeded), mixed path
     batched = None
     if not args.no_batch and dist.rank == 0:
-        batched = batched_leg(G, ctx, stream, torch, dev, params_for(G, "mixed", "cgs1"))
+        batched = batched_leg(G, ctx, stream, torch, dev, params_for(G, "mixed_fp32", "cgs1"))
 
     # 2D Brusselator: 2048^2 periodic, 2 species, 20 implicit-Euler steps, NK + FGMRES(40) with the
     # FP32 coupled-block multigrid (FP64 outer), beside the all-FP64 form
@@ -485,22 +497,22 @@ def run_ours(args) -> int:
     h_out = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
     mgp = G.FP64 if args.path == "fp64" else G.FP32
 
-    def e2e_leg(mg_prec, prm_e, steps):
+    def e2e_leg(path, prm_e, steps):
+        kind, mg_prec = ("mg", G.FP64) if path == "fp64" else ("jacobian_mg", G.FP32)
         for _ in range(2):  # warm: allocations, the host entry's operator, hierarchy and captured graphs
-            G.solve_bratu3d_host(ctx, n, args.lam, h_in, h_out, args.method, "mg", mg_prec, prm_e)
+            G.solve_bratu3d_host(ctx, n, args.lam, h_in, h_out, args.method, kind, mg_prec, prm_e)
         dist.barrier()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with quiet_gc():
             ev0.record(stream)
             for _ in range(steps):
-                G.solve_bratu3d_host(ctx, n, args.lam, h_in, h_out, args.method, "mg", mg_prec, prm_e)
+                G.solve_bratu3d_host(ctx, n, args.lam, h_in, h_out, args.method, kind, mg_prec, prm_e)
             ev1.record(stream)
             ev1.synchronize()
         return dist.max(ev0.elapsed_time(ev1) * 1e-3 / steps), h_out.copy()
 
-    e2e_sec, x_e2e = e2e_leg(mgp, prm, max(1, args.steps))
-    other_mgp = G.FP32 if mgp == G.FP64 else G.FP64
-    e2e_other, _ = e2e_leg(other_mgp, prmo, max(1, args.steps // 2))
+    e2e_sec, x_e2e = e2e_leg(args.path, prm, max(1, args.steps))
+    e2e_other, _ = e2e_leg(other, prmo, max(1, args.steps // 2))
 
     # per-primitive breakdown of one solve of each path (CUDA-event timers inside the library)
     breakdown = {}
@@ -577,6 +589,7 @@ def run_ours(args) -> int:
                              f"{rcpu.get('iters')}/{rcpu.get('n_JVP')}/{rcpu.get('n_prec')}",
                    "single_thread": {"value": t_one, "unit": "s", "cores": 1}}
         err = float(np.linalg.norm(x_other - x_head) / np.linalg.norm(x_head))
+        x_fp64 = x_head if args.path == "fp64" else x_other
         fp64_sec = sec if args.path == "fp64" else sec_o
         mixed_sec = sec_o if args.path == "fp64" else sec
         line = {
@@ -589,15 +602,15 @@ def run_ours(args) -> int:
             "mixed_vs_plain": {"plain_fp64_s": fp64_sec, "mixed_s": mixed_sec, "ratio": fp64_sec / mixed_sec,
                                "rel_err_between_paths": err,
                                "other_counts": {k: res_o[k] for k in ("iters", "n_JVP", "n_prec", "converged")},
-                               "note": "mixed = FP32 V-cycle + FP32 Jacobian products inside FGMRES(30) with one-pass "
-                                       "classical Gram-Schmidt, FP64 residual / updates / Arnoldi; no learned "
-                                       "preconditioner"},
+                               "note": "mixed = FP32 V-cycle with Jacobian-aware coarse levels inside FGMRES(30) "
+                                       "with one-pass classical Gram-Schmidt, FP32 Jacobian products while the "
+                                       "forcing term is >= 1e-5 and products of FP64 accuracy below, FP64 residual / "
+                                       "updates / Arnoldi; no learned preconditioner"},
             "chebyshev": cheb,
             "learned_mixed": learned_summary(learned, fp64_sec, x_head if args.path == "fp64" else x_other),
-            "jacobian_coarse": (None if jac is None else dict(
-                {k: v for k, v in jac.items() if k != "x"},
-                rel_err_vs_fp64=float(np.linalg.norm(jac["x"] - (x_head if args.path == "fp64" else x_other)) /
-                                      np.linalg.norm(x_head if args.path == "fp64" else x_other)))),
+            "mixed_steps": {tag: dict({k: v for k, v in st.items() if k != "x"},
+                                      rel_err_vs_fp64=float(np.linalg.norm(st["x"] - x_fp64) / np.linalg.norm(x_fp64)))
+                            for tag, st in steps_mixed.items()},
             "batched": batched,
             "brusselator2d": bruss,
             "clocks": clk.summary(),
@@ -822,7 +835,7 @@ def run_kernel_case(G, ctx, args) -> int:
     if args.kernel_case == "batch":
         # the batched configuration through the batched solver: one warm batch, then args.steps batches
         inst = G.batch_config_instances(128, seed=42)
-        bs = G.BatchSolver(ctx, inst, params_for(G, "mixed", "cgs1"))
+        bs = G.BatchSolver(ctx, inst, params_for(G, "mixed_fp32", "cgs1"))
         bs.solve()
         t = 0.0
         for _ in range(max(1, args.steps)):
@@ -884,7 +897,8 @@ def run_kernel_case(G, ctx, args) -> int:
             ctx.sync()
     else:
         op = G.Bratu3D(ctx, n, args.lam)
-        pc = G.Provider.poisson_mg(ctx, n, precision=G.FP64 if args.path == "fp64" else G.FP32)
+        pc = (G.Provider.poisson_mg(ctx, n, precision=G.FP64) if args.path == "fp64" else
+              G.Provider.jacobian_mg(ctx, n))
         x = ctx.vec(N)
         for _ in range(max(1, args.steps)):
             x.fill(0.0)

@@ -314,6 +314,75 @@ __global__ void __launch_bounds__(BX* BY) k_jvp32f(const float* __restrict__ c32
     }
 }
 
+// One point of k_jvp32x: the product from FP32 values to FP64 accuracy on the FP32 pipe.  The
+// Laplacian sum 6v - (six neighbours) in double-FP32 arithmetic: 6v exact as a product and its FMA
+// error, each neighbour subtracted by two-sum with the rounding errors gathered in lo; scaled by
+// h^-2 (an FP32 integer below 2^24, so h^-2 hi is exact with its FMA error); widened to FP64 in one
+// addition; out = T - c v in one FP64 FMA with the FP64 coefficient.  Two FP64 instructions a point
+// (the FP64 product takes ten), and an error of a few 2^-48 of the largest partial sum.
+__device__ __forceinline__ void df_sub(float& hi, float& lo, float x) {
+    float s, e;
+    two_sum(hi, -x, s, e);
+    hi = s;
+    lo = __fadd_rn(lo, e);
+}
+__device__ __forceinline__ double jvp32x_point(float below, float cur, float above, float jm, float jp, float km,
+                                               float kp, double c, float h2inv) {
+    float hi = __fmul_rn(6.0f, cur);
+    float lo = __fmaf_rn(6.0f, cur, -hi);
+    df_sub(hi, lo, below);
+    df_sub(hi, lo, above);
+    df_sub(hi, lo, jm);
+    df_sub(hi, lo, jp);
+    df_sub(hi, lo, km);
+    df_sub(hi, lo, kp);
+    const float ph = __fmul_rn(h2inv, hi);
+    const float pl = __fmaf_rn(h2inv, lo, __fmaf_rn(h2inv, hi, -ph));
+    const double t = __dadd_rn(f32_to_f64(ph), f32_to_f64(pl));
+    return __fma_rn(-c, f32_to_f64(cur), t);
+}
+
+// The bound product from an FP32 v (the V-cycle's output) to FP64 accuracy, FP64 coefficient c and
+// FP64 out, for Krylov solves whose tolerance is below what FP32 arithmetic reaches.  Same march as
+// k_jvp32f: a (k, j) column walks i two planes a step with planes i-1, i, i+1 in registers.
+__global__ void __launch_bounds__(BX* BY) k_jvp32x(const double* __restrict__ c, const float* __restrict__ v,
+                                                   double* __restrict__ out, int n, int ichunk, float h2inv) {
+    pdl_wait();
+    pdl_trigger();
+    const int k = blockIdx.x * BX + threadIdx.x;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    if (k >= n || j >= n) return;
+    const int i0 = blockIdx.z * ichunk;
+    const int i1 = min(i0 + ichunk, n);
+    const size_t plane = (size_t)n * n;
+    const size_t col = (size_t)j * n + k;
+    const bool jlo = j > 0, jhi = j + 1 < n, klo = k > 0, khi = k + 1 < n;
+    float below = i0 > 0 ? v[(size_t)(i0 - 1) * plane + col] : 0.0f;
+    float cur = i0 < i1 ? v[(size_t)i0 * plane + col] : 0.0f;
+    int i = i0;
+    for (; i + 1 < i1; i += 2) {
+        const size_t p = (size_t)i * plane + col, q = p + plane;
+        const float a1 = v[q];  // i + 1 < i1 <= n
+        const float a2 = (i + 2 < n) ? v[q + plane] : 0.0f;
+        const float jm0 = jlo ? v[p - n] : 0.0f, jp0 = jhi ? v[p + n] : 0.0f;
+        const float km0 = klo ? v[p - 1] : 0.0f, kp0 = khi ? v[p + 1] : 0.0f;
+        const float jm1 = jlo ? v[q - n] : 0.0f, jp1 = jhi ? v[q + n] : 0.0f;
+        const float km1 = klo ? v[q - 1] : 0.0f, kp1 = khi ? v[q + 1] : 0.0f;
+        const double c0 = c[p], c1 = c[q];
+        out[p] = jvp32x_point(below, cur, a1, jm0, jp0, km0, kp0, c0, h2inv);
+        out[q] = jvp32x_point(cur, a1, a2, jm1, jp1, km1, kp1, c1, h2inv);
+        below = a1;
+        cur = a2;
+    }
+    if (i < i1) {
+        const size_t p = (size_t)i * plane + col;
+        const float above = (i + 1 < n) ? v[p + plane] : 0.0f;
+        const float jm = jlo ? v[p - n] : 0.0f, jp = jhi ? v[p + n] : 0.0f;
+        const float km = klo ? v[p - 1] : 0.0f, kp = khi ? v[p + 1] : 0.0f;
+        out[p] = jvp32x_point(below, cur, above, jm, jp, km, kp, c[p], h2inv);
+    }
+}
+
 // c32 = RN32(c) (integer conversion)
 __global__ void k_coef32(const double* __restrict__ c, float* __restrict__ c32, size_t N) {
     pdl_wait();
@@ -402,6 +471,19 @@ void Bratu3D::jvp_bound32f(const float* v32, float* out32) {
                (float)h2inv_);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d jvp32 (fp32 input and output)");
+}
+
+void Bratu3D::jvp_bound32x(const float* v32, double* out) {
+    if (!has_jvp32x()) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Bratu3D: no FP32-input FP64-accuracy product bound");
+    jvp_c32x(bound_c_, v32, out);
+}
+
+void Bratu3D::jvp_c32x(const double* c, const float* v32, double* out) {
+    if (n_ >= 4095) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "Bratu3D: the double-FP32 product needs n < 4095");
+    March m = march_shape((int)n_, false);
+    launch_pdl(k_jvp32x, m.grid, dim3(BX, BY), 0, ctx_.stream, c, v32, out, (int)n_, m.ichunk, (float)h2inv_);
+    ctx_.count_launch();
+    ctx_.check_launch("bratu3d jvp32x (fp32 input, fp64 accuracy)");
 }
 
 void Bratu3D::jvp_bound(const double* v, double* out) {

@@ -551,6 +551,13 @@ int numa_gpu_bratu3d_jvp(numa_gpu_bratu3d* op, const numa_gpu_vec* x, const numa
             f.coef32(c64.p, c32.p);
             f.jvp_c32(c32.p, v->d, out->d);
             c.sync();  // the temporaries are freed on return
+        } else if (mode == NUMA_GPU_DERIV_ANALYTIC_FP32X) {
+            DeviceArray<double> c64(f.size());
+            DeviceArray<float> v32(f.size());
+            f.coef(x->d, c64.p);
+            f.coef32(v->d, v32.p);  // RN32(v): the same integer conversion as RN32(c)
+            f.jvp_c32x(c64.p, v32.p, out->d);
+            c.sync();
         } else {
             need(mode == NUMA_GPU_DERIV_ANALYTIC, NUMA_GPU_ERR_INVALID_ARGUMENT, "unknown derivative mode");
             f.jvp_x(x->d, v->d, out->d);
@@ -931,7 +938,8 @@ int numa_gpu_solve_bratu3d_host(numa_gpu_ctx* ctx, size_t n, double lambda, int 
         need(n > 0 && n <= 65535, NUMA_GPU_ERR_INVALID_ARGUMENT, "grid size out of range");
         need(method >= NUMA_GPU_METHOD_NK && method <= NUMA_GPU_METHOD_TF2018, NUMA_GPU_ERR_INVALID_ARGUMENT,
              "unknown method");
-        need(precond_kind >= NUMA_GPU_PRECOND_NONE && precond_kind <= NUMA_GPU_PRECOND_JACOBI,
+        need((precond_kind >= NUMA_GPU_PRECOND_NONE && precond_kind <= NUMA_GPU_PRECOND_JACOBI) ||
+                 precond_kind == NUMA_GPU_PRECOND_JACOBIAN_MG,
              NUMA_GPU_ERR_INVALID_ARGUMENT, "unknown preconditioner");
         Context& c = *ctx->impl;
         CtxExtras& e = extras(ctx);
@@ -945,6 +953,7 @@ int numa_gpu_solve_bratu3d_host(numa_gpu_ctx* ctx, size_t n, double lambda, int 
         if (e.host_kind != precond_kind || e.host_prec != mg_precision || !e.host_pc) {
             if (precond_kind == NUMA_GPU_PRECOND_POISSON_MG) e.host_pc = make_mg_provider(c, n, 2, 2, mg_precision, 0);
             else if (precond_kind == NUMA_GPU_PRECOND_JACOBI) e.host_pc = make_jacobi_provider(*e.host_op);
+            else if (precond_kind == NUMA_GPU_PRECOND_JACOBIAN_MG) e.host_pc = make_jacobian_mg_provider(c, n, 2, 2);
             else e.host_pc = make_identity_provider(c, n * n * n);
             e.host_kind = precond_kind;
             e.host_prec = mg_precision;

@@ -200,6 +200,11 @@ public:
         Timers::Scope s(&t_, kT_JVP);
         f_.jvp_bound32f(v32, out32);
     }
+    bool has_apply32x() const override { return mode_ != NUMA_GPU_DERIV_FD && f_.has_jvp32x(); }
+    void apply32x(const float* v32, double* out) override {
+        Timers::Scope s(&t_, kT_JVP);
+        f_.jvp_bound32x(v32, out);
+    }
 
 private:
     NonlinearOp& f_;
@@ -329,6 +334,7 @@ GmresOptions gmres_opts(const KrylovParams& p, double rtol, double bnorm = -1.0,
     o.zero_guess = true;
     o.orth = p.orth;
     o.flexible = p.flexible;
+    o.precise_tight = p.jvp_tight;
     return o;
 }
 
@@ -374,6 +380,7 @@ KrylovParams params_from_c(const numa_krylov_params* c) {
     p.orth = c->orth;
     p.flexible = c->flexible != 0;
     p.jvp_precision = c->jvp_precision;
+    p.jvp_tight = c->jvp_tight != 0;
     return p;
 }
 

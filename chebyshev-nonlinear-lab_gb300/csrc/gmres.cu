@@ -589,6 +589,10 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
     // residual near that; inner products, updates and the solution update are computed in
     // double-FP32 and reduced in FP64, and the Hessenberg matrix and least squares stay FP64.
     const bool v32 = z32 && M->has_apply32f() && A.has_apply32f() && o.rtol >= kV32MinRtol;
+    // ... below that tolerance the basis is FP64, and the products of the FP32 vectors can be taken to
+    // FP64 accuracy (FP32 arithmetic in the Laplacian of a smooth vector loses digits to cancellation
+    // and bounds the attainable true residual well above the tolerance)
+    const bool precise = z32 && !v32 && o.precise_tight && A.has_apply32x();
     double* sigd = ctx_.scalar(kSlotGmresSig);
     if (v32) {
         V32_.resize((m + 1) * N);
@@ -675,7 +679,8 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
                 float* zj = Z32_.p + j * N;
                 M->apply32(vj, zj);
                 ++res.precs;
-                A.apply32(zj, w_.p);
+                if (precise) A.apply32x(zj, w_.p);
+                else A.apply32(zj, w_.p);
             } else {
                 double* zj = Z_.p + j * N;
                 precond_apply(M, vj, zj);

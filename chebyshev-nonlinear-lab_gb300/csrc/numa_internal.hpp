@@ -100,6 +100,13 @@ public:
         (void)v32;
         (void)out32;
     }
+    // The bound product from an FP32 v to FP64 accuracy (FP64 out), where has_jvp32x(): for linear
+    // tolerances below what FP32 arithmetic reaches.
+    virtual bool has_jvp32x() const { return false; }
+    virtual void jvp_bound32x(const float* v32, double* out) {
+        (void)v32;
+        (void)out;
+    }
 
     // Finite-difference forms of operators/operator.hpp:101-134 over eval.  f0 = F(x) must be
     // supplied (the same vector the reference recomputes inside the call); xnorm = ||x|| as a
@@ -150,6 +157,9 @@ public:
     void jvp_bound32(const float* v32, double* out) override;
     bool has_jvp32f() const override { return bound_precision_ == NUMA_GPU_FP32; }
     void jvp_bound32f(const float* v32, float* out32) override;
+    // h^-2 = (n + 1)^2 must be an FP32 integer (n < 4095) for the double-FP32 scaling
+    bool has_jvp32x() const override { return bound_precision_ == NUMA_GPU_FP32 && bound_c_ && n_ < 4095; }
+    void jvp_bound32x(const float* v32, double* out) override;
     void jvp_at(const double* x, const double* v, double* out) override { jvp_x(x, v, out); }
     void jvp_cached(const double*, const double* cache, const double* v, double* out) override {
         jvp_c(cache, v, out);
@@ -164,6 +174,8 @@ public:
     void jvp_c(const double* c, const double* v, double* out);
     // Mixed precision: the same with FP32 arithmetic (c32 = RN32(c)), FP64 in and out.
     void jvp_c32(const float* c32, const double* v, double* out);
+    // The product of an FP32 v to FP64 accuracy (double-FP32 stencil, FP64 c), FP64 out; n < 4095.
+    void jvp_c32x(const double* c, const float* v32, double* out);
     void coef32(const double* c, float* c32);
     // out = F'(x) v computing e^x in the kernel.
     void jvp_x(const double* x, const double* v, double* out);
@@ -488,6 +500,12 @@ struct LinearOp {
         (void)v32;
         (void)out32;
     }
+    // out = A v from an FP32 v to FP64 accuracy, where has_apply32x().
+    virtual bool has_apply32x() const { return false; }
+    virtual void apply32x(const float* v32, double* out) {
+        (void)v32;
+        (void)out;
+    }
 };
 struct Precond {
     virtual ~Precond() = default;
@@ -521,6 +539,9 @@ struct GmresOptions {
     bool flexible = false;
     double bnorm = -1.0;  // ||b|| when the caller knows it (>= 0), used by the flexible CGS1 solver
     const float* b32 = nullptr;  // RN32(b) when the caller has it (the FP32 Arnoldi basis starts from it)
+    // With FP32 preconditioned vectors and an FP64 basis (linear tolerance below 1e-5): compute
+    // A z_j to FP64 accuracy where the operator offers it (LinearOp::has_apply32x)
+    bool precise_tight = false;
     // When given (a Newton driver): the solution update also writes x_step = x_base - x, the full
     // Newton step, and reports it in GmresResult::stepped if that update was the solve's last
     const double* x_base = nullptr;
@@ -574,6 +595,7 @@ struct KrylovParams {
     bool recycle = false;
     int jvp_mode = 0, d2_mode = 0, orth = 0, jvp_precision = 0;
     bool flexible = false;
+    bool jvp_tight = false;  // GmresOptions::precise_tight for the Newton and Chebyshev solves
 };
 
 KrylovParams params_from_c(const numa_krylov_params* p);

@@ -26,7 +26,7 @@ LIB_PATH = Path(os.environ.get("NUMA_GPU_LIB", HERE / "libnuma_gpu.so"))
 # enums (include/numa_gpu.h)
 OK = 0
 FP64, FP32 = 0, 1
-ANALYTIC, FD, ANALYTIC_FP32 = 0, 1, 2
+ANALYTIC, FD, ANALYTIC_FP32, ANALYTIC_FP32X = 0, 1, 2, 3
 MGS, CGS2, CGS1 = 0, 1, 2
 METHODS = {"nk": 0, "cheb": 1, "rec": 2, "tf2018": 3}
 PRECONDS = {"none": 0, "mg": 1, "jacobi": 2, "burgers_mg": 3, "bruss_jacobi": 5, "bruss_mg": 6, "jacobian_mg": 7}
@@ -41,7 +41,7 @@ class KrylovParams(C.Structure):
         ("gmres_max_iters", C.c_uint64), ("armijo", C.c_double), ("min_lambda", C.c_double),
         ("recycle", C.c_int32), ("jvp_mode", C.c_int32), ("d2_mode", C.c_int32),
         ("orth", C.c_int32), ("flexible", C.c_int32), ("jvp_precision", C.c_int32),
-        ("reserved", C.c_int32 * 4),
+        ("jvp_tight", C.c_int32), ("reserved", C.c_int32 * 3),
     ]
 
 

@@ -54,8 +54,11 @@ typedef enum numa_gpu_precision {
 typedef enum numa_gpu_deriv_mode {
     NUMA_GPU_DERIV_ANALYTIC = 0,     /* Bratu3D::jvp / Bratu3D::d2 (problems/bratu3d.hpp:33-56) */
     NUMA_GPU_DERIV_FD = 1,           /* jvp_fd / d2_fd (operators/operator.hpp:100-134) */
-    NUMA_GPU_DERIV_ANALYTIC_FP32 = 2 /* extension, jvp only: the analytic product in FP32 arithmetic
+    NUMA_GPU_DERIV_ANALYTIC_FP32 = 2, /* extension, jvp only: the analytic product in FP32 arithmetic
                                         (Bratu3D, Brusselator2D; FP64 for operators without one) */
+    NUMA_GPU_DERIV_ANALYTIC_FP32X = 3 /* extension, Bratu3D jvp only: the analytic product of RN32(v) to
+                                        FP64 accuracy (double-FP32 stencil, FP64 lambda e^x), as the
+                                        mixed path's tight linear solves take it (jvp_tight) */
 } numa_gpu_deriv_mode;
 
 /* Arnoldi orthogonalisation. */
@@ -116,7 +119,11 @@ typedef struct numa_krylov_params {
     int32_t orth;              /* numa_gpu_orth */
     int32_t flexible;          /* 1 = FGMRES (stores Z_j = M^-1 v_j; no extra precond per cycle) */
     int32_t jvp_precision;     /* numa_gpu_precision of the Krylov matvec arithmetic */
-    int32_t reserved[4];
+    int32_t jvp_tight;         /* 1 = with jvp_precision FP32, linear solves whose tolerance is below 1e-5
+                                  (an FP64 Arnoldi basis) take the product of each FP32 preconditioned
+                                  vector to FP64 accuracy (double-FP32 stencil, FP64 coefficient) where
+                                  the operator offers it (Bratu3D); 0 = FP32 arithmetic throughout */
+    int32_t reserved[3];
 } numa_krylov_params;
 
 /* KrylovResult (krylov_newton.hpp:40-49) without x (the solution is written into the caller's
@@ -334,7 +341,9 @@ int numa_gpu_burgers2d_solve(numa_gpu_burgers2d* op, int method, numa_gpu_vec* x
                              numa_krylov_result* result);
 
 /* One call from host buffers to host buffers: Bratu3D(n, lambda), provider of precond_kind
- * (MG with pre = post = 2 and mg_precision), method of numa_gpu_method, x0[n^3] -> x_out[n^3].
+ * (NONE, POISSON_MG with pre = post = 2 and mg_precision, JACOBI, or JACOBIAN_MG: the FP32 V(2,2)
+ * with Jacobian-aware coarse levels, mg_precision ignored), method of numa_gpu_method,
+ * x0[n^3] -> x_out[n^3].
  * The shape of apps/smoke_bratu.cpp:125-148 and apps/run_campaign.cpp:344-390.  With
  * NUMA_GPU_METHOD_NK and page-locked buffers the transfers overlap the solve: a pinned x0 goes up
  * in plane pieces under the first residual evaluation, and the iterate predicted to be the last is

@@ -162,6 +162,50 @@ def test_fp32_jvp_bit_exact(gpu, n):
     assert same.all(), np.flatnonzero(~same)[:10]
 
 
+@pytest.mark.parametrize("n", [5, 31, 64])
+@pytest.mark.parametrize("smooth", [False, True])
+def test_fp32_input_product_to_fp64_accuracy(gpu, n, smooth):
+    """The product the mixed path's tight linear solves take (jvp_tight): F'(u) RN32(v) by a
+    double-FP32 stencil with the FP64 coefficient, against the FP64 product of the same FP32 values
+    in numpy (sums of FP32 values of these magnitudes are exact in FP64).  Bound: 2^-44 of the
+    stencil's largest partial sum plus a few FP64 roundings of c v and the result.  On a smooth v,
+    whose Laplacian cancels, FP32 arithmetic misses that accuracy by orders of magnitude."""
+    G = _G()
+    N = n ** 3
+    u = make_point(N, 0.3)
+    if smooth:
+        t = np.arange(1, n + 1) / (n + 1.0)
+        s1 = np.sin(np.pi * t)
+        v = (s1[:, None, None] * s1[None, :, None] * s1[None, None, :]).ravel()
+    else:
+        v = np.random.default_rng(n).uniform(-1, 1, N)
+    op = G.Bratu3D(gpu, n, 6.0)
+    out = gpu.vec(N)
+    op.jvp(gpu.from_numpy(u), gpu.from_numpy(v), out, G.ANALYTIC_FP32X)
+    vf = v.astype(F).astype(np.float64).reshape(n, n, n)
+    h2 = (n + 1.0) ** 2
+    s = 6.0 * vf
+    mag = 6.0 * np.abs(vf)
+    for axis in (0, 1, 2):
+        for d in (-1, 1):
+            nb = shifted(vf, axis, d)
+            s = s - nb
+            mag = mag + np.abs(nb)
+    c = 6.0 * np.exp(u.reshape(n, n, n))
+    want = h2 * s - c * vf
+    tol = (2.0 ** -44 * h2 * mag + 2.0 ** -50 * (np.abs(c * vf) + np.abs(want))).ravel()
+    want = want.ravel()
+    got = out.numpy()
+    bad = np.abs(got - want) > tol
+    assert not bad.any(), (np.flatnonzero(bad)[:10], np.abs(got - want)[bad][:5], tol[bad][:5])
+    if smooth and n >= 31:
+        out32 = gpu.vec(N)
+        op.jvp(gpu.from_numpy(u), gpu.from_numpy(vf.ravel()), out32, G.ANALYTIC_FP32)
+        ex = rel_err(got, want)
+        e32 = rel_err(out32.numpy(), want)
+        assert ex < 1e-13 and e32 > 1e3 * ex, (ex, e32)
+
+
 def test_mixed_solve_agrees_with_fp64(gpu):
     G = _G()
     n = 31
@@ -176,6 +220,36 @@ def test_mixed_solve_agrees_with_fp64(gpu):
     assert r32["res"] <= 1e-10 * r32["res0"]
     a, b = x32.numpy(), x64.numpy()
     assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-8
+
+
+@pytest.mark.parametrize("lam", [3.1, 6.0])
+def test_tight_products_save_a_newton_step(gpu, lam):
+    """With the Jacobian-aware coarse levels, FP32 products leave the last linear solves short of the
+    accuracy the quadratic Newton step needs (FP32 arithmetic on the Laplacian of a smooth vector
+    loses digits to cancellation); taking those products to FP64 accuracy (jvp_tight) converges
+    in fewer Newton steps and linear iterations, to the same solution (1e-8 of the FP64 drop-in's)."""
+    G = _G()
+    n = 127
+    op = G.Bratu3D(gpu, n, lam)
+    p = G.default_params(rtol_nl=1e-10, gmres_restart=30, flexible=1, jvp_precision=G.FP32, orth=G.CGS1)
+    pt = G.default_params(rtol_nl=1e-10, gmres_restart=30, flexible=1, jvp_precision=G.FP32, orth=G.CGS1,
+                          jvp_tight=1)
+    pcj = G.Provider.jacobian_mg(gpu, n)
+    x64, xf, xt = gpu.vec(n ** 3), gpu.vec(n ** 3), gpu.vec(n ** 3)
+    G.newton_krylov(op, x64, G.default_params(rtol_nl=1e-10, gmres_restart=30), G.Provider.poisson_mg(gpu, n))
+    rf = G.newton_krylov(op, xf, p, pcj)
+    rt = G.newton_krylov(op, xt, pt, pcj)
+    assert rf["converged"] and rt["converged"]
+    assert rt["res"] <= 1e-10 * rt["res0"]
+    assert rel_err(xt.numpy(), x64.numpy()) < 1e-8
+    assert rt["iters"] <= rf["iters"] and rt["n_lin_iters"] <= rf["n_lin_iters"], (rt, rf)
+    if lam == 6.0:  # the benchmark's lambda: 4 Newton steps and 9 linear iterations against 5 and 11
+        assert rt["iters"] < rf["iters"] and rt["n_lin_iters"] < rf["n_lin_iters"], (rt, rf)
+    # the host entry with the same preconditioner and parameters gives the same solve
+    xh, rh = G.solve_bratu3d_host(gpu, n, lam, np.zeros(n ** 3), method="nk", precond="jacobian_mg",
+                                  mg_precision=G.FP32, params=pt)
+    assert rh["iters"] == rt["iters"] and rh["n_lin_iters"] == rt["n_lin_iters"]
+    assert np.array_equal(xh, xt.numpy())
 
 
 @pytest.mark.parametrize("lam", [2.5, 4.7, 6.3])

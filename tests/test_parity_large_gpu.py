@@ -10,8 +10,9 @@ fixed strided indices.
 * The plain FP64 path (the drop-in) must give the reference's counts within +-1 and its solution
   within 1e-12 relative (reductions are not bit-exact, so not bit for bit).
 * The mixed path (FP32 V-cycle and FP32 Jacobian products inside FGMRES, FP64 residual, updates
-  and Arnoldi coefficients) and the learned preconditioner must reach the same tolerance with the
-  Newton count within +-1, and their solutions must lie within 1e-8 of the reference's.
+  and Arnoldi coefficients), its benchmark form (coarse levels with the Jacobian, products of FP64
+  accuracy in the tight linear solves) and the learned preconditioner must reach the same tolerance
+  with the Newton count within +-1, and their solutions must lie within 1e-8 of the reference's.
 """
 from __future__ import annotations
 
@@ -92,6 +93,27 @@ def test_mixed_path_within_1e8_of_reference(gpu, large, n, method, orth):
     r = G.solve(op, x, method, _params(G, c, True, getattr(G, orth)), pc)
     assert r["converged"] == 1 and r["res"] <= 1e-10 * r["res0"]
     assert abs(int(r["iters"]) - int(c["result"]["iters"])) <= 1
+    _check_solution(x.numpy(), c, vec, 1e-8)
+
+
+@pytest.mark.parametrize("n,method", [(255, "nk"), (255, "cheb"), (255, "rec"), (127, "nk"), (127, "cheb")])
+def test_benchmark_mixed_path_within_1e8_of_reference(gpu, large, n, method):
+    """The benchmark's mixed path: the FP32 V-cycle with Jacobian-aware coarse levels, FP32 products
+    while the forcing term is >= 1e-5 and products of FP64 accuracy below (jvp_tight).  It takes one
+    Newton step fewer than the reference (4 against 5): the count is within +-1."""
+    G = _G()
+    cases, vec = large
+    c = cases[(n, method)]
+    op = G.Bratu3D(gpu, n, c["lam"])
+    pc = G.Provider.jacobian_mg(gpu, n)
+    x = gpu.vec(n ** 3).fill(0.0)
+    p = _params(G, c, True)
+    p.jvp_tight = 1
+    r = G.solve(op, x, method, p, pc)
+    assert r["converged"] == 1 and r["res"] <= 1e-10 * r["res0"]
+    assert abs(int(r["iters"]) - int(c["result"]["iters"])) <= 1
+    if method != "rec":  # the recycled solves take the non-flexible GMRES path
+        assert r["n_lin_iters"] < c["result"]["n_lin_iters"], (r, c["result"])
     _check_solution(x.numpy(), c, vec, 1e-8)
 
 
