@@ -64,8 +64,9 @@ __device__ __forceinline__ double lap_sum(const double* __restrict__ v, size_t p
 // (F differs from the reference's two roundings by at most half an ulp, as e^u already may).
 // C32: also c32 = RN32(c) (the mixed path's FP32 Jacobian coefficient) and f32 = RN32(F) (the
 // first FP32 Krylov vector of the next linear solve), integer conversions; this is the mixed
-// path's evaluation, and it forms 6u - (i-1 neighbour) as one FMA (one rounding fewer than the
-// reference's two).  LT: lambda e^u from the operator's lambda-scaled exp table (lt2, ltf).
+// path's evaluation, and it forms 6u - (the six neighbours) in 64-bit fixed point on the integer pipe,
+// rounded once (lap7_fixed; the reference rounds six times).  LT: lambda e^u from the operator's
+// lambda-scaled exp table (lt2, ltf).
 template <bool WRITE_C, bool NORM, bool C32, bool LT>
 __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, double* __restrict__ F,
                                                  double* __restrict__ c_out, float* __restrict__ c32_out,
@@ -94,12 +95,7 @@ __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, d
                 const double jp = (j + 1 < n) ? u[p + n] : 0.0;
                 const double km = (k > 0) ? u[p - 1] : 0.0;
                 const double kp = (k + 1 < n) ? u[p + 1] : 0.0;
-                s = __fma_rn(6.0, cur, -below);
-                s = s - above;
-                s = s - jm;
-                s = s - jp;
-                s = s - km;
-                s = s - kp;
+                s = lap7_fixed(cur, below, above, jm, jp, km, kp);
             } else {
                 s = lap_sum(u, p, plane, n, i, j, k, below, cur, above);
             }
@@ -345,8 +341,15 @@ __device__ __forceinline__ double jvp32x_point(float below, float cur, float abo
 // The bound product from an FP32 v (the V-cycle's output) to FP64 accuracy, FP64 coefficient c and
 // FP64 out, for Krylov solves whose tolerance is below what FP32 arithmetic reaches.  Same march as
 // k_jvp32f: a (k, j) column walks i two planes a step with planes i-1, i, i+1 in registers.
+template <class OT>
+__device__ __forceinline__ void jvp32x_store(OT* __restrict__ out, size_t p, double r) {
+    if constexpr (sizeof(OT) == 4) out[p] = f64_to_f32(r);  // rounded once: within half an FP32 ulp
+    else out[p] = r;
+}
+
+template <class OT>
 __global__ void __launch_bounds__(BX* BY) k_jvp32x(const double* __restrict__ c, const float* __restrict__ v,
-                                                   double* __restrict__ out, int n, int ichunk, float h2inv) {
+                                                   OT* __restrict__ out, int n, int ichunk, float h2inv) {
     pdl_wait();
     pdl_trigger();
     const int k = blockIdx.x * BX + threadIdx.x;
@@ -369,8 +372,8 @@ __global__ void __launch_bounds__(BX* BY) k_jvp32x(const double* __restrict__ c,
         const float jm1 = jlo ? v[q - n] : 0.0f, jp1 = jhi ? v[q + n] : 0.0f;
         const float km1 = klo ? v[q - 1] : 0.0f, kp1 = khi ? v[q + 1] : 0.0f;
         const double c0 = c[p], c1 = c[q];
-        out[p] = jvp32x_point(below, cur, a1, jm0, jp0, km0, kp0, c0, h2inv);
-        out[q] = jvp32x_point(cur, a1, a2, jm1, jp1, km1, kp1, c1, h2inv);
+        jvp32x_store(out, p, jvp32x_point(below, cur, a1, jm0, jp0, km0, kp0, c0, h2inv));
+        jvp32x_store(out, q, jvp32x_point(cur, a1, a2, jm1, jp1, km1, kp1, c1, h2inv));
         below = a1;
         cur = a2;
     }
@@ -379,7 +382,7 @@ __global__ void __launch_bounds__(BX* BY) k_jvp32x(const double* __restrict__ c,
         const float above = (i + 1 < n) ? v[p + plane] : 0.0f;
         const float jm = jlo ? v[p - n] : 0.0f, jp = jhi ? v[p + n] : 0.0f;
         const float km = klo ? v[p - 1] : 0.0f, kp = khi ? v[p + 1] : 0.0f;
-        out[p] = jvp32x_point(below, cur, above, jm, jp, km, kp, c[p], h2inv);
+        jvp32x_store(out, p, jvp32x_point(below, cur, above, jm, jp, km, kp, c[p], h2inv));
     }
 }
 
@@ -481,9 +484,19 @@ void Bratu3D::jvp_bound32x(const float* v32, double* out) {
 void Bratu3D::jvp_c32x(const double* c, const float* v32, double* out) {
     if (n_ >= 4095) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "Bratu3D: the double-FP32 product needs n < 4095");
     March m = march_shape((int)n_, false);
-    launch_pdl(k_jvp32x, m.grid, dim3(BX, BY), 0, ctx_.stream, c, v32, out, (int)n_, m.ichunk, (float)h2inv_);
+    launch_pdl(k_jvp32x<double>, m.grid, dim3(BX, BY), 0, ctx_.stream, c, v32, out, (int)n_, m.ichunk,
+               (float)h2inv_);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d jvp32x (fp32 input, fp64 accuracy)");
+}
+
+void Bratu3D::jvp_bound32xf(const float* v32, float* out32) {
+    if (!has_jvp32x()) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Bratu3D: no FP32-input FP64-accuracy product bound");
+    March m = march_shape((int)n_, false);
+    launch_pdl(k_jvp32x<float>, m.grid, dim3(BX, BY), 0, ctx_.stream, bound_c_, v32, out32, (int)n_, m.ichunk,
+               (float)h2inv_);
+    ctx_.count_launch();
+    ctx_.check_launch("bratu3d jvp32x (fp32 input, fp64 accuracy, rounded to fp32)");
 }
 
 void Bratu3D::jvp_bound(const double* v, double* out) {
@@ -494,6 +507,17 @@ void Bratu3D::jvp_bound(const double* v, double* out) {
 void Bratu3D::eval(const double* x, double* out, double* c_out, double* norm_out) {
     const March m = march_shape((int)n_, norm_out != nullptr);
     eval_launch(x, out, c_out, norm_out, m.grid, m.ichunk, 0, 0);
+}
+
+void Bratu3D::eval_as(const double* x, int precision, double* out, double* norm_host) {
+    const bool keep = mixed_cache_;
+    prepare_cache(precision);
+    DeviceArray<double> cache(cache_size());
+    double* nrm = ctx_.scalar(kSlotTmp0);
+    eval(x, out, cache.p, nrm);
+    const double v = ctx_.fetch1(nrm);
+    if (norm_host) *norm_host = v;
+    mixed_cache_ = keep;
 }
 
 double Bratu3D::time_eval(const double* x, int precision, int reps) {

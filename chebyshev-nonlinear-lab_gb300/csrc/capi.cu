@@ -1813,6 +1813,19 @@ int numa_gpu_diag_time_smoother(numa_gpu_mg* mg, int reps, double* ms_per_pass) 
     return guard(mg->ctx, [&] { *ms_per_pass = mg->impl->time_finest_pass(reps); });
 }
 
+int numa_gpu_diag_eval(numa_gpu_bratu3d* op, const numa_gpu_vec* x, int precision, numa_gpu_vec* out, double* norm) {
+    if (!op) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    if (precision != NUMA_GPU_FP64 && precision != NUMA_GPU_FP32) return NUMA_GPU_ERR_INVALID_ARGUMENT;
+    return guard(op->ctx, [&] {
+        same_ctx(op->ctx, x);
+        same_ctx(op->ctx, out);
+        sized(x, op->impl->size());
+        sized(out, op->impl->size());
+        need(out->d != x->d, NUMA_GPU_ERR_INVALID_ARGUMENT, "eval output must not alias its input");
+        op->impl->eval_as(x->d, precision, out->d, norm);
+    });
+}
+
 int numa_gpu_diag_time_eval(numa_gpu_bratu3d* op, const numa_gpu_vec* x, int precision, int reps, double* ms_per_eval) {
     if (!op || !ms_per_eval || reps < 1) return NUMA_GPU_ERR_INVALID_ARGUMENT;
     if (precision != NUMA_GPU_FP64 && precision != NUMA_GPU_FP32) return NUMA_GPU_ERR_INVALID_ARGUMENT;

@@ -330,6 +330,69 @@ __device__ __forceinline__ double lam_exp_tang(double x, double lam, const doubl
 }
 
 // ------------------------------------------------------------------------------------------
+// 6c - (a1 + ... + a6) of seven FP64 values in 64-bit fixed point on the integer pipe, rounded once to
+// FP64: GB300's FP64 pipe issues about two instructions a clock per SM, its integer pipe thirty-two
+// times that, and the six FP64 operations of the sum were half of a residual evaluation's FP64 work.
+// Each value's 53-bit significand is placed 4 bits up in a signed 64-bit integer, aligned to the
+// largest exponent E of the seven (bits below 2^(E-1079) truncated: an error of at most 7 such
+// units, 2^-56 of the largest value); 6c and the sum stay below 2^61; the total is normalised and
+// rounded to nearest-even.  So the result is within 2^-56 |largest value| + half an ulp of the exact
+// sum (the FP64 chain of six roundings: up to ~3 2^-53 of the largest partial sum).  Infinities,
+// NaN and results outside the normal range go to the FP64 chain (a call that is not inlined).
+static __device__ __noinline__ double lap7_fp64_rare(double c, double a1, double a2, double a3, double a4, double a5,
+                                                      double a6) {
+    double s = __fma_rn(6.0, c, -a1);
+    s = s - a2;
+    s = s - a3;
+    s = s - a4;
+    s = s - a5;
+    return s - a6;
+}
+__device__ __forceinline__ void fx_split(double x, unsigned long long& mag, int& e, bool& neg) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int eb = (int)((b >> 52) & 0x7FFu);
+    mag = (b & 0xFFFFFFFFFFFFFull) | (eb ? (1ull << 52) : 0ull);
+    e = eb ? eb : 1;  // a subnormal: exponent 1 without the hidden bit
+    neg = (long long)b < 0;
+}
+__device__ __forceinline__ long long fx_term(unsigned long long mag, int e, bool neg, int E) {
+    const int d = E - e;
+    const unsigned long long t = d < 60 ? (mag << 4) >> d : 0ull;
+    return neg ? -(long long)t : (long long)t;
+}
+__device__ __forceinline__ double lap7_fixed(double c, double a1, double a2, double a3, double a4, double a5,
+                                             double a6) {
+    unsigned long long m0, m1, m2, m3, m4, m5, m6;
+    int e0, e1, e2, e3, e4, e5, e6;
+    bool n0, n1, n2, n3, n4, n5, n6;
+    fx_split(c, m0, e0, n0);
+    fx_split(a1, m1, e1, n1);
+    fx_split(a2, m2, e2, n2);
+    fx_split(a3, m3, e3, n3);
+    fx_split(a4, m4, e4, n4);
+    fx_split(a5, m5, e5, n5);
+    fx_split(a6, m6, e6, n6);
+    const int E = max(max(max(e0, e1), max(e2, e3)), max(max(e4, e5), e6));
+    if (E >= 2040) return lap7_fp64_rare(c, a1, a2, a3, a4, a5, a6);  // infinities, NaN, near overflow
+    const long long t0 = fx_term(m0, e0, n0, E);
+    const long long S = ((t0 << 2) + (t0 << 1)) - fx_term(m1, e1, n1, E) - fx_term(m2, e2, n2, E) -
+                        fx_term(m3, e3, n3, E) - fx_term(m4, e4, n4, E) - fx_term(m5, e5, n5, E) -
+                        fx_term(m6, e6, n6, E);
+    if (S == 0) return 0.0;
+    const unsigned long long sign = S < 0 ? (1ull << 63) : 0ull;
+    unsigned long long A = S < 0 ? (unsigned long long)(-S) : (unsigned long long)S;
+    const int lz = __clzll((long long)A);  // >= 3
+    const int eb = E + 7 - lz;             // the biased exponent of A 2^(E - 1079)
+    if (eb <= 0) return lap7_fp64_rare(c, a1, a2, a3, a4, a5, a6);  // a subnormal result
+    A <<= lz;                                   // leading one at bit 63
+    unsigned long long mant = A >> 11;          // 53 bits
+    const unsigned rem = (unsigned)(A & 0x7FFu);
+    mant += (rem > 0x400u || (rem == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
+    // the hidden bit adds one to the exponent field; a carry out of the significand adds one more
+    return __longlong_as_double((long long)(sign | ((((unsigned long long)(eb - 1)) << 52) + mant)));
+}
+
+// ------------------------------------------------------------------------------------------
 // One process-wide lock held across every CUDA-graph capture and around every device or pinned
 // allocation and free: cudaFree / cudaMallocHost may synchronise the whole device, which would
 // break a capture another thread (another context) has in progress.  Recursive, so a capture

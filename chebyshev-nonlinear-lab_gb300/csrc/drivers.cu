@@ -205,6 +205,10 @@ public:
         Timers::Scope s(&t_, kT_JVP);
         f_.jvp_bound32x(v32, out);
     }
+    void apply32xf(const float* v32, float* out32) override {
+        Timers::Scope s(&t_, kT_JVP);
+        f_.jvp_bound32xf(v32, out32);
+    }
 
 private:
     NonlinearOp& f_;

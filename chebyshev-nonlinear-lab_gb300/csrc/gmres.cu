@@ -473,8 +473,10 @@ __global__ void k_set_scalar(double* __restrict__ out, double v) {
     *out = v;
 }
 
-// Smallest linear tolerance for which FGMRES keeps its basis in FP32 (the FP32 hand-off only).
+// Smallest linear tolerance for which FGMRES keeps its basis in FP32 (the FP32 hand-off only), with
+// FP32-arithmetic products and with products of FP64 accuracy rounded to FP32 (GmresOptions::precise_tight).
 constexpr double kV32MinRtol = 1e-5;
+constexpr double kV32MinRtolPrecise = 1e-6;
 
 unsigned ew_grid(const Context& ctx, size_t N) {
     size_t want = (N + 255) / 256;
@@ -588,11 +590,16 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
     // perturbs the Arnoldi relation A Z = V H by 6e-8 relative, which bounds the attainable linear
     // residual near that; inner products, updates and the solution update are computed in
     // double-FP32 and reduced in FP64, and the Hessenberg matrix and least squares stay FP64.
-    const bool v32 = z32 && M->has_apply32f() && A.has_apply32f() && o.rtol >= kV32MinRtol;
-    // ... below that tolerance the basis is FP64, and the products of the FP32 vectors can be taken to
-    // FP64 accuracy (FP32 arithmetic in the Laplacian of a smooth vector loses digits to cancellation
-    // and bounds the attainable true residual well above the tolerance)
-    const bool precise = z32 && !v32 && o.precise_tight && A.has_apply32x();
+    // With products of FP64 accuracy (precise_tight): FP32 arithmetic in the Laplacian of a smooth vector loses
+    // digits to cancellation and bounds the attainable true residual well above a tight tolerance, while a
+    // product computed accurately and rounded once to FP32 perturbs it by 6e-8 relative, like the stored basis.
+    // So between 1e-6 and 1e-5 the basis stays FP32 with those products; below 1e-6 it is FP64 and the products
+    // are kept in FP64.
+    const bool can_precise = z32 && o.precise_tight && A.has_apply32x();
+    const bool v32 = z32 && M->has_apply32f() && A.has_apply32f() &&
+                     o.rtol >= (can_precise ? kV32MinRtolPrecise : kV32MinRtol);
+    const bool precise = can_precise && !v32;
+    const bool precise_v32 = can_precise && v32 && o.rtol < kV32MinRtol;
     double* sigd = ctx_.scalar(kSlotGmresSig);
     if (v32) {
         V32_.resize((m + 1) * N);
@@ -674,7 +681,8 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
                 float* zj = Z32_.p + j * N;
                 M->apply32f(j == 0 ? u0 : V32_.p + j * N, zj);
                 ++res.precs;
-                A.apply32f(zj, W32_.p);
+                if (precise_v32) A.apply32xf(zj, W32_.p);
+                else A.apply32f(zj, W32_.p);
             } else if (z32) {
                 float* zj = Z32_.p + j * N;
                 M->apply32(vj, zj);

@@ -107,6 +107,11 @@ public:
         (void)v32;
         (void)out;
     }
+    // The same product rounded once to FP32 (for an FP32 Krylov basis), where has_jvp32x().
+    virtual void jvp_bound32xf(const float* v32, float* out32) {
+        (void)v32;
+        (void)out32;
+    }
 
     // Finite-difference forms of operators/operator.hpp:101-134 over eval.  f0 = F(x) must be
     // supplied (the same vector the reference recomputes inside the call); xnorm = ||x|| as a
@@ -160,6 +165,7 @@ public:
     // h^-2 = (n + 1)^2 must be an FP32 integer (n < 4095) for the double-FP32 scaling
     bool has_jvp32x() const override { return bound_precision_ == NUMA_GPU_FP32 && bound_c_ && n_ < 4095; }
     void jvp_bound32x(const float* v32, double* out) override;
+    void jvp_bound32xf(const float* v32, float* out32) override;
     void jvp_at(const double* x, const double* v, double* out) override { jvp_x(x, v, out); }
     void jvp_cached(const double*, const double* cache, const double* v, double* out) override {
         jvp_c(cache, v, out);
@@ -186,6 +192,9 @@ public:
     // Average ms of one residual evaluation with its fused norm and the cache the drivers keep
     // (c = lambda e^x; with precision FP32 also RN32(c) and RN32(F)), reps launches back to back.
     double time_eval(const double* x, int precision, int reps);
+    // out = F(x) and *norm_host = ||F(x)|| as the drivers' evaluation at that precision forms them
+    // (FP32: the mixed path's evaluation, with its fixed-point 7-point sum).
+    void eval_as(const double* x, int precision, double* out, double* norm_host);
 
 private:
     size_t n_, N_;
@@ -506,6 +515,11 @@ struct LinearOp {
         (void)v32;
         (void)out;
     }
+    // ... rounded once to FP32, where has_apply32x().
+    virtual void apply32xf(const float* v32, float* out32) {
+        (void)v32;
+        (void)out32;
+    }
 };
 struct Precond {
     virtual ~Precond() = default;
@@ -539,8 +553,9 @@ struct GmresOptions {
     bool flexible = false;
     double bnorm = -1.0;  // ||b|| when the caller knows it (>= 0), used by the flexible CGS1 solver
     const float* b32 = nullptr;  // RN32(b) when the caller has it (the FP32 Arnoldi basis starts from it)
-    // With FP32 preconditioned vectors and an FP64 basis (linear tolerance below 1e-5): compute
-    // A z_j to FP64 accuracy where the operator offers it (LinearOp::has_apply32x)
+    // With FP32 preconditioned vectors and a linear tolerance below 1e-5: compute A z_j to FP64 accuracy
+    // where the operator offers it (LinearOp::has_apply32x), rounded once to FP32 into an FP32 basis down
+    // to a tolerance of 1e-6, kept in FP64 with an FP64 basis below
     bool precise_tight = false;
     // When given (a Newton driver): the solution update also writes x_step = x_base - x, the full
     // Newton step, and reports it in GmresResult::stepped if that update was the solve's last

@@ -454,7 +454,9 @@ const float* PoissonMG::fine_b32() const { return levels_[0]->b32.p; }
 namespace {
 
 // cc = the full-weighting restriction of a natural-layout coefficient (weights (1/4, 1/2, 1/4) per
-// dimension, summed z outer, y, x inner), FP32 out.
+// dimension, summed z outer, y, x inner), FP32 out.  An FP64 input is rounded to FP32 by the integer
+// conversion (the hardware one issues on the FP64 pipe: 27 of them per coarse point made the 255^3
+// restriction FP64-bound at ~95 us).
 template <class TI>
 __global__ void k_restrict_coef(const TI* __restrict__ cf, float* __restrict__ cc, int nf, int nc) {
     pdl_wait();
@@ -469,7 +471,7 @@ __global__ void k_restrict_coef(const TI* __restrict__ cf, float* __restrict__ c
             for (int b = 0; b < 3; ++b)
                 for (int c = 0; c < 3; ++c) {
                     const size_t f = ((size_t)(2 * I + a) * nf + 2 * J + b) * nf + 2 * K + c;
-                    acc = __fmaf_rn(w[a] * w[b] * w[c], (float)cf[f], acc);
+                    acc = __fmaf_rn(w[a] * w[b] * w[c], f64_to_f32(cf[f]), acc);
                 }
         cc[q] = acc;
     }

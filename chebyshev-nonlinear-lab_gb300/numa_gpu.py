@@ -227,6 +227,7 @@ SIGNATURES = {
     "numa_gpu_diag_fp64_peak": ([_P, _F64P], _I),
     "numa_gpu_diag_time_smoother": ([_P, _I, _F64P], _I),
     "numa_gpu_diag_time_eval": ([_P, _P, _I, _I, _F64P], _I),
+    "numa_gpu_diag_eval": ([_P, _P, _I, _P, _F64P], _I),
     "numa_gpu_diag_time_bmg2d_pass": ([_P, _I, _F64P], _I),
     "numa_gpu_diag_exp": ([_P, _P, _P], _I),
     "numa_gpu_diag_div": ([_P, C.c_double, _P], _I),
@@ -495,6 +496,13 @@ class Bratu3D:
 
     def jacobi_diag(self, x: Vec, d: Vec):
         self.ctx.check(self.lib.numa_gpu_bratu3d_jacobi_diag(self.h, x.h, d.h), "bratu3d_jacobi_diag")
+
+    def eval_as(self, x: Vec, out: Vec, precision: int = FP64) -> float:
+        """out = F(x) as the drivers' evaluation at that precision forms it (FP32: the mixed path's);
+        returns ||F(x)|| (diagnostic)."""
+        v = C.c_double()
+        self.ctx.check(self.lib.numa_gpu_diag_eval(self.h, x.h, precision, out.h, C.byref(v)), "diag_eval")
+        return v.value
 
     def time_eval(self, x: Vec, precision: int = FP64, reps: int = 20) -> float:
         """Average ms of one residual evaluation with its fused norm and cache (diagnostic)."""

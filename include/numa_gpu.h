@@ -120,9 +120,10 @@ typedef struct numa_krylov_params {
     int32_t flexible;          /* 1 = FGMRES (stores Z_j = M^-1 v_j; no extra precond per cycle) */
     int32_t jvp_precision;     /* numa_gpu_precision of the Krylov matvec arithmetic */
     int32_t jvp_tight;         /* 1 = with jvp_precision FP32, linear solves whose tolerance is below 1e-5
-                                  (an FP64 Arnoldi basis) take the product of each FP32 preconditioned
-                                  vector to FP64 accuracy (double-FP32 stencil, FP64 coefficient) where
-                                  the operator offers it (Bratu3D); 0 = FP32 arithmetic throughout */
+                                  take the product of each FP32 preconditioned vector to FP64 accuracy
+                                  (double-FP32 stencil, FP64 coefficient) where the operator offers it
+                                  (Bratu3D): rounded once to FP32 into the FP32 Arnoldi basis down to a
+                                  tolerance of 1e-6, with an FP64 basis below; 0 = FP32 arithmetic */
     int32_t reserved[3];
 } numa_krylov_params;
 
@@ -582,6 +583,11 @@ int numa_gpu_diag_time_smoother(numa_gpu_mg* mg, int reps, double* ms_per_pass);
  * on the mixed path), over reps back-to-back launches timed with CUDA events. */
 int numa_gpu_diag_time_eval(numa_gpu_bratu3d* op, const numa_gpu_vec* x, int precision, int reps,
                             double* ms_per_eval);
+/* out = F(x) and *norm (may be NULL) = ||F(x)|| as the drivers' residual evaluation at that precision
+ * forms them: FP64 as numa_gpu_bratu3d_eval; FP32 the mixed path's evaluation (FP64 result, its
+ * 7-point sum in 64-bit fixed point rounded once, 6u - sum - lambda e^u with one rounding). */
+int numa_gpu_diag_eval(numa_gpu_bratu3d* op, const numa_gpu_vec* x, int precision, numa_gpu_vec* out,
+                       double* norm);
 /* The same for the finest level of a Brusselator2D multigrid (its blocks must have been set). */
 int numa_gpu_diag_time_bmg2d_pass(numa_gpu_bmg2d* mg, int reps, double* ms_per_pass);
 /* out = e^x as the residual kernels compute it (Tang's table-driven method, FP64); cuda_ref

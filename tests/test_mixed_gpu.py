@@ -206,6 +206,55 @@ def test_fp32_input_product_to_fp64_accuracy(gpu, n, smooth):
         assert ex < 1e-13 and e32 > 1e3 * ex, (ex, e32)
 
 
+def _exact_lap_sum(u):
+    """6u - (the six neighbours) of every point, the exact sum rounded once (math.fsum)."""
+    import math
+    n = u.shape[0]
+    nb = [shifted(u, axis, d).ravel() for axis in (0, 1, 2) for d in (-1, 1)]
+    c = u.ravel()
+    return np.array([math.fsum((c[p],) * 6 + tuple(-a[p] for a in nb)) for p in range(n ** 3)]), nb
+
+
+@pytest.mark.parametrize("n,case", [(7, "point"), (31, "point"), (31, "wide"), (20, "special"), (64, "point")])
+def test_mixed_evaluation_fixed_point_sum(gpu, n, case):
+    """The mixed path's residual evaluation forms 6u - (six neighbours) in 64-bit fixed point and
+    rounds it once, then F = h^-2 s - lambda e^u with one rounding.  Bound against the exactly
+    rounded sum (fsum): h^-2 (7 2^-56 max|values| + 2^-52 |S|) for the sum, an ulp of lambda e^u
+    (the table-driven exponential against numpy's), half an ulp of F.  Cases: the reference's test
+    point, magnitudes spread over 25 decades (deep truncation of the aligned values), and zeros,
+    signed zeros and subnormals (a subnormal result takes the FP64 chain)."""
+    G = _G()
+    N = n ** 3
+    rng = np.random.default_rng(n)
+    if case == "point":
+        u = make_point(N, 0.3)
+    elif case == "wide":
+        u = rng.uniform(-1, 1, N) * 10.0 ** rng.integers(-20, 2, N)
+    else:
+        u = rng.uniform(-1, 1, N) * 1e-3
+        u[: N // 4] = 0.0
+        u[N // 4: N // 3] = -0.0
+        u[N // 3: N // 2] = rng.uniform(-1, 1, N // 2 - N // 3) * 1e-310  # subnormals
+    lam = 2.0 ** -10  # the smallest lambda of the scaled exp table: lambda e^u small beside the stencil
+    op = G.Bratu3D(gpu, n, lam)
+    out, out64 = gpu.vec(N), gpu.vec(N)
+    nrm = op.eval_as(gpu.from_numpy(u), out, G.FP32)
+    u3 = u.reshape(n, n, n)
+    S, nb = _exact_lap_sum(u3)
+    h2 = (n + 1.0) ** 2
+    e = lam * np.exp(u)
+    want = h2 * S - e
+    vmax = np.maximum.reduce([np.abs(u)] + [np.abs(a) for a in nb])
+    tol = h2 * (7 * 2.0 ** -56 * vmax + 2.0 ** -52 * np.abs(S)) + 2.0 ** -51 * np.abs(e) + 2.0 ** -52 * np.abs(want)
+    got = out.numpy()
+    bad = ~(np.abs(got - want) <= tol)
+    assert not bad.any(), (np.flatnonzero(bad)[:5], got[bad][:5], want[bad][:5])
+    assert nrm == pytest.approx(np.linalg.norm(want), rel=1e-13)
+    # no less accurate than the FP64 chain of the drop-in evaluation
+    op.eval(gpu.from_numpy(u), out64)
+    assert np.abs(got - want).max() <= np.abs(out64.numpy() - want).max() + tol.max()
+
+
 def test_mixed_solve_agrees_with_fp64(gpu):
     G = _G()
     n = 31
