@@ -10,6 +10,7 @@
 // an ulp between the table-driven exp_tang (common.cuh) and the host C library.
 #include <cmath>
 #include <limits>
+#include <type_traits>
 
 #include "numa_internal.hpp"
 
@@ -338,18 +339,45 @@ __device__ __forceinline__ double jvp32x_point(float below, float cur, float abo
     return __fma_rn(-c, f32_to_f64(cur), t);
 }
 
-// The bound product from an FP32 v (the V-cycle's output) to FP64 accuracy, FP64 coefficient c and
-// FP64 out, for Krylov solves whose tolerance is below what FP32 arithmetic reaches.  Same march as
-// k_jvp32f: a (k, j) column walks i two planes a step with planes i-1, i, i+1 in registers.
-template <class OT>
-__device__ __forceinline__ void jvp32x_store(OT* __restrict__ out, size_t p, double r) {
-    if constexpr (sizeof(OT) == 4) out[p] = f64_to_f32(r);  // rounded once: within half an FP32 ulp
-    else out[p] = r;
+// The same product rounded to FP32 (the FP32 Krylov basis' vector), on the FP32 pipe alone: the stencil
+// sum in double-FP32 as above, h^-2 s exactly as ph + pl, c v with the FP32 coefficient RN32(c) as an exact
+// product (two-product), the difference in double-FP32, rounded once.  Against the product with the FP64
+// coefficient this adds |c - RN32(c)| |v| <= 2^-24 |c v|, the size of the final rounding itself.
+__device__ __forceinline__ float jvp32xf_point(float below, float cur, float above, float jm, float jp, float km,
+                                               float kp, float c32, float h2inv) {
+    float hi = __fmul_rn(6.0f, cur);
+    float lo = __fmaf_rn(6.0f, cur, -hi);
+    df_sub(hi, lo, below);
+    df_sub(hi, lo, above);
+    df_sub(hi, lo, jm);
+    df_sub(hi, lo, jp);
+    df_sub(hi, lo, km);
+    df_sub(hi, lo, kp);
+    const float ph = __fmul_rn(h2inv, hi);
+    const float pl = __fmaf_rn(h2inv, lo, __fmaf_rn(h2inv, hi, -ph));
+    const float q = __fmul_rn(c32, cur);
+    const float qe = __fmaf_rn(c32, cur, -q);
+    float s, e;
+    two_sum(ph, -q, s, e);
+    return __fadd_rn(s, __fadd_rn(e, __fsub_rn(pl, qe)));
 }
 
+// FP32 out: the coefficient array is RN32(c) and jvp32xf_point forms the result (no FP64 instruction).
+// FP64 out: the FP64 coefficient and jvp32x_point.
+template <class OT, class CT>
+__device__ __forceinline__ OT jvp32x_any(float below, float cur, float above, float jm, float jp, float km, float kp,
+                                         CT c, float h2inv) {
+    if constexpr (sizeof(OT) == 4) return jvp32xf_point(below, cur, above, jm, jp, km, kp, c, h2inv);
+    else return jvp32x_point(below, cur, above, jm, jp, km, kp, c, h2inv);
+}
+
+// The bound product from an FP32 v (the V-cycle's output) for Krylov solves whose tolerance is below
+// what FP32 arithmetic reaches: FP64 out with the FP64 coefficient, or FP32 out with RN32(c).  Same
+// march as k_jvp32f: a (k, j) column walks i two planes a step with planes i-1, i, i+1 in registers.
 template <class OT>
-__global__ void __launch_bounds__(BX* BY) k_jvp32x(const double* __restrict__ c, const float* __restrict__ v,
-                                                   OT* __restrict__ out, int n, int ichunk, float h2inv) {
+__global__ void __launch_bounds__(BX* BY) k_jvp32x(const std::conditional_t<sizeof(OT) == 4, float, double>* __restrict__ c,
+                                                   const float* __restrict__ v, OT* __restrict__ out, int n, int ichunk,
+                                                   float h2inv) {
     pdl_wait();
     pdl_trigger();
     const int k = blockIdx.x * BX + threadIdx.x;
@@ -371,9 +399,9 @@ __global__ void __launch_bounds__(BX* BY) k_jvp32x(const double* __restrict__ c,
         const float km0 = klo ? v[p - 1] : 0.0f, kp0 = khi ? v[p + 1] : 0.0f;
         const float jm1 = jlo ? v[q - n] : 0.0f, jp1 = jhi ? v[q + n] : 0.0f;
         const float km1 = klo ? v[q - 1] : 0.0f, kp1 = khi ? v[q + 1] : 0.0f;
-        const double c0 = c[p], c1 = c[q];
-        jvp32x_store(out, p, jvp32x_point(below, cur, a1, jm0, jp0, km0, kp0, c0, h2inv));
-        jvp32x_store(out, q, jvp32x_point(cur, a1, a2, jm1, jp1, km1, kp1, c1, h2inv));
+        const auto c0 = c[p], c1 = c[q];
+        out[p] = jvp32x_any<OT>(below, cur, a1, jm0, jp0, km0, kp0, c0, h2inv);
+        out[q] = jvp32x_any<OT>(cur, a1, a2, jm1, jp1, km1, kp1, c1, h2inv);
         below = a1;
         cur = a2;
     }
@@ -382,7 +410,7 @@ __global__ void __launch_bounds__(BX* BY) k_jvp32x(const double* __restrict__ c,
         const float above = (i + 1 < n) ? v[p + plane] : 0.0f;
         const float jm = jlo ? v[p - n] : 0.0f, jp = jhi ? v[p + n] : 0.0f;
         const float km = klo ? v[p - 1] : 0.0f, kp = khi ? v[p + 1] : 0.0f;
-        jvp32x_store(out, p, jvp32x_point(below, cur, above, jm, jp, km, kp, c[p], h2inv));
+        out[p] = jvp32x_any<OT>(below, cur, above, jm, jp, km, kp, c[p], h2inv);
     }
 }
 
@@ -493,7 +521,7 @@ void Bratu3D::jvp_c32x(const double* c, const float* v32, double* out) {
 void Bratu3D::jvp_bound32xf(const float* v32, float* out32) {
     if (!has_jvp32x()) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "Bratu3D: no FP32-input FP64-accuracy product bound");
     March m = march_shape((int)n_, false);
-    launch_pdl(k_jvp32x<float>, m.grid, dim3(BX, BY), 0, ctx_.stream, bound_c_, v32, out32, (int)n_, m.ichunk,
+    launch_pdl(k_jvp32x<float>, m.grid, dim3(BX, BY), 0, ctx_.stream, bound_c32_, v32, out32, (int)n_, m.ichunk,
                (float)h2inv_);
     ctx_.count_launch();
     ctx_.check_launch("bratu3d jvp32x (fp32 input, fp64 accuracy, rounded to fp32)");

@@ -64,6 +64,7 @@ public:
         if (!c) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "Jacobian-aware multigrid: the operator keeps no coefficient");
         mg_.set_coarse_coefficient(c);
     }
+    void make_c32(const double*, const double* c, const float* c32) override { mg_.set_coarse_coefficient(c, c32); }
     void apply(const double* r, double* z) override { mg_.apply(r, z); }
     bool has_apply32() const override { return true; }
     void apply32(const double* r, float* z32) override { mg_.apply32(r, z32); }
@@ -318,7 +319,9 @@ struct SolveState {
         J.bind(x, Fx, xnorm.p);
         if (pc) {
             Timers::Scope s(&timers, kT_SETUP);
-            pc->make(x, cx);
+            const float* c32 = f.coef32_of_cache(cx);
+            if (c32) pc->make_c32(x, cx, c32);
+            else pc->make(x, cx);
         }
     }
     // Copies the final iterate into the caller's vector if the swaps left it elsewhere.

@@ -338,13 +338,23 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs_df(const float* w, const fl
     }
 }
 
-// x += scale * sum_r coef[r] Z_r (ASSIGN: x = scale * sum_r coef[r] Z_r, x not read) with FP32 Z and
-// |coef| <= 1 (the host normalises them by scale): the sum in double-FP32, then one FMA (or multiply)
-// into x — two FP64 instructions a point
+// v 2^k for a power-of-two scale: the exponent field moved by integer addition where v and the result are
+// normal numbers (exact either way), else the FP64 multiply (a call that is not inlined).
+static __device__ __noinline__ double scale_pow2_rare(double v, double scale) { return __dmul_rn(v, scale); }
+__device__ __forceinline__ double scale_pow2(double v, int k, double scale) {
+    const int hi = __double2hiint(v);
+    const int e = (hi >> 20) & 0x7FF;
+    if (e == 0 || e + k < 1 || e + k > 2046) return scale_pow2_rare(v, scale);
+    return __hiloint2double(hi + (k << 20), __double2loint(v));
+}
+
+// x += scale * sum_r coef[r] Z_r (ASSIGN: x = scale * sum_r coef[r] Z_r, x not read) with FP32 Z,
+// |coef| <= 1 and scale = 2^k (the host normalises the coefficients by a power of two): the sum in
+// double-FP32, widened by one FP64 addition and scaled exactly (ASSIGN), or added into x by one FMA.
 // STEP (with ASSIGN): also xs = xb - x, the full Newton step from the value just stored.
 template <int CNT, bool ASSIGN, bool STEP = false>
 __global__ void k_combine_df(const float* __restrict__ Z, size_t ldz, const double* __restrict__ coef, double scale,
-                             double* x, size_t N, const double* __restrict__ xb = nullptr,
+                             int kscale, double* x, size_t N, const double* __restrict__ xb = nullptr,
                              double* __restrict__ xs = nullptr) {
     pdl_wait();
     pdl_trigger();
@@ -359,7 +369,7 @@ __global__ void k_combine_df(const float* __restrict__ Z, size_t ldz, const doub
         DF t{0.0f, 0.0f};
 #pragma unroll
         for (int r = 0; r < CNT; ++r) df_mac(t, c[r], Z[(size_t)r * ldz + i]);
-        const double v = ASSIGN ? __dmul_rn(scale, df_to_f64(t)) : __fma_rn(scale, df_to_f64(t), x[i]);
+        const double v = ASSIGN ? scale_pow2(df_to_f64(t), kscale, scale) : __fma_rn(scale, df_to_f64(t), x[i]);
         x[i] = v;
         if (STEP) xs[i] = xb[i] - v;
     }
@@ -368,10 +378,15 @@ __global__ void k_combine_df(const float* __restrict__ Z, size_t ldz, const doub
 template <bool ASSIGN, bool STEP>
 void launch_combine_df_block(Context& ctx, unsigned grid, int cnt, const float* Z, size_t N, const double* coef,
                              double scale, double* x, const double* xb, double* xs) {
+    int kscale = 0;
+    const double mant = std::frexp(scale, &kscale);  // scale = 2^(kscale - 1) when mant = 1/2
+    if (mant != 0.5) throw Status(NUMA_GPU_ERR_INVALID_ARGUMENT, "gmres: the combine scale must be a power of two");
+    kscale -= 1;
     switch (cnt) {
 #define NUMA_COMBINE_DF_CASE(K)                                                                               \
     case K:                                                                                                   \
-        launch_pdl(k_combine_df<K, ASSIGN, STEP>, grid, 256, 0, ctx.stream, Z, N, coef, scale, x, N, xb, xs);   \
+        launch_pdl(k_combine_df<K, ASSIGN, STEP>, grid, 256, 0, ctx.stream, Z, N, coef, scale, kscale, x, N, xb, \
+                   xs);                                                                                       \
         break;
         NUMA_COMBINE_DF_CASE(1)
         NUMA_COMBINE_DF_CASE(2)
@@ -763,11 +778,16 @@ GmresResult Gmres::solve_lazy(LinearOp& A, Precond* M, const double* b, double* 
         }
         double* yh = pin_.get(m);
         for (size_t jj = 0; jj < k; ++jj) yh[jj] = y[jj] * sig[jj];
-        double scale = 0.0;
+        double scale = 1.0;  // a power of two at or above max |yh|: the division is exact
         if (v32) {
-            for (size_t jj = 0; jj < k; ++jj) scale = std::max(scale, std::abs(yh[jj]));
-            if (scale > 0.0)
+            double amax = 0.0;
+            for (size_t jj = 0; jj < k; ++jj) amax = std::max(amax, std::abs(yh[jj]));
+            if (amax > 0.0 && std::isfinite(amax)) {
+                int e = 0;
+                std::frexp(amax, &e);  // amax < 2^e
+                scale = std::ldexp(1.0, e);
                 for (size_t jj = 0; jj < k; ++jj) yh[jj] /= scale;
+            }
         }
         NUMA_CUDA(cudaMemcpyAsync(ydev, yh, k * sizeof(double), cudaMemcpyHostToDevice, ctx_.stream));
         if (v32) {

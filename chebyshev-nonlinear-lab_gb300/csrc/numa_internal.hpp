@@ -72,6 +72,11 @@ public:
         (void)cache;
         return nullptr;
     }
+    // RN32 of the Jacobian coefficient in cache, where the operator keeps it (else null)
+    virtual const float* coef32_of_cache(const double* cache) const {
+        (void)cache;
+        return nullptr;
+    }
     // out = F(x); cache := the Jacobian data at x (when cache_size() > 0); norm_out := ||F(x)||
     // as a device scalar (optional).
     virtual void eval(const double* x, double* out, double* cache, double* norm_out) = 0;
@@ -107,7 +112,8 @@ public:
         (void)v32;
         (void)out;
     }
-    // The same product rounded once to FP32 (for an FP32 Krylov basis), where has_jvp32x().
+    // The same product to FP32 accuracy with FP32 output (for an FP32 Krylov basis; its error near
+    // the final rounding's), where has_jvp32x().
     virtual void jvp_bound32xf(const float* v32, float* out32) {
         (void)v32;
         (void)out32;
@@ -149,6 +155,9 @@ public:
     size_t cache_size() const override { return mixed_cache_ ? N_ + 2 * ((N_ + 1) / 2) : N_; }
     const float* f32_of_cache(const double* cache) const override {
         return mixed_cache_ && cache ? reinterpret_cast<const float*>(cache + N_ + (N_ + 1) / 2) : nullptr;
+    }
+    const float* coef32_of_cache(const double* cache) const override {
+        return mixed_cache_ && cache ? reinterpret_cast<const float*>(cache + N_) : nullptr;
     }
     void prepare_cache(int precision) override { mixed_cache_ = precision == NUMA_GPU_FP32; }
     void eval(const double* x, double* out, double* cache, double* norm_out) override;
@@ -371,7 +380,8 @@ public:
     // with -Lap_h - c instead of -Lap_h, c the full-weighting restriction of the fine coefficient c
     // (for Bratu3D's Jacobian, c = lambda e^u) set by set_coarse_coefficient.
     bool supports_coarse_jacobian() const { return precision_ == NUMA_GPU_FP32 && tail_l_ != SIZE_MAX; }
-    void set_coarse_coefficient(const double* c_fine);
+    // c32_fine (may be null): RN32(c_fine), read instead of c_fine (the same values, half the bytes).
+    void set_coarse_coefficient(const double* c_fine, const float* c32_fine = nullptr);
     void clear_coarse_coefficient() { coarse_jac_ = false; }
 
     struct Level;
@@ -440,6 +450,11 @@ public:
     // Binds at the nonlinear iterate x; cache = the operator's Jacobian data at x (for Bratu3D
     // c = lambda e^x) when the caller has it (may be null).
     virtual void make(const double* x, const double* cache) = 0;
+    // The same where the operator also keeps RN32 of its coefficient (c32, not null).
+    virtual void make_c32(const double* x, const double* cache, const float* c32) {
+        (void)c32;
+        make(x, cache);
+    }
     virtual void apply(const double* r, double* z) = 0;
     virtual int kind() const = 0;
     virtual void progress(size_t iters, double rel_res) {

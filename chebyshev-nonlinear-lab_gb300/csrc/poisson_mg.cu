@@ -455,31 +455,56 @@ namespace {
 
 // cc = the full-weighting restriction of a natural-layout coefficient (weights (1/4, 1/2, 1/4) per
 // dimension, summed z outer, y, x inner), FP32 out.  An FP64 input is rounded to FP32 by the integer
-// conversion (the hardware one issues on the FP64 pipe: 27 of them per coarse point made the 255^3
-// restriction FP64-bound at ~95 us).
+// conversion (the hardware one issues on the FP64 pipe).  A thread owns a coarse (K, J) column and
+// marches I: fine plane 2I+2 of one step is plane 2I of the next, kept in registers, so a coarse point
+// loads 18 fine values, not 27.
 template <class TI>
-__global__ void k_restrict_coef(const TI* __restrict__ cf, float* __restrict__ cc, int nf, int nc) {
+__global__ void __launch_bounds__(BX* BY) k_restrict_coef(const TI* __restrict__ cf, float* __restrict__ cc, int nf,
+                                                          int nc, int ichunk) {
     pdl_wait();
     pdl_trigger();
-    const int Nc = nc * nc * nc;
+    const int K = blockIdx.x * BX + threadIdx.x;
+    const int J = blockIdx.y * BY + threadIdx.y;
+    if (K >= nc || J >= nc) return;
+    const int I0 = blockIdx.z * ichunk;
+    const int I1 = min(I0 + ichunk, nc);
     const float w[3] = {0.25f, 0.5f, 0.25f};
-    const int stride = gridDim.x * blockDim.x;
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < Nc; q += stride) {
-        const int K = q % nc, J = (q / nc) % nc, I = q / (nc * nc);
+    const size_t pf = (size_t)nf * nf;
+    const size_t col = (size_t)(2 * J) * nf + 2 * K;  // fine (2J, 2K) within a plane
+    auto load_plane = [&](int i, float (&v)[9]) {
+        const TI* q = cf + (size_t)i * pf + col;
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) v[b * 3 + c] = f64_to_f32(q[(size_t)b * nf + c]);
+    };
+    float p0[9], p1[9], p2[9];
+    load_plane(2 * I0, p0);
+    for (int I = I0; I < I1; ++I) {
+        load_plane(2 * I + 1, p1);
+        load_plane(2 * I + 2, p2);
         float acc = 0.0f;
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b)
-                for (int c = 0; c < 3; ++c) {
-                    const size_t f = ((size_t)(2 * I + a) * nf + 2 * J + b) * nf + 2 * K + c;
-                    acc = __fmaf_rn(w[a] * w[b] * w[c], f64_to_f32(cf[f]), acc);
-                }
-        cc[q] = acc;
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) acc = __fmaf_rn(w[0] * w[b] * w[c], p0[b * 3 + c], acc);
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) acc = __fmaf_rn(w[1] * w[b] * w[c], p1[b * 3 + c], acc);
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) acc = __fmaf_rn(w[2] * w[b] * w[c], p2[b * 3 + c], acc);
+        cc[((size_t)I * nc + J) * nc + K] = acc;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) p0[q] = p2[q];
     }
 }
 
 }  // namespace
 
-void PoissonMG::set_coarse_coefficient(const double* c_fine) {
+void PoissonMG::set_coarse_coefficient(const double* c_fine, const float* c32_fine) {
     if (!supports_coarse_jacobian())
         throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "Jacobian-aware coarse levels need the FP32 cycle with a one-CTA tail");
     if (cl_off_.empty()) {
@@ -493,11 +518,17 @@ void PoissonMG::set_coarse_coefficient(const double* c_fine) {
     }
     for (size_t l = 1; l < levels_.size(); ++l) {
         const int nf = levels_[l - 1]->n, nc = levels_[l]->n;
-        const size_t Nc = (size_t)nc * nc * nc;
-        const unsigned g = ew_grid(ctx_, Nc);
-        if (l == 1) launch_pdl(k_restrict_coef<double>, g, 256, 0, ctx_.stream, c_fine, cl_.p + cl_off_[1], nf, nc);
-        else launch_pdl(k_restrict_coef<float>, g, 256, 0, ctx_.stream, (const float*)(cl_.p + cl_off_[l - 1]),
-                        cl_.p + cl_off_[l], nf, nc);
+        const int ichunk = nc >= 64 ? 8 : (nc >= 16 ? 4 : 1);
+        const dim3 g((nc + BX - 1) / BX, (nc + BY - 1) / BY, (nc + ichunk - 1) / ichunk);
+        if (l == 1 && c32_fine)
+            launch_pdl(k_restrict_coef<float>, g, dim3(BX, BY), 0, ctx_.stream, c32_fine, cl_.p + cl_off_[1], nf, nc,
+                       ichunk);
+        else if (l == 1)
+            launch_pdl(k_restrict_coef<double>, g, dim3(BX, BY), 0, ctx_.stream, c_fine, cl_.p + cl_off_[1], nf, nc,
+                       ichunk);
+        else
+            launch_pdl(k_restrict_coef<float>, g, dim3(BX, BY), 0, ctx_.stream, (const float*)(cl_.p + cl_off_[l - 1]),
+                       cl_.p + cl_off_[l], nf, nc, ichunk);
         ctx_.count_launch();
     }
     ctx_.check_launch("mg coarse coefficient");
