@@ -540,18 +540,24 @@ def run_ours(args) -> int:
         eb = 8 if mgp == G.FP64 else 4
         # the residual evaluation: algorithmic 16 B a point (u read, F written once); the drivers'
         # cache adds c = lambda e^u (8 B) and, on the mixed path, RN32(c) and RN32(F) (4 + 4 B).
-        # FP64 instructions a point: ncu's count from the committed capture of the mixed path's
-        # evaluation (13.7: the 7-point sum with one FMA, e^u 5 with lambda in the table, F, the norm
-        # and the block reduction); the plain FP64 evaluation has one more (6u and the subtraction)
+        # Instructions a point: ncu's counts from the committed capture of the mixed path's evaluation
+        # (FP64: e^u 4 with lambda in the table, F 1, the norm 1 and the block reduction; ALU: the 7-point
+        # sum in 64-bit fixed point, the FP32 conversions, addressing); the plain FP64 evaluation sums
+        # in the reference's FP64 chain instead: 13.4 FP64 instructions a point by an earlier capture
         eval_bytes = 16.0 * N
         eval_moved = (32.0 if mgp == G.FP32 else 24.0) * N
         prof = load_profile(ROOT / "profiles" / "k_eval_fp32cache_255.json")
-        dp_mixed = prof["fp64_thread_instructions"] / prof["points"] if prof.get("points") else 13.7
-        eval_dp_per_pt = dp_mixed if mgp == G.FP32 else dp_mixed + 1.0
+        dp_mixed = prof["fp64_thread_instructions"] / prof["points"] if prof.get("points") else 6.4
+        alu_mixed = 32.0 * prof["alu_warp_instructions"] / prof["points"] if prof.get("alu_warp_instructions") else None
+        eval_dp_per_pt = dp_mixed if mgp == G.FP32 else 13.4
         if mgp != G.FP32:
-            prof = {}
+            prof, alu_mixed = {}, None
         ach_eval = eval_bytes / (ms_eval * 1e-3) / 1e9
         dp_rate = eval_dp_per_pt * N / (ms_eval * 1e-3) / 1e12
+        sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+        sm_mhz = (clk.summary().get("sm_mhz") or 2070.0)
+        alu_peak = 64.0 * sm_count * sm_mhz * 1e6 / 1e12  # 64 ALU operations a clock an SM
+        alu_rate = alu_mixed * N / (ms_eval * 1e-3) / 1e12 if alu_mixed else None
         # one red-black colour pass: the own-colour right-hand side (N/2) and the other-colour
         # neighbours (N/2) read once, the own-colour values (N/2) written once
         pass_bytes = 3 * (N / 2) * eb
@@ -566,10 +572,16 @@ def run_ours(args) -> int:
                 "achieved_tinstr_per_s": dp_rate, "peak_tinstr_per_s": fp64_peak / 2,
                 "peak_fma_tflops_measured": fp64_peak, "frac": dp_rate / (fp64_peak / 2),
                 "dp_instr_per_point": eval_dp_per_pt,
-                "note": f"the bound that holds: FP64 arithmetic (e^u and the 7-point sum, {eval_dp_per_pt:.1f} FP64 "
-                        "instructions a point by ncu) against the FMA-chain peak measured live; HBM would allow "
-                        "~14x the rate",
+                "note": f"FP64 arithmetic ({eval_dp_per_pt:.1f} FP64 instructions a point by ncu) against the FMA-chain "
+                        "peak measured live",
             },
+            "alu_pipe": (None if alu_rate is None else {
+                "achieved_tops": alu_rate, "peak_tops": alu_peak, "frac": alu_rate / alu_peak,
+                "alu_ops_per_point": alu_mixed,
+                "note": "the bound that holds on the mixed path: the integer work of the fixed-point 7-point sum "
+                        "(ALU operations a point by ncu) against 64 ALU operations a clock an SM at the sampled SM "
+                        "clock; ncu reads the ALU pipe 81 % and the FP64 pipe 70 % busy, HBM 15 %",
+            }),
             "vcycle_colour_pass": {
                 "kernel": (f"k_rbgs<double> colour pass, {n}^3" if mgp == G.FP64 else
                            f"k_pass_split colour pass (FP32, colour-split layout), {n}^3"),
