@@ -145,7 +145,8 @@ struct BClass {
 // F = h^-2 (6 u - sum) - lambda e^u at the instances with eval[t] set, from x_a or x_b (the one
 // selected by cur[t] ^ which), with RN32(lambda e^u) into c32, RN32(F) into f32 (the first FP32
 // Krylov vector of the next linear solve) and the block's sum of F^2 into partials: the arithmetic
-// of the single-instance residual kernel, point for point.
+// of the single-instance residual kernel (its fixed-point 7-point sum), with lambda e^u as lambda times
+// e^u (the single-instance operator scales its exp table by its one lambda instead).
 __global__ void __launch_bounds__(kBX* kBY) k_beval(const double* __restrict__ xa, const double* __restrict__ xb,
                                                     const int* __restrict__ cur, int which,
                                                     const int* __restrict__ eval, const double* __restrict__ lam,
@@ -176,12 +177,8 @@ __global__ void __launch_bounds__(kBX* kBY) k_beval(const double* __restrict__ x
             const double jp = (j + 1 < n) ? u[p + n] : 0.0;
             const double km = (k > 0) ? u[p - 1] : 0.0;
             const double kp = (k + 1 < n) ? u[p + 1] : 0.0;
-            double s = __fma_rn(6.0, curv, -below);  // as the single-instance mixed evaluation
-            s = s - above;
-            s = s - jm;
-            s = s - jp;
-            s = s - km;
-            s = s - kp;
+            // as the single-instance mixed evaluation: the 7-point sum in 64-bit fixed point, rounded once
+            const double s = lap7_fixed(curv, below, above, jm, jp, km, kp);
             const double e = lm * exp_tang(curv);
             const double f = __fma_rn(h2inv, s, -e);
             F[base + p] = f;

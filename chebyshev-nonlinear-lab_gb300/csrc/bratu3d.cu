@@ -87,6 +87,12 @@ __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, d
         size_t p = ((size_t)i0 * n + j) * n + k;
         double below = (i0 > 0) ? u[p - plane] : 0.0;
         double cur = u[p];
+        // the mixed path's fixed-point parts of the column values, split once and carried along i
+        FxParts fb{}, fc{};
+        if (C32) {
+            fb = fx_split(below);
+            fc = fx_split(cur);
+        }
         for (int i = i0; i < i1; ++i) {
             double above;
             double s;
@@ -96,7 +102,11 @@ __global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, d
                 const double jp = (j + 1 < n) ? u[p + n] : 0.0;
                 const double km = (k > 0) ? u[p - 1] : 0.0;
                 const double kp = (k + 1 < n) ? u[p + 1] : 0.0;
-                s = lap7_fixed(cur, below, above, jm, jp, km, kp);
+                const FxParts fa = fx_split(above);
+                s = lap7_fixed(fc, fb, fa, fx_split(jm), fx_split(jp), fx_split(km), fx_split(kp), cur, below, above,
+                               jm, jp, km, kp);
+                fb = fc;
+                fc = fa;
             } else {
                 s = lap_sum(u, p, plane, n, i, j, k, below, cur, above);
             }

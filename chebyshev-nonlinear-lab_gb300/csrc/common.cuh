@@ -348,36 +348,36 @@ static __device__ __noinline__ double lap7_fp64_rare(double c, double a1, double
     s = s - a5;
     return s - a6;
 }
-__device__ __forceinline__ void fx_split(double x, unsigned long long& mag, int& e, bool& neg) {
+// A value's fixed-point parts: 53-bit significand (hidden bit set for normal numbers), exponent
+// (1 for zeros and subnormals), sign.
+struct FxParts {
+    unsigned long long mag;
+    int e;
+    bool neg;
+};
+__device__ __forceinline__ FxParts fx_split(double x) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const int eb = (int)((b >> 52) & 0x7FFu);
-    mag = (b & 0xFFFFFFFFFFFFFull) | (eb ? (1ull << 52) : 0ull);
-    e = eb ? eb : 1;  // a subnormal: exponent 1 without the hidden bit
-    neg = (long long)b < 0;
+    FxParts f;
+    f.mag = (b & 0xFFFFFFFFFFFFFull) | (eb ? (1ull << 52) : 0ull);
+    f.e = eb ? eb : 1;  // a subnormal: exponent 1 without the hidden bit
+    f.neg = (long long)b < 0;
+    return f;
 }
-__device__ __forceinline__ long long fx_term(unsigned long long mag, int e, bool neg, int E) {
-    const int d = E - e;
-    const unsigned long long t = d < 60 ? (mag << 4) >> d : 0ull;
-    return neg ? -(long long)t : (long long)t;
+__device__ __forceinline__ long long fx_term(const FxParts& f, int E) {
+    // E - f.e >= 57 leaves nothing of the 57-bit value; 63 keeps the shift defined
+    const unsigned long long t = (f.mag << 4) >> min(E - f.e, 63);
+    return f.neg ? -(long long)t : (long long)t;
 }
-__device__ __forceinline__ double lap7_fixed(double c, double a1, double a2, double a3, double a4, double a5,
-                                             double a6) {
-    unsigned long long m0, m1, m2, m3, m4, m5, m6;
-    int e0, e1, e2, e3, e4, e5, e6;
-    bool n0, n1, n2, n3, n4, n5, n6;
-    fx_split(c, m0, e0, n0);
-    fx_split(a1, m1, e1, n1);
-    fx_split(a2, m2, e2, n2);
-    fx_split(a3, m3, e3, n3);
-    fx_split(a4, m4, e4, n4);
-    fx_split(a5, m5, e5, n5);
-    fx_split(a6, m6, e6, n6);
-    const int E = max(max(max(e0, e1), max(e2, e3)), max(max(e4, e5), e6));
+// The sum from the seven values' parts (c first); the values themselves for the rare cases.
+__device__ __forceinline__ double lap7_fixed(const FxParts& f0, const FxParts& f1, const FxParts& f2, const FxParts& f3,
+                                             const FxParts& f4, const FxParts& f5, const FxParts& f6, double c,
+                                             double a1, double a2, double a3, double a4, double a5, double a6) {
+    const int E = max(max(max(f0.e, f1.e), max(f2.e, f3.e)), max(max(f4.e, f5.e), f6.e));
     if (E >= 2040) return lap7_fp64_rare(c, a1, a2, a3, a4, a5, a6);  // infinities, NaN, near overflow
-    const long long t0 = fx_term(m0, e0, n0, E);
-    const long long S = ((t0 << 2) + (t0 << 1)) - fx_term(m1, e1, n1, E) - fx_term(m2, e2, n2, E) -
-                        fx_term(m3, e3, n3, E) - fx_term(m4, e4, n4, E) - fx_term(m5, e5, n5, E) -
-                        fx_term(m6, e6, n6, E);
+    const long long t0 = fx_term(f0, E);
+    const long long S = ((t0 << 2) + (t0 << 1)) - fx_term(f1, E) - fx_term(f2, E) - fx_term(f3, E) - fx_term(f4, E) -
+                        fx_term(f5, E) - fx_term(f6, E);
     if (S == 0) return 0.0;
     const unsigned long long sign = S < 0 ? (1ull << 63) : 0ull;
     unsigned long long A = S < 0 ? (unsigned long long)(-S) : (unsigned long long)S;
@@ -390,6 +390,11 @@ __device__ __forceinline__ double lap7_fixed(double c, double a1, double a2, dou
     mant += (rem > 0x400u || (rem == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
     // the hidden bit adds one to the exponent field; a carry out of the significand adds one more
     return __longlong_as_double((long long)(sign | ((((unsigned long long)(eb - 1)) << 52) + mant)));
+}
+__device__ __forceinline__ double lap7_fixed(double c, double a1, double a2, double a3, double a4, double a5,
+                                             double a6) {
+    return lap7_fixed(fx_split(c), fx_split(a1), fx_split(a2), fx_split(a3), fx_split(a4), fx_split(a5),
+                      fx_split(a6), c, a1, a2, a3, a4, a5, a6);
 }
 
 // ------------------------------------------------------------------------------------------
