@@ -78,7 +78,8 @@ def parse_args(argv=None):
     ap.add_argument("--cpu-reps", type=int, default=2, help="all-core CPU solves of the cpu_baseline leg")
     ap.add_argument("--ref-budget", type=float, default=270.0,
                     help="seconds the reference arm may spend on its warm-up and timed solves")
-    ap.add_argument("--kernel-case", choices=["none", "vcycle", "solve", "conv", "bruss", "stencils", "eval", "batch"],
+    ap.add_argument("--kernel-case", choices=["none", "vcycle", "solve", "conv", "bruss", "stencils", "eval", "batch",
+                                              "learned-config"],
                     default="none",
                     help="profiling driver: run only this small case (for ncu)")
     return ap.parse_args(argv)
@@ -580,7 +581,7 @@ def run_ours(args) -> int:
                 "alu_ops_per_point": alu_mixed,
                 "note": "the bound that holds on the mixed path: the integer work of the fixed-point 7-point sum "
                         "(ALU operations a point by ncu) against 64 ALU operations a clock an SM at the sampled SM "
-                        "clock; ncu reads the ALU pipe 81 % and the FP64 pipe 70 % busy, HBM 15 %",
+                        "clock; ncu reads the ALU pipe 77 % and the FP64 pipe 72 % busy, HBM 16 %",
             }),
             "vcycle_colour_pass": {
                 "kernel": (f"k_rbgs<double> colour pass, {n}^3" if mgp == G.FP64 else
@@ -812,6 +813,59 @@ def learned_summary(learned, fp64_sec, x_fp64):
     }
 
 
+def learned_config_case(G, ctx, args) -> int:
+    """The learned preconditioner at the scale of the learned-preconditioner configuration: trained on
+    ~20k residual-error pairs from GMG-preconditioned solves of Bratu3D 127^3 at seeded lambda ~ U[1, 6.5]
+    (200 instances x 3 states x (F(u), 29 Arnoldi vectors of its solve, 4 sums of 8 seeded Gaussian
+    bumps)), then evaluated inside FGMRES(30) against the mixed path without it and the plain FP64 path
+    at lambda values the training did not draw, at 127^3 and 255^3 (u0 = 0, rtol 1e-10).  Opt-in: it
+    takes a few minutes and is not part of the default run."""
+    import time
+    net = G.LearnedNet(ctx, 31, seed=3)
+    t0 = time.perf_counter()
+    rep = net.train(127, instances=200, states=3, rhs_per_state=4, krylov_per_state=29, epochs=2, batch=8,
+                    lr=1e-3, lambda_min=1.0, lambda_max=6.5, seed=2024, solve_rtol=1e-6)
+    t_train = time.perf_counter() - t0
+    rows = []
+    for n, lams in ((127, (2.0, 4.0, 6.0)), (255, (3.0, 6.0))):
+        N = n ** 3
+        x = ctx.vec(N)
+        pcs = {"fp64": G.Provider.poisson_mg(ctx, n, precision=G.FP64),
+               "mixed": G.Provider.poisson_mg(ctx, n, precision=G.FP32),
+               "learned": G.Provider.learned(ctx, n, net, stall=0.9)}
+        prm = {"fp64": params_for(G, "fp64"), "mixed": params_for(G, "mixed_fp32"),
+               "learned": params_for(G, "mixed_fp32")}
+        for lam in lams:
+            op = G.Bratu3D(ctx, n, lam)
+            row = {"n": n, "lambda": lam}
+            xref = None
+            for tag in ("fp64", "mixed", "learned"):
+                x.fill(0.0)
+                G.solve(op, x, "nk", prm[tag], pcs[tag])  # warm
+                ctx.sync()
+                x.fill(0.0)
+                t1 = time.perf_counter()
+                r = G.solve(op, x, "nk", prm[tag], pcs[tag])
+                ctx.sync()
+                dt = time.perf_counter() - t1
+                xv = x.numpy()
+                if tag == "fp64":
+                    xref = xv
+                row[tag] = {"s": dt, "iters": r["iters"], "lin_iters": r["n_lin_iters"], "converged": r["converged"],
+                            "rel_err_vs_fp64": float(np.linalg.norm(xv - xref) / np.linalg.norm(xref))}
+            applies, fallbacks = pcs["learned"].learned_stats()
+            row["learned"]["net_applies"], row["learned"]["fallbacks"] = applies, fallbacks
+            rows.append(row)
+            op.close()
+        for pc in pcs.values():
+            pc.close()
+    print(json.dumps({"kernel_case": "learned-config", "params": net.num_params(),
+                      "training": {k: rep[k] for k in ("samples", "gen_seconds", "train_seconds", "loss_first",
+                                                        "loss_last", "target_ms")},
+                      "training_wall_s": t_train, "held_out": rows}), flush=True)
+    return 0
+
+
 def load_profile(f: Path) -> dict:
     """A committed ncu summary (JSON beside its .md), or {} when absent."""
     try:
@@ -857,6 +911,8 @@ def run_kernel_case(G, ctx, args) -> int:
         print(json.dumps({"kernel_case": "batch", "instances": len(inst), "s_per_batch": t / max(1, args.steps),
                           "launches": ctx.kernel_launches()}))
         return 0
+    if args.kernel_case == "learned-config":
+        return learned_config_case(G, ctx, args)
     if args.kernel_case == "eval":
         # the residual evaluation with the mixed path's cache, on a smooth iterate of the solve's size
         op = G.Bratu3D(ctx, n, args.lam)
