@@ -289,22 +289,17 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs_df(const float* w, const fl
     DF acc[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) acc[r] = DF{0.0f, 0.0f};
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) {
+    // One element: its w (or partial sum) and basis values already loaded.
+    auto body = [&](size_t i, float wi, float2 pin, const float (&ur)[CNT]) {
         if (MODE == 0) {
-            const float wi = w[i];
 #pragma unroll
-            for (int r = 0; r < CNT; ++r) df_mac(acc[r], wi, r == 0 ? u0[i] : U[(size_t)r * ldu + i]);
+            for (int r = 0; r < CNT; ++r) df_mac(acc[r], wi, ur[r]);
         } else {
             DF t{0.0f, 0.0f};
-            if (part_in) {
-                const float2 p = part_in[i];
-                t = DF{p.x, p.y};
-            } else {
-                df_mac(t, cw, w[i]);
-            }
+            if (part_in) t = DF{pin.x, pin.y};
+            else df_mac(t, cw, wi);
 #pragma unroll
-            for (int r = 0; r < CNT; ++r) df_mac(t, c[r], r == 0 ? u0[i] : U[(size_t)r * ldu + i]);
+            for (int r = 0; r < CNT; ++r) df_mac(t, c[r], ur[r]);
             if (MODE == 3) {
                 part_out[i] = make_float2(t.hi, t.lo);
             } else {
@@ -314,10 +309,36 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs_df(const float* w, const fl
                     df_mac(acc[0], u, u);
                 } else {
 #pragma unroll
-                    for (int r = 0; r < CNT; ++r) df_mac(acc[r], u, r == 0 ? u0[i] : U[(size_t)r * ldu + i]);
+                    for (int r = 0; r < CNT; ++r) df_mac(acc[r], u, ur[r]);
                 }
             }
         }
+    };
+    auto load = [&](size_t i, float& wi, float2& pin, float (&ur)[CNT]) {
+        if (MODE != 0 && part_in) pin = part_in[i];
+        else wi = w[i];
+#pragma unroll
+        for (int r = 0; r < CNT; ++r) ur[r] = r == 0 ? u0[i] : U[(size_t)r * ldu + i];
+    };
+    // UF elements a thread an iteration, all their loads issued before any arithmetic: with one element a
+    // thread the loads in flight were too few to cover DRAM latency (the passes ran at ~50 % of HBM).  Each
+    // thread still visits its elements in the same order, so the sums are unchanged.
+    constexpr int UF = CNT <= 3 ? 4 : 2;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    for (; i + (UF - 1) * stride < N; i += UF * stride) {
+        float wv[UF] = {}, uv[UF][CNT];
+        float2 pv[UF] = {};
+#pragma unroll
+        for (int q = 0; q < UF; ++q) load(i + q * stride, wv[q], pv[q], uv[q]);
+#pragma unroll
+        for (int q = 0; q < UF; ++q) body(i + q * stride, wv[q], pv[q], uv[q]);
+    }
+    for (; i < N; i += stride) {
+        float wi = 0.0f, ur[CNT];
+        float2 pin = make_float2(0.0f, 0.0f);
+        load(i, wi, pin, ur);
+        body(i, wi, pin, ur);
     }
     if constexpr (MODE != 3) {
         double s[R];
@@ -364,14 +385,37 @@ __global__ void k_combine_df(const float* __restrict__ Z, size_t ldz, const doub
     DF c[CNT];
 #pragma unroll
     for (int r = 0; r < CNT; ++r) c[r] = cs[r];
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) {
+    // as in k_cgs_df: UF elements a thread an iteration, all loads first
+    auto body = [&](size_t i, const float (&zr)[CNT], double xi, double xbi) {
         DF t{0.0f, 0.0f};
 #pragma unroll
-        for (int r = 0; r < CNT; ++r) df_mac(t, c[r], Z[(size_t)r * ldz + i]);
-        const double v = ASSIGN ? scale_pow2(df_to_f64(t), kscale, scale) : __fma_rn(scale, df_to_f64(t), x[i]);
+        for (int r = 0; r < CNT; ++r) df_mac(t, c[r], zr[r]);
+        const double v = ASSIGN ? scale_pow2(df_to_f64(t), kscale, scale) : __fma_rn(scale, df_to_f64(t), xi);
         x[i] = v;
-        if (STEP) xs[i] = xb[i] - v;
+        if (STEP) xs[i] = xbi - v;
+    };
+    auto load = [&](size_t i, float (&zr)[CNT], double& xi, double& xbi) {
+#pragma unroll
+        for (int r = 0; r < CNT; ++r) zr[r] = Z[(size_t)r * ldz + i];
+        if (!ASSIGN) xi = x[i];
+        if (STEP) xbi = xb[i];
+    };
+    constexpr int UF = CNT <= 3 ? 4 : 2;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    for (; i + (UF - 1) * stride < N; i += UF * stride) {
+        float zv[UF][CNT];
+        double xv[UF] = {}, xbv[UF] = {};
+#pragma unroll
+        for (int q = 0; q < UF; ++q) load(i + q * stride, zv[q], xv[q], xbv[q]);
+#pragma unroll
+        for (int q = 0; q < UF; ++q) body(i + q * stride, zv[q], xv[q], xbv[q]);
+    }
+    for (; i < N; i += stride) {
+        float zr[CNT];
+        double xi = 0.0, xbi = 0.0;
+        load(i, zr, xi, xbi);
+        body(i, zr, xi, xbi);
     }
 }
 
