@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(BX* BY) k_bresidual(MgPool P, const int* __res
     pdl_trigger();
     const int q = blockIdx.z / zch;
     if (!pool_active(P, act, q)) return;
-    residual_split_body(P.x + q * P.sx, P.b + q * P.sb, P.r + q * P.sr, g, h2inv, blockIdx.x, blockIdx.y,
+    residual_split_body<false>(P.x + q * P.sx, P.b + q * P.sb, P.r + q * P.sr, g, h2inv, blockIdx.x, blockIdx.y,
                         blockIdx.z - q * zch);
 }
 
@@ -302,7 +302,24 @@ __global__ void __launch_bounds__(kEwThreads) k_bdots(const float* __restrict__ 
 #pragma unroll
     for (int r = 0; r < CNT; ++r) acc[r] = DF{0.0f, 0.0f};
     const float* u = U + (long long)b0 * T;
-    for (long long i = B.beg[blockIdx.x] + threadIdx.x; i < B.end[blockIdx.x]; i += kEwThreads) {
+    // UF elements a thread an iteration, all loads first (more DRAM bytes in flight), same order
+    constexpr int UF = CNT <= 3 ? 4 : 2;
+    const long long e1 = B.end[blockIdx.x];
+    long long i = B.beg[blockIdx.x] + threadIdx.x;
+    for (; i + (UF - 1) * kEwThreads < e1; i += UF * kEwThreads) {
+        float wv[UF], uv[UF][CNT];
+#pragma unroll
+        for (int q = 0; q < UF; ++q) {
+            wv[q] = w[i + q * kEwThreads];
+#pragma unroll
+            for (int r = 0; r < CNT; ++r) uv[q][r] = u[(long long)r * T + i + q * kEwThreads];
+        }
+#pragma unroll
+        for (int q = 0; q < UF; ++q)
+#pragma unroll
+            for (int r = 0; r < CNT; ++r) df_mac(acc[r], wv[q], uv[q][r]);
+    }
+    for (; i < e1; i += kEwThreads) {
         const float wi = w[i];
 #pragma unroll
         for (int r = 0; r < CNT; ++r) df_mac(acc[r], wi, u[(long long)r * T + i]);
@@ -337,16 +354,12 @@ __global__ void __launch_bounds__(kEwThreads) k_bupdate(const float* __restrict_
     const float* u = U + (long long)b0 * T;
     float* uout = U + (long long)(j + 1) * T;
     DF acc{0.0f, 0.0f};
-    for (long long i = B.beg[blockIdx.x] + threadIdx.x; i < B.end[blockIdx.x]; i += kEwThreads) {
+    auto body = [&](long long i, float wi, float2 pv, const float (&ur)[CNT]) {
         DF s{0.0f, 0.0f};
-        if (first) {
-            df_mac(s, cw, w[i]);
-        } else {
-            const float2 pv = part[i];
-            s = DF{pv.x, pv.y};
-        }
+        if (first) df_mac(s, cw, wi);
+        else s = DF{pv.x, pv.y};
 #pragma unroll
-        for (int r = 0; r < CNT; ++r) df_mac(s, c[r], u[(long long)r * T + i]);
+        for (int r = 0; r < CNT; ++r) df_mac(s, c[r], ur[r]);
         if (LAST) {
             const float v = __fadd_rn(s.hi, s.lo);
             uout[i] = v;
@@ -354,6 +367,31 @@ __global__ void __launch_bounds__(kEwThreads) k_bupdate(const float* __restrict_
         } else {
             part[i] = make_float2(s.hi, s.lo);
         }
+    };
+    auto load = [&](long long i, float& wi, float2& pv, float (&ur)[CNT]) {
+        if (first) wi = w[i];
+        else pv = part[i];
+#pragma unroll
+        for (int r = 0; r < CNT; ++r) ur[r] = u[(long long)r * T + i];
+    };
+    // UF elements a thread an iteration, all loads first (more DRAM bytes in flight), same order; each
+    // element of part is read before it is written, by one thread
+    constexpr int UF = CNT <= 3 ? 4 : 2;
+    const long long e1 = B.end[blockIdx.x];
+    long long i = B.beg[blockIdx.x] + threadIdx.x;
+    for (; i + (UF - 1) * kEwThreads < e1; i += UF * kEwThreads) {
+        float wv[UF] = {}, uv[UF][CNT];
+        float2 pv[UF] = {};
+#pragma unroll
+        for (int q = 0; q < UF; ++q) load(i + q * kEwThreads, wv[q], pv[q], uv[q]);
+#pragma unroll
+        for (int q = 0; q < UF; ++q) body(i + q * kEwThreads, wv[q], pv[q], uv[q]);
+    }
+    for (; i < e1; i += kEwThreads) {
+        float wi = 0.0f, ur[CNT];
+        float2 pv = make_float2(0.0f, 0.0f);
+        load(i, wi, pv, ur);
+        body(i, wi, pv, ur);
     }
     if (LAST) {
         double sv[1] = {df_to_f64(acc)};
@@ -384,14 +422,38 @@ __global__ void __launch_bounds__(kEwThreads) k_bcombine(const float* __restrict
     const double* x = cur[t] ? xb : xa;
     double* xn = cur[t] ? const_cast<double*>(xa) : xb;
     const float* Zb = Z + (long long)b0 * T;
-    for (long long i = B.beg[blockIdx.x] + threadIdx.x; i < B.end[blockIdx.x]; i += kEwThreads) {
+    auto body = [&](long long i, const float (&zr)[CNT], double zi, double xi) {
         DF s{0.0f, 0.0f};
 #pragma unroll
         for (int r = 0; r < CNT; ++r)
-            if (b0 + r < kd) df_mac(s, c[r], Zb[(long long)r * T + i]);
-        const double v = asg ? __dmul_rn(sc, df_to_f64(s)) : __fma_rn(sc, df_to_f64(s), z[i]);
+            if (b0 + r < kd) df_mac(s, c[r], zr[r]);
+        const double v = asg ? __dmul_rn(sc, df_to_f64(s)) : __fma_rn(sc, df_to_f64(s), zi);
         z[i] = v;
-        if (last) xn[i] = x[i] - v;
+        if (last) xn[i] = xi - v;
+    };
+    auto load = [&](long long i, float (&zr)[CNT], double& zi, double& xi) {
+#pragma unroll
+        for (int r = 0; r < CNT; ++r) zr[r] = b0 + r < kd ? Zb[(long long)r * T + i] : 0.0f;
+        if (!asg) zi = z[i];
+        if (last) xi = x[i];
+    };
+    // UF elements a thread an iteration, all loads first (more DRAM bytes in flight)
+    constexpr int UF = CNT <= 3 ? 4 : 2;
+    const long long e1 = B.end[blockIdx.x];
+    long long i = B.beg[blockIdx.x] + threadIdx.x;
+    for (; i + (UF - 1) * kEwThreads < e1; i += UF * kEwThreads) {
+        float zv[UF][CNT];
+        double zs[UF] = {}, xs[UF] = {};
+#pragma unroll
+        for (int q = 0; q < UF; ++q) load(i + q * kEwThreads, zv[q], zs[q], xs[q]);
+#pragma unroll
+        for (int q = 0; q < UF; ++q) body(i + q * kEwThreads, zv[q], zs[q], xs[q]);
+    }
+    for (; i < e1; i += kEwThreads) {
+        float zr[CNT];
+        double zi = 0.0, xi = 0.0;
+        load(i, zr, zi, xi);
+        body(i, zr, zi, xi);
     }
 }
 
