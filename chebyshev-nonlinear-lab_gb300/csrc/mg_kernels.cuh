@@ -382,6 +382,10 @@ __device__ __forceinline__ void residual_pair(float* __restrict__ r, int LA, boo
     }
 }
 
+// BNAT: b is the natural-layout FP32 right-hand side itself (the finest level of an apply from an FP32
+// vector, whose b = RN32(r) = r is then not copied into the split layout); its last element has no
+// padding after it, so the second member's load is guarded.
+template <bool BNAT = false>
 __device__ __forceinline__ void residual_split_body(const float* __restrict__ x, const float* __restrict__ b,
                                                     float* __restrict__ r, Split g, float h2inv, int bx, int by,
                                                     int bz) {
@@ -401,7 +405,8 @@ __device__ __forceinline__ void residual_split_body(const float* __restrict__ x,
     const float* own0 = x + (cA0 ? g.half : 0);
     const float* oth0 = x + (cA0 ? 0 : g.half);
     const float xa0 = own0[mA0], xb0 = oth0[mA0 + cA0];
-    const float ba0 = b[(cA0 ? g.half : 0) + mA0], bb0 = b[(cB0 ? g.half : 0) + mB0];
+    const float ba0 = BNAT ? b[LA0] : b[(cA0 ? g.half : 0) + mA0];
+    const float bb0 = BNAT ? (hasB ? b[LA0 + 1] : 0.0f) : b[(cB0 ? g.half : 0) + mB0];
     const float a_im0 = oth0[mA0 + cA0 - g.hP - 1], a_jm0 = oth0[mA0 + cA0 - g.hn - 1], a_jp0 = oth0[mA0 + cA0 + g.hn];
     const float a_km0 = oth0[mA0 + cA0 - 1];
     const float b_im0 = own0[mB0 + cB0 - g.hP - 1], b_jm0 = own0[mB0 + cB0 - g.hn - 1], b_jp0 = own0[mB0 + cB0 + g.hn];
@@ -412,7 +417,8 @@ __device__ __forceinline__ void residual_split_body(const float* __restrict__ x,
     const float* own1 = x + (cA1 ? g.half : 0);
     const float* oth1 = x + (cA1 ? 0 : g.half);
     const float xa1 = own1[mA1], xb1 = oth1[mA1 + cA1];
-    const float ba1 = b[(cA1 ? g.half : 0) + mA1], bb1 = b[(cB1 ? g.half : 0) + mB1];
+    const float ba1 = BNAT ? b[LA1] : b[(cA1 ? g.half : 0) + mA1];
+    const float bb1 = BNAT ? (hasB ? b[LA1 + 1] : 0.0f) : b[(cB1 ? g.half : 0) + mB1];
     const float a_ip1 = oth1[mA1 + cA1 + g.hP], a_jm1 = oth1[mA1 + cA1 - g.hn - 1], a_jp1 = oth1[mA1 + cA1 + g.hn];
     const float a_km1 = oth1[mA1 + cA1 - 1];
     const float b_ip1 = own1[mB1 + cB1 + g.hP], b_jm1 = own1[mB1 + cB1 - g.hn - 1], b_jp1 = own1[mB1 + cB1 + g.hn];
@@ -424,11 +430,12 @@ __device__ __forceinline__ void residual_split_body(const float* __restrict__ x,
                       a_jp1, a_km1, xb0, b_ip1, b_jm1, b_jp1, b_kp1, h2inv);
 }
 
+template <bool BNAT = false>
 __global__ void __launch_bounds__(BX* BY) k_residual_split(const float* __restrict__ x, const float* __restrict__ b,
                                                             float* __restrict__ r, Split g, float h2inv) {
     pdl_wait();
     pdl_trigger();
-    residual_split_body(x, b, r, g, h2inv, blockIdx.x, blockIdx.y, blockIdx.z);
+    residual_split_body<BNAT>(x, b, r, g, h2inv, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // Restriction from a natural-layout fine residual into a split coarse level (odd nc): the
@@ -597,7 +604,8 @@ __global__ void __launch_bounds__(BX* BY) k_prolong_split(const float* __restric
 // b32 = RN32(r), bs32 = RN32(b32 * inv) into the split layout at the finest level; WRITE_X: also
 // the cycle's first smoothing pass (colour 0 from x = 0: x = bs / 6).  Thread t handles the
 // natural pair L = 2t (colour 0, index t) and L = 2t + 1 (colour 1, index half + t).
-template <bool WRITE_X, class RT>
+// WRITE_B = false: b is not stored (the residual reads the FP32 right-hand side itself, BNAT).
+template <bool WRITE_X, class RT, bool WRITE_B = true>
 __global__ void k_scale_in32_split(const RT* __restrict__ r, float* __restrict__ b, float* __restrict__ bs,
                                    float* __restrict__ x, float inv, int N, int half) {
     pdl_wait();
@@ -607,12 +615,12 @@ __global__ void k_scale_in32_split(const RT* __restrict__ r, float* __restrict__
         const int L = 2 * t;
         const float v0 = f64_to_f32(r[L]);
         const float s0 = v0 * inv;
-        b[t] = v0;
+        if (WRITE_B) b[t] = v0;
         bs[t] = s0;
         if (WRITE_X) x[t] = div6(s0);
         if (L + 1 < N) {
             const float v1 = f64_to_f32(r[L + 1]);
-            b[half + t] = v1;
+            if (WRITE_B) b[half + t] = v1;
             bs[half + t] = v1 * inv;
         }
     }

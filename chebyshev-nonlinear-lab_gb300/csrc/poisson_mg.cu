@@ -345,7 +345,9 @@ void PoissonMG::cycle32(size_t l) {
         // two planes a thread sharing their i-neighbours (a four-plane march without the sharing took 80
         // registers)
         const dim3 rgd(((n + 1) / 2 + BX - 1) / BX, (n + BY - 1) / BY, (n + 1) / 2);
-        launch_pdl(k_residual_split, rgd, blk, 0, s, x, b, r, g, (float)L.h2inv);
+        // the finest level of an apply from an FP32 vector reads b = r32 itself (never copied, see apply)
+        if (finest && in32_) launch_pdl(k_residual_split<true>, rgd, blk, 0, s, x, in32_, r, g, (float)L.h2inv);
+        else launch_pdl(k_residual_split<false>, rgd, blk, 0, s, x, b, r, g, (float)L.h2inv);
         ctx_.count_launch();
     }
     const Split gc = make_split(nc);
@@ -429,7 +431,12 @@ void PoissonMG::apply(const double* r, double* z) {
             if (L0.n & 1) {
                 const Split g = make_split(L0.n);
                 const unsigned grid = ew_grid(ctx_, (size_t)g.half);
-                if (first_fused32(0))
+                // from an FP32 vector with a coarser level below, the residual reads b from the input itself
+                const bool keep_b = !(std::is_same_v<RT, float> && levels_.size() > 1 && tail_l_ != 0);
+                if (first_fused32(0) && !keep_b)
+                    launch_pdl(k_scale_in32_split<true, RT, false>, grid, 256, 0, ctx_.stream, rin, L0.b32.p,
+                               L0.bs32.p, L0.xs, (float)L0.inv, (int)N, g.half);
+                else if (first_fused32(0))
                     launch_pdl(k_scale_in32_split<true, RT>, grid, 256, 0, ctx_.stream, rin, L0.b32.p, L0.bs32.p,
                                L0.xs, (float)L0.inv, (int)N, g.half);
                 else
