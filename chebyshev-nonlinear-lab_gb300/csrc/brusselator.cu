@@ -142,7 +142,10 @@ __device__ __forceinline__ double lap5(const double* __restrict__ a, int n, int 
 // thread marches down its rows.  Five FP64 instructions for each Laplacian instead of seven, the
 // same bits.  A warp covers 31 columns: lane 0 is the halo column whose east difference lane 1 needs.
 constexpr int kB2EvalRows = 32;  // rows a thread marches
-template <bool NORM>
+// FIXED (the mixed path's evaluation): each Laplacian as W + E + S + N - 4c in 64-bit fixed point, rounded
+// once (lap5_fixed, common.cuh; more accurate than the sum of rounded differences), on the integer pipe
+// instead of five FP64 instructions a species.
+template <bool NORM, bool FIXED = false>
 __global__ void __launch_bounds__(256) k_b2_eval(const double* __restrict__ w, const double* __restrict__ prev,
                                                  double* __restrict__ out, B2Geom G, RedArgs red, double* norm_out) {
     pdl_wait();
@@ -160,15 +163,32 @@ __global__ void __launch_bounds__(256) k_b2_eval(const double* __restrict__ w, c
     if (i0 < n) {
         const int im0 = i0 == 0 ? n - 1 : i0 - 1;
         double u = wu[(size_t)i0 * n + j], v = wv[(size_t)i0 * n + j];
-        double su = wu[(size_t)im0 * n + j] - u, sv = wv[(size_t)im0 * n + j] - v;  // S - c of row i0
+        double su = 0.0, sv = 0.0;  // S - c of row i0 (FIXED: S itself)
+        if (FIXED) {
+            su = wu[(size_t)im0 * n + j];
+            sv = wv[(size_t)im0 * n + j];
+        } else {
+            su = wu[(size_t)im0 * n + j] - u;
+            sv = wv[(size_t)im0 * n + j] - v;
+        }
         for (int i = i0; i < i1; ++i) {
             const size_t r = (size_t)i * n, p = r + j;
             const size_t rn = (size_t)(i + 1 == n ? 0 : i + 1) * n;
             const double un = wu[rn + j], vn = wv[rn + j];
-            const double eu = wu[r + jp] - u, ev = wv[r + jp] - v;                  // E - c
-            const double wu_ = -__shfl_up_sync(0xffffffffu, eu, 1), wv_ = -__shfl_up_sync(0xffffffffu, ev, 1);  // W - c
-            const double nu_ = un - u, nv_ = vn - v;                                // N - c
-            const double lu = (wu_ + eu) + (su + nu_), lv = (wv_ + ev) + (sv + nv_);
+            double lu, lv, nu_ = 0.0, nv_ = 0.0;
+            if (FIXED) {
+                const double Eu = wu[r + jp], Ev = wv[r + jp];
+                const double Wu = __shfl_up_sync(0xffffffffu, u, 1), Wv = __shfl_up_sync(0xffffffffu, v, 1);
+                lu = lap5_fixed(u, Wu, Eu, su, un);
+                lv = lap5_fixed(v, Wv, Ev, sv, vn);
+            } else {
+                const double eu = wu[r + jp] - u, ev = wv[r + jp] - v;                  // E - c
+                const double wu_ = -__shfl_up_sync(0xffffffffu, eu, 1), wv_ = -__shfl_up_sync(0xffffffffu, ev, 1);  // W - c
+                nu_ = un - u;                                                           // N - c
+                nv_ = vn - v;
+                lu = (wu_ + eu) + (su + nu_);
+                lv = (wv_ + ev) + (sv + nv_);
+            }
             const double uu = u * u;
             const double fu =
                 __fma_rn(G.Bp1, u, __fma_rn(-uu, v, __fma_rn(-G.duh, lu, __fma_rn(u - prev[p], G.invdt, -G.A))));
@@ -178,8 +198,13 @@ __global__ void __launch_bounds__(256) k_b2_eval(const double* __restrict__ w, c
                 out[nn + p] = fv;
                 if (NORM) acc[0] = __fma_rn(fv, fv, __fma_rn(fu, fu, acc[0]));
             }
-            su = -nu_;  // the next row's S - c
-            sv = -nv_;
+            if (FIXED) {  // the next row's S
+                su = u;
+                sv = v;
+            } else {      // the next row's S - c
+                su = -nu_;
+                sv = -nv_;
+            }
             u = un;
             v = vn;
         }
@@ -961,10 +986,13 @@ void Brusselator2D::set_previous(const double* w) { dev_copy(ctx_, w, prev_.p, s
 void Brusselator2D::eval(const double* x, double* out, double*, double* norm_out) {
     const dim3 grid = b2_eval_grid((int)n_);
     if (grid.x * grid.y > (unsigned)kMaxRedBlocks) throw Status(NUMA_GPU_ERR_NOT_SUPPORTED, "Brusselator2D grid too large");
-    if (norm_out)
-        launch_pdl(k_b2_eval<true>, grid, dim3(32, 8), 0, ctx_.stream, x, prev_.p, out, b2_geom(n_, P_), ctx_.red, norm_out);
-    else
-        launch_pdl(k_b2_eval<false>, grid, dim3(32, 8), 0, ctx_.stream, x, prev_.p, out, b2_geom(n_, P_), ctx_.red, nullptr);
+    const B2Geom G = b2_geom(n_, P_);
+    if (norm_out && fixed_sum_)
+        launch_pdl(k_b2_eval<true, true>, grid, dim3(32, 8), 0, ctx_.stream, x, prev_.p, out, G, ctx_.red, norm_out);
+    else if (norm_out)
+        launch_pdl(k_b2_eval<true>, grid, dim3(32, 8), 0, ctx_.stream, x, prev_.p, out, G, ctx_.red, norm_out);
+    else  // an evaluation without the norm (the reference-facing F) keeps the FP64 differences
+        launch_pdl(k_b2_eval<false>, grid, dim3(32, 8), 0, ctx_.stream, x, prev_.p, out, G, ctx_.red, nullptr);
     ctx_.count_launch();
     ctx_.check_launch("Brusselator2D eval");
 }

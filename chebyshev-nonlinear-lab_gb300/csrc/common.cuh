@@ -369,6 +369,26 @@ __device__ __forceinline__ long long fx_term(const FxParts& f, int E) {
     const unsigned long long t = (f.mag << 4) >> min(E - f.e, 63);
     return f.neg ? -(long long)t : (long long)t;
 }
+// S 2^(E - 1079) rounded to nearest-even as an FP64 value, for |S| < 2^61; false where the result would be
+// subnormal (the caller's rare path).
+__device__ __forceinline__ bool fx_round(long long S, int E, double& out) {
+    if (S == 0) {
+        out = 0.0;
+        return true;
+    }
+    const unsigned long long sign = S < 0 ? (1ull << 63) : 0ull;
+    unsigned long long A = S < 0 ? (unsigned long long)(-S) : (unsigned long long)S;
+    const int lz = __clzll((long long)A);  // >= 3
+    const int eb = E + 7 - lz;             // the biased exponent of A 2^(E - 1079)
+    if (eb <= 0) return false;
+    A <<= lz;                                   // leading one at bit 63
+    unsigned long long mant = A >> 11;          // 53 bits
+    const unsigned rem = (unsigned)(A & 0x7FFu);
+    mant += (rem > 0x400u || (rem == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
+    // the hidden bit adds one to the exponent field; a carry out of the significand adds one more
+    out = __longlong_as_double((long long)(sign | ((((unsigned long long)(eb - 1)) << 52) + mant)));
+    return true;
+}
 // The sum from the seven values' parts (c first); the values themselves for the rare cases.
 __device__ __forceinline__ double lap7_fixed(const FxParts& f0, const FxParts& f1, const FxParts& f2, const FxParts& f3,
                                              const FxParts& f4, const FxParts& f5, const FxParts& f6, double c,
@@ -378,18 +398,24 @@ __device__ __forceinline__ double lap7_fixed(const FxParts& f0, const FxParts& f
     const long long t0 = fx_term(f0, E);
     const long long S = ((t0 << 2) + (t0 << 1)) - fx_term(f1, E) - fx_term(f2, E) - fx_term(f3, E) - fx_term(f4, E) -
                         fx_term(f5, E) - fx_term(f6, E);
-    if (S == 0) return 0.0;
-    const unsigned long long sign = S < 0 ? (1ull << 63) : 0ull;
-    unsigned long long A = S < 0 ? (unsigned long long)(-S) : (unsigned long long)S;
-    const int lz = __clzll((long long)A);  // >= 3
-    const int eb = E + 7 - lz;             // the biased exponent of A 2^(E - 1079)
-    if (eb <= 0) return lap7_fp64_rare(c, a1, a2, a3, a4, a5, a6);  // a subnormal result
-    A <<= lz;                                   // leading one at bit 63
-    unsigned long long mant = A >> 11;          // 53 bits
-    const unsigned rem = (unsigned)(A & 0x7FFu);
-    mant += (rem > 0x400u || (rem == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
-    // the hidden bit adds one to the exponent field; a carry out of the significand adds one more
-    return __longlong_as_double((long long)(sign | ((((unsigned long long)(eb - 1)) << 52) + mant)));
+    double out;
+    if (!fx_round(S, E, out)) return lap7_fp64_rare(c, a1, a2, a3, a4, a5, a6);  // a subnormal result
+    return out;
+}
+
+// (a1 + a2) + (a3 + a4) - 4c, the 5-point sum of a 2D Laplacian, in the same fixed point, rounded once
+// (|sum| < 2^60 of the aligned units); the FP64 form of the differences for the rare cases.
+static __device__ __noinline__ double lap5_fp64_rare(double c, double a1, double a2, double a3, double a4) {
+    return ((a1 - c) + (a2 - c)) + ((a3 - c) + (a4 - c));
+}
+__device__ __forceinline__ double lap5_fixed(double c, double a1, double a2, double a3, double a4) {
+    const FxParts f0 = fx_split(c), f1 = fx_split(a1), f2 = fx_split(a2), f3 = fx_split(a3), f4 = fx_split(a4);
+    const int E = max(max(f0.e, f1.e), max(max(f2.e, f3.e), f4.e));
+    if (E >= 2040) return lap5_fp64_rare(c, a1, a2, a3, a4);
+    const long long S = (fx_term(f1, E) + fx_term(f2, E)) + (fx_term(f3, E) + fx_term(f4, E)) - (fx_term(f0, E) << 2);
+    double out;
+    if (!fx_round(S, E, out)) return lap5_fp64_rare(c, a1, a2, a3, a4);
+    return out;
 }
 __device__ __forceinline__ double lap7_fixed(double c, double a1, double a2, double a3, double a4, double a5,
                                              double a6) {

@@ -292,6 +292,9 @@ public:
     const double* previous() const { return prev_.p; }
     void set_previous(const double* w);
     size_t cache_size() const override { return 0; }
+    // FP32 products announced: the drivers' evaluations (with the norm) form the Laplacians in fixed point
+    // (k_b2_eval FIXED); an evaluation without the norm keeps the FP64 differences
+    void prepare_cache(int precision) override { fixed_sum_ = precision == NUMA_GPU_FP32; }
     void eval(const double* x, double* out, double* cache, double* norm_out) override;
     // FP32 binding: the coefficients (2uv, u^2) of the iterate in FP32; products in FP32 arithmetic
     void bind(const double* x, const double*, int precision) override;
@@ -309,6 +312,7 @@ private:
     DeviceArray<double> prev_, coef32_;
     const double* bound_x_ = nullptr;
     int bound_precision_ = NUMA_GPU_FP64;
+    bool fixed_sum_ = false;
 };
 
 // Periodic geometric multigrid V(pre, post) for the coupled 2x2-block Jacobian of Brusselator2D,
