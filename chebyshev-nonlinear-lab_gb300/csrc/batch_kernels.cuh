@@ -121,13 +121,31 @@ __global__ void __launch_bounds__(BX* BY) k_bprolong(MgPool C, MgPool F, const i
                                   blockIdx.z - q * (nc + 1));
 }
 
-// the levels n <= 15 of every pool grid: one CTA per grid
+// the levels n <= 15 of every pool grid: one CTA per grid.  With tp.c set (Jacobian-aware tail), level m's
+// coefficients of grid q are at tp.c[m] + q n_m^3.
 __global__ void __launch_bounds__(1024) k_btail(MgPool P, const int* __restrict__ act, TailParams tp) {
     pdl_wait();
     pdl_trigger();
     const int q = blockIdx.x;
     if (!pool_active(P, act, q)) return;
+    if (tp.c[0])
+        for (int m = 0; m < tp.levels; ++m) tp.c[m] += (size_t)q * tp.n[m] * tp.n[m] * tp.n[m];
     mg_tail_body<float, true>(P.b + q * P.sb, P.bs + q * P.sb, P.x + q * P.sx, tp);
+}
+
+// The Jacobian coefficient of grids g0 .. of a coarse level: the full-weighting restriction of the
+// finer level's (natural layout, grid q of the source at src + (q - g0) ss), into dst + q sd; zch plane
+// chunks of ichunk coarse planes a grid.  The arithmetic of the single-instance hierarchy's.
+__global__ void __launch_bounds__(BX* BY) k_brestrict_coef(const float* __restrict__ src, long long ss,
+                                                           float* __restrict__ dst, long long sd,
+                                                           const int* __restrict__ inst, const int* __restrict__ act,
+                                                           int g0, int nf, int nc, int ichunk, int zch) {
+    pdl_wait();
+    pdl_trigger();
+    const int gq = blockIdx.z / zch, q = g0 + gq;
+    if (act && !act[inst[q]]) return;
+    restrict_coef_body(src + (long long)gq * ss, dst + (long long)q * sd, nf, nc, ichunk, blockIdx.x, blockIdx.y,
+                       blockIdx.z - gq * zch);
 }
 
 // ------------------------------------------------------------------------------ stencils
@@ -210,12 +228,21 @@ __device__ __forceinline__ float bjvp_point(float below, float cur, float above,
 
 // out = F'(x) v in FP32 arithmetic from an FP32 v (the V-cycle's output) and c32, at the
 // instances with act[t] set: the single-instance FP32 product's arithmetic (two planes a step).
+// eta (may be null): an instance whose forcing term is below tight takes the product to FP32 accuracy
+// (jvp32xf_point: the stencil sum in double-FP32), as the single-instance path's tight linear solves do.
 __global__ void __launch_bounds__(kBX* kBY) k_bjvp32f(const float* __restrict__ c32, const float* __restrict__ v,
-                                                      float* __restrict__ out, const int* __restrict__ act, BClass C) {
+                                                      float* __restrict__ out, const int* __restrict__ act, BClass C,
+                                                      const double* __restrict__ eta, double tight) {
     pdl_wait();
     pdl_trigger();
     const int gq = blockIdx.z / C.zch, bz = blockIdx.z - gq * C.zch;
     if (!act[C.t0 + gq]) return;
+    const bool precise = eta != nullptr && eta[C.t0 + gq] < tight;  // uniform over the block
+    auto point = [precise](float below, float cur, float above, float jm, float jp, float km, float kp, float cc,
+                           float h2inv) {
+        return precise ? jvp32xf_point(below, cur, above, jm, jp, km, kp, cc, h2inv)
+                       : bjvp_point(below, cur, above, jm, jp, km, kp, cc, h2inv);
+    };
     const int n = C.n;
     const int k = blockIdx.x * kBX + threadIdx.x;
     const int j = blockIdx.y * kBY + threadIdx.y;
@@ -242,8 +269,8 @@ __global__ void __launch_bounds__(kBX* kBY) k_bjvp32f(const float* __restrict__ 
         const float jm1 = jlo ? v[q - n] : 0.0f, jp1 = jhi ? v[q + n] : 0.0f;
         const float km1 = klo ? v[q - 1] : 0.0f, kp1 = khi ? v[q + 1] : 0.0f;
         const float c0 = c32[p], c1 = c32[q];
-        out[p] = bjvp_point(below, cur, a1, jm0, jp0, km0, kp0, c0, h2inv);
-        out[q] = bjvp_point(cur, a1, a2, jm1, jp1, km1, kp1, c1, h2inv);
+        out[p] = point(below, cur, a1, jm0, jp0, km0, kp0, c0, h2inv);
+        out[q] = point(cur, a1, a2, jm1, jp1, km1, kp1, c1, h2inv);
         below = a1;
         cur = a2;
     }
@@ -252,7 +279,7 @@ __global__ void __launch_bounds__(kBX* kBY) k_bjvp32f(const float* __restrict__ 
         const float above = (i + 1 < n) ? v[p + plane] : 0.0f;
         const float jm = jlo ? v[p - n] : 0.0f, jp = jhi ? v[p + n] : 0.0f;
         const float km = klo ? v[p - 1] : 0.0f, kp = khi ? v[p + 1] : 0.0f;
-        out[p] = bjvp_point(below, cur, above, jm, jp, km, kp, c32[p], h2inv);
+        out[p] = point(below, cur, above, jm, jp, km, kp, c32[p], h2inv);
     }
 }
 

@@ -355,6 +355,12 @@ struct BatchSolver::Impl {
     };
     std::vector<std::unique_ptr<Pool>> pools;  // sizes n_max ... 15 (the last one is the tail)
     size_t tail_smem = 0;
+    // Jacobian-aware tail (kp.coarse_jacobian): the coefficient c = lambda e^u of each pool grid below the
+    // finest pool (natural layout, grid q at q s^3), and of the tail's levels 7, 3, 1 (grid q of the last pool)
+    bool jac_tail = false;
+    double tight = 0.0;  // forcing terms below this take the accurate product (kp.jvp_tight), else 0
+    std::vector<DeviceArray<float>> cpool;
+    DeviceArray<float> ctail[3];
 
     // packed vectors
     DeviceArray<double> xa, xb, F, z, R;
@@ -402,6 +408,7 @@ struct BatchSolver::Impl {
     void solve(double* x_out, numa_batch_result* res, double* seconds);
     void launch_dots(int cnt_total, const float* w);
     void launch_update(int j);
+    void restrict_coef();
 };
 
 namespace {
@@ -428,6 +435,8 @@ BatchSolver::BatchSolver(Context& ctx, const numa_batch_instance* inst, size_t c
     M.kp = p;
     M.I = (int)count;
     M.m = (int)p.restart;
+    M.jac_tail = p.coarse_jacobian;
+    M.tight = p.jvp_tight ? 1e-5 : 0.0;
     // table order: larger grids first, then the caller's order
     std::vector<int> order(count);
     std::iota(order.begin(), order.end(), 0);
@@ -540,10 +549,18 @@ void BatchSolver::Impl::alloc_state() {
         NUMA_CUDA(cudaMemsetAsync(P->bs.p, 0, P->bs.n * sizeof(float), ctx.stream));
         pools.push_back(std::move(P));
     }
-    // the tail: levels 15, 7, 3, 1 of every instance in one CTA each
+    if (jac_tail) {
+        cpool.resize(pools.size());
+        for (size_t q = 1; q < pools.size(); ++q) cpool[q].resize((size_t)pools[q]->K * pools[q]->N);
+        const int Kt = pools.back()->K;
+        ctail[0].resize((size_t)Kt * 343);
+        ctail[1].resize((size_t)Kt * 27);
+        ctail[2].resize((size_t)Kt);
+    }
+    // the tail: levels 15, 7, 3, 1 of every instance in one CTA each (and, Jacobian-aware, c h^2 of each)
     size_t elems = 0;
     for (int s = 15; s >= 1; s = (s - 1) / 2) {
-        elems += 3 * (size_t)s * s * s;
+        elems += (jac_tail ? 4 : 3) * (size_t)s * s * s;
         if (s == 1) break;
     }
     elems += 15 * 15 * 15;
@@ -746,6 +763,7 @@ void BatchSolver::Impl::vcycle(int j) {
         tp.pre = pre;
         tp.post = post;
         tp.half = make_split(15).half;
+        for (int m2 = 0; m2 < kMaxTail; ++m2) tp.c[m2] = nullptr;
         const MgPool V = P.view();
         for (int a = 0; a < P.K; a += 65535) {
             MgPool W = V;
@@ -753,7 +771,14 @@ void BatchSolver::Impl::vcycle(int j) {
             W.b += (long long)a * V.sb;
             W.bs += (long long)a * V.sb;
             W.inst += a;
-            launch_pdl(k_btail, std::min(65535, P.K - a), 1024, tail_smem, s, W, act, tp);
+            TailParams ta = tp;
+            if (jac_tail) {  // levels 15, 7, 3, 1 of grid a onwards
+                ta.c[0] = cpool[np - 1].p + (size_t)a * 3375;
+                ta.c[1] = ctail[0].p + (size_t)a * 343;
+                ta.c[2] = ctail[1].p + (size_t)a * 27;
+                ta.c[3] = ctail[2].p + (size_t)a;
+            }
+            launch_pdl(k_btail, std::min(65535, P.K - a), 1024, tail_smem, s, W, act, ta);
             ctx.count_launch();
         }
     }
@@ -839,6 +864,45 @@ void BatchSolver::Impl::launch_update(int j) {
     ctx.count_launch();
 }
 
+// The Jacobian coefficient of every pool level below each instance's finest and of the tail levels,
+// restricted from RN32(lambda e^u) of the current iterates (k_beval's c32), for the instances still in
+// Newton: the single-instance Jacobian-aware hierarchy's restriction chain (PoissonMG::set_coarse_coefficient).
+void BatchSolver::Impl::restrict_coef() {
+    cudaStream_t s = ctx.stream;
+    const dim3 blk(BX, BY);
+    const int np = (int)pools.size();
+    auto launch = [&](const float* src, long long ss, float* dst, long long sd, const int* inst, int g0, int count,
+                      int nf, int nc) {
+        const int ichunk = nc >= 64 ? 8 : (nc >= 16 ? 4 : 1);
+        const int zch = (nc + ichunk - 1) / ichunk;
+        over_pool(0, count, zch, [&](int a, int cnt) {
+            const dim3 grid((nc + BX - 1) / BX, (nc + BY - 1) / BY, cnt * zch);
+            launch_pdl(k_brestrict_coef, grid, blk, 0, s, src + (long long)a * ss, ss, dst, sd, inst,
+                       (const int*)S.nl_act, g0 + a, nf, nc, ichunk, zch);
+            ctx.count_launch();
+        });
+    };
+    for (int p = 1; p < np; ++p) {
+        Pool& F = *pools[p - 1];
+        Pool& C = *pools[p];
+        const int nf = F.s, nc = C.s;
+        // grids whose finest level is finer than nf: from the finer pool's coefficients
+        if (p >= 2 && F.top0 > 0)
+            launch(cpool[p - 1].p, F.N, cpool[p].p, C.N, F.inst.p, 0, F.top0, nf, nc);
+        // grids whose finest level is nf: from the class's RN32(lambda e^u)
+        if (F.cls >= 0) {
+            const Cls& c = cls[F.cls];
+            launch(c32.p + c.off0, c.N, cpool[p].p, C.N, F.inst.p, F.top0, c.count, nf, nc);
+        }
+    }
+    // the tail levels 7, 3, 1 from level 15 (every instance)
+    const int Kt = pools.back()->K;
+    launch(cpool[np - 1].p, 3375, ctail[0].p, 343, pools.back()->inst.p, 0, Kt, 15, 7);
+    launch(ctail[0].p, 343, ctail[1].p, 27, pools.back()->inst.p, 0, Kt, 7, 3);
+    launch(ctail[1].p, 27, ctail[2].p, 1, pools.back()->inst.p, 0, Kt, 3, 1);
+    ctx.check_launch("batched coarse coefficients");
+}
+
 // One Arnoldi step j of every instance whose linear solve is active.
 void BatchSolver::Impl::step(int j) {
     cudaStream_t s = ctx.stream;
@@ -847,7 +911,8 @@ void BatchSolver::Impl::step(int j) {
     for (const BClass& c : ccfg) {
         const int count = cls[&c - ccfg.data()].count;
         over_class(c, count, [&](const BClass& cc, dim3 grid) {
-            launch_pdl(k_bjvp32f, grid, dim3(kBX, kBY), 0, s, (const float*)c32.p, zj, W32.p, (const int*)S.lin_act, cc);
+            launch_pdl(k_bjvp32f, grid, dim3(kBX, kBY), 0, s, (const float*)c32.p, zj, W32.p, (const int*)S.lin_act, cc,
+                       tight > 0.0 ? (const double*)S.eta : nullptr, tight);
             ctx.count_launch();
         });
     }
@@ -925,7 +990,7 @@ void BatchSolver::Impl::restart() {
     for (size_t ci = 0; ci < ccfg.size(); ++ci)
         over_class(ccfg[ci], cls[ci].count, [&](const BClass& cc, dim3 grid) {
             launch_pdl(k_bjvp32f, grid, dim3(kBX, kBY), 0, s, (const float*)c32.p, (const float*)S32.p, W32.p,
-                       (const int*)S.rs_act, cc);
+                       (const int*)S.rs_act, cc, tight > 0.0 ? (const double*)S.eta : nullptr, tight);
             ctx.count_launch();
         });
     launch_pdl(k_bsub, nblocks, kEwThreads, 0, s, (const double*)F.p, (const float*)W32.p, R.p, (const int*)S.rs_act, B,
@@ -985,6 +1050,7 @@ void BatchSolver::Impl::solve(double* x_out, numa_batch_result* res, double* sec
         launch_pdl(k_bnl_begin, sb, kScalarThreads, 0, s, S, bp, K, (int)k);
         ctx.count_launch();
         if (!(read_flags() & kFlagNL)) break;
+        if (jac_tail) restrict_coef();  // the coarse levels' Jacobian at the new iterates
         // FGMRES: cycles of up to m steps, restarts while an instance needs one (every cycle adds at
         // least one iteration to each instance it runs, so gmres_max_iters bounds the cycles)
         for (size_t cycle = 0; cycle <= kp.max_iters; ++cycle) {

@@ -327,12 +327,6 @@ __global__ void __launch_bounds__(BX* BY) k_jvp32f(const float* __restrict__ c32
 // h^-2 (an FP32 integer below 2^24, so h^-2 hi is exact with its FMA error); widened to FP64 in one
 // addition; out = T - c v in one FP64 FMA with the FP64 coefficient.  Two FP64 instructions a point
 // (the FP64 product takes ten), and an error of a few 2^-48 of the largest partial sum.
-__device__ __forceinline__ void df_sub(float& hi, float& lo, float x) {
-    float s, e;
-    two_sum(hi, -x, s, e);
-    hi = s;
-    lo = __fadd_rn(lo, e);
-}
 __device__ __forceinline__ double jvp32x_point(float below, float cur, float above, float jm, float jp, float km,
                                                float kp, double c, float h2inv) {
     float hi = __fmul_rn(6.0f, cur);
@@ -347,29 +341,6 @@ __device__ __forceinline__ double jvp32x_point(float below, float cur, float abo
     const float pl = __fmaf_rn(h2inv, lo, __fmaf_rn(h2inv, hi, -ph));
     const double t = __dadd_rn(f32_to_f64(ph), f32_to_f64(pl));
     return __fma_rn(-c, f32_to_f64(cur), t);
-}
-
-// The same product rounded to FP32 (the FP32 Krylov basis' vector), on the FP32 pipe alone: the stencil
-// sum in double-FP32 as above, h^-2 s exactly as ph + pl, c v with the FP32 coefficient RN32(c) as an exact
-// product (two-product), the difference in double-FP32, rounded once.  Against the product with the FP64
-// coefficient this adds |c - RN32(c)| |v| <= 2^-24 |c v|, the size of the final rounding itself.
-__device__ __forceinline__ float jvp32xf_point(float below, float cur, float above, float jm, float jp, float km,
-                                               float kp, float c32, float h2inv) {
-    float hi = __fmul_rn(6.0f, cur);
-    float lo = __fmaf_rn(6.0f, cur, -hi);
-    df_sub(hi, lo, below);
-    df_sub(hi, lo, above);
-    df_sub(hi, lo, jm);
-    df_sub(hi, lo, jp);
-    df_sub(hi, lo, km);
-    df_sub(hi, lo, kp);
-    const float ph = __fmul_rn(h2inv, hi);
-    const float pl = __fmaf_rn(h2inv, lo, __fmaf_rn(h2inv, hi, -ph));
-    const float q = __fmul_rn(c32, cur);
-    const float qe = __fmaf_rn(c32, cur, -q);
-    float s, e;
-    two_sum(ph, -q, s, e);
-    return __fadd_rn(s, __fadd_rn(e, __fsub_rn(pl, qe)));
 }
 
 // FP32 out: the coefficient array is RN32(c) and jvp32xf_point forms the result (no FP64 instruction).

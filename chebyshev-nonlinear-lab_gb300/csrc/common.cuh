@@ -231,6 +231,39 @@ __device__ __forceinline__ DF df_split(double d) {
 }
 __device__ __forceinline__ double df_to_f64(DF a) { return __dadd_rn(f32_to_f64(a.hi), f32_to_f64(a.lo)); }
 
+// hi + lo -= x, the rounding error of the subtraction gathered in lo (two-sum)
+__device__ __forceinline__ void df_sub(float& hi, float& lo, float x) {
+    float s, e;
+    two_sum(hi, -x, s, e);
+    hi = s;
+    lo = __fadd_rn(lo, e);
+}
+
+// The Bratu3D Jacobian product h^-2 (6v - the six neighbours) - c v of FP32 values, to the accuracy of an FP32
+// result, on the FP32 pipe alone: the stencil sum in double-FP32 (6v exact with its FMA error, each neighbour
+// subtracted by two-sum), h^-2 s exactly as ph + pl, c v with the FP32 coefficient RN32(c) as an exact
+// product (two-product), the difference in double-FP32, rounded once.  Against the product with the FP64
+// coefficient this adds |c - RN32(c)| |v| <= 2^-24 |c v|, the size of the final rounding itself.
+__device__ __forceinline__ float jvp32xf_point(float below, float cur, float above, float jm, float jp, float km,
+                                               float kp, float c32, float h2inv) {
+    float hi = __fmul_rn(6.0f, cur);
+    float lo = __fmaf_rn(6.0f, cur, -hi);
+    df_sub(hi, lo, below);
+    df_sub(hi, lo, above);
+    df_sub(hi, lo, jm);
+    df_sub(hi, lo, jp);
+    df_sub(hi, lo, km);
+    df_sub(hi, lo, kp);
+    const float ph = __fmul_rn(h2inv, hi);
+    const float pl = __fmaf_rn(h2inv, lo, __fmaf_rn(h2inv, hi, -ph));
+    const float q = __fmul_rn(c32, cur);
+    const float qe = __fmaf_rn(c32, cur, -q);
+    float s, e;
+    two_sum(ph, -q, s, e);
+    return __fadd_rn(s, __fadd_rn(e, __fsub_rn(pl, qe)));
+}
+
+
 // RN(a / b) from y = RN(1/b), for many a divided by one b (Markstein's correction): q = RN(a y) is
 // within one ulp of a/b, r = a - b q is exact by FMA, and RN(q + r y) is the correctly rounded
 // quotient.  That needs a, q and y well inside the normal range (r ~ 2^-52 a must not underflow):

@@ -388,6 +388,7 @@ KrylovParams params_from_c(const numa_krylov_params* c) {
     p.flexible = c->flexible != 0;
     p.jvp_precision = c->jvp_precision;
     p.jvp_tight = c->jvp_tight != 0;
+    p.coarse_jacobian = c->coarse_jacobian != 0;
     return p;
 }
 

@@ -626,6 +626,53 @@ __global__ void k_scale_in32_split(const RT* __restrict__ r, float* __restrict__
     }
 }
 
+// cc = the full-weighting restriction of a natural-layout coefficient (weights (1/4, 1/2, 1/4) per
+// dimension, summed z outer, y, x inner), FP32 out.  An FP64 input is rounded to FP32 by the integer
+// conversion (the hardware one issues on the FP64 pipe).  A thread owns a coarse (K, J) column and
+// marches I: fine plane 2I+2 of one step is plane 2I of the next, kept in registers, so a coarse point
+// loads 18 fine values, not 27.
+template <class TI>
+__device__ __forceinline__ void restrict_coef_body(const TI* __restrict__ cf, float* __restrict__ cc, int nf, int nc,
+                                                   int ichunk, int bx, int by, int bz) {
+    const int K = bx * BX + threadIdx.x;
+    const int J = by * BY + threadIdx.y;
+    if (K >= nc || J >= nc) return;
+    const int I0 = bz * ichunk;
+    const int I1 = min(I0 + ichunk, nc);
+    const float w[3] = {0.25f, 0.5f, 0.25f};
+    const size_t pf = (size_t)nf * nf;
+    const size_t col = (size_t)(2 * J) * nf + 2 * K;  // fine (2J, 2K) within a plane
+    auto load_plane = [&](int i, float (&v)[9]) {
+        const TI* q = cf + (size_t)i * pf + col;
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) v[b * 3 + c] = f64_to_f32(q[(size_t)b * nf + c]);
+    };
+    float p0[9], p1[9], p2[9];
+    load_plane(2 * I0, p0);
+    for (int I = I0; I < I1; ++I) {
+        load_plane(2 * I + 1, p1);
+        load_plane(2 * I + 2, p2);
+        float acc = 0.0f;
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) acc = __fmaf_rn(w[0] * w[b] * w[c], p0[b * 3 + c], acc);
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) acc = __fmaf_rn(w[1] * w[b] * w[c], p1[b * 3 + c], acc);
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) acc = __fmaf_rn(w[2] * w[b] * w[c], p2[b * 3 + c], acc);
+        cc[((size_t)I * nc + J) * nc + K] = acc;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) p0[q] = p2[q];
+    }
+}
+
 // z (FP64, natural) = x (FP32, split)
 __global__ void k_to64_split(const float* __restrict__ x, double* __restrict__ z, int N, int half) {
     pdl_wait();

@@ -630,6 +630,7 @@ struct KrylovParams {
     int jvp_mode = 0, d2_mode = 0, orth = 0, jvp_precision = 0;
     bool flexible = false;
     bool jvp_tight = false;  // GmresOptions::precise_tight for the Newton and Chebyshev solves
+    bool coarse_jacobian = false;  // batched solver: Jacobian-aware multigrid tail
 };
 
 KrylovParams params_from_c(const numa_krylov_params* p);

@@ -460,53 +460,13 @@ const float* PoissonMG::fine_b32() const { return levels_[0]->b32.p; }
 
 namespace {
 
-// cc = the full-weighting restriction of a natural-layout coefficient (weights (1/4, 1/2, 1/4) per
-// dimension, summed z outer, y, x inner), FP32 out.  An FP64 input is rounded to FP32 by the integer
-// conversion (the hardware one issues on the FP64 pipe).  A thread owns a coarse (K, J) column and
-// marches I: fine plane 2I+2 of one step is plane 2I of the next, kept in registers, so a coarse point
-// loads 18 fine values, not 27.
+// cc = the full-weighting restriction of a natural-layout coefficient (restrict_coef_body, mg_kernels.cuh)
 template <class TI>
 __global__ void __launch_bounds__(BX* BY) k_restrict_coef(const TI* __restrict__ cf, float* __restrict__ cc, int nf,
                                                           int nc, int ichunk) {
     pdl_wait();
     pdl_trigger();
-    const int K = blockIdx.x * BX + threadIdx.x;
-    const int J = blockIdx.y * BY + threadIdx.y;
-    if (K >= nc || J >= nc) return;
-    const int I0 = blockIdx.z * ichunk;
-    const int I1 = min(I0 + ichunk, nc);
-    const float w[3] = {0.25f, 0.5f, 0.25f};
-    const size_t pf = (size_t)nf * nf;
-    const size_t col = (size_t)(2 * J) * nf + 2 * K;  // fine (2J, 2K) within a plane
-    auto load_plane = [&](int i, float (&v)[9]) {
-        const TI* q = cf + (size_t)i * pf + col;
-#pragma unroll
-        for (int b = 0; b < 3; ++b)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) v[b * 3 + c] = f64_to_f32(q[(size_t)b * nf + c]);
-    };
-    float p0[9], p1[9], p2[9];
-    load_plane(2 * I0, p0);
-    for (int I = I0; I < I1; ++I) {
-        load_plane(2 * I + 1, p1);
-        load_plane(2 * I + 2, p2);
-        float acc = 0.0f;
-#pragma unroll
-        for (int b = 0; b < 3; ++b)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) acc = __fmaf_rn(w[0] * w[b] * w[c], p0[b * 3 + c], acc);
-#pragma unroll
-        for (int b = 0; b < 3; ++b)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) acc = __fmaf_rn(w[1] * w[b] * w[c], p1[b * 3 + c], acc);
-#pragma unroll
-        for (int b = 0; b < 3; ++b)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) acc = __fmaf_rn(w[2] * w[b] * w[c], p2[b * 3 + c], acc);
-        cc[((size_t)I * nc + J) * nc + K] = acc;
-#pragma unroll
-        for (int q = 0; q < 9; ++q) p0[q] = p2[q];
-    }
+    restrict_coef_body(cf, cc, nf, nc, ichunk, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 }  // namespace

@@ -41,7 +41,7 @@ class KrylovParams(C.Structure):
         ("gmres_max_iters", C.c_uint64), ("armijo", C.c_double), ("min_lambda", C.c_double),
         ("recycle", C.c_int32), ("jvp_mode", C.c_int32), ("d2_mode", C.c_int32),
         ("orth", C.c_int32), ("flexible", C.c_int32), ("jvp_precision", C.c_int32),
-        ("jvp_tight", C.c_int32), ("reserved", C.c_int32 * 3),
+        ("jvp_tight", C.c_int32), ("coarse_jacobian", C.c_int32), ("reserved", C.c_int32 * 2),
     ]
 
 

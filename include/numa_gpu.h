@@ -124,7 +124,10 @@ typedef struct numa_krylov_params {
                                   (double-FP32 stencil, FP64 coefficient) where the operator offers it
                                   (Bratu3D): rounded once to FP32 into the FP32 Arnoldi basis down to a
                                   tolerance of 1e-6, with an FP64 basis below; 0 = FP32 arithmetic */
-    int32_t reserved[3];
+    int32_t coarse_jacobian;   /* batched solver only (numa_gpu_bsolver_*): 1 = its FP32 multigrid's levels
+                                  n <= 15 solve with the Jacobian -Lap_h - lambda e^u of each iterate, as
+                                  numa_gpu_provider_create_jacobian_mg does for one instance; 0 = Poisson */
+    int32_t reserved[2];
 } numa_krylov_params;
 
 /* KrylovResult (krylov_newton.hpp:40-49) without x (the solution is written into the caller's

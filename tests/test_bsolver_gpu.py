@@ -36,13 +36,14 @@ def _sample_idx(N: int, target: int) -> np.ndarray:
     return np.arange(stride // 2, N, stride, dtype=np.int64)
 
 
-def test_bsolver_config_matches_reference(gpu):
+@pytest.mark.parametrize("jac", [0, 1])
+def test_bsolver_config_matches_reference(gpu, jac):
     G = _G()
     fx = json.loads((GOLDEN / "reference_batch.json").read_text())
     vec = np.load(GOLDEN / "reference_batch.npz")
     inst = G.batch_config_instances(128, seed=42)
     assert [(e["n"], e["lam"]) for e in fx["instances"]] == inst
-    bs = G.BatchSolver(gpu, inst, _mixed(G))
+    bs = G.BatchSolver(gpu, inst, _mixed(G, jvp_tight=jac, coarse_jacobian=jac))
     try:
         res, secs, xs = bs.solve(want_x=True)
     finally:
@@ -79,6 +80,38 @@ def test_bsolver_matches_single_instance_mixed_path(gpu):
         assert (r["iters"], r["n_F"]) == (rs["iters"], rs["n_F"]), (n, lam, r, rs)
         assert abs(int(r["n_lin_iters"]) - int(rs["n_lin_iters"])) <= 2, (n, lam, r, rs)
         assert rel_err(xb, x.numpy()) < 1e-10, (n, lam)
+
+
+def test_bsolver_jacobian_tail_and_tight_products(gpu):
+    """The benchmark's form of the batched solver: the multigrid tail (levels n <= 15) solving with the
+    Jacobian of each iterate (coarse_jacobian) and products of FP32 accuracy in the linear solves with
+    forcing terms below 1e-5 (jvp_tight).  Against each instance solved alone by the single-instance path
+    with the same settings (the Jacobian-aware provider): the same Newton count and n_F, linear
+    iterations within 2, solutions within 1e-10; and fewer Newton steps and linear iterations in total
+    than the batched solver with the Poisson tail and FP32 products (the batched configuration's mix)."""
+    G = _G()
+    inst = [(63, 6.2), (31, 1.5), (127, 4.0), (31, 6.4), (63, 2.5), (127, 6.0), (31, 3.0)]
+    p = _mixed(G, jvp_tight=1, coarse_jacobian=1)
+    bs = G.BatchSolver(gpu, inst, p)
+    try:
+        res, _, xs = bs.solve(want_x=True)
+    finally:
+        bs.close()
+    for (n, lam), r, xb in zip(inst, res, xs):
+        op = G.Bratu3D(gpu, n, lam)
+        x = gpu.vec(n ** 3).fill(0.0)
+        rs = G.newton_krylov(op, x, _mixed(G, jvp_tight=1), G.Provider.jacobian_mg(gpu, n))
+        assert r["converged"] == rs["converged"] == 1 and r["res_rel"] <= 1e-10
+        assert (r["iters"], r["n_F"]) == (rs["iters"], rs["n_F"]), (n, lam, r, rs)
+        assert abs(int(r["n_lin_iters"]) - int(rs["n_lin_iters"])) <= 2, (n, lam, r, rs)
+        assert rel_err(xb, x.numpy()) < 1e-10, (n, lam)
+    bp = G.BatchSolver(gpu, inst, _mixed(G))
+    try:
+        rp, _, _ = bp.solve()
+    finally:
+        bp.close()
+    assert sum(r["iters"] for r in res) < sum(r["iters"] for r in rp)
+    assert sum(r["n_lin_iters"] for r in res) < sum(r["n_lin_iters"] for r in rp)
 
 
 def test_bsolver_restarted_cycles(gpu):
