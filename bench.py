@@ -352,6 +352,14 @@ def params_for(G, path: str, orth: str = "cgs1"):
     return p
 
 
+def batch_params(G):
+    """The batched leg's settings: the headline's mixed path (accurate products below forcing 1e-5) with the
+    batched solver's multigrid tail solving with the Jacobian, as the headline's provider does."""
+    p = params_for(G, "mixed", "cgs1")
+    p.coarse_jacobian = 1
+    return p
+
+
 def timed_solves(G, ctx, op, pc, x, u0, method, params, steps, warmup, dist: Dist, stream):
     import torch
     for _ in range(warmup):
@@ -484,9 +492,7 @@ def run_ours(args) -> int:
     # batched solves: 128 instances, n from {31, 63, 127}, lambda ~ U[1, 6.5] (seeded), mixed path
     batched = None
     if not args.no_batch and dist.rank == 0:
-        pbat = params_for(G, "mixed", "cgs1")
-        pbat.coarse_jacobian = 1  # the batched solver's tail with the Jacobian, as the headline's provider
-        batched = batched_leg(G, ctx, stream, torch, dev, pbat)
+        batched = batched_leg(G, ctx, stream, torch, dev, batch_params(G))
 
     # 2D Brusselator: 2048^2 periodic, 2 species, 20 implicit-Euler steps, NK + FGMRES(40) with the
     # FP32 coupled-block multigrid (FP64 outer), beside the all-FP64 form
@@ -905,7 +911,7 @@ def run_kernel_case(G, ctx, args) -> int:
     if args.kernel_case == "batch":
         # the batched configuration through the batched solver: one warm batch, then args.steps batches
         inst = G.batch_config_instances(128, seed=42)
-        bs = G.BatchSolver(ctx, inst, params_for(G, "mixed_fp32", "cgs1"))
+        bs = G.BatchSolver(ctx, inst, batch_params(G))
         bs.solve()
         t = 0.0
         for _ in range(max(1, args.steps)):
