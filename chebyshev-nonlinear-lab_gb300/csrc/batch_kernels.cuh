@@ -97,16 +97,17 @@ __global__ void __launch_bounds__(BX* BY) k_bresidual(MgPool P, const int* __res
                         blockIdx.z - q * zch);
 }
 
-// fine pool grid q -> coarse pool grid q (the same instance), nc planes per grid
+// fine pool grid q -> coarse pool grid q (the same instance), (nc + 1) / 2 plane pairs per grid
 template <bool FIRST_X>
 __global__ void __launch_bounds__(BX* BY) k_brestrict(MgPool F, MgPool C, const int* __restrict__ act, int nf, int nc,
                                                       int halfc, float inv_c) {
     pdl_wait();
     pdl_trigger();
-    const int q = blockIdx.z / nc;
+    const int zc = (nc + 1) / 2;  // two coarse planes a thread
+    const int q = blockIdx.z / zc;
     if (!pool_active(F, act, q)) return;
     restrict_split_body<FIRST_X>(F.r + q * F.sr, C.b + q * C.sb, C.bs + q * C.sb, C.x + q * C.sx, nf, nc, halfc, inv_c,
-                                 blockIdx.x, blockIdx.y, blockIdx.z - q * nc);
+                                 blockIdx.x, blockIdx.y, blockIdx.z - q * zc);
 }
 
 // coarse pool grid q -> fine pool grid q, nc + 1 cell planes per grid

@@ -730,7 +730,8 @@ void BatchSolver::Impl::vcycle(int j) {
         const Split gc = make_split(nc);
         const bool fused = (p + 2 < np);  // the tail level's first pass is its own
         const MgPool CV = C.view();
-        over_pool(0, P.K, nc, [&](int a, int cnt) {
+        const int zc = (nc + 1) / 2;  // two coarse planes a thread
+        over_pool(0, P.K, zc, [&](int a, int cnt) {
             MgPool Fw = V, Cw = CV;
             Fw.r += (long long)a * V.sr;
             Fw.inst += a;
@@ -738,7 +739,7 @@ void BatchSolver::Impl::vcycle(int j) {
             Cw.b += (long long)a * CV.sb;
             Cw.bs += (long long)a * CV.sb;
             Cw.inst += a;
-            const dim3 rg((nc + BX - 1) / BX, (nc + BY - 1) / BY, cnt * nc);
+            const dim3 rg((nc + BX - 1) / BX, (nc + BY - 1) / BY, cnt * zc);
             const float invc = (float)(1.0 / (((double)nc + 1.0) * ((double)nc + 1.0)));
             if (fused) launch_pdl(k_brestrict<true>, rg, blk, 0, s, Fw, Cw, act, n, nc, gc.half, invc);
             else launch_pdl(k_brestrict<false>, rg, blk, 0, s, Fw, Cw, act, n, nc, gc.half, invc);

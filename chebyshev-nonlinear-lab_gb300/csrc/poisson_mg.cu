@@ -352,10 +352,11 @@ void PoissonMG::cycle32(size_t l) {
     }
     const Split gc = make_split(nc);
     const dim3 rg((nc + BX - 1) / BX, (nc + BY - 1) / BY, nc);
+    const dim3 rg2((nc + BX - 1) / BX, (nc + BY - 1) / BY, (nc + 1) / 2);  // two coarse planes a thread
     if (csplit && first_fused32(l + 1))
-        launch_pdl(k_restrict_split<true>, rg, blk, 0, s, r, C.b32.p, C.bs32.p, C.xs, n, nc, gc.half, (float)C.inv);
+        launch_pdl(k_restrict_split<true>, rg2, blk, 0, s, r, C.b32.p, C.bs32.p, C.xs, n, nc, gc.half, (float)C.inv);
     else if (csplit)
-        launch_pdl(k_restrict_split<false>, rg, blk, 0, s, r, C.b32.p, C.bs32.p, C.xs, n, nc, gc.half, (float)C.inv);
+        launch_pdl(k_restrict_split<false>, rg2, blk, 0, s, r, C.b32.p, C.bs32.p, C.xs, n, nc, gc.half, (float)C.inv);
     else
         launch_pdl(k_restrict<float>, rg, blk, 0, s, r, C.b32.p, C.bs32.p, n, nc, C.inv);
     ctx_.count_launch();
