@@ -164,13 +164,30 @@ struct BClass {
 // F = h^-2 (6 u - sum) - lambda e^u at the instances with eval[t] set, from x_a or x_b (the one
 // selected by cur[t] ^ which), with RN32(lambda e^u) into c32, RN32(F) into f32 (the first FP32
 // Krylov vector of the next linear solve) and the block's sum of F^2 into partials: the arithmetic
-// of the single-instance residual kernel (its fixed-point 7-point sum), with lambda e^u as lambda times
-// e^u (the single-instance operator scales its exp table by its one lambda instead).
+// of the single-instance residual kernel (its fixed-point 7-point sum, lambda e^u from a lambda-scaled
+// exp table per instance).
+// The exp table scaled by each instance's lambda (the single-instance operator's k_lam_table, one table of
+// 2^kExpTableBits entries an instance, blockIdx.y = instance - t0): T2 = (RN(lambda T_hi), lambda T_hi -
+// RN(lambda T_hi) + lambda T_lo), TF their RN32.  Instances with lambda outside [2^-10, 2^10] keep no table.
+__global__ void k_blam_tables(const double* __restrict__ lam, double2* __restrict__ T2, float2* __restrict__ TF,
+                              int t0) {
+    const int t = t0 + blockIdx.y;
+    const int jj = blockIdx.x * blockDim.x + threadIdx.x;
+    if (jj >= (1 << kExpTableBits)) return;
+    const double l = lam[t];
+    const double2 T = kExp2Frac[jj];
+    const double hi = __dmul_rn(l, T.x);
+    const double lo = __dadd_rn(__fma_rn(l, T.x, -hi), __dmul_rn(l, T.y));
+    T2[(size_t)t * (1 << kExpTableBits) + jj] = make_double2(hi, lo);
+    TF[(size_t)t * (1 << kExpTableBits) + jj] = make_float2(__double2float_rn(hi), __double2float_rn(lo));
+}
+
 __global__ void __launch_bounds__(kBX* kBY) k_beval(const double* __restrict__ xa, const double* __restrict__ xb,
                                                     const int* __restrict__ cur, int which,
                                                     const int* __restrict__ eval, const double* __restrict__ lam,
                                                     BClass C, double* __restrict__ F, float* __restrict__ c32,
-                                                    float* __restrict__ f32, double* __restrict__ partials) {
+                                                    float* __restrict__ f32, double* __restrict__ partials,
+                                                    const double2* __restrict__ lt2, const float2* __restrict__ ltf) {
     pdl_wait();
     pdl_trigger();
     const int gq = blockIdx.z / C.zch, bz = blockIdx.z - gq * C.zch;
@@ -180,6 +197,11 @@ __global__ void __launch_bounds__(kBX* kBY) k_beval(const double* __restrict__ x
     const long long base = C.off0 + (long long)gq * C.N;
     const double* u = ((cur[t] ^ which) ? xb : xa) + base;
     const double lm = lam[t], h2inv = C.h2inv;
+    // lambda e^u from the instance's lambda-scaled table (one FP64 multiply fewer), as the single-instance
+    // operator does for lambda in [2^-10, 2^10]
+    const bool lt_on = lm >= 0x1p-10 && lm <= 0x1p10;
+    const double2* T2 = lt2 + (size_t)t * (1 << kExpTableBits);
+    const float2* TF = ltf + (size_t)t * (1 << kExpTableBits);
     const int k = blockIdx.x * kBX + threadIdx.x;
     const int j = blockIdx.y * kBY + threadIdx.y;
     const int i0 = bz * C.ichunk;
@@ -198,7 +220,7 @@ __global__ void __launch_bounds__(kBX* kBY) k_beval(const double* __restrict__ x
             const double kp = (k + 1 < n) ? u[p + 1] : 0.0;
             // as the single-instance mixed evaluation: the 7-point sum in 64-bit fixed point, rounded once
             const double s = lap7_fixed(curv, below, above, jm, jp, km, kp);
-            const double e = lm * exp_tang(curv);
+            const double e = lt_on ? lam_exp_tang(curv, lm, T2, TF) : lm * exp_tang(curv);
             const double f = __fma_rn(h2inv, s, -e);
             F[base + p] = f;
             c32[base + p] = f64_to_f32(e);

@@ -364,6 +364,9 @@ struct BatchSolver::Impl {
 
     // packed vectors
     DeviceArray<double> xa, xb, F, z, R;
+    // the exp table scaled by each instance's lambda (k_blam_tables)
+    DeviceArray<double2> lt2;
+    DeviceArray<float2> ltf;
     DeviceArray<float> c32, V32, Z32, W32, S32;
     // per-instance state
     DeviceArray<int> ibuf;
@@ -514,6 +517,14 @@ void BatchSolver::Impl::alloc_state() {
     S.m = m;
     lam_d.resize(I);
     NUMA_CUDA(cudaMemcpyAsync(lam_d.p, lam_of.data(), I * sizeof(double), cudaMemcpyHostToDevice, ctx.stream));
+    lt2.resize((size_t)I << kExpTableBits);
+    ltf.resize((size_t)I << kExpTableBits);
+    for (int t0 = 0; t0 < I; t0 += 65535) {
+        k_blam_tables<<<dim3((1 << kExpTableBits) / 256, std::min(65535, I - t0)), 256, 0, ctx.stream>>>(lam_d.p, lt2.p,
+                                                                                                      ltf.p, t0);
+        ctx.count_launch();
+    }
+    ctx.check_launch("batched lambda tables");
     bp = BParams{kp.rtol_nl, kp.eta_init, kp.eta_max, kp.gamma, kp.alpha, kp.armijo, kp.min_lambda,
                  (int)std::min<size_t>(kp.max_iters, (size_t)1 << 30)};
     {
@@ -932,7 +943,8 @@ void BatchSolver::Impl::eval_all(int which) {
         const BClass& c = ccfg[ci];
         over_class(c, cls[ci].count, [&](const BClass& cc, dim3 grid) {
             launch_pdl(k_beval, grid, dim3(kBX, kBY), 0, s, (const double*)xa.p, (const double*)xb.p, (const int*)S.cur,
-                       which, (const int*)S.eval, (const double*)lam_d.p, cc, F.p, c32.p, V32.p, partials.p);
+                       which, (const int*)S.eval, (const double*)lam_d.p, cc, F.p, c32.p, V32.p, partials.p,
+                       (const double2*)lt2.p, (const float2*)ltf.p);
             ctx.count_launch();
         });
     }

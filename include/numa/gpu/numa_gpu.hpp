@@ -203,6 +203,14 @@ public:
         check(numa_gpu_provider_create_poisson_mg(ctx.get(), n, 2, 2, precision, &h), ctx.get(), "PoissonMGProvider");
         return Provider(ctx, h);
     }
+    // Extension: the FP32 V-cycle whose levels n <= 15 solve with the Jacobian -Lap_h - lambda e^u of the
+    // iterate it is made at (numa_gpu_provider_create_jacobian_mg; with flexible = 1, jvp_precision = FP32
+    // and jvp_tight = 1 in the parameters, the benchmark's mixed path).
+    static Provider jacobian_mg(const Context& ctx, std::size_t n) {
+        numa_gpu_provider* h = nullptr;
+        check(numa_gpu_provider_create_jacobian_mg(ctx.get(), n, 2, 2, &h), ctx.get(), "JacobianMGProvider");
+        return Provider(ctx, h);
+    }
     static Provider jacobi(const Bratu3D& f) {
         numa_gpu_provider* h = nullptr;
         check(numa_gpu_provider_create_jacobi(f.get(), &h), f.context().get(), "BratuJacobi");

@@ -65,3 +65,6 @@ def test_native_driver_program(lib_path, tmp_path, ref_counts):
     assert [int(v) for v in nk[1:5]] == [ref["nk"]["iters"], ref["nk"]["n_F"], ref["nk"]["n_JVP"], ref["nk"]["n_prec"]]
     assert [int(v) for v in ch[1:6]] == [ref["cheb"]["iters"], ref["cheb"]["n_F"], ref["cheb"]["n_JVP"],
                                          ref["cheb"]["n_D2"], ref["cheb"]["n_prec"]]
+    mx = out.stdout.split("\n")[2].split()
+    assert mx[0] == "mixed" and int(mx[3]) == 1 and abs(int(mx[1]) - ref["nk"]["iters"]) <= 1
+    assert float(mx[4]) < 1e-8
