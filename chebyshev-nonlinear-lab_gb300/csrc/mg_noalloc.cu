@@ -10,11 +10,13 @@
 // 4.8 MB (NUMA_GPU_NOALLOC_MAX_DOUBLES doubles), enough for grids up to 63^3.  Each GPU that
 // loads this library holds that array until the process exits.
 //
-// Set-up: the first call on a device, with that device current, resolves the array's device
-// address with cudaGetSymbolAddress (that may load the module) and keeps it for that device;
-// make that first call before any stream capture.  Later calls only launch kernels.  The kept
-// address belongs to the device's primary context: after cudaDeviceReset, or with another
-// context made current on the device, it is stale, and this entry point must not be used there.
+// Set-up: each call that is not being captured into a CUDA graph resolves the array's device
+// address with cudaGetSymbolAddress (the first one on a device may load the module) and keeps
+// it for that device; a call under stream capture launches with the kept address and makes no
+// other runtime call that capture forbids.  So make one uncaptured call on the device, in the
+// context the graph will run in, before capturing; after cudaDeviceReset or a change of
+// context, the next uncaptured call finds the new address (graphs captured before keep the old
+// one and must be captured again).
 //
 // Sharing: every call uses the same array and leaves its contents behind.  The V-cycle writes
 // every value before it reads it, except the level iterates when pre = 0, which are cleared
@@ -142,10 +144,18 @@ extern "C" int numa_gpu_mg_apply_noalloc(size_t n, int pre, int post, const doub
     }
     if (dev < 0 || dev >= kMaxDevices) return NUMA_GPU_ERR_NOT_SUPPORTED;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // Outside stream capture the array's address is looked up on every call, so a call after
+    // cudaDeviceReset or under another context of the device finds the current one; a call
+    // being captured uses the address its device's last uncaptured call found.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        return NUMA_GPU_ERR_CUDA;
+    }
     double* base = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_mu);
-        if (!g_scratch[dev]) {
+        if (!g_scratch[dev] || cap == cudaStreamCaptureStatusNone) {
             void* p = nullptr;
             const cudaError_t e = cudaGetSymbolAddress(&p, g_mg_scratch);
             if (e != cudaSuccess || p == nullptr) {

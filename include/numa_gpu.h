@@ -564,10 +564,13 @@ int numa_gpu_bsolver_autotune(numa_gpu_bsolver* s, const int* planes, int np, co
  * library until the process exits).  r and z are distinct device arrays of n^3 doubles on the
  * current device; the work is enqueued on `stream` (a cudaStream_t, NULL for the default stream)
  * and the call returns without waiting.  It calls no cudaMalloc, cudaFree or allocating library
- * routine.  The first call on each device, with that device current, resolves the array's
- * address with cudaGetSymbolAddress and keeps it: make it before any stream capture.  The kept
- * address belongs to the device's primary context; after cudaDeviceReset, or with another
- * context current on the device, do not call this entry point.  Every call shares the array,
+ * routine.  Every call not under stream capture resolves the array's address with
+ * cudaGetSymbolAddress (the first on a device may load the module) and keeps it for the device; a
+ * call being captured into a CUDA graph uses the kept address and makes no call that capture
+ * forbids.  So make one uncaptured call, in the context the graph will run in, before capturing;
+ * graphs captured before a cudaDeviceReset or a change of context must be captured again.  The
+ * iterates of the levels are cleared with cudaMemsetAsync when pre = 0 (a memset node in a
+ * captured graph).  Every call shares the array,
  * so calls that may run concurrently on the GPU race: order them on one stream.  Returns
  * NUMA_GPU_ERR_TOO_LARGE when the hierarchy of n does not fit the array, and NUMA_GPU_ERR_CUDA,
  * leaving the error pending, when a CUDA error was already pending on entry. */

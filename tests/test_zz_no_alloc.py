@@ -68,3 +68,36 @@ def test_noalloc_rejects_what_does_not_fit(gpu):
     assert G.mg_apply_noalloc(0, v, gpu.vec(27)) == INVALID
     assert G.mg_apply_noalloc(3, v, v) == INVALID  # r and z must differ
     assert G.mg_apply_noalloc(3, v, gpu.vec(27), pre=-1) == INVALID
+
+
+@pytest.mark.parametrize("n,pre,post", [(31, 2, 2), (15, 0, 2)])
+def test_noalloc_captured_in_a_graph(gpu, n, pre, post):
+    """One uncaptured call, then one call captured into a CUDA graph on a side stream (global
+    capture mode, which fails the capture on any forbidden runtime call); two replays of the graph
+    on fresh right-hand sides give the V-cycle bit for bit, the pre = 0 case through the memset node."""
+    import torch
+    G = _G()
+    N = n ** 3
+    mg = G.PoissonMG(gpu, n, pre, post)
+    rng = np.random.default_rng(100 + n)
+    r = torch.zeros(N, dtype=torch.float64, device="cuda")
+    z = torch.full((N,), -3.0, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    lib = G.load()
+    assert lib.numa_gpu_mg_apply_noalloc(n, pre, post, r.data_ptr(), z.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    with torch.cuda.graph(graph, stream=side, capture_error_mode="global"):
+        rc = lib.numa_gpu_mg_apply_noalloc(n, pre, post, r.data_ptr(), z.data_ptr(), side.cuda_stream)
+    assert rc == 0
+    for rep in range(2):
+        rh = rng.uniform(-1.0, 1.0, N)
+        r.copy_(torch.from_numpy(rh))
+        z.fill_(5.0)
+        graph.replay()
+        torch.cuda.synchronize()
+        dr, z_ref = gpu.from_numpy(rh), gpu.vec(N)
+        mg(dr, z_ref)
+        gpu.sync()
+        assert np.array_equal(z.cpu().numpy(), z_ref.numpy()), (n, pre, rep)
