@@ -313,6 +313,15 @@ def _f64(a) -> np.ndarray:
 _live_contexts: "weakref.WeakSet" = weakref.WeakSet()  # contexts and batch executors
 
 
+def _ctx_open(ctx) -> bool:
+    """Whether a child object may still call its C destroy function.  Objects close before their context
+    (Context.close closes them first), except when the context and its children become garbage together:
+    the collector clears the context's weak references to them before it runs any finalizer, in no fixed
+    order, so a child can be finalised after the context's C handle is gone.  Its C handle then points at
+    a destroyed context and is dropped without a call (its device memory is released with the process)."""
+    return bool(getattr(ctx, "h", None))
+
+
 @atexit.register
 def _close_live_contexts():
     for ctx in list(_live_contexts):
@@ -413,7 +422,8 @@ class Vec:
 
     def close(self):
         if self.owned and self.h:
-            self.lib.numa_gpu_vec_destroy(self.h)
+            if _ctx_open(self.ctx):
+                self.lib.numa_gpu_vec_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -472,9 +482,9 @@ class Bratu3D:
         self.ctx._adopt(self)
 
     def close(self):
-        if self.h:
+        if self.h and _ctx_open(self.ctx):
             self.lib.numa_gpu_bratu3d_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -524,9 +534,9 @@ class Burgers2D:
         self.ctx._adopt(self)
 
     def close(self):
-        if self.h:
+        if self.h and _ctx_open(self.ctx):
             self.lib.numa_gpu_burgers2d_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -560,9 +570,9 @@ class _Handle:
     _destroy = ""
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and _ctx_open(getattr(self, "ctx", None)):
             getattr(self.lib, self._destroy)(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -703,9 +713,9 @@ class HelmholtzMG2D:
         self.ctx._adopt(self)
 
     def close(self):
-        if self.h:
+        if self.h and _ctx_open(self.ctx):
             self.lib.numa_gpu_hmg2d_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -733,9 +743,9 @@ class LearnedNet:
         self.ctx._adopt(self)
 
     def close(self):
-        if self.h:
+        if self.h and _ctx_open(self.ctx):
             self.lib.numa_gpu_learned_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -798,9 +808,9 @@ class PoissonMG:
         self.ctx._adopt(self)
 
     def close(self):
-        if self.h:
+        if self.h and _ctx_open(self.ctx):
             self.lib.numa_gpu_mg_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -914,9 +924,9 @@ class Provider:
         return cls.identity(ctx)
 
     def close(self):
-        if self.h:
+        if self.h and _ctx_open(self.ctx):
             self.lib.numa_gpu_provider_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -943,9 +953,9 @@ class KrylovSpace:
         self.ctx._adopt(self)
 
     def close(self):
-        if self.h:
+        if self.h and _ctx_open(self.ctx):
             self.lib.numa_gpu_krylov_space_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -1268,9 +1278,9 @@ class BatchSolver:
         ctx._adopt(self)
 
     def close(self):
-        if self.h:
+        if self.h and _ctx_open(self.ctx):
             self.lib.numa_gpu_bsolver_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:

@@ -99,3 +99,38 @@ def test_missing_library_is_an_import_error(tmp_path):
     import numa_gpu
     with pytest.raises(ImportError):
         numa_gpu.load(tmp_path / "nope.so")
+
+
+def test_child_finalised_after_its_context_makes_no_c_call(lib_path):
+    """Objects close before their context, except when the context and its children become garbage
+    together: the collector clears the context's weak references to its children before it runs any
+    finaliser, so a child can be finalised after the context's C handle is destroyed.  Such a child
+    must drop its handle without calling its C destroy function (which would read the destroyed
+    context); with the context open it calls it once."""
+    import numa_gpu
+
+    calls = []
+
+    class RecordingLib:
+        def __getattr__(self, name):
+            return lambda *args: calls.append(name) or 0
+
+    class FakeContext:
+        def __init__(self, h):
+            self.h = h
+
+    kinds = [(numa_gpu.Vec, {"owned": True}), (numa_gpu.Bratu3D, {}), (numa_gpu.Burgers2D, {}),
+             (numa_gpu.Brusselator2D, {}), (numa_gpu.HelmholtzMG2D, {}),
+             (numa_gpu.LearnedNet, {}), (numa_gpu.PoissonMG, {}), (numa_gpu.Provider, {}),
+             (numa_gpu.KrylovSpace, {}), (numa_gpu.BatchSolver, {})]
+    for ctx_open in (False, True):
+        calls.clear()
+        for cls, extra in kinds:
+            obj = object.__new__(cls)
+            obj.__dict__.update(h=C.c_void_p(1), ctx=FakeContext(C.c_void_p(1) if ctx_open else None),
+                                lib=RecordingLib(), **extra)
+            obj.close()
+            assert obj.h is None, cls.__name__
+            obj.close()  # a second close (the finaliser's) does nothing
+        assert len(calls) == (len(kinds) if ctx_open else 0), calls
+        assert all(c.endswith("_destroy") for c in calls)

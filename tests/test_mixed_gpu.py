@@ -13,6 +13,7 @@ from oracle.oracle_lib import make_point
 pytestmark = pytest.mark.gpu
 
 F = np.float32
+NOT_SUPPORTED = 8  # NUMA_GPU_ERR_NOT_SUPPORTED
 
 
 def _G():
@@ -320,3 +321,40 @@ def test_jacobian_aware_coarse_levels_save_iterations(gpu, lam):
     assert rel_err(xj.numpy(), x64.numpy()) < 1e-8
     assert rj["iters"] <= rp["iters"]
     assert rj["n_lin_iters"] < rp["n_lin_iters"], (rj, rp)
+
+
+@pytest.mark.parametrize("n,lam,start", [(2, 6.0, "zero"), (7, 6.0, "zero"), (16, 6.0, "zero"), (33, 9.0, "zero"),
+                                         (31, 6.0, "profile"), (31, 0.0, "zero")])
+def test_benchmark_mixed_path_sizes_lambdas_starts(gpu, n, lam, start):
+    """The benchmark's mixed path (FGMRES(30) with one-pass classical Gram-Schmidt, the FP32 V-cycle with
+    Jacobian-aware coarse levels, FP32 products and, in the tight linear solves, products of FP64
+    accuracy) away from the benchmark's grid: a hierarchy of one level (n = 2, 16), an odd chain ending
+    in 1 (7, 31), an even coarsest level (33 -> 16), near the fold (lambda = 9), a nonzero start, and
+    lambda = 0 from u0 = 0, where F(u0) = 0 and both paths stop before a step.  Grids without an odd
+    chain down to n <= 15 have no Jacobian-aware levels (NOT_SUPPORTED) and take the FP32 Poisson
+    V-cycle.  It reaches the FP64 drop-in's solution to 1e-8."""
+    G = _G()
+    N = n ** 3
+    op = G.Bratu3D(gpu, n, lam)
+    pm = G.default_params(rtol_nl=1e-10, gmres_restart=30, flexible=1, jvp_precision=G.FP32, orth=G.CGS1,
+                          jvp_tight=1)
+    x64, xm = gpu.vec(N), gpu.vec(N)
+    if start == "profile":
+        i, j, k = np.indices((n, n, n)) + 1.0
+        u0 = (0.3 * np.sin(np.pi * i / (n + 1)) * np.sin(np.pi * j / (n + 1)) * np.sin(np.pi * k / (n + 1))).ravel()
+        x64.copy_from(gpu.from_numpy(u0))
+        xm.copy_from(gpu.from_numpy(u0))
+    try:
+        pc = G.Provider.jacobian_mg(gpu, n)
+    except G.NumaGPUError as e:  # no odd chain of levels down to n <= 15: the FP32 Poisson V-cycle instead
+        assert e.code == NOT_SUPPORTED and n in (2, 16, 33), (n, str(e))
+        pc = G.Provider.poisson_mg(gpu, n, precision=G.FP32)
+    r64 = G.newton_krylov(op, x64, G.default_params(rtol_nl=1e-10, gmres_restart=30), G.Provider.poisson_mg(gpu, n))
+    rm = G.newton_krylov(op, xm, pm, pc)
+    assert r64["converged"] and rm["converged"], (r64, rm)
+    if lam == 0.0:
+        assert rm["iters"] == 0 and r64["iters"] == 0
+        assert not xm.numpy().any() and not x64.numpy().any()
+        return
+    assert rm["res"] <= 1e-10 * rm["res0"]
+    assert rel_err(xm.numpy(), x64.numpy()) < 1e-8, (rel_err(xm.numpy(), x64.numpy()), r64, rm)
