@@ -42,6 +42,8 @@ inline void check(int status, numa_gpu_ctx* ctx, const char* where) {
     throw Error(status, msg);
 }
 
+// One device and its stream.  Objects made on a context must be destroyed before it (declare the
+// Context first: locals and members are destroyed in the reverse order).
 class Context {
 public:
     explicit Context(int device = 0) { check(numa_gpu_ctx_create(device, &h_), nullptr, "numa_gpu_ctx_create"); }

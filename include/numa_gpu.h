@@ -183,6 +183,8 @@ const char* numa_gpu_status_string(int status);
 void numa_krylov_params_default(numa_krylov_params* p);  /* KrylovParams{} defaults */
 
 int numa_gpu_ctx_create(int device, numa_gpu_ctx** out);
+/* Destroy every object created on a context (vectors, operators, hierarchies, providers, Krylov
+ * spaces, solvers) before the context: their destroy functions use the context's stream. */
 int numa_gpu_ctx_destroy(numa_gpu_ctx* ctx);
 int numa_gpu_ctx_synchronize(numa_gpu_ctx* ctx);
 /* Message of the last failing call on this context ("" if none). */
