@@ -10,9 +10,9 @@ HBM.  Inputs are synthetic and deterministic (u0 = 0).
 
 Paths.  mixed (the headline, default): flexible GMRES(30) whose cycles run to 30 steps, classical
 Gram-Schmidt (one pass by default, --orth cgs2 for two) on lazily normalised basis vectors (an
-FP32 basis in double-FP32 arithmetic while the forcing term is >= 1e-5), FP32 V-cycle and FP32
-Jacobian products; FP64 residual, Newton update, Arnoldi coefficients and Hessenberg least
-squares.  fp64 (the drop-in): the reference's right-preconditioned GMRES(30) with modified
+FP32 basis in double-FP32 arithmetic while the forcing term is >= 1e-6), FP32 V-cycle, FP32
+Jacobian products while the forcing term is >= 1e-5 and products of FP64 accuracy below; FP64
+residual, Newton update, Arnoldi coefficients and Hessenberg least squares.  fp64 (the drop-in): the reference's right-preconditioned GMRES(30) with modified
 Gram-Schmidt, FP64 V-cycle and FP64 Jacobian products.
 
 Printed JSON line: value = seconds per solve of the headline path (CUDA events, vectors resident),
@@ -317,12 +317,13 @@ def workload_config(args, path: str, levels: int | None) -> dict:
     if path == "mixed":
         orth = "two-pass (CGS2)" if args.orth == "cgs2" else "one-pass (CGS1)"
         solver = (f"FGMRES(30) (cycles up to 30 steps; {orth} classical Gram-Schmidt on lazily normalised basis "
-                  f"vectors, FP32 basis in double-FP32 arithmetic while the forcing term is >= 1e-5, FP64 basis "
+                  f"vectors, the basis FP32 in double-FP32 arithmetic while the forcing term is >= 1e-6 and FP64 "
                   f"below) right-preconditioned by the FP32 GMG V(2,2) ({lv}; the levels n <= 15 with the "
                   f"Jacobian -Lap_h - lambda e^u of the iterate), Jacobian products of the FP32 preconditioned "
-                  f"vectors in FP32 arithmetic while the forcing term is >= 1e-5 and to FP64 accuracy "
-                  f"(double-FP32 stencil, FP64 coefficient) below; FP64 residual, Newton update, Arnoldi "
-                  f"coefficients and least squares")
+                  f"vectors in FP32 arithmetic while the forcing term is >= 1e-5 and to FP64 accuracy below "
+                  f"(double-FP32 stencil; rounded once to FP32 with RN32(lambda e^u) for the FP32 basis, with the "
+                  f"FP64 coefficient for the FP64 basis); FP64 residual, Newton update, Arnoldi coefficients and "
+                  f"least squares")
     else:
         solver = (f"GMRES(30) with modified Gram-Schmidt (the reference's) right-preconditioned by the FP64 GMG "
                   f"V(2,2) ({lv}), FP64 Jacobian products")
