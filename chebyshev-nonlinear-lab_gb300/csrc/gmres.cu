@@ -19,6 +19,7 @@
 // On this GPU FP64 arithmetic, not bandwidth, bounds these kernels, so MGS is the cheaper of
 // the two; CGS2 issues fewer launches and is the better-conditioned choice.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 
@@ -256,6 +257,10 @@ __global__ void k_to32_scaled(const double* __restrict__ src, double s, float* _
         dst[i] = f64_to_f32(__dmul_rn(src[i], s));
 }
 
+// Elements of each vector a thread loads ahead of the arithmetic in k_cgs_df.
+template <int CNT>
+constexpr int kCgsUnroll = CNT <= 2 ? 8 : (CNT <= 3 ? 4 : 2);
+
 // MODE 0: h[r] = <w, u_r> for r < CNT.
 // MODE 1: u = RN32(a (w - sum_r h[r] s2[r] u_r)) into uout (a = *ascale, or 1 when null), then
 //         h[r] = <u, u_r> (the second pass of CGS2).
@@ -323,7 +328,7 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs_df(const float* w, const fl
     // UF elements a thread an iteration, all their loads issued before any arithmetic: with one element a
     // thread the loads in flight were too few to cover DRAM latency (the passes ran at ~50 % of HBM).  Each
     // thread still visits its elements in the same order, so the sums are unchanged.
-    constexpr int UF = CNT <= 3 ? 4 : 2;
+    constexpr int UF = kCgsUnroll<CNT>;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     for (; i + (UF - 1) * stride < N; i += UF * stride) {
@@ -464,17 +469,30 @@ void launch_combine_df(Context& ctx, unsigned grid, int cnt, const float* Z, siz
     }
 }
 
+// One wave of k_cgs_df<CNT, MODE>: the reduction grid, capped at the blocks that fit on the device at
+// once (the longer unrolls hold more registers, and a second partial wave would double the pass).
+template <int CNT, int MODE>
+unsigned cgs_grid(Context& ctx, size_t N) {
+    static std::atomic<int> per_sm{0};  // resident blocks an SM, found once
+    int b = per_sm.load();
+    if (b == 0) {
+        NUMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_cgs_df<CNT, MODE>, kRedThreads, 0));
+        b = b > 0 ? b : 1;
+        per_sm.store(b);
+    }
+    return std::min(ctx.red_grid(N), (unsigned)(b * ctx.sm_count));
+}
+
 // Launches k_cgs_df<cnt, MODE> for 1 <= cnt <= kCgsBlock.
 template <int MODE>
 void launch_cgs_df(Context& ctx, int cnt, const float* w, const float2* part_in, const float* u0, const float* U,
                    size_t N, const double* hin, const double* s2c, const double* ascale, double* sig2, double* sig,
                    int j, double* hout, float* uout, float2* part_out) {
-    const unsigned g = ctx.red_grid(N);
     switch (cnt) {
 #define NUMA_CGS_DF_CASE(K)                                                                                  \
     case K:                                                                                                  \
-        launch_pdl(k_cgs_df<K, MODE>, g, kRedThreads, 0, ctx.stream, w, part_in, u0, U, N, hin, s2c, ascale, sig2, \
-                   sig, j, N, ctx.red, hout, uout, part_out);                                                \
+        launch_pdl(k_cgs_df<K, MODE>, cgs_grid<K, MODE>(ctx, N), kRedThreads, 0, ctx.stream, w, part_in, \
+                   u0, U, N, hin, s2c, ascale, sig2, sig, j, N, ctx.red, hout, uout, part_out);             \
         break;
         NUMA_CGS_DF_CASE(1)
         NUMA_CGS_DF_CASE(2)
