@@ -67,9 +67,10 @@ __device__ __forceinline__ double lap_sum(const double* __restrict__ v, size_t p
 // first FP32 Krylov vector of the next linear solve), integer conversions; this is the mixed
 // path's evaluation, and it forms 6u - (the six neighbours) in 64-bit fixed point on the integer pipe,
 // rounded once (lap7_fixed; the reference rounds six times).  LT: lambda e^u from the operator's
-// lambda-scaled exp table (lt2, ltf).
+// lambda-scaled exp table (lt2, ltf).  The C32 form is held to five resident CTAs an SM (48 registers):
+// its integer and FP64 pipes are both busy, and the extra warps cover more of their latency.
 template <bool WRITE_C, bool NORM, bool C32, bool LT>
-__global__ void __launch_bounds__(BX* BY) k_eval(const double* __restrict__ u, double* __restrict__ F,
+__global__ void __launch_bounds__(BX* BY, C32 ? 5 : 1) k_eval(const double* __restrict__ u, double* __restrict__ F,
                                                  double* __restrict__ c_out, float* __restrict__ c32_out,
                                                  float* __restrict__ f32_out, int n,
                                                  int ichunk, double lam, double h2inv, RedArgs red, double* norm_out,
