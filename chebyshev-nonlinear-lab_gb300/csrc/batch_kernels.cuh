@@ -161,11 +161,6 @@ struct BClass {
     int pbase;  // first partial slot of the class (stencil reductions)
 };
 
-// F = h^-2 (6 u - sum) - lambda e^u at the instances with eval[t] set, from x_a or x_b (the one
-// selected by cur[t] ^ which), with RN32(lambda e^u) into c32, RN32(F) into f32 (the first FP32
-// Krylov vector of the next linear solve) and the block's sum of F^2 into partials: the arithmetic
-// of the single-instance residual kernel (its fixed-point 7-point sum, lambda e^u from a lambda-scaled
-// exp table per instance).
 // The exp table scaled by each instance's lambda (the single-instance operator's k_lam_table, one table of
 // 2^kExpTableBits entries an instance, blockIdx.y = instance - t0): T2 = (RN(lambda T_hi), lambda T_hi -
 // RN(lambda T_hi) + lambda T_lo), TF their RN32.  Instances with lambda outside [2^-10, 2^10] keep no table.
@@ -182,7 +177,13 @@ __global__ void k_blam_tables(const double* __restrict__ lam, double2* __restric
     TF[(size_t)t * (1 << kExpTableBits) + jj] = make_float2(__double2float_rn(hi), __double2float_rn(lo));
 }
 
-__global__ void __launch_bounds__(kBX* kBY) k_beval(const double* __restrict__ xa, const double* __restrict__ xb,
+// F = h^-2 (6 u - sum) - lambda e^u at the instances with eval[t] set, from x_a or x_b (the one
+// selected by cur[t] ^ which), with RN32(lambda e^u) into c32, RN32(F) into f32 (the first FP32
+// Krylov vector of the next linear solve) and the block's sum of F^2 into partials: the arithmetic
+// of the single-instance residual kernel (its fixed-point 7-point sum, lambda e^u from a lambda-scaled
+// exp table per instance).  Held to five resident CTAs an SM (48 registers), as the
+// single-instance kernel: its integer and FP64 pipes are both busy, and the extra warps cover latency.
+__global__ void __launch_bounds__(kBX* kBY, 5) k_beval(const double* __restrict__ xa, const double* __restrict__ xb,
                                                     const int* __restrict__ cur, int which,
                                                     const int* __restrict__ eval, const double* __restrict__ lam,
                                                     BClass C, double* __restrict__ F, float* __restrict__ c32,
@@ -353,7 +354,7 @@ __global__ void __launch_bounds__(kEwThreads) k_bdots(const float* __restrict__ 
     for (int r = 0; r < CNT; ++r) acc[r] = DF{0.0f, 0.0f};
     const float* u = U + (long long)b0 * T;
     // UF elements a thread an iteration, all loads first (more DRAM bytes in flight), same order
-    constexpr int UF = CNT <= 3 ? 4 : 2;
+    constexpr int UF = CNT <= 2 ? 8 : (CNT <= 3 ? 4 : 2);
     const long long e1 = B.end[blockIdx.x];
     long long i = B.beg[blockIdx.x] + threadIdx.x;
     for (; i + (UF - 1) * kEwThreads < e1; i += UF * kEwThreads) {
@@ -426,7 +427,7 @@ __global__ void __launch_bounds__(kEwThreads) k_bupdate(const float* __restrict_
     };
     // UF elements a thread an iteration, all loads first (more DRAM bytes in flight), same order; each
     // element of part is read before it is written, by one thread
-    constexpr int UF = CNT <= 3 ? 4 : 2;
+    constexpr int UF = CNT <= 2 ? 8 : (CNT <= 3 ? 4 : 2);
     const long long e1 = B.end[blockIdx.x];
     long long i = B.beg[blockIdx.x] + threadIdx.x;
     for (; i + (UF - 1) * kEwThreads < e1; i += UF * kEwThreads) {
@@ -488,7 +489,7 @@ __global__ void __launch_bounds__(kEwThreads) k_bcombine(const float* __restrict
         if (last) xi = x[i];
     };
     // UF elements a thread an iteration, all loads first (more DRAM bytes in flight)
-    constexpr int UF = CNT <= 3 ? 4 : 2;
+    constexpr int UF = CNT <= 2 ? 8 : (CNT <= 3 ? 4 : 2);
     const long long e1 = B.end[blockIdx.x];
     long long i = B.beg[blockIdx.x] + threadIdx.x;
     for (; i + (UF - 1) * kEwThreads < e1; i += UF * kEwThreads) {
